@@ -1,0 +1,180 @@
+/*
+ * smartcore_gb300 — C ABI of the GB300 (sm_103a) distance-argmin path of
+ * smartcore 0.4.0: the Lloyd loop of KMeans::fit / KMeans::predict and the
+ * brute-force LinearKNNSearch::find behind KNNClassifier / KNNRegressor.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Sizes are int64_t (Rust usize);
+ *     labels and neighbour indices are int64_t (usize), -1 for "None".
+ *   - Matrices: element (i, j) of an n x d matrix is x[i*ld + j] for
+ *     SC_ROW_MAJOR and x[j*ld + i] for SC_COL_MAJOR (DenseMatrix keeps both,
+ *     column-major by default: src/linalg/basic/matrix.rs:187-238, :367-381).
+ *   - Every call is blocking on the handle's own CUDA stream unless stated.
+ *     Handles are not thread-safe; different handles may be used from
+ *     different threads.
+ *   - Errors: every entry point returns sc_status; sc_last_error() gives the
+ *     message of the calling thread's last failure.  Parameter validation
+ *     keeps the reference's messages (src/cluster/kmeans.rs:257-269,
+ *     src/algorithm/neighbour/linear_search.rs:53-58) so a Rust shim can map
+ *     SC_ERR_INVALID to Failed::fit / Failed::because(FindFailed, ...)
+ *     (src/error/mod.rs:47-91) unchanged.
+ *   - The GPU is required: there is no CPU fallback.  Without a usable
+ *     CUDA device every compute call returns SC_ERR_CUDA.
+ */
+#ifndef SMARTCORE_GB300_H
+#define SMARTCORE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t sc_status;
+#define SC_OK 0
+#define SC_ERR_INVALID 1  /* bad argument; message follows the reference */
+#define SC_ERR_CUDA 2     /* CUDA runtime / launch failure, or no GPU */
+#define SC_ERR_OOM 3      /* device allocation failed */
+#define SC_ERR_TIMEOUT 4  /* a bounded device-side wait ran out */
+#define SC_ERR_INTERNAL 5 /* a device-side consistency check failed */
+
+#define SC_F32 0
+#define SC_F64 1
+#define SC_ROW_MAJOR 0
+#define SC_COL_MAJOR 1
+#define SC_MEM_HOST 0   /* pointer is host memory (pageable or pinned) */
+#define SC_MEM_DEVICE 1 /* pointer is device memory of the current device */
+
+/* Arithmetic form of the distance step.
+ *   SC_FORM_FP64: every distance in FP64 with the reference's own operation
+ *     order (src/metrics/distance/euclidian.rs:51-67).
+ *   SC_FORM_SPLIT_BF16: -2 x.c^T as a split-BF16 tcgen05 GEMM (FP32
+ *     accumulate) plus ||x||^2 + ||c||^2, with a certified error bound; every
+ *     decision inside the bound is re-scored in FP64.  Results are identical
+ *     to SC_FORM_FP64. */
+#define SC_FORM_FP64 0
+#define SC_FORM_SPLIT_BF16 1
+
+/* Random generator behind get_rng_impl (src/rand_custom.rs:1-32). */
+#define SC_RNG_SMALL 0 /* default features: rand 0.8 SmallRng (xoshiro256++) */
+#define SC_RNG_STD 1   /* feature std_rand: rand 0.8 StdRng (ChaCha12) */
+
+#define SC_KNN_UNIFORM 0  /* KNNWeightFunction::Uniform (src/neighbors/mod.rs:53-59) */
+#define SC_KNN_DISTANCE 1 /* KNNWeightFunction::Distance */
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *sc_last_error(void);
+/* ABI version of this library (major * 100 + minor). */
+int32_t sc_abi_version(void);
+/* 1 if a CUDA device of compute capability 10.3 is usable, else 0. */
+int32_t sc_device_ok(void);
+
+/* ------------------------------------------------------------------ */
+/* k-means++ draws                                                     */
+/* ------------------------------------------------------------------ */
+/* The random draws of KMeans::kmeans_plus_plus (src/cluster/kmeans.rs:354-
+ * 413) do not depend on the data: gen_range(0..n) once (:359), then
+ * gen::<f64>() once per further seed (:385).  A Rust shim draws them with the
+ * crate's own get_rng_impl(seed) and passes them in; this helper restates the
+ * same rand 0.8.5 generators for non-Rust callers.  uniforms has k-1 slots. */
+sc_status sc_kmeanspp_draws(int32_t rng, uint64_t seed, int64_t n, int64_t k,
+                            int64_t *first_index, double *uniforms);
+
+/* ------------------------------------------------------------------ */
+/* KMeans                                                              */
+/* ------------------------------------------------------------------ */
+/* One-call KMeans::fit (src/cluster/kmeans.rs:254-323): k-means++ seeding
+ * from the given draws, initial centroids = means of the seeding partition
+ * (:275-292), then up to max_iter Lloyd iterations that stop when the
+ * distortion did not strictly decrease (:305-309).  Replaces the BBDTree
+ * filtering step (src/algorithm/neighbour/bbd_tree.rs:62-163) by a
+ * brute-force assignment with the same labels.
+ * x: n x d, host memory.  Outputs (host): centroids k*d (row-major),
+ * sizes k, labels n, the final distortion and the number of iterations run.
+ * SC_ERR_INVALID with "invalid number of clusters: {k}" for k < 2 and
+ * "invalid maximum number of iterations: {max_iter}" for max_iter == 0. */
+sc_status sc_kmeans_fit(const void *x, int32_t dtype, int32_t layout, int64_t n,
+                        int64_t d, int64_t ld, int64_t k, int64_t max_iter,
+                        int64_t first_index, const double *uniforms,
+                        int32_t form, double *centroids_out, int64_t *sizes_out,
+                        int64_t *labels_out, double *distortion_out,
+                        int64_t *iters_out);
+
+/* KMeans::predict (src/cluster/kmeans.rs:327-352): label of the nearest
+ * centroid (strict <, lowest index wins ties) for each row of x (host). */
+sc_status sc_kmeans_predict(const void *x, int32_t dtype, int32_t layout,
+                            int64_t n, int64_t d, int64_t ld,
+                            const double *centroids, int64_t k, int32_t form,
+                            int64_t *labels_out);
+
+/* Handle API: data resident on the device across calls. */
+typedef struct sc_kmeans sc_kmeans;
+/* Copies x (host or device memory, see mem) into a row-major device copy. */
+sc_status sc_kmeans_create(const void *x, int32_t dtype, int32_t layout,
+                           int32_t mem, int64_t n, int64_t d, int64_t ld,
+                           int32_t form, sc_kmeans **out);
+/* k-means++ on the device (kmeans.rs:354-413) plus the initial means. */
+sc_status sc_kmeans_seed(sc_kmeans *h, int64_t k, int64_t first_index,
+                         const double *uniforms);
+/* Sets k and the current centroids (host, k*d row-major) directly. */
+sc_status sc_kmeans_set_centroids(sc_kmeans *h, int64_t k,
+                                  const double *centroids);
+/* Runs Lloyd iterations.  stop_on_converge = 1: the reference loop (at most
+ * max_iter iterations, break rule of kmeans.rs:305-309).  0: exactly
+ * max_iter full iterations with the break rule disabled (throughput runs).
+ * iters_done may be NULL; otherwise the call waits for completion. */
+sc_status sc_kmeans_iterate(sc_kmeans *h, int64_t max_iter,
+                            int32_t stop_on_converge, int64_t *iters_done);
+/* Copies the state to host buffers (any may be NULL). */
+sc_status sc_kmeans_get(sc_kmeans *h, double *centroids, int64_t *sizes,
+                        int64_t *labels, double *distortion, int64_t *iters);
+/* The handle's CUDA stream (a cudaStream_t), for event timing. */
+void *sc_kmeans_stream(sc_kmeans *h);
+/* Counters of the last sc_kmeans_iterate: near-tie points re-scored in FP64
+ * (split form) and k-means++ draws that needed the sequential replay. */
+sc_status sc_kmeans_stats(sc_kmeans *h, int64_t *rescored, int64_t *pp_replays);
+sc_status sc_kmeans_sync(sc_kmeans *h);
+void sc_kmeans_destroy(sc_kmeans *h);
+
+/* ------------------------------------------------------------------ */
+/* Brute-force kNN (LinearKNNSearch)                                   */
+/* ------------------------------------------------------------------ */
+typedef struct sc_knn sc_knn;
+/* LinearKNNSearch::new (src/algorithm/neighbour/linear_search.rs:45-47) over
+ * the n training rows of train (host or device memory). */
+sc_status sc_knn_create(const void *train, int32_t dtype, int32_t layout,
+                        int32_t mem, int64_t n, int64_t d, int64_t ld,
+                        sc_knn **out);
+/* LinearKNNSearch::find (linear_search.rs:52-84) for m query rows at once.
+ * Row q of idx_out / dist_out (m x k, host or device per out_mem) is the
+ * reference's heap array in its own order: idx = training row, dist =
+ * sqrt of the element-type squared distance; an empty slot is -1 / +inf.
+ * SC_ERR_INVALID with "k should be >= 1 and <= length(data)" otherwise. */
+sc_status sc_knn_find(sc_knn *h, const void *queries, int32_t layout,
+                      int32_t mem, int64_t m, int64_t ld, int64_t k,
+                      int32_t form, int32_t out_mem, int64_t *idx_out,
+                      double *dist_out);
+/* KNNClassifier / KNNRegressor aggregation on the device over a find()
+ * result already in idx/dist (device memory of this handle, m x k):
+ * y_class = class index per training row (KNNClassifier::fit,
+ * src/neighbors/knn_classifier.rs:229-235); classes_out = winning class
+ * index per query (knn_classifier.rs:279-299). */
+sc_status sc_knn_classify(sc_knn *h, const void *queries, int32_t layout,
+                          int32_t mem, int64_t m, int64_t ld, int64_t k,
+                          int32_t form, int32_t weight, const int64_t *y_class,
+                          int64_t n_classes, int64_t *classes_out);
+/* KNNRegressor::predict (src/neighbors/knn_regressor.rs:254-282), f64 y. */
+sc_status sc_knn_regress(sc_knn *h, const void *queries, int32_t layout,
+                         int32_t mem, int64_t m, int64_t ld, int64_t k,
+                         int32_t form, int32_t weight, const double *y,
+                         double *out);
+void *sc_knn_stream(sc_knn *h);
+/* Number of candidates re-scored in FP64 by the last split-form find. */
+sc_status sc_knn_stats(sc_knn *h, int64_t *rescored);
+void sc_knn_destroy(sc_knn *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,189 @@
+"""KMeans on the GPU, with smartcore's API (src/cluster/kmeans.rs).
+
+    from smartcore_gb300.cluster import KMeans, KMeansParameters
+    km = KMeans.fit(x, KMeansParameters().with_k(2))
+    y = km.predict(x)
+
+fit = k-means++ seeding (host draws from the rand 0.8 generator the crate
+would use, device D^2 passes) + the Lloyd loop on the device; predict = the
+nearest-centroid assignment.  Labels equal the reference's; centroids agree
+to ~1e-15 relative (exact fixed-point sums rounded once).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from .error import Failed, FailedError
+from .linalg import as_matrix, layout_of
+
+
+@dataclass
+class KMeansParameters:
+    """KMeansParameters (kmeans.rs:109-146): k, max_iter, seed.
+
+    `form` selects the distance arithmetic (FP64 or split-BF16, identical
+    results) and `rng` which rand 0.8 generator stands in for get_rng_impl
+    (SmallRng without std_rand, StdRng with it); neither exists in the
+    reference, both default to the reference's behaviour."""
+    k: int = 2
+    max_iter: int = 100
+    seed: Optional[int] = None
+    form: int = _lib.FORM_FP64
+    rng: int = _lib.RNG_SMALL
+
+    def with_k(self, k):
+        self.k = k
+        return self
+
+    def with_max_iter(self, max_iter):
+        self.max_iter = max_iter
+        return self
+
+    def with_seed(self, seed):
+        self.seed = seed
+        return self
+
+    def with_form(self, form):
+        self.form = form
+        return self
+
+
+def kmeanspp_draws(n, k, seed=None, rng=_lib.RNG_SMALL):
+    """The draws kmeans_plus_plus takes from get_rng_impl(seed): seed None is
+    seed 0 without std_rand (src/rand_custom.rs:26-27)."""
+    L = _lib.load()
+    first = np.zeros(1, np.int64)
+    u = np.zeros(max(k - 1, 1), np.float64)
+    _lib.check(L.sc_kmeanspp_draws(rng, 0 if seed is None else seed, n, k, _lib.ptr(first), _lib.ptr(u)))
+    return int(first[0]), u[: max(k - 1, 0)]
+
+
+class KMeans:
+    """Fitted model: k, size, _y, _distortion, centroids (kmeans.rs:73-83)."""
+
+    def __init__(self, k, y, size, distortion, centroids, iters, form):
+        self.k = k
+        self._y = y
+        self.size = size
+        self._distortion = distortion
+        self.centroids = centroids
+        self.iters = iters
+        self.form = form
+
+    @staticmethod
+    def fit(x, parameters: KMeansParameters = None) -> "KMeans":
+        p = parameters or KMeansParameters()
+        a = as_matrix(x)
+        n, d = a.shape
+        if p.k < 2:
+            raise Failed(FailedError.FitFailed, f"invalid number of clusters: {p.k}")
+        if p.max_iter == 0:
+            raise Failed(FailedError.FitFailed, f"invalid maximum number of iterations: {p.max_iter}")
+        first, u = kmeanspp_draws(n, p.k, p.seed, p.rng)
+        L = _lib.load()
+        lay, ld = layout_of(a)
+        dt = _lib.F32 if a.dtype == np.float32 else _lib.F64
+        cent = np.zeros((p.k, d), np.float64)
+        sizes = np.zeros(p.k, np.int64)
+        labels = np.zeros(n, np.int64)
+        dist = np.zeros(1, np.float64)
+        iters = np.zeros(1, np.int64)
+        uu = np.ascontiguousarray(u, np.float64) if len(u) else np.zeros(1)
+        _lib.check(L.sc_kmeans_fit(_lib.ptr(a), dt, lay, n, d, ld, p.k, p.max_iter, first, _lib.ptr(uu),
+                                   p.form, _lib.ptr(cent), _lib.ptr(sizes), _lib.ptr(labels),
+                                   _lib.ptr(dist), _lib.ptr(iters)))
+        return KMeans(p.k, labels, sizes, float(dist[0]), cent, int(iters[0]), p.form)
+
+    def predict(self, x) -> np.ndarray:
+        a = as_matrix(x)
+        n, d = a.shape
+        L = _lib.load()
+        lay, ld = layout_of(a)
+        dt = _lib.F32 if a.dtype == np.float32 else _lib.F64
+        labels = np.zeros(n, np.int64)
+        c = np.ascontiguousarray(self.centroids, np.float64)
+        _lib.check(L.sc_kmeans_predict(_lib.ptr(a), dt, lay, n, d, ld, _lib.ptr(c), self.k, self.form,
+                                       _lib.ptr(labels)), FailedError.PredictFailed)
+        return labels
+
+    def __eq__(self, other):
+        """PartialEq of kmeans.rs:85-107: k, size and centroids within f64::EPSILON."""
+        if self.k != other.k or not np.array_equal(self.size, other.size):
+            return False
+        if self.centroids.shape != other.centroids.shape:
+            return False
+        return bool(np.all(np.abs(self.centroids - other.centroids) <= np.finfo(np.float64).eps))
+
+
+class KMeansHandle:
+    """Device-resident dataset for repeated Lloyd runs (sc_kmeans_* handle API)."""
+
+    def __init__(self, x, form=_lib.FORM_FP64, device_ptr=None, dtype=None, shape=None):
+        L = _lib.load()
+        self._L = L
+        h = C.c_void_p()
+        if device_ptr is not None:
+            n, d = shape
+            dt = _lib.F32 if dtype == np.float32 else _lib.F64
+            _lib.check(L.sc_kmeans_create(C.c_void_p(device_ptr), dt, _lib.ROW_MAJOR, _lib.MEM_DEVICE, n, d, d,
+                                          form, C.byref(h)))
+        else:
+            a = as_matrix(x)
+            n, d = a.shape
+            lay, ld = layout_of(a)
+            dt = _lib.F32 if a.dtype == np.float32 else _lib.F64
+            _lib.check(L.sc_kmeans_create(_lib.ptr(a), dt, lay, _lib.MEM_HOST, n, d, ld, form, C.byref(h)))
+        self.h, self.n, self.d, self.k = h, n, d, 0
+
+    def seed(self, k, first, uniforms):
+        u = np.ascontiguousarray(uniforms, np.float64) if len(uniforms) else np.zeros(1)
+        _lib.check(self._L.sc_kmeans_seed(self.h, k, first, _lib.ptr(u)))
+        self.k = k
+
+    def set_centroids(self, c):
+        c = np.ascontiguousarray(c, np.float64)
+        _lib.check(self._L.sc_kmeans_set_centroids(self.h, c.shape[0], _lib.ptr(c)))
+        self.k = c.shape[0]
+
+    def iterate(self, max_iter, stop_on_converge=True, wait=True):
+        it = np.zeros(1, np.int64)
+        _lib.check(self._L.sc_kmeans_iterate(self.h, max_iter, 1 if stop_on_converge else 0,
+                                             _lib.ptr(it) if wait else None))
+        return int(it[0])
+
+    def get(self):
+        cent = np.zeros((self.k, self.d), np.float64)
+        sizes = np.zeros(self.k, np.int64)
+        labels = np.zeros(self.n, np.int64)
+        dist = np.zeros(1, np.float64)
+        iters = np.zeros(1, np.int64)
+        _lib.check(self._L.sc_kmeans_get(self.h, _lib.ptr(cent), _lib.ptr(sizes), _lib.ptr(labels),
+                                         _lib.ptr(dist), _lib.ptr(iters)))
+        return cent, sizes, labels, float(dist[0]), int(iters[0])
+
+    def stats(self):
+        a = np.zeros(2, np.int64)
+        _lib.check(self._L.sc_kmeans_stats(self.h, _lib.ptr(a[:1]), _lib.ptr(a[1:])))
+        return int(a[0]), int(a[1])
+
+    def stream(self):
+        return self._L.sc_kmeans_stream(self.h)
+
+    def sync(self):
+        _lib.check(self._L.sc_kmeans_sync(self.h))
+
+    def close(self):
+        if self.h:
+            self._L.sc_kmeans_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,530 @@
+// extern "C" entry points of libsmartcore_gb300 (declared in
+// include/smartcore_gb300.h): argument checks with the reference's messages,
+// device buffers owned by handles, and the launch sequences of the Lloyd
+// loop, k-means++ and kNN.
+#include <float.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "split.cuh"
+
+namespace sc {
+
+static thread_local char g_err[512];
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+sc_status cuda_fail(cudaError_t e, const char *what) {
+  set_error("CUDA error %s (%s) in %s", cudaGetErrorName(e), cudaGetErrorString(e), what);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();  // allocation failures are not sticky
+    return SC_ERR_OOM;
+  }
+  return SC_ERR_CUDA;
+}
+
+namespace {
+
+template <class T>
+sc_status dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  SC_CUDA(cudaMalloc((void **)p, count * sizeof(T)));
+  return SC_OK;
+}
+
+template <class T>
+void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+size_t esize(int dtype) { return dtype == SC_F32 ? 4 : 8; }
+
+sc_status check_matrix(const void *x, int32_t dtype, int32_t layout, int32_t mem,
+                       int64_t n, int64_t d, int64_t ld) {
+  if (dtype != SC_F32 && dtype != SC_F64) { set_error("unsupported dtype %d", dtype); return SC_ERR_INVALID; }
+  if (layout != SC_ROW_MAJOR && layout != SC_COL_MAJOR) { set_error("unsupported layout %d", layout); return SC_ERR_INVALID; }
+  if (mem != SC_MEM_HOST && mem != SC_MEM_DEVICE) { set_error("unsupported memory kind %d", mem); return SC_ERR_INVALID; }
+  if (n < 0 || d < 1 || d > (1 << 16)) { set_error("invalid shape (%lld, %lld)", (long long)n, (long long)d); return SC_ERR_INVALID; }
+  if (layout == SC_ROW_MAJOR && ld < d) { set_error("leading dimension %lld < number of columns %lld", (long long)ld, (long long)d); return SC_ERR_INVALID; }
+  if (layout == SC_COL_MAJOR && ld < n) { set_error("leading dimension %lld < number of rows %lld", (long long)ld, (long long)n); return SC_ERR_INVALID; }
+  if (n > 0 && !x) { set_error("null matrix pointer"); return SC_ERR_INVALID; }
+  return SC_OK;
+}
+
+// Copies an n x d matrix (host or device, either layout) into a contiguous
+// row-major device buffer dst.
+sc_status upload_matrix(const void *x, int32_t dtype, int32_t layout, int32_t mem,
+                        int64_t n, int64_t d, int64_t ld, void *dst, cudaStream_t s) {
+  if (n == 0) return SC_OK;
+  const size_t es = esize(dtype);
+  const cudaMemcpyKind kind = mem == SC_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  if (layout == SC_ROW_MAJOR) {
+    if (ld == d) SC_CUDA(cudaMemcpyAsync(dst, x, (size_t)(n * d) * es, kind, s));
+    else SC_CUDA(cudaMemcpy2DAsync(dst, (size_t)d * es, x, (size_t)ld * es, (size_t)d * es, (size_t)n, kind, s));
+    return SC_OK;
+  }
+  void *tmp = nullptr;
+  const size_t span = (size_t)((d - 1) * ld + n);
+  const void *src = x;
+  if (mem == SC_MEM_HOST) {
+    SC_CUDA(cudaMallocAsync(&tmp, span * es, s));
+    SC_CUDA(cudaMemcpyAsync(tmp, x, span * es, cudaMemcpyHostToDevice, s));
+    src = tmp;
+  }
+  sc_status r = launch_to_row_major(dtype, src, n, d, ld, dst, s);
+  if (tmp) cudaFreeAsync(tmp, s);
+  return r;
+}
+
+int fixed_scale(double absmax, int64_t n) {
+  int e = 0;
+  if (absmax > 0) frexp(absmax, &e);  // absmax < 2^e
+  int ln = 0;
+  while ((1ll << ln) <= n) ++ln;  // n < 2^ln
+  return 125 - e - ln;
+}
+
+}  // namespace
+}  // namespace sc
+
+using namespace sc;
+
+// ---------------------------------------------------------------------------
+// KMeans handle
+// ---------------------------------------------------------------------------
+struct sc_kmeans {
+  int dtype = SC_F32, form = SC_FORM_FP64;
+  int64_t n = 0, d = 0, k = 0;
+  cudaStream_t stream = nullptr;
+  void *x = nullptr;  // row-major n x d
+  int scale = 0;
+  double *cent = nullptr;       // k x d
+  int32_t *labels = nullptr;    // n
+  double *dd = nullptr;         // n, k-means++ distances
+  double *part = nullptr;       // block partials
+  Acc128 *acc = nullptr;        // k x d
+  unsigned long long *cnt = nullptr;
+  int64_t *sizes = nullptr;     // k
+  double *cterms = nullptr;     // k
+  double *uniforms = nullptr;   // k - 1
+  double *xnorm_total = nullptr;
+  LloydState *st = nullptr;
+  unsigned long long *bits = nullptr;
+  SplitState split;             // split-BF16 form buffers
+  int64_t k_alloc = 0;
+};
+
+static sc_status kmeans_alloc_k(sc_kmeans *h, int64_t k) {
+  if (k <= h->k_alloc) { h->k = k; return SC_OK; }
+  dfree(h->cent); dfree(h->acc); dfree(h->cnt); dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
+  SC_TRY(dalloc(&h->cent, (size_t)(k * h->d)));
+  SC_TRY(dalloc(&h->acc, (size_t)(k * h->d)));
+  SC_TRY(dalloc(&h->cnt, (size_t)k));
+  SC_TRY(dalloc(&h->sizes, (size_t)k));
+  SC_TRY(dalloc(&h->cterms, (size_t)k));
+  SC_TRY(dalloc(&h->uniforms, (size_t)k));
+  SC_CUDA(cudaMemsetAsync(h->acc, 0, (size_t)(k * h->d) * sizeof(Acc128), h->stream));
+  SC_CUDA(cudaMemsetAsync(h->cnt, 0, (size_t)k * sizeof(unsigned long long), h->stream));
+  h->k_alloc = k;
+  h->k = k;
+  return SC_OK;
+}
+
+static sc_status reset_state(sc_kmeans *h) {
+  LloydState s;
+  memset(&s, 0, sizeof s);
+  s.distortion = DBL_MAX;
+  s.stop = 1;
+  SC_CUDA(cudaMemcpyAsync(h->st, &s, sizeof s, cudaMemcpyHostToDevice, h->stream));
+  return SC_OK;
+}
+
+extern "C" {
+
+const char *sc_last_error(void) { return g_err; }
+int32_t sc_abi_version(void) { return 100; }
+
+int32_t sc_device_ok(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) { cudaGetLastError(); return 0; }
+  int dev = 0, major = 0, minor = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  return (major == 10 && minor == 3) ? 1 : 0;
+}
+
+void sc_kmeans_destroy(sc_kmeans *h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  dfree(h->x); dfree(h->cent); dfree(h->labels); dfree(h->dd); dfree(h->part);
+  dfree(h->acc); dfree(h->cnt); dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
+  dfree(h->xnorm_total); dfree(h->st); dfree(h->bits);
+  split_free(&h->split);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+sc_status sc_kmeans_create(const void *x, int32_t dtype, int32_t layout, int32_t mem,
+                           int64_t n, int64_t d, int64_t ld, int32_t form,
+                           sc_kmeans **out) {
+  if (!out) { set_error("null output handle"); return SC_ERR_INVALID; }
+  *out = nullptr;
+  SC_TRY(check_matrix(x, dtype, layout, mem, n, d, ld));
+  if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
+  if (n > ((int64_t)1 << 40)) { set_error("n=%lld is too large", (long long)n); return SC_ERR_INVALID; }
+  sc_kmeans *h = new sc_kmeans();
+  h->dtype = dtype; h->form = form; h->n = n; h->d = d;
+  sc_status r = SC_OK;
+  do {
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "cudaStreamCreate");
+      h->stream = nullptr;
+      break;
+    }
+    const int nparts = std::max(assign_block_count(n), pp_block_count(n));
+    if ((r = dalloc((char **)&h->x, (size_t)(n * d) * esize(dtype))) != SC_OK) break;
+    if ((r = dalloc(&h->labels, (size_t)n)) != SC_OK) break;
+    if ((r = dalloc(&h->dd, (size_t)n)) != SC_OK) break;
+    if ((r = dalloc(&h->part, (size_t)nparts)) != SC_OK) break;
+    if ((r = dalloc(&h->st, 1)) != SC_OK) break;
+    if ((r = dalloc(&h->bits, 1)) != SC_OK) break;
+    if ((r = dalloc(&h->xnorm_total, 1)) != SC_OK) break;
+    if ((r = upload_matrix(x, dtype, layout, mem, n, d, ld, h->x, h->stream)) != SC_OK) break;
+    if ((r = launch_absmax(dtype, h->x, n * d, h->bits, h->stream)) != SC_OK) break;
+    unsigned long long bits = 0;
+    if (cudaMemcpyAsync(&bits, h->bits, sizeof bits, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "absmax");
+      break;
+    }
+    double amax;
+    memcpy(&amax, &bits, sizeof amax);
+    if (!(amax <= DBL_MAX)) {
+      set_error("x contains NaN or infinity; the GPU path requires finite input");
+      r = SC_ERR_INVALID;
+      break;
+    }
+    h->scale = fixed_scale(amax, n);
+    if ((r = reset_state(h)) != SC_OK) break;
+    if (form == SC_FORM_SPLIT_BF16 &&
+        (r = split_prepare(&h->split, dtype, h->x, n, (int)d, h->xnorm_total, h->stream)) != SC_OK)
+      break;
+  } while (0);
+  if (r != SC_OK) { sc_kmeans_destroy(h); return r; }
+  *out = h;
+  return SC_OK;
+}
+
+void *sc_kmeans_stream(sc_kmeans *h) { return h ? (void *)h->stream : nullptr; }
+
+sc_status sc_kmeans_seed(sc_kmeans *h, int64_t k, int64_t first_index, const double *uniforms) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (k < 1) { set_error("invalid number of clusters: %lld", (long long)k); return SC_ERR_INVALID; }
+  if (h->n < 1) { set_error("cannot seed an empty dataset"); return SC_ERR_INVALID; }
+  if (first_index < 0 || first_index >= h->n) { set_error("first seed index %lld out of range", (long long)first_index); return SC_ERR_INVALID; }
+  if (k > 1 && !uniforms) { set_error("null uniforms"); return SC_ERR_INVALID; }
+  if (k > (1 << 20)) { set_error("k=%lld is too large", (long long)k); return SC_ERR_INVALID; }
+  SC_TRY(kmeans_alloc_k(h, k));
+  SC_TRY(reset_state(h));
+  cudaStream_t s = h->stream;
+  if (k > 1) SC_CUDA(cudaMemcpyAsync(h->uniforms, uniforms, (size_t)(k - 1) * sizeof(double), cudaMemcpyHostToDevice, s));
+  SC_CUDA(cudaMemcpyAsync(&h->st->pp_chosen, &first_index, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  const int nb = pp_block_count(h->n);
+  for (int64_t j = 1; j < k; ++j) {  // kmeans.rs:367-397
+    SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(j - 1), h->dd, h->labels, h->part, j == 1, s));
+    SC_TRY(launch_pp_select(h->dd, h->part, h->n, nb, h->uniforms + (j - 1), h->st, s));
+  }
+  SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(k - 1), h->dd, h->labels, nullptr, k == 1, s));  // :399-410
+  // initial centroids: means of the seeding partition (kmeans.rs:275-292)
+  SC_TRY(launch_update_fixed(h->dtype, h->x, h->n, (int)h->d, h->labels, h->acc, h->cnt, h->scale, nullptr, s));
+  SC_TRY(launch_finalize_centroids(h->acc, h->cnt, h->cent, h->sizes, (int)k, (int)h->d, h->scale, nullptr, 1, nullptr, s));
+  if (h->form == SC_FORM_SPLIT_BF16) SC_TRY(split_centroids_changed(&h->split, h->cent, (int)k, s));
+  SC_CUDA(cudaStreamSynchronize(s));
+  return SC_OK;
+}
+
+sc_status sc_kmeans_set_centroids(sc_kmeans *h, int64_t k, const double *centroids) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (k < 1 || !centroids) { set_error("invalid number of clusters: %lld", (long long)k); return SC_ERR_INVALID; }
+  SC_TRY(kmeans_alloc_k(h, k));
+  SC_TRY(reset_state(h));
+  SC_CUDA(cudaMemcpyAsync(h->cent, centroids, (size_t)(k * h->d) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (h->form == SC_FORM_SPLIT_BF16) SC_TRY(split_centroids_changed(&h->split, h->cent, (int)k, h->stream));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+// One Lloyd iteration: assignment, sums, new centroids, distortion + break.
+static sc_status lloyd_step(sc_kmeans *h) {
+  cudaStream_t s = h->stream;
+  const int k = (int)h->k, d = (int)h->d;
+  if (h->form == SC_FORM_FP64) {
+    SC_TRY(launch_assign_fp64(h->dtype, h->x, h->n, d, h->cent, k, h->labels, h->part, h->st, s));
+    SC_TRY(launch_update_fixed(h->dtype, h->x, h->n, d, h->labels, h->acc, h->cnt, h->scale, h->st, s));
+    SC_TRY(launch_finalize_centroids(h->acc, h->cnt, h->cent, h->sizes, k, d, h->scale, h->cterms, 0, h->st, s));
+    SC_TRY(launch_finalize_scalar(h->part, assign_block_count(h->n), nullptr, k, nullptr, h->st, s));
+  } else {
+    SC_TRY(split_assign(&h->split, h->dtype, h->x, h->n, d, h->cent, k, h->labels, h->acc, h->cnt,
+                        h->scale, h->st, s));
+    SC_TRY(launch_finalize_centroids(h->acc, h->cnt, h->cent, h->sizes, k, d, h->scale, h->cterms, 0, h->st, s));
+    SC_TRY(launch_finalize_scalar(nullptr, 0, h->cterms, k, h->xnorm_total, h->st, s));
+    SC_TRY(split_centroids_changed(&h->split, h->cent, k, s));
+  }
+  return SC_OK;
+}
+
+sc_status sc_kmeans_iterate(sc_kmeans *h, int64_t max_iter, int32_t stop_on_converge, int64_t *iters_done) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (h->k < 1) { set_error("centroids are not set"); return SC_ERR_INVALID; }
+  if (max_iter < 0) { set_error("invalid maximum number of iterations: %lld", (long long)max_iter); return SC_ERR_INVALID; }
+  cudaStream_t s = h->stream;
+  const int32_t flags[2] = {0, stop_on_converge ? 1 : 0};  // done, stop
+  SC_CUDA(cudaMemcpyAsync(&h->st->done, flags, sizeof flags, cudaMemcpyHostToDevice, s));
+  const int64_t zero = 0;
+  SC_CUDA(cudaMemcpyAsync(&h->st->iters, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
+  SC_CUDA(cudaMemcpyAsync(&h->st->rescored, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
+  for (int64_t t = 0; t < max_iter; ++t) SC_TRY(lloyd_step(h));
+  if (iters_done) {
+    SC_CUDA(cudaMemcpyAsync(iters_done, &h->st->iters, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    SC_CUDA(cudaStreamSynchronize(s));
+    int32_t err = 0;
+    SC_CUDA(cudaMemcpy(&err, &h->st->err, sizeof err, cudaMemcpyDeviceToHost));
+    if (err) { set_error("device-side check failed (code %d)", err); return err == 4 ? SC_ERR_TIMEOUT : SC_ERR_INTERNAL; }
+  }
+  return SC_OK;
+}
+
+sc_status sc_kmeans_get(sc_kmeans *h, double *centroids, int64_t *sizes, int64_t *labels,
+                        double *distortion, int64_t *iters) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  cudaStream_t s = h->stream;
+  SC_CUDA(cudaStreamSynchronize(s));
+  if (centroids) SC_CUDA(cudaMemcpy(centroids, h->cent, (size_t)(h->k * h->d) * sizeof(double), cudaMemcpyDeviceToHost));
+  if (sizes) SC_CUDA(cudaMemcpy(sizes, h->sizes, (size_t)h->k * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  if (labels && h->n > 0) {
+    std::vector<int32_t> tmp((size_t)h->n);
+    SC_CUDA(cudaMemcpy(tmp.data(), h->labels, (size_t)h->n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < h->n; ++i) labels[i] = tmp[(size_t)i];
+  }
+  LloydState st;
+  SC_CUDA(cudaMemcpy(&st, h->st, sizeof st, cudaMemcpyDeviceToHost));
+  if (distortion) *distortion = st.distortion;
+  if (iters) *iters = st.iters;
+  return SC_OK;
+}
+
+sc_status sc_kmeans_stats(sc_kmeans *h, int64_t *rescored, int64_t *pp_replays) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  LloydState st;
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  SC_CUDA(cudaMemcpy(&st, h->st, sizeof st, cudaMemcpyDeviceToHost));
+  if (rescored) *rescored = st.rescored;
+  if (pp_replays) *pp_replays = st.pp_replays;
+  return SC_OK;
+}
+
+sc_status sc_kmeans_sync(sc_kmeans *h) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+sc_status sc_kmeans_fit(const void *x, int32_t dtype, int32_t layout, int64_t n, int64_t d,
+                        int64_t ld, int64_t k, int64_t max_iter, int64_t first_index,
+                        const double *uniforms, int32_t form, double *centroids_out,
+                        int64_t *sizes_out, int64_t *labels_out, double *distortion_out,
+                        int64_t *iters_out) {
+  // validation order and messages of KMeans::fit (kmeans.rs:257-269)
+  if (k < 2) { set_error("invalid number of clusters: %lld", (long long)k); return SC_ERR_INVALID; }
+  if (max_iter == 0) { set_error("invalid maximum number of iterations: %lld", (long long)max_iter); return SC_ERR_INVALID; }
+  sc_kmeans *h = nullptr;
+  SC_TRY(sc_kmeans_create(x, dtype, layout, SC_MEM_HOST, n, d, ld, form, &h));
+  sc_status r = sc_kmeans_seed(h, k, first_index, uniforms);
+  if (r == SC_OK) r = sc_kmeans_iterate(h, max_iter, 1, nullptr);
+  if (r == SC_OK) r = sc_kmeans_get(h, centroids_out, sizes_out, labels_out, distortion_out, iters_out);
+  sc_kmeans_destroy(h);
+  return r;
+}
+
+sc_status sc_kmeans_predict(const void *x, int32_t dtype, int32_t layout, int64_t n, int64_t d,
+                            int64_t ld, const double *centroids, int64_t k, int32_t form,
+                            int64_t *labels_out) {
+  if (k < 1 || !centroids) { set_error("invalid number of clusters: %lld", (long long)k); return SC_ERR_INVALID; }
+  sc_kmeans *h = nullptr;
+  SC_TRY(sc_kmeans_create(x, dtype, layout, SC_MEM_HOST, n, d, ld, form, &h));
+  sc_status r = sc_kmeans_set_centroids(h, k, centroids);
+  if (r == SC_OK) {
+    if (form == SC_FORM_FP64)
+      r = launch_assign_fp64(h->dtype, h->x, h->n, (int)h->d, h->cent, (int)k, h->labels, nullptr, nullptr, h->stream);
+    else
+      r = split_assign(&h->split, h->dtype, h->x, h->n, (int)h->d, h->cent, (int)k, h->labels, nullptr, nullptr,
+                       h->scale, h->st, h->stream);
+  }
+  if (r == SC_OK) r = sc_kmeans_get(h, nullptr, nullptr, labels_out, nullptr, nullptr);
+  sc_kmeans_destroy(h);
+  return r;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// kNN handle
+// ---------------------------------------------------------------------------
+struct sc_knn {
+  int dtype = SC_F32;
+  int64_t n = 0, d = 0;
+  cudaStream_t stream = nullptr;
+  void *train = nullptr;  // row-major n x d
+  void *q = nullptr;      // queries, row-major
+  int64_t q_cap = 0;
+  int64_t *idx = nullptr;
+  double *dist = nullptr;
+  int64_t res_cap = 0;
+  int64_t *aux_i = nullptr;  // class indices / outputs
+  double *aux_d = nullptr;
+  int64_t aux_cap = 0;
+  int64_t rescored = 0;
+  SplitKnnState split;
+};
+
+static sc_status knn_reserve(sc_knn *h, int64_t m, int64_t k) {
+  if (m > h->q_cap) {
+    dfree(h->q);
+    SC_TRY(dalloc((char **)&h->q, (size_t)(m * h->d) * esize(h->dtype)));
+    h->q_cap = m;
+  }
+  if (m * k > h->res_cap) {
+    dfree(h->idx); dfree(h->dist);
+    SC_TRY(dalloc(&h->idx, (size_t)(m * k)));
+    SC_TRY(dalloc(&h->dist, (size_t)(m * k)));
+    h->res_cap = m * k;
+  }
+  return SC_OK;
+}
+
+static sc_status knn_run(sc_knn *h, const void *queries, int32_t layout, int32_t mem, int64_t m,
+                         int64_t ld, int64_t k, int32_t form) {
+  SC_TRY(check_matrix(queries, h->dtype, layout, mem, m, h->d, ld));
+  if (k < 1 || k > h->n) {  // linear_search.rs:53-58
+    set_error("k should be >= 1 and <= length(data)");
+    return SC_ERR_INVALID;
+  }
+  if (k > kMaxKnnK) { set_error("k=%lld exceeds the supported maximum %d", (long long)k, kMaxKnnK); return SC_ERR_INVALID; }
+  if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
+  SC_TRY(knn_reserve(h, m, k));
+  SC_TRY(upload_matrix(queries, h->dtype, layout, mem, m, h->d, ld, h->q, h->stream));
+  if (form == SC_FORM_FP64)
+    return launch_knn_fp64(h->dtype, h->train, h->n, (int)h->d, h->q, m, (int)k, h->idx, h->dist, h->stream);
+  return split_knn(&h->split, h->dtype, h->train, h->n, (int)h->d, h->q, m, (int)k, h->idx, h->dist,
+                   &h->rescored, h->stream);
+}
+
+extern "C" {
+
+void sc_knn_destroy(sc_knn *h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  dfree(h->train); dfree(h->q); dfree(h->idx); dfree(h->dist); dfree(h->aux_i); dfree(h->aux_d);
+  split_knn_free(&h->split);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+sc_status sc_knn_create(const void *train, int32_t dtype, int32_t layout, int32_t mem, int64_t n,
+                        int64_t d, int64_t ld, sc_knn **out) {
+  if (!out) { set_error("null output handle"); return SC_ERR_INVALID; }
+  *out = nullptr;
+  SC_TRY(check_matrix(train, dtype, layout, mem, n, d, ld));
+  if (n >= ((int64_t)1 << 31)) { set_error("n=%lld exceeds 2^31-1 training rows", (long long)n); return SC_ERR_INVALID; }
+  sc_knn *h = new sc_knn();
+  h->dtype = dtype; h->n = n; h->d = d;
+  sc_status r = SC_OK;
+  do {
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "cudaStreamCreate");
+      h->stream = nullptr;
+      break;
+    }
+    if ((r = dalloc((char **)&h->train, (size_t)(n * d) * esize(dtype))) != SC_OK) break;
+    if ((r = upload_matrix(train, dtype, layout, mem, n, d, ld, h->train, h->stream)) != SC_OK) break;
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "upload"); break; }
+  } while (0);
+  if (r != SC_OK) { sc_knn_destroy(h); return r; }
+  *out = h;
+  return SC_OK;
+}
+
+void *sc_knn_stream(sc_knn *h) { return h ? (void *)h->stream : nullptr; }
+
+sc_status sc_knn_stats(sc_knn *h, int64_t *rescored) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (rescored) *rescored = h->rescored;
+  return SC_OK;
+}
+
+sc_status sc_knn_find(sc_knn *h, const void *queries, int32_t layout, int32_t mem, int64_t m,
+                      int64_t ld, int64_t k, int32_t form, int32_t out_mem, int64_t *idx_out,
+                      double *dist_out) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  SC_TRY(knn_run(h, queries, layout, mem, m, ld, k, form));
+  const cudaMemcpyKind kind = out_mem == SC_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (m > 0) {
+    if (idx_out) SC_CUDA(cudaMemcpyAsync(idx_out, h->idx, (size_t)(m * k) * sizeof(int64_t), kind, h->stream));
+    if (dist_out) SC_CUDA(cudaMemcpyAsync(dist_out, h->dist, (size_t)(m * k) * sizeof(double), kind, h->stream));
+  }
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+sc_status sc_knn_classify(sc_knn *h, const void *queries, int32_t layout, int32_t mem, int64_t m,
+                          int64_t ld, int64_t k, int32_t form, int32_t weight,
+                          const int64_t *y_class, int64_t n_classes, int64_t *classes_out) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (!y_class || n_classes < 1) { set_error("invalid class labels"); return SC_ERR_INVALID; }
+  SC_TRY(knn_run(h, queries, layout, mem, m, ld, k, form));
+  if (h->aux_cap < std::max(h->n, m)) {
+    dfree(h->aux_i); dfree(h->aux_d);
+    SC_TRY(dalloc(&h->aux_i, (size_t)(h->n + m)));
+    SC_TRY(dalloc(&h->aux_d, (size_t)(h->n + m)));
+    h->aux_cap = std::max(h->n, m);
+  }
+  SC_CUDA(cudaMemcpyAsync(h->aux_i, y_class, (size_t)h->n * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+  SC_TRY(launch_knn_vote(h->idx, h->dist, m, (int)k, weight, h->aux_i, h->aux_i + h->n, h->stream));
+  if (m > 0) SC_CUDA(cudaMemcpyAsync(classes_out, h->aux_i + h->n, (size_t)m * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+sc_status sc_knn_regress(sc_knn *h, const void *queries, int32_t layout, int32_t mem, int64_t m,
+                         int64_t ld, int64_t k, int32_t form, int32_t weight, const double *y,
+                         double *out) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (!y) { set_error("null targets"); return SC_ERR_INVALID; }
+  SC_TRY(knn_run(h, queries, layout, mem, m, ld, k, form));
+  if (h->aux_cap < std::max(h->n, m)) {
+    dfree(h->aux_i); dfree(h->aux_d);
+    SC_TRY(dalloc(&h->aux_i, (size_t)(h->n + m)));
+    SC_TRY(dalloc(&h->aux_d, (size_t)(h->n + m)));
+    h->aux_cap = std::max(h->n, m);
+  }
+  SC_CUDA(cudaMemcpyAsync(h->aux_d, y, (size_t)h->n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SC_TRY(launch_knn_regress(h->idx, h->dist, m, (int)k, weight, h->aux_d, h->aux_d + h->n, h->stream));
+  if (m > 0) SC_CUDA(cudaMemcpyAsync(out, h->aux_d + h->n, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+// Shared declarations of the smartcore_gb300 CUDA library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/smartcore_gb300.h"
+
+namespace sc {
+
+// ---- host-side error reporting (thread-local message, see sc_last_error) ----
+void set_error(const char *fmt, ...);
+sc_status cuda_fail(cudaError_t e, const char *what);
+
+#define SC_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess) return ::sc::cuda_fail(e_, #call);                \
+  } while (0)
+
+#define SC_TRY(expr)                                                         \
+  do {                                                                       \
+    sc_status s_ = (expr);                                                   \
+    if (s_ != SC_OK) return s_;                                              \
+  } while (0)
+
+// ---- device-resident state of one Lloyd loop ----
+struct LloydState {
+  double distortion;   // the reference's `distortion` (starts at f64::MAX)
+  double last_dist;    // distortion of the most recent clustering step
+  int64_t iters;       // clustering steps executed
+  int64_t rescored;    // split form: points re-scored in FP64
+  int64_t pp_replays;  // k-means++ draws resolved by the sequential replay
+  int32_t done;        // break rule taken (kmeans.rs:305-309)
+  int32_t stop;        // 1: apply the break rule; 0: run every iteration
+  int32_t err;         // device-side consistency failure code (0 = none)
+  int32_t pp_flag;     // k-means++: current draw needs the sequential replay
+  int64_t pp_chosen;   // k-means++: row index of the current seed
+};
+
+// 128-bit fixed-point accumulator word pair (lo, hi), two's complement.
+struct Acc128 {
+  unsigned long long lo, hi;
+};
+
+constexpr int kMaxKnnK = 64;  // largest k served by the kNN kernels
+
+// ---- kernel launchers (defined in the .cu files) ----
+// exact.cu: FP64 forms with the reference's operation order.
+sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
+                             const double *cent, int k, int32_t *labels,
+                             double *part, const LloydState *st,
+                             cudaStream_t s);
+sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
+                           const LloydState *st, int32_t label_of_seed,
+                           double *dd, int32_t *labels, double *part,
+                           int first_pass, cudaStream_t s);
+sc_status launch_pp_select(const double *dd, const double *part, int64_t n,
+                           int nb, const double *uniform, LloydState *st,
+                           cudaStream_t s);
+sc_status launch_knn_fp64(int dtype, const void *train, int64_t n, int d,
+                          const void *queries, int64_t m, int k, int64_t *idx,
+                          double *dist, cudaStream_t s);
+sc_status launch_knn_vote(const int64_t *idx, const double *dist, int64_t m,
+                          int k, int weight, const int64_t *y_class,
+                          int64_t *out, cudaStream_t s);
+sc_status launch_knn_regress(const int64_t *idx, const double *dist,
+                             int64_t m, int k, int weight, const double *y,
+                             double *out, cudaStream_t s);
+int pp_block_count(int64_t n);
+int assign_block_count(int64_t n);
+
+// update.cu: centroid sums, counts and the end-of-iteration step.
+sc_status launch_update_fixed(int dtype, const void *x, int64_t n, int d,
+                              const int32_t *labels, Acc128 *acc,
+                              unsigned long long *cnt, int scale,
+                              const LloydState *st, cudaStream_t s);
+sc_status launch_finalize_centroids(Acc128 *acc, unsigned long long *cnt,
+                                    double *cent, int64_t *sizes, int k, int d,
+                                    int scale, double *cluster_terms,
+                                    int empty_nan, const LloydState *st,
+                                    cudaStream_t s);
+sc_status launch_finalize_scalar(const double *part, int nparts,
+                                 const double *cluster_terms, int k,
+                                 const double *xnorm_total, LloydState *st,
+                                 cudaStream_t s);
+sc_status launch_absmax(int dtype, const void *x, int64_t count,
+                        unsigned long long *out_bits, cudaStream_t s);
+sc_status launch_to_row_major(int dtype, const void *src, int64_t n, int64_t d,
+                              int64_t ld, void *dst, cudaStream_t s);
+
+}  // namespace sc

@@ -1,0 +1,185 @@
+"""Brute-force kNN on the GPU with smartcore's API.
+
+Mirrors LinearKNNSearch (src/algorithm/neighbour/linear_search.rs),
+KNNClassifier (src/neighbors/knn_classifier.rs) and KNNRegressor
+(src/neighbors/knn_regressor.rs).  find() returns, per query, the
+reference's heap array in its own order; the classifier vote and the
+regressor mean run on the device in that order.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .error import Failed, FailedError
+from .linalg import as_matrix, layout_of
+
+
+class KNNAlgorithmName(enum.Enum):
+    """src/algorithm/neighbour/mod.rs:53-59.  Both names are served by the
+    GPU brute-force search: it returns the exact k nearest neighbours, which
+    is also what the cover tree returns (only the order of exact ties inside
+    the returned set can differ from a cover-tree search)."""
+    LinearSearch = 0
+    CoverTree = 1
+
+
+class KNNWeightFunction(enum.IntEnum):
+    """src/neighbors/mod.rs:53-59."""
+    Uniform = 0
+    Distance = 1
+
+
+class LinearKNNSearch:
+    """Training rows resident on the device (sc_knn handle)."""
+
+    def __init__(self, data, form=_lib.FORM_FP64):
+        L = _lib.load()
+        a = as_matrix(data)
+        self.dtype = a.dtype
+        self.n, self.d = a.shape
+        lay, ld = layout_of(a)
+        dt = _lib.F32 if a.dtype == np.float32 else _lib.F64
+        h = C.c_void_p()
+        _lib.check(L.sc_knn_create(_lib.ptr(a), dt, lay, _lib.MEM_HOST, self.n, self.d, ld, C.byref(h)))
+        self._L, self.h, self.form = L, h, form
+
+    def _q(self, queries):
+        a = as_matrix(queries, dtype=self.dtype)
+        if a.shape[1] != self.d:
+            raise Failed(FailedError.FindFailed, "Input vector sizes are different.")
+        return a
+
+    def find_batch(self, queries, k):
+        """find() for every row of queries: (idx, dist), each m x k, heap order."""
+        a = self._q(queries)
+        m = a.shape[0]
+        lay, ld = layout_of(a)
+        idx = np.zeros((m, max(k, 1)), np.int64)
+        dist = np.zeros((m, max(k, 1)), np.float64)
+        _lib.check(self._L.sc_knn_find(self.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, k, self.form,
+                                       _lib.MEM_HOST, _lib.ptr(idx), _lib.ptr(dist)), FailedError.FindFailed)
+        return idx, dist
+
+    def find(self, from_, k):
+        """LinearKNNSearch::find: list of (index, distance) in heap order,
+        entries with index None dropped (linear_search.rs:79-83)."""
+        idx, dist = self.find_batch(np.asarray(from_)[None, :], k)
+        return [(int(i), float(dd)) for i, dd in zip(idx[0], dist[0]) if i >= 0]
+
+    def classify(self, queries, k, weight, y_class, n_classes):
+        a = self._q(queries)
+        m = a.shape[0]
+        lay, ld = layout_of(a)
+        out = np.zeros(m, np.int64)
+        yc = np.ascontiguousarray(y_class, np.int64)
+        _lib.check(self._L.sc_knn_classify(self.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, k, self.form,
+                                           int(weight), _lib.ptr(yc), n_classes, _lib.ptr(out)),
+                   FailedError.PredictFailed)
+        return out
+
+    def regress(self, queries, k, weight, y):
+        a = self._q(queries)
+        m = a.shape[0]
+        lay, ld = layout_of(a)
+        out = np.zeros(m, np.float64)
+        yy = np.ascontiguousarray(y, np.float64)
+        _lib.check(self._L.sc_knn_regress(self.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, k, self.form,
+                                          int(weight), _lib.ptr(yy), _lib.ptr(out)),
+                   FailedError.PredictFailed)
+        return out
+
+    def rescored(self):
+        v = np.zeros(1, np.int64)
+        _lib.check(self._L.sc_knn_stats(self.h, _lib.ptr(v)))
+        return int(v[0])
+
+    def stream(self):
+        return self._L.sc_knn_stream(self.h)
+
+    def close(self):
+        if self.h:
+            self._L.sc_knn_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class KNNClassifierParameters:
+    """knn_classifier.rs:48-69, :144-154 (defaults: k=3, CoverTree, Uniform,
+    Euclidean).  `form` selects FP64 or split-BF16 distances."""
+    k: int = 3
+    algorithm: KNNAlgorithmName = KNNAlgorithmName.CoverTree
+    weight: KNNWeightFunction = KNNWeightFunction.Uniform
+    form: int = _lib.FORM_FP64
+
+    def with_k(self, k):
+        self.k = k
+        return self
+
+    def with_algorithm(self, a):
+        self.algorithm = a
+        return self
+
+    def with_weight(self, w):
+        self.weight = w
+        return self
+
+    def with_form(self, f):
+        self.form = f
+        return self
+
+
+@dataclass
+class KNNRegressorParameters(KNNClassifierParameters):
+    """knn_regressor.rs defaults: k=3, CoverTree, Uniform, Euclidean."""
+
+
+class KNNClassifier:
+    @staticmethod
+    def fit(x, y, parameters: KNNClassifierParameters = None) -> "KNNClassifier":
+        p = parameters or KNNClassifierParameters()
+        a = as_matrix(x)
+        y = np.asarray(y)
+        classes = np.unique(y)  # y.unique(): sorted, deduplicated (arrays.rs:223-231)
+        yi = np.searchsorted(classes, y).astype(np.int64)
+        if a.shape[0] != y.shape[0]:  # knn_classifier.rs:237-241
+            raise Failed.fit(f"Size of x should equal size of y; |x|=[{a.shape[0]}], |y|=[{y.shape[0]}]")
+        if p.k <= 1:  # :243-248
+            raise Failed.fit(f"k should be > 1, k=[{p.k}]")
+        m = KNNClassifier()
+        m.classes, m.y, m.k, m.weight = classes, yi, p.k, p.weight
+        m.knn = LinearKNNSearch(a, form=p.form)
+        return m
+
+    def predict(self, x) -> np.ndarray:
+        cls = self.knn.classify(x, self.k, self.weight, self.y, len(self.classes))
+        return self.classes[cls]
+
+
+class KNNRegressor:
+    @staticmethod
+    def fit(x, y, parameters: KNNRegressorParameters = None) -> "KNNRegressor":
+        p = parameters or KNNRegressorParameters()
+        a = as_matrix(x)
+        y = np.asarray(y, np.float64)
+        if a.shape[0] != y.shape[0]:  # knn_regressor.rs:224-228
+            raise Failed.fit(f"Size of x should equal size of y; |x|=[{a.shape[0]}], |y|=[{y.shape[0]}]")
+        if p.k < 1:  # :230-235
+            raise Failed.fit(f"k should be > 0, k=[{p.k}]")
+        m = KNNRegressor()
+        m.y, m.k, m.weight = y, p.k, p.weight
+        m.knn = LinearKNNSearch(a, form=p.form)
+        return m
+
+    def predict(self, x) -> np.ndarray:
+        return self.knn.regress(x, self.k, self.weight, self.y)

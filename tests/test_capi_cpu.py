@@ -1,0 +1,88 @@
+"""CPU-side checks of the C ABI: the library builds, loads and exports every
+symbol the header declares; argument validation answers with the
+reference's messages without touching a GPU; the host-side rand 0.8
+restatement agrees with the oracle's independent one."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from smartcore_gb300 import _lib, build
+from smartcore_gb300.cluster import KMeans, KMeansParameters, kmeanspp_draws
+from smartcore_gb300.error import Failed, FailedError
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    build.build()
+    return _lib.load()
+
+
+def header_symbols():
+    with open(os.path.join(ROOT, "include", "smartcore_gb300.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(L):
+    syms = header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(L, s), s
+    assert set(syms) == set(_lib.SIGNATURES), set(syms) ^ set(_lib.SIGNATURES)
+
+
+def test_version_and_device(L):
+    assert L.sc_abi_version() == 100
+    assert L.sc_device_ok() in (0, 1)
+
+
+def test_kmeans_fit_validation_messages(L):
+    x = np.array([[1.0, 2.0, 3.0], [4.0, 5.0, 6.0]])
+    out = np.zeros(16)
+    for k, msg in ((0, "invalid number of clusters: 0"), (1, "invalid number of clusters: 1")):
+        rc = L.sc_kmeans_fit(_lib.ptr(x), _lib.F64, _lib.ROW_MAJOR, 2, 3, 3, k, 100, 0, _lib.ptr(out), 0,
+                             _lib.ptr(out), _lib.ptr(out), _lib.ptr(out), _lib.ptr(out), _lib.ptr(out))
+        assert rc == _lib.SC_ERR_INVALID
+        assert _lib.last_error() == msg
+    rc = L.sc_kmeans_fit(_lib.ptr(x), _lib.F64, _lib.ROW_MAJOR, 2, 3, 3, 2, 0, 0, _lib.ptr(out), 0,
+                         _lib.ptr(out), _lib.ptr(out), _lib.ptr(out), _lib.ptr(out), _lib.ptr(out))
+    assert rc == _lib.SC_ERR_INVALID
+    assert _lib.last_error() == "invalid maximum number of iterations: 0"
+
+
+def test_python_mirror_messages():
+    x = np.array([[1.0, 2.0, 3.0], [4.0, 5.0, 6.0]])
+    with pytest.raises(Failed) as e:
+        KMeans.fit(x, KMeansParameters().with_k(1))
+    assert str(e.value) == "Fit failed: invalid number of clusters: 1"  # kmeans.rs:434-442
+    assert e.value.error() == FailedError.FitFailed
+
+
+def test_bad_arguments_rejected(L):
+    h = C.c_void_p()
+    x = np.zeros((4, 3))
+    assert L.sc_kmeans_create(_lib.ptr(x), 7, 0, 0, 4, 3, 3, 0, C.byref(h)) == _lib.SC_ERR_INVALID
+    assert L.sc_kmeans_create(_lib.ptr(x), 1, 0, 0, 4, 3, 2, 0, C.byref(h)) == _lib.SC_ERR_INVALID
+    assert "leading dimension" in _lib.last_error()
+    assert L.sc_knn_create(None, 1, 0, 0, 4, 3, 3, C.byref(h)) == _lib.SC_ERR_INVALID
+
+
+@pytest.mark.parametrize("rng", [_lib.RNG_SMALL, _lib.RNG_STD])
+@pytest.mark.parametrize("n,k,seed", [(10, 3, 0), (10_000, 8, 42), (1_000_000, 256, 3), (7, 2, 2**63 + 5)])
+def test_draws_match_oracle(rng, n, k, seed):
+    first, u = kmeanspp_draws(n, k, seed, rng)
+    of, ou = oracle.kmeanspp_draws(n, k, seed, rng)
+    assert first == of
+    assert np.array_equal(u, ou)
+
+
+def test_draws_reject_empty(L):
+    a = np.zeros(2, np.int64)
+    assert L.sc_kmeanspp_draws(0, 0, 0, 2, _lib.ptr(a), _lib.ptr(a)) == _lib.SC_ERR_INVALID

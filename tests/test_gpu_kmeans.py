@@ -1,0 +1,127 @@
+"""GPU parity of the KMeans path against the CPU oracle (through the C ABI).
+
+Bar: labels bit-identical, centroids within 1e-12 relative, distortion within
+1e-12 relative, iteration count equal (both stop when the distortion stops
+strictly decreasing, kmeans.rs:305-309).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from smartcore_gb300 import _lib
+from smartcore_gb300.cluster import KMeans, KMeansHandle, KMeansParameters, kmeanspp_draws
+from smartcore_gb300.linalg import DenseMatrix
+from tests.datagen import blobs, kmeans_small_f64
+
+pytestmark = pytest.mark.gpu
+
+FORMS = [pytest.param(_lib.FORM_FP64, id="fp64"), pytest.param(_lib.FORM_SPLIT_BF16, id="split")]
+CENT_RTOL = 1e-12
+
+
+def rel_err(a, b):
+    scale = np.maximum(np.abs(b).max(axis=-1, keepdims=True), 1e-300)
+    return float((np.abs(a - b) / scale).max())
+
+
+def assert_fit_parity(x, k, max_iter, seed, form):
+    gpu = KMeans.fit(x, KMeansParameters(k=k, max_iter=max_iter, seed=seed, form=form))
+    ref = oracle.kmeans_fit(x, k, max_iter, seed=0 if seed is None else seed)
+    assert np.array_equal(gpu._y, ref.labels)
+    assert np.array_equal(gpu.size, ref.sizes)
+    assert rel_err(gpu.centroids, ref.centroids) <= CENT_RTOL
+    assert abs(gpu._distortion - ref.distortion) <= 1e-12 * abs(ref.distortion)
+    assert gpu.iters == ref.iters
+    return gpu, ref
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_small_f64_blobs(form):
+    """Plain KMeans f64: 10,000 x 16, k=8, max_iter=100, seed 42."""
+    x, _ = kmeans_small_f64()
+    assert_fit_parity(x, 8, 100, 42, form)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_f32_layouts(form, order):
+    x, _ = blobs(5000, 24, 12, seed=4, dtype=np.float32)
+    assert_fit_parity(np.asarray(x, order=order), 12, 60, 7, form)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_iris_fit_predict(kats, form):
+    """kmeans.rs:473-505 on the GPU: predict(x) == fit labels, default params."""
+    x = DenseMatrix.from_2d_array(kats["kmeans_fit_predict"]["x"])
+    gpu, ref = assert_fit_parity(x.array(), 2, 100, None, form)
+    p = KMeans.fit(x, KMeansParameters(form=form)).predict(x)
+    assert np.array_equal(p, gpu._y)
+
+
+def test_bbdtree_iris_step(kats):
+    """One clustering step from the bbdtree_iris centroids (bbd_tree.rs:323-364)."""
+    kat = kats["bbdtree_iris"]
+    x = np.array(kat["x"])
+    h = KMeansHandle(x)
+    h.set_centroids(np.array(kat["centroids"]))
+    assert h.iterate(1) == 1
+    cent, sizes, labels, dist, _ = h.get()
+    r_dist, r_sums, r_counts, r_memb = oracle.bbd_clustering(x, np.array(kat["centroids"]))
+    assert np.array_equal(labels, r_memb)
+    assert np.array_equal(sizes, r_counts)
+    assert abs(dist - r_dist) <= 1e-12 * r_dist
+    for name, want, tol in kat["expect_close"]:
+        if name == "dist":
+            assert abs(dist - want) < tol
+    assert rel_err(cent, r_sums / r_counts[:, None]) <= CENT_RTOL
+    h.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_kmeanspp_labels(dtype):
+    x, _ = blobs(20_000, 8, 16, seed=12, dtype=dtype)
+    first, u = kmeanspp_draws(len(x), 16, 5)
+    h = KMeansHandle(x)
+    h.seed(16, first, u)
+    _, sizes, labels, _, _ = h.get()
+    y, _ = oracle.kmeanspp(x, 16, first, u)
+    assert np.array_equal(labels, y)
+    assert np.array_equal(sizes, np.bincount(y, minlength=16))
+    h.close()
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_predict_matches_oracle(form):
+    x, _ = blobs(7000, 20, 9, seed=21, dtype=np.float32)
+    c = np.random.default_rng(3).normal(size=(9, 20)) * 5
+    km = KMeans(9, None, None, 0.0, c, 0, form)
+    assert np.array_equal(km.predict(x), oracle.kmeans_predict(x, c))
+
+
+def test_predict_ties_lowest_index():
+    # integer grid: many exact ties between duplicated centroids
+    x = np.random.default_rng(0).integers(-3, 4, size=(3000, 4)).astype(np.float64)
+    c = np.array([[0, 0, 0, 0], [1, 1, 0, 0], [0, 0, 0, 0], [1, 1, 0, 0], [2, 2, 2, 2.0]])
+    km = KMeans(5, None, None, 0.0, c, 0, _lib.FORM_FP64)
+    got = km.predict(x)
+    assert np.array_equal(got, oracle.kmeans_predict(x, c))
+    assert not np.any(got == 2) and not np.any(got == 3)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_edge_shapes(form):
+    x, _ = blobs(64, 3, 4, seed=2)
+    assert_fit_parity(x, 64, 10, 1, form)  # k == n
+    x1 = np.random.default_rng(1).normal(size=(257, 1))
+    assert_fit_parity(x1, 3, 20, 9, form)  # d == 1, n not a multiple of any tile
+    xd = np.repeat(np.random.default_rng(2).normal(size=(10, 5)), 30, axis=0)
+    assert_fit_parity(xd, 4, 20, 3, form)  # duplicated points
+
+
+def test_throughput_mode_runs_all_iterations():
+    x, _ = blobs(4000, 8, 4, seed=5, dtype=np.float32)
+    h = KMeansHandle(x)
+    first, u = kmeanspp_draws(len(x), 4, 0)
+    h.seed(4, first, u)
+    assert h.iterate(17, stop_on_converge=False) == 17
+    h.close()

@@ -1,0 +1,113 @@
+"""GPU parity of LinearKNNSearch::find and the kNN estimators (through the C
+ABI) against the CPU oracle: neighbour indices and distances bit-identical,
+in the reference's heap-array order."""
+import numpy as np
+import pytest
+
+import oracle
+from smartcore_gb300 import _lib
+from smartcore_gb300.neighbors import (KNNAlgorithmName, KNNClassifier, KNNClassifierParameters,
+                                       KNNRegressor, KNNRegressorParameters, KNNWeightFunction,
+                                       LinearKNNSearch)
+from tests.datagen import knn_blobs_f32
+
+pytestmark = pytest.mark.gpu
+
+FORMS = [pytest.param(_lib.FORM_FP64, id="fp64"), pytest.param(_lib.FORM_SPLIT_BF16, id="split")]
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("k", [1, 5, 16])
+def test_find_heap_order(form, dtype, k):
+    rng = np.random.default_rng(k)
+    train = rng.normal(size=(3000, 13)).astype(dtype)
+    q = rng.normal(size=(300, 13)).astype(dtype)
+    s = LinearKNNSearch(train, form=form)
+    idx, dist = s.find_batch(q, k)
+    ridx, rdist = oracle.knn_find(train, q, k)
+    assert np.array_equal(idx, ridx)
+    assert np.array_equal(dist, rdist)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_find_ties_and_duplicates(form):
+    # integer grid data: many exact distance ties, replay order matters
+    rng = np.random.default_rng(0)
+    train = rng.integers(-2, 3, size=(2000, 3)).astype(np.float32)
+    q = rng.integers(-2, 3, size=(200, 3)).astype(np.float32)
+    s = LinearKNNSearch(train, form=form)
+    for k in (1, 4, 7):
+        idx, dist = s.find_batch(q, k)
+        ridx, rdist = oracle.knn_find(train, q, k)
+        assert np.array_equal(idx, ridx)
+        assert np.array_equal(dist, rdist)
+
+
+def test_find_k_equals_n_and_errors():
+    train = np.random.default_rng(1).normal(size=(9, 4))
+    s = LinearKNNSearch(train)
+    idx, dist = s.find_batch(train, 9)
+    ridx, rdist = oracle.knn_find(train, train, 9)
+    assert np.array_equal(idx, ridx) and np.array_equal(dist, rdist)
+    for bad in (0, 10):
+        with pytest.raises(Exception) as e:
+            s.find_batch(train, bad)
+        assert "k should be >= 1 and <= length(data)" in str(e.value)
+
+
+def test_reference_kats(kats):
+    kat = kats["knn_find"]
+    e = kat["euclid"]
+    s = LinearKNNSearch(np.array(e["data"]))
+    got = s.find(np.array(e["query"]), e["k"])
+    assert sorted(i for i, _ in got) == e["expect_sorted_idx"]
+    sc = kat["scalar"]
+    s1 = LinearKNNSearch(np.array(sc["data"], np.float64)[:, None])
+    assert sorted(i for i, _ in s1.find(np.array([float(sc["query"])]), sc["k"])) == sc["expect_sorted_idx"]
+
+    w = kats["knn_classifier_weighted"]
+    m = KNNClassifier.fit(np.array(w["x"]), np.array(w["y"], np.int64),
+                          KNNClassifierParameters().with_k(w["k"])
+                          .with_algorithm(KNNAlgorithmName.LinearSearch)
+                          .with_weight(KNNWeightFunction.Distance))
+    assert list(m.predict(np.array(w["query"]))) == w["expect"]
+
+    dflt = kats["knn_classifier_default"]
+    x = np.array(dflt["x"])
+    m = KNNClassifier.fit(x, np.array(dflt["y"], np.int64))
+    assert list(m.predict(x)) == dflt["y"]
+
+    for key in ("knn_regressor_weighted", "knn_regressor_uniform"):
+        r = kats[key]
+        p = KNNRegressorParameters().with_k(r["k"]).with_algorithm(KNNAlgorithmName.LinearSearch)
+        if r["weight"] == "distance":
+            p = p.with_weight(KNNWeightFunction.Distance)
+        m = KNNRegressor.fit(np.array(r["x"]), np.array(r["y"]), p)
+        out = m.predict(np.array(r["x"]))
+        assert np.all(np.abs(out - np.array(r["expect"])) < r["tol"])
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("weight", [0, 1])
+def test_classifier_matches_oracle(form, weight):
+    xt, yt, xq, _ = knn_blobs_f32(n_train=20_000, n_query=2_000, seed=3)
+    m = KNNClassifier.fit(xt, yt, KNNClassifierParameters(k=5, algorithm=KNNAlgorithmName.LinearSearch,
+                                                         weight=KNNWeightFunction(weight), form=form))
+    got = m.predict(xq)
+    idx, dist = oracle.knn_find(xt, xq, 5)
+    want = oracle.knn_vote(idx, dist, yt, 10, weight=weight)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("weight", [0, 1])
+def test_regressor_matches_oracle(weight):
+    rng = np.random.default_rng(8)
+    xt = rng.normal(size=(5000, 6))
+    y = rng.normal(size=5000)
+    xq = rng.normal(size=(500, 6))
+    m = KNNRegressor.fit(xt, y, KNNRegressorParameters(k=4, algorithm=KNNAlgorithmName.LinearSearch,
+                                                       weight=KNNWeightFunction(weight)))
+    got = m.predict(xq)
+    idx, dist = oracle.knn_find(xt, xq, 4)
+    assert np.array_equal(got, oracle.knn_regress(idx, dist, y, weight=weight))
