@@ -1,0 +1,342 @@
+"""Benchmark of the distance-argmin path: Lloyd iterations per second of
+KMeans on 1,000,000 x 64 float32 points, k = 256 (anisotropic Gaussian
+clusters, Dirichlet(2) sizes), split-BF16 form.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one full Lloyd iteration over the whole dataset (assignment,
+FP64 re-score of near ties, centroid sums, new centroids, distortion and
+break test), inputs resident in HBM.  Under torchrun each rank runs an
+independent replica of the workload on its own GPU (the path has no
+cross-GPU exchange); value = iterations of all ranks / max-over-ranks time.
+
+--impl reference times the reference algorithm on the host CPU: the C
+restatement of smartcore's KMeans Lloyd step (BBD-tree filtering, single
+thread, as the reference) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, D, K_CLUSTERS, MAX_ITER = 1_000_000, 64, 256, 50
+SEED_DATA, SEED_KMEANS = 3, 42
+CPU_SAMPLE = 32_768  # points of the workload timed on the host CPU
+METRIC = "k-means Lloyd iter/s (1Mx64, k=256)"
+UNIT = "iter/s"
+WORKLOAD = "kmeans_f32_1Mx64_k256_anisotropic_dirichlet"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 20 ms) of SM clocks and throttle reasons;
+    summary() keeps the samples taken inside the timed region."""
+
+    Q = ("timestamp,clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.p, self.rows, self.t0, self.t1 = index, None, [], None, None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "20"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(1.0)  # let the sampler start before the timed region
+        except OSError:
+            self.p = None
+        return self
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
+    def __exit__(self, *a):
+        if self.p is None:
+            return
+        time.sleep(0.1)
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        import datetime
+        for line in out.strip().splitlines():
+            f = [t.strip() for t in line.split(",")]
+            if len(f) != 7:
+                continue
+            try:
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                continue
+            self.rows.append((ts, f[1:]))
+
+    def summary(self):
+        inside = [r for ts, r in self.rows if self.t0 is not None and self.t0 - 0.02 <= ts <= self.t1 + 0.02]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no sample inside the timed region"],
+                    "samples": 0}
+        num = lambda v: float(v) if v.replace(".", "", 1).isdigit() else None
+        sm = [num(r[0]) for r in inside if num(r[0]) is not None]
+        mx = [num(r[1]) for r in inside if num(r[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in inside for i in range(4) if r[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(inside)}
+
+
+def cpu_baseline(x, seed_centroids, iters=3):
+    """The reference Lloyd step (BBD tree, 1 thread) on a CPU_SAMPLE-point
+    sample; returns the full-size rate by linear scaling in n."""
+    import oracle
+    sub = np.ascontiguousarray(x[:CPU_SAMPLE])
+    build, secs, _, _ = oracle.bbd_lloyd_timed(sub, seed_centroids, iters)
+    per_iter = float(np.median(secs))
+    return {
+        "value": (1.0 / per_iter) * (CPU_SAMPLE / N),
+        "unit": UNIT,
+        "cores": 1,
+        "kind": "port",
+        "sample": (f"C restatement of KMeans Lloyd step (BBD-tree filtering, src/algorithm/neighbour/"
+                   f"bbd_tree.rs) on the first {CPU_SAMPLE} of {N} points, k={K_CLUSTERS}; median of "
+                   f"{iters} iterations = {per_iter:.3f} s; rate scaled by {CPU_SAMPLE}/{N}; tree build "
+                   f"{build:.3f} s excluded; single thread (the reference is single-threaded); "
+                   f"host has {os.cpu_count()} cores"),
+    }
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from smartcore_gb300.synthetic import anisotropic_dirichlet_f32
+    x, _ = anisotropic_dirichlet_f32(N, D, K_CLUSTERS, seed=SEED_DATA)
+    import oracle
+
+    def start(m):
+        sub = np.ascontiguousarray(x[:m])
+        first, u = oracle.kmeanspp_draws(m, K_CLUSTERS, SEED_KMEANS)
+        y0, _ = oracle.kmeanspp(sub, K_CLUSTERS, first, u)
+        c0 = np.zeros((K_CLUSTERS, D))
+        np.add.at(c0, y0, sub.astype(np.float64))
+        c0 /= np.maximum(np.bincount(y0, minlength=K_CLUSTERS), 1)[:, None]
+        return sub, c0
+
+    # size the per-step sample so that warmup + steps stay within ~2 minutes
+    sub, c0 = start(4096)
+    _, secs, _, _ = oracle.bbd_lloyd_timed(sub, c0, 3)
+    per_point = float(np.median(secs)) / 4096
+    budget = 120.0 / (args.warmup + args.steps)
+    m = int(min(CPU_SAMPLE, max(2048, budget / per_point)) // 1024 * 1024)
+    sub, c0 = start(m)
+    build, secs, _, _ = oracle.bbd_lloyd_timed(sub, c0, args.warmup + args.steps)
+    timed = secs[args.warmup:]
+    total = float(timed.sum())
+    value = (args.steps / total) * (m / N)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps * (N / m),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "n": N, "d": D, "k": K_CLUSTERS,
+                                        "form": "reference CPU (BBD tree)", "sample_points": m},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": (f"each step = one BBD-tree Lloyd iteration on the first {m} of "
+                                    f"{N} points (k={K_CLUSTERS}, d={D}); rate scaled by {m}/{N}; "
+                                    f"tree build {build:.3f} s excluded; single thread, host has "
+                                    f"{os.cpu_count()} cores")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from smartcore_gb300 import _lib
+    from smartcore_gb300.cluster import KMeans, KMeansHandle, KMeansParameters, kmeanspp_draws
+    from smartcore_gb300.synthetic import anisotropic_dirichlet_f32
+    L = _lib.load()
+    if not L.sc_device_ok():
+        raise RuntimeError("no usable sm_103 device")
+
+    x, _ = anisotropic_dirichlet_f32(N, D, K_CLUSTERS, seed=SEED_DATA)
+    x_pinned = torch.from_numpy(x).pin_memory()
+    x_dev = x_pinned.to(f"cuda:{local}", non_blocking=False)
+    first, u = kmeanspp_draws(N, K_CLUSTERS, SEED_KMEANS)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident throughput, split-BF16 form ----
+    h = KMeansHandle(None, form=_lib.FORM_SPLIT_BF16, device_ptr=x_dev.data_ptr(), dtype=np.float32,
+                     shape=(N, D))
+    h.seed(K_CLUSTERS, first, u)
+    c_start, _, _, _, _ = h.get()
+    stream = torch.cuda.ExternalStream(h.stream())
+    for _ in range(args.warmup):
+        h.iterate(1, stop_on_converge=False, wait=False)
+    h.sync()
+    L.sc_kmeans_profile(h.h, 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = L.sc_kernel_launches()
+    barrier()
+    with ClockSampler(local) as clk:
+        clk.mark_start()
+        e0.record(stream)
+        h.iterate(args.steps, stop_on_converge=False, wait=False)
+        e1.record(stream)
+        e1.synchronize()
+        clk.mark_end()
+    launches = L.sc_kernel_launches() - launches0
+    barrier()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    kms = np.zeros(1)
+    kl = np.zeros(1, np.int64)
+    L.sc_kmeans_profile_read(h.h, _lib.ptr(kms), _lib.ptr(kl))
+    L.sc_kmeans_profile(h.h, 0)
+    rescored, _ = h.stats()
+    kernel_ms = float(kms[0]) / max(int(kl[0]), 1)
+    value = ws * args.steps / (ms / 1e3)
+
+    if rank != 0 or args.lloyd_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "steps": args.steps,
+                              "ms_per_step": ms / args.steps, "kernel_ms": kernel_ms,
+                              "gpu_launches": int(launches), "mode": "lloyd-only"}), flush=True)
+        h.close()
+        return
+
+    # ---- same start, FP64 form: rate and agreement of labels / distortion ----
+    hf = KMeansHandle(None, form=_lib.FORM_FP64, device_ptr=x_dev.data_ptr(), dtype=np.float32,
+                      shape=(N, D))
+    hs = KMeansHandle(None, form=_lib.FORM_SPLIT_BF16, device_ptr=x_dev.data_ptr(), dtype=np.float32,
+                      shape=(N, D))
+    agree = []
+    fp64_ms = []
+    for hh in (hf, hs):
+        hh.set_centroids(c_start)
+    for it in range(2):
+        t0 = time.perf_counter()
+        hf.iterate(1, stop_on_converge=False)
+        fp64_ms.append((time.perf_counter() - t0) * 1e3)
+        hs.iterate(1, stop_on_converge=False)
+        cf, sf, lf, df, _ = hf.get()
+        cs, ss, ls, dsp, _ = hs.get()
+        agree.append({"labels_equal": bool(np.array_equal(lf, ls)),
+                      "inertia_rel_err": abs(dsp - df) / abs(df),
+                      "centroid_max_rel_err": float(np.max(np.abs(cs - cf)) / np.max(np.abs(cf)))})
+    hf.close()
+    hs.close()
+
+    # ---- end to end through the public API: host buffers in and out ----
+    e2e_steps = max(1, min(3, args.steps))
+    e2e_iters, e2e_time = 0, 0.0
+    xh = x_pinned.numpy()
+    for s in range(e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        km = KMeans.fit(xh, KMeansParameters(k=K_CLUSTERS, max_iter=MAX_ITER, seed=SEED_KMEANS,
+                                             form=_lib.FORM_SPLIT_BF16))
+        dt = time.perf_counter() - t0
+        if s > 0:  # first call warms the allocator and the module
+            e2e_iters += km.iters
+            e2e_time += dt
+    h2d = N * D * 4 + 8 * K_CLUSTERS
+    d2h = K_CLUSTERS * D * 8 + K_CLUSTERS * 8 + N * 8 + 16
+
+    pk, pk_kind = peaks()
+    flop = 2.0 * N * K_CLUSTERS * D
+    achieved = flop / (kernel_ms / 1e3) / 1e12
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "split_assign_kmeans_1Mx64_k256.txt")
+    if os.path.exists(tfile):
+        for line in open(tfile):
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = float(line.split(":", 1)[1])
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3-split/fp32-acc/f64-rescore",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": N, "d": D, "k": K_CLUSTERS, "form": "split_bf16",
+                   "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (256 MB bf16 + 256 MB f32 "
+                   "read per step)"},
+        "roofline": {"bound": "tensor", "kernel": "split_assign_kernel", "achieved": achieved,
+                     "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"],
+                     "peak_kind": f"{pk_kind} bf16 burst", "traffic": traffic,
+                     "algorithmic_flop_per_launch": flop, "issued_flop_per_launch": 3 * flop,
+                     "kernel_ms": kernel_ms, "algorithmic_bytes_per_launch": N * D * 2 * 2},
+        "cpu_baseline": cpu_baseline(x, c_start),
+        "e2e": {"value": e2e_iters / e2e_time, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "note": f"KMeans.fit with host input: upload, k-means++, up to {MAX_ITER} Lloyd iterations, "
+                        f"results to host; {e2e_iters} iterations in {e2e_time:.3f} s over {e2e_steps} fits"},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "fp64_form": {"value": 1e3 / float(np.median(fp64_ms)), "unit": UNIT,
+                      "split_speedup": value / ws / (1e3 / float(np.median(fp64_ms)))},
+        "parity_vs_fp64_form": agree,
+        "rescored_points": int(rescored),
+    }
+    print(json.dumps(line), flush=True)
+    h.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--lloyd-only", action="store_true",
+                    help="time the device-resident Lloyd loop only (for profiler runs)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

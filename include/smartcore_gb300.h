@@ -69,6 +69,8 @@ const char *sc_last_error(void);
 int32_t sc_abi_version(void);
 /* 1 if a CUDA device of compute capability 10.3 is usable, else 0. */
 int32_t sc_device_ok(void);
+/* Number of CUDA kernels this library has launched in this process. */
+int64_t sc_kernel_launches(void);
 
 /* ------------------------------------------------------------------ */
 /* k-means++ draws                                                     */
@@ -134,6 +136,13 @@ void *sc_kmeans_stream(sc_kmeans *h);
 /* Counters of the last sc_kmeans_iterate: near-tie points re-scored in FP64
  * (split form) and k-means++ draws that needed the sequential replay. */
 sc_status sc_kmeans_stats(sc_kmeans *h, int64_t *rescored, int64_t *pp_replays);
+/* Timing of the assignment kernel: with profiling enabled, every Lloyd
+ * iteration records a CUDA event pair on the handle's stream around its
+ * assignment kernel; profile_read returns the summed elapsed time and the
+ * number of timed launches since the last read (and resets them). */
+sc_status sc_kmeans_profile(sc_kmeans *h, int32_t enable);
+sc_status sc_kmeans_profile_read(sc_kmeans *h, double *total_ms,
+                                 int64_t *launches);
 sc_status sc_kmeans_sync(sc_kmeans *h);
 void sc_kmeans_destroy(sc_kmeans *h);
 

@@ -59,6 +59,8 @@ def lib():
             L.orc_bbd_clustering.argtypes = [I, I, P, I64, I64, I64, P, I64, P, P, P]
             L.orc_bbd_clustering.restype = D
             L.orc_lloyd_bruteforce.argtypes = [I, I, P, I64, I64, I64, I64, I64, P, P, P, P, P]
+            L.orc_bbd_lloyd_timed.argtypes = [I, I, P, I64, I64, I64, I64, I64, P, P, P]
+            L.orc_bbd_lloyd_timed.restype = D
             L.orc_heap_add_sequence.argtypes = [P, I64, I64, P]
             L.orc_heap_add_sequence.restype = I64
             L.orc_knn_find.argtypes = [I, P, I64, I64, P, I64, I64, P, P]
@@ -243,3 +245,15 @@ def knn_regress(idx, dist, y, weight=0):
     out = np.zeros(m, np.float64)
     lib().orc_knn_regress(_ptr(idx), _ptr(dist), m, k, _ptr(y), weight, _ptr(out))
     return out
+
+
+def bbd_lloyd_timed(x, centroids, iters):
+    """(tree build seconds, per-iteration seconds, final centroids, labels)."""
+    dt, lay, x, ld = _mat(x)
+    n, d = x.shape
+    c = np.array(centroids, np.float64, copy=True, order="C")
+    labels = np.zeros(n, np.int64)
+    secs = np.zeros(max(iters, 1), np.float64)
+    build = lib().orc_bbd_lloyd_timed(dt, lay, _ptr(x), n, d, ld, c.shape[0], iters, _ptr(c),
+                                      _ptr(labels), _ptr(secs))
+    return build, secs[:iters], c, labels

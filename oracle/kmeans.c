@@ -4,6 +4,7 @@
  * oracle.h).  Compiled with -ffp-contract=off: every sum below is evaluated
  * left to right, one rounding per operation, as rustc emits it.
  */
+#define _POSIX_C_SOURCE 199309L
 #include "oracle.h"
 
 #include <float.h>
@@ -11,6 +12,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 static char g_err[256];
 const char *orc_last_error(void) { return g_err; }
@@ -393,4 +395,38 @@ void orc_lloyd_bruteforce(int dtype, int layout, const void *x, int64_t n,
   *distortion_out = distortion;
   *iters = it;
   free(row); free(sums);
+}
+
+/* Timing harness for the CPU baseline: builds the BBD tree once, then runs
+ * `iters` Lloyd iterations of KMeans::fit's loop body (kmeans.rs:295-303:
+ * clustering + centroid update; the break rule is not applied) from the
+ * given centroids, recording each iteration's wall time in iter_seconds. */
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+double orc_bbd_lloyd_timed(int dtype, int layout, const void *x, int64_t n,
+                           int64_t d, int64_t ld, int64_t k, int64_t iters,
+                           double *centroids, int64_t *labels,
+                           double *iter_seconds) {
+  mat m = {dtype, layout, x, n, d, ld};
+  double t0 = now_s();
+  tree t;
+  tree_new(&t, &m);
+  double build = now_s() - t0;
+  double *sums = calloc((size_t)(k * d), sizeof(double));
+  int64_t *size = calloc((size_t)k, sizeof(int64_t));
+  for (int64_t it = 0; it < iters; ++it) {
+    double a = now_s();
+    clustering(&t, centroids, k, sums, size, labels);
+    for (int64_t i = 0; i < k; ++i)
+      if (size[i] > 0)
+        for (int64_t j = 0; j < d; ++j) centroids[i * d + j] = sums[i * d + j] / (double)size[i];
+    iter_seconds[it] = now_s() - a;
+  }
+  free(sums); free(size);
+  tree_free(&t);
+  return build;
 }

@@ -74,6 +74,13 @@ void orc_lloyd_bruteforce(int dtype, int layout, const void *x, int64_t n,
                           int64_t *sizes, int64_t *labels, double *distortion,
                           int64_t *iters);
 
+/* CPU-baseline harness: BBD tree built once (returns its build seconds),
+ * then `iters` untested Lloyd iterations from `centroids`, each timed. */
+double orc_bbd_lloyd_timed(int dtype, int layout, const void *x, int64_t n,
+                           int64_t d, int64_t ld, int64_t k, int64_t iters,
+                           double *centroids, int64_t *labels,
+                           double *iter_seconds);
+
 /* ---- HeapSelection (src/algorithm/sort/heap_select.rs) ---- */
 /* Feeds values through HeapSelection::add; writes the k-slot heap array
  * (heap.get()) and returns the element count n. */

@@ -38,6 +38,9 @@ SIGNATURES = {
     "sc_kmeans_get": ([_P, _P, _P, _P, _P, _P], _I32),
     "sc_kmeans_stream": ([_P], _P),
     "sc_kmeans_stats": ([_P, _P, _P], _I32),
+    "sc_kmeans_profile": ([_P, _I32], _I32),
+    "sc_kmeans_profile_read": ([_P, _P, _P], _I32),
+    "sc_kernel_launches": ([], _I64),
     "sc_kmeans_sync": ([_P], _I32),
     "sc_kmeans_destroy": ([_P], None),
     "sc_knn_create": ([_P, _I32, _I32, _I32, _I64, _I64, _I64, _P], _I32),

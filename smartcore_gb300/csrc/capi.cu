@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <vector>
 
 #include "common.cuh"
@@ -16,6 +17,9 @@
 namespace sc {
 
 static thread_local char g_err[512];
+static std::atomic<long long> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const char *fmt, ...) {
   va_list ap;
@@ -124,7 +128,26 @@ struct sc_kmeans {
   unsigned long long *bits = nullptr;
   SplitState split;             // split-BF16 form buffers
   int64_t k_alloc = 0;
+  int profile = 0;                   // record events around each assignment kernel
+  std::vector<cudaEvent_t> events;   // begin/end pairs
+  size_t events_used = 0;
 };
+
+// Next begin/end event pair for timing one assignment kernel (nullptr when
+// profiling is off).
+static cudaEvent_t *next_timing(sc_kmeans *h) {
+  if (!h->profile) return nullptr;
+  if (h->events_used + 2 > h->events.size()) {
+    for (int i = 0; i < 64; ++i) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      h->events.push_back(e);
+    }
+  }
+  cudaEvent_t *ev = &h->events[h->events_used];
+  h->events_used += 2;
+  return ev;
+}
 
 static sc_status kmeans_alloc_k(sc_kmeans *h, int64_t k) {
   if (k <= h->k_alloc) { h->k = k; return SC_OK; }
@@ -173,6 +196,7 @@ void sc_kmeans_destroy(sc_kmeans *h) {
   dfree(h->acc); dfree(h->cnt); dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
   dfree(h->xnorm_total); dfree(h->st); dfree(h->bits);
   split_free(&h->split);
+  for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -272,13 +296,16 @@ static sc_status lloyd_step(sc_kmeans *h) {
   cudaStream_t s = h->stream;
   const int k = (int)h->k, d = (int)h->d;
   if (h->form == SC_FORM_FP64) {
+    cudaEvent_t *ev = next_timing(h);
+    if (ev) SC_CUDA(cudaEventRecord(ev[0], s));
     SC_TRY(launch_assign_fp64(h->dtype, h->x, h->n, d, h->cent, k, h->labels, h->part, h->st, s));
+    if (ev) SC_CUDA(cudaEventRecord(ev[1], s));
     SC_TRY(launch_update_fixed(h->dtype, h->x, h->n, d, h->labels, h->acc, h->cnt, h->scale, h->st, s));
     SC_TRY(launch_finalize_centroids(h->acc, h->cnt, h->cent, h->sizes, k, d, h->scale, h->cterms, 0, h->st, s));
     SC_TRY(launch_finalize_scalar(h->part, assign_block_count(h->n), nullptr, k, nullptr, h->st, s));
   } else {
     SC_TRY(split_assign(&h->split, h->dtype, h->x, h->n, d, h->cent, k, h->labels, h->acc, h->cnt,
-                        h->scale, h->st, s));
+                        h->scale, h->st, s, next_timing(h)));
     SC_TRY(launch_finalize_centroids(h->acc, h->cnt, h->cent, h->sizes, k, d, h->scale, h->cterms, 0, h->st, s));
     SC_TRY(launch_finalize_scalar(nullptr, 0, h->cterms, k, h->xnorm_total, h->st, s));
     SC_TRY(split_centroids_changed(&h->split, h->cent, k, s));
@@ -335,6 +362,30 @@ sc_status sc_kmeans_stats(sc_kmeans *h, int64_t *rescored, int64_t *pp_replays) 
   if (pp_replays) *pp_replays = st.pp_replays;
   return SC_OK;
 }
+
+sc_status sc_kmeans_profile(sc_kmeans *h, int32_t enable) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  h->profile = enable ? 1 : 0;
+  h->events_used = 0;
+  return SC_OK;
+}
+
+sc_status sc_kmeans_profile_read(sc_kmeans *h, double *total_ms, int64_t *launches) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  double tot = 0.0;
+  for (size_t i = 0; i + 1 < h->events_used; i += 2) {
+    float ms = 0.f;
+    SC_CUDA(cudaEventElapsedTime(&ms, h->events[i], h->events[i + 1]));
+    tot += ms;
+  }
+  if (total_ms) *total_ms = tot;
+  if (launches) *launches = (int64_t)(h->events_used / 2);
+  h->events_used = 0;
+  return SC_OK;
+}
+
+int64_t sc_kernel_launches(void) { return (int64_t)g_launches.load(); }
 
 sc_status sc_kmeans_sync(sc_kmeans *h) {
   if (!h) { set_error("null handle"); return SC_ERR_INVALID; }

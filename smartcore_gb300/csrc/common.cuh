@@ -18,6 +18,15 @@ sc_status cuda_fail(cudaError_t e, const char *what);
     if (e_ != cudaSuccess) return ::sc::cuda_fail(e_, #call);                \
   } while (0)
 
+// Every kernel launch of the library is followed by SC_LAUNCHED(): it counts
+// the launch (sc_kernel_launches) and surfaces launch errors.
+void note_launch();
+#define SC_LAUNCHED()                                                        \
+  do {                                                                       \
+    ::sc::note_launch();                                                     \
+    SC_CUDA(cudaGetLastError());                                             \
+  } while (0)
+
 #define SC_TRY(expr)                                                         \
   do {                                                                       \
     sc_status s_ = (expr);                                                   \

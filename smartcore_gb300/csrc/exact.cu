@@ -119,7 +119,7 @@ sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<grid, kAssignThreads, smem, s>>>((const double *)x, n, d, cent, k, ktile, labels, part, st);
   }
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -175,7 +175,7 @@ sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
     pp_update_kernel<float><<<grid, kPPThreads, smem, s>>>((const float *)x, n, d, st, label_of_seed, dd, labels, part, first_pass);
   else
     pp_update_kernel<double><<<grid, kPPThreads, smem, s>>>((const double *)x, n, d, st, label_of_seed, dd, labels, part, first_pass);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -292,9 +292,9 @@ sc_status launch_pp_select(const double *dd, const double *part, int64_t n,
                            int nb, const double *uniform, LloydState *st,
                            cudaStream_t s) {
   pp_select_kernel<<<1, kSelThreads, 0, s>>>(dd, part, n, nb, uniform, st);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   pp_replay_kernel<<<1, 1, 0, s>>>(dd, n, uniform, st);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -401,7 +401,7 @@ sc_status launch_knn_fp64(int dtype, const void *train, int64_t n, int d,
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<grid, nt, smem, s>>>((const double *)train, n, d, (const double *)queries, m, k, idx, dist);
   }
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -479,7 +479,7 @@ sc_status launch_knn_vote(const int64_t *idx, const double *dist, int64_t m,
                           int64_t *out, cudaStream_t s) {
   if (m == 0) return SC_OK;
   knn_vote_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(idx, dist, m, k, weight, y_class, out);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -488,7 +488,7 @@ sc_status launch_knn_regress(const int64_t *idx, const double *dist,
                              double *out, cudaStream_t s) {
   if (m == 0) return SC_OK;
   knn_regress_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(idx, dist, m, k, weight, y, out);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 

@@ -1,19 +1,593 @@
+// Split-BF16 assignment (K5) and FP64 re-score (K6) for the Lloyd loop and
+// KMeans::predict.
+//
+// For a point x and centroids c_j the label is argmin_j D_j, D_j the FP64
+// squared distance in the reference's operation order.  ||x||^2 is common to
+// every j, so the kernel ranks A_j = ||c_j||^2 - 2 x.c_j, with x.c_j from a
+// tcgen05 GEMM on BF16 halves: x = x_h + x_l + r_x, c = c_h + c_l + r_c
+// (|r| <= 2^-16 |.|), x.c ~ x_h.c_h + x_h.c_l + x_l.c_h, FP32 accumulate in
+// TMEM.  A rigorous per-point bound E on |A_j - (D_j - ||x||^2)| certifies the
+// label when the gap between the best and second-best A exceeds 2E; every
+// other point is re-scored in FP64 over the candidates within the bound.
+#include <float.h>
+#include <math.h>
+#include <string.h>
+
 #include "split.cuh"
+#include "tc.cuh"
 
 namespace sc {
 
-static sc_status not_built() {
-  set_error("the split-BF16 form is not available in this build");
-  return SC_ERR_INVALID;
+namespace {
+
+constexpr int kBM = 128;           // points per tile (UMMA M)
+constexpr int kAssignThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every barrier wait
+
+enum { kErrTimeout = 4 };
+
+__device__ __forceinline__ double sqd_term(double a, double b) {
+  const double r = __dsub_rn(a, b);
+  return __dmul_rn(r, r);
 }
 
-sc_status split_prepare(SplitState *, int, const void *, int64_t, int, double *, cudaStream_t) { return not_built(); }
-sc_status split_centroids_changed(SplitState *, const double *, int, cudaStream_t) { return not_built(); }
-sc_status split_assign(SplitState *, int, const void *, int64_t, int, const double *, int, int32_t *, Acc128 *,
-                       unsigned long long *, int, LloydState *, cudaStream_t) { return not_built(); }
-void split_free(SplitState *) {}
+// ---------------------------------------------------------------------------
+// Preparation of the point operand: BF16 halves (row-major, d padded to
+// d_pad), an upper bound of ||x|| in f32, and block sums of ||x||^2 in f64.
+// One warp per point.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void split2(T v, __nv_bfloat16 &h, __nv_bfloat16 &l);
+template <>
+__device__ __forceinline__ void split2<float>(float v, __nv_bfloat16 &h, __nv_bfloat16 &l) {
+  h = __float2bfloat16_rn(v);
+  l = __float2bfloat16_rn(v - __bfloat162float(h));  // v - h is exact in f32
+}
+template <>
+__device__ __forceinline__ void split2<double>(double v, __nv_bfloat16 &h, __nv_bfloat16 &l) {
+  h = __double2bfloat16(v);
+  l = __double2bfloat16(v - (double)__bfloat162float(h));  // exact in f64
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+prep_x_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_pad,
+              __nv_bfloat16 *__restrict__ xh, __nv_bfloat16 *__restrict__ xl,
+              float *__restrict__ xnrm, double *__restrict__ part) {
+  __shared__ double ws[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 8 + w;
+  double s = 0.0;
+  if (i < n_pad) {
+    for (int j = lane; j < d_pad; j += 32) {
+      __nv_bfloat16 h = __float2bfloat16_rn(0.f), l = h;
+      if (i < n && j < d) {
+        const T v = x[i * d + j];
+        split2<T>(v, h, l);
+        s = fma((double)v, (double)v, s);
+      }
+      xh[i * d_pad + j] = h;
+      xl[i * d_pad + j] = l;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    if (i < n_pad) {
+      // sqrt rounded up, then one more f32 ulp: an upper bound of ||x||
+      const float r = __fsqrt_ru(__double2float_ru(s));
+      xnrm[i] = __uint_as_float(__float_as_uint(r) + 1u);
+    }
+    ws[w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < 8; ++q) t += ws[q];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void sum_parts_kernel(const double *__restrict__ part, int nparts, double *__restrict__ out) {
+  __shared__ double ws[32];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += part[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+    *out = t;
+  }
+}
+
+// Centroid operand: BF16 halves of the f64 centroids, ||c||^2 rounded to f32
+// (+inf for padding columns), and an upper bound of max_j ||c_j||.
+__global__ void __launch_bounds__(128)
+prep_c_kernel(const double *__restrict__ cent, int k, int d, int d_pad, int k_cols,
+              __nv_bfloat16 *__restrict__ ch, __nv_bfloat16 *__restrict__ cl,
+              float *__restrict__ cn2, unsigned int *__restrict__ cmax) {
+  __shared__ double ws[4];
+  const int j = blockIdx.x;
+  double s = 0.0;
+  for (int t = threadIdx.x; t < d_pad; t += 128) {
+    __nv_bfloat16 h = __float2bfloat16_rn(0.f), l = h;
+    if (j < k && t < d) {
+      const double v = cent[(int64_t)j * d + t];
+      split2<double>(v, h, l);
+      s = fma(v, v, s);
+    }
+    if (ch) {
+      ch[(int64_t)j * d_pad + t] = h;
+      cl[(int64_t)j * d_pad + t] = l;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double t = ws[0] + ws[1] + ws[2] + ws[3];
+    if (j < k) {
+      cn2[j] = __double2float_rn(t);
+      const float r = __fsqrt_ru(__double2float_ru(t));
+      atomicMax(cmax, __float_as_uint(r) + 1u);
+    } else if (j < k_cols) {
+      cn2[j] = __int_as_float(0x7f800000);  // padding: never the minimum
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K5: persistent tcgen05 assignment kernel.
+// ---------------------------------------------------------------------------
+struct AssignParams {
+  int64_t n;
+  int n_tiles;
+  int nkt, kt_elems, row_bytes;
+  int k, k_pad, k_cols;  // k_cols = k_pad rounded up to 32 (epilogue chunking)
+  int stages;
+  uint32_t tmem_cols;
+  const float *xnrm;
+  const float *cn2;
+  const unsigned int *cmax;
+  float coef_dot;   // |x.c - dot| <= coef_dot * ||x|| * ||c||
+  float coef_ref;   // reference rounding of D: <= coef_ref * (||x|| + ||c||)^2
+  int32_t *labels;
+  int32_t *flag_count;
+  int32_t *flag_list;
+  int32_t *cand;
+  LloydState *st;
+};
+
+__global__ void __launch_bounds__(kAssignThreads, 1)
+split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
+                    const __grid_constant__ CUtensorMap tm_ch, const __grid_constant__ CUtensorMap tm_cl,
+                    const AssignParams p) {
+  if (p.st && p.st->done) return;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int a_blk = kBM * p.row_bytes;               // one (part, k-tile) block of a stage
+  const int a_stage = 2 * p.nkt * a_blk;
+  const int b_blk = p.k_pad * p.row_bytes;           // one (part, k-tile) block of B
+  const int b_bytes = (2 * p.nkt * b_blk + 1023) & ~1023;
+  uint8_t *sB = base;
+  uint8_t *sA = base + b_bytes;
+  float *s_cn2 = (float *)(sA + (size_t)p.stages * a_stage);
+  uint64_t *bars = (uint64_t *)(s_cn2 + p.k_cols);
+  uint64_t *full = bars, *empty = bars + p.stages, *bfull = bars + 2 * p.stages;
+  uint64_t *accfull = bfull + 1, *accempty = bfull + 3, *mma_done = bfull + 5;
+  uint32_t *s_tmem = (uint32_t *)(bfull + 6);
+  int *s_abort = (int *)(s_tmem + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int j = threadIdx.x; j < p.k_cols; j += kAssignThreads) s_cn2[j] = p.cn2[j];
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < p.stages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(bfull, 1);
+    tc::mbar_init(mma_done, 1);
+    for (int a = 0; a < 2; ++a) {
+      tc::mbar_init(&accfull[a], 1);
+      tc::mbar_init(&accempty[a], 128);
+    }
+    *s_abort = 0;
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&tm_xh);
+    tc::prefetch_tmap(&tm_xl);
+    tc::prefetch_tmap(&tm_ch);
+    tc::prefetch_tmap(&tm_cl);
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(s_tmem, p.tmem_cols);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *s_tmem;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      tc::mbar_expect_tx(bfull, (uint32_t)(2 * p.nkt * b_blk));
+      for (int part = 0; part < 2; ++part)
+        for (int kt = 0; kt < p.nkt; ++kt)
+          tc::tma_load_2d(sB + (part * p.nkt + kt) * b_blk, part ? &tm_cl : &tm_ch, bfull, kt * p.kt_elems, 0);
+      int it = 0;
+      for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x, ++it) {
+        const int s = it % p.stages;
+        const uint32_t ph = (uint32_t)(it / p.stages) & 1u;
+        if (!tc::mbar_wait(&empty[s], ph ^ 1u, kWaitNs)) { atomicExch(s_abort, 1); break; }
+        if (*(volatile int *)s_abort) break;
+        tc::mbar_expect_tx(&full[s], (uint32_t)a_stage);
+        uint8_t *dst = sA + (size_t)s * a_stage;
+        for (int part = 0; part < 2; ++part)
+          for (int kt = 0; kt < p.nkt; ++kt)
+            tc::tma_load_2d(dst + (part * p.nkt + kt) * a_blk, part ? &tm_xl : &tm_xh, &full[s],
+                            kt * p.kt_elems, t * kBM);
+      }
+      // drain: every issued stage must land before the CTA may exit
+      const int issued = it;
+      for (int j = (issued > p.stages ? issued - p.stages : 0); j < issued; ++j)
+        tc::mbar_wait(&full[j % p.stages], (uint32_t)(j / p.stages) & 1u, kWaitNs);
+      tc::mbar_wait(bfull, 0, kWaitNs);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_bf16_f32(kBM, p.k_pad);
+      bool ok = tc::mbar_wait(bfull, 0, kWaitNs);
+      const uint32_t sA0 = tc::smem_u32(sA), sB0 = tc::smem_u32(sB);
+      int it = 0;
+      for (int t = blockIdx.x; ok && t < p.n_tiles; t += gridDim.x, ++it) {
+        const int s = it % p.stages, acc = it & 1;
+        const uint32_t ph = (uint32_t)(it / p.stages) & 1u, aph = (uint32_t)(it >> 1) & 1u;
+        if (!tc::mbar_wait(&accempty[acc], aph ^ 1u, kWaitNs) || !tc::mbar_wait(&full[s], ph, kWaitNs)) {
+          ok = false;
+          break;
+        }
+        if (*(volatile int *)s_abort) { ok = false; break; }
+        tc::fence_after_sync();
+        const uint32_t d_tmem = tmem + (uint32_t)(acc * p.k_cols);
+        const uint32_t a0 = sA0 + (uint32_t)(s * a_stage);
+        uint32_t accumulate = 0;
+        // x_h.c_h + x_h.c_l + x_l.c_h
+        for (int prod = 0; prod < 3; ++prod) {
+          const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
+          for (int kt = 0; kt < p.nkt; ++kt)
+            for (int ks = 0; ks < p.kt_elems / 16; ++ks) {
+              const uint64_t ad = tc::smem_desc(a0 + (uint32_t)((pa * p.nkt + kt) * a_blk + ks * 32), p.row_bytes);
+              const uint64_t bd = tc::smem_desc(sB0 + (uint32_t)((pb * p.nkt + kt) * b_blk + ks * 32), p.row_bytes);
+              tc::mma_f16(d_tmem, ad, bd, idesc, accumulate);
+              accumulate = 1;
+            }
+        }
+        tc::mma_commit(&empty[s]);
+        tc::mma_commit(&accfull[acc]);
+      }
+      if (!ok) atomicExch(s_abort, 1);
+      // every MMA of this CTA must be complete before TMEM is released
+      tc::mma_commit(mma_done);
+      tc::mbar_wait(mma_done, 0, kWaitNs);
+    }
+  } else {
+    // ---------------- epilogue: 4 warps, one point per thread ----------------
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int row = q * 32 + lane;
+    const float cmax = __uint_as_float(*p.cmax);
+    int it = 0;
+    for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x, ++it) {
+      const int acc = it & 1;
+      const uint32_t aph = (uint32_t)(it >> 1) & 1u;
+      const bool got = tc::mbar_wait(&accfull[acc], aph, kWaitNs);
+      if (!__all_sync(0xffffffffu, got)) { atomicExch(s_abort, 1); break; }
+      if (__any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) break;
+      tc::fence_after_sync();
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * p.k_cols);
+      float min1 = __int_as_float(0x7f800000), min2 = min1;
+      int arg = 0;
+      for (int c0 = 0; c0 < p.k_cols; c0 += 32) {
+        uint32_t v[32];
+        tc::tmem_ld32(taddr + (uint32_t)c0, v);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          const float a = fmaf(-2.f, __uint_as_float(v[jj]), s_cn2[c0 + jj]);
+          if (a < min1) { min2 = min1; min1 = a; arg = c0 + jj; }
+          else if (a < min2) min2 = a;
+        }
+      }
+      const int64_t i = (int64_t)t * kBM + row;
+      const bool live = i < p.n;
+      const float xn = live ? p.xnrm[i] : 0.f;
+      const float e = p.coef_dot * 2.f * xn * cmax + 0x1p-22f * (cmax * cmax + xn * cmax) +
+                      p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
+      const float thr = 2.1f * e;
+      const bool flagged = live && !(min2 - min1 > thr);
+      if (__any_sync(0xffffffffu, flagged)) {
+        // second pass over the accumulator for the near-tie rows of this warp
+        int nc = 0;
+        int32_t cands[kMaxCand];
+        const float lim = min1 + thr;
+        for (int c0 = 0; c0 < p.k_cols; c0 += 32) {
+          uint32_t v[32];
+          tc::tmem_ld32(taddr + (uint32_t)c0, v);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj) {
+            const float a = fmaf(-2.f, __uint_as_float(v[jj]), s_cn2[c0 + jj]);
+            if (flagged && a <= lim) {
+              if (nc < kMaxCand) cands[nc] = c0 + jj;
+              ++nc;
+            }
+          }
+        }
+        if (flagged) {
+          const int slot = atomicAdd(p.flag_count, 1);
+          p.flag_list[slot] = (int32_t)i;
+          int32_t *cr = p.cand + (int64_t)slot * (1 + kMaxCand);
+          cr[0] = nc <= kMaxCand ? nc : -1;
+          for (int c = 0; c < kMaxCand && c < nc; ++c) cr[1 + c] = cands[c];
+        }
+      }
+      tc::fence_before_sync();
+      tc::mbar_arrive(&accempty[acc]);
+      if (live) p.labels[i] = arg;
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, p.tmem_cols);
+  }
+  if (threadIdx.x == 0 && *s_abort && p.st) atomicExch(&p.st->err, kErrTimeout);
+}
+
+// ---------------------------------------------------------------------------
+// K6: FP64 re-score of the near-tie points.  One warp per point: each lane
+// takes candidates (or all centroids when the candidate list overflowed),
+// computes D_j in the reference order (kmeans.rs:338-346, bbd_tree.rs:101-
+// 111), and the warp keeps the minimum, lowest index on ties.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256)
+rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, int k,
+               const int32_t *__restrict__ flag_count, const int32_t *__restrict__ flag_list,
+               const int32_t *__restrict__ cand, int32_t *__restrict__ labels, LloydState *st) {
+  if (st && st->done) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int cnt = *flag_count;
+  if (gw == 0 && lane == 0 && st) atomicAdd((unsigned long long *)&st->rescored, (unsigned long long)cnt);
+  for (int64_t f = gw; f < cnt; f += nw) {
+    const int64_t i = flag_list[f];
+    const int32_t *cr = cand + f * (1 + kMaxCand);
+    const int nc = cr[0];
+    const int total = nc < 0 ? k : nc;
+    const T *xr = x + i * (int64_t)d;
+    double best = DBL_MAX;
+    int bi = 0x7fffffff;
+    for (int c = lane; c < total; c += 32) {
+      const int j = nc < 0 ? c : cr[1 + c];
+      const double *cj = cent + (int64_t)j * d;
+      double s = 0.0;
+      for (int t = 0; t < d; ++t) s = __dadd_rn(s, sqd_term((double)xr[t], cj[t]));
+      if (s < best || (s == best && j < bi)) { best = s; bi = j; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) labels[i] = bi == 0x7fffffff ? 0 : bi;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+sc_status make_map(CUtensorMap *m, void *ptr, int64_t rows, int cols, int box_cols, int box_rows, int row_bytes) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) { set_error("cuTensorMapEncodeTiled is unavailable"); return SC_ERR_CUDA; }
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUtensorMapSwizzle sw = row_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                                  : CU_TENSOR_MAP_SWIZZLE_32B;
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return SC_ERR_CUDA; }
+  return SC_OK;
+}
+
+template <class T>
+sc_status dalloc(T **p, size_t count) {
+  *p = nullptr;
+  SC_CUDA(cudaMalloc((void **)p, (count ? count : 1) * sizeof(T)));
+  return SC_OK;
+}
+template <class T>
+void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+int pad_d(int d) { return (d + 63) / 64 * 64; }  // 128-byte rows: one SW128 layout for every d
+
+size_t assign_smem(const SplitState *s, int stages, int k_pad, int k_cols) {
+  const size_t a_stage = (size_t)2 * s->nkt * kBM * s->row_bytes;
+  const size_t b_bytes = (((size_t)2 * s->nkt * k_pad * s->row_bytes) + 1023) & ~(size_t)1023;
+  return 1024 + b_bytes + (size_t)stages * a_stage + (size_t)k_cols * 4 + (size_t)(2 * stages + 6) * 8 + 16;
+}
+
+}  // namespace
+
+sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int d, double *xnorm_total,
+                        cudaStream_t st) {
+  split_free(s);
+  s->dtype = dtype;
+  s->n = n;
+  s->n_pad = (n + kBM - 1) / kBM * kBM;
+  if (s->n_pad == 0) s->n_pad = kBM;
+  s->d = d;
+  s->d_pad = pad_d(d);
+  s->kt_elems = s->d_pad >= 64 ? 64 : s->d_pad;
+  s->nkt = s->d_pad / s->kt_elems;
+  s->row_bytes = s->kt_elems * 2;
+  if (s->d_pad > 256) {
+    set_error("d=%d exceeds the split-BF16 kernel's limit of 256 features", d);
+    return SC_ERR_INVALID;
+  }
+  int dev = 0;
+  SC_CUDA(cudaGetDevice(&dev));
+  SC_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
+  SC_TRY(dalloc(&s->xh, (size_t)(s->n_pad * s->d_pad)));
+  SC_TRY(dalloc(&s->xl, (size_t)(s->n_pad * s->d_pad)));
+  SC_TRY(dalloc(&s->xnrm, (size_t)s->n_pad));
+  const int nb = (int)((s->n_pad + 7) / 8);
+  SC_TRY(dalloc(&s->part, (size_t)nb));
+  SC_TRY(dalloc(&s->flag_count, 1));
+  SC_TRY(dalloc(&s->flag_list, (size_t)s->n_pad));
+  SC_TRY(dalloc(&s->cand, (size_t)s->n_pad * (1 + kMaxCand)));
+  SC_TRY(dalloc(&s->cmax, 1));
+  if (dtype == SC_F32)
+    prep_x_kernel<float><<<nb, 256, 0, st>>>((const float *)x, n, s->n_pad, d, s->d_pad, s->xh, s->xl, s->xnrm, s->part);
+  else
+    prep_x_kernel<double><<<nb, 256, 0, st>>>((const double *)x, n, s->n_pad, d, s->d_pad, s->xh, s->xl, s->xnrm, s->part);
+  SC_LAUNCHED();
+  sum_parts_kernel<<<1, 1024, 0, st>>>(s->part, nb, xnorm_total);
+  SC_LAUNCHED();
+  SC_TRY(make_map(&s->tm_xh, s->xh, s->n_pad, s->d_pad, s->kt_elems, kBM, s->row_bytes));
+  SC_TRY(make_map(&s->tm_xl, s->xl, s->n_pad, s->d_pad, s->kt_elems, kBM, s->row_bytes));
+  s->ready = 1;
+  return SC_OK;
+}
+
+sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cudaStream_t st) {
+  if (!s->ready) { set_error("split-BF16 state is not prepared"); return SC_ERR_INTERNAL; }
+  const int k_pad = (k + 15) / 16 * 16;
+  const int k_cols = (k_pad + 31) / 32 * 32;
+  if (k_pad > 256) {
+    set_error("k=%d exceeds the split-BF16 kernel's limit of 256 clusters", k);
+    return SC_ERR_INVALID;
+  }
+  if (k_cols > s->k_alloc) {
+    dfree(s->ch); dfree(s->cl); dfree(s->cn2);
+    SC_TRY(dalloc(&s->ch, (size_t)k_cols * s->d_pad));
+    SC_TRY(dalloc(&s->cl, (size_t)k_cols * s->d_pad));
+    SC_TRY(dalloc(&s->cn2, (size_t)k_cols));
+    s->k_alloc = k_cols;
+    s->k_pad = 0;
+  }
+  if (k_pad != s->k_pad) {
+    SC_TRY(make_map(&s->tm_ch, s->ch, k_pad, s->d_pad, s->kt_elems, k_pad, s->row_bytes));
+    SC_TRY(make_map(&s->tm_cl, s->cl, k_pad, s->d_pad, s->kt_elems, k_pad, s->row_bytes));
+  }
+  s->k = k;
+  s->k_pad = k_pad;
+  SC_CUDA(cudaMemsetAsync(s->cmax, 0, sizeof(unsigned int), st));
+  prep_c_kernel<<<k_cols, 128, 0, st>>>(cent, k, s->d, s->d_pad, k_cols, s->ch, s->cl, s->cn2, s->cmax);
+  SC_LAUNCHED();
+  return SC_OK;
+}
+
+sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d, const double *cent, int k,
+                       int32_t *labels, Acc128 *acc, unsigned long long *cnt, int scale, LloydState *lst,
+                       cudaStream_t st, cudaEvent_t *timing) {
+  if (!s->ready || s->k != k) { set_error("split-BF16 centroids are not prepared"); return SC_ERR_INTERNAL; }
+  if (n == 0) return SC_OK;
+  const int k_cols = (s->k_pad + 31) / 32 * 32;
+  uint32_t tmem_cols = 32;
+  while (tmem_cols < (uint32_t)(2 * k_cols)) tmem_cols <<= 1;
+  int stages = 6;
+  while (stages > 2 && assign_smem(s, stages, s->k_pad, k_cols) > 227 * 1024) --stages;
+  const size_t smem = assign_smem(s, stages, s->k_pad, k_cols);
+  if (smem > 227 * 1024) {
+    set_error("d=%d, k=%d exceed the split-BF16 kernel's shared memory", d, k);
+    return SC_ERR_INVALID;
+  }
+  AssignParams p;
+  memset(&p, 0, sizeof p);
+  p.n = n;
+  p.n_tiles = (int)(s->n_pad / kBM);
+  p.nkt = s->nkt;
+  p.kt_elems = s->kt_elems;
+  p.row_bytes = s->row_bytes;
+  p.k = k;
+  p.k_pad = s->k_pad;
+  p.k_cols = k_cols;
+  p.stages = stages;
+  p.tmem_cols = tmem_cols;
+  p.xnrm = s->xnrm;
+  p.cn2 = s->cn2;
+  p.cmax = s->cmax;
+  p.coef_dot = (float)(3.02 * 0x1p-16 + 1.02 * 3.0 * s->d_pad * 0x1p-22);
+  p.coef_ref = (float)((d + 4) * 0x1p-52);
+  p.labels = labels;
+  p.flag_count = s->flag_count;
+  p.flag_list = s->flag_list;
+  p.cand = s->cand;
+  p.st = lst;
+  SC_CUDA(cudaMemsetAsync(s->flag_count, 0, sizeof(int32_t), st));
+  SC_CUDA(cudaFuncSetAttribute(split_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int grid = p.n_tiles < s->num_sms ? p.n_tiles : s->num_sms;
+  if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
+  split_assign_kernel<<<grid, kAssignThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, p);
+  SC_LAUNCHED();
+  if (timing) SC_CUDA(cudaEventRecord(timing[1], st));
+  const int rgrid = 2 * s->num_sms;
+  if (dtype == SC_F32)
+    rescore_kernel<float><<<rgrid, 256, 0, st>>>((const float *)x, d, cent, k, s->flag_count, s->flag_list, s->cand,
+                                                labels, lst);
+  else
+    rescore_kernel<double><<<rgrid, 256, 0, st>>>((const double *)x, d, cent, k, s->flag_count, s->flag_list,
+                                                 s->cand, labels, lst);
+  SC_LAUNCHED();
+  if (acc) SC_TRY(launch_update_fixed(dtype, x, n, d, labels, acc, cnt, scale, lst, st));
+  return SC_OK;
+}
+
+void split_free(SplitState *s) {
+  dfree(s->xh); dfree(s->xl); dfree(s->xnrm); dfree(s->part);
+  dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cmax);
+  dfree(s->flag_count); dfree(s->flag_list); dfree(s->cand);
+  s->ready = 0;
+  s->k_alloc = 0;
+  s->k_pad = 0;
+}
+
 sc_status split_knn(SplitKnnState *, int, const void *, int64_t, int, const void *, int64_t, int, int64_t *,
-                    double *, int64_t *, cudaStream_t) { return not_built(); }
+                    double *, int64_t *, cudaStream_t) {
+  set_error("the split-BF16 kNN form is not available in this build");
+  return SC_ERR_INVALID;
+}
 void split_knn_free(SplitKnnState *) {}
 
 }  // namespace sc

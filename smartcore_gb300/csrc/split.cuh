@@ -2,12 +2,32 @@
 // error bound, FP64 re-score of every decision inside the bound.
 #pragma once
 
+#include <cuda.h>
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace sc {
 
+constexpr int kMaxCand = 6;  // candidates recorded per near-tie point
+
 struct SplitState {
   int ready = 0;
+  int dtype = 0;
+  int64_t n = 0, n_pad = 0;
+  int d = 0, d_pad = 0, kt_elems = 0, nkt = 0, row_bytes = 0;
+  __nv_bfloat16 *xh = nullptr, *xl = nullptr;  // n_pad x d_pad
+  float *xnrm = nullptr;                        // n_pad: upper bound of ||x||
+  double *part = nullptr;                       // block partials of ||x||^2
+  int k = 0, k_pad = 0, k_alloc = 0;
+  __nv_bfloat16 *ch = nullptr, *cl = nullptr;  // k_pad x d_pad
+  float *cn2 = nullptr;                         // k_pad: ||c||^2 rounded to f32 (+inf for padding)
+  unsigned int *cmax = nullptr;                 // bits of an upper bound of max ||c||
+  int32_t *flag_count = nullptr;                // near-tie points of the last assignment
+  int32_t *flag_list = nullptr;                 // n entries
+  int32_t *cand = nullptr;                      // n x (1 + kMaxCand): count (-1 = all), indices
+  CUtensorMap tm_xh, tm_xl, tm_ch, tm_cl;
+  int num_sms = 0;
 };
 
 struct SplitKnnState {
@@ -19,7 +39,8 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
 sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cudaStream_t st);
 sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d,
                        const double *cent, int k, int32_t *labels, Acc128 *acc,
-                       unsigned long long *cnt, int scale, LloydState *lst, cudaStream_t st);
+                       unsigned long long *cnt, int scale, LloydState *lst, cudaStream_t st,
+                       cudaEvent_t *timing = nullptr);
 void split_free(SplitState *s);
 
 sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,

@@ -106,7 +106,7 @@ sc_status launch_update_fixed(int dtype, const void *x, int64_t n, int d,
     update_fixed_kernel<float><<<(unsigned)blocks, 256, 0, s>>>((const float *)x, n, d, labels, acc, cnt, scale, st);
   else
     update_fixed_kernel<double><<<(unsigned)blocks, 256, 0, s>>>((const double *)x, n, d, labels, acc, cnt, scale, st);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -160,7 +160,7 @@ sc_status launch_finalize_centroids(Acc128 *acc, unsigned long long *cnt,
                                     int empty_nan, const LloydState *st,
                                     cudaStream_t s) {
   finalize_centroids_kernel<<<k, kFinThreads, 0, s>>>(acc, cnt, cent, sizes, d, scale, cluster_terms, empty_nan, st);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -202,7 +202,7 @@ sc_status launch_finalize_scalar(const double *part, int nparts,
                                  const double *xnorm_total, LloydState *st,
                                  cudaStream_t s) {
   finalize_scalar_kernel<<<1, kScalarThreads, 0, s>>>(part, nparts, cluster_terms, k, xnorm_total, st);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -239,7 +239,7 @@ sc_status launch_absmax(int dtype, const void *x, int64_t count,
     absmax_kernel<float><<<(unsigned)blocks, 256, 0, s>>>((const float *)x, count, out_bits);
   else
     absmax_kernel<double><<<(unsigned)blocks, 256, 0, s>>>((const double *)x, count, out_bits);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 
@@ -267,7 +267,7 @@ sc_status launch_to_row_major(int dtype, const void *src, int64_t n, int64_t d,
     to_row_major_kernel<float><<<grid, block, 0, s>>>((const float *)src, n, d, ld, (float *)dst);
   else
     to_row_major_kernel<double><<<grid, block, 0, s>>>((const double *)src, n, d, ld, (double *)dst);
-  SC_CUDA(cudaGetLastError());
+  SC_LAUNCHED();
   return SC_OK;
 }
 

@@ -54,15 +54,16 @@ def anisotropic_dirichlet_f32(n=1_000_000, d=64, k=256, seed=3, chunk=1 << 17):
     w = rng.dirichlet(np.full(k, 2.0))
     sizes = np.floor(w * n).astype(np.int64)
     sizes[: n - sizes.sum()] += 1
-    lab = rng.permutation(np.repeat(np.arange(k), sizes))
     x = np.empty((n, d), np.float32)
-    for s in range(0, n, chunk):
-        e = min(n, s + chunk)
-        z = rng.normal(size=(e - s, d))
-        li = lab[s:e]
-        # x = c + z A  (row vector convention: covariance A^T A)
-        x[s:e] = (centers[li] + np.einsum("nd,nde->ne", z, A[li])).astype(np.float32)
-    return x, lab
+    lab = np.repeat(np.arange(k), sizes)
+    s = 0
+    for c in range(k):
+        # rows c + z A (row-vector convention: covariance A^T A)
+        z = rng.normal(size=(sizes[c], d))
+        x[s:s + sizes[c]] = (centers[c] + z @ A[c]).astype(np.float32)
+        s += sizes[c]
+    p = rng.permutation(n)
+    return np.ascontiguousarray(x[p]), lab[p]
 
 
 def batched_problems(count=512, seed0=0, n_range=(1_000, 100_000), ds=(8, 16, 32, 64),
