@@ -92,13 +92,6 @@ sc_status upload_matrix(const void *x, int32_t dtype, int32_t layout, int32_t me
   return r;
 }
 
-int fixed_scale(double absmax, int64_t n) {
-  int e = 0;
-  if (absmax > 0) frexp(absmax, &e);  // absmax < 2^e
-  int ln = 0;
-  while ((1ll << ln) <= n) ++ln;  // n < 2^ln
-  return 125 - e - ln;
-}
 
 }  // namespace
 }  // namespace sc
@@ -113,13 +106,13 @@ struct sc_kmeans {
   int64_t n = 0, d = 0, k = 0;
   cudaStream_t stream = nullptr;
   void *x = nullptr;  // row-major n x d
-  int scale = 0;
+  double absmax = 0.0;          // max |x|, sets the fixed-point scales
+  int num_sms = 0;
+  UpdateBuf upd;                // centroid-sum buffers (per k)
   double *cent = nullptr;       // k x d
   int32_t *labels = nullptr;    // n
   double *dd = nullptr;         // n, k-means++ distances
   double *part = nullptr;       // block partials
-  Acc128 *acc = nullptr;        // k x d
-  unsigned long long *cnt = nullptr;
   int64_t *sizes = nullptr;     // k
   double *cterms = nullptr;     // k
   double *uniforms = nullptr;   // k - 1
@@ -150,16 +143,14 @@ static cudaEvent_t *next_timing(sc_kmeans *h) {
 }
 
 static sc_status kmeans_alloc_k(sc_kmeans *h, int64_t k) {
-  if (k <= h->k_alloc) { h->k = k; return SC_OK; }
-  dfree(h->cent); dfree(h->acc); dfree(h->cnt); dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
+  if (k == h->k_alloc) { h->k = k; return SC_OK; }
+  dfree(h->cent); dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
   SC_TRY(dalloc(&h->cent, (size_t)(k * h->d)));
-  SC_TRY(dalloc(&h->acc, (size_t)(k * h->d)));
-  SC_TRY(dalloc(&h->cnt, (size_t)k));
   SC_TRY(dalloc(&h->sizes, (size_t)k));
-  SC_TRY(dalloc(&h->cterms, (size_t)k));
+  SC_TRY(dalloc(&h->cterms, (size_t)(k * h->d)));
   SC_TRY(dalloc(&h->uniforms, (size_t)k));
-  SC_CUDA(cudaMemsetAsync(h->acc, 0, (size_t)(k * h->d) * sizeof(Acc128), h->stream));
-  SC_CUDA(cudaMemsetAsync(h->cnt, 0, (size_t)k * sizeof(unsigned long long), h->stream));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  SC_TRY(update_alloc(&h->upd, h->dtype, h->n, (int)h->d, (int)k, h->absmax, h->num_sms));
   h->k_alloc = k;
   h->k = k;
   return SC_OK;
@@ -193,7 +184,8 @@ void sc_kmeans_destroy(sc_kmeans *h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
   dfree(h->x); dfree(h->cent); dfree(h->labels); dfree(h->dd); dfree(h->part);
-  dfree(h->acc); dfree(h->cnt); dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
+  dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
+  update_free(&h->upd);
   dfree(h->xnorm_total); dfree(h->st); dfree(h->bits);
   split_free(&h->split);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
@@ -241,7 +233,15 @@ sc_status sc_kmeans_create(const void *x, int32_t dtype, int32_t layout, int32_t
       r = SC_ERR_INVALID;
       break;
     }
-    h->scale = fixed_scale(amax, n);
+    h->absmax = amax;
+    {
+      int dev = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        r = cuda_fail(cudaGetLastError(), "device attributes");
+        break;
+      }
+    }
     if ((r = reset_state(h)) != SC_OK) break;
     if (form == SC_FORM_SPLIT_BF16 &&
         (r = split_prepare(&h->split, dtype, h->x, n, (int)d, h->xnorm_total, h->stream)) != SC_OK)
@@ -273,8 +273,8 @@ sc_status sc_kmeans_seed(sc_kmeans *h, int64_t k, int64_t first_index, const dou
   }
   SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(k - 1), h->dd, h->labels, nullptr, k == 1, s));  // :399-410
   // initial centroids: means of the seeding partition (kmeans.rs:275-292)
-  SC_TRY(launch_update_fixed(h->dtype, h->x, h->n, (int)h->d, h->labels, h->acc, h->cnt, h->scale, nullptr, s));
-  SC_TRY(launch_finalize_centroids(h->acc, h->cnt, h->cent, h->sizes, (int)k, (int)h->d, h->scale, nullptr, 1, nullptr, s));
+  SC_TRY(launch_update(&h->upd, h->dtype, h->x, h->n, (int)h->d, h->labels, (int)k, nullptr, s));
+  SC_TRY(launch_finalize(&h->upd, h->cent, h->sizes, (int)k, (int)h->d, nullptr, 1, nullptr, s));
   if (h->form == SC_FORM_SPLIT_BF16) SC_TRY(split_centroids_changed(&h->split, h->cent, (int)k, s));
   SC_CUDA(cudaStreamSynchronize(s));
   return SC_OK;
@@ -300,14 +300,14 @@ static sc_status lloyd_step(sc_kmeans *h) {
     if (ev) SC_CUDA(cudaEventRecord(ev[0], s));
     SC_TRY(launch_assign_fp64(h->dtype, h->x, h->n, d, h->cent, k, h->labels, h->part, h->st, s));
     if (ev) SC_CUDA(cudaEventRecord(ev[1], s));
-    SC_TRY(launch_update_fixed(h->dtype, h->x, h->n, d, h->labels, h->acc, h->cnt, h->scale, h->st, s));
-    SC_TRY(launch_finalize_centroids(h->acc, h->cnt, h->cent, h->sizes, k, d, h->scale, h->cterms, 0, h->st, s));
+    SC_TRY(launch_update(&h->upd, h->dtype, h->x, h->n, d, h->labels, k, h->st, s));
+    SC_TRY(launch_finalize(&h->upd, h->cent, h->sizes, k, d, h->cterms, 0, h->st, s));
     SC_TRY(launch_finalize_scalar(h->part, assign_block_count(h->n), nullptr, k, nullptr, h->st, s));
   } else {
-    SC_TRY(split_assign(&h->split, h->dtype, h->x, h->n, d, h->cent, k, h->labels, h->acc, h->cnt,
-                        h->scale, h->st, s, next_timing(h)));
-    SC_TRY(launch_finalize_centroids(h->acc, h->cnt, h->cent, h->sizes, k, d, h->scale, h->cterms, 0, h->st, s));
-    SC_TRY(launch_finalize_scalar(nullptr, 0, h->cterms, k, h->xnorm_total, h->st, s));
+    SC_TRY(split_assign(&h->split, h->dtype, h->x, h->n, d, h->cent, k, h->labels, h->st, s, next_timing(h)));
+    SC_TRY(launch_update(&h->upd, h->dtype, h->x, h->n, d, h->labels, k, h->st, s));
+    SC_TRY(launch_finalize(&h->upd, h->cent, h->sizes, k, d, h->cterms, 0, h->st, s));
+    SC_TRY(launch_finalize_scalar(nullptr, 0, h->cterms, update_nterms(&h->upd, k, d), h->xnorm_total, h->st, s));
     SC_TRY(split_centroids_changed(&h->split, h->cent, k, s));
   }
   return SC_OK;
@@ -421,8 +421,7 @@ sc_status sc_kmeans_predict(const void *x, int32_t dtype, int32_t layout, int64_
     if (form == SC_FORM_FP64)
       r = launch_assign_fp64(h->dtype, h->x, h->n, (int)h->d, h->cent, (int)k, h->labels, nullptr, nullptr, h->stream);
     else
-      r = split_assign(&h->split, h->dtype, h->x, h->n, (int)h->d, h->cent, (int)k, h->labels, nullptr, nullptr,
-                       h->scale, h->st, h->stream);
+      r = split_assign(&h->split, h->dtype, h->x, h->n, (int)h->d, h->cent, (int)k, h->labels, h->st, h->stream);
   }
   if (r == SC_OK) r = sc_kmeans_get(h, nullptr, nullptr, labels_out, nullptr, nullptr);
   sc_kmeans_destroy(h);

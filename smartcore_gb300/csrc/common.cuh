@@ -54,6 +54,23 @@ struct Acc128 {
 
 constexpr int kMaxKnnK = 64;  // largest k served by the kNN kernels
 
+// Buffers of the centroid-sum step.  mode 0: one 128-bit fixed-point
+// accumulator per (cluster, feature) updated with global atomics.  mode 1:
+// each CTA accumulates its contiguous chunk of points in shared memory as
+// int64 fixed point and writes one partial per CTA; the finalize step adds
+// the partials exactly in 128 bits.  Both are order independent.
+struct UpdateBuf {
+  int mode = 0;
+  int grid = 0;      // mode 1: number of CTAs (partials)
+  int threads = 0;   // mode 1: threads per CTA
+  int scale = 0;     // fixed-point scale 2^scale of the active mode
+  size_t smem = 0;   // mode 1: dynamic shared memory per CTA
+  Acc128 *acc = nullptr;            // mode 0: k x d
+  unsigned long long *cnt = nullptr;  // mode 0: k
+  long long *part = nullptr;        // mode 1: grid x k x d
+  unsigned int *cpart = nullptr;    // mode 1: grid x k
+};
+
 // ---- kernel launchers (defined in the .cu files) ----
 // exact.cu: FP64 forms with the reference's operation order.
 sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
@@ -90,9 +107,19 @@ sc_status launch_finalize_centroids(Acc128 *acc, unsigned long long *cnt,
                                     int empty_nan, const LloydState *st,
                                     cudaStream_t s);
 sc_status launch_finalize_scalar(const double *part, int nparts,
-                                 const double *cluster_terms, int k,
+                                 const double *cluster_terms, int64_t nterms,
                                  const double *xnorm_total, LloydState *st,
                                  cudaStream_t s);
+// Chooses the mode for (n, d, k) and allocates; absmax = max |x|.
+sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms);
+// Number of distortion terms launch_finalize writes (k, or k*d).
+inline int64_t update_nterms(const UpdateBuf *u, int k, int d) { return u->mode == 1 ? (int64_t)k * d : k; }
+void update_free(UpdateBuf *u);
+sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n, int d,
+                        const int32_t *labels, int k, const LloydState *st, cudaStream_t s);
+sc_status launch_finalize(const UpdateBuf *u, double *cent, int64_t *sizes, int k, int d,
+                          double *cluster_terms, int empty_nan, const LloydState *st,
+                          cudaStream_t s);
 sc_status launch_absmax(int dtype, const void *x, int64_t count,
                         unsigned long long *out_bits, cudaStream_t s);
 sc_status launch_to_row_major(int dtype, const void *src, int64_t n, int64_t d,

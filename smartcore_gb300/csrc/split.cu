@@ -7,8 +7,10 @@
 // tcgen05 GEMM on BF16 halves: x = x_h + x_l + r_x, c = c_h + c_l + r_c
 // (|r| <= 2^-16 |.|), x.c ~ x_h.c_h + x_h.c_l + x_l.c_h, FP32 accumulate in
 // TMEM.  A rigorous per-point bound E on |A_j - (D_j - ||x||^2)| certifies the
-// label when the gap between the best and second-best A exceeds 2E; every
-// other point is re-scored in FP64 over the candidates within the bound.
+// label when the gap between the best and second-best A exceeds 2E.  Every
+// other point is re-ranked with an FP32 CUDA-core dot product (a bound ~50x
+// tighter), and the candidates that remain within that bound are re-scored
+// in FP64 in the reference's operation order.
 #include <float.h>
 #include <math.h>
 #include <string.h>
@@ -21,7 +23,9 @@ namespace sc {
 namespace {
 
 constexpr int kBM = 128;           // points per tile (UMMA M)
-constexpr int kAssignThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kEpiWarps = 8;       // two warpgroups, one per TMEM accumulator buffer
+constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kAssignThreads = 64 + kEpiThreads;  // warp 0 TMA, warp 1 MMA, then epilogue
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every barrier wait
 
 enum { kErrTimeout = 4 };
@@ -108,7 +112,7 @@ __global__ void sum_parts_kernel(const double *__restrict__ part, int nparts, do
 __global__ void __launch_bounds__(128)
 prep_c_kernel(const double *__restrict__ cent, int k, int d, int d_pad, int k_cols,
               __nv_bfloat16 *__restrict__ ch, __nv_bfloat16 *__restrict__ cl,
-              float *__restrict__ cn2, unsigned int *__restrict__ cmax) {
+              float *__restrict__ cn2, unsigned int *__restrict__ cmax, float *__restrict__ cT) {
   __shared__ double ws[4];
   const int j = blockIdx.x;
   double s = 0.0;
@@ -123,6 +127,7 @@ prep_c_kernel(const double *__restrict__ cent, int k, int d, int d_pad, int k_co
       ch[(int64_t)j * d_pad + t] = h;
       cl[(int64_t)j * d_pad + t] = l;
     }
+    cT[(int64_t)t * k_cols + j] = (j < k && t < d) ? (float)cent[(int64_t)j * d + t] : 0.f;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -158,9 +163,9 @@ struct AssignParams {
   int32_t *labels;
   int32_t *flag_count;
   int32_t *flag_list;
-  int32_t *cand;
   LloydState *st;
 };
+
 
 __global__ void __launch_bounds__(kAssignThreads, 1)
 split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
@@ -193,7 +198,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
     tc::mbar_init(mma_done, 1);
     for (int a = 0; a < 2; ++a) {
       tc::mbar_init(&accfull[a], 1);
-      tc::mbar_init(&accempty[a], 128);
+      tc::mbar_init(&accempty[a], kEpiThreads / 2);
     }
     *s_abort = 0;
     tc::fence_mbar_init();
@@ -276,68 +281,64 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       tc::mbar_wait(mma_done, 0, kWaitNs);
     }
   } else {
-    // ---------------- epilogue: 4 warps, one point per thread ----------------
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    // ---------------- epilogue: 2 warpgroups ----------------
+    // Warpgroup g handles the tiles of accumulator buffer g (every other
+    // tile); warp w reads TMEM lanes 32*(w%4).., one point per thread, all
+    // columns.  Two interleaved (best, second, argmin) trackers per thread
+    // keep the dependency chains short; they merge with lowest index on ties.
+    const int g = (warp - 2) >> 2;
+    const int q = warp & 3;
     const int row = q * 32 + lane;
     const float cmax = __uint_as_float(*p.cmax);
+    const float inf = __int_as_float(0x7f800000);
     int it = 0;
     for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x, ++it) {
-      const int acc = it & 1;
+      if ((it & 1) != g) continue;
       const uint32_t aph = (uint32_t)(it >> 1) & 1u;
-      const bool got = tc::mbar_wait(&accfull[acc], aph, kWaitNs);
-      if (!__all_sync(0xffffffffu, got)) { atomicExch(s_abort, 1); break; }
-      if (__any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) break;
+      const bool got = tc::mbar_wait(&accfull[g], aph, kWaitNs);
+      if (!__all_sync(0xffffffffu, got) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
+        atomicExch(s_abort, 1);
+        break;
+      }
       tc::fence_after_sync();
-      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * p.k_cols);
-      float min1 = __int_as_float(0x7f800000), min2 = min1;
-      int arg = 0;
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * p.k_cols);
+      float a1 = inf, a2 = inf, b1 = inf, b2 = inf;
+      int ai = 0x7fffffff, bi = 0x7fffffff;
       for (int c0 = 0; c0 < p.k_cols; c0 += 32) {
         uint32_t v[32];
         tc::tmem_ld32(taddr + (uint32_t)c0, v);
         tc::tmem_wait_ld();
 #pragma unroll
-        for (int jj = 0; jj < 32; ++jj) {
-          const float a = fmaf(-2.f, __uint_as_float(v[jj]), s_cn2[c0 + jj]);
-          if (a < min1) { min2 = min1; min1 = a; arg = c0 + jj; }
-          else if (a < min2) min2 = a;
-        }
-      }
-      const int64_t i = (int64_t)t * kBM + row;
-      const bool live = i < p.n;
-      const float xn = live ? p.xnrm[i] : 0.f;
-      const float e = p.coef_dot * 2.f * xn * cmax + 0x1p-22f * (cmax * cmax + xn * cmax) +
-                      p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
-      const float thr = 2.1f * e;
-      const bool flagged = live && !(min2 - min1 > thr);
-      if (__any_sync(0xffffffffu, flagged)) {
-        // second pass over the accumulator for the near-tie rows of this warp
-        int nc = 0;
-        int32_t cands[kMaxCand];
-        const float lim = min1 + thr;
-        for (int c0 = 0; c0 < p.k_cols; c0 += 32) {
-          uint32_t v[32];
-          tc::tmem_ld32(taddr + (uint32_t)c0, v);
-          tc::tmem_wait_ld();
-#pragma unroll
-          for (int jj = 0; jj < 32; ++jj) {
-            const float a = fmaf(-2.f, __uint_as_float(v[jj]), s_cn2[c0 + jj]);
-            if (flagged && a <= lim) {
-              if (nc < kMaxCand) cands[nc] = c0 + jj;
-              ++nc;
-            }
-          }
-        }
-        if (flagged) {
-          const int slot = atomicAdd(p.flag_count, 1);
-          p.flag_list[slot] = (int32_t)i;
-          int32_t *cr = p.cand + (int64_t)slot * (1 + kMaxCand);
-          cr[0] = nc <= kMaxCand ? nc : -1;
-          for (int c = 0; c < kMaxCand && c < nc; ++c) cr[1 + c] = cands[c];
+        for (int jj = 0; jj < 32; jj += 2) {
+          const float x0 = fmaf(-2.f, __uint_as_float(v[jj]), s_cn2[c0 + jj]);
+          const float x1 = fmaf(-2.f, __uint_as_float(v[jj + 1]), s_cn2[c0 + jj + 1]);
+          const bool l0 = x0 < a1, l1 = x1 < b1;
+          a2 = l0 ? a1 : fminf(a2, x0);
+          b2 = l1 ? b1 : fminf(b2, x1);
+          ai = l0 ? c0 + jj : ai;
+          bi = l1 ? c0 + jj + 1 : bi;
+          a1 = l0 ? x0 : a1;
+          b1 = l1 ? x1 : b1;
         }
       }
       tc::fence_before_sync();
-      tc::mbar_arrive(&accempty[acc]);
-      if (live) p.labels[i] = arg;
+      tc::mbar_arrive(&accempty[g]);
+      // merge the even- and odd-column trackers
+      float m1, m2;
+      int a;
+      if (b1 < a1 || (b1 == a1 && bi < ai)) {
+        m1 = b1; a = bi; m2 = fminf(b2, a1);
+      } else {
+        m1 = a1; a = ai; m2 = fminf(a2, b1);
+      }
+      const int64_t i = (int64_t)t * kBM + row;
+      if (i < p.n) {
+        const float xn = p.xnrm[i];
+        const float e = p.coef_dot * 2.f * xn * cmax + 0x1p-22f * (cmax * cmax + xn * cmax) +
+                        p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
+        p.labels[i] = a == 0x7fffffff ? 0 : a;
+        if (!(m2 - m1 > 2.1f * e)) p.flag_list[atomicAdd(p.flag_count, 1)] = (int32_t)i;
+      }
     }
   }
   tc::fence_before_sync();
@@ -350,44 +351,99 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
 }
 
 // ---------------------------------------------------------------------------
-// K6: FP64 re-score of the near-tie points.  One warp per point: each lane
-// takes candidates (or all centroids when the candidate list overflowed),
-// computes D_j in the reference order (kmeans.rs:338-346, bbd_tree.rs:101-
-// 111), and the warp keeps the minimum, lowest index on ties.
+// K6: re-score of the near-tie points.  One warp per point.
+//   1. a_j = ||c_j||^2 - 2 x.c_j for every centroid with FP32 CUDA-core dot
+//      products (lane = centroid), rigorous bound e32 (error of the f32
+//      conversions, the FMA chain and the reference's own rounding of D).
+//   2. Candidates: a_j <= min_j a_j + 2 e32.  One candidate is the label.
+//   3. Otherwise D_j in FP64 in the reference order (kmeans.rs:338-346,
+//      bbd_tree.rs:101-111) for the candidates; minimum, lowest index on ties.
 // ---------------------------------------------------------------------------
+constexpr int kRescoreWarps = 8;
+
 template <typename T>
-__global__ void __launch_bounds__(256)
-rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, int k,
+__global__ void __launch_bounds__(32 * kRescoreWarps)
+rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, int k, int k_cols,
+               const float *__restrict__ cT, const float *__restrict__ cn2,
+               const unsigned int *__restrict__ cmax_bits, const float *__restrict__ xnrm,
                const int32_t *__restrict__ flag_count, const int32_t *__restrict__ flag_list,
-               const int32_t *__restrict__ cand, int32_t *__restrict__ labels, LloydState *st) {
+               int32_t *__restrict__ labels, LloydState *st, int stage_ct) {
   if (st && st->done) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  __shared__ float xs[kRescoreWarps][256];
+  extern __shared__ __align__(16) float s_ct[];  // d x k_cols when stage_ct
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * kRescoreWarps + w;
+  const int64_t nw = (int64_t)gridDim.x * kRescoreWarps;
   const int cnt = *flag_count;
   if (gw == 0 && lane == 0 && st) atomicAdd((unsigned long long *)&st->rescored, (unsigned long long)cnt);
+  if ((int64_t)blockIdx.x * kRescoreWarps >= cnt) return;  // no point for this block
+  if (stage_ct) {
+    const int total = d * k_cols;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) s_ct[t] = cT[t];
+    __syncthreads();
+    cT = s_ct;
+  }
+  const float cmax = __uint_as_float(*cmax_bits);
   for (int64_t f = gw; f < cnt; f += nw) {
     const int64_t i = flag_list[f];
-    const int32_t *cr = cand + f * (1 + kMaxCand);
-    const int nc = cr[0];
-    const int total = nc < 0 ? k : nc;
     const T *xr = x + i * (int64_t)d;
-    double best = DBL_MAX;
-    int bi = 0x7fffffff;
-    for (int c = lane; c < total; c += 32) {
-      const int j = nc < 0 ? c : cr[1 + c];
-      const double *cj = cent + (int64_t)j * d;
-      double s = 0.0;
-      for (int t = 0; t < d; ++t) s = __dadd_rn(s, sqd_term((double)xr[t], cj[t]));
-      if (s < best || (s == best && j < bi)) { best = s; bi = j; }
+    for (int t = lane; t < d; t += 32) xs[w][t] = (float)xr[t];
+    __syncwarp();
+    float av[8];
+    float m1 = __int_as_float(0x7f800000);
+    const int mchunks = k_cols >> 5;  // 32-centroid chunks present in cT (uniform)
+#pragma unroll
+    for (int m = 0; m < 8; ++m) av[m] = 0.f;
+    for (int t = 0; t < d; ++t) {
+      const float xt = xs[w][t];
+      const float *row = cT + (int64_t)t * k_cols + lane;
+#pragma unroll
+      for (int m = 0; m < 8; ++m)
+        if (m < mchunks) av[m] = fmaf(xt, row[32 * m], av[m]);
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ob = __shfl_down_sync(0xffffffffu, best, o);
-      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-      if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    for (int m = 0; m < 8; ++m) {
+      const int j = lane + 32 * m;
+      av[m] = (m < mchunks && j < k) ? fmaf(-2.f, av[m], cn2[j]) : __int_as_float(0x7f800000);
+      m1 = fminf(m1, av[m]);
     }
-    if (lane == 0) labels[i] = bi == 0x7fffffff ? 0 : bi;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m1 = fminf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    const float xn = xnrm[i];
+    const float e32 = 1.05f * ((2.f * d + 8.f) * 0x1p-24f * xn * cmax + 0x1p-23f * (cmax * cmax + 2.f * xn * cmax) +
+                               (float)((d + 4) * 0x1p-52) * (xn + cmax) * (xn + cmax)) + 1e-30f;
+    const float lim = m1 + 2.f * e32;
+    int ncand = 0, first = 0x7fffffff;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const unsigned b = __ballot_sync(0xffffffffu, av[m] <= lim);
+      ncand += __popc(b);
+      if (b && first == 0x7fffffff) first = 32 * m + __ffs(b) - 1;
+    }
+    int label = first;
+    if (ncand > 1) {
+      double best = DBL_MAX;
+      int bi = 0x7fffffff;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const int j = lane + 32 * m;
+        if (av[m] <= lim) {
+          const double *cj = cent + (int64_t)j * d;
+          double s = 0.0;
+          for (int t = 0; t < d; ++t) s = __dadd_rn(s, sqd_term((double)xr[t], cj[t]));
+          if (s < best || (s == best && j < bi)) { best = s; bi = j; }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      label = __shfl_sync(0xffffffffu, bi, 0);
+    }
+    if (lane == 0) labels[i] = label == 0x7fffffff ? 0 : label;
+    __syncwarp();
   }
 }
 
@@ -439,7 +495,9 @@ void dfree(T *&p) {
   p = nullptr;
 }
 
-int pad_d(int d) { return (d + 63) / 64 * 64; }  // 128-byte rows: one SW128 layout for every d
+// Feature padding: rows of 32 B (d <= 16, 32-byte swizzle), 64 B (d <= 32,
+// 64-byte swizzle) or multiples of 128 B (128-byte swizzle, 64-feature tiles).
+int pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
 
 size_t assign_smem(const SplitState *s, int stages, int k_pad, int k_cols) {
   const size_t a_stage = (size_t)2 * s->nkt * kBM * s->row_bytes;
@@ -475,7 +533,6 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
   SC_TRY(dalloc(&s->part, (size_t)nb));
   SC_TRY(dalloc(&s->flag_count, 1));
   SC_TRY(dalloc(&s->flag_list, (size_t)s->n_pad));
-  SC_TRY(dalloc(&s->cand, (size_t)s->n_pad * (1 + kMaxCand)));
   SC_TRY(dalloc(&s->cmax, 1));
   if (dtype == SC_F32)
     prep_x_kernel<float><<<nb, 256, 0, st>>>((const float *)x, n, s->n_pad, d, s->d_pad, s->xh, s->xl, s->xnrm, s->part);
@@ -499,10 +556,11 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
     return SC_ERR_INVALID;
   }
   if (k_cols > s->k_alloc) {
-    dfree(s->ch); dfree(s->cl); dfree(s->cn2);
+    dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cT);
     SC_TRY(dalloc(&s->ch, (size_t)k_cols * s->d_pad));
     SC_TRY(dalloc(&s->cl, (size_t)k_cols * s->d_pad));
     SC_TRY(dalloc(&s->cn2, (size_t)k_cols));
+    SC_TRY(dalloc(&s->cT, (size_t)k_cols * s->d_pad));
     s->k_alloc = k_cols;
     s->k_pad = 0;
   }
@@ -513,14 +571,13 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
   s->k = k;
   s->k_pad = k_pad;
   SC_CUDA(cudaMemsetAsync(s->cmax, 0, sizeof(unsigned int), st));
-  prep_c_kernel<<<k_cols, 128, 0, st>>>(cent, k, s->d, s->d_pad, k_cols, s->ch, s->cl, s->cn2, s->cmax);
+  prep_c_kernel<<<k_cols, 128, 0, st>>>(cent, k, s->d, s->d_pad, k_cols, s->ch, s->cl, s->cn2, s->cmax, s->cT);
   SC_LAUNCHED();
   return SC_OK;
 }
 
 sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d, const double *cent, int k,
-                       int32_t *labels, Acc128 *acc, unsigned long long *cnt, int scale, LloydState *lst,
-                       cudaStream_t st, cudaEvent_t *timing) {
+                       int32_t *labels, LloydState *lst, cudaStream_t st, cudaEvent_t *timing) {
   if (!s->ready || s->k != k) { set_error("split-BF16 centroids are not prepared"); return SC_ERR_INTERNAL; }
   if (n == 0) return SC_OK;
   const int k_cols = (s->k_pad + 31) / 32 * 32;
@@ -548,12 +605,12 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   p.xnrm = s->xnrm;
   p.cn2 = s->cn2;
   p.cmax = s->cmax;
+  // split remainders 3.02 * 2^-16, FP32 accumulation of 3 d_pad products <= 2^-22 each
   p.coef_dot = (float)(3.02 * 0x1p-16 + 1.02 * 3.0 * s->d_pad * 0x1p-22);
   p.coef_ref = (float)((d + 4) * 0x1p-52);
   p.labels = labels;
   p.flag_count = s->flag_count;
   p.flag_list = s->flag_list;
-  p.cand = s->cand;
   p.st = lst;
   SC_CUDA(cudaMemsetAsync(s->flag_count, 0, sizeof(int32_t), st));
   SC_CUDA(cudaFuncSetAttribute(split_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -563,21 +620,28 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   SC_LAUNCHED();
   if (timing) SC_CUDA(cudaEventRecord(timing[1], st));
   const int rgrid = 2 * s->num_sms;
-  if (dtype == SC_F32)
-    rescore_kernel<float><<<rgrid, 256, 0, st>>>((const float *)x, d, cent, k, s->flag_count, s->flag_list, s->cand,
-                                                labels, lst);
-  else
-    rescore_kernel<double><<<rgrid, 256, 0, st>>>((const double *)x, d, cent, k, s->flag_count, s->flag_list,
-                                                 s->cand, labels, lst);
+  const size_t ct_bytes = (size_t)d * k_cols * sizeof(float);
+  const int stage = ct_bytes <= 96 * 1024 ? 1 : 0;
+  const size_t rsmem = stage ? ct_bytes : 0;
+  if (dtype == SC_F32) {
+    auto kern = rescore_kernel<float>;
+    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
+    kern<<<rgrid, 32 * kRescoreWarps, rsmem, st>>>((const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
+                                                   s->xnrm, s->flag_count, s->flag_list, labels, lst, stage);
+  } else {
+    auto kern = rescore_kernel<double>;
+    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
+    kern<<<rgrid, 32 * kRescoreWarps, rsmem, st>>>((const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
+                                                   s->xnrm, s->flag_count, s->flag_list, labels, lst, stage);
+  }
   SC_LAUNCHED();
-  if (acc) SC_TRY(launch_update_fixed(dtype, x, n, d, labels, acc, cnt, scale, lst, st));
   return SC_OK;
 }
 
 void split_free(SplitState *s) {
   dfree(s->xh); dfree(s->xl); dfree(s->xnrm); dfree(s->part);
   dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cmax);
-  dfree(s->flag_count); dfree(s->flag_list); dfree(s->cand);
+  dfree(s->flag_count); dfree(s->flag_list); dfree(s->cT);
   s->ready = 0;
   s->k_alloc = 0;
   s->k_pad = 0;

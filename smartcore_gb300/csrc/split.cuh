@@ -9,8 +9,6 @@
 
 namespace sc {
 
-constexpr int kMaxCand = 6;  // candidates recorded per near-tie point
-
 struct SplitState {
   int ready = 0;
   int dtype = 0;
@@ -23,9 +21,9 @@ struct SplitState {
   __nv_bfloat16 *ch = nullptr, *cl = nullptr;  // k_pad x d_pad
   float *cn2 = nullptr;                         // k_pad: ||c||^2 rounded to f32 (+inf for padding)
   unsigned int *cmax = nullptr;                 // bits of an upper bound of max ||c||
+  float *cT = nullptr;                          // d_pad x k_cols: centroids in f32, transposed
   int32_t *flag_count = nullptr;                // near-tie points of the last assignment
   int32_t *flag_list = nullptr;                 // n entries
-  int32_t *cand = nullptr;                      // n x (1 + kMaxCand): count (-1 = all), indices
   CUtensorMap tm_xh, tm_xl, tm_ch, tm_cl;
   int num_sms = 0;
 };
@@ -38,9 +36,8 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
                         double *xnorm_total, cudaStream_t st);
 sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cudaStream_t st);
 sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d,
-                       const double *cent, int k, int32_t *labels, Acc128 *acc,
-                       unsigned long long *cnt, int scale, LloydState *lst, cudaStream_t st,
-                       cudaEvent_t *timing = nullptr);
+                       const double *cent, int k, int32_t *labels, LloydState *lst,
+                       cudaStream_t st, cudaEvent_t *timing = nullptr);
 void split_free(SplitState *s);
 
 sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,

@@ -10,6 +10,7 @@
 // reference's tree-ordered f64 sums (src/algorithm/neighbour/bbd_tree.rs:
 // 151-155) and (src/cluster/kmeans.rs:297-303).
 #include <float.h>
+#include <math.h>
 
 #include "common.cuh"
 
@@ -111,6 +112,133 @@ sc_status launch_update_fixed(int dtype, const void *x, int64_t n, int d,
 }
 
 // ---------------------------------------------------------------------------
+// K2, partial form: each CTA owns a contiguous chunk of points.  It sorts the
+// chunk's point indices by label in shared memory (32-bit counting sort),
+// then each warp sums whole clusters in int64 fixed-point registers (lane =
+// feature), with no atomics on the data path, and writes one partial per
+// (CTA, cluster, feature).  The scale keeps every partial below 2^63:
+// |x| < 2^E, chunk < 2^C points, scale = 62 - E - C.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long to_fixed64(float v, float pow2scale) {
+  return __float2ll_rn(__fmul_rn(v, pow2scale));  // exact scaling, one rounding
+}
+
+template <typename T, int MAXJ>
+__global__ void __launch_bounds__(1024)
+update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *__restrict__ labels, int k,
+                     long long *__restrict__ part, unsigned int *__restrict__ cpart, int scale,
+                     const LloydState *st) {
+  if (st && st->done) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  int *cnt = reinterpret_cast<int *>(smraw);  // k
+  int *off = cnt + k;                         // k + 1
+  int *cur = off + k + 1;                     // k
+  int *idx = cur + k;                         // chunk
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+  const int len = i1 > i0 ? (int)(i1 - i0) : 0;
+  for (int t = threadIdx.x; t < k; t += blockDim.x) cnt[t] = 0;
+  __syncthreads();
+  for (int t = threadIdx.x; t < len; t += blockDim.x) atomicAdd(&cnt[labels[i0 + t]], 1);
+  __syncthreads();
+  if (threadIdx.x < 32) {  // exclusive scan of the counts by one warp
+    int carry = 0;
+    for (int base = 0; base < k; base += 32) {
+      const int c = base + threadIdx.x;
+      const int v = c < k ? cnt[c] : 0;
+      int incl = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)threadIdx.x >= o) incl += y;
+      }
+      if (c < k) { off[c] = carry + incl - v; cur[c] = carry + incl - v; }
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (threadIdx.x == 0) off[k] = carry;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < len; t += blockDim.x) idx[atomicAdd(&cur[labels[i0 + t]], 1)] = t;
+  for (int t = threadIdx.x; t < k; t += blockDim.x) cpart[(size_t)blockIdx.x * k + t] = (unsigned int)cnt[t];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const float p2 = ldexpf(1.f, scale);
+  constexpr int kRows = MAXJ >= 16 ? 1 : 16 / MAXJ;  // rows in flight per warp (memory-level parallelism)
+  for (int c = w; c < k; c += nw) {
+    long long acc[MAXJ];
+#pragma unroll
+    for (int q = 0; q < MAXJ; ++q) acc[q] = 0;
+    const int s0 = off[c], s1 = off[c + 1];
+    for (int s = s0; s < s1; s += kRows) {
+      T v[kRows][MAXJ];
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        const bool ok = s + r < s1;
+        const T *xr = x + (i0 + (ok ? idx[s + r] : 0)) * (int64_t)d;
+#pragma unroll
+        for (int q = 0; q < MAXJ; ++q) {
+          const int j = lane + 32 * q;
+          v[r][q] = (ok && j < d) ? __ldg(xr + j) : T(0);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kRows; ++r)
+#pragma unroll
+        for (int q = 0; q < MAXJ; ++q) acc[q] += to_fixed64(v[r][q], p2);
+    }
+    long long *pc = part + ((size_t)blockIdx.x * k + c) * d;
+#pragma unroll
+    for (int q = 0; q < MAXJ; ++q) {
+      const int j = lane + 32 * q;
+      if (j < d) pc[j] = acc[q];
+    }
+  }
+}
+
+// New centroids from the per-CTA partials.  A block handles 32 (cluster,
+// feature) elements with 8 threads each; thread g adds the partials b = g
+// (mod 8) exactly in 128 bits, the 8 sums meet in shared memory.  Also the
+// distortion-identity term n_c c_j^2 - 2 c_j S_j of the element (with the
+// centroid used for the assignment), summed later by the scalar step.
+__global__ void __launch_bounds__(256)
+finalize_partials_kernel(const long long *__restrict__ part, const unsigned int *__restrict__ cpart,
+                         int nparts, int k, double *__restrict__ cent, int64_t *__restrict__ sizes, int d,
+                         int scale, double *__restrict__ terms, int empty_nan, const LloydState *st) {
+  if (st && st->done) return;
+  __shared__ unsigned long long s_lo[8][32], s_hi[8][32];
+  __shared__ unsigned long long s_cn[8][32];
+  const int64_t kd = (int64_t)k * d;
+  const int e = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int64_t t = (int64_t)blockIdx.x * 32 + e;
+  unsigned __int128 v = 0;
+  unsigned long long cn = 0;
+  if (t < kd) {
+    const int c = (int)(t / d);
+    for (int b = g; b < nparts; b += 8) {
+      v += (unsigned __int128)(__int128)part[b * kd + t];
+      cn += cpart[(size_t)b * k + c];
+    }
+  }
+  s_lo[g][e] = (unsigned long long)v;
+  s_hi[g][e] = (unsigned long long)(v >> 64);
+  s_cn[g][e] = cn;
+  __syncthreads();
+  if (g != 0 || t >= kd) return;
+  for (int q = 1; q < 8; ++q) {
+    v += ((unsigned __int128)s_hi[q][e] << 64) | s_lo[q][e];
+    cn += s_cn[q][e];
+  }
+  const int c = (int)(t / d);
+  const double sum = fixed_to_double((unsigned long long)v, (unsigned long long)(v >> 64), scale);
+  const double dn = (double)cn;
+  const double old = cent[t];
+  if (terms) terms[t] = __fma_rn(old, __fma_rn(dn, old, -2.0 * sum), 0.0);
+  if (cn > 0) cent[t] = __ddiv_rn(sum, dn);
+  else if (empty_nan) cent[t] = __longlong_as_double(0x7ff8000000000000ll);
+  if (sizes && t % d == 0) sizes[c] = (int64_t)cn;
+}
+
+// ---------------------------------------------------------------------------
 // New centroids (kmeans.rs:297-303: c = sums / size when size > 0, else the
 // old centroid; the initial means of :288-292 divide unconditionally, so an
 // empty cluster becomes NaN there: empty_nan = 1).  One block per cluster.
@@ -173,7 +301,7 @@ constexpr int kScalarThreads = 1024;
 
 __global__ void __launch_bounds__(kScalarThreads)
 finalize_scalar_kernel(const double *__restrict__ part, int nparts,
-                       const double *__restrict__ cluster_terms, int k,
+                       const double *__restrict__ cluster_terms, int64_t k,
                        const double *__restrict__ xnorm_total, LloydState *st) {
   if (st->done) return;
   __shared__ double ws[kScalarThreads / 32];
@@ -181,7 +309,7 @@ finalize_scalar_kernel(const double *__restrict__ part, int nparts,
   if (part) {
     for (int i = threadIdx.x; i < nparts; i += kScalarThreads) v += part[i];
   } else {
-    for (int i = threadIdx.x; i < k; i += kScalarThreads) v += cluster_terms[i];
+    for (int64_t i = threadIdx.x; i < k; i += kScalarThreads) v += cluster_terms[i];
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -198,7 +326,7 @@ finalize_scalar_kernel(const double *__restrict__ part, int nparts,
 }
 
 sc_status launch_finalize_scalar(const double *part, int nparts,
-                                 const double *cluster_terms, int k,
+                                 const double *cluster_terms, int64_t k,
                                  const double *xnorm_total, LloydState *st,
                                  cudaStream_t s) {
   finalize_scalar_kernel<<<1, kScalarThreads, 0, s>>>(part, nparts, cluster_terms, k, xnorm_total, st);
@@ -267,6 +395,96 @@ sc_status launch_to_row_major(int dtype, const void *src, int64_t n, int64_t d,
     to_row_major_kernel<float><<<grid, block, 0, s>>>((const float *)src, n, d, ld, (float *)dst);
   else
     to_row_major_kernel<double><<<grid, block, 0, s>>>((const double *)src, n, d, ld, (double *)dst);
+  SC_LAUNCHED();
+  return SC_OK;
+}
+
+}  // namespace sc
+
+namespace sc {
+
+static int ceil_log2(int64_t v) {
+  int l = 0;
+  while ((1ll << l) < v) ++l;
+  return l;
+}
+
+sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms) {
+  update_free(u);
+  int e = 0;
+  if (absmax > 0) frexp(absmax, &e);  // |x| < 2^e
+  int grid = num_sms;
+  int64_t chunk = (n + grid - 1) / grid;
+  if (chunk > 40000) {  // keep the per-CTA index list in shared memory
+    grid = (int)((n + 39999) / 40000);
+    chunk = (n + grid - 1) / grid;
+  }
+  const size_t smem = (size_t)(3 * k + 1 + chunk) * 4;
+  const size_t part_bytes = (size_t)grid * k * d * sizeof(long long);
+  if (dtype == SC_F32 && d <= 256 && smem <= 200 * 1024 && part_bytes <= ((size_t)512 << 20) && n > 0) {
+    u->mode = 1;
+    u->grid = grid;
+    u->threads = 1024;
+    u->smem = smem;
+    u->scale = 62 - e - ceil_log2(chunk + 1);
+    if (u->scale > 127) u->scale = 127;  // 2^scale must stay a finite float
+    if (u->scale < -126) u->scale = -126;
+    if (cudaMalloc((void **)&u->part, part_bytes) != cudaSuccess ||
+        cudaMalloc((void **)&u->cpart, (size_t)grid * k * sizeof(unsigned int)) != cudaSuccess)
+      return cuda_fail(cudaErrorMemoryAllocation, "update partials");
+    return SC_OK;
+  }
+  u->mode = 0;
+  u->scale = 125 - e - ceil_log2(n + 1);
+  if (cudaMalloc((void **)&u->acc, (size_t)k * d * sizeof(Acc128)) != cudaSuccess ||
+      cudaMalloc((void **)&u->cnt, (size_t)k * sizeof(unsigned long long)) != cudaSuccess)
+    return cuda_fail(cudaErrorMemoryAllocation, "update accumulators");
+  SC_CUDA(cudaMemset(u->acc, 0, (size_t)k * d * sizeof(Acc128)));
+  SC_CUDA(cudaMemset(u->cnt, 0, (size_t)k * sizeof(unsigned long long)));
+  return SC_OK;
+}
+
+void update_free(UpdateBuf *u) {
+  if (u->acc) cudaFree(u->acc);
+  if (u->cnt) cudaFree(u->cnt);
+  if (u->part) cudaFree(u->part);
+  if (u->cpart) cudaFree(u->cpart);
+  *u = UpdateBuf();
+}
+
+template <int MAXJ>
+static sc_status launch_sorted(const UpdateBuf *u, const float *x, int64_t n, int d, const int32_t *labels, int k,
+                               const LloydState *st, cudaStream_t s) {
+  auto kern = update_sorted_kernel<float, MAXJ>;
+  SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem));
+  kern<<<u->grid, u->threads, u->smem, s>>>(x, n, d, labels, k, u->part, u->cpart, u->scale, st);
+  SC_LAUNCHED();
+  return SC_OK;
+}
+
+sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n, int d,
+                        const int32_t *labels, int k, const LloydState *st, cudaStream_t s) {
+  if (n == 0) return SC_OK;
+  if (u->mode == 0) return launch_update_fixed(dtype, x, n, d, labels, u->acc, u->cnt, u->scale, st, s);
+  if (dtype != SC_F32) {  // the partial form scales f32 values exactly with one FMUL
+    set_error("internal: partial update form needs f32 data");
+    return SC_ERR_INTERNAL;
+  }
+  const float *xf = (const float *)x;
+  if (d <= 32) return launch_sorted<1>(u, xf, n, d, labels, k, st, s);
+  if (d <= 64) return launch_sorted<2>(u, xf, n, d, labels, k, st, s);
+  if (d <= 128) return launch_sorted<4>(u, xf, n, d, labels, k, st, s);
+  return launch_sorted<8>(u, xf, n, d, labels, k, st, s);
+}
+
+sc_status launch_finalize(const UpdateBuf *u, double *cent, int64_t *sizes, int k, int d,
+                          double *terms, int empty_nan, const LloydState *st, cudaStream_t s) {
+  if (u->mode == 0)
+    return launch_finalize_centroids(u->acc, u->cnt, cent, sizes, k, d, u->scale, terms, empty_nan, st, s);
+  const int64_t kd = (int64_t)k * d;
+  const int blocks = (int)((kd + 31) / 32);
+  finalize_partials_kernel<<<blocks, 256, 0, s>>>(u->part, u->cpart, u->grid, k, cent, sizes, d, u->scale, terms,
+                                                  empty_nan, st);
   SC_LAUNCHED();
   return SC_OK;
 }
