@@ -132,6 +132,66 @@ def cpu_baseline(x, seed_centroids, iters=3):
     }
 
 
+KNN_N, KNN_M, KNN_D, KNN_K = 200_000, 50_000, 32, 5
+KNN_CPU_QUERIES = 200
+
+
+def bench_knn(torch, local, reps=5):
+    """Brute-force kNN classifier workload: 200,000 x 32 f32 training rows in
+    10 Gaussian classes, 50,000 queries from the same mixture, k=5, uniform
+    weights.  Device-resident queries/s of find() for both forms, agreement of
+    the two forms' heap arrays and votes, and the reference's CPU search on a
+    sample of the queries."""
+    import oracle
+    from smartcore_gb300 import _lib
+    from smartcore_gb300.neighbors import LinearKNNSearch
+    from smartcore_gb300.synthetic import knn_blobs_f32
+    L = _lib.load()
+    xt, yt, xq, _ = knn_blobs_f32(KNN_N, KNN_M, KNN_D)
+    q_dev = torch.from_numpy(xq).to(f"cuda:{local}")
+    out = {}
+    res = {}
+    for name, form in (("split_bf16", _lib.FORM_SPLIT_BF16), ("fp64", _lib.FORM_FP64)):
+        s = LinearKNNSearch(xt, form=form)
+        idx = torch.empty((KNN_M, KNN_K), dtype=torch.int64, device=f"cuda:{local}")
+        dist = torch.empty((KNN_M, KNN_K), dtype=torch.float64, device=f"cuda:{local}")
+        stream = torch.cuda.ExternalStream(s.stream())
+
+        def find():
+            _lib.check(L.sc_knn_find(s.h, C.c_void_p(q_dev.data_ptr()), _lib.ROW_MAJOR, _lib.MEM_DEVICE, KNN_M,
+                                     KNN_D, KNN_K, form, _lib.MEM_DEVICE, C.c_void_p(idx.data_ptr()),
+                                     C.c_void_p(dist.data_ptr())))
+        find()  # warm-up (also builds the split training operand)
+        n_rep = reps if form == _lib.FORM_SPLIT_BF16 else 1
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(n_rep):
+            find()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / n_rep
+        out[name] = {"queries_per_s": KNN_M / (ms / 1e3), "ms_per_find": ms,
+                     "exact_distance_evals": s.rescored() if form == _lib.FORM_SPLIT_BF16 else KNN_M * KNN_N}
+        res[name] = (idx.cpu().numpy(), dist.cpu().numpy())
+        s.close()
+    out["heaps_equal"] = bool(np.array_equal(res["split_bf16"][0], res["fp64"][0]) and
+                              np.array_equal(res["split_bf16"][1], res["fp64"][1]))
+    votes = [oracle.knn_vote(res[f][0], res[f][1], yt, 10) for f in ("split_bf16", "fp64")]
+    out["labels_equal"] = bool(np.array_equal(votes[0], votes[1]))
+    t0 = time.perf_counter()
+    ridx, rdist = oracle.knn_find(xt, xq[:KNN_CPU_QUERIES], KNN_K)
+    cpu_s = time.perf_counter() - t0
+    out["oracle_sample_equal"] = bool(np.array_equal(ridx, res["split_bf16"][0][:KNN_CPU_QUERIES]) and
+                                      np.array_equal(rdist, res["split_bf16"][1][:KNN_CPU_QUERIES]))
+    out["split_speedup_vs_fp64"] = out["split_bf16"]["queries_per_s"] / out["fp64"]["queries_per_s"]
+    out["cpu_baseline"] = {"value": KNN_CPU_QUERIES / cpu_s, "unit": "queries/s", "cores": 1, "kind": "port",
+                           "sample": f"C restatement of LinearKNNSearch::find + heap replay on the first "
+                                     f"{KNN_CPU_QUERIES} of {KNN_M} queries against all {KNN_N} rows, single thread"}
+    out["config"] = {"n_train": KNN_N, "n_query": KNN_M, "d": KNN_D, "k": KNN_K, "classes": 10, "dtype": "f32"}
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -292,6 +352,8 @@ def run_ours(args):
             if line.startswith("traffic_bytes_per_launch:"):
                 traffic = float(line.split(":", 1)[1])
 
+    knn = bench_knn(torch, local) if not args.no_knn else None
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -316,6 +378,7 @@ def run_ours(args):
                       "split_speedup": value / ws / (1e3 / float(np.median(fp64_ms)))},
         "parity_vs_fp64_form": agree,
         "rescored_points": int(rescored),
+        "knn": knn,
     }
     print(json.dumps(line), flush=True)
     h.close()
@@ -327,6 +390,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-knn", action="store_true", help="skip the kNN block of the JSON line")
     ap.add_argument("--lloyd-only", action="store_true",
                     help="time the device-resident Lloyd loop only (for profiler runs)")
     args = ap.parse_args()

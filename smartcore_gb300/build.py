@@ -27,6 +27,7 @@ SOURCES = {
     "exact.cu": ["-fmad=false"],
     "update.cu": [],
     "split.cu": [],
+    "knn_split.cu": [],
     "host_rng.cpp": None,  # host compiler
 }
 

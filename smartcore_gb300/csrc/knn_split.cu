@@ -1,0 +1,488 @@
+// Split-BF16 form of LinearKNNSearch::find (src/algorithm/neighbour/
+// linear_search.rs:52-84).
+//
+// The queries are the A operand of a tcgen05 GEMM (128 per tile, one query
+// per epilogue thread) and the training rows stream through the B operand in
+// index order, 256 per tile.  From x.t_j (split-BF16, FP32 accumulate) each
+// thread forms a_j = ||t_j||^2 - 2 q.t_j, which with ||q||^2 approximates the
+// reference's squared distance D_j to within a certified bound E_q.  The
+// thread keeps the reference's k-slot heap and replays it exactly: row j can
+// only enter when D_j < root^2, so every row with a_j > root^2 - ||q||^2 + E_q
+// is skipped, and every other row gets the reference distance
+// sqrt(sum_t (double)((q_t - x_t)^2)) in FP64 and the reference's insertion
+// test and heapify (src/algorithm/sort/heap_select.rs:42-50, :71-86).  The
+// result is the reference's heap array, bit for bit.
+#include <float.h>
+#include <math.h>
+#include <string.h>
+
+#include "split.cuh"
+#include "splitprep.cuh"
+#include "tc.cuh"
+
+namespace sc {
+
+namespace {
+
+constexpr int kQM = 128;   // queries per tile (UMMA M)
+constexpr int kTN = 256;   // training rows per tile (UMMA N)
+constexpr int kKnnThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr uint64_t kWaitNs = 2000000000ull;
+
+// One term of Euclidian::squared_distance (src/metrics/distance/
+// euclidian.rs:56-62): r = a - b and r * r in the element type, then to_f64.
+__device__ __forceinline__ double ref_term(float a, float b) {
+  const float r = __fsub_rn(a, b);
+  return (double)__fmul_rn(r, r);
+}
+__device__ __forceinline__ double ref_term(double a, double b) {
+  const double r = __dsub_rn(a, b);
+  return __dmul_rn(r, r);
+}
+
+// Rows of a matrix as split-BF16 operand: halves, f32 upper bound of the norm,
+// ||row||^2 rounded to f32 (+inf for padding rows) and in f64.
+template <typename T>
+__global__ void __launch_bounds__(256)
+knn_prep_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_pad,
+                __nv_bfloat16 *__restrict__ xh, __nv_bfloat16 *__restrict__ xl, float *__restrict__ nrm,
+                float *__restrict__ n2f, double *__restrict__ n2d, unsigned int *__restrict__ nmax) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * 8 + w;
+  if (i >= n_pad) return;
+  double s = 0.0;
+  for (int j = lane; j < d_pad; j += 32) {
+    __nv_bfloat16 h = __float2bfloat16_rn(0.f), l = h;
+    if (i < n && j < d) {
+      const T v = x[i * d + j];
+      split2<T>(v, h, l);
+      s = fma((double)v, (double)v, s);
+    }
+    xh[i * d_pad + j] = h;
+    xl[i * d_pad + j] = l;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    const float r = __fsqrt_ru(__double2float_ru(s));
+    const float up = __uint_as_float(__float_as_uint(r) + 1u);
+    if (nrm) nrm[i] = up;
+    if (n2f) n2f[i] = i < n ? __double2float_rn(s) : __int_as_float(0x7f800000);
+    if (n2d) n2d[i] = s;
+    if (nmax && i < n) atomicMax(nmax, __float_as_uint(up));
+  }
+}
+
+struct KnnParams {
+  int64_t n, m;
+  int n_tiles_t, n_tiles_q;
+  int nkt, kt_elems, row_bytes;
+  int stages;
+  int k, d;
+  const float *tn2;
+  const float *qnrm;
+  const double *qn2;
+  const unsigned int *tmax;
+  float coef_dot, coef_ref;
+  int64_t *idx_out;
+  double *dist_out;
+  unsigned long long *evals;
+  int *err;
+};
+
+__device__ __forceinline__ void heap_sift(double *hd, int32_t *hi, int kk, int nn) {
+  // sift_down of heap_select.rs:71-86: node kk has children 2kk and 2kk+1
+  while (2 * kk <= nn) {
+    int j = 2 * kk;
+    if (j < nn && hd[j] < hd[j + 1]) ++j;
+    const double a = hd[kk], b = hd[j];
+    if (a == b || a > b) break;
+    if (j == kk) break;
+    hd[kk] = b;
+    hd[j] = a;
+    const int32_t t = hi[kk];
+    hi[kk] = hi[j];
+    hi[j] = t;
+    kk = j;
+  }
+}
+
+// Threshold on a_j below which a row may enter the heap: root^2 - ||q||^2 + E,
+// rounded up (a larger threshold only admits more rows to the exact test).
+__device__ __forceinline__ float knn_threshold(double root, double qn2, float eq) {
+  if (!(root < DBL_MAX)) return __int_as_float(0x7f800000);
+  const double r2 = root * root * (1.0 + 0x1p-50);
+  return __double2float_ru(r2 - qn2 + (double)eq + 1e-300);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kKnnThreads, 1)
+knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constant__ CUtensorMap tm_ql,
+                 const __grid_constant__ CUtensorMap tm_th, const __grid_constant__ CUtensorMap tm_tl,
+                 const T *__restrict__ train, const T *__restrict__ queries, const KnnParams p) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int a_blk = kQM * p.row_bytes;
+  const int a_bytes = 2 * p.nkt * a_blk;
+  const int b_blk = kTN * p.row_bytes;
+  const int b_stage = 2 * p.nkt * b_blk;
+  uint8_t *sA = base;
+  uint8_t *sB = base + a_bytes;
+  uint64_t *bars = (uint64_t *)(sB + (size_t)p.stages * b_stage);
+  uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
+  uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
+  uint32_t *s_tmem = (uint32_t *)(afull + 7);
+  int *s_abort = (int *)(s_tmem + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < p.stages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(afull, 1);
+    tc::mbar_init(aempty, 1);
+    tc::mbar_init(mma_done, 1);
+    for (int a = 0; a < 2; ++a) {
+      tc::mbar_init(&accfull[a], 1);
+      tc::mbar_init(&accempty[a], 128);
+    }
+    *s_abort = 0;
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&tm_qh);
+    tc::prefetch_tmap(&tm_ql);
+    tc::prefetch_tmap(&tm_th);
+    tc::prefetch_tmap(&tm_tl);
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(s_tmem, 2 * kTN);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *s_tmem;
+
+  if (warp == 0) {
+    if (lane == 0) {  // ---------------- TMA producer ----------------
+      int it = 0, ql = 0;
+      bool ok = true;
+      for (int qt = blockIdx.x; ok && qt < p.n_tiles_q; qt += gridDim.x, ++ql) {
+        if (!tc::mbar_wait(aempty, (uint32_t)(ql & 1) ^ 1u, kWaitNs)) { ok = false; break; }
+        tc::mbar_expect_tx(afull, (uint32_t)a_bytes);
+        for (int part = 0; part < 2; ++part)
+          for (int kt = 0; kt < p.nkt; ++kt)
+            tc::tma_load_2d(sA + (part * p.nkt + kt) * a_blk, part ? &tm_ql : &tm_qh, afull, kt * p.kt_elems,
+                            qt * kQM);
+        for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
+          const int s = it % p.stages;
+          const uint32_t ph = (uint32_t)(it / p.stages) & 1u;
+          if (!tc::mbar_wait(&empty[s], ph ^ 1u, kWaitNs) || *(volatile int *)s_abort) { ok = false; break; }
+          tc::mbar_expect_tx(&full[s], (uint32_t)b_stage);
+          uint8_t *dst = sB + (size_t)s * b_stage;
+          for (int part = 0; part < 2; ++part)
+            for (int kt = 0; kt < p.nkt; ++kt)
+              tc::tma_load_2d(dst + (part * p.nkt + kt) * b_blk, part ? &tm_tl : &tm_th, &full[s],
+                              kt * p.kt_elems, tt * kTN);
+        }
+      }
+      if (!ok) atomicExch(s_abort, 1);
+      for (int j = (it > p.stages ? it - p.stages : 0); j < it; ++j)  // drain in-flight copies
+        tc::mbar_wait(&full[j % p.stages], (uint32_t)(j / p.stages) & 1u, kWaitNs);
+      if (ql > 0) tc::mbar_wait(afull, (uint32_t)((ql - 1) & 1), kWaitNs);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // ---------------- MMA issuer ----------------
+      const uint32_t idesc = tc::idesc_bf16_f32(kQM, kTN);
+      const uint32_t sA0 = tc::smem_u32(sA), sB0 = tc::smem_u32(sB);
+      int it = 0, ql = 0;
+      bool ok = true;
+      for (int qt = blockIdx.x; ok && qt < p.n_tiles_q; qt += gridDim.x, ++ql) {
+        if (!tc::mbar_wait(afull, (uint32_t)(ql & 1), kWaitNs)) { ok = false; break; }
+        for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
+          const int s = it % p.stages, acc = it & 1;
+          const uint32_t ph = (uint32_t)(it / p.stages) & 1u, aph = (uint32_t)(it >> 1) & 1u;
+          if (!tc::mbar_wait(&accempty[acc], aph ^ 1u, kWaitNs) || !tc::mbar_wait(&full[s], ph, kWaitNs) ||
+              *(volatile int *)s_abort) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint32_t d_tmem = tmem + (uint32_t)(acc * kTN);
+          const uint32_t b0 = sB0 + (uint32_t)(s * b_stage);
+          uint32_t accumulate = 0;
+          for (int prod = 0; prod < 3; ++prod) {  // q_h.t_h + q_h.t_l + q_l.t_h
+            const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
+            for (int kt = 0; kt < p.nkt; ++kt)
+              for (int ks = 0; ks < p.kt_elems / 16; ++ks) {
+                const uint64_t ad = tc::smem_desc(sA0 + (uint32_t)((pa * p.nkt + kt) * a_blk + ks * 32), p.row_bytes);
+                const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((pb * p.nkt + kt) * b_blk + ks * 32), p.row_bytes);
+                tc::mma_f16(d_tmem, ad, bd, idesc, accumulate);
+                accumulate = 1;
+              }
+          }
+          tc::mma_commit(&empty[s]);
+          tc::mma_commit(&accfull[acc]);
+        }
+        tc::mma_commit(aempty);  // the query tile's smem is free once these MMAs complete
+      }
+      if (!ok) atomicExch(s_abort, 1);
+      tc::mma_commit(mma_done);
+      tc::mbar_wait(mma_done, 0, kWaitNs);
+    }
+  } else {
+    // ---------------- epilogue: one query per thread ----------------
+    const int q4 = warp & 3;
+    const int row = q4 * 32 + lane;
+    const float tmax = __uint_as_float(*p.tmax);
+    double hd[kMaxKnnK];
+    int32_t hi[kMaxKnnK];
+    unsigned long long evals = 0;
+    int it = 0;
+    bool stop = false;
+    for (int qt = blockIdx.x; !stop && qt < p.n_tiles_q; qt += gridDim.x) {
+      const int64_t q = (int64_t)qt * kQM + row;
+      const bool live = q < p.m;
+      for (int s = 0; s < p.k; ++s) {
+        hd[s] = __longlong_as_double(0x7ff0000000000000ll);
+        hi[s] = -1;
+      }
+      const float qn = live ? p.qnrm[q] : 0.f;
+      const double qn2 = live ? p.qn2[q] : 0.0;
+      const float eq = 2.1f * (p.coef_dot * 2.f * qn * tmax + 0x1p-22f * (tmax * tmax + qn * tmax) +
+                               p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
+      float thr = live ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000);
+      const T *qr = queries + (live ? q : 0) * (int64_t)p.d;
+      for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
+        const int acc = it & 1;
+        const bool got = tc::mbar_wait(&accfull[acc], (uint32_t)(it >> 1) & 1u, kWaitNs);
+        if (!__all_sync(0xffffffffu, got) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
+          atomicExch(s_abort, 1);
+          stop = true;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(acc * kTN);
+        const int64_t j0 = (int64_t)tt * kTN;
+        for (int c0 = 0; c0 < kTN; c0 += 32) {
+          uint32_t v[32];
+          __syncwarp();
+          tc::tmem_ld32(taddr + (uint32_t)c0, v);
+          tc::tmem_wait_ld();
+          const float4 *t4 = reinterpret_cast<const float4 *>(p.tn2 + j0 + c0);
+#pragma unroll
+          for (int j4 = 0; j4 < 8; ++j4) {
+            const float4 tv = __ldg(t4 + j4);
+            const float tn[4] = {tv.x, tv.y, tv.z, tv.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int jj = 4 * j4 + e;
+              const float a = fmaf(-2.f, __uint_as_float(v[jj]), tn[e]);
+              if (a <= thr) {  // cannot be excluded: exact reference distance and heap step
+                const int64_t j = j0 + c0 + jj;
+                if (j < p.n) {
+                  const T *tr = train + j * (int64_t)p.d;
+                  double sq = 0.0;
+                  for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qr[t], tr[t]));
+                  const double dist = __dsqrt_rn(sq);
+                  ++evals;
+                  if (dist < hd[0]) {
+                    hd[0] = dist;
+                    hi[0] = (int32_t)j;
+                    if (p.k > 1)
+                      for (int s = p.k / 2 - 1; s >= 0; --s) heap_sift(hd, hi, s, p.k - 1);
+                    thr = knn_threshold(hd[0], qn2, eq);
+                  }
+                }
+              }
+            }
+          }
+        }
+        tc::fence_before_sync();
+        tc::mbar_arrive(&accempty[acc]);
+      }
+      if (live && !stop)
+        for (int s = 0; s < p.k; ++s) {
+          p.idx_out[q * p.k + s] = hi[s];
+          p.dist_out[q * p.k + s] = hd[s];
+        }
+    }
+    if (evals) atomicAdd(p.evals, evals);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 2 * kTN);
+  }
+  if (threadIdx.x == 0 && *s_abort) atomicExch(p.err, 4);
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+sc_status map2d(CUtensorMap *m, void *ptr, int64_t rows, int cols, int box_cols, int box_rows, int row_bytes) {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &f, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      set_error("cuTensorMapEncodeTiled is unavailable");
+      return SC_ERR_CUDA;
+    }
+    fn = (EncodeTiledFn)f;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUtensorMapSwizzle sw = row_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                                  : CU_TENSOR_MAP_SWIZZLE_32B;
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return SC_ERR_CUDA; }
+  return SC_OK;
+}
+
+template <class T>
+sc_status dal(T **p, size_t count) {
+  *p = nullptr;
+  SC_CUDA(cudaMalloc((void **)p, (count ? count : 1) * sizeof(T)));
+  return SC_OK;
+}
+template <class T>
+void dfr(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
+
+size_t knn_smem(int nkt, int row_bytes, int stages) {
+  return 1024 + (size_t)2 * nkt * kQM * row_bytes + (size_t)stages * 2 * nkt * kTN * row_bytes +
+         (size_t)(2 * stages + 8) * 8 + 16;
+}
+
+}  // namespace
+
+sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
+                    int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, cudaStream_t st) {
+  if (rescored) *rescored = 0;
+  if (m == 0 || n == 0) return SC_OK;
+  const int d_pad = knn_pad_d(d);
+  const int kt_elems = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt_elems, row_bytes = kt_elems * 2;
+  int stages = 6;
+  while (stages > 2 && knn_smem(nkt, row_bytes, stages) > 227 * 1024) --stages;
+  const size_t smem = knn_smem(nkt, row_bytes, stages);
+  if (d_pad > 256 || smem > 227 * 1024) {
+    set_error("d=%d exceeds the split-BF16 kNN kernel's shared memory", d);
+    return SC_ERR_INVALID;
+  }
+  int dev = 0;
+  SC_CUDA(cudaGetDevice(&dev));
+  if (!s->num_sms) SC_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t n_pad = (n + kTN - 1) / kTN * kTN;
+  if (!s->ready || s->train != train || s->n != n || s->d != d) {  // training operand, once per handle
+    dfr(s->th); dfr(s->tl); dfr(s->tn2); dfr(s->tmax);
+    SC_TRY(dal(&s->th, (size_t)n_pad * d_pad));
+    SC_TRY(dal(&s->tl, (size_t)n_pad * d_pad));
+    SC_TRY(dal(&s->tn2, (size_t)n_pad));
+    SC_TRY(dal(&s->tmax, 1));
+    SC_CUDA(cudaMemsetAsync(s->tmax, 0, sizeof(unsigned int), st));
+    const int nb = (int)((n_pad + 7) / 8);
+    if (dtype == SC_F32)
+      knn_prep_kernel<float><<<nb, 256, 0, st>>>((const float *)train, n, n_pad, d, d_pad, s->th, s->tl, nullptr,
+                                                s->tn2, nullptr, s->tmax);
+    else
+      knn_prep_kernel<double><<<nb, 256, 0, st>>>((const double *)train, n, n_pad, d, d_pad, s->th, s->tl,
+                                                 nullptr, s->tn2, nullptr, s->tmax);
+    SC_LAUNCHED();
+    SC_TRY(map2d(&s->tm_th, s->th, n_pad, d_pad, kt_elems, kTN, row_bytes));
+    SC_TRY(map2d(&s->tm_tl, s->tl, n_pad, d_pad, kt_elems, kTN, row_bytes));
+    s->train = train;
+    s->n = n;
+    s->d = d;
+    s->ready = 1;
+  }
+  const int64_t m_pad = (m + kQM - 1) / kQM * kQM;
+  if (m_pad > s->m_cap) {
+    dfr(s->qh); dfr(s->ql); dfr(s->qnrm); dfr(s->qn2);
+    SC_TRY(dal(&s->qh, (size_t)m_pad * d_pad));
+    SC_TRY(dal(&s->ql, (size_t)m_pad * d_pad));
+    SC_TRY(dal(&s->qnrm, (size_t)m_pad));
+    SC_TRY(dal(&s->qn2, (size_t)m_pad));
+    s->m_cap = m_pad;
+  }
+  if (!s->evals) SC_TRY(dal(&s->evals, 2));
+  SC_CUDA(cudaMemsetAsync(s->evals, 0, 2 * sizeof(unsigned long long), st));
+  const int nbq = (int)((m_pad + 7) / 8);
+  if (dtype == SC_F32)
+    knn_prep_kernel<float><<<nbq, 256, 0, st>>>((const float *)queries, m, m_pad, d, d_pad, s->qh, s->ql, s->qnrm,
+                                               nullptr, s->qn2, nullptr);
+  else
+    knn_prep_kernel<double><<<nbq, 256, 0, st>>>((const double *)queries, m, m_pad, d, d_pad, s->qh, s->ql,
+                                                s->qnrm, nullptr, s->qn2, nullptr);
+  SC_LAUNCHED();
+  CUtensorMap tm_qh, tm_ql;
+  SC_TRY(map2d(&tm_qh, s->qh, m_pad, d_pad, kt_elems, kQM, row_bytes));
+  SC_TRY(map2d(&tm_ql, s->ql, m_pad, d_pad, kt_elems, kQM, row_bytes));
+  KnnParams p;
+  memset(&p, 0, sizeof p);
+  p.n = n;
+  p.m = m;
+  p.n_tiles_t = (int)(n_pad / kTN);
+  p.n_tiles_q = (int)(m_pad / kQM);
+  p.nkt = nkt;
+  p.kt_elems = kt_elems;
+  p.row_bytes = row_bytes;
+  p.stages = stages;
+  p.k = k;
+  p.d = d;
+  p.tn2 = s->tn2;
+  p.qnrm = s->qnrm;
+  p.qn2 = s->qn2;
+  p.tmax = s->tmax;
+  p.coef_dot = (float)(3.02 * 0x1p-16 + 1.02 * 3.0 * d_pad * 0x1p-22);
+  p.coef_ref = (float)((d + 4) * 0x1p-52);
+  p.idx_out = idx;
+  p.dist_out = dist;
+  p.evals = s->evals;
+  p.err = (int *)(s->evals + 1);
+  const int grid = p.n_tiles_q < s->num_sms ? p.n_tiles_q : s->num_sms;
+  if (dtype == SC_F32) {
+    auto kern = knn_split_kernel<float>;
+    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, (const float *)train,
+                                          (const float *)queries, p);
+  } else {
+    auto kern = knn_split_kernel<double>;
+    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, (const double *)train,
+                                          (const double *)queries, p);
+  }
+  SC_LAUNCHED();
+  unsigned long long host[2];
+  SC_CUDA(cudaMemcpyAsync(host, s->evals, sizeof host, cudaMemcpyDeviceToHost, st));
+  SC_CUDA(cudaStreamSynchronize(st));
+  if (host[1]) {
+    set_error("split-BF16 kNN kernel: a bounded wait timed out");
+    return SC_ERR_TIMEOUT;
+  }
+  if (rescored) *rescored = (int64_t)host[0];
+  return SC_OK;
+}
+
+void split_knn_free(SplitKnnState *s) {
+  dfr(s->th); dfr(s->tl); dfr(s->tn2); dfr(s->tmax);
+  dfr(s->qh); dfr(s->ql); dfr(s->qnrm); dfr(s->qn2); dfr(s->evals);
+  s->ready = 0;
+  s->m_cap = 0;
+}
+
+}  // namespace sc

@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include "split.cuh"
+#include "splitprep.cuh"
 #include "tc.cuh"
 
 namespace sc {
@@ -33,78 +34,6 @@ enum { kErrTimeout = 4 };
 __device__ __forceinline__ double sqd_term(double a, double b) {
   const double r = __dsub_rn(a, b);
   return __dmul_rn(r, r);
-}
-
-// ---------------------------------------------------------------------------
-// Preparation of the point operand: BF16 halves (row-major, d padded to
-// d_pad), an upper bound of ||x|| in f32, and block sums of ||x||^2 in f64.
-// One warp per point.
-// ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ void split2(T v, __nv_bfloat16 &h, __nv_bfloat16 &l);
-template <>
-__device__ __forceinline__ void split2<float>(float v, __nv_bfloat16 &h, __nv_bfloat16 &l) {
-  h = __float2bfloat16_rn(v);
-  l = __float2bfloat16_rn(v - __bfloat162float(h));  // v - h is exact in f32
-}
-template <>
-__device__ __forceinline__ void split2<double>(double v, __nv_bfloat16 &h, __nv_bfloat16 &l) {
-  h = __double2bfloat16(v);
-  l = __double2bfloat16(v - (double)__bfloat162float(h));  // exact in f64
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256)
-prep_x_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_pad,
-              __nv_bfloat16 *__restrict__ xh, __nv_bfloat16 *__restrict__ xl,
-              float *__restrict__ xnrm, double *__restrict__ part) {
-  __shared__ double ws[8];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t i = (int64_t)blockIdx.x * 8 + w;
-  double s = 0.0;
-  if (i < n_pad) {
-    for (int j = lane; j < d_pad; j += 32) {
-      __nv_bfloat16 h = __float2bfloat16_rn(0.f), l = h;
-      if (i < n && j < d) {
-        const T v = x[i * d + j];
-        split2<T>(v, h, l);
-        s = fma((double)v, (double)v, s);
-      }
-      xh[i * d_pad + j] = h;
-      xl[i * d_pad + j] = l;
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) {
-    if (i < n_pad) {
-      // sqrt rounded up, then one more f32 ulp: an upper bound of ||x||
-      const float r = __fsqrt_ru(__double2float_ru(s));
-      xnrm[i] = __uint_as_float(__float_as_uint(r) + 1u);
-    }
-    ws[w] = s;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int q = 0; q < 8; ++q) t += ws[q];
-    part[blockIdx.x] = t;
-  }
-}
-
-__global__ void sum_parts_kernel(const double *__restrict__ part, int nparts, double *__restrict__ out) {
-  __shared__ double ws[32];
-  double v = 0.0;
-  for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += part[i];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
-    *out = t;
-  }
 }
 
 // Centroid operand: BF16 halves of the f64 centroids, ||c||^2 rounded to f32
@@ -302,42 +231,58 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       }
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * p.k_cols);
-      float a1 = inf, a2 = inf, b1 = inf, b2 = inf;
-      int ai = 0x7fffffff, bi = 0x7fffffff;
-      for (int c0 = 0; c0 < p.k_cols; c0 += 32) {
-        uint32_t v[32];
-        tc::tmem_ld32(taddr + (uint32_t)c0, v);
+      // four trackers on columns j = 4c + r (r = 0..3) for instruction-level parallelism
+      float m1[4] = {inf, inf, inf, inf}, m2[4] = {inf, inf, inf, inf};
+      int mi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+      for (int c0 = 0; c0 < p.k_cols; c0 += 64) {
+        uint32_t v[64];
+        if (c0 + 64 <= p.k_cols) {
+          tc::tmem_ld64(taddr + (uint32_t)c0, v);
+        } else {
+          uint32_t (&lo)[32] = *reinterpret_cast<uint32_t (*)[32]>(v);
+          tc::tmem_ld32(taddr + (uint32_t)c0, lo);
+        }
         tc::tmem_wait_ld();
+        const int nc = p.k_cols - c0 < 64 ? 32 : 64;
 #pragma unroll
-        for (int jj = 0; jj < 32; jj += 2) {
-          const float x0 = fmaf(-2.f, __uint_as_float(v[jj]), s_cn2[c0 + jj]);
-          const float x1 = fmaf(-2.f, __uint_as_float(v[jj + 1]), s_cn2[c0 + jj + 1]);
-          const bool l0 = x0 < a1, l1 = x1 < b1;
-          a2 = l0 ? a1 : fminf(a2, x0);
-          b2 = l1 ? b1 : fminf(b2, x1);
-          ai = l0 ? c0 + jj : ai;
-          bi = l1 ? c0 + jj + 1 : bi;
-          a1 = l0 ? x0 : a1;
-          b1 = l1 ? x1 : b1;
+        for (int jj = 0; jj < 64; jj += 4) {
+          if (jj >= nc) break;
+          const float4 cc = *reinterpret_cast<const float4 *>(s_cn2 + c0 + jj);
+          const float cv[4] = {cc.x, cc.y, cc.z, cc.w};
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            const float x = fmaf(-2.f, __uint_as_float(v[jj + r]), cv[r]);
+            const bool lt = x < m1[r];
+            m2[r] = lt ? m1[r] : fminf(m2[r], x);
+            mi[r] = lt ? c0 + jj + r : mi[r];
+            m1[r] = lt ? x : m1[r];
+          }
         }
       }
       tc::fence_before_sync();
       tc::mbar_arrive(&accempty[g]);
-      // merge the even- and odd-column trackers
-      float m1, m2;
-      int a;
-      if (b1 < a1 || (b1 == a1 && bi < ai)) {
-        m1 = b1; a = bi; m2 = fminf(b2, a1);
-      } else {
-        m1 = a1; a = ai; m2 = fminf(a2, b1);
+      // merge the four trackers: lowest value, lowest index on ties
+      float mm1 = m1[0], mm2 = m2[0];
+      int a = mi[0];
+#pragma unroll
+      for (int r = 1; r < 4; ++r) {
+        if (m1[r] < mm1 || (m1[r] == mm1 && mi[r] < a)) {
+          mm2 = fminf(mm1, m2[r]);
+          mm1 = m1[r];
+          a = mi[r];
+        } else {
+          mm2 = fminf(mm2, m1[r]);
+        }
+        mm2 = fminf(mm2, m2[r]);
       }
+      const float m1v = mm1, m2v = mm2;
       const int64_t i = (int64_t)t * kBM + row;
       if (i < p.n) {
         const float xn = p.xnrm[i];
         const float e = p.coef_dot * 2.f * xn * cmax + 0x1p-22f * (cmax * cmax + xn * cmax) +
                         p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
         p.labels[i] = a == 0x7fffffff ? 0 : a;
-        if (!(m2 - m1 > 2.1f * e)) p.flag_list[atomicAdd(p.flag_count, 1)] = (int32_t)i;
+        if (!(m2v - m1v > 2.1f * e)) p.flag_list[atomicAdd(p.flag_count, 1)] = (int32_t)i;
       }
     }
   }
@@ -647,11 +592,6 @@ void split_free(SplitState *s) {
   s->k_pad = 0;
 }
 
-sc_status split_knn(SplitKnnState *, int, const void *, int64_t, int, const void *, int64_t, int, int64_t *,
-                    double *, int64_t *, cudaStream_t) {
-  set_error("the split-BF16 kNN form is not available in this build");
-  return SC_ERR_INVALID;
-}
-void split_knn_free(SplitKnnState *) {}
+
 
 }  // namespace sc

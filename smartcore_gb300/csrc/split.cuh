@@ -30,6 +30,18 @@ struct SplitState {
 
 struct SplitKnnState {
   int ready = 0;
+  const void *train = nullptr;  // device rows the training operand was built from
+  int64_t n = 0;
+  int d = 0, num_sms = 0;
+  __nv_bfloat16 *th = nullptr, *tl = nullptr;  // n_pad x d_pad training halves
+  float *tn2 = nullptr;                         // n_pad: ||t||^2 in f32 (+inf padding)
+  unsigned int *tmax = nullptr;                 // bits of an upper bound of max ||t||
+  CUtensorMap tm_th, tm_tl;
+  __nv_bfloat16 *qh = nullptr, *ql = nullptr;  // query halves (per call)
+  float *qnrm = nullptr;
+  double *qn2 = nullptr;
+  int64_t m_cap = 0;
+  unsigned long long *evals = nullptr;          // [0] exact evaluations, [1] error flag
 };
 
 sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int d,

@@ -119,8 +119,25 @@ sc_status launch_update_fixed(int dtype, const void *x, int64_t n, int d,
 // (CTA, cluster, feature).  The scale keeps every partial below 2^63:
 // |x| < 2^E, chunk < 2^C points, scale = 62 - E - C.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ long long to_fixed64(float v, float pow2scale) {
-  return __float2ll_rn(__fmul_rn(v, pow2scale));  // exact scaling, one rounding
+// v * 2^scale rounded to the nearest integer (ties to even), integer ALU only
+// (a 64-bit float-to-int conversion would run on the FP64 pipe).  The scale
+// guarantees |v| * 2^scale < 2^62, so left shifts stay within 62 bits.
+__device__ __forceinline__ long long to_fixed64(float v, int scale) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  const uint32_t m = (b & 0x7fffffu) | (e ? 0x800000u : 0u);
+  const int sh = (e ? e : 1) - 150 + scale;
+  long long mag;
+  if (sh >= 0) {
+    mag = (long long)m << sh;
+  } else if (sh > -25) {
+    const int r = -sh;
+    const uint32_t q = m >> r, rem = m & ((1u << r) - 1u), half = 1u << (r - 1);
+    mag = (long long)(q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u));
+  } else {
+    mag = 0;  // |v| * 2^scale < 2^-1
+  }
+  return (b >> 31) ? -mag : mag;
 }
 
 template <typename T, int MAXJ>
@@ -162,7 +179,6 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
   for (int t = threadIdx.x; t < k; t += blockDim.x) cpart[(size_t)blockIdx.x * k + t] = (unsigned int)cnt[t];
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const float p2 = ldexpf(1.f, scale);
   constexpr int kRows = MAXJ >= 16 ? 1 : 16 / MAXJ;  // rows in flight per warp (memory-level parallelism)
   for (int c = w; c < k; c += nw) {
     long long acc[MAXJ];
@@ -184,7 +200,7 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
 #pragma unroll
       for (int r = 0; r < kRows; ++r)
 #pragma unroll
-        for (int q = 0; q < MAXJ; ++q) acc[q] += to_fixed64(v[r][q], p2);
+        for (int q = 0; q < MAXJ; ++q) acc[q] += to_fixed64(v[r][q], scale);
     }
     long long *pc = part + ((size_t)blockIdx.x * k + c) * d;
 #pragma unroll
@@ -427,8 +443,7 @@ sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double 
     u->threads = 1024;
     u->smem = smem;
     u->scale = 62 - e - ceil_log2(chunk + 1);
-    if (u->scale > 127) u->scale = 127;  // 2^scale must stay a finite float
-    if (u->scale < -126) u->scale = -126;
+    if (u->scale > 160) u->scale = 160;  // values below 2^-160 contribute 0
     if (cudaMalloc((void **)&u->part, part_bytes) != cudaSuccess ||
         cudaMalloc((void **)&u->cpart, (size_t)grid * k * sizeof(unsigned int)) != cudaSuccess)
       return cuda_fail(cudaErrorMemoryAllocation, "update partials");
