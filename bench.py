@@ -136,7 +136,7 @@ KNN_N, KNN_M, KNN_D, KNN_K = 200_000, 50_000, 32, 5
 KNN_CPU_QUERIES = 200
 
 
-def bench_knn(torch, local, reps=5):
+def bench_knn(torch, local, reps=5, n_query=None, with_fp64=True):
     """Brute-force kNN classifier workload: 200,000 x 32 f32 training rows in
     10 Gaussian classes, 50,000 queries from the same mixture, k=5, uniform
     weights.  Device-resident queries/s of find() for both forms, agreement of
@@ -147,18 +147,21 @@ def bench_knn(torch, local, reps=5):
     from smartcore_gb300.neighbors import LinearKNNSearch
     from smartcore_gb300.synthetic import knn_blobs_f32
     L = _lib.load()
-    xt, yt, xq, _ = knn_blobs_f32(KNN_N, KNN_M, KNN_D)
+    m = n_query or KNN_M
+    xt, yt, xq, _ = knn_blobs_f32(KNN_N, m, KNN_D)
     q_dev = torch.from_numpy(xq).to(f"cuda:{local}")
     out = {}
     res = {}
-    for name, form in (("split_bf16", _lib.FORM_SPLIT_BF16), ("fp64", _lib.FORM_FP64)):
+    forms = (("split_bf16", _lib.FORM_SPLIT_BF16), ("fp64", _lib.FORM_FP64)) if with_fp64 else \
+        (("split_bf16", _lib.FORM_SPLIT_BF16),)
+    for name, form in forms:
         s = LinearKNNSearch(xt, form=form)
-        idx = torch.empty((KNN_M, KNN_K), dtype=torch.int64, device=f"cuda:{local}")
-        dist = torch.empty((KNN_M, KNN_K), dtype=torch.float64, device=f"cuda:{local}")
+        idx = torch.empty((m, KNN_K), dtype=torch.int64, device=f"cuda:{local}")
+        dist = torch.empty((m, KNN_K), dtype=torch.float64, device=f"cuda:{local}")
         stream = torch.cuda.ExternalStream(s.stream())
 
         def find():
-            _lib.check(L.sc_knn_find(s.h, C.c_void_p(q_dev.data_ptr()), _lib.ROW_MAJOR, _lib.MEM_DEVICE, KNN_M,
+            _lib.check(L.sc_knn_find(s.h, C.c_void_p(q_dev.data_ptr()), _lib.ROW_MAJOR, _lib.MEM_DEVICE, m,
                                      KNN_D, KNN_K, form, _lib.MEM_DEVICE, C.c_void_p(idx.data_ptr()),
                                      C.c_void_p(dist.data_ptr())))
         find()  # warm-up (also builds the split training operand)
@@ -171,10 +174,12 @@ def bench_knn(torch, local, reps=5):
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1) / n_rep
-        out[name] = {"queries_per_s": KNN_M / (ms / 1e3), "ms_per_find": ms,
-                     "exact_distance_evals": s.rescored() if form == _lib.FORM_SPLIT_BF16 else KNN_M * KNN_N}
+        out[name] = {"queries_per_s": m / (ms / 1e3), "ms_per_find": ms,
+                     "exact_distance_evals": s.rescored() if form == _lib.FORM_SPLIT_BF16 else m * KNN_N}
         res[name] = (idx.cpu().numpy(), dist.cpu().numpy())
         s.close()
+    if not with_fp64:
+        return out
     out["heaps_equal"] = bool(np.array_equal(res["split_bf16"][0], res["fp64"][0]) and
                               np.array_equal(res["split_bf16"][1], res["fp64"][1]))
     votes = [oracle.knn_vote(res[f][0], res[f][1], yt, 10) for f in ("split_bf16", "fp64")]
@@ -393,9 +398,16 @@ def main():
     ap.add_argument("--no-knn", action="store_true", help="skip the kNN block of the JSON line")
     ap.add_argument("--lloyd-only", action="store_true",
                     help="time the device-resident Lloyd loop only (for profiler runs)")
+    ap.add_argument("--knn-only", type=int, default=0, metavar="QUERIES",
+                    help="time only the split-BF16 kNN find with this many queries (for profiler runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.knn_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(bench_knn(torch, 0, reps=2, n_query=args.knn_only, with_fp64=False)), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

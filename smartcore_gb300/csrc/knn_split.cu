@@ -128,7 +128,8 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   const int b_stage = 2 * p.nkt * b_blk;
   uint8_t *sA = base;
   uint8_t *sB = base + a_bytes;
-  uint64_t *bars = (uint64_t *)(sB + (size_t)p.stages * b_stage);
+  float *sT = (float *)(sB + (size_t)p.stages * b_stage);  // ||t||^2 of each stage's tile
+  uint64_t *bars = (uint64_t *)(sT + (size_t)p.stages * kTN);
   uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
   uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
   uint32_t *s_tmem = (uint32_t *)(afull + 7);
@@ -137,7 +138,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   if (threadIdx.x == 0) {
     for (int s = 0; s < p.stages; ++s) {
       tc::mbar_init(&full[s], 1);
-      tc::mbar_init(&empty[s], 1);
+      tc::mbar_init(&empty[s], 1 + 128);  // the MMAs' commit and the epilogue's read of sT
     }
     tc::mbar_init(afull, 1);
     tc::mbar_init(aempty, 1);
@@ -177,12 +178,13 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
           const int s = it % p.stages;
           const uint32_t ph = (uint32_t)(it / p.stages) & 1u;
           if (!tc::mbar_wait(&empty[s], ph ^ 1u, kWaitNs) || *(volatile int *)s_abort) { ok = false; break; }
-          tc::mbar_expect_tx(&full[s], (uint32_t)b_stage);
+          tc::mbar_expect_tx(&full[s], (uint32_t)(b_stage + kTN * 4));
           uint8_t *dst = sB + (size_t)s * b_stage;
           for (int part = 0; part < 2; ++part)
             for (int kt = 0; kt < p.nkt; ++kt)
               tc::tma_load_2d(dst + (part * p.nkt + kt) * b_blk, part ? &tm_tl : &tm_th, &full[s],
                               kt * p.kt_elems, tt * kTN);
+          tc::bulk_load(sT + s * kTN, p.tn2 + (int64_t)tt * kTN, kTN * 4, &full[s]);
         }
       }
       if (!ok) atomicExch(s_abort, 1);
@@ -263,42 +265,44 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         tc::fence_after_sync();
         const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(acc * kTN);
         const int64_t j0 = (int64_t)tt * kTN;
+        const float *tn = sT + (it % p.stages) * kTN;
         for (int c0 = 0; c0 < kTN; c0 += 32) {
           uint32_t v[32];
           __syncwarp();
           tc::tmem_ld32(taddr + (uint32_t)c0, v);
           tc::tmem_wait_ld();
-          const float4 *t4 = reinterpret_cast<const float4 *>(p.tn2 + j0 + c0);
+          // branch-free scan: which columns cannot be excluded at the chunk-start threshold
+          uint32_t mask = 0;
 #pragma unroll
-          for (int j4 = 0; j4 < 8; ++j4) {
-            const float4 tv = __ldg(t4 + j4);
-            const float tn[4] = {tv.x, tv.y, tv.z, tv.w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const int jj = 4 * j4 + e;
-              const float a = fmaf(-2.f, __uint_as_float(v[jj]), tn[e]);
-              if (a <= thr) {  // cannot be excluded: exact reference distance and heap step
-                const int64_t j = j0 + c0 + jj;
-                if (j < p.n) {
-                  const T *tr = train + j * (int64_t)p.d;
-                  double sq = 0.0;
-                  for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qr[t], tr[t]));
-                  const double dist = __dsqrt_rn(sq);
-                  ++evals;
-                  if (dist < hd[0]) {
-                    hd[0] = dist;
-                    hi[0] = (int32_t)j;
-                    if (p.k > 1)
-                      for (int s = p.k / 2 - 1; s >= 0; --s) heap_sift(hd, hi, s, p.k - 1);
-                    thr = knn_threshold(hd[0], qn2, eq);
-                  }
-                }
-              }
+          for (int jj = 0; jj < 32; jj += 4) {
+            const float4 tv = *reinterpret_cast<const float4 *>(tn + c0 + jj);
+            mask |= (fmaf(-2.f, __uint_as_float(v[jj]), tv.x) <= thr ? 1u : 0u) << jj;
+            mask |= (fmaf(-2.f, __uint_as_float(v[jj + 1]), tv.y) <= thr ? 1u : 0u) << (jj + 1);
+            mask |= (fmaf(-2.f, __uint_as_float(v[jj + 2]), tv.z) <= thr ? 1u : 0u) << (jj + 2);
+            mask |= (fmaf(-2.f, __uint_as_float(v[jj + 3]), tv.w) <= thr ? 1u : 0u) << (jj + 3);
+          }
+          while (mask) {  // in index order: exact reference distance and heap step
+            const int jj = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int64_t j = j0 + c0 + jj;
+            if (j >= p.n) break;
+            const T *tr = train + j * (int64_t)p.d;
+            double sq = 0.0;
+            for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qr[t], tr[t]));
+            const double dist = __dsqrt_rn(sq);
+            ++evals;
+            if (dist < hd[0]) {
+              hd[0] = dist;
+              hi[0] = (int32_t)j;
+              if (p.k > 1)
+                for (int s = p.k / 2 - 1; s >= 0; --s) heap_sift(hd, hi, s, p.k - 1);
+              thr = knn_threshold(hd[0], qn2, eq);
             }
           }
         }
         tc::fence_before_sync();
         tc::mbar_arrive(&accempty[acc]);
+        tc::mbar_arrive(&empty[it % p.stages]);
       }
       if (live && !stop)
         for (int s = 0; s < p.k; ++s) {
@@ -365,7 +369,7 @@ void dfr(T *&p) {
 int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
 
 size_t knn_smem(int nkt, int row_bytes, int stages) {
-  return 1024 + (size_t)2 * nkt * kQM * row_bytes + (size_t)stages * 2 * nkt * kTN * row_bytes +
+  return 1024 + (size_t)2 * nkt * kQM * row_bytes + (size_t)stages * (2 * nkt * kTN * row_bytes + kTN * 4) +
          (size_t)(2 * stages + 8) * 8 + 16;
 }
 
