@@ -46,7 +46,8 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 knn_prep_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_pad,
                 __nv_bfloat16 *__restrict__ xh, __nv_bfloat16 *__restrict__ xl, float *__restrict__ nrm,
-                float *__restrict__ n2f, double *__restrict__ n2d, unsigned int *__restrict__ nmax) {
+                float *__restrict__ n2f, double *__restrict__ n2d, unsigned int *__restrict__ nmax,
+                __nv_bfloat16 *__restrict__ bx) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t i = (int64_t)blockIdx.x * 8 + w;
   if (i >= n_pad) return;
@@ -70,6 +71,16 @@ knn_prep_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_
     if (n2f) n2f[i] = i < n ? __double2float_rn(s) : __int_as_float(0x7f800000);
     if (n2d) n2d[i] = s;
     if (nmax && i < n) atomicMax(nmax, __float_as_uint(up));
+    if (bx) {  // norm-folding row: BF16 terms of -||row||^2/2 (padding rows never pass)
+      const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
+      __nv_bfloat16 h = __float2bfloat16_rn(-1e30f), mm = zero, l = zero;
+      if (i < n) split3(-0.5 * s, h, mm, l);
+      __nv_bfloat16 *row = bx + i * 16;
+      row[0] = h;
+      row[1] = mm;
+      row[2] = l;
+      for (int c = 3; c < 16; ++c) row[c] = zero;
+    }
   }
 }
 
@@ -79,11 +90,10 @@ struct KnnParams {
   int nkt, kt_elems, row_bytes;
   int stages;
   int k, d;
-  const float *tn2;
   const float *qnrm;
   const double *qn2;
   const unsigned int *tmax;
-  float coef_dot, coef_ref;
+  float coef_xc, coef_cc, coef_ref;
   int64_t *idx_out;
   double *dist_out;
   unsigned long long *evals;
@@ -119,17 +129,18 @@ template <typename T>
 __global__ void __launch_bounds__(kKnnThreads, 1)
 knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constant__ CUtensorMap tm_ql,
                  const __grid_constant__ CUtensorMap tm_th, const __grid_constant__ CUtensorMap tm_tl,
+                 const __grid_constant__ CUtensorMap tm_ones, const __grid_constant__ CUtensorMap tm_tbx,
                  const T *__restrict__ train, const T *__restrict__ queries, const KnnParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int a_blk = kQM * p.row_bytes;
   const int a_bytes = 2 * p.nkt * a_blk;
   const int b_blk = kTN * p.row_bytes;
-  const int b_stage = 2 * p.nkt * b_blk;
+  const int b_stage = 2 * p.nkt * b_blk + kTN * 32;  // halves + norm-folding rows
   uint8_t *sA = base;
-  uint8_t *sB = base + a_bytes;
-  float *sT = (float *)(sB + (size_t)p.stages * b_stage);  // ||t||^2 of each stage's tile
-  uint64_t *bars = (uint64_t *)(sT + (size_t)p.stages * kTN);
+  uint8_t *sOnes = base + a_bytes;                   // 128 x 32 B
+  uint8_t *sB = sOnes + kQM * 32;
+  uint64_t *bars = (uint64_t *)(sB + (size_t)p.stages * b_stage);
   uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
   uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
   uint32_t *s_tmem = (uint32_t *)(afull + 7);
@@ -138,7 +149,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   if (threadIdx.x == 0) {
     for (int s = 0; s < p.stages; ++s) {
       tc::mbar_init(&full[s], 1);
-      tc::mbar_init(&empty[s], 1 + 128);  // the MMAs' commit and the epilogue's read of sT
+      tc::mbar_init(&empty[s], 1);
     }
     tc::mbar_init(afull, 1);
     tc::mbar_init(aempty, 1);
@@ -153,6 +164,8 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     tc::prefetch_tmap(&tm_ql);
     tc::prefetch_tmap(&tm_th);
     tc::prefetch_tmap(&tm_tl);
+    tc::prefetch_tmap(&tm_ones);
+    tc::prefetch_tmap(&tm_tbx);
   }
   if (warp == 1) {
     tc::tmem_alloc(s_tmem, 2 * kTN);
@@ -169,22 +182,23 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       bool ok = true;
       for (int qt = blockIdx.x; ok && qt < p.n_tiles_q; qt += gridDim.x, ++ql) {
         if (!tc::mbar_wait(aempty, (uint32_t)(ql & 1) ^ 1u, kWaitNs)) { ok = false; break; }
-        tc::mbar_expect_tx(afull, (uint32_t)a_bytes);
+        tc::mbar_expect_tx(afull, (uint32_t)(a_bytes + (ql == 0 ? kQM * 32 : 0)));
         for (int part = 0; part < 2; ++part)
           for (int kt = 0; kt < p.nkt; ++kt)
             tc::tma_load_2d(sA + (part * p.nkt + kt) * a_blk, part ? &tm_ql : &tm_qh, afull, kt * p.kt_elems,
                             qt * kQM);
+        if (ql == 0) tc::tma_load_2d(sOnes, &tm_ones, afull, 0, 0);
         for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
           const int s = it % p.stages;
           const uint32_t ph = (uint32_t)(it / p.stages) & 1u;
           if (!tc::mbar_wait(&empty[s], ph ^ 1u, kWaitNs) || *(volatile int *)s_abort) { ok = false; break; }
-          tc::mbar_expect_tx(&full[s], (uint32_t)(b_stage + kTN * 4));
+          tc::mbar_expect_tx(&full[s], (uint32_t)b_stage);
           uint8_t *dst = sB + (size_t)s * b_stage;
           for (int part = 0; part < 2; ++part)
             for (int kt = 0; kt < p.nkt; ++kt)
               tc::tma_load_2d(dst + (part * p.nkt + kt) * b_blk, part ? &tm_tl : &tm_th, &full[s],
                               kt * p.kt_elems, tt * kTN);
-          tc::bulk_load(sT + s * kTN, p.tn2 + (int64_t)tt * kTN, kTN * 4, &full[s]);
+          tc::tma_load_2d(dst + 2 * p.nkt * b_blk, &tm_tbx, &full[s], 0, tt * kTN);
         }
       }
       if (!ok) atomicExch(s_abort, 1);
@@ -196,6 +210,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     if (lane == 0) {  // ---------------- MMA issuer ----------------
       const uint32_t idesc = tc::idesc_bf16_f32(kQM, kTN);
       const uint32_t sA0 = tc::smem_u32(sA), sB0 = tc::smem_u32(sB);
+      const uint64_t ones_desc = tc::smem_desc(tc::smem_u32(sOnes), 32);
       int it = 0, ql = 0;
       bool ok = true;
       for (int qt = blockIdx.x; ok && qt < p.n_tiles_q; qt += gridDim.x, ++ql) {
@@ -211,15 +226,15 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
           tc::fence_after_sync();
           const uint32_t d_tmem = tmem + (uint32_t)(acc * kTN);
           const uint32_t b0 = sB0 + (uint32_t)(s * b_stage);
-          uint32_t accumulate = 0;
-          for (int prod = 0; prod < 3; ++prod) {  // q_h.t_h + q_h.t_l + q_l.t_h
+          // -||t||^2 / 2 first, then q_h.t_h + q_h.t_l + q_l.t_h
+          tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(2 * p.nkt * b_blk), 32), idesc, 0u);
+          for (int prod = 0; prod < 3; ++prod) {
             const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
             for (int kt = 0; kt < p.nkt; ++kt)
               for (int ks = 0; ks < p.kt_elems / 16; ++ks) {
                 const uint64_t ad = tc::smem_desc(sA0 + (uint32_t)((pa * p.nkt + kt) * a_blk + ks * 32), p.row_bytes);
                 const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((pb * p.nkt + kt) * b_blk + ks * 32), p.row_bytes);
-                tc::mma_f16(d_tmem, ad, bd, idesc, accumulate);
-                accumulate = 1;
+                tc::mma_f16(d_tmem, ad, bd, idesc, 1u);
               }
           }
           tc::mma_commit(&empty[s]);
@@ -250,9 +265,11 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       }
       const float qn = live ? p.qnrm[q] : 0.f;
       const double qn2 = live ? p.qn2[q] : 0.0;
-      const float eq = 2.1f * (p.coef_dot * 2.f * qn * tmax + 0x1p-22f * (tmax * tmax + qn * tmax) +
-                               p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
-      float thr = live ? __int_as_float(0x7f800000) : -__int_as_float(0x7f800000);
+      // |a_j - (D_j - ||q||^2)| <= e, a_j = -2 acc_j (see split.cu for the terms)
+      const float eq = 1.05f * (2.f * (p.coef_xc * qn * tmax + p.coef_cc * tmax * tmax) +
+                                p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
+      // row j can enter only if acc_j >= lo = -thr / 2 (thr = root^2 - ||q||^2 + e)
+      float lo = live ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
       const T *qr = queries + (live ? q : 0) * (int64_t)p.d;
       for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
         const int acc = it & 1;
@@ -265,22 +282,18 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         tc::fence_after_sync();
         const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(acc * kTN);
         const int64_t j0 = (int64_t)tt * kTN;
-        const float *tn = sT + (it % p.stages) * kTN;
         for (int c0 = 0; c0 < kTN; c0 += 32) {
           uint32_t v[32];
           __syncwarp();
           tc::tmem_ld32(taddr + (uint32_t)c0, v);
           tc::tmem_wait_ld();
-          // branch-free scan: which columns cannot be excluded at the chunk-start threshold
+          float mx = __uint_as_float(v[0]);
+#pragma unroll
+          for (int jj = 1; jj < 32; ++jj) mx = fmaxf(mx, __uint_as_float(v[jj]));
+          if (!(mx >= lo)) continue;  // no row of this chunk can enter the heap
           uint32_t mask = 0;
 #pragma unroll
-          for (int jj = 0; jj < 32; jj += 4) {
-            const float4 tv = *reinterpret_cast<const float4 *>(tn + c0 + jj);
-            mask |= (fmaf(-2.f, __uint_as_float(v[jj]), tv.x) <= thr ? 1u : 0u) << jj;
-            mask |= (fmaf(-2.f, __uint_as_float(v[jj + 1]), tv.y) <= thr ? 1u : 0u) << (jj + 1);
-            mask |= (fmaf(-2.f, __uint_as_float(v[jj + 2]), tv.z) <= thr ? 1u : 0u) << (jj + 2);
-            mask |= (fmaf(-2.f, __uint_as_float(v[jj + 3]), tv.w) <= thr ? 1u : 0u) << (jj + 3);
-          }
+          for (int jj = 0; jj < 32; ++jj) mask |= (__uint_as_float(v[jj]) >= lo ? 1u : 0u) << jj;
           while (mask) {  // in index order: exact reference distance and heap step
             const int jj = __ffs(mask) - 1;
             mask &= mask - 1;
@@ -296,13 +309,12 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
               hi[0] = (int32_t)j;
               if (p.k > 1)
                 for (int s = p.k / 2 - 1; s >= 0; --s) heap_sift(hd, hi, s, p.k - 1);
-              thr = knn_threshold(hd[0], qn2, eq);
+              lo = -0.5f * knn_threshold(hd[0], qn2, eq);
             }
           }
         }
         tc::fence_before_sync();
         tc::mbar_arrive(&accempty[acc]);
-        tc::mbar_arrive(&empty[it % p.stages]);
       }
       if (live && !stop)
         for (int s = 0; s < p.k; ++s) {
@@ -369,7 +381,7 @@ void dfr(T *&p) {
 int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
 
 size_t knn_smem(int nkt, int row_bytes, int stages) {
-  return 1024 + (size_t)2 * nkt * kQM * row_bytes + (size_t)stages * (2 * nkt * kTN * row_bytes + kTN * 4) +
+  return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * kTN * row_bytes + kTN * 32) +
          (size_t)(2 * stages + 8) * 8 + 16;
 }
 
@@ -393,22 +405,27 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   if (!s->num_sms) SC_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t n_pad = (n + kTN - 1) / kTN * kTN;
   if (!s->ready || s->train != train || s->n != n || s->d != d) {  // training operand, once per handle
-    dfr(s->th); dfr(s->tl); dfr(s->tn2); dfr(s->tmax);
+    dfr(s->th); dfr(s->tl); dfr(s->tbx); dfr(s->tmax); dfr(s->ones);
     SC_TRY(dal(&s->th, (size_t)n_pad * d_pad));
     SC_TRY(dal(&s->tl, (size_t)n_pad * d_pad));
-    SC_TRY(dal(&s->tn2, (size_t)n_pad));
+    SC_TRY(dal(&s->tbx, (size_t)n_pad * 16));
     SC_TRY(dal(&s->tmax, 1));
+    SC_TRY(dal(&s->ones, (size_t)kQM * 16));
+    ones_tile_kernel<<<1, kQM, 0, st>>>(s->ones);
+    SC_LAUNCHED();
+    SC_TRY(map2d(&s->tm_ones, s->ones, kQM, 16, 16, kQM, 32));
     SC_CUDA(cudaMemsetAsync(s->tmax, 0, sizeof(unsigned int), st));
     const int nb = (int)((n_pad + 7) / 8);
     if (dtype == SC_F32)
       knn_prep_kernel<float><<<nb, 256, 0, st>>>((const float *)train, n, n_pad, d, d_pad, s->th, s->tl, nullptr,
-                                                s->tn2, nullptr, s->tmax);
+                                                nullptr, nullptr, s->tmax, s->tbx);
     else
       knn_prep_kernel<double><<<nb, 256, 0, st>>>((const double *)train, n, n_pad, d, d_pad, s->th, s->tl,
-                                                 nullptr, s->tn2, nullptr, s->tmax);
+                                                 nullptr, nullptr, nullptr, s->tmax, s->tbx);
     SC_LAUNCHED();
     SC_TRY(map2d(&s->tm_th, s->th, n_pad, d_pad, kt_elems, kTN, row_bytes));
     SC_TRY(map2d(&s->tm_tl, s->tl, n_pad, d_pad, kt_elems, kTN, row_bytes));
+    SC_TRY(map2d(&s->tm_tbx, s->tbx, n_pad, 16, 16, kTN, 32));
     s->train = train;
     s->n = n;
     s->d = d;
@@ -428,10 +445,10 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   const int nbq = (int)((m_pad + 7) / 8);
   if (dtype == SC_F32)
     knn_prep_kernel<float><<<nbq, 256, 0, st>>>((const float *)queries, m, m_pad, d, d_pad, s->qh, s->ql, s->qnrm,
-                                               nullptr, s->qn2, nullptr);
+                                               nullptr, s->qn2, nullptr, nullptr);
   else
     knn_prep_kernel<double><<<nbq, 256, 0, st>>>((const double *)queries, m, m_pad, d, d_pad, s->qh, s->ql,
-                                                s->qnrm, nullptr, s->qn2, nullptr);
+                                                s->qnrm, nullptr, s->qn2, nullptr, nullptr);
   SC_LAUNCHED();
   CUtensorMap tm_qh, tm_ql;
   SC_TRY(map2d(&tm_qh, s->qh, m_pad, d_pad, kt_elems, kQM, row_bytes));
@@ -448,11 +465,12 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   p.stages = stages;
   p.k = k;
   p.d = d;
-  p.tn2 = s->tn2;
   p.qnrm = s->qnrm;
   p.qn2 = s->qn2;
   p.tmax = s->tmax;
-  p.coef_dot = (float)(3.02 * 0x1p-16 + 1.02 * 3.0 * d_pad * 0x1p-22);
+  const double nacc = 3.0 * d_pad + 3.0;
+  p.coef_xc = (float)(3.02 * 0x1p-16 + 1.02 * nacc * 0x1p-22);
+  p.coef_cc = (float)(1.01 * 0x1p-25 + 0.51 * nacc * 0x1p-22);
   p.coef_ref = (float)((d + 4) * 0x1p-52);
   p.idx_out = idx;
   p.dist_out = dist;
@@ -462,12 +480,12 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   if (dtype == SC_F32) {
     auto kern = knn_split_kernel<float>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, (const float *)train,
+    kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, (const float *)train,
                                           (const float *)queries, p);
   } else {
     auto kern = knn_split_kernel<double>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, (const double *)train,
+    kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, (const double *)train,
                                           (const double *)queries, p);
   }
   SC_LAUNCHED();
@@ -483,7 +501,7 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
 }
 
 void split_knn_free(SplitKnnState *s) {
-  dfr(s->th); dfr(s->tl); dfr(s->tn2); dfr(s->tmax);
+  dfr(s->th); dfr(s->tl); dfr(s->tbx); dfr(s->tmax); dfr(s->ones);
   dfr(s->qh); dfr(s->ql); dfr(s->qnrm); dfr(s->qn2); dfr(s->evals);
   s->ready = 0;
   s->m_cap = 0;

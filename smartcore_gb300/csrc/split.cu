@@ -36,11 +36,13 @@ __device__ __forceinline__ double sqd_term(double a, double b) {
   return __dmul_rn(r, r);
 }
 
-// Centroid operand: BF16 halves of the f64 centroids, ||c||^2 rounded to f32
-// (+inf for padding columns), and an upper bound of max_j ||c_j||.
+// Centroid operand: BF16 halves of the f64 centroids, the norm-folding row
+// (three BF16 terms of -||c||^2/2; padding rows -1e30 so they never win),
+// ||c||^2 rounded to f32, an upper bound of max_j ||c_j||, and the
+// centroids in f32, transposed, for the re-score.
 __global__ void __launch_bounds__(128)
-prep_c_kernel(const double *__restrict__ cent, int k, int d, int d_pad, int k_cols,
-              __nv_bfloat16 *__restrict__ ch, __nv_bfloat16 *__restrict__ cl,
+prep_c_kernel(const double *__restrict__ cent, int k, int d, int d_pad, int k_pad, int k_cols,
+              __nv_bfloat16 *__restrict__ ch, __nv_bfloat16 *__restrict__ cl, __nv_bfloat16 *__restrict__ cbx,
               float *__restrict__ cn2, unsigned int *__restrict__ cmax, float *__restrict__ cT) {
   __shared__ double ws[4];
   const int j = blockIdx.x;
@@ -52,7 +54,7 @@ prep_c_kernel(const double *__restrict__ cent, int k, int d, int d_pad, int k_co
       split2<double>(v, h, l);
       s = fma(v, v, s);
     }
-    if (ch) {
+    if (j < k_pad) {
       ch[(int64_t)j * d_pad + t] = h;
       cl[(int64_t)j * d_pad + t] = l;
     }
@@ -64,30 +66,43 @@ prep_c_kernel(const double *__restrict__ cent, int k, int d, int d_pad, int k_co
   __syncthreads();
   if (threadIdx.x == 0) {
     const double t = ws[0] + ws[1] + ws[2] + ws[3];
+    __nv_bfloat16 zero = __float2bfloat16_rn(0.f), h = zero, m = zero, l = zero;
     if (j < k) {
       cn2[j] = __double2float_rn(t);
       const float r = __fsqrt_ru(__double2float_ru(t));
       atomicMax(cmax, __float_as_uint(r) + 1u);
-    } else if (j < k_cols) {
+      split3(-0.5 * t, h, m, l);
+    } else {
       cn2[j] = __int_as_float(0x7f800000);  // padding: never the minimum
+      h = __float2bfloat16_rn(-1e30f);
+    }
+    if (j < k_pad) {
+      __nv_bfloat16 *row = cbx + (int64_t)j * 16;
+      row[0] = h;
+      row[1] = m;
+      row[2] = l;
+      for (int c = 3; c < 16; ++c) row[c] = zero;
     }
   }
 }
 
 // ---------------------------------------------------------------------------
 // K5: persistent tcgen05 assignment kernel.
+//   accumulator(m, j) = x_h.c_h + x_h.c_l + x_l.c_h  - ||c_j||^2 / 2
+//                     ~ x.c_j - ||c_j||^2 / 2 = (||x||^2 - D_j) / 2,
+// so the nearest centroid is the column with the largest accumulator.
 // ---------------------------------------------------------------------------
 struct AssignParams {
   int64_t n;
   int n_tiles;
   int nkt, kt_elems, row_bytes;
-  int k, k_pad, k_cols;  // k_cols = k_pad rounded up to 32 (epilogue chunking)
+  int k, k_pad, k_cols;  // k_cols = k_pad rounded up to 32 (TMEM stride)
   int stages;
   uint32_t tmem_cols;
   const float *xnrm;
-  const float *cn2;
   const unsigned int *cmax;
-  float coef_dot;   // |x.c - dot| <= coef_dot * ||x|| * ||c||
+  float coef_xc;    // accumulator error: coef_xc * ||x|| * ||c|| + coef_cc * ||c||^2
+  float coef_cc;
   float coef_ref;   // reference rounding of D: <= coef_ref * (||x|| + ||c||)^2
   int32_t *labels;
   int32_t *flag_count;
@@ -95,10 +110,10 @@ struct AssignParams {
   LloydState *st;
 };
 
-
 __global__ void __launch_bounds__(kAssignThreads, 1)
 split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
                     const __grid_constant__ CUtensorMap tm_ch, const __grid_constant__ CUtensorMap tm_cl,
+                    const __grid_constant__ CUtensorMap tm_ones, const __grid_constant__ CUtensorMap tm_cbx,
                     const AssignParams p) {
   if (p.st && p.st->done) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -107,17 +122,18 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
   const int a_stage = 2 * p.nkt * a_blk;
   const int b_blk = p.k_pad * p.row_bytes;           // one (part, k-tile) block of B
   const int b_bytes = (2 * p.nkt * b_blk + 1023) & ~1023;
+  const int x_bytes = (kBM * 32 + p.k_pad * 32 + 1023) & ~1023;  // norm-folding operands
   uint8_t *sB = base;
-  uint8_t *sA = base + b_bytes;
-  float *s_cn2 = (float *)(sA + (size_t)p.stages * a_stage);
-  uint64_t *bars = (uint64_t *)(s_cn2 + p.k_cols);
+  uint8_t *sOnes = base + b_bytes;
+  uint8_t *sBx = sOnes + kBM * 32;
+  uint8_t *sA = base + b_bytes + x_bytes;
+  uint64_t *bars = (uint64_t *)(sA + (size_t)p.stages * a_stage);
   uint64_t *full = bars, *empty = bars + p.stages, *bfull = bars + 2 * p.stages;
   uint64_t *accfull = bfull + 1, *accempty = bfull + 3, *mma_done = bfull + 5;
   uint32_t *s_tmem = (uint32_t *)(bfull + 6);
   int *s_abort = (int *)(s_tmem + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int j = threadIdx.x; j < p.k_cols; j += kAssignThreads) s_cn2[j] = p.cn2[j];
   if (threadIdx.x == 0) {
     for (int s = 0; s < p.stages; ++s) {
       tc::mbar_init(&full[s], 1);
@@ -135,6 +151,8 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
     tc::prefetch_tmap(&tm_xl);
     tc::prefetch_tmap(&tm_ch);
     tc::prefetch_tmap(&tm_cl);
+    tc::prefetch_tmap(&tm_ones);
+    tc::prefetch_tmap(&tm_cbx);
   }
   if (warp == 1) {
     tc::tmem_alloc(s_tmem, p.tmem_cols);
@@ -148,10 +166,12 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
   if (warp == 0) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
-      tc::mbar_expect_tx(bfull, (uint32_t)(2 * p.nkt * b_blk));
+      tc::mbar_expect_tx(bfull, (uint32_t)(2 * p.nkt * b_blk + kBM * 32 + p.k_pad * 32));
       for (int part = 0; part < 2; ++part)
         for (int kt = 0; kt < p.nkt; ++kt)
           tc::tma_load_2d(sB + (part * p.nkt + kt) * b_blk, part ? &tm_cl : &tm_ch, bfull, kt * p.kt_elems, 0);
+      tc::tma_load_2d(sOnes, &tm_ones, bfull, 0, 0);
+      tc::tma_load_2d(sBx, &tm_cbx, bfull, 0, 0);
       int it = 0;
       for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x, ++it) {
         const int s = it % p.stages;
@@ -177,6 +197,8 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       const uint32_t idesc = tc::idesc_bf16_f32(kBM, p.k_pad);
       bool ok = tc::mbar_wait(bfull, 0, kWaitNs);
       const uint32_t sA0 = tc::smem_u32(sA), sB0 = tc::smem_u32(sB);
+      const uint64_t ones_desc = tc::smem_desc(tc::smem_u32(sOnes), 32);
+      const uint64_t bx_desc = tc::smem_desc(tc::smem_u32(sBx), 32);
       int it = 0;
       for (int t = blockIdx.x; ok && t < p.n_tiles; t += gridDim.x, ++it) {
         const int s = it % p.stages, acc = it & 1;
@@ -189,16 +211,15 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
         tc::fence_after_sync();
         const uint32_t d_tmem = tmem + (uint32_t)(acc * p.k_cols);
         const uint32_t a0 = sA0 + (uint32_t)(s * a_stage);
-        uint32_t accumulate = 0;
-        // x_h.c_h + x_h.c_l + x_l.c_h
+        // -||c||^2 / 2 first, then x_h.c_h + x_h.c_l + x_l.c_h
+        tc::mma_f16(d_tmem, ones_desc, bx_desc, idesc, 0u);
         for (int prod = 0; prod < 3; ++prod) {
           const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
           for (int kt = 0; kt < p.nkt; ++kt)
             for (int ks = 0; ks < p.kt_elems / 16; ++ks) {
               const uint64_t ad = tc::smem_desc(a0 + (uint32_t)((pa * p.nkt + kt) * a_blk + ks * 32), p.row_bytes);
               const uint64_t bd = tc::smem_desc(sB0 + (uint32_t)((pb * p.nkt + kt) * b_blk + ks * 32), p.row_bytes);
-              tc::mma_f16(d_tmem, ad, bd, idesc, accumulate);
-              accumulate = 1;
+              tc::mma_f16(d_tmem, ad, bd, idesc, 1u);
             }
         }
         tc::mma_commit(&empty[s]);
@@ -212,17 +233,20 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
   } else {
     // ---------------- epilogue: 2 warpgroups ----------------
     // Warpgroup g handles the tiles of accumulator buffer g (every other
-    // tile); warp w reads TMEM lanes 32*(w%4).., one point per thread, all
-    // columns.  Two interleaved (best, second, argmin) trackers per thread
+    // tile); warp w reads TMEM lanes 32*(w%4).., one point per thread, the
+    // k_pad valid columns.  Four interleaved (best, second, argmax) trackers
     // keep the dependency chains short; they merge with lowest index on ties.
     const int g = (warp - 2) >> 2;
     const int q = warp & 3;
     const int row = q * 32 + lane;
     const float cmax = __uint_as_float(*p.cmax);
-    const float inf = __int_as_float(0x7f800000);
+    const float ninf = -__int_as_float(0x7f800000);
     int it = 0;
     for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x, ++it) {
       if ((it & 1) != g) continue;
+      const int64_t i = (int64_t)t * kBM + row;
+      const bool live = i < p.n;
+      const float xn = live ? __ldg(p.xnrm + i) : 0.f;  // issued before the accumulator wait
       const uint32_t aph = (uint32_t)(it >> 1) & 1u;
       const bool got = tc::mbar_wait(&accfull[g], aph, kWaitNs);
       if (!__all_sync(0xffffffffu, got) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
@@ -231,58 +255,60 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       }
       tc::fence_after_sync();
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * p.k_cols);
-      // four trackers on columns j = 4c + r (r = 0..3) for instruction-level parallelism
-      float m1[4] = {inf, inf, inf, inf}, m2[4] = {inf, inf, inf, inf};
+      float m1[4] = {ninf, ninf, ninf, ninf}, m2[4] = {ninf, ninf, ninf, ninf};
       int mi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
-      for (int c0 = 0; c0 < p.k_cols; c0 += 64) {
+      for (int c0 = 0; c0 < p.k_pad;) {
         uint32_t v[64];
-        if (c0 + 64 <= p.k_cols) {
+        int nc;
+        if (c0 + 64 <= p.k_pad) {
           tc::tmem_ld64(taddr + (uint32_t)c0, v);
+          nc = 64;
+        } else if (c0 + 32 <= p.k_pad) {
+          tc::tmem_ld32(taddr + (uint32_t)c0, *reinterpret_cast<uint32_t (*)[32]>(v));
+          nc = 32;
         } else {
-          uint32_t (&lo)[32] = *reinterpret_cast<uint32_t (*)[32]>(v);
-          tc::tmem_ld32(taddr + (uint32_t)c0, lo);
+          tc::tmem_ld16(taddr + (uint32_t)c0, *reinterpret_cast<uint32_t (*)[16]>(v));
+          nc = 16;
         }
         tc::tmem_wait_ld();
-        const int nc = p.k_cols - c0 < 64 ? 32 : 64;
 #pragma unroll
         for (int jj = 0; jj < 64; jj += 4) {
           if (jj >= nc) break;
-          const float4 cc = *reinterpret_cast<const float4 *>(s_cn2 + c0 + jj);
-          const float cv[4] = {cc.x, cc.y, cc.z, cc.w};
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
-            const float x = fmaf(-2.f, __uint_as_float(v[jj + r]), cv[r]);
-            const bool lt = x < m1[r];
-            m2[r] = lt ? m1[r] : fminf(m2[r], x);
-            mi[r] = lt ? c0 + jj + r : mi[r];
-            m1[r] = lt ? x : m1[r];
+            const float x = __uint_as_float(v[jj + r]);
+            const bool gt = x > m1[r];
+            m2[r] = gt ? m1[r] : fmaxf(m2[r], x);
+            mi[r] = gt ? c0 + jj + r : mi[r];
+            m1[r] = gt ? x : m1[r];
           }
         }
+        c0 += nc;
       }
       tc::fence_before_sync();
       tc::mbar_arrive(&accempty[g]);
-      // merge the four trackers: lowest value, lowest index on ties
+      // merge the four trackers: largest value, lowest index on ties
       float mm1 = m1[0], mm2 = m2[0];
       int a = mi[0];
 #pragma unroll
       for (int r = 1; r < 4; ++r) {
-        if (m1[r] < mm1 || (m1[r] == mm1 && mi[r] < a)) {
-          mm2 = fminf(mm1, m2[r]);
+        if (m1[r] > mm1 || (m1[r] == mm1 && mi[r] < a)) {
+          mm2 = fmaxf(mm1, m2[r]);
           mm1 = m1[r];
           a = mi[r];
         } else {
-          mm2 = fminf(mm2, m1[r]);
+          mm2 = fmaxf(mm2, m1[r]);
         }
-        mm2 = fminf(mm2, m2[r]);
+        mm2 = fmaxf(mm2, m2[r]);
       }
-      const float m1v = mm1, m2v = mm2;
-      const int64_t i = (int64_t)t * kBM + row;
-      if (i < p.n) {
-        const float xn = p.xnrm[i];
-        const float e = p.coef_dot * 2.f * xn * cmax + 0x1p-22f * (cmax * cmax + xn * cmax) +
-                        p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
+      if (live) {
+        // |acc_j - (x.c_j - ||c_j||^2/2)| <= E_acc, and D_j = ||x||^2 - 2 (x.c_j - ||c_j||^2/2)
+        // up to the reference's own rounding: the label is certain when the
+        // best and second-best D differ by more than 2 (2 E_acc + E_ref).
+        const float e_acc = p.coef_xc * xn * cmax + p.coef_cc * cmax * cmax;
+        const float e = 2.f * e_acc + p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
         p.labels[i] = a == 0x7fffffff ? 0 : a;
-        if (!(m2v - m1v > 2.1f * e)) p.flag_list[atomicAdd(p.flag_count, 1)] = (int32_t)i;
+        if (!(2.f * (mm1 - mm2) > 2.1f * e)) p.flag_list[atomicAdd(p.flag_count, 1)] = (int32_t)i;
       }
     }
   }
@@ -444,10 +470,11 @@ void dfree(T *&p) {
 // 64-byte swizzle) or multiples of 128 B (128-byte swizzle, 64-feature tiles).
 int pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
 
-size_t assign_smem(const SplitState *s, int stages, int k_pad, int k_cols) {
+size_t assign_smem(const SplitState *s, int stages, int k_pad) {
   const size_t a_stage = (size_t)2 * s->nkt * kBM * s->row_bytes;
   const size_t b_bytes = (((size_t)2 * s->nkt * k_pad * s->row_bytes) + 1023) & ~(size_t)1023;
-  return 1024 + b_bytes + (size_t)stages * a_stage + (size_t)k_cols * 4 + (size_t)(2 * stages + 6) * 8 + 16;
+  const size_t x_bytes = ((size_t)kBM * 32 + (size_t)k_pad * 32 + 1023) & ~(size_t)1023;
+  return 1024 + b_bytes + x_bytes + (size_t)stages * a_stage + (size_t)(2 * stages + 6) * 8 + 16;
 }
 
 }  // namespace
@@ -488,6 +515,10 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
   SC_LAUNCHED();
   SC_TRY(make_map(&s->tm_xh, s->xh, s->n_pad, s->d_pad, s->kt_elems, kBM, s->row_bytes));
   SC_TRY(make_map(&s->tm_xl, s->xl, s->n_pad, s->d_pad, s->kt_elems, kBM, s->row_bytes));
+  SC_TRY(dalloc(&s->ones, (size_t)kBM * 16));
+  ones_tile_kernel<<<1, kBM, 0, st>>>(s->ones);
+  SC_LAUNCHED();
+  SC_TRY(make_map(&s->tm_ones, s->ones, kBM, 16, 16, kBM, 32));
   s->ready = 1;
   return SC_OK;
 }
@@ -501,9 +532,10 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
     return SC_ERR_INVALID;
   }
   if (k_cols > s->k_alloc) {
-    dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cT);
+    dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cT); dfree(s->cbx);
     SC_TRY(dalloc(&s->ch, (size_t)k_cols * s->d_pad));
     SC_TRY(dalloc(&s->cl, (size_t)k_cols * s->d_pad));
+    SC_TRY(dalloc(&s->cbx, (size_t)k_cols * 16));
     SC_TRY(dalloc(&s->cn2, (size_t)k_cols));
     SC_TRY(dalloc(&s->cT, (size_t)k_cols * s->d_pad));
     s->k_alloc = k_cols;
@@ -512,11 +544,13 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
   if (k_pad != s->k_pad) {
     SC_TRY(make_map(&s->tm_ch, s->ch, k_pad, s->d_pad, s->kt_elems, k_pad, s->row_bytes));
     SC_TRY(make_map(&s->tm_cl, s->cl, k_pad, s->d_pad, s->kt_elems, k_pad, s->row_bytes));
+    SC_TRY(make_map(&s->tm_cbx, s->cbx, k_pad, 16, 16, k_pad, 32));
   }
   s->k = k;
   s->k_pad = k_pad;
   SC_CUDA(cudaMemsetAsync(s->cmax, 0, sizeof(unsigned int), st));
-  prep_c_kernel<<<k_cols, 128, 0, st>>>(cent, k, s->d, s->d_pad, k_cols, s->ch, s->cl, s->cn2, s->cmax, s->cT);
+  prep_c_kernel<<<k_cols, 128, 0, st>>>(cent, k, s->d, s->d_pad, k_pad, k_cols, s->ch, s->cl, s->cbx, s->cn2,
+                                        s->cmax, s->cT);
   SC_LAUNCHED();
   return SC_OK;
 }
@@ -529,8 +563,8 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   uint32_t tmem_cols = 32;
   while (tmem_cols < (uint32_t)(2 * k_cols)) tmem_cols <<= 1;
   int stages = 6;
-  while (stages > 2 && assign_smem(s, stages, s->k_pad, k_cols) > 227 * 1024) --stages;
-  const size_t smem = assign_smem(s, stages, s->k_pad, k_cols);
+  while (stages > 2 && assign_smem(s, stages, s->k_pad) > 227 * 1024) --stages;
+  const size_t smem = assign_smem(s, stages, s->k_pad);
   if (smem > 227 * 1024) {
     set_error("d=%d, k=%d exceed the split-BF16 kernel's shared memory", d, k);
     return SC_ERR_INVALID;
@@ -548,10 +582,13 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   p.stages = stages;
   p.tmem_cols = tmem_cols;
   p.xnrm = s->xnrm;
-  p.cn2 = s->cn2;
   p.cmax = s->cmax;
-  // split remainders 3.02 * 2^-16, FP32 accumulation of 3 d_pad products <= 2^-22 each
-  p.coef_dot = (float)(3.02 * 0x1p-16 + 1.02 * 3.0 * s->d_pad * 0x1p-22);
+  // |acc - (x.c - ||c||^2/2)|: split remainders 3.02 * 2^-16 ||x|| ||c||; three-term
+  // split of ||c||^2/2 (2^-24 relative); FP32 accumulation of 3 d_pad + 3 exact
+  // terms, <= 2^-22 of their absolute sum per term
+  const double nacc = 3.0 * s->d_pad + 3.0;
+  p.coef_xc = (float)(3.02 * 0x1p-16 + 1.02 * nacc * 0x1p-22);
+  p.coef_cc = (float)(1.01 * 0x1p-25 + 0.51 * nacc * 0x1p-22);
   p.coef_ref = (float)((d + 4) * 0x1p-52);
   p.labels = labels;
   p.flag_count = s->flag_count;
@@ -561,7 +598,8 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   SC_CUDA(cudaFuncSetAttribute(split_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = p.n_tiles < s->num_sms ? p.n_tiles : s->num_sms;
   if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
-  split_assign_kernel<<<grid, kAssignThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, p);
+  split_assign_kernel<<<grid, kAssignThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, s->tm_ones,
+                                                          s->tm_cbx, p);
   SC_LAUNCHED();
   if (timing) SC_CUDA(cudaEventRecord(timing[1], st));
   const int rgrid = 2 * s->num_sms;
@@ -585,7 +623,7 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
 
 void split_free(SplitState *s) {
   dfree(s->xh); dfree(s->xl); dfree(s->xnrm); dfree(s->part);
-  dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cmax);
+  dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cmax); dfree(s->cbx); dfree(s->ones);
   dfree(s->flag_count); dfree(s->flag_list); dfree(s->cT);
   s->ready = 0;
   s->k_alloc = 0;

@@ -19,6 +19,9 @@ struct SplitState {
   double *part = nullptr;                       // block partials of ||x||^2
   int k = 0, k_pad = 0, k_alloc = 0;
   __nv_bfloat16 *ch = nullptr, *cl = nullptr;  // k_pad x d_pad
+  __nv_bfloat16 *cbx = nullptr;                 // k_pad x 16: BF16 terms of -||c||^2/2
+  __nv_bfloat16 *ones = nullptr;                // 128 x 16: [1, 1, 1, 0...] rows
+  CUtensorMap tm_cbx, tm_ones;
   float *cn2 = nullptr;                         // k_pad: ||c||^2 rounded to f32 (+inf for padding)
   unsigned int *cmax = nullptr;                 // bits of an upper bound of max ||c||
   float *cT = nullptr;                          // d_pad x k_cols: centroids in f32, transposed
@@ -34,9 +37,10 @@ struct SplitKnnState {
   int64_t n = 0;
   int d = 0, num_sms = 0;
   __nv_bfloat16 *th = nullptr, *tl = nullptr;  // n_pad x d_pad training halves
-  float *tn2 = nullptr;                         // n_pad: ||t||^2 in f32 (+inf padding)
+  __nv_bfloat16 *tbx = nullptr;                 // n_pad x 16: BF16 terms of -||t||^2/2
+  __nv_bfloat16 *ones = nullptr;                // 128 x 16: [1, 1, 1, 0...] rows
   unsigned int *tmax = nullptr;                 // bits of an upper bound of max ||t||
-  CUtensorMap tm_th, tm_tl;
+  CUtensorMap tm_th, tm_tl, tm_tbx, tm_ones;
   __nv_bfloat16 *qh = nullptr, *ql = nullptr;  // query halves (per call)
   float *qnrm = nullptr;
   double *qn2 = nullptr;

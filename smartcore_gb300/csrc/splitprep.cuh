@@ -65,6 +65,23 @@ prep_x_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_pa
   }
 }
 
+// Three BF16 terms h + m + l of v (|v - (h + m + l)| <= 2^-24 |v|).
+__device__ __forceinline__ void split3(double v, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
+  h = __double2bfloat16(v);
+  const double r1 = v - (double)__bfloat162float(h);
+  m = __double2bfloat16(r1);
+  l = __double2bfloat16(r1 - (double)__bfloat162float(m));
+}
+
+// The constant A operand of the norm-folding MMA: 128 rows of 16 BF16
+// columns, [1, 1, 1, 0, ..., 0].  Paired with a B operand whose row j holds
+// the three BF16 terms of -||c_j||^2 / 2, one extra K=16 step adds
+// -||c_j||^2 / 2 to every x.c_j of the accumulator.
+__global__ void ones_tile_kernel(__nv_bfloat16 *__restrict__ ones) {
+  const int t = threadIdx.x;  // 128 x 16 elements, 16 per thread
+  for (int c = 0; c < 16; ++c) ones[t * 16 + c] = __float2bfloat16_rn(c < 3 ? 1.f : 0.f);
+}
+
 __global__ void sum_parts_kernel(const double *__restrict__ part, int nparts, double *__restrict__ out) {
   __shared__ double ws[32];
   double v = 0.0;
