@@ -7,6 +7,7 @@
 #include <float.h>
 
 #include "common.cuh"
+#include "exactsum.cuh"
 
 namespace sc {
 
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(kPPThreads)
 pp_update_kernel(const T *__restrict__ x, int64_t n, int d, const LloydState *st,
                  int32_t label_of_seed, double *__restrict__ dd,
                  int32_t *__restrict__ labels, double *__restrict__ part,
-                 int first_pass) {
+                 int first_pass, int lg_d) {
   extern __shared__ unsigned char smraw[];
   T *cen = reinterpret_cast<T *>(smraw);
   const int64_t ci = st->pp_chosen;
@@ -149,7 +150,13 @@ pp_update_kernel(const T *__restrict__ x, int64_t n, int d, const LloydState *st
   if (i < n) {
     const T *xr = x + i * (int64_t)d;
     double s = 0.0;
-    for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term(xr[j], cen[j]));
+    bool exact = false;
+    // f32 rows: the same value from an integer exact sum when no partial sum rounds
+    if constexpr (sizeof(T) == 4) exact = sqd_exact_f32(xr, cen, d, lg_d, s);
+    if (!exact) {
+      s = 0.0;
+      for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term(xr[j], cen[j]));
+    }
     double cur = first_pass ? DBL_MAX : dd[i];
     int32_t lab = first_pass ? 0 : labels[i];
     if (s < cur) { cur = s; lab = label_of_seed; }
@@ -171,10 +178,12 @@ sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
     set_error("d=%d is too large for the k-means++ kernel", d);
     return SC_ERR_INVALID;
   }
+  int lg_d = 0;
+  while ((1 << lg_d) < d) ++lg_d;
   if (dtype == SC_F32)
-    pp_update_kernel<float><<<grid, kPPThreads, smem, s>>>((const float *)x, n, d, st, label_of_seed, dd, labels, part, first_pass);
+    pp_update_kernel<float><<<grid, kPPThreads, smem, s>>>((const float *)x, n, d, st, label_of_seed, dd, labels, part, first_pass, lg_d);
   else
-    pp_update_kernel<double><<<grid, kPPThreads, smem, s>>>((const double *)x, n, d, st, label_of_seed, dd, labels, part, first_pass);
+    pp_update_kernel<double><<<grid, kPPThreads, smem, s>>>((const double *)x, n, d, st, label_of_seed, dd, labels, part, first_pass, lg_d);
   SC_LAUNCHED();
   return SC_OK;
 }

@@ -16,6 +16,7 @@
 #include <math.h>
 #include <string.h>
 
+#include "exactsum.cuh"
 #include "split.cuh"
 #include "splitprep.cuh"
 #include "tc.cuh"
@@ -89,7 +90,7 @@ struct KnnParams {
   int n_tiles_t, n_tiles_q;
   int nkt, kt_elems, row_bytes;
   int stages;
-  int k, d;
+  int k, d, lg_d;
   const float *qnrm;
   const double *qn2;
   const unsigned int *tmax;
@@ -100,8 +101,8 @@ struct KnnParams {
   int *err;
 };
 
-__device__ __forceinline__ void heap_sift(double *hd, int32_t *hi, int kk, int nn) {
-  // sift_down of heap_select.rs:71-86: node kk has children 2kk and 2kk+1
+__device__ __forceinline__ void heap_sift(double *hd, double *hD, int32_t *hi, int kk, int nn) {
+  // sift_down of heap_select.rs:71-86 (on the distances): node kk has children 2kk and 2kk+1
   while (2 * kk <= nn) {
     int j = 2 * kk;
     if (j < nn && hd[j] < hd[j + 1]) ++j;
@@ -110,6 +111,9 @@ __device__ __forceinline__ void heap_sift(double *hd, int32_t *hi, int kk, int n
     if (j == kk) break;
     hd[kk] = b;
     hd[j] = a;
+    const double t2 = hD[kk];
+    hD[kk] = hD[j];
+    hD[j] = t2;
     const int32_t t = hi[kk];
     hi[kk] = hi[j];
     hi[j] = t;
@@ -251,7 +255,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     const int q4 = warp & 3;
     const int row = q4 * 32 + lane;
     const float tmax = __uint_as_float(*p.tmax);
-    double hd[kMaxKnnK];
+    double hd[kMaxKnnK], hD[kMaxKnnK];  // heap distances and their squares
     int32_t hi[kMaxKnnK];
     unsigned long long evals = 0;
     int it = 0;
@@ -260,7 +264,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       const int64_t q = (int64_t)qt * kQM + row;
       const bool live = q < p.m;
       for (int s = 0; s < p.k; ++s) {
-        hd[s] = __longlong_as_double(0x7ff0000000000000ll);
+        hd[s] = hD[s] = __longlong_as_double(0x7ff0000000000000ll);
         hi[s] = -1;
       }
       const float qn = live ? p.qnrm[q] : 0.f;
@@ -301,15 +305,24 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
             if (j >= p.n) break;
             const T *tr = train + j * (int64_t)p.d;
             double sq = 0.0;
-            for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qr[t], tr[t]));
-            const double dist = __dsqrt_rn(sq);
+            bool exact = false;
+            if constexpr (sizeof(T) == 4) exact = sqd_exact_f32(qr, tr, p.d, p.lg_d, sq);
+            if (!exact) {
+              sq = 0.0;
+              for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qr[t], tr[t]));
+            }
             ++evals;
-            if (dist < hd[0]) {
-              hd[0] = dist;
-              hi[0] = (int32_t)j;
-              if (p.k > 1)
-                for (int s = p.k / 2 - 1; s >= 0; --s) heap_sift(hd, hi, s, p.k - 1);
-              lo = -0.5f * knn_threshold(hd[0], qn2, eq);
+            // sqrt is monotone: sq >= root^2 means sqrt(sq) >= root, no entry
+            if (sq < hD[0]) {
+              const double dist = __dsqrt_rn(sq);
+              if (dist < hd[0]) {  // the reference's test (linear_search.rs:72)
+                hd[0] = dist;
+                hD[0] = sq;
+                hi[0] = (int32_t)j;
+                if (p.k > 1)
+                  for (int s = p.k / 2 - 1; s >= 0; --s) heap_sift(hd, hD, hi, s, p.k - 1);
+                lo = -0.5f * knn_threshold(hd[0], qn2, eq);
+              }
             }
           }
         }
@@ -465,6 +478,8 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   p.stages = stages;
   p.k = k;
   p.d = d;
+  p.lg_d = 0;
+  while ((1 << p.lg_d) < d) ++p.lg_d;
   p.qnrm = s->qnrm;
   p.qn2 = s->qn2;
   p.tmax = s->tmax;

@@ -105,8 +105,7 @@ struct AssignParams {
   float coef_cc;
   float coef_ref;   // reference rounding of D: <= coef_ref * (||x|| + ||c||)^2
   int32_t *labels;
-  int32_t *flag_count;
-  int32_t *flag_list;
+  uint32_t *flag_bits;  // bit i: point i is a near tie (one word per warp and tile)
   LloydState *st;
 };
 
@@ -301,15 +300,15 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
         }
         mm2 = fmaxf(mm2, m2[r]);
       }
-      if (live) {
-        // |acc_j - (x.c_j - ||c_j||^2/2)| <= E_acc, and D_j = ||x||^2 - 2 (x.c_j - ||c_j||^2/2)
-        // up to the reference's own rounding: the label is certain when the
-        // best and second-best D differ by more than 2 (2 E_acc + E_ref).
-        const float e_acc = p.coef_xc * xn * cmax + p.coef_cc * cmax * cmax;
-        const float e = 2.f * e_acc + p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
-        p.labels[i] = a == 0x7fffffff ? 0 : a;
-        if (!(2.f * (mm1 - mm2) > 2.1f * e)) p.flag_list[atomicAdd(p.flag_count, 1)] = (int32_t)i;
-      }
+      // |acc_j - (x.c_j - ||c_j||^2/2)| <= E_acc, and D_j = ||x||^2 - 2 (x.c_j - ||c_j||^2/2)
+      // up to the reference's own rounding: the label is certain when the
+      // best and second-best D differ by more than 2 (2 E_acc + E_ref).
+      const float e_acc = p.coef_xc * xn * cmax + p.coef_cc * cmax * cmax;
+      const float e = 2.f * e_acc + p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
+      const bool flagged = live && !(2.f * (mm1 - mm2) > 2.1f * e);
+      if (live) p.labels[i] = a == 0x7fffffff ? 0 : a;
+      const uint32_t fm = __ballot_sync(0xffffffffu, flagged);
+      if (lane == 0) p.flag_bits[(int64_t)t * (kBM / 32) + q] = fm;
     }
   }
   tc::fence_before_sync();
@@ -337,17 +336,22 @@ __global__ void __launch_bounds__(32 * kRescoreWarps)
 rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, int k, int k_cols,
                const float *__restrict__ cT, const float *__restrict__ cn2,
                const unsigned int *__restrict__ cmax_bits, const float *__restrict__ xnrm,
-               const int32_t *__restrict__ flag_count, const int32_t *__restrict__ flag_list,
+               const uint32_t *__restrict__ flag_bits, int64_t nwords,
                int32_t *__restrict__ labels, LloydState *st, int stage_ct) {
   if (st && st->done) return;
   __shared__ float xs[kRescoreWarps][256];
+  __shared__ int s_any;
   extern __shared__ __align__(16) float s_ct[];  // d x k_cols when stage_ct
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t gw = (int64_t)blockIdx.x * kRescoreWarps + w;
-  const int64_t nw = (int64_t)gridDim.x * kRescoreWarps;
-  const int cnt = *flag_count;
-  if (gw == 0 && lane == 0 && st) atomicAdd((unsigned long long *)&st->rescored, (unsigned long long)cnt);
-  if ((int64_t)blockIdx.x * kRescoreWarps >= cnt) return;  // no point for this block
+  // this block's words: [w0, w1)
+  const int64_t per = (nwords + gridDim.x - 1) / gridDim.x;
+  const int64_t w0 = (int64_t)blockIdx.x * per, w1 = min(nwords, w0 + per);
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  for (int64_t q = w0 + threadIdx.x; q < w1; q += blockDim.x)
+    if (flag_bits[q]) s_any = 1;
+  __syncthreads();
+  if (!s_any) return;  // no near tie in this block's range
   if (stage_ct) {
     const int total = d * k_cols;
     for (int t = threadIdx.x; t < total; t += blockDim.x) s_ct[t] = cT[t];
@@ -355,8 +359,13 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
     cT = s_ct;
   }
   const float cmax = __uint_as_float(*cmax_bits);
-  for (int64_t f = gw; f < cnt; f += nw) {
-    const int64_t i = flag_list[f];
+  unsigned long long done_here = 0;
+  for (int64_t word = w0 + w; word < w1; word += kRescoreWarps) {
+   uint32_t bits = flag_bits[word];
+   done_here += __popc(bits);
+   while (bits) {
+    const int64_t i = word * 32 + (__ffs(bits) - 1);
+    bits &= bits - 1;
     const T *xr = x + i * (int64_t)d;
     for (int t = lane; t < d; t += 32) xs[w][t] = (float)xr[t];
     __syncwarp();
@@ -415,7 +424,9 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
     }
     if (lane == 0) labels[i] = label == 0x7fffffff ? 0 : label;
     __syncwarp();
+   }
   }
+  if (lane == 0 && done_here && st) atomicAdd((unsigned long long *)&st->rescored, done_here);
 }
 
 // ---------------------------------------------------------------------------
@@ -503,8 +514,7 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
   SC_TRY(dalloc(&s->xnrm, (size_t)s->n_pad));
   const int nb = (int)((s->n_pad + 7) / 8);
   SC_TRY(dalloc(&s->part, (size_t)nb));
-  SC_TRY(dalloc(&s->flag_count, 1));
-  SC_TRY(dalloc(&s->flag_list, (size_t)s->n_pad));
+  SC_TRY(dalloc(&s->flag_bits, (size_t)(s->n_pad / 32)));
   SC_TRY(dalloc(&s->cmax, 1));
   if (dtype == SC_F32)
     prep_x_kernel<float><<<nb, 256, 0, st>>>((const float *)x, n, s->n_pad, d, s->d_pad, s->xh, s->xl, s->xnrm, s->part);
@@ -591,10 +601,8 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   p.coef_cc = (float)(1.01 * 0x1p-25 + 0.51 * nacc * 0x1p-22);
   p.coef_ref = (float)((d + 4) * 0x1p-52);
   p.labels = labels;
-  p.flag_count = s->flag_count;
-  p.flag_list = s->flag_list;
+  p.flag_bits = s->flag_bits;
   p.st = lst;
-  SC_CUDA(cudaMemsetAsync(s->flag_count, 0, sizeof(int32_t), st));
   SC_CUDA(cudaFuncSetAttribute(split_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid = p.n_tiles < s->num_sms ? p.n_tiles : s->num_sms;
   if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
@@ -610,12 +618,12 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
     auto kern = rescore_kernel<float>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
     kern<<<rgrid, 32 * kRescoreWarps, rsmem, st>>>((const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
-                                                   s->xnrm, s->flag_count, s->flag_list, labels, lst, stage);
+                                                   s->xnrm, s->flag_bits, s->n_pad / 32, labels, lst, stage);
   } else {
     auto kern = rescore_kernel<double>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
     kern<<<rgrid, 32 * kRescoreWarps, rsmem, st>>>((const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
-                                                   s->xnrm, s->flag_count, s->flag_list, labels, lst, stage);
+                                                   s->xnrm, s->flag_bits, s->n_pad / 32, labels, lst, stage);
   }
   SC_LAUNCHED();
   return SC_OK;
@@ -624,7 +632,7 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
 void split_free(SplitState *s) {
   dfree(s->xh); dfree(s->xl); dfree(s->xnrm); dfree(s->part);
   dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cmax); dfree(s->cbx); dfree(s->ones);
-  dfree(s->flag_count); dfree(s->flag_list); dfree(s->cT);
+  dfree(s->flag_bits); dfree(s->cT);
   s->ready = 0;
   s->k_alloc = 0;
   s->k_pad = 0;

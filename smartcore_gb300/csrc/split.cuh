@@ -25,8 +25,7 @@ struct SplitState {
   float *cn2 = nullptr;                         // k_pad: ||c||^2 rounded to f32 (+inf for padding)
   unsigned int *cmax = nullptr;                 // bits of an upper bound of max ||c||
   float *cT = nullptr;                          // d_pad x k_cols: centroids in f32, transposed
-  int32_t *flag_count = nullptr;                // near-tie points of the last assignment
-  int32_t *flag_list = nullptr;                 // n entries
+  uint32_t *flag_bits = nullptr;                // n_pad / 32 words: near ties of the last assignment
   CUtensorMap tm_xh, tm_xl, tm_ch, tm_cl;
   int num_sms = 0;
 };

@@ -121,15 +121,15 @@ sc_status launch_update_fixed(int dtype, const void *x, int64_t n, int d,
 // ---------------------------------------------------------------------------
 // v * 2^scale rounded to the nearest integer (ties to even), integer ALU only
 // (a 64-bit float-to-int conversion would run on the FP64 pipe).  The scale
-// guarantees |v| * 2^scale < 2^62, so left shifts stay within 62 bits.
-__device__ __forceinline__ long long to_fixed64(float v, int scale) {
-  const uint32_t b = __float_as_uint(v);
+// guarantees |v| * 2^scale < 2^62.  Normal values whose scaled mantissa is an
+// integer (the common case) take the short path.
+__device__ __noinline__ long long to_fixed64_slow(uint32_t b, int scale) {
   const int e = (int)((b >> 23) & 0xffu);
   const uint32_t m = (b & 0x7fffffu) | (e ? 0x800000u : 0u);
   const int sh = (e ? e : 1) - 150 + scale;
   long long mag;
   if (sh >= 0) {
-    mag = (long long)m << sh;
+    mag = (long long)((unsigned long long)m << sh);
   } else if (sh > -25) {
     const int r = -sh;
     const uint32_t q = m >> r, rem = m & ((1u << r) - 1u), half = 1u << (r - 1);
@@ -138,6 +138,18 @@ __device__ __forceinline__ long long to_fixed64(float v, int scale) {
     mag = 0;  // |v| * 2^scale < 2^-1
   }
   return (b >> 31) ? -mag : mag;
+}
+
+__device__ __forceinline__ void add_fixed64(long long &acc, float v, int scale) {
+  const uint32_t b = __float_as_uint(v);
+  if ((b << 1) == 0u) return;  // +-0
+  const int sh = (int)((b >> 23) & 0xffu) - 150 + scale;
+  if ((b & 0x7f800000u) == 0u || sh < 0) {  // subnormal or below the integer grid: rare
+    acc += to_fixed64_slow(b, scale);
+    return;
+  }
+  const long long mag = (long long)((unsigned long long)((b & 0x7fffffu) | 0x800000u) << sh);
+  acc += (b >> 31) ? -mag : mag;
 }
 
 template <typename T, int MAXJ>
@@ -200,7 +212,7 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
 #pragma unroll
       for (int r = 0; r < kRows; ++r)
 #pragma unroll
-        for (int q = 0; q < MAXJ; ++q) acc[q] += to_fixed64(v[r][q], scale);
+        for (int q = 0; q < MAXJ; ++q) add_fixed64(acc[q], v[r][q], scale);
     }
     long long *pc = part + ((size_t)blockIdx.x * k + c) * d;
 #pragma unroll
