@@ -55,10 +55,11 @@ struct Acc128 {
 constexpr int kMaxKnnK = 64;  // largest k served by the kNN kernels
 
 // Buffers of the centroid-sum step.  mode 0: one 128-bit fixed-point
-// accumulator per (cluster, feature) updated with global atomics.  mode 1:
-// each CTA accumulates its contiguous chunk of points in shared memory as
-// int64 fixed point and writes one partial per CTA; the finalize step adds
-// the partials exactly in 128 bits.  Both are order independent.
+// accumulator per (cluster, feature) updated with global atomics.  modes 1
+// and 2: each CTA accumulates its contiguous chunk of points as int64 fixed
+// point (1: label-sorted gather, 2: in-order streaming through shared
+// memory) and writes one partial per CTA; the finalize step adds the
+// partials exactly in 128 bits.  All are order independent.
 struct UpdateBuf {
   int mode = 0;
   int grid = 0;      // mode 1: number of CTAs (partials)
@@ -113,7 +114,7 @@ sc_status launch_finalize_scalar(const double *part, int nparts,
 // Chooses the mode for (n, d, k) and allocates; absmax = max |x|.
 sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms);
 // Number of distortion terms launch_finalize writes (k, or k*d).
-inline int64_t update_nterms(const UpdateBuf *u, int k, int d) { return u->mode == 1 ? (int64_t)k * d : k; }
+inline int64_t update_nterms(const UpdateBuf *u, int k, int d) { return u->mode != 0 ? (int64_t)k * d : k; }
 void update_free(UpdateBuf *u);
 sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n, int d,
                         const int32_t *labels, int k, const LloydState *st, cudaStream_t s);

@@ -257,10 +257,13 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       float m1[4] = {ninf, ninf, ninf, ninf}, m2[4] = {ninf, ninf, ninf, ninf};
       int mi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
       for (int c0 = 0; c0 < p.k_pad;) {
-        uint32_t v[64];
+        uint32_t v[128];
         int nc;
-        if (c0 + 64 <= p.k_pad) {
-          tc::tmem_ld64(taddr + (uint32_t)c0, v);
+        if (c0 + 128 <= p.k_pad) {
+          tc::tmem_ld128(taddr + (uint32_t)c0, v);
+          nc = 128;
+        } else if (c0 + 64 <= p.k_pad) {
+          tc::tmem_ld64(taddr + (uint32_t)c0, *reinterpret_cast<uint32_t (*)[64]>(v));
           nc = 64;
         } else if (c0 + 32 <= p.k_pad) {
           tc::tmem_ld32(taddr + (uint32_t)c0, *reinterpret_cast<uint32_t (*)[32]>(v));
@@ -271,7 +274,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
         }
         tc::tmem_wait_ld();
 #pragma unroll
-        for (int jj = 0; jj < 64; jj += 4) {
+        for (int jj = 0; jj < 128; jj += 4) {
           if (jj >= nc) break;
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
