@@ -55,11 +55,10 @@ struct Acc128 {
 constexpr int kMaxKnnK = 64;  // largest k served by the kNN kernels
 
 // Buffers of the centroid-sum step.  mode 0: one 128-bit fixed-point
-// accumulator per (cluster, feature) updated with global atomics.  modes 1
-// and 2: each CTA accumulates its contiguous chunk of points as int64 fixed
-// point (1: label-sorted gather, 2: in-order streaming through shared
-// memory) and writes one partial per CTA; the finalize step adds the
-// partials exactly in 128 bits.  All are order independent.
+// accumulator per (cluster, feature) updated with global atomics.  mode 1:
+// each CTA sorts its contiguous chunk of points by label and sums each
+// cluster's rows as int64 fixed point, one partial per CTA; the finalize step
+// adds the partials exactly in 128 bits.  Both are order independent.
 struct UpdateBuf {
   int mode = 0;
   int grid = 0;      // mode 1: number of CTAs (partials)

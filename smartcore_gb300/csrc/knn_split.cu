@@ -144,7 +144,8 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   uint8_t *sA = base;
   uint8_t *sOnes = base + a_bytes;                   // 128 x 32 B
   uint8_t *sB = sOnes + kQM * 32;
-  uint64_t *bars = (uint64_t *)(sB + (size_t)p.stages * b_stage);
+  double *sD = (double *)(sB + (size_t)p.stages * b_stage);  // 4 warps x 32 x 32 exact distances
+  uint64_t *bars = (uint64_t *)(sD + 4 * 32 * 32);
   uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
   uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
   uint32_t *s_tmem = (uint32_t *)(afull + 7);
@@ -274,7 +275,6 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
                                 p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
       // row j can enter only if acc_j >= lo = -thr / 2 (thr = root^2 - ||q||^2 + e)
       float lo = live ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
-      const T *qr = queries + (live ? q : 0) * (int64_t)p.d;
       for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
         const int acc = it & 1;
         const bool got = tc::mbar_wait(&accfull[acc], (uint32_t)(it >> 1) & 1u, kWaitNs);
@@ -294,24 +294,60 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
           float mx = __uint_as_float(v[0]);
 #pragma unroll
           for (int jj = 1; jj < 32; ++jj) mx = fmaxf(mx, __uint_as_float(v[jj]));
-          if (!(mx >= lo)) continue;  // no row of this chunk can enter the heap
+          if (!__any_sync(0xffffffffu, mx >= lo)) continue;  // no row of this chunk can enter any heap
           uint32_t mask = 0;
 #pragma unroll
           for (int jj = 0; jj < 32; ++jj) mask |= (__uint_as_float(v[jj]) >= lo ? 1u : 0u) << jj;
-          while (mask) {  // in index order: exact reference distance and heap step
+          // The exact distances of all the warp's candidates in this chunk are
+          // computed lane-parallel: candidate c (in lane-major, bit order) goes
+          // to lane c % 32; lane L's own candidates start at pref_L.
+          const uint32_t cnt = __popc(mask);
+          const uint32_t total = __reduce_add_sync(0xffffffffu, cnt);
+          uint32_t incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const uint32_t pref = incl - cnt;
+          double *myD = sD + (q4 * 32) * 32;
+          for (uint32_t base_c = 0; base_c < total; base_c += 32) {
+            const uint32_t c = base_c + (uint32_t)lane;
+            int owner = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+              const int cand = owner + step;
+              const uint32_t pc = __shfl_sync(0xffffffffu, pref, cand & 31);
+              if (cand < 32 && pc <= c) owner = cand;
+            }
+            const uint32_t om = __shfl_sync(0xffffffffu, mask, owner);
+            const uint32_t op = __shfl_sync(0xffffffffu, pref, owner);
+            if (c < total) {
+              const int bit = (int)__fns(om, 0u, (int)(c - op) + 1);
+              const int64_t j = j0 + c0 + bit;
+              double sq = __longlong_as_double(0x7ff0000000000000ll);
+              const int64_t qo = (int64_t)qt * kQM + q4 * 32 + owner;
+              if (j < p.n && qo < p.m) {
+                const T *tr = train + j * (int64_t)p.d;
+                const T *qrow = queries + qo * (int64_t)p.d;
+                bool exact = false;
+                if constexpr (sizeof(T) == 4) exact = sqd_exact_f32(qrow, tr, p.d, p.lg_d, sq);
+                if (!exact) {
+                  sq = 0.0;
+                  for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qrow[t], tr[t]));
+                }
+              }
+              myD[owner * 32 + bit] = sq;
+            }
+          }
+          evals += cnt;
+          __syncwarp();
+          while (mask) {  // in index order: the reference's heap step
             const int jj = __ffs(mask) - 1;
             mask &= mask - 1;
             const int64_t j = j0 + c0 + jj;
             if (j >= p.n) break;
-            const T *tr = train + j * (int64_t)p.d;
-            double sq = 0.0;
-            bool exact = false;
-            if constexpr (sizeof(T) == 4) exact = sqd_exact_f32(qr, tr, p.d, p.lg_d, sq);
-            if (!exact) {
-              sq = 0.0;
-              for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qr[t], tr[t]));
-            }
-            ++evals;
+            const double sq = myD[lane * 32 + jj];
             // sqrt is monotone: sq >= root^2 means sqrt(sq) >= root, no entry
             if (sq < hD[0]) {
               const double dist = __dsqrt_rn(sq);
@@ -325,6 +361,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
               }
             }
           }
+          __syncwarp();
         }
         tc::fence_before_sync();
         tc::mbar_arrive(&accempty[acc]);
@@ -395,7 +432,7 @@ int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; 
 
 size_t knn_smem(int nkt, int row_bytes, int stages) {
   return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * kTN * row_bytes + kTN * 32) +
-         (size_t)(2 * stages + 8) * 8 + 16;
+         4 * 32 * 32 * 8 + (size_t)(2 * stages + 8) * 8 + 16;
 }
 
 }  // namespace

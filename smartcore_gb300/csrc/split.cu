@@ -24,7 +24,7 @@ namespace sc {
 namespace {
 
 constexpr int kBM = 128;           // points per tile (UMMA M)
-constexpr int kEpiWarps = 8;       // two warpgroups, one per TMEM accumulator buffer
+constexpr int kEpiWarps = 16;      // 2 accumulator buffers x 2 column halves x 4 lane quarters
 constexpr int kEpiThreads = 32 * kEpiWarps;
 constexpr int kAssignThreads = 64 + kEpiThreads;  // warp 0 TMA, warp 1 MMA, then epilogue
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on every barrier wait
@@ -126,7 +126,8 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
   uint8_t *sOnes = base + b_bytes;
   uint8_t *sBx = sOnes + kBM * 32;
   uint8_t *sA = base + b_bytes + x_bytes;
-  uint64_t *bars = (uint64_t *)(sA + (size_t)p.stages * a_stage);
+  float4 *s_xch = (float4 *)(sA + (size_t)p.stages * a_stage);  // [2 buffers][2 accumulators][128 rows]
+  uint64_t *bars = (uint64_t *)(s_xch + 4 * kBM);
   uint64_t *full = bars, *empty = bars + p.stages, *bfull = bars + 2 * p.stages;
   uint64_t *accfull = bfull + 1, *accempty = bfull + 3, *mma_done = bfull + 5;
   uint32_t *s_tmem = (uint32_t *)(bfull + 6);
@@ -142,7 +143,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
     tc::mbar_init(mma_done, 1);
     for (int a = 0; a < 2; ++a) {
       tc::mbar_init(&accfull[a], 1);
-      tc::mbar_init(&accempty[a], kEpiThreads / 2);
+      tc::mbar_init(&accempty[a], kEpiThreads / 2);  // both column halves of the buffer
     }
     *s_abort = 0;
     tc::fence_mbar_init();
@@ -230,14 +231,18 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       tc::mbar_wait(mma_done, 0, kWaitNs);
     }
   } else {
-    // ---------------- epilogue: 2 warpgroups ----------------
-    // Warpgroup g handles the tiles of accumulator buffer g (every other
-    // tile); warp w reads TMEM lanes 32*(w%4).., one point per thread, the
-    // k_pad valid columns.  Four interleaved (best, second, argmax) trackers
-    // keep the dependency chains short; they merge with lowest index on ties.
-    const int g = (warp - 2) >> 2;
-    const int q = warp & 3;
+    // ---------------- epilogue: 4 warpgroups ----------------
+    // Warpgroup (g, h) handles the tiles of accumulator buffer g (every
+    // other tile) and the column half h; warp w reads TMEM lanes 32*(w%4)..,
+    // one point per thread.  Four interleaved (best, second, argmax) trackers
+    // per thread; the two halves of a row meet in shared memory behind a
+    // 64-thread named barrier, merged with the lowest index winning ties.
+    const int ew = warp - 2;
+    const int g = ew >> 3, h = (ew >> 2) & 1, q = warp & 3;
     const int row = q * 32 + lane;
+    const uint32_t bar_id = 1u + (uint32_t)(g * 4 + q);
+    const int split = ((p.k_pad / 2) + 15) & ~15;
+    const int c_lo = h ? split : 0, c_hi = h ? p.k_pad : split;
     const float cmax = __uint_as_float(*p.cmax);
     const float ninf = -__int_as_float(0x7f800000);
     int it = 0;
@@ -245,10 +250,10 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       if ((it & 1) != g) continue;
       const int64_t i = (int64_t)t * kBM + row;
       const bool live = i < p.n;
-      const float xn = live ? __ldg(p.xnrm + i) : 0.f;  // issued before the accumulator wait
+      const float xn = (h == 0 && live) ? __ldg(p.xnrm + i) : 0.f;
       const uint32_t aph = (uint32_t)(it >> 1) & 1u;
       const bool got = tc::mbar_wait(&accfull[g], aph, kWaitNs);
-      if (!__all_sync(0xffffffffu, got) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
+      if (tc::bar_red_or(!got || *(volatile int *)s_abort != 0, bar_id, 64)) {  // uniform over the pair
         atomicExch(s_abort, 1);
         break;
       }
@@ -256,16 +261,13 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * p.k_cols);
       float m1[4] = {ninf, ninf, ninf, ninf}, m2[4] = {ninf, ninf, ninf, ninf};
       int mi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
-      for (int c0 = 0; c0 < p.k_pad;) {
-        uint32_t v[128];
+      for (int c0 = c_lo; c0 < c_hi;) {
+        uint32_t v[64];
         int nc;
-        if (c0 + 128 <= p.k_pad) {
-          tc::tmem_ld128(taddr + (uint32_t)c0, v);
-          nc = 128;
-        } else if (c0 + 64 <= p.k_pad) {
-          tc::tmem_ld64(taddr + (uint32_t)c0, *reinterpret_cast<uint32_t (*)[64]>(v));
+        if (c0 + 64 <= c_hi) {
+          tc::tmem_ld64(taddr + (uint32_t)c0, v);
           nc = 64;
-        } else if (c0 + 32 <= p.k_pad) {
+        } else if (c0 + 32 <= c_hi) {
           tc::tmem_ld32(taddr + (uint32_t)c0, *reinterpret_cast<uint32_t (*)[32]>(v));
           nc = 32;
         } else {
@@ -274,7 +276,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
         }
         tc::tmem_wait_ld();
 #pragma unroll
-        for (int jj = 0; jj < 128; jj += 4) {
+        for (int jj = 0; jj < 64; jj += 4) {
           if (jj >= nc) break;
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
@@ -302,6 +304,22 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
           mm2 = fmaxf(mm2, m1[r]);
         }
         mm2 = fmaxf(mm2, m2[r]);
+      }
+      float4 *slot = s_xch + (((it >> 1) & 1) * 2 + g) * kBM + row;
+      if (h == 1) *slot = make_float4(mm1, mm2, __int_as_float(a), 0.f);
+      tc::bar_sync(bar_id, 64);
+      if (h == 1) continue;
+      {  // the second half of the row (higher column indices)
+        const float4 o = *slot;
+        const int oa = __float_as_int(o.z);
+        if (o.x > mm1 || (o.x == mm1 && oa < a)) {
+          mm2 = fmaxf(mm1, o.y);
+          mm1 = o.x;
+          a = oa;
+        } else {
+          mm2 = fmaxf(mm2, o.x);
+        }
+        mm2 = fmaxf(mm2, o.y);
       }
       // |acc_j - (x.c_j - ||c_j||^2/2)| <= E_acc, and D_j = ||x||^2 - 2 (x.c_j - ||c_j||^2/2)
       // up to the reference's own rounding: the label is certain when the
@@ -488,7 +506,7 @@ size_t assign_smem(const SplitState *s, int stages, int k_pad) {
   const size_t a_stage = (size_t)2 * s->nkt * kBM * s->row_bytes;
   const size_t b_bytes = (((size_t)2 * s->nkt * k_pad * s->row_bytes) + 1023) & ~(size_t)1023;
   const size_t x_bytes = ((size_t)kBM * 32 + (size_t)k_pad * 32 + 1023) & ~(size_t)1023;
-  return 1024 + b_bytes + x_bytes + (size_t)stages * a_stage + (size_t)(2 * stages + 6) * 8 + 16;
+  return 1024 + b_bytes + x_bytes + (size_t)stages * a_stage + 4 * kBM * 16 + (size_t)(2 * stages + 6) * 8 + 16;
 }
 
 }  // namespace

@@ -223,64 +223,6 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
   }
 }
 
-// ---------------------------------------------------------------------------
-// K2, streaming form: each CTA streams its contiguous chunk of rows through
-// shared memory in order (coalesced, no gather), 256 rows at a time; warp w
-// owns the clusters c with c % 32 == w and adds their rows into int64
-// fixed-point accumulators in shared memory (owner-exclusive: no atomics).
-// Partial sums per (CTA, cluster, feature) as in the sorted form.
-// ---------------------------------------------------------------------------
-constexpr int kStreamRows = 256;
-
-template <int D4>  // d = 4 * D4 (float4 rows)
-__global__ void __launch_bounds__(1024, 1)
-update_stream_kernel(const float *__restrict__ x, int64_t n, const int32_t *__restrict__ labels, int k,
-                     long long *__restrict__ part, unsigned int *__restrict__ cpart, int scale,
-                     const LloydState *st) {
-  if (st && st->done) return;
-  constexpr int d = 4 * D4;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  long long *sacc = reinterpret_cast<long long *>(smraw);            // k x d
-  unsigned int *scnt = reinterpret_cast<unsigned int *>(sacc + (size_t)k * d);  // k
-  float4 *sx = reinterpret_cast<float4 *>(scnt + ((k + 3) & ~3));     // kStreamRows x D4
-  int *slab = reinterpret_cast<int *>(sx + kStreamRows * D4);         // kStreamRows
-  for (int t = threadIdx.x; t < k * d; t += blockDim.x) sacc[t] = 0;
-  for (int t = threadIdx.x; t < k; t += blockDim.x) scnt[t] = 0u;
-  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-  const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const float4 *x4 = reinterpret_cast<const float4 *>(x);
-  for (int64_t r0 = i0; r0 < i1; r0 += kStreamRows) {
-    const int rows = (int)min((int64_t)kStreamRows, i1 - r0);
-    __syncthreads();  // previous block of rows consumed
-    for (int t = threadIdx.x; t < rows * D4; t += blockDim.x) sx[t] = __ldg(x4 + r0 * D4 + t);
-    for (int t = threadIdx.x; t < rows; t += blockDim.x) slab[t] = labels[r0 + t];
-    __syncthreads();
-    for (int b = 0; b < rows; b += 32) {
-      const int lab = b + lane < rows ? slab[b + lane] : -1;
-      uint32_t mine = __ballot_sync(0xffffffffu, lab >= 0 && (lab & 31) == w);
-      while (mine) {
-        const int r = b + __ffs(mine) - 1;
-        mine &= mine - 1;
-        const int c = slab[r];
-        const float *xr = reinterpret_cast<const float *>(sx + r * D4);
-        long long *ac = sacc + (size_t)c * d;
-        for (int j = lane; j < d; j += 32) {
-          long long a = ac[j];
-          add_fixed64(a, xr[j], scale);
-          ac[j] = a;
-        }
-        if (lane == 0) scnt[c] += 1u;
-      }
-    }
-  }
-  __syncthreads();
-  long long *pb = part + (size_t)blockIdx.x * k * d;
-  for (int t = threadIdx.x; t < k * d; t += blockDim.x) pb[t] = sacc[t];
-  unsigned int *cb = cpart + (size_t)blockIdx.x * k;
-  for (int t = threadIdx.x; t < k; t += blockDim.x) cb[t] = scnt[t];
-}
-
 // New centroids from the per-CTA partials.  A block handles 32 (cluster,
 // feature) elements with 8 threads each; thread g adds the partials b = g
 // (mod 8) exactly in 128 bits, the 8 sums meet in shared memory.  Also the
@@ -507,21 +449,6 @@ sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double 
   }
   const size_t smem = (size_t)(3 * k + 1 + chunk) * 4;
   const size_t part_bytes = (size_t)grid * k * d * sizeof(long long);
-  const size_t stream_smem = (size_t)k * d * 8 + (size_t)((k + 3) & ~3) * 4 + (size_t)kStreamRows * (d * 4 + 4);
-  const bool stream_d = d % 4 == 0 && (d <= 64 || d == 96 || d == 128);
-  if (dtype == SC_F32 && stream_d && stream_smem <= 220 * 1024 && n > 0) {
-    u->mode = 2;
-    u->grid = num_sms;
-    u->threads = 1024;
-    u->smem = stream_smem;
-    const int64_t ch = (n + u->grid - 1) / u->grid;
-    u->scale = 62 - e - ceil_log2(ch + 1);
-    if (u->scale > 160) u->scale = 160;
-    if (cudaMalloc((void **)&u->part, (size_t)u->grid * k * d * sizeof(long long)) != cudaSuccess ||
-        cudaMalloc((void **)&u->cpart, (size_t)u->grid * k * sizeof(unsigned int)) != cudaSuccess)
-      return cuda_fail(cudaErrorMemoryAllocation, "update partials");
-    return SC_OK;
-  }
   if (dtype == SC_F32 && d <= 256 && smem <= 200 * 1024 && part_bytes <= ((size_t)512 << 20) && n > 0) {
     u->mode = 1;
     u->grid = grid;
@@ -571,29 +498,6 @@ sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n,
     return SC_ERR_INTERNAL;
   }
   const float *xf = (const float *)x;
-  if (u->mode == 2) {
-    const void *kern = nullptr;
-    switch (d / 4) {
-#define SC_STREAM_CASE(D4)                                                                  \
-  case D4:                                                                                 \
-    kern = (const void *)update_stream_kernel<D4>;                                         \
-    SC_CUDA(cudaFuncSetAttribute(update_stream_kernel<D4>,                                 \
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem)); \
-    update_stream_kernel<D4><<<u->grid, u->threads, u->smem, s>>>(xf, n, labels, k, u->part, u->cpart, \
-                                                                 u->scale, st);           \
-    break;
-      SC_STREAM_CASE(1) SC_STREAM_CASE(2) SC_STREAM_CASE(3) SC_STREAM_CASE(4) SC_STREAM_CASE(5) SC_STREAM_CASE(6)
-      SC_STREAM_CASE(7) SC_STREAM_CASE(8) SC_STREAM_CASE(9) SC_STREAM_CASE(10) SC_STREAM_CASE(11) SC_STREAM_CASE(12)
-      SC_STREAM_CASE(13) SC_STREAM_CASE(14) SC_STREAM_CASE(15) SC_STREAM_CASE(16) SC_STREAM_CASE(24) SC_STREAM_CASE(32)
-#undef SC_STREAM_CASE
-      default:
-        break;
-    }
-    if (kern) {
-      SC_LAUNCHED();
-      return SC_OK;
-    }
-  }
   if (d <= 32) return launch_sorted<1>(u, xf, n, d, labels, k, st, s);
   if (d <= 64) return launch_sorted<2>(u, xf, n, d, labels, k, st, s);
   if (d <= 128) return launch_sorted<4>(u, xf, n, d, labels, k, st, s);
