@@ -29,6 +29,8 @@ constexpr int kQM = 128;   // queries per tile (UMMA M)
 constexpr int kTN = 256;   // training rows per tile (UMMA N)
 constexpr int kKnnThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr uint64_t kWaitNs = 2000000000ull;
+constexpr int kQueue = 2048;    // per-warp ring of pending candidates (owner lane << 27 | row)
+constexpr int kRowBits = 27;    // training rows per handle < 2^27
 
 // One term of Euclidian::squared_distance (src/metrics/distance/
 // euclidian.rs:56-62): r = a - b and r * r in the element type, then to_f64.
@@ -144,8 +146,8 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   uint8_t *sA = base;
   uint8_t *sOnes = base + a_bytes;                   // 128 x 32 B
   uint8_t *sB = sOnes + kQM * 32;
-  double *sD = (double *)(sB + (size_t)p.stages * b_stage);  // 4 warps x 32 x 32 exact distances
-  uint64_t *bars = (uint64_t *)(sD + 4 * 32 * 32);
+  uint32_t *sQ = (uint32_t *)(sB + (size_t)p.stages * b_stage);  // 4 warps x kQueue candidate entries
+  uint64_t *bars = (uint64_t *)(sQ + 4 * kQueue);
   uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
   uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
   uint32_t *s_tmem = (uint32_t *)(afull + 7);
@@ -253,9 +255,15 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     }
   } else {
     // ---------------- epilogue: one query per thread ----------------
+    // Candidate rows (those a certified bound cannot exclude) are appended,
+    // per query in index order, to a per-warp queue; whenever 32 are pending
+    // the warp computes their exact reference distances lane-parallel and each
+    // owner replays its heap steps in order.  Deferring only makes the filter
+    // threshold staler, i.e. more conservative.
     const int q4 = warp & 3;
     const int row = q4 * 32 + lane;
     const float tmax = __uint_as_float(*p.tmax);
+    uint32_t *Q = sQ + q4 * kQueue;
     double hd[kMaxKnnK], hD[kMaxKnnK];  // heap distances and their squares
     int32_t hi[kMaxKnnK];
     unsigned long long evals = 0;
@@ -275,6 +283,45 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
                                 p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
       // row j can enter only if acc_j >= lo = -thr / 2 (thr = root^2 - ||q||^2 + e)
       float lo = live ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
+      uint32_t qhead = 0, qtail = 0;  // warp-uniform queue cursors
+      const int64_t qbase = (int64_t)qt * kQM + q4 * 32;
+      // one round: exact distances of up to 32 queued entries, then the owners' heap steps
+      auto round = [&](uint32_t cnt) {
+        const uint32_t e = (uint32_t)lane < cnt ? Q[(qhead + lane) & (kQueue - 1)] : 0u;
+        const int owner = (int)(e >> kRowBits);
+        const int64_t j = (int64_t)(e & ((1u << kRowBits) - 1u));
+        double sq = __longlong_as_double(0x7ff0000000000000ll);
+        if ((uint32_t)lane < cnt && qbase + owner < p.m) {
+          const T *tr = train + j * (int64_t)p.d;
+          const T *qrow = queries + (qbase + owner) * (int64_t)p.d;
+          bool exact = false;
+          if constexpr (sizeof(T) == 4) exact = sqd_exact_f32(qrow, tr, p.d, p.lg_d, sq);
+          if (!exact) {
+            sq = 0.0;
+            for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qrow[t], tr[t]));
+          }
+        }
+        for (uint32_t r = 0; r < cnt; ++r) {  // queue order = index order per owner
+          const int o = __shfl_sync(0xffffffffu, owner, (int)r);
+          const double sr = __shfl_sync(0xffffffffu, sq, (int)r);
+          const int jr = __shfl_sync(0xffffffffu, (int)j, (int)r);
+          // sqrt is monotone: sq >= root^2 means sqrt(sq) >= root, no entry
+          if (lane == o && sr < hD[0]) {
+            const double dist = __dsqrt_rn(sr);
+            if (dist < hd[0]) {  // the reference's test (linear_search.rs:72)
+              hd[0] = dist;
+              hD[0] = sr;
+              hi[0] = jr;
+              if (p.k > 1)
+                for (int s2 = p.k / 2 - 1; s2 >= 0; --s2) heap_sift(hd, hD, hi, s2, p.k - 1);
+              lo = -0.5f * knn_threshold(hd[0], qn2, eq);
+            }
+          }
+        }
+        qhead += cnt;
+        evals += (uint32_t)lane < cnt ? 1u : 0u;
+        __syncwarp();
+      };
       for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
         const int acc = it & 1;
         const bool got = tc::mbar_wait(&accfull[acc], (uint32_t)(it >> 1) & 1u, kWaitNs);
@@ -298,9 +345,8 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
           uint32_t mask = 0;
 #pragma unroll
           for (int jj = 0; jj < 32; ++jj) mask |= (__uint_as_float(v[jj]) >= lo ? 1u : 0u) << jj;
-          // The exact distances of all the warp's candidates in this chunk are
-          // computed lane-parallel: candidate c (in lane-major, bit order) goes
-          // to lane c % 32; lane L's own candidates start at pref_L.
+          const int64_t rem = p.n - (j0 + c0);  // rows past the end of the training set
+          if (rem < 32) mask &= rem <= 0 ? 0u : ((1u << rem) - 1u);
           const uint32_t cnt = __popc(mask);
           const uint32_t total = __reduce_add_sync(0xffffffffu, cnt);
           uint32_t incl = cnt;
@@ -309,63 +355,17 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
             const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += y;
           }
-          const uint32_t pref = incl - cnt;
-          double *myD = sD + (q4 * 32) * 32;
-          for (uint32_t base_c = 0; base_c < total; base_c += 32) {
-            const uint32_t c = base_c + (uint32_t)lane;
-            int owner = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-              const int cand = owner + step;
-              const uint32_t pc = __shfl_sync(0xffffffffu, pref, cand & 31);
-              if (cand < 32 && pc <= c) owner = cand;
-            }
-            const uint32_t om = __shfl_sync(0xffffffffu, mask, owner);
-            const uint32_t op = __shfl_sync(0xffffffffu, pref, owner);
-            if (c < total) {
-              const int bit = (int)__fns(om, 0u, (int)(c - op) + 1);
-              const int64_t j = j0 + c0 + bit;
-              double sq = __longlong_as_double(0x7ff0000000000000ll);
-              const int64_t qo = (int64_t)qt * kQM + q4 * 32 + owner;
-              if (j < p.n && qo < p.m) {
-                const T *tr = train + j * (int64_t)p.d;
-                const T *qrow = queries + qo * (int64_t)p.d;
-                bool exact = false;
-                if constexpr (sizeof(T) == 4) exact = sqd_exact_f32(qrow, tr, p.d, p.lg_d, sq);
-                if (!exact) {
-                  sq = 0.0;
-                  for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qrow[t], tr[t]));
-                }
-              }
-              myD[owner * 32 + bit] = sq;
-            }
-          }
-          evals += cnt;
+          uint32_t pos = qtail + incl - cnt;
+          for (uint32_t m = mask; m; m &= m - 1)
+            Q[(pos++) & (kQueue - 1)] = ((uint32_t)lane << kRowBits) | (uint32_t)(j0 + c0 + __ffs(m) - 1);
+          qtail += total;
           __syncwarp();
-          while (mask) {  // in index order: the reference's heap step
-            const int jj = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const int64_t j = j0 + c0 + jj;
-            if (j >= p.n) break;
-            const double sq = myD[lane * 32 + jj];
-            // sqrt is monotone: sq >= root^2 means sqrt(sq) >= root, no entry
-            if (sq < hD[0]) {
-              const double dist = __dsqrt_rn(sq);
-              if (dist < hd[0]) {  // the reference's test (linear_search.rs:72)
-                hd[0] = dist;
-                hD[0] = sq;
-                hi[0] = (int32_t)j;
-                if (p.k > 1)
-                  for (int s = p.k / 2 - 1; s >= 0; --s) heap_sift(hd, hD, hi, s, p.k - 1);
-                lo = -0.5f * knn_threshold(hd[0], qn2, eq);
-              }
-            }
-          }
-          __syncwarp();
+          while (qtail - qhead >= 32) round(32);
         }
         tc::fence_before_sync();
         tc::mbar_arrive(&accempty[acc]);
       }
+      while (!stop && qtail != qhead) round(min(32u, qtail - qhead));
       if (live && !stop)
         for (int s = 0; s < p.k; ++s) {
           p.idx_out[q * p.k + s] = hi[s];
@@ -432,7 +432,7 @@ int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; 
 
 size_t knn_smem(int nkt, int row_bytes, int stages) {
   return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * kTN * row_bytes + kTN * 32) +
-         4 * 32 * 32 * 8 + (size_t)(2 * stages + 8) * 8 + 16;
+         4 * kQueue * 4 + (size_t)(2 * stages + 8) * 8 + 16;
 }
 
 }  // namespace
@@ -441,6 +441,10 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
                     int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, cudaStream_t st) {
   if (rescored) *rescored = 0;
   if (m == 0 || n == 0) return SC_OK;
+  if (n >= ((int64_t)1 << kRowBits)) {
+    set_error("n=%lld exceeds the split-BF16 kNN kernel's limit of 2^27 training rows", (long long)n);
+    return SC_ERR_INVALID;
+  }
   const int d_pad = knn_pad_d(d);
   const int kt_elems = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt_elems, row_bytes = kt_elems * 2;
   int stages = 6;

@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(32 * kRescoreWarps)
 rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, int k, int k_cols,
                const float *__restrict__ cT, const float *__restrict__ cn2,
                const unsigned int *__restrict__ cmax_bits, const float *__restrict__ xnrm,
-               const uint32_t *__restrict__ flag_bits, int64_t nwords,
+               const uint32_t *__restrict__ flag_bits, int64_t nwords, int64_t n,
                int32_t *__restrict__ labels, LloydState *st, int stage_ct) {
   if (st && st->done) return;
   __shared__ float xs[kRescoreWarps][256];
@@ -387,6 +387,7 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
    while (bits) {
     const int64_t i = word * 32 + (__ffs(bits) - 1);
     bits &= bits - 1;
+    if (i >= n) break;  // padding rows are never flagged by a completed assignment
     const T *xr = x + i * (int64_t)d;
     for (int t = lane; t < d; t += 32) xs[w][t] = (float)xr[t];
     __syncwarp();
@@ -639,12 +640,12 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
     auto kern = rescore_kernel<float>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
     kern<<<rgrid, 32 * kRescoreWarps, rsmem, st>>>((const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
-                                                   s->xnrm, s->flag_bits, s->n_pad / 32, labels, lst, stage);
+                                                   s->xnrm, s->flag_bits, s->n_pad / 32, n, labels, lst, stage);
   } else {
     auto kern = rescore_kernel<double>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
     kern<<<rgrid, 32 * kRescoreWarps, rsmem, st>>>((const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
-                                                   s->xnrm, s->flag_bits, s->n_pad / 32, labels, lst, stage);
+                                                   s->xnrm, s->flag_bits, s->n_pad / 32, n, labels, lst, stage);
   }
   SC_LAUNCHED();
   return SC_OK;
