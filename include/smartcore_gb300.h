@@ -146,6 +146,43 @@ sc_status sc_kmeans_profile_read(sc_kmeans *h, double *total_ms,
 sc_status sc_kmeans_sync(sc_kmeans *h);
 void sc_kmeans_destroy(sc_kmeans *h);
 
+/* One Lloyd iteration of the FP64 form that allocates nothing.  No
+ * counterpart in the reference: it is the body of the loop in KMeans::fit
+ * (src/cluster/kmeans.rs:294-310) as one call on buffers the caller owns.
+ *
+ * For callers that cannot allocate device memory during the call: a process
+ * whose device memory is already reserved by its own pool allocator (a
+ * cudaMalloc would fail or fragment that pool), or a loop that re-clusters
+ * at a high rate, where cudaMalloc / cudaFree would take the driver's
+ * allocation lock and cudaFree would synchronise the whole device.
+ *
+ * x          n x d row-major (ld = d) SC_F32 / SC_F64 matrix, device memory.
+ * centroids  k x d row-major f64, device memory: read as the current
+ *            centroids, overwritten with the new ones (an empty cluster
+ *            keeps its centroid, kmeans.rs:297-303).
+ * labels     n int32 labels out, device memory.
+ * sizes      k int64 cluster sizes out, device memory, may be NULL.
+ * distortion host pointer, may be NULL: sum over points of the FP64 squared
+ *            distance to the assigned (old) centroid.
+ * stream     cudaStream_t to run on (NULL: the legacy default stream).
+ * Results are identical to sc_kmeans_set_centroids + one sc_kmeans_iterate
+ * (max_iter 1, stop_on_converge 0) + sc_kmeans_get with SC_FORM_FP64.
+ *
+ * Scratch is a 1.6 MB static device array of this library, one per device,
+ * so the limits are k <= 4096, k*d <= 65536 and n <= 8,388,608; larger
+ * problems return SC_ERR_INVALID with the limit in the message.  The call
+ * clears the parts of the scratch that must start at zero before it uses
+ * them.  Every call in the process shares that array: overlapping calls on
+ * one device would race on it, so calls are serialised by a process-wide
+ * lock and each returns only after its work on the stream has finished.
+ * The first call on each device looks the array's address up with
+ * cudaGetSymbolAddress (which may load the library's device code): make it
+ * outside any stream capture. */
+sc_status sc_kmeans_step_noalloc(const void *x, int32_t dtype, int64_t n,
+                                 int64_t d, double *centroids, int64_t k,
+                                 int32_t *labels, int64_t *sizes,
+                                 double *distortion, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Brute-force kNN (LinearKNNSearch)                                   */
 /* ------------------------------------------------------------------ */

@@ -42,6 +42,7 @@ SIGNATURES = {
     "sc_kmeans_profile_read": ([_P, _P, _P], _I32),
     "sc_kernel_launches": ([], _I64),
     "sc_kmeans_sync": ([_P], _I32),
+    "sc_kmeans_step_noalloc": ([_P, _I32, _I64, _I64, _P, _I64, _P, _P, _P, _P], _I32),
     "sc_kmeans_destroy": ([_P], None),
     "sc_knn_create": ([_P, _I32, _I32, _I32, _I64, _I64, _I64, _P], _I32),
     "sc_knn_find": ([_P, _P, _I32, _I32, _I64, _I64, _I64, _I32, _I32, _P, _P], _I32),

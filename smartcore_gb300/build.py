@@ -28,6 +28,7 @@ SOURCES = {
     "update.cu": [],
     "split.cu": [],
     "knn_split.cu": [],
+    "noalloc.cu": [],
     "host_rng.cpp": None,  # host compiler
 }
 
