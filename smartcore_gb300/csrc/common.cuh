@@ -57,14 +57,17 @@ constexpr int kMaxKnnK = 64;  // largest k served by the kNN kernels
 // Buffers of the centroid-sum step.  mode 0: one 128-bit fixed-point
 // accumulator per (cluster, feature) updated with global atomics.  mode 1:
 // each CTA sorts its contiguous chunk of points by label and sums each
-// cluster's rows as int64 fixed point, one partial per CTA; the finalize step
-// adds the partials exactly in 128 bits.  Both are order independent.
+// cluster's rows as int64 fixed point, one partial per CTA (equal row slices
+// per warp with shared-memory accumulators when k x d of them fit, else one
+// warp per cluster); the finalize step adds the partials exactly in 128 bits.
+// All are order independent, so every variant gives the same bits.
 struct UpdateBuf {
   int mode = 0;
   int grid = 0;      // mode 1: number of CTAs (partials)
   int threads = 0;   // mode 1: threads per CTA
   int scale = 0;     // fixed-point scale 2^scale of the active mode
   size_t smem = 0;   // mode 1: dynamic shared memory per CTA
+  size_t balanced_smem = 0;  // mode 1: shared memory of the balanced kernel (0: per-cluster warps)
   Acc128 *acc = nullptr;            // mode 0: k x d
   unsigned long long *cnt = nullptr;  // mode 0: k
   long long *part = nullptr;        // mode 1: grid x k x d

@@ -342,29 +342,62 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
 }
 
 // ---------------------------------------------------------------------------
-// K6: re-score of the near-tie points.  One warp per point.
+// K6: re-score of the near-tie points.  A block takes a contiguous range of
+// flag words and works in passes of up to kRsRows flagged rows (whole words):
 //   1. a_j = ||c_j||^2 - 2 x.c_j for every centroid with FP32 CUDA-core dot
-//      products (lane = centroid), rigorous bound e32 (error of the f32
-//      conversions, the FMA chain and the reference's own rounding of D).
+//      products, register-tiled (warp = 4 rows, lane = 8 centroids), rigorous
+//      bound e32 (error of the f32 conversions, the FMA chain and the
+//      reference's own rounding of D).
 //   2. Candidates: a_j <= min_j a_j + 2 e32.  One candidate is the label.
-//   3. Otherwise D_j in FP64 in the reference order (kmeans.rs:338-346,
-//      bbd_tree.rs:101-111) for the candidates; minimum, lowest index on ties.
+//   3. Otherwise every (row, candidate) pair gets its own thread: D_j in FP64
+//      in the reference order (kmeans.rs:338-346, bbd_tree.rs:101-111); per
+//      row the minimum, lowest index on ties, is the label.
 // ---------------------------------------------------------------------------
-constexpr int kRescoreWarps = 8;
+constexpr int kRsRows = 32;      // flagged rows per pass
+constexpr int kRsThreads = 256;  // 8 warps x 4 rows
+constexpr int kRsPairs = 1024;   // pairs held per pass (more: one row at a time)
 
 template <typename T>
-__global__ void __launch_bounds__(32 * kRescoreWarps)
+__device__ __forceinline__ double exact_sqd(const T *__restrict__ xr, const double *__restrict__ cj, int d) {
+  double s = 0.0;
+  for (int t = 0; t < d; ++t) s = __dadd_rn(s, sqd_term((double)xr[t], cj[t]));
+  return s;
+}
+
+// Column of the u-th candidate (ascending) in an 8-word mask.
+__device__ __forceinline__ int nth_candidate(const uint32_t *mask, int u) {
+  for (int m = 0; m < 8; ++m) {
+    uint32_t b = mask[m];
+    const int c = __popc(b);
+    if (u < c) {
+      for (int q = 0; q < u; ++q) b &= b - 1u;
+      return 32 * m + __ffs(b) - 1;
+    }
+    u -= c;
+  }
+  return 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRsThreads)
 rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, int k, int k_cols,
                const float *__restrict__ cT, const float *__restrict__ cn2,
                const unsigned int *__restrict__ cmax_bits, const float *__restrict__ xnrm,
                const uint32_t *__restrict__ flag_bits, int64_t nwords, int64_t n,
                int32_t *__restrict__ labels, LloydState *st, int stage_ct) {
   if (st && st->done) return;
-  __shared__ float xs[kRescoreWarps][256];
-  __shared__ int s_any;
+  __shared__ __align__(16) float xs[256][kRsRows];  // x^T of the pass's rows
+  __shared__ int64_t s_row[kRsRows];
+  __shared__ uint32_t s_mask[kRsRows][8];          // candidate columns per row
+  __shared__ int s_cnt[kRsRows];                   // candidates per row (0: resolved)
+  __shared__ int s_pre[kRsRows + 1];
+  __shared__ double q_s[kRsPairs];
+  __shared__ int16_t q_j[kRsPairs];
+  __shared__ unsigned long long s_best;
+  __shared__ int s_bj, s_any, s_nr;
+  __shared__ long long s_next;
   extern __shared__ __align__(16) float s_ct[];  // d x k_cols when stage_ct
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // this block's words: [w0, w1)
   const int64_t per = (nwords + gridDim.x - 1) / gridDim.x;
   const int64_t w0 = (int64_t)blockIdx.x * per, w1 = min(nwords, w0 + per);
   if (threadIdx.x == 0) s_any = 0;
@@ -376,79 +409,162 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
   if (stage_ct) {
     const int total = d * k_cols;
     for (int t = threadIdx.x; t < total; t += blockDim.x) s_ct[t] = cT[t];
-    __syncthreads();
     cT = s_ct;
   }
   const float cmax = __uint_as_float(*cmax_bits);
+  const int mchunks = k_cols >> 5;  // 32-centroid chunks present in cT (uniform)
   unsigned long long done_here = 0;
-  for (int64_t word = w0 + w; word < w1; word += kRescoreWarps) {
-   uint32_t bits = flag_bits[word];
-   done_here += __popc(bits);
-   while (bits) {
-    const int64_t i = word * 32 + (__ffs(bits) - 1);
-    bits &= bits - 1;
-    if (i >= n) break;  // padding rows are never flagged by a completed assignment
-    const T *xr = x + i * (int64_t)d;
-    for (int t = lane; t < d; t += 32) xs[w][t] = (float)xr[t];
-    __syncwarp();
-    float av[8];
-    float m1 = __int_as_float(0x7f800000);
-    const int mchunks = k_cols >> 5;  // 32-centroid chunks present in cT (uniform)
+  int64_t cursor = w0;
+  while (cursor < w1) {
+    // ---- gather (warp 0): whole flag words while the pass holds <= kRsRows rows
+    if (w == 0) {
+      int nr = 0;
+      int64_t cur = cursor;
+      while (cur < w1) {
+        const int64_t q = cur + lane;
+        uint32_t bits = q < w1 ? flag_bits[q] : 0u;
+        if (q * 32 >= n) bits = 0u;  // padding rows: only stale bits of an aborted assignment
+        else if (q * 32 + 32 > n) bits &= (1u << (int)(n - q * 32)) - 1u;
+        const int c = __popc(bits);
+        int incl = c;
 #pragma unroll
-    for (int m = 0; m < 8; ++m) av[m] = 0.f;
-    for (int t = 0; t < d; ++t) {
-      const float xt = xs[w][t];
-      const float *row = cT + (int64_t)t * k_cols + lane;
-#pragma unroll
-      for (int m = 0; m < 8; ++m)
-        if (m < mchunks) av[m] = fmaf(xt, row[32 * m], av[m]);
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const bool fits = nr + incl <= kRsRows;  // a prefix of the lanes: incl grows with the lane
+        const int ntake = __popc(__ballot_sync(0xffffffffu, fits));
+        if (fits) {
+          int r = nr + incl - c;
+          for (uint32_t b = bits; b; b &= b - 1u) s_row[r++] = q * 32 + (__ffs(b) - 1);
+        }
+        if (ntake > 0) nr += __shfl_sync(0xffffffffu, incl, ntake - 1);
+        cur += ntake;
+        if (ntake < 32) break;
+      }
+      if (lane == 0) { s_nr = nr; s_next = (long long)min(cur, w1); }
     }
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const int j = lane + 32 * m;
-      av[m] = (m < mchunks && j < k) ? fmaf(-2.f, av[m], cn2[j]) : __int_as_float(0x7f800000);
-      m1 = fminf(m1, av[m]);
+    __syncthreads();
+    const int nr = s_nr;
+    cursor = s_next;
+    if (nr == 0) continue;  // block-uniform
+    if (threadIdx.x == 0) done_here += (unsigned long long)nr;
+    // ---- the pass's rows in f32, transposed (rows >= nr are zero)
+    for (int e = threadIdx.x; e < kRsRows * d; e += kRsThreads) {
+      const int r = e / d, t = e - r * d;
+      xs[t][r] = r < nr ? (float)x[s_row[r] * (int64_t)d + t] : 0.f;
     }
+    __syncthreads();
+    // ---- FP32 scores and candidates: warp w has rows 4w..4w+3
+    if (4 * w < nr) {
+      float acc[4][8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m1 = fminf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
-    const float xn = xnrm[i];
-    const float e32 = 1.05f * ((2.f * d + 8.f) * 0x1p-24f * xn * cmax + 0x1p-23f * (cmax * cmax + 2.f * xn * cmax) +
-                               (float)((d + 4) * 0x1p-52) * (xn + cmax) * (xn + cmax)) + 1e-30f;
-    const float lim = m1 + 2.f * e32;
-    int ncand = 0, first = 0x7fffffff;
+      for (int rr = 0; rr < 4; ++rr)
 #pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const unsigned b = __ballot_sync(0xffffffffu, av[m] <= lim);
-      ncand += __popc(b);
-      if (b && first == 0x7fffffff) first = 32 * m + __ffs(b) - 1;
-    }
-    int label = first;
-    if (ncand > 1) {
-      double best = DBL_MAX;
-      int bi = 0x7fffffff;
+        for (int m = 0; m < 8; ++m) acc[rr][m] = 0.f;
+      for (int t = 0; t < d; ++t) {
+        const float4 xv = *reinterpret_cast<const float4 *>(&xs[t][4 * w]);
+        const float *crow = cT + (int64_t)t * k_cols + lane;
 #pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        const int j = lane + 32 * m;
-        if (av[m] <= lim) {
-          const double *cj = cent + (int64_t)j * d;
-          double s = 0.0;
-          for (int t = 0; t < d; ++t) s = __dadd_rn(s, sqd_term((double)xr[t], cj[t]));
-          if (s < best || (s == best && j < bi)) { best = s; bi = j; }
+        for (int m = 0; m < 8; ++m) {
+          if (m < mchunks) {
+            const float cv = crow[32 * m];
+            acc[0][m] = fmaf(xv.x, cv, acc[0][m]);
+            acc[1][m] = fmaf(xv.y, cv, acc[1][m]);
+            acc[2][m] = fmaf(xv.z, cv, acc[2][m]);
+            acc[3][m] = fmaf(xv.w, cv, acc[3][m]);
+          }
         }
       }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_down_sync(0xffffffffu, best, o);
-        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-        if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      for (int rr = 0; rr < 4; ++rr) {
+        const int r = 4 * w + rr;
+        float mn = __int_as_float(0x7f800000);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+          const int j = lane + 32 * m;
+          acc[rr][m] = (m < mchunks && j < k) ? fmaf(-2.f, acc[rr][m], cn2[j]) : __int_as_float(0x7f800000);
+          mn = fminf(mn, acc[rr][m]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        if (r < nr) {  // warp-uniform
+          const int64_t i = s_row[r];
+          const float xn = xnrm[i];
+          const float e32 = 1.05f * ((2.f * d + 8.f) * 0x1p-24f * xn * cmax + 0x1p-23f * (cmax * cmax + 2.f * xn * cmax) +
+                                     (float)((d + 4) * 0x1p-52) * (xn + cmax) * (xn + cmax)) + 1e-30f;
+          const float lim = mn + 2.f * e32;
+          int count = 0, first = 0x7fffffff;
+#pragma unroll
+          for (int m = 0; m < 8; ++m) {
+            const uint32_t b = __ballot_sync(0xffffffffu, acc[rr][m] <= lim);
+            count += __popc(b);
+            if (b && first == 0x7fffffff) first = 32 * m + __ffs(b) - 1;
+            if (lane == m) s_mask[r][m] = b;
+          }
+          if (lane == 0) {
+            s_cnt[r] = count > 1 ? count : 0;
+            if (count <= 1) labels[i] = first == 0x7fffffff ? 0 : first;
+          }
+        } else if (lane == 0) {
+          s_cnt[r] = 0;
+        }
       }
-      label = __shfl_sync(0xffffffffu, bi, 0);
+    } else if (lane < 4) {
+      s_cnt[4 * w + lane] = 0;
     }
-    if (lane == 0) labels[i] = label == 0x7fffffff ? 0 : label;
-    __syncwarp();
-   }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      for (int r = 0; r < kRsRows; ++r) { s_pre[r] = acc; acc += s_cnt[r]; }
+      s_pre[kRsRows] = acc;
+    }
+    __syncthreads();
+    const int npairs = s_pre[kRsRows];
+    if (npairs <= kRsPairs) {
+      // ---- one thread per (row, candidate) pair
+      for (int p = threadIdx.x; p < npairs; p += kRsThreads) {
+        int lo = 0, hi = kRsRows - 1;  // the row: largest r with s_pre[r] <= p
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_pre[mid] <= p) lo = mid; else hi = mid - 1;
+        }
+        const int j = nth_candidate(s_mask[lo], p - s_pre[lo]);
+        q_j[p] = (int16_t)j;
+        q_s[p] = exact_sqd(x + s_row[lo] * (int64_t)d, cent + (int64_t)j * d, d);
+      }
+      __syncthreads();
+      if (threadIdx.x < kRsRows && s_cnt[threadIdx.x] > 0) {
+        const int r = threadIdx.x, b = s_pre[r], e = s_pre[r + 1];
+        double best = q_s[b];
+        int bj = q_j[b];
+        for (int u = b + 1; u < e; ++u)  // ascending j: strict < keeps the lowest index
+          if (q_s[u] < best) { best = q_s[u]; bj = q_j[u]; }
+        labels[s_row[r]] = bj;
+      }
+    } else {
+      // ---- many candidates: one row at a time, one thread per candidate
+      for (int r = 0; r < kRsRows; ++r) {
+        const int c = s_cnt[r];  // <= k_cols <= kRsThreads
+        if (c == 0) continue;
+        if (threadIdx.x == 0) { s_best = ~0ull; s_bj = 0x7fffffff; }
+        __syncthreads();
+        double sv = 0.0;
+        int j = 0;
+        if ((int)threadIdx.x < c) {
+          j = nth_candidate(s_mask[r], threadIdx.x);
+          sv = exact_sqd(x + s_row[r] * (int64_t)d, cent + (int64_t)j * d, d);
+          atomicMin(&s_best, (unsigned long long)__double_as_longlong(sv));  // sv >= 0: bits order as values
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < c && (unsigned long long)__double_as_longlong(sv) == s_best) atomicMin(&s_bj, j);
+        __syncthreads();
+        if (threadIdx.x == 0) labels[s_row[r]] = s_bj;
+      }
+    }
+    __syncthreads();
   }
-  if (lane == 0 && done_here && st) atomicAdd((unsigned long long *)&st->rescored, done_here);
+  if (threadIdx.x == 0 && done_here && st) atomicAdd((unsigned long long *)&st->rescored, done_here);
 }
 
 // ---------------------------------------------------------------------------
@@ -639,12 +755,12 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   if (dtype == SC_F32) {
     auto kern = rescore_kernel<float>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
-    kern<<<rgrid, 32 * kRescoreWarps, rsmem, st>>>((const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
+    kern<<<rgrid, kRsThreads, rsmem, st>>>((const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
                                                    s->xnrm, s->flag_bits, s->n_pad / 32, n, labels, lst, stage);
   } else {
     auto kern = rescore_kernel<double>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
-    kern<<<rgrid, 32 * kRescoreWarps, rsmem, st>>>((const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
+    kern<<<rgrid, kRsThreads, rsmem, st>>>((const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
                                                    s->xnrm, s->flag_bits, s->n_pad / 32, n, labels, lst, stage);
   }
   SC_LAUNCHED();

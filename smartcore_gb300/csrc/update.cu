@@ -152,20 +152,10 @@ __device__ __forceinline__ void add_fixed64(long long &acc, float v, int scale) 
   acc += (b >> 31) ? -mag : mag;
 }
 
-template <typename T, int MAXJ>
-__global__ void __launch_bounds__(1024)
-update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *__restrict__ labels, int k,
-                     long long *__restrict__ part, unsigned int *__restrict__ cpart, int scale,
-                     const LloydState *st) {
-  if (st && st->done) return;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  int *cnt = reinterpret_cast<int *>(smraw);  // k
-  int *off = cnt + k;                         // k + 1
-  int *cur = off + k + 1;                     // k
-  int *idx = cur + k;                         // chunk
-  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-  const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
-  const int len = i1 > i0 ? (int)(i1 - i0) : 0;
+// Counting sort of a CTA's chunk by label (shared memory): cnt[c] points of
+// cluster c, off[c] .. off[c + 1] their positions in idx (chunk-relative rows).
+__device__ __forceinline__ void sort_chunk_by_label(const int32_t *__restrict__ labels, int64_t i0, int len, int k,
+                                                    int *cnt, int *off, int *cur, int *idx) {
   for (int t = threadIdx.x; t < k; t += blockDim.x) cnt[t] = 0;
   __syncthreads();
   for (int t = threadIdx.x; t < len; t += blockDim.x) atomicAdd(&cnt[labels[i0 + t]], 1);
@@ -188,6 +178,101 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
   }
   __syncthreads();
   for (int t = threadIdx.x; t < len; t += blockDim.x) idx[atomicAdd(&cur[labels[i0 + t]], 1)] = t;
+}
+
+// K2, balanced partial form: after the counting sort, warp w sums the w-th
+// equal slice of the label-sorted rows (lane = feature) in int64 registers
+// and flushes them into a k x d shared accumulator whenever the cluster
+// changes, so every warp gathers the same number of rows whatever the
+// cluster sizes.  Same partials as update_sorted_kernel.
+template <int MAXJ>
+__global__ void __launch_bounds__(1024)
+update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int32_t *__restrict__ labels, int k,
+                       long long *__restrict__ part, unsigned int *__restrict__ cpart, int scale,
+                       const LloydState *st) {
+  if (st && st->done) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  unsigned long long *acc = reinterpret_cast<unsigned long long *>(smraw);  // k x d
+  const int kd = k * d;
+  int *cnt = reinterpret_cast<int *>(acc + kd);  // k
+  int *off = cnt + k;                            // k + 1
+  int *cur = off + k + 1;                        // k
+  int *idx = cur + k;                            // chunk
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+  const int len = i1 > i0 ? (int)(i1 - i0) : 0;
+  for (int t = threadIdx.x; t < kd; t += blockDim.x) acc[t] = 0ull;
+  sort_chunk_by_label(labels, i0, len, k, cnt, off, cur, idx);
+  for (int t = threadIdx.x; t < k; t += blockDim.x) cpart[(size_t)blockIdx.x * k + t] = (unsigned int)cnt[t];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  constexpr int kRows = 16 / MAXJ;  // rows in flight per warp
+  const int seg = (len + nw - 1) / nw;
+  const int s_begin = min(len, w * seg), s_end = min(len, s_begin + seg);
+  if (s_begin < s_end) {
+    int lo = 0, hi = k - 1;  // cluster of position s_begin: the largest c with off[c] <= s_begin
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (off[mid] <= s_begin) lo = mid; else hi = mid - 1;
+    }
+    int c = lo;
+    long long a[MAXJ];
+#pragma unroll
+    for (int q = 0; q < MAXJ; ++q) a[q] = 0;
+    for (int s = s_begin; s < s_end; s += kRows) {
+      float v[kRows][MAXJ];
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        const bool ok = s + r < s_end;
+        const float *xr = x + (i0 + (ok ? idx[s + r] : 0)) * (int64_t)d;
+#pragma unroll
+        for (int q = 0; q < MAXJ; ++q) {
+          const int j = lane + 32 * q;
+          v[r][q] = (ok && j < d) ? __ldg(xr + j) : 0.f;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kRows; ++r) {
+        if (s + r >= s_end) break;
+        while (s + r >= off[c + 1]) {  // cluster boundary: flush
+#pragma unroll
+          for (int q = 0; q < MAXJ; ++q) {
+            const int j = lane + 32 * q;
+            if (j < d && a[q] != 0) atomicAdd(acc + c * d + j, (unsigned long long)a[q]);
+            a[q] = 0;
+          }
+          ++c;
+        }
+#pragma unroll
+        for (int q = 0; q < MAXJ; ++q) add_fixed64(a[q], v[r][q], scale);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < MAXJ; ++q) {
+      const int j = lane + 32 * q;
+      if (j < d && a[q] != 0) atomicAdd(acc + c * d + j, (unsigned long long)a[q]);
+    }
+  }
+  __syncthreads();
+  long long *pc = part + (size_t)blockIdx.x * kd;
+  for (int t = threadIdx.x; t < kd; t += blockDim.x) pc[t] = (long long)acc[t];
+}
+
+template <typename T, int MAXJ>
+__global__ void __launch_bounds__(1024)
+update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *__restrict__ labels, int k,
+                     long long *__restrict__ part, unsigned int *__restrict__ cpart, int scale,
+                     const LloydState *st) {
+  if (st && st->done) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  int *cnt = reinterpret_cast<int *>(smraw);  // k
+  int *off = cnt + k;                         // k + 1
+  int *cur = off + k + 1;                     // k
+  int *idx = cur + k;                         // chunk
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+  const int len = i1 > i0 ? (int)(i1 - i0) : 0;
+  sort_chunk_by_label(labels, i0, len, k, cnt, off, cur, idx);
   for (int t = threadIdx.x; t < k; t += blockDim.x) cpart[(size_t)blockIdx.x * k + t] = (unsigned int)cnt[t];
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -456,6 +541,8 @@ sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double 
     u->smem = smem;
     u->scale = 62 - e - ceil_log2(chunk + 1);
     if (u->scale > 160) u->scale = 160;  // values below 2^-160 contribute 0
+    const size_t bal = smem + (size_t)k * d * sizeof(long long);
+    u->balanced_smem = (d <= 128 && bal <= 200 * 1024) ? bal : 0;
     if (cudaMalloc((void **)&u->part, part_bytes) != cudaSuccess ||
         cudaMalloc((void **)&u->cpart, (size_t)grid * k * sizeof(unsigned int)) != cudaSuccess)
       return cuda_fail(cudaErrorMemoryAllocation, "update partials");
@@ -480,6 +567,16 @@ void update_free(UpdateBuf *u) {
 }
 
 template <int MAXJ>
+static sc_status launch_balanced(const UpdateBuf *u, const float *x, int64_t n, int d, const int32_t *labels, int k,
+                                 const LloydState *st, cudaStream_t s) {
+  auto kern = update_balanced_kernel<MAXJ>;
+  SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->balanced_smem));
+  kern<<<u->grid, 1024, u->balanced_smem, s>>>(x, n, d, labels, k, u->part, u->cpart, u->scale, st);
+  SC_LAUNCHED();
+  return SC_OK;
+}
+
+template <int MAXJ>
 static sc_status launch_sorted(const UpdateBuf *u, const float *x, int64_t n, int d, const int32_t *labels, int k,
                                const LloydState *st, cudaStream_t s) {
   auto kern = update_sorted_kernel<float, MAXJ>;
@@ -498,6 +595,11 @@ sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n,
     return SC_ERR_INTERNAL;
   }
   const float *xf = (const float *)x;
+  if (u->balanced_smem) {
+    if (d <= 32) return launch_balanced<1>(u, xf, n, d, labels, k, st, s);
+    if (d <= 64) return launch_balanced<2>(u, xf, n, d, labels, k, st, s);
+    return launch_balanced<4>(u, xf, n, d, labels, k, st, s);
+  }
   if (d <= 32) return launch_sorted<1>(u, xf, n, d, labels, k, st, s);
   if (d <= 64) return launch_sorted<2>(u, xf, n, d, labels, k, st, s);
   if (d <= 128) return launch_sorted<4>(u, xf, n, d, labels, k, st, s);

@@ -114,6 +114,24 @@ def test_predict_ties_lowest_index():
 
 
 @pytest.mark.parametrize("form", FORMS)
+def test_predict_many_tied_candidates(form):
+    # 40 centroids drawn from the 16 vectors +-e_t (duplicates included), all
+    # of norm 1: points at the origin tie with every centroid exactly, points
+    # near it are near ties with many.  Exercises the split form's fallback
+    # for rows with more candidates than one list holds.
+    rng = np.random.default_rng(11)
+    basis = np.concatenate([np.eye(8), -np.eye(8)])
+    c = basis[rng.integers(0, 16, size=40)]
+    x = np.concatenate([np.zeros((300, 8)), rng.normal(scale=1e-7, size=(700, 8)), rng.normal(size=(1000, 8))])
+    for dt in (np.float64, np.float32):
+        xd = x.astype(dt)
+        km = KMeans(40, None, None, 0.0, c, 0, form)
+        got = km.predict(xd)
+        assert np.array_equal(got, oracle.kmeans_predict(xd, c))
+        assert np.all(got[:300] == 0)
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_edge_shapes(form):
     x, _ = blobs(64, 3, 4, seed=2)
     assert_fit_parity(x, 64, 10, 1, form)  # k == n
