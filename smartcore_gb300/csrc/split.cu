@@ -105,7 +105,12 @@ struct AssignParams {
   float coef_cc;
   float coef_ref;   // reference rounding of D: <= coef_ref * (||x|| + ||c||)^2
   int32_t *labels;
-  uint32_t *flag_bits;  // bit i: point i is a near tie (one word per warp and tile)
+  int64_t n_pad;
+  int region;                // near-tie list entries reserved per CTA
+  unsigned int *list_count;  // near-tie rows listed by each CTA
+  int64_t *list_rows;        //   CTA b's rows at [b * region, ...)
+  uint32_t *cand4;           // [2 halves][n_pad]: up to 4 candidate columns of a listed row (bytes)
+  uint8_t *cmeta;            // [2 halves][n_pad]: bits 0-3 valid bytes of cand4, bit 4 list complete
   LloydState *st;
 };
 
@@ -126,12 +131,13 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
   uint8_t *sOnes = base + b_bytes;
   uint8_t *sBx = sOnes + kBM * 32;
   uint8_t *sA = base + b_bytes + x_bytes;
-  float4 *s_xch = (float4 *)(sA + (size_t)p.stages * a_stage);  // [2 buffers][2 accumulators][128 rows]
-  uint64_t *bars = (uint64_t *)(s_xch + 4 * kBM);
+  float4 *s_xch = (float4 *)(sA + (size_t)p.stages * a_stage);  // [2 buffers][2 accumulators][2 halves][128 rows]
+  uint64_t *bars = (uint64_t *)(s_xch + 8 * kBM);
   uint64_t *full = bars, *empty = bars + p.stages, *bfull = bars + 2 * p.stages;
   uint64_t *accfull = bfull + 1, *accempty = bfull + 3, *mma_done = bfull + 5;
   uint32_t *s_tmem = (uint32_t *)(bfull + 6);
   int *s_abort = (int *)(s_tmem + 1);
+  unsigned int *s_nlist = (unsigned int *)(s_abort + 1);  // near-tie rows listed by this CTA
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -146,6 +152,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       tc::mbar_init(&accempty[a], kEpiThreads / 2);  // both column halves of the buffer
     }
     *s_abort = 0;
+    *s_nlist = 0u;
     tc::fence_mbar_init();
     tc::prefetch_tmap(&tm_xh);
     tc::prefetch_tmap(&tm_xl);
@@ -250,7 +257,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       if ((it & 1) != g) continue;
       const int64_t i = (int64_t)t * kBM + row;
       const bool live = i < p.n;
-      const float xn = (h == 0 && live) ? __ldg(p.xnrm + i) : 0.f;
+      const float xn = live ? __ldg(p.xnrm + i) : 0.f;
       const uint32_t aph = (uint32_t)(it >> 1) & 1u;
       const bool got = tc::mbar_wait(&accfull[g], aph, kWaitNs);
       if (tc::bar_red_or(!got || *(volatile int *)s_abort != 0, bar_id, 64)) {  // uniform over the pair
@@ -305,31 +312,60 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
         }
         mm2 = fmaxf(mm2, m2[r]);
       }
-      float4 *slot = s_xch + (((it >> 1) & 1) * 2 + g) * kBM + row;
-      if (h == 1) *slot = make_float4(mm1, mm2, __int_as_float(a), 0.f);
+      // the two halves of the row meet in shared memory; both merge them in
+      // column order (lower half first), so both reach the same decision
+      float4 *xs = s_xch + (((it >> 1) & 1) * 2 + g) * 2 * kBM;
+      xs[h * kBM + row] = make_float4(mm1, mm2, __int_as_float(a), 0.f);
       tc::bar_sync(bar_id, 64);
-      if (h == 1) continue;
-      {  // the second half of the row (higher column indices)
-        const float4 o = *slot;
-        const int oa = __float_as_int(o.z);
-        if (o.x > mm1 || (o.x == mm1 && oa < a)) {
-          mm2 = fmaxf(mm1, o.y);
-          mm1 = o.x;
-          a = oa;
+      const float4 o = xs[(h ^ 1) * kBM + row];
+      float b1 = h ? o.x : mm1, b2 = h ? o.y : mm2;
+      int ba = h ? __float_as_int(o.z) : a;
+      {
+        const float u1 = h ? mm1 : o.x, u2 = h ? mm2 : o.y;
+        const int ua = h ? a : __float_as_int(o.z);
+        if (u1 > b1 || (u1 == b1 && ua < ba)) {
+          b2 = fmaxf(b1, u2);
+          b1 = u1;
+          ba = ua;
         } else {
-          mm2 = fmaxf(mm2, o.x);
+          b2 = fmaxf(b2, u1);
         }
-        mm2 = fmaxf(mm2, o.y);
+        b2 = fmaxf(b2, u2);
       }
       // |acc_j - (x.c_j - ||c_j||^2/2)| <= E_acc, and D_j = ||x||^2 - 2 (x.c_j - ||c_j||^2/2)
       // up to the reference's own rounding: the label is certain when the
       // best and second-best D differ by more than 2 (2 E_acc + E_ref).
+      // Otherwise the reference's minimum is among the columns whose score
+      // is within 2 E_acc + E_ref of the best (margin 1.05): the candidates.
       const float e_acc = p.coef_xc * xn * cmax + p.coef_cc * cmax * cmax;
       const float e = 2.f * e_acc + p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
-      const bool flagged = live && !(2.f * (mm1 - mm2) > 2.1f * e);
-      if (live) p.labels[i] = a == 0x7fffffff ? 0 : a;
-      const uint32_t fm = __ballot_sync(0xffffffffu, flagged);
-      if (lane == 0) p.flag_bits[(int64_t)t * (kBM / 32) + q] = fm;
+      const bool flagged = live && !(2.f * (b1 - b2) > 2.1f * e);
+      if (h == 0) {
+        if (live) p.labels[i] = ba == 0x7fffffff ? 0 : ba;
+        const uint32_t fm = __ballot_sync(0xffffffffu, flagged);
+        if (fm) {
+          unsigned int first = 0;
+          if (lane == 0) first = atomicAdd(s_nlist, (unsigned int)__popc(fm));
+          first = __shfl_sync(0xffffffffu, first, 0);
+          if (flagged)
+            p.list_rows[(int64_t)blockIdx.x * p.region + first + __popc(fm & ((1u << lane) - 1u))] = i;
+        }
+      }
+      if (flagged) {
+        // Tracker r saw this half's columns c with (c - c_lo) = r (mod 4).  When
+        // its second value is below the threshold, only its maximum can be a
+        // candidate; when every tracker's is, the maxima above the threshold
+        // are this half's complete candidate list.
+        const float thr = b1 - 1.05f * e;
+        uint32_t cw = 0u, meta = 16u;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          if (m1[r] >= thr) { cw |= (uint32_t)mi[r] << (8 * r); meta |= 1u << r; }
+          if (m2[r] >= thr) meta &= ~16u;
+        }
+        p.cand4[(size_t)h * p.n_pad + i] = cw;
+        p.cmeta[(size_t)h * p.n_pad + i] = (uint8_t)meta;
+      }
     }
   }
   tc::fence_before_sync();
@@ -338,24 +374,26 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
     tc::fence_after_sync();
     tc::tmem_dealloc(tmem, p.tmem_cols);
   }
+  if (threadIdx.x == 0) p.list_count[blockIdx.x] = *s_nlist;
   if (threadIdx.x == 0 && *s_abort && p.st) atomicExch(&p.st->err, kErrTimeout);
 }
 
 // ---------------------------------------------------------------------------
-// K6: re-score of the near-tie points.  A block takes a contiguous range of
-// flag words and works in passes of up to kRsRows flagged rows (whole words):
-//   1. a_j = ||c_j||^2 - 2 x.c_j for every centroid with FP32 CUDA-core dot
-//      products, register-tiled (warp = 4 rows, lane = 8 centroids), rigorous
-//      bound e32 (error of the f32 conversions, the FMA chain and the
-//      reference's own rounding of D).
-//   2. Candidates: a_j <= min_j a_j + 2 e32.  One candidate is the label.
-//   3. Otherwise every (row, candidate) pair gets its own thread: D_j in FP64
+// K6: re-score of the near-tie rows the assignment kernel listed.  Block b
+// takes CTA b's list in passes of up to kRsRows rows:
+//   1. a_j = ||c_j||^2 - 2 x.c_j with FP32 CUDA-core dot products and the
+//      rigorous bound e32 (error of the f32 conversions, the FMA chain and the
+//      reference's own rounding of D), for the row's listed candidates (8
+//      threads per row) or, when a list is not complete, for every centroid
+//      (register-tiled: warp = 2 rows, lane = 8 centroids).
+//   2. Survivors: a_j <= min_j a_j + 2 e32.  One survivor is the label.
+//   3. Otherwise every (row, survivor) pair gets its own thread: D_j in FP64
 //      in the reference order (kmeans.rs:338-346, bbd_tree.rs:101-111); per
 //      row the minimum, lowest index on ties, is the label.
 // ---------------------------------------------------------------------------
-constexpr int kRsRows = 32;      // flagged rows per pass
-constexpr int kRsThreads = 256;  // 8 warps x 4 rows
-constexpr int kRsPairs = 1024;   // pairs held per pass (more: one row at a time)
+constexpr int kRsRows = 128;      // listed rows per pass
+constexpr int kRsThreads = 1024;  // 8 threads per row in the listed pass
+constexpr int kRsPairs = 1024;    // pairs held per pass (more: one row at a time)
 
 template <typename T>
 __device__ __forceinline__ double exact_sqd(const T *__restrict__ xr, const double *__restrict__ cj, int d) {
@@ -364,7 +402,7 @@ __device__ __forceinline__ double exact_sqd(const T *__restrict__ xr, const doub
   return s;
 }
 
-// Column of the u-th candidate (ascending) in an 8-word mask.
+// Column of the u-th set bit (ascending) of an 8-word mask.
 __device__ __forceinline__ int nth_candidate(const uint32_t *mask, int u) {
   for (int m = 0; m < 8; ++m) {
     uint32_t b = mask[m];
@@ -378,107 +416,110 @@ __device__ __forceinline__ int nth_candidate(const uint32_t *mask, int u) {
   return 0;
 }
 
+__device__ __forceinline__ float e32_bound(float xn, float cmax, int d) {
+  return 1.05f * ((2.f * d + 8.f) * 0x1p-24f * xn * cmax + 0x1p-23f * (cmax * cmax + 2.f * xn * cmax) +
+                  (float)((d + 4) * 0x1p-52) * (xn + cmax) * (xn + cmax)) + 1e-30f;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(kRsThreads)
+__global__ void __launch_bounds__(kRsThreads, 1)
 rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, int k, int k_cols,
                const float *__restrict__ cT, const float *__restrict__ cn2,
                const unsigned int *__restrict__ cmax_bits, const float *__restrict__ xnrm,
-               const uint32_t *__restrict__ flag_bits, int64_t nwords, int64_t n,
+               const int64_t *__restrict__ list_rows, const unsigned int *__restrict__ list_count, int region,
+               const uint32_t *__restrict__ cand4, const uint8_t *__restrict__ cmeta, int64_t n_pad,
                int32_t *__restrict__ labels, LloydState *st, int stage_ct) {
   if (st && st->done) return;
-  __shared__ __align__(16) float xs[256][kRsRows];  // x^T of the pass's rows
+  extern __shared__ __align__(16) float dyn[];  // [d x k_cols centroids^T when stage_ct] [d x kRsRows rows^T]
   __shared__ int64_t s_row[kRsRows];
-  __shared__ uint32_t s_mask[kRsRows][8];          // candidate columns per row
-  __shared__ int s_cnt[kRsRows];                   // candidates per row (0: resolved)
+  __shared__ uint32_t s_mask[kRsRows][8];  // survivors per row
+  __shared__ int s_cnt[kRsRows];           // survivors per row (0: resolved)
   __shared__ int s_pre[kRsRows + 1];
+  __shared__ int s_full[kRsRows];          // rows whose candidate list is not complete
+  __shared__ int s_nfull;
   __shared__ double q_s[kRsPairs];
   __shared__ int16_t q_j[kRsPairs];
   __shared__ unsigned long long s_best;
-  __shared__ int s_bj, s_any, s_nr;
-  __shared__ long long s_next;
-  extern __shared__ __align__(16) float s_ct[];  // d x k_cols when stage_ct
+  __shared__ int s_bj;
+  const unsigned int total = list_count[blockIdx.x];
+  if (total == 0) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t per = (nwords + gridDim.x - 1) / gridDim.x;
-  const int64_t w0 = (int64_t)blockIdx.x * per, w1 = min(nwords, w0 + per);
-  if (threadIdx.x == 0) s_any = 0;
-  __syncthreads();
-  for (int64_t q = w0 + threadIdx.x; q < w1; q += blockDim.x)
-    if (flag_bits[q]) s_any = 1;
-  __syncthreads();
-  if (!s_any) return;  // no near tie in this block's range
+  float *xs = dyn + (stage_ct ? d * k_cols : 0);  // xs[t * kRsRows + r]
   if (stage_ct) {
-    const int total = d * k_cols;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) s_ct[t] = cT[t];
-    cT = s_ct;
+    const int n_ct = d * k_cols;
+    for (int t = threadIdx.x; t < n_ct; t += kRsThreads) dyn[t] = cT[t];
+    cT = dyn;
   }
   const float cmax = __uint_as_float(*cmax_bits);
   const int mchunks = k_cols >> 5;  // 32-centroid chunks present in cT (uniform)
-  unsigned long long done_here = 0;
-  int64_t cursor = w0;
-  while (cursor < w1) {
-    // ---- gather (warp 0): whole flag words while the pass holds <= kRsRows rows
-    if (w == 0) {
-      int nr = 0;
-      int64_t cur = cursor;
-      while (cur < w1) {
-        const int64_t q = cur + lane;
-        uint32_t bits = q < w1 ? flag_bits[q] : 0u;
-        if (q * 32 >= n) bits = 0u;  // padding rows: only stale bits of an aborted assignment
-        else if (q * 32 + 32 > n) bits &= (1u << (int)(n - q * 32)) - 1u;
-        const int c = __popc(bits);
-        int incl = c;
+  const int64_t *rows = list_rows + (int64_t)blockIdx.x * region;
+  for (unsigned int base = 0; base < total; base += kRsRows) {
+    const int nr = (int)min((unsigned int)kRsRows, total - base);
+    if (threadIdx.x < kRsRows) {
+      const int r = threadIdx.x;
+      s_cnt[r] = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        const bool fits = nr + incl <= kRsRows;  // a prefix of the lanes: incl grows with the lane
-        const int ntake = __popc(__ballot_sync(0xffffffffu, fits));
-        if (fits) {
-          int r = nr + incl - c;
-          for (uint32_t b = bits; b; b &= b - 1u) s_row[r++] = q * 32 + (__ffs(b) - 1);
-        }
-        if (ntake > 0) nr += __shfl_sync(0xffffffffu, incl, ntake - 1);
-        cur += ntake;
-        if (ntake < 32) break;
-      }
-      if (lane == 0) { s_nr = nr; s_next = (long long)min(cur, w1); }
+      for (int m = 0; m < 8; ++m) s_mask[r][m] = 0u;
+      if (r < nr) s_row[r] = rows[base + r];
     }
+    if (threadIdx.x == 0) s_nfull = 0;
     __syncthreads();
-    const int nr = s_nr;
-    cursor = s_next;
-    if (nr == 0) continue;  // block-uniform
-    if (threadIdx.x == 0) done_here += (unsigned long long)nr;
-    // ---- the pass's rows in f32, transposed (rows >= nr are zero)
     for (int e = threadIdx.x; e < kRsRows * d; e += kRsThreads) {
       const int r = e / d, t = e - r * d;
-      xs[t][r] = r < nr ? (float)x[s_row[r] * (int64_t)d + t] : 0.f;
+      xs[t * kRsRows + r] = r < nr ? (float)x[s_row[r] * (int64_t)d + t] : 0.f;
+    }
+    if (threadIdx.x < nr) {
+      const int64_t i = s_row[threadIdx.x];
+      if (!(cmeta[i] & cmeta[n_pad + i] & 16u)) s_full[atomicAdd(&s_nfull, 1)] = threadIdx.x;
     }
     __syncthreads();
-    // ---- FP32 scores and candidates: warp w has rows 4w..4w+3
-    if (4 * w < nr) {
-      float acc[4][8];
+    // ---- listed candidates: 8 threads per row (u = half * 4 + tracker)
+    {
+      const int r = threadIdx.x >> 3, u = threadIdx.x & 7;
+      const int64_t i = r < nr ? s_row[r] : 0;
+      const bool listed = r < nr && (cmeta[i] & cmeta[n_pad + i] & 16u);  // uniform over the 8 threads
+      int j = -1;
+      float a = __int_as_float(0x7f800000);
+      if (listed && ((cmeta[(size_t)(u >> 2) * n_pad + i] >> (u & 3)) & 1u)) {
+        j = (int)((cand4[(size_t)(u >> 2) * n_pad + i] >> (8 * (u & 3))) & 0xffu);
+        float dot = 0.f;
+        for (int t = 0; t < d; ++t) dot = fmaf(xs[t * kRsRows + r], cT[(int64_t)t * k_cols + j], dot);
+        a = fmaf(-2.f, dot, cn2[j]);
+      }
+      float mn = a;
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, 1));
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, 2));
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, 4));
+      const float lim = listed ? mn + 2.f * e32_bound(xnrm[i], cmax, d) : 0.f;
+      const bool surv = j >= 0 && a <= lim;
+      const uint32_t grp = (__ballot_sync(0xffffffffu, surv) >> (lane & 24)) & 0xffu;
+      if (surv) atomicOr(&s_mask[r][j >> 5], 1u << (j & 31));
+      if (listed && u == 0) s_cnt[r] = __popc(grp) > 1 ? __popc(grp) : 0;
+      if (surv && __popc(grp) == 1) labels[i] = j;
+    }
+    // ---- rows without a complete list: every centroid (warp = 2 rows)
+    const int nfull = s_nfull;
+    for (int f0 = 2 * w; f0 < nfull; f0 += 2 * (kRsThreads / 32)) {
+      const int r0 = s_full[f0], r1 = f0 + 1 < nfull ? s_full[f0 + 1] : r0;
+      float acc[2][8];
 #pragma unroll
-      for (int rr = 0; rr < 4; ++rr)
-#pragma unroll
-        for (int m = 0; m < 8; ++m) acc[rr][m] = 0.f;
+      for (int m = 0; m < 8; ++m) { acc[0][m] = 0.f; acc[1][m] = 0.f; }
       for (int t = 0; t < d; ++t) {
-        const float4 xv = *reinterpret_cast<const float4 *>(&xs[t][4 * w]);
+        const float x0 = xs[t * kRsRows + r0], x1 = xs[t * kRsRows + r1];
         const float *crow = cT + (int64_t)t * k_cols + lane;
 #pragma unroll
         for (int m = 0; m < 8; ++m) {
           if (m < mchunks) {
             const float cv = crow[32 * m];
-            acc[0][m] = fmaf(xv.x, cv, acc[0][m]);
-            acc[1][m] = fmaf(xv.y, cv, acc[1][m]);
-            acc[2][m] = fmaf(xv.z, cv, acc[2][m]);
-            acc[3][m] = fmaf(xv.w, cv, acc[3][m]);
+            acc[0][m] = fmaf(x0, cv, acc[0][m]);
+            acc[1][m] = fmaf(x1, cv, acc[1][m]);
           }
         }
       }
 #pragma unroll
-      for (int rr = 0; rr < 4; ++rr) {
-        const int r = 4 * w + rr;
+      for (int rr = 0; rr < 2; ++rr) {
+        if (rr == 1 && f0 + 1 >= nfull) break;  // warp-uniform
+        const int r = rr ? r1 : r0;
         float mn = __int_as_float(0x7f800000);
 #pragma unroll
         for (int m = 0; m < 8; ++m) {
@@ -488,41 +529,42 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        if (r < nr) {  // warp-uniform
-          const int64_t i = s_row[r];
-          const float xn = xnrm[i];
-          const float e32 = 1.05f * ((2.f * d + 8.f) * 0x1p-24f * xn * cmax + 0x1p-23f * (cmax * cmax + 2.f * xn * cmax) +
-                                     (float)((d + 4) * 0x1p-52) * (xn + cmax) * (xn + cmax)) + 1e-30f;
-          const float lim = mn + 2.f * e32;
-          int count = 0, first = 0x7fffffff;
+        const int64_t i = s_row[r];
+        const float lim = mn + 2.f * e32_bound(xnrm[i], cmax, d);
+        int count = 0, first = 0x7fffffff;
 #pragma unroll
-          for (int m = 0; m < 8; ++m) {
-            const uint32_t b = __ballot_sync(0xffffffffu, acc[rr][m] <= lim);
-            count += __popc(b);
-            if (b && first == 0x7fffffff) first = 32 * m + __ffs(b) - 1;
-            if (lane == m) s_mask[r][m] = b;
-          }
-          if (lane == 0) {
-            s_cnt[r] = count > 1 ? count : 0;
-            if (count <= 1) labels[i] = first == 0x7fffffff ? 0 : first;
-          }
-        } else if (lane == 0) {
-          s_cnt[r] = 0;
+        for (int m = 0; m < 8; ++m) {
+          const uint32_t b = __ballot_sync(0xffffffffu, acc[rr][m] <= lim);
+          count += __popc(b);
+          if (b && first == 0x7fffffff) first = 32 * m + __ffs(b) - 1;
+          if (lane == m) s_mask[r][m] = b;
+        }
+        if (lane == 0) {
+          s_cnt[r] = count > 1 ? count : 0;
+          if (count <= 1) labels[i] = first == 0x7fffffff ? 0 : first;
         }
       }
-    } else if (lane < 4) {
-      s_cnt[4 * w + lane] = 0;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int acc = 0;
-      for (int r = 0; r < kRsRows; ++r) { s_pre[r] = acc; acc += s_cnt[r]; }
-      s_pre[kRsRows] = acc;
+    if (threadIdx.x < 32) {  // exclusive prefix of the survivor counts
+      int carry = 0;
+      for (int r0 = 0; r0 < kRsRows; r0 += 32) {
+        const int v = s_cnt[r0 + lane];
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        s_pre[r0 + lane] = carry + incl - v;
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0) s_pre[kRsRows] = carry;
     }
     __syncthreads();
     const int npairs = s_pre[kRsRows];
     if (npairs <= kRsPairs) {
-      // ---- one thread per (row, candidate) pair
+      // ---- one thread per (row, survivor) pair
       for (int p = threadIdx.x; p < npairs; p += kRsThreads) {
         int lo = 0, hi = kRsRows - 1;  // the row: largest r with s_pre[r] <= p
         while (lo < hi) {
@@ -543,7 +585,7 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
         labels[s_row[r]] = bj;
       }
     } else {
-      // ---- many candidates: one row at a time, one thread per candidate
+      // ---- many survivors: one row at a time, one thread per survivor
       for (int r = 0; r < kRsRows; ++r) {
         const int c = s_cnt[r];  // <= k_cols <= kRsThreads
         if (c == 0) continue;
@@ -564,7 +606,7 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0 && done_here && st) atomicAdd((unsigned long long *)&st->rescored, done_here);
+  if (threadIdx.x == 0 && st) atomicAdd((unsigned long long *)&st->rescored, (unsigned long long)total);
 }
 
 // ---------------------------------------------------------------------------
@@ -623,7 +665,7 @@ size_t assign_smem(const SplitState *s, int stages, int k_pad) {
   const size_t a_stage = (size_t)2 * s->nkt * kBM * s->row_bytes;
   const size_t b_bytes = (((size_t)2 * s->nkt * k_pad * s->row_bytes) + 1023) & ~(size_t)1023;
   const size_t x_bytes = ((size_t)kBM * 32 + (size_t)k_pad * 32 + 1023) & ~(size_t)1023;
-  return 1024 + b_bytes + x_bytes + (size_t)stages * a_stage + 4 * kBM * 16 + (size_t)(2 * stages + 6) * 8 + 16;
+  return 1024 + b_bytes + x_bytes + (size_t)stages * a_stage + 8 * kBM * 16 + (size_t)(2 * stages + 6) * 8 + 16;
 }
 
 }  // namespace
@@ -652,7 +694,10 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
   SC_TRY(dalloc(&s->xnrm, (size_t)s->n_pad));
   const int nb = (int)((s->n_pad + 7) / 8);
   SC_TRY(dalloc(&s->part, (size_t)nb));
-  SC_TRY(dalloc(&s->flag_bits, (size_t)(s->n_pad / 32)));
+  SC_TRY(dalloc(&s->list_rows, (size_t)(s->n_pad + (int64_t)s->num_sms * kBM)));
+  SC_TRY(dalloc(&s->list_count, (size_t)s->num_sms));
+  SC_TRY(dalloc(&s->cand4, (size_t)(2 * s->n_pad)));
+  SC_TRY(dalloc(&s->cmeta, (size_t)(2 * s->n_pad)));
   SC_TRY(dalloc(&s->cmax, 1));
   if (dtype == SC_F32)
     prep_x_kernel<float><<<nb, 256, 0, st>>>((const float *)x, n, s->n_pad, d, s->d_pad, s->xh, s->xl, s->xnrm, s->part);
@@ -721,6 +766,7 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   memset(&p, 0, sizeof p);
   p.n = n;
   p.n_tiles = (int)(s->n_pad / kBM);
+  const int grid = p.n_tiles < s->num_sms ? p.n_tiles : s->num_sms;
   p.nkt = s->nkt;
   p.kt_elems = s->kt_elems;
   p.row_bytes = s->row_bytes;
@@ -739,29 +785,36 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   p.coef_cc = (float)(1.01 * 0x1p-25 + 0.51 * nacc * 0x1p-22);
   p.coef_ref = (float)((d + 4) * 0x1p-52);
   p.labels = labels;
-  p.flag_bits = s->flag_bits;
+  p.n_pad = s->n_pad;
+  p.region = (int)((p.n_tiles + grid - 1) / grid) * kBM;
+  p.list_count = s->list_count;
+  p.list_rows = s->list_rows;
+  p.cand4 = s->cand4;
+  p.cmeta = s->cmeta;
   p.st = lst;
   SC_CUDA(cudaFuncSetAttribute(split_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int grid = p.n_tiles < s->num_sms ? p.n_tiles : s->num_sms;
   if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
   split_assign_kernel<<<grid, kAssignThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, s->tm_ones,
                                                           s->tm_cbx, p);
   SC_LAUNCHED();
   if (timing) SC_CUDA(cudaEventRecord(timing[1], st));
-  const int rgrid = 2 * s->num_sms;
+  // near ties: re-score the rows each CTA listed
   const size_t ct_bytes = (size_t)d * k_cols * sizeof(float);
-  const int stage = ct_bytes <= 96 * 1024 ? 1 : 0;
-  const size_t rsmem = stage ? ct_bytes : 0;
+  const size_t xs_bytes = (size_t)d * kRsRows * sizeof(float);
+  const int stage = ct_bytes + xs_bytes <= 180 * 1024 ? 1 : 0;
+  const size_t rsmem = xs_bytes + (stage ? ct_bytes : 0);
   if (dtype == SC_F32) {
     auto kern = rescore_kernel<float>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
-    kern<<<rgrid, kRsThreads, rsmem, st>>>((const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
-                                                   s->xnrm, s->flag_bits, s->n_pad / 32, n, labels, lst, stage);
+    kern<<<grid, kRsThreads, rsmem, st>>>((const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax, s->xnrm,
+                                          s->list_rows, s->list_count, p.region, s->cand4, s->cmeta, s->n_pad,
+                                          labels, lst, stage);
   } else {
     auto kern = rescore_kernel<double>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
-    kern<<<rgrid, kRsThreads, rsmem, st>>>((const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
-                                                   s->xnrm, s->flag_bits, s->n_pad / 32, n, labels, lst, stage);
+    kern<<<grid, kRsThreads, rsmem, st>>>((const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
+                                          s->xnrm, s->list_rows, s->list_count, p.region, s->cand4, s->cmeta,
+                                          s->n_pad, labels, lst, stage);
   }
   SC_LAUNCHED();
   return SC_OK;
@@ -770,7 +823,7 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
 void split_free(SplitState *s) {
   dfree(s->xh); dfree(s->xl); dfree(s->xnrm); dfree(s->part);
   dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cmax); dfree(s->cbx); dfree(s->ones);
-  dfree(s->flag_bits); dfree(s->cT);
+  dfree(s->cT); dfree(s->list_rows); dfree(s->list_count); dfree(s->cand4); dfree(s->cmeta);
   s->ready = 0;
   s->k_alloc = 0;
   s->k_pad = 0;

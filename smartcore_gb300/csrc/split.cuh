@@ -25,7 +25,10 @@ struct SplitState {
   float *cn2 = nullptr;                         // k_pad: ||c||^2 rounded to f32 (+inf for padding)
   unsigned int *cmax = nullptr;                 // bits of an upper bound of max ||c||
   float *cT = nullptr;                          // d_pad x k_cols: centroids in f32, transposed
-  uint32_t *flag_bits = nullptr;                // n_pad / 32 words: near ties of the last assignment
+  unsigned int *list_count = nullptr;           // near ties of the last assignment: rows per CTA,
+  int64_t *list_rows = nullptr;                 //   their rows (per-CTA regions),
+  uint32_t *cand4 = nullptr;                    //   [2][n_pad] candidate columns by row (bytes)
+  uint8_t *cmeta = nullptr;                     //   [2][n_pad] valid bytes, list complete
   CUtensorMap tm_xh, tm_xl, tm_ch, tm_cl;
   int num_sms = 0;
 };
