@@ -115,8 +115,11 @@ sc_status launch_finalize_scalar(const double *part, int nparts,
                                  cudaStream_t s);
 // Chooses the mode for (n, d, k) and allocates; absmax = max |x|.
 sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms);
-// Number of distortion terms launch_finalize writes (k, or k*d).
-inline int64_t update_nterms(const UpdateBuf *u, int k, int d) { return u->mode != 0 ? (int64_t)k * d : k; }
+// Number of distortion terms launch_finalize writes: one per cluster (mode 0)
+// or one per block of 32 (cluster, feature) elements (mode 1).
+inline int64_t update_nterms(const UpdateBuf *u, int k, int d) {
+  return u->mode != 0 ? ((int64_t)k * d + 31) / 32 : k;
+}
 void update_free(UpdateBuf *u);
 sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n, int d,
                         const int32_t *labels, int k, const LloydState *st, cudaStream_t s);

@@ -140,16 +140,37 @@ __device__ __noinline__ long long to_fixed64_slow(uint32_t b, int scale) {
   return (b >> 31) ? -mag : mag;
 }
 
-__device__ __forceinline__ void add_fixed64(long long &acc, float v, int scale) {
+// Fast path of the conversion: a normal value whose scaled mantissa is an
+// integer shifted left by sh in [0, 30] (exponent field e in [lo, lo + span]),
+// so that v * 2^scale = (signed mantissa) * 2^sh is one 32 x 32 -> 64-bit
+// multiply-add on the FMA pipe.  The partial-form scales keep sh <= 38 - C
+// for chunks of 2^C rows, so chunks of 128 rows or more never leave it.
+struct FixedConv {
+  uint32_t lo, span;
+  int sh0, scale;
+};
+
+__device__ __forceinline__ FixedConv fixed_conv(int scale) {
+  FixedConv f;
+  const int lo = max(1, 150 - scale), hi = 180 - scale;  // sh = e - 150 + scale in [0, 30], e >= 1
+  f.lo = hi >= lo ? (uint32_t)lo : 0xffffffffu;
+  f.span = hi >= lo ? (uint32_t)(hi - lo) : 0u;
+  f.sh0 = lo - 150 + scale;
+  f.scale = scale;
+  return f;
+}
+
+__device__ __forceinline__ void add_fixed64(long long &acc, float v, const FixedConv &f) {
   const uint32_t b = __float_as_uint(v);
-  if ((b << 1) == 0u) return;  // +-0
-  const int sh = (int)((b >> 23) & 0xffu) - 150 + scale;
-  if ((b & 0x7f800000u) == 0u || sh < 0) {  // subnormal or below the integer grid: rare
-    acc += to_fixed64_slow(b, scale);
+  const uint32_t de = ((b >> 23) & 0xffu) - f.lo;
+  if (de <= f.span) {
+    const int m = (int)((b & 0x7fffffu) | 0x800000u);
+    const int sm = (int)b < 0 ? -m : m;
+    asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(acc) : "r"(sm), "r"(1 << ((int)de + f.sh0)));
     return;
   }
-  const long long mag = (long long)((unsigned long long)((b & 0x7fffffu) | 0x800000u) << sh);
-  acc += (b >> 31) ? -mag : mag;
+  if ((b << 1) == 0u) return;  // +-0
+  acc += to_fixed64_slow(b, f.scale);  // subnormal, below the integer grid, or sh > 30: rare
 }
 
 // Counting sort of a CTA's chunk by label (shared memory): cnt[c] points of
@@ -207,6 +228,7 @@ update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int3
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   constexpr int kRows = 16 / MAXJ;  // rows in flight per warp
+  const FixedConv fc = fixed_conv(scale);
   const int seg = (len + nw - 1) / nw;
   const int s_begin = min(len, w * seg), s_end = min(len, s_begin + seg);
   if (s_begin < s_end) {
@@ -215,7 +237,7 @@ update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int3
       const int mid = (lo + hi + 1) >> 1;
       if (off[mid] <= s_begin) lo = mid; else hi = mid - 1;
     }
-    int c = lo;
+    int c = lo, next = off[lo + 1];
     long long a[MAXJ];
 #pragma unroll
     for (int q = 0; q < MAXJ; ++q) a[q] = 0;
@@ -234,7 +256,7 @@ update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int3
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         if (s + r >= s_end) break;
-        while (s + r >= off[c + 1]) {  // cluster boundary: flush
+        while (s + r >= next) {  // cluster boundary: flush
 #pragma unroll
           for (int q = 0; q < MAXJ; ++q) {
             const int j = lane + 32 * q;
@@ -242,9 +264,10 @@ update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int3
             a[q] = 0;
           }
           ++c;
+          next = off[c + 1];
         }
 #pragma unroll
-        for (int q = 0; q < MAXJ; ++q) add_fixed64(a[q], v[r][q], scale);
+        for (int q = 0; q < MAXJ; ++q) add_fixed64(a[q], v[r][q], fc);
       }
     }
 #pragma unroll
@@ -277,6 +300,7 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   constexpr int kRows = MAXJ >= 16 ? 1 : 16 / MAXJ;  // rows in flight per warp (memory-level parallelism)
+  const FixedConv fc = fixed_conv(scale);
   for (int c = w; c < k; c += nw) {
     long long acc[MAXJ];
 #pragma unroll
@@ -297,7 +321,7 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
 #pragma unroll
       for (int r = 0; r < kRows; ++r)
 #pragma unroll
-        for (int q = 0; q < MAXJ; ++q) add_fixed64(acc[q], v[r][q], scale);
+        for (int q = 0; q < MAXJ; ++q) add_fixed64(acc[q], v[r][q], fc);
     }
     long long *pc = part + ((size_t)blockIdx.x * k + c) * d;
 #pragma unroll
@@ -312,7 +336,7 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
 // feature) elements with 8 threads each; thread g adds the partials b = g
 // (mod 8) exactly in 128 bits, the 8 sums meet in shared memory.  Also the
 // distortion-identity term n_c c_j^2 - 2 c_j S_j of the element (with the
-// centroid used for the assignment), summed later by the scalar step.
+// centroid used for the assignment); terms[b] is block b's sum of them.
 __global__ void __launch_bounds__(256)
 finalize_partials_kernel(const long long *__restrict__ part, const unsigned int *__restrict__ cpart,
                          int nparts, int k, double *__restrict__ cent, int64_t *__restrict__ sizes, int d,
@@ -336,19 +360,27 @@ finalize_partials_kernel(const long long *__restrict__ part, const unsigned int 
   s_hi[g][e] = (unsigned long long)(v >> 64);
   s_cn[g][e] = cn;
   __syncthreads();
-  if (g != 0 || t >= kd) return;
-  for (int q = 1; q < 8; ++q) {
-    v += ((unsigned __int128)s_hi[q][e] << 64) | s_lo[q][e];
-    cn += s_cn[q][e];
+  if (g != 0) return;
+  double term = 0.0;
+  if (t < kd) {
+    for (int q = 1; q < 8; ++q) {
+      v += ((unsigned __int128)s_hi[q][e] << 64) | s_lo[q][e];
+      cn += s_cn[q][e];
+    }
+    const int c = (int)(t / d);
+    const double sum = fixed_to_double((unsigned long long)v, (unsigned long long)(v >> 64), scale);
+    const double dn = (double)cn;
+    const double old = cent[t];
+    term = __fma_rn(old, __fma_rn(dn, old, -2.0 * sum), 0.0);
+    if (cn > 0) cent[t] = __ddiv_rn(sum, dn);
+    else if (empty_nan) cent[t] = __longlong_as_double(0x7ff8000000000000ll);
+    if (sizes && t % d == 0) sizes[c] = (int64_t)cn;
   }
-  const int c = (int)(t / d);
-  const double sum = fixed_to_double((unsigned long long)v, (unsigned long long)(v >> 64), scale);
-  const double dn = (double)cn;
-  const double old = cent[t];
-  if (terms) terms[t] = __fma_rn(old, __fma_rn(dn, old, -2.0 * sum), 0.0);
-  if (cn > 0) cent[t] = __ddiv_rn(sum, dn);
-  else if (empty_nan) cent[t] = __longlong_as_double(0x7ff8000000000000ll);
-  if (sizes && t % d == 0) sizes[c] = (int64_t)cn;
+  if (terms) {  // the block's 32 terms summed here: the scalar step adds one value per block
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) term += __shfl_down_sync(0xffffffffu, term, o);
+    if (e == 0) terms[blockIdx.x] = term;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -418,12 +450,18 @@ finalize_scalar_kernel(const double *__restrict__ part, int nparts,
                        const double *__restrict__ xnorm_total, LloydState *st) {
   if (st->done) return;
   __shared__ double ws[kScalarThreads / 32];
-  double v = 0.0;
-  if (part) {
-    for (int i = threadIdx.x; i < nparts; i += kScalarThreads) v += part[i];
-  } else {
-    for (int64_t i = threadIdx.x; i < k; i += kScalarThreads) v += cluster_terms[i];
+  const double *a = part ? part : cluster_terms;
+  const int64_t cnt = part ? (int64_t)nparts : k;
+  double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;  // four loads in flight per thread
+  int64_t i = threadIdx.x;
+  for (; i + 3 * kScalarThreads < cnt; i += 4 * kScalarThreads) {
+    v0 += a[i];
+    v1 += a[i + kScalarThreads];
+    v2 += a[i + 2 * kScalarThreads];
+    v3 += a[i + 3 * kScalarThreads];
   }
+  for (; i < cnt; i += kScalarThreads) v0 += a[i];
+  double v = (v0 + v1) + (v2 + v3);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
