@@ -45,6 +45,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(ms, device):
+    """Largest per-rank time (ms) over all ranks of the process group; the
+    local value when the job runs without one."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(steps, world_size, max_ms):
+    """Whole-job throughput: every rank runs `steps` steps of its own replica,
+    and the slowest rank's time is the job's time."""
+    return world_size * steps / (max_ms / 1e3)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -288,18 +306,14 @@ def run_ours(args):
         clk.mark_end()
     launches = L.sc_kernel_launches() - launches0
     barrier()
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), f"cuda:{local}")
     kms = np.zeros(1)
     kl = np.zeros(1, np.int64)
     L.sc_kmeans_profile_read(h.h, _lib.ptr(kms), _lib.ptr(kl))
     L.sc_kmeans_profile(h.h, 0)
     rescored, _ = h.stats()
     kernel_ms = float(kms[0]) / max(int(kl[0]), 1)
-    value = ws * args.steps / (ms / 1e3)
+    value = job_rate(args.steps, ws, ms)
 
     if rank != 0 or args.lloyd_only:
         if rank == 0:
