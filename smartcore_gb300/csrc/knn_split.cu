@@ -25,12 +25,14 @@ namespace sc {
 
 namespace {
 
-constexpr int kQM = 128;   // queries per tile (UMMA M)
-constexpr int kTN = 256;   // training rows per tile (UMMA N)
-constexpr int kKnnThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kQM = 128;         // queries per tile (UMMA M)
+constexpr int kOwnerWarps = 4;   // one query per thread: heap, exact replay
+constexpr int kFilterWarps = 16; // 2 accumulator buffers x 2 column halves x 4 TMEM lane quarters
+constexpr int kKnnThreads = 32 * (2 + kOwnerWarps + kFilterWarps);  // + warp 0 TMA, warp 1 MMA
+constexpr int kMaskSlots = 4;    // candidate-mask tiles between the filters and the owners
 constexpr uint64_t kWaitNs = 2000000000ull;
-constexpr int kQueue = 2048;    // per-warp ring of pending candidates (owner lane << 27 | row)
-constexpr int kRowBits = 27;    // training rows per handle < 2^27
+constexpr int kQueue = 1024;     // per owner warp: ring of pending candidates (owner lane << 27 | row)
+constexpr int kRowBits = 27;     // training rows per handle < 2^27
 
 // One term of Euclidian::squared_distance (src/metrics/distance/
 // euclidian.rs:56-62): r = a - b and r * r in the element type, then to_f64.
@@ -104,12 +106,14 @@ struct KnnParams {
 };
 
 __device__ __forceinline__ void heap_sift(double *hd, double *hD, int32_t *hi, int kk, int nn) {
-  // sift_down of heap_select.rs:71-86 (on the distances): node kk has children 2kk and 2kk+1
+  // sift_down of heap_select.rs:71-86 (on the distances): node kk has children 2kk and 2kk+1.
+  // Distances are >= 0 or +inf, so their bit patterns order as their values:
+  // the comparisons run on the integer pipe.
   while (2 * kk <= nn) {
     int j = 2 * kk;
-    if (j < nn && hd[j] < hd[j + 1]) ++j;
+    if (j < nn && __double_as_longlong(hd[j]) < __double_as_longlong(hd[j + 1])) ++j;
     const double a = hd[kk], b = hd[j];
-    if (a == b || a > b) break;
+    if (__double_as_longlong(a) >= __double_as_longlong(b)) break;
     if (j == kk) break;
     hd[kk] = b;
     hd[j] = a;
@@ -131,26 +135,41 @@ __device__ __forceinline__ float knn_threshold(double root, double qn2, float eq
   return __double2float_ru(r2 - qn2 + (double)eq + 1e-300);
 }
 
-template <typename T>
+// Roles: warp 0 TMA (query tile once, training tiles in index order), warp 1
+// MMA (one elected thread), warps 2-5 owners (one query per thread: the
+// reference heap, replayed exactly in index order), warps 6-21 filters.  A
+// filter warp reads its accumulator buffer's TMEM lanes for one column half
+// and writes, per query, the bit mask of the rows a certified bound cannot
+// exclude; the owners consume the masks of each tile in order.  A filter may
+// use a threshold up to two tiles stale: the heap root only decreases, so a
+// staler threshold admits more rows, never fewer.
+template <typename T, int TN>
 __global__ void __launch_bounds__(kKnnThreads, 1)
 knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constant__ CUtensorMap tm_ql,
                  const __grid_constant__ CUtensorMap tm_th, const __grid_constant__ CUtensorMap tm_tl,
                  const __grid_constant__ CUtensorMap tm_ones, const __grid_constant__ CUtensorMap tm_tbx,
                  const T *__restrict__ train, const T *__restrict__ queries, const KnnParams p) {
+  constexpr int kWords = TN / 32;  // mask words per query and tile
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int a_blk = kQM * p.row_bytes;
   const int a_bytes = 2 * p.nkt * a_blk;
-  const int b_blk = kTN * p.row_bytes;
-  const int b_stage = 2 * p.nkt * b_blk + kTN * 32;  // halves + norm-folding rows
+  const int b_blk = TN * p.row_bytes;
+  const int b_stage = 2 * p.nkt * b_blk + TN * 32;  // halves + norm-folding rows
   uint8_t *sA = base;
   uint8_t *sOnes = base + a_bytes;                   // 128 x 32 B
   uint8_t *sB = sOnes + kQM * 32;
-  uint32_t *sQ = (uint32_t *)(sB + (size_t)p.stages * b_stage);  // 4 warps x kQueue candidate entries
-  uint64_t *bars = (uint64_t *)(sQ + 4 * kQueue);
+  uint32_t *sQ = (uint32_t *)(sB + (size_t)p.stages * b_stage);  // owner warps x kQueue entries
+  uint32_t *sMask = sQ + kOwnerWarps * kQueue;                   // [slot][query][word]
+  float *s_lo = (float *)(sMask + kMaskSlots * kQM * kWords);    // per query: filter threshold on acc
+  double *s_rs = (double *)(s_lo + kQM);                          // owner warps x 32: round distances
+  int32_t *s_rj = (int32_t *)(s_rs + kOwnerWarps * 32);            //   rows
+  uint32_t *s_rg = (uint32_t *)(s_rj + kOwnerWarps * 32);          //   entries per owner lane
+  uint64_t *bars = (uint64_t *)(s_rg + kOwnerWarps * 32);
   uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
   uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
-  uint32_t *s_tmem = (uint32_t *)(afull + 7);
+  uint64_t *maskfull = afull + 7, *maskempty = maskfull + kMaskSlots;
+  uint32_t *s_tmem = (uint32_t *)(maskempty + kMaskSlots);
   int *s_abort = (int *)(s_tmem + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -163,7 +182,11 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     tc::mbar_init(mma_done, 1);
     for (int a = 0; a < 2; ++a) {
       tc::mbar_init(&accfull[a], 1);
-      tc::mbar_init(&accempty[a], 128);
+      tc::mbar_init(&accempty[a], 32 * kFilterWarps / 2);
+    }
+    for (int s = 0; s < kMaskSlots; ++s) {
+      tc::mbar_init(&maskfull[s], 32 * kFilterWarps / 2);
+      tc::mbar_init(&maskempty[s], 32 * kOwnerWarps);
     }
     *s_abort = 0;
     tc::fence_mbar_init();
@@ -175,7 +198,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     tc::prefetch_tmap(&tm_tbx);
   }
   if (warp == 1) {
-    tc::tmem_alloc(s_tmem, 2 * kTN);
+    tc::tmem_alloc(s_tmem, 2 * TN);
     tc::tmem_relinquish();
   }
   tc::fence_before_sync();
@@ -204,8 +227,8 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
           for (int part = 0; part < 2; ++part)
             for (int kt = 0; kt < p.nkt; ++kt)
               tc::tma_load_2d(dst + (part * p.nkt + kt) * b_blk, part ? &tm_tl : &tm_th, &full[s],
-                              kt * p.kt_elems, tt * kTN);
-          tc::tma_load_2d(dst + 2 * p.nkt * b_blk, &tm_tbx, &full[s], 0, tt * kTN);
+                              kt * p.kt_elems, tt * TN);
+          tc::tma_load_2d(dst + 2 * p.nkt * b_blk, &tm_tbx, &full[s], 0, tt * TN);
         }
       }
       if (!ok) atomicExch(s_abort, 1);
@@ -215,7 +238,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     }
   } else if (warp == 1) {
     if (lane == 0) {  // ---------------- MMA issuer ----------------
-      const uint32_t idesc = tc::idesc_bf16_f32(kQM, kTN);
+      const uint32_t idesc = tc::idesc_bf16_f32(kQM, TN);
       const uint32_t sA0 = tc::smem_u32(sA), sB0 = tc::smem_u32(sB);
       const uint64_t ones_desc = tc::smem_desc(tc::smem_u32(sOnes), 32);
       int it = 0, ql = 0;
@@ -231,7 +254,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
             break;
           }
           tc::fence_after_sync();
-          const uint32_t d_tmem = tmem + (uint32_t)(acc * kTN);
+          const uint32_t d_tmem = tmem + (uint32_t)(acc * TN);
           const uint32_t b0 = sB0 + (uint32_t)(s * b_stage);
           // -||t||^2 / 2 first, then q_h.t_h + q_h.t_l + q_l.t_h
           tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(2 * p.nkt * b_blk), 32), idesc, 0u);
@@ -253,17 +276,19 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       tc::mma_commit(mma_done);
       tc::mbar_wait(mma_done, 0, kWaitNs);
     }
-  } else {
-    // ---------------- epilogue: one query per thread ----------------
-    // Candidate rows (those a certified bound cannot exclude) are appended,
-    // per query in index order, to a per-warp queue; whenever 32 are pending
-    // the warp computes their exact reference distances lane-parallel and each
-    // owner replays its heap steps in order.  Deferring only makes the filter
-    // threshold staler, i.e. more conservative.
-    const int q4 = warp & 3;
-    const int row = q4 * 32 + lane;
+  } else if (warp < 2 + kOwnerWarps) {
+    // ---------------- owners: one query per thread ----------------
+    // The candidates of a tile arrive as bit masks in index order; they are
+    // appended, per query in index order, to the warp's queue; whenever 32
+    // are pending the warp computes their exact reference distances
+    // lane-parallel and each owner replays its heap steps in order.
+    const int lq = warp & 3;
+    const int row = lq * 32 + lane;
     const float tmax = __uint_as_float(*p.tmax);
-    uint32_t *Q = sQ + q4 * kQueue;
+    uint32_t *Q = sQ + (warp - 2) * kQueue;
+    double *Rs = s_rs + (warp - 2) * 32;
+    int32_t *Rj = s_rj + (warp - 2) * 32;
+    uint32_t *Rg = s_rg + (warp - 2) * 32;
     double hd[kMaxKnnK], hD[kMaxKnnK];  // heap distances and their squares
     int32_t hi[kMaxKnnK];
     unsigned long long evals = 0;
@@ -283,8 +308,9 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
                                 p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
       // row j can enter only if acc_j >= lo = -thr / 2 (thr = root^2 - ||q||^2 + e)
       float lo = live ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
+      s_lo[row] = lo;
       uint32_t qhead = 0, qtail = 0;  // warp-uniform queue cursors
-      const int64_t qbase = (int64_t)qt * kQM + q4 * 32;
+      const int64_t qbase = (int64_t)qt * kQM + lq * 32;
       // one round: exact distances of up to 32 queued entries, then the owners' heap steps
       auto round = [&](uint32_t cnt) {
         const uint32_t e = (uint32_t)lane < cnt ? Q[(qhead + lane) & (kQueue - 1)] : 0u;
@@ -301,69 +327,75 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
             for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qrow[t], tr[t]));
           }
         }
-        for (uint32_t r = 0; r < cnt; ++r) {  // queue order = index order per owner
-          const int o = __shfl_sync(0xffffffffu, owner, (int)r);
-          const double sr = __shfl_sync(0xffffffffu, sq, (int)r);
-          const int jr = __shfl_sync(0xffffffffu, (int)j, (int)r);
+        // every owner replays its own entries of the round (ascending = index
+        // order), all owners at once: entry r's owner learns the set of
+        // entries it owns from the group of equal owners
+        Rs[lane] = sq;
+        Rj[lane] = (int32_t)j;
+        Rg[lane] = 0u;
+        const int own = (uint32_t)lane < cnt ? owner : 32;
+        const uint32_t grp = __match_any_sync(0xffffffffu, own);
+        __syncwarp();
+        if (own < 32 && lane == __ffs(grp) - 1) Rg[own] = grp;
+        __syncwarp();
+        for (uint32_t mine = Rg[lane]; mine; mine &= mine - 1u) {
+          const int r = __ffs(mine) - 1;
+          const double sr = Rs[r];
           // sqrt is monotone: sq >= root^2 means sqrt(sq) >= root, no entry
-          if (lane == o && sr < hD[0]) {
+          if (__double_as_longlong(sr) < __double_as_longlong(hD[0])) {
             const double dist = __dsqrt_rn(sr);
-            if (dist < hd[0]) {  // the reference's test (linear_search.rs:72)
+            if (__double_as_longlong(dist) < __double_as_longlong(hd[0])) {  // dist < root (linear_search.rs:72)
               hd[0] = dist;
               hD[0] = sr;
-              hi[0] = jr;
+              hi[0] = Rj[r];
               if (p.k > 1)
                 for (int s2 = p.k / 2 - 1; s2 >= 0; --s2) heap_sift(hd, hD, hi, s2, p.k - 1);
               lo = -0.5f * knn_threshold(hd[0], qn2, eq);
             }
           }
         }
+        __syncwarp();
         qhead += cnt;
         evals += (uint32_t)lane < cnt ? 1u : 0u;
         __syncwarp();
       };
       for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
-        const int acc = it & 1;
-        const bool got = tc::mbar_wait(&accfull[acc], (uint32_t)(it >> 1) & 1u, kWaitNs);
+        const int slot = it % kMaskSlots;
+        const bool got = tc::mbar_wait(&maskfull[slot], (uint32_t)(it / kMaskSlots) & 1u, kWaitNs);
         if (!__all_sync(0xffffffffu, got) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
           atomicExch(s_abort, 1);
           stop = true;
           break;
         }
-        tc::fence_after_sync();
-        const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(acc * kTN);
-        const int64_t j0 = (int64_t)tt * kTN;
-        for (int c0 = 0; c0 < kTN; c0 += 32) {
-          uint32_t v[32];
-          __syncwarp();
-          tc::tmem_ld32(taddr + (uint32_t)c0, v);
-          tc::tmem_wait_ld();
-          float mx = __uint_as_float(v[0]);
+        const uint32_t *mrow = sMask + ((size_t)slot * kQM + row) * kWords;
+        const int64_t j0 = (int64_t)tt * TN;
 #pragma unroll
-          for (int jj = 1; jj < 32; ++jj) mx = fmaxf(mx, __uint_as_float(v[jj]));
-          if (!__any_sync(0xffffffffu, mx >= lo)) continue;  // no row of this chunk can enter any heap
-          uint32_t mask = 0;
+        for (int w = 0; w < kWords; ++w) {
+          const uint32_t mw = mrow[w];
+          if (!__any_sync(0xffffffffu, mw != 0u)) continue;
 #pragma unroll
-          for (int jj = 0; jj < 32; ++jj) mask |= (__uint_as_float(v[jj]) >= lo ? 1u : 0u) << jj;
-          const int64_t rem = p.n - (j0 + c0);  // rows past the end of the training set
-          if (rem < 32) mask &= rem <= 0 ? 0u : ((1u << rem) - 1u);
-          const uint32_t cnt = __popc(mask);
-          const uint32_t total = __reduce_add_sync(0xffffffffu, cnt);
-          uint32_t incl = cnt;
+          for (int half = 0; half < 2; ++half) {  // <= 32 x 16 new entries per step: the ring never overflows
+            const uint32_t mask = (mw >> (16 * half)) & 0xffffu;
+            const uint32_t cnt = __popc(mask);
+            const uint32_t total = __reduce_add_sync(0xffffffffu, cnt);
+            if (total == 0) continue;
+            uint32_t incl = cnt;
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
+            for (int o = 1; o < 32; o <<= 1) {
+              const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+              if (lane >= o) incl += y;
+            }
+            uint32_t pos = qtail + incl - cnt;
+            for (uint32_t m = mask; m; m &= m - 1)
+              Q[(pos++) & (kQueue - 1)] =
+                  ((uint32_t)lane << kRowBits) | (uint32_t)(j0 + 32 * w + 16 * half + __ffs(m) - 1);
+            qtail += total;
+            __syncwarp();
+            while (qtail - qhead >= 32) round(32);
           }
-          uint32_t pos = qtail + incl - cnt;
-          for (uint32_t m = mask; m; m &= m - 1)
-            Q[(pos++) & (kQueue - 1)] = ((uint32_t)lane << kRowBits) | (uint32_t)(j0 + c0 + __ffs(m) - 1);
-          qtail += total;
-          __syncwarp();
-          while (qtail - qhead >= 32) round(32);
         }
-        tc::fence_before_sync();
-        tc::mbar_arrive(&accempty[acc]);
+        s_lo[row] = lo;                     // threshold for the filters, published before the release
+        tc::mbar_arrive(&maskempty[slot]);  // tile replayed (queued entries only make lo staler)
       }
       while (!stop && qtail != qhead) round(min(32u, qtail - qhead));
       if (live && !stop)
@@ -373,12 +405,99 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         }
     }
     if (evals) atomicAdd(p.evals, evals);
+  } else {
+    // ---------------- filters: candidate masks from TMEM ----------------
+    const int f = warp - 2 - kOwnerWarps;  // 0 .. 15
+    const int g = (f >> 2) & 1, h = f >> 3, lq = warp & 3;
+    const int row = lq * 32 + lane;
+    constexpr int kCols = TN / 2;
+    const int c_lo = h * kCols;
+    int it = 0;
+    bool stop = false;
+    for (int qt = blockIdx.x; !stop && qt < p.n_tiles_q; qt += gridDim.x) {
+      for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
+        if ((it & 1) != g) continue;
+        const int slot = it % kMaskSlots;
+        bool ok = tc::mbar_wait(&accfull[g], (uint32_t)(it >> 1) & 1u, kWaitNs);
+        // threshold: tile 0 of a query tile admits every row; tile 1 waits for
+        // the owners' replay of tile 0; later tiles use the replay of tile
+        // tt - 2.  Either wait also frees this tile's mask slot.
+        const bool live_q = (int64_t)qt * kQM + row < p.m;
+        float lo = live_q ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
+        if (tt >= 1) {
+          const int u = it - (tt == 1 ? 1 : 2);
+          ok = ok && tc::mbar_wait(&maskempty[u % kMaskSlots], (uint32_t)(u / kMaskSlots) & 1u, kWaitNs);
+          lo = *(volatile float *)&s_lo[row];
+        } else if (it >= kMaskSlots) {
+          const int u = it - kMaskSlots;
+          ok = ok && tc::mbar_wait(&maskempty[u % kMaskSlots], (uint32_t)(u / kMaskSlots) & 1u, kWaitNs);
+        }
+        if (!__all_sync(0xffffffffu, ok) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
+          atomicExch(s_abort, 1);
+          stop = true;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t tbase = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(g * TN);
+        const uint32_t taddr = tbase + (uint32_t)c_lo;
+        uint32_t *mrow = sMask + ((size_t)slot * kQM + row) * kWords + c_lo / 32;
+        const int64_t j0 = (int64_t)tt * TN + c_lo;
+        float lo_rest = lo;  // threshold for the rows after the tile's first 32
+        if (tt == 0 && p.k <= 32) {
+          // No heap yet.  Once any k rows have been seen the root is at most
+          // the largest of their distances, so every row after the first 32
+          // needs acc_j > (k-th largest acc of those 32) - e: |acc - (||q||^2 -
+          // D)/2| <= e/2 for both rows.  The 1% margin covers the f32 rounding.
+          uint32_t v[32];
+          tc::tmem_ld32(tbase, v);
+          tc::tmem_wait_ld();
+          float top[32];
+          int nt = 0;
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj) {  // k largest, descending (insertion)
+            float x = __uint_as_float(v[jj]);
+            if (nt < p.k) ++nt;
+            else if (!(x > top[nt - 1])) continue;
+            int pos = nt - 1;
+            while (pos > 0 && top[pos - 1] < x) { top[pos] = top[pos - 1]; --pos; }
+            top[pos] = x;
+          }
+          const int64_t q = (int64_t)qt * kQM + row;
+          const float tmax = __uint_as_float(*p.tmax);
+          const float qn = q < p.m ? p.qnrm[q] : 0.f;
+          const float eq = 1.05f * (2.f * (p.coef_xc * qn * tmax + p.coef_cc * tmax * tmax) +
+                                    p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
+          lo_rest = live_q && p.n >= 32 ? top[p.k - 1] - 1.01f * eq - 1e-30f : lo;
+        }
+#pragma unroll
+        for (int c0 = 0; c0 < kCols; c0 += 32) {
+          uint32_t v[32];
+          tc::tmem_ld32(taddr + (uint32_t)c0, v);
+          tc::tmem_wait_ld();
+          if (c_lo + c0 >= 32) lo = lo_rest;
+          float mx = __uint_as_float(v[0]);
+#pragma unroll
+          for (int jj = 1; jj < 32; ++jj) mx = fmaxf(mx, __uint_as_float(v[jj]));
+          uint32_t mask = 0u;
+          if (__any_sync(0xffffffffu, mx >= lo)) {
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) mask |= (__uint_as_float(v[jj]) >= lo ? 1u : 0u) << jj;
+            const int64_t rem = p.n - (j0 + c0);  // rows past the end of the training set
+            if (rem < 32) mask &= rem <= 0 ? 0u : ((1u << rem) - 1u);
+          }
+          mrow[c0 / 32] = mask;
+        }
+        tc::fence_before_sync();
+        tc::mbar_arrive(&accempty[g]);
+        tc::mbar_arrive(&maskfull[slot]);
+      }
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 1) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tmem, 2 * kTN);
+    tc::tmem_dealloc(tmem, 2 * TN);
   }
   if (threadIdx.x == 0 && *s_abort) atomicExch(p.err, 4);
 }
@@ -430,9 +549,27 @@ void dfr(T *&p) {
 
 int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
 
-size_t knn_smem(int nkt, int row_bytes, int stages) {
-  return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * kTN * row_bytes + kTN * 32) +
-         4 * kQueue * 4 + (size_t)(2 * stages + 8) * 8 + 16;
+// Training rows per tile: 256 up to d = 32, then narrower so that the
+// resident query tile and two or more training stages fit in shared memory.
+int knn_tile_n(int d_pad) { return d_pad <= 32 ? 256 : d_pad <= 64 ? 128 : 64; }
+
+size_t knn_smem(int nkt, int row_bytes, int stages, int tn) {
+  return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * tn * row_bytes + tn * 32) +
+         (size_t)kOwnerWarps * kQueue * 4 + (size_t)kMaskSlots * kQM * (tn / 32) * 4 + kQM * 4 +
+         (size_t)kOwnerWarps * 32 * 16 +
+         (size_t)(2 * stages + 7 + 2 * kMaskSlots) * 8 + 16;
+}
+
+template <typename T, int TN>
+sc_status launch_knn_split(int grid, size_t smem, const CUtensorMap &tm_qh, const CUtensorMap &tm_ql,
+                           const SplitKnnState *s, const void *train, const void *queries, const KnnParams &p,
+                           cudaStream_t st) {
+  auto kern = knn_split_kernel<T, TN>;
+  SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, (const T *)train,
+                                        (const T *)queries, p);
+  SC_LAUNCHED();
+  return SC_OK;
 }
 
 }  // namespace
@@ -447,9 +584,10 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   }
   const int d_pad = knn_pad_d(d);
   const int kt_elems = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt_elems, row_bytes = kt_elems * 2;
-  int stages = 6;
-  while (stages > 2 && knn_smem(nkt, row_bytes, stages) > 227 * 1024) --stages;
-  const size_t smem = knn_smem(nkt, row_bytes, stages);
+  const int tn = knn_tile_n(d_pad);
+  int stages = 4;
+  while (stages > 2 && knn_smem(nkt, row_bytes, stages, tn) > 227 * 1024) --stages;
+  const size_t smem = knn_smem(nkt, row_bytes, stages, tn);
   if (d_pad > 256 || smem > 227 * 1024) {
     set_error("d=%d exceeds the split-BF16 kNN kernel's shared memory", d);
     return SC_ERR_INVALID;
@@ -457,7 +595,7 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   int dev = 0;
   SC_CUDA(cudaGetDevice(&dev));
   if (!s->num_sms) SC_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
-  const int64_t n_pad = (n + kTN - 1) / kTN * kTN;
+  const int64_t n_pad = (n + tn - 1) / tn * tn;
   if (!s->ready || s->train != train || s->n != n || s->d != d) {  // training operand, once per handle
     dfr(s->th); dfr(s->tl); dfr(s->tbx); dfr(s->tmax); dfr(s->ones);
     SC_TRY(dal(&s->th, (size_t)n_pad * d_pad));
@@ -477,9 +615,9 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
       knn_prep_kernel<double><<<nb, 256, 0, st>>>((const double *)train, n, n_pad, d, d_pad, s->th, s->tl,
                                                  nullptr, nullptr, nullptr, s->tmax, s->tbx);
     SC_LAUNCHED();
-    SC_TRY(map2d(&s->tm_th, s->th, n_pad, d_pad, kt_elems, kTN, row_bytes));
-    SC_TRY(map2d(&s->tm_tl, s->tl, n_pad, d_pad, kt_elems, kTN, row_bytes));
-    SC_TRY(map2d(&s->tm_tbx, s->tbx, n_pad, 16, 16, kTN, 32));
+    SC_TRY(map2d(&s->tm_th, s->th, n_pad, d_pad, kt_elems, tn, row_bytes));
+    SC_TRY(map2d(&s->tm_tl, s->tl, n_pad, d_pad, kt_elems, tn, row_bytes));
+    SC_TRY(map2d(&s->tm_tbx, s->tbx, n_pad, 16, 16, tn, 32));
     s->train = train;
     s->n = n;
     s->d = d;
@@ -511,7 +649,7 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   memset(&p, 0, sizeof p);
   p.n = n;
   p.m = m;
-  p.n_tiles_t = (int)(n_pad / kTN);
+  p.n_tiles_t = (int)(n_pad / tn);
   p.n_tiles_q = (int)(m_pad / kQM);
   p.nkt = nkt;
   p.kt_elems = kt_elems;
@@ -533,18 +671,16 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   p.evals = s->evals;
   p.err = (int *)(s->evals + 1);
   const int grid = p.n_tiles_q < s->num_sms ? p.n_tiles_q : s->num_sms;
-  if (dtype == SC_F32) {
-    auto kern = knn_split_kernel<float>;
-    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, (const float *)train,
-                                          (const float *)queries, p);
-  } else {
-    auto kern = knn_split_kernel<double>;
-    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, (const double *)train,
-                                          (const double *)queries, p);
-  }
-  SC_LAUNCHED();
+  sc_status r;
+  if (dtype == SC_F32)
+    r = tn == 256 ? launch_knn_split<float, 256>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)
+      : tn == 128 ? launch_knn_split<float, 128>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)
+                  : launch_knn_split<float, 64>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st);
+  else
+    r = tn == 256 ? launch_knn_split<double, 256>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)
+      : tn == 128 ? launch_knn_split<double, 128>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)
+                  : launch_knn_split<double, 64>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st);
+  SC_TRY(r);
   unsigned long long host[2];
   SC_CUDA(cudaMemcpyAsync(host, s->evals, sizeof host, cudaMemcpyDeviceToHost, st));
   SC_CUDA(cudaStreamSynchronize(st));

@@ -11,7 +11,7 @@ import oracle
 from smartcore_gb300 import _lib
 from smartcore_gb300.cluster import KMeans, KMeansHandle, KMeansParameters, kmeanspp_draws
 from smartcore_gb300.linalg import DenseMatrix
-from tests.datagen import blobs, kmeans_small_f64
+from tests.datagen import batched_problems, blobs, kmeans_small_f64
 
 pytestmark = pytest.mark.gpu
 
@@ -111,6 +111,21 @@ def test_predict_ties_lowest_index():
     got = km.predict(x)
     assert np.array_equal(got, oracle.kmeans_predict(x, c))
     assert not np.any(got == 2) and not np.any(got == 3)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_plain_kmeans_10k_x16_k8(form):
+    # the plain-KMeans workload: 8 blobs, 10,000 x 16 f64, k = 8, max_iter = 100, seed 42
+    x, _ = kmeans_small_f64(42)
+    assert_fit_parity(x, 8, 100, 42, form)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_independent_small_problems(form):
+    # the first 8 of the 512-problem workload: n log-uniform in [1e3, 1e5],
+    # d in {8, 16, 32, 64}, k in [4, 64], max_iter = 30, f32
+    for x, k, seed in batched_problems(count=8):
+        assert_fit_parity(x, k, 30, seed, form)
 
 
 @pytest.mark.parametrize("form", FORMS)

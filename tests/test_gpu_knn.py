@@ -31,6 +31,20 @@ def test_find_heap_order(form, dtype, k):
 
 
 @pytest.mark.parametrize("form", FORMS)
+def test_find_d128_k10(form):
+    # the shape of the large kNN workload (d = 128, k = 10) at a reduced size
+    rng = np.random.default_rng(128)
+    centres = rng.uniform(-50, 50, size=(64, 128))
+    train = (centres[rng.integers(0, 64, 20000)] + rng.normal(scale=2.0, size=(20000, 128))).astype(np.float32)
+    q = (centres[rng.integers(0, 64, 400)] + rng.normal(scale=2.0, size=(400, 128))).astype(np.float32)
+    s = LinearKNNSearch(train, form=form)
+    idx, dist = s.find_batch(q, 10)
+    ridx, rdist = oracle.knn_find(train, q, 10)
+    assert np.array_equal(idx, ridx)
+    assert np.array_equal(dist, rdist)
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_find_ties_and_duplicates(form):
     # integer grid data: many exact distance ties, replay order matters
     rng = np.random.default_rng(0)
