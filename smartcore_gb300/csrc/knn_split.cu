@@ -27,7 +27,7 @@ namespace {
 
 constexpr int kQM = 128;         // queries per tile (UMMA M)
 constexpr int kOwnerWarps = 4;   // one query per thread: heap, exact replay
-constexpr int kFilterWarps = 16; // 2 accumulator buffers x 2 column halves x 4 TMEM lane quarters
+constexpr int kFilterWarps = 8;  // 2 accumulator buffers x 4 TMEM lane quarters
 constexpr int kKnnThreads = 32 * (2 + kOwnerWarps + kFilterWarps);  // + warp 0 TMA, warp 1 MMA
 constexpr int kMaskSlots = 4;    // candidate-mask tiles between the filters and the owners
 constexpr uint64_t kWaitNs = 2000000000ull;
@@ -105,45 +105,67 @@ struct KnnParams {
   int *err;
 };
 
-__device__ __forceinline__ void heap_sift(double *hd, double *hD, int32_t *hi, int kk, int nn) {
-  // sift_down of heap_select.rs:71-86 (on the distances): node kk has children 2kk and 2kk+1.
-  // Distances are >= 0 or +inf, so their bit patterns order as their values:
-  // the comparisons run on the integer pipe.
+// The reference keys its heap on d = sqrt(D) (f64).  The heap here holds D
+// itself: correctly rounded sqrt is monotone, so sqrt(a) < sqrt(b) exactly
+// when a < b, except that values a few ulps apart may round to the same
+// sqrt.  Keys are >= 0 or +inf, so their bit patterns order as their values
+// (integer compares); only keys within 8 ulps take the two square roots.
+__device__ __forceinline__ bool sqrt_less(double a, double b) {
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  if (ia >= ib) return false;
+  if (ib - ia > 8) return true;
+  return __dsqrt_rn(a) < __dsqrt_rn(b);
+}
+
+// sift_down of heap_select.rs:71-86 on the distances: node kk has children 2kk
+// and 2kk+1.  Heap entry e of a query lives at [e * S]: S = 1 for a
+// per-thread array, S = 128 for the shared-memory heaps of a query tile.
+template <int S>
+__device__ __forceinline__ void heap_sift(double *hD, int32_t *hi, int kk, int nn) {
   while (2 * kk <= nn) {
     int j = 2 * kk;
-    if (j < nn && __double_as_longlong(hd[j]) < __double_as_longlong(hd[j + 1])) ++j;
-    const double a = hd[kk], b = hd[j];
-    if (__double_as_longlong(a) >= __double_as_longlong(b)) break;
+    if (j < nn && sqrt_less(hD[j * S], hD[(j + 1) * S])) ++j;
+    const double a = hD[kk * S], b = hD[j * S];
+    if (!sqrt_less(a, b)) break;  // a == b || a > b
     if (j == kk) break;
-    hd[kk] = b;
-    hd[j] = a;
-    const double t2 = hD[kk];
-    hD[kk] = hD[j];
-    hD[j] = t2;
-    const int32_t t = hi[kk];
-    hi[kk] = hi[j];
-    hi[j] = t;
+    hD[kk * S] = b;
+    hD[j * S] = a;
+    const int32_t t = hi[kk * S];
+    hi[kk * S] = hi[j * S];
+    hi[j * S] = t;
     kk = j;
   }
 }
 
-// Threshold on a_j below which a row may enter the heap: root^2 - ||q||^2 + E,
-// rounded up (a larger threshold only admits more rows to the exact test).
-__device__ __forceinline__ float knn_threshold(double root, double qn2, float eq) {
-  if (!(root < DBL_MAX)) return __int_as_float(0x7f800000);
-  const double r2 = root * root * (1.0 + 0x1p-50);
-  return __double2float_ru(r2 - qn2 + (double)eq + 1e-300);
+// Pulls training row j toward L1 when it is queued, tiles before its exact
+// distance is computed.
+template <typename T>
+__device__ __forceinline__ void prefetch_row(const T *train, int64_t j, int d) {
+  const char *a = (const char *)(train + j * (int64_t)d);
+  const char *b = a + (size_t)d * sizeof(T) - 1;
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+  if (((uintptr_t)a >> 7) != ((uintptr_t)b >> 7)) asm volatile("prefetch.global.L1 [%0];" ::"l"(b));
+}
+
+// Threshold on a_j below which a row may enter the heap: D_root - ||q||^2 + E,
+// rounded up (a larger threshold only admits more rows to the exact test),
+// in f32 with a margin of 2^-22 (D_root + ||q||^2) for the f32 roundings.
+__device__ __forceinline__ float knn_threshold(double droot, double qn2, float eq) {
+  if (!(droot < DBL_MAX)) return __int_as_float(0x7f800000);
+  const float r = __double2float_ru(droot), qf = __double2float_rd(qn2);
+  return __fadd_ru(__fadd_ru(__fsub_ru(r, qf), eq), __fmul_ru(0x1p-22f, __fadd_ru(r, qf)));
 }
 
 // Roles: warp 0 TMA (query tile once, training tiles in index order), warp 1
 // MMA (one elected thread), warps 2-5 owners (one query per thread: the
-// reference heap, replayed exactly in index order), warps 6-21 filters.  A
-// filter warp reads its accumulator buffer's TMEM lanes for one column half
-// and writes, per query, the bit mask of the rows a certified bound cannot
-// exclude; the owners consume the masks of each tile in order.  A filter may
+// reference heap, replayed exactly in index order), warps 6-13 filters.  A
+// filter warp reads its accumulator buffer's TMEM lanes (32 queries, every
+// column of the tile) and writes, per query, the bit mask of the rows a
+// certified bound cannot exclude; the owners consume the masks of each tile
+// in order.  A filter may
 // use a threshold up to two tiles stale: the heap root only decreases, so a
 // staler threshold admits more rows, never fewer.
-template <typename T, int TN>
+template <typename T, int TN, bool SH>
 __global__ void __launch_bounds__(kKnnThreads, 1)
 knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constant__ CUtensorMap tm_ql,
                  const __grid_constant__ CUtensorMap tm_th, const __grid_constant__ CUtensorMap tm_tl,
@@ -165,7 +187,9 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   double *s_rs = (double *)(s_lo + kQM);                          // owner warps x 32: round distances
   int32_t *s_rj = (int32_t *)(s_rs + kOwnerWarps * 32);            //   rows
   uint32_t *s_rg = (uint32_t *)(s_rj + kOwnerWarps * 32);          //   entries per owner lane
-  uint64_t *bars = (uint64_t *)(s_rg + kOwnerWarps * 32);
+  double *s_hD = (double *)(s_rg + kOwnerWarps * 32);  // SH: heaps of the tile's queries, [k][128]
+  int32_t *s_hi = (int32_t *)(s_hD + (SH ? p.k * kQM : 0));
+  uint64_t *bars = (uint64_t *)(s_hi + (SH ? ((p.k * kQM + 1) & ~1) : 0));
   uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
   uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
   uint64_t *maskfull = afull + 7, *maskempty = maskfull + kMaskSlots;
@@ -289,8 +313,11 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     double *Rs = s_rs + (warp - 2) * 32;
     int32_t *Rj = s_rj + (warp - 2) * 32;
     uint32_t *Rg = s_rg + (warp - 2) * 32;
-    double hd[kMaxKnnK], hD[kMaxKnnK];  // heap distances and their squares
-    int32_t hi[kMaxKnnK];
+    constexpr int HS = SH ? kQM : 1;  // heap entry stride
+    double hD_l[SH ? 1 : kMaxKnnK];   // heap keys: the squared distances D
+    int32_t hi_l[SH ? 1 : kMaxKnnK];
+    double *hD = SH ? s_hD + row : hD_l;
+    int32_t *hi = SH ? s_hi + row : hi_l;
     unsigned long long evals = 0;
     int it = 0;
     bool stop = false;
@@ -298,8 +325,8 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       const int64_t q = (int64_t)qt * kQM + row;
       const bool live = q < p.m;
       for (int s = 0; s < p.k; ++s) {
-        hd[s] = hD[s] = __longlong_as_double(0x7ff0000000000000ll);
-        hi[s] = -1;
+        hD[s * HS] = __longlong_as_double(0x7ff0000000000000ll);
+        hi[s * HS] = -1;
       }
       const float qn = live ? p.qnrm[q] : 0.f;
       const double qn2 = live ? p.qn2[q] : 0.0;
@@ -320,9 +347,15 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         if ((uint32_t)lane < cnt && qbase + owner < p.m) {
           const T *tr = train + j * (int64_t)p.d;
           const T *qrow = queries + (qbase + owner) * (int64_t)p.d;
-          bool exact = false;
-          if constexpr (sizeof(T) == 4) exact = sqd_exact_f32(qrow, tr, p.d, p.lg_d, sq);
-          if (!exact) {
+          bool done = false;
+          if constexpr (sizeof(T) == 4) {
+            if (p.d <= 32) {
+              done = sqd_seq_f32_d32((const float *)qrow, (const float *)tr, p.d, p.lg_d, sq);
+            } else {
+              done = sqd_exact_f32(qrow, tr, p.d, p.lg_d, sq);
+            }
+          }
+          if (!done) {
             sq = 0.0;
             for (int t = 0; t < p.d; ++t) sq = __dadd_rn(sq, ref_term(qrow[t], tr[t]));
           }
@@ -341,17 +374,12 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         for (uint32_t mine = Rg[lane]; mine; mine &= mine - 1u) {
           const int r = __ffs(mine) - 1;
           const double sr = Rs[r];
-          // sqrt is monotone: sq >= root^2 means sqrt(sq) >= root, no entry
-          if (__double_as_longlong(sr) < __double_as_longlong(hD[0])) {
-            const double dist = __dsqrt_rn(sr);
-            if (__double_as_longlong(dist) < __double_as_longlong(hd[0])) {  // dist < root (linear_search.rs:72)
-              hd[0] = dist;
-              hD[0] = sr;
-              hi[0] = Rj[r];
-              if (p.k > 1)
-                for (int s2 = p.k / 2 - 1; s2 >= 0; --s2) heap_sift(hd, hD, hi, s2, p.k - 1);
-              lo = -0.5f * knn_threshold(hd[0], qn2, eq);
-            }
+          if (sqrt_less(sr, hD[0])) {  // sqrt(D) < root (linear_search.rs:72)
+            hD[0] = sr;
+            hi[0] = Rj[r];
+            if (p.k > 1)
+              for (int s2 = p.k / 2 - 1; s2 >= 0; --s2) heap_sift<HS>(hD, hi, s2, p.k - 1);
+            lo = -0.5f * knn_threshold(hD[0], qn2, eq);
           }
         }
         __syncwarp();
@@ -369,13 +397,39 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         }
         const uint32_t *mrow = sMask + ((size_t)slot * kQM + row) * kWords;
         const int64_t j0 = (int64_t)tt * TN;
+        uint32_t mw[kWords], mcnt = 0u;
 #pragma unroll
         for (int w = 0; w < kWords; ++w) {
-          const uint32_t mw = mrow[w];
-          if (!__any_sync(0xffffffffu, mw != 0u)) continue;
+          mw[w] = mrow[w];
+          mcnt += __popc(mw[w]);
+        }
+        const uint32_t mtotal = __reduce_add_sync(0xffffffffu, mcnt);
+        if (mtotal != 0u && mtotal <= (uint32_t)(kQueue - 32)) {
+          // the whole tile at once: one scan, entries in index order per owner
+          uint32_t incl = mcnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          uint32_t pos = qtail + incl - mcnt;
+#pragma unroll
+          for (int w = 0; w < kWords; ++w)
+            for (uint32_t m = mw[w]; m; m &= m - 1) {
+              const int64_t jr = j0 + 32 * w + __ffs(m) - 1;
+              prefetch_row(train, jr, p.d);
+              Q[(pos++) & (kQueue - 1)] = ((uint32_t)lane << kRowBits) | (uint32_t)jr;
+            }
+          qtail += mtotal;
+          __syncwarp();
+          while (qtail - qhead >= 32) round(32);
+        }
+#pragma unroll
+        for (int w = 0; w < kWords && mtotal > (uint32_t)(kQueue - 32); ++w) {  // rare: a tile too large for the ring
+          if (!__any_sync(0xffffffffu, mw[w] != 0u)) continue;
 #pragma unroll
           for (int half = 0; half < 2; ++half) {  // <= 32 x 16 new entries per step: the ring never overflows
-            const uint32_t mask = (mw >> (16 * half)) & 0xffffu;
+            const uint32_t mask = (mw[w] >> (16 * half)) & 0xffffu;
             const uint32_t cnt = __popc(mask);
             const uint32_t total = __reduce_add_sync(0xffffffffu, cnt);
             if (total == 0) continue;
@@ -386,9 +440,11 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
               if (lane >= o) incl += y;
             }
             uint32_t pos = qtail + incl - cnt;
-            for (uint32_t m = mask; m; m &= m - 1)
-              Q[(pos++) & (kQueue - 1)] =
-                  ((uint32_t)lane << kRowBits) | (uint32_t)(j0 + 32 * w + 16 * half + __ffs(m) - 1);
+            for (uint32_t m = mask; m; m &= m - 1) {
+              const int64_t jr = j0 + 32 * w + 16 * half + __ffs(m) - 1;
+              prefetch_row(train, jr, p.d);
+              Q[(pos++) & (kQueue - 1)] = ((uint32_t)lane << kRowBits) | (uint32_t)jr;
+            }
             qtail += total;
             __syncwarp();
             while (qtail - qhead >= 32) round(32);
@@ -400,18 +456,18 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       while (!stop && qtail != qhead) round(min(32u, qtail - qhead));
       if (live && !stop)
         for (int s = 0; s < p.k; ++s) {
-          p.idx_out[q * p.k + s] = hi[s];
-          p.dist_out[q * p.k + s] = hd[s];
+          p.idx_out[q * p.k + s] = hi[s * HS];
+          p.dist_out[q * p.k + s] = __dsqrt_rn(hD[s * HS]);  // sqrt(+inf) = +inf for an empty slot
         }
     }
     if (evals) atomicAdd(p.evals, evals);
   } else {
     // ---------------- filters: candidate masks from TMEM ----------------
-    const int f = warp - 2 - kOwnerWarps;  // 0 .. 15
-    const int g = (f >> 2) & 1, h = f >> 3, lq = warp & 3;
+    const int f = warp - 2 - kOwnerWarps;  // 0 .. 7
+    const int g = f >> 2, lq = warp & 3;
     const int row = lq * 32 + lane;
-    constexpr int kCols = TN / 2;
-    const int c_lo = h * kCols;
+    constexpr int kCols = TN;
+    constexpr int c_lo = 0;
     int it = 0;
     bool stop = false;
     for (int qt = blockIdx.x; !stop && qt < p.n_tiles_q; qt += gridDim.x) {
@@ -470,22 +526,26 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
           lo_rest = live_q && p.n >= 32 ? top[p.k - 1] - 1.01f * eq - 1e-30f : lo;
         }
 #pragma unroll
-        for (int c0 = 0; c0 < kCols; c0 += 32) {
-          uint32_t v[32];
-          tc::tmem_ld32(taddr + (uint32_t)c0, v);
+        for (int c1 = 0; c1 < kCols; c1 += 64) {  // 64 columns per TMEM round trip
+          uint32_t v[64];
+          tc::tmem_ld64(taddr + (uint32_t)c1, v);
           tc::tmem_wait_ld();
-          if (c_lo + c0 >= 32) lo = lo_rest;
-          float mx = __uint_as_float(v[0]);
 #pragma unroll
-          for (int jj = 1; jj < 32; ++jj) mx = fmaxf(mx, __uint_as_float(v[jj]));
-          uint32_t mask = 0u;
-          if (__any_sync(0xffffffffu, mx >= lo)) {
+          for (int c2 = 0; c2 < 64; c2 += 32) {
+            const int c0 = c1 + c2;
+            if (c_lo + c0 >= 32) lo = lo_rest;
+            float mx = __uint_as_float(v[c2]);
 #pragma unroll
-            for (int jj = 0; jj < 32; ++jj) mask |= (__uint_as_float(v[jj]) >= lo ? 1u : 0u) << jj;
-            const int64_t rem = p.n - (j0 + c0);  // rows past the end of the training set
-            if (rem < 32) mask &= rem <= 0 ? 0u : ((1u << rem) - 1u);
+            for (int jj = 1; jj < 32; ++jj) mx = fmaxf(mx, __uint_as_float(v[c2 + jj]));
+            uint32_t mask = 0u;
+            if (__any_sync(0xffffffffu, mx >= lo)) {
+#pragma unroll
+              for (int jj = 0; jj < 32; ++jj) mask |= (__uint_as_float(v[c2 + jj]) >= lo ? 1u : 0u) << jj;
+              const int64_t rem = p.n - (j0 + c0);  // rows past the end of the training set
+              if (rem < 32) mask &= rem <= 0 ? 0u : ((1u << rem) - 1u);
+            }
+            mrow[c0 / 32] = mask;
           }
-          mrow[c0 / 32] = mask;
         }
         tc::fence_before_sync();
         tc::mbar_arrive(&accempty[g]);
@@ -553,18 +613,18 @@ int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; 
 // resident query tile and two or more training stages fit in shared memory.
 int knn_tile_n(int d_pad) { return d_pad <= 32 ? 256 : d_pad <= 64 ? 128 : 64; }
 
-size_t knn_smem(int nkt, int row_bytes, int stages, int tn) {
+size_t knn_smem(int nkt, int row_bytes, int stages, int tn, int heap_k) {
   return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * tn * row_bytes + tn * 32) +
          (size_t)kOwnerWarps * kQueue * 4 + (size_t)kMaskSlots * kQM * (tn / 32) * 4 + kQM * 4 +
-         (size_t)kOwnerWarps * 32 * 16 +
+         (size_t)kOwnerWarps * 32 * 16 + (size_t)heap_k * kQM * 12 + 8 +
          (size_t)(2 * stages + 7 + 2 * kMaskSlots) * 8 + 16;
 }
 
-template <typename T, int TN>
+template <typename T, int TN, bool SH>
 sc_status launch_knn_split(int grid, size_t smem, const CUtensorMap &tm_qh, const CUtensorMap &tm_ql,
                            const SplitKnnState *s, const void *train, const void *queries, const KnnParams &p,
                            cudaStream_t st) {
-  auto kern = knn_split_kernel<T, TN>;
+  auto kern = knn_split_kernel<T, TN, SH>;
   SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<grid, kKnnThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, (const T *)train,
                                         (const T *)queries, p);
@@ -585,9 +645,12 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   const int d_pad = knn_pad_d(d);
   const int kt_elems = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt_elems, row_bytes = kt_elems * 2;
   const int tn = knn_tile_n(d_pad);
+  // heaps in shared memory when they fit beside at least two training stages
+  bool sh = knn_smem(nkt, row_bytes, 2, tn, k) <= 227 * 1024;
+  const int heap_k = sh ? k : 0;
   int stages = 4;
-  while (stages > 2 && knn_smem(nkt, row_bytes, stages, tn) > 227 * 1024) --stages;
-  const size_t smem = knn_smem(nkt, row_bytes, stages, tn);
+  while (stages > 2 && knn_smem(nkt, row_bytes, stages, tn, heap_k) > 227 * 1024) --stages;
+  const size_t smem = knn_smem(nkt, row_bytes, stages, tn, heap_k);
   if (d_pad > 256 || smem > 227 * 1024) {
     set_error("d=%d exceeds the split-BF16 kNN kernel's shared memory", d);
     return SC_ERR_INVALID;
@@ -672,14 +735,14 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   p.err = (int *)(s->evals + 1);
   const int grid = p.n_tiles_q < s->num_sms ? p.n_tiles_q : s->num_sms;
   sc_status r;
+#define SC_KNN_LAUNCH(TT, NN)                                                                        \
+  (sh ? launch_knn_split<TT, NN, true>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)            \
+      : launch_knn_split<TT, NN, false>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st))
   if (dtype == SC_F32)
-    r = tn == 256 ? launch_knn_split<float, 256>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)
-      : tn == 128 ? launch_knn_split<float, 128>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)
-                  : launch_knn_split<float, 64>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st);
+    r = tn == 256 ? SC_KNN_LAUNCH(float, 256) : tn == 128 ? SC_KNN_LAUNCH(float, 128) : SC_KNN_LAUNCH(float, 64);
   else
-    r = tn == 256 ? launch_knn_split<double, 256>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)
-      : tn == 128 ? launch_knn_split<double, 128>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)
-                  : launch_knn_split<double, 64>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st);
+    r = tn == 256 ? SC_KNN_LAUNCH(double, 256) : tn == 128 ? SC_KNN_LAUNCH(double, 128) : SC_KNN_LAUNCH(double, 64);
+#undef SC_KNN_LAUNCH
   SC_TRY(r);
   unsigned long long host[2];
   SC_CUDA(cudaMemcpyAsync(host, s->evals, sizeof host, cudaMemcpyDeviceToHost, st));

@@ -51,3 +51,57 @@ def test_shortcut_matches_sequential_sum():
             used += 1
             assert got == reference(a, b)
     assert used > 1000
+
+
+def seq_rounding(a, b):
+    """Model of sqd_seq_f32_d32: exact integer running sum of the f32 squares
+    in units of 2^(emin - 150), rounded to 53 significant bits (nearest, ties
+    to even) after every term, as each f64 addition rounds; the span limit
+    38 - ceil(log2 d) keeps the sum below 2^63."""
+    q = (a.astype(np.float32) - b.astype(np.float32)).astype(np.float32)
+    q = (q * q).astype(np.float32)
+    bits = q.view(np.uint32)
+    nz = bits[bits != 0]
+    if len(nz) == 0:
+        return 0.0
+    e_all = np.maximum(nz >> 23, 1).astype(np.int64)
+    emin, emax = int(e_all.min()), int(e_all.max())
+    lg_d = max(0, math.ceil(math.log2(len(a)))) if len(a) > 1 else 0
+    if emax >= 255 or emax - emin > 38 - lg_d:
+        return None
+    S = 0
+    for u in bits:
+        u = int(u)
+        if u == 0:
+            continue
+        e = u >> 23
+        m = (u & 0x7FFFFF) | (0x800000 if e else 0)
+        S += m << (max(e, 1) - emin)
+        assert S < 2 ** 63
+        if S >> 53:
+            drop = S.bit_length() - 53
+            half = 1 << (drop - 1)
+            rem = S & ((half << 1) - 1)
+            qv = S >> drop
+            if rem > half or (rem == half and (qv & 1)):
+                qv += 1
+            S = qv << drop
+    return math.ldexp(float(S), emin - 150)
+
+
+def test_sequential_rounding_matches_sequential_sum():
+    rng = np.random.default_rng(1)
+    used = 0
+    for trial in range(4000):
+        d = int(rng.integers(1, 33))
+        span = rng.uniform(0, 7)
+        scale = 10.0 ** rng.uniform(-span, span, size=d)
+        a = (rng.normal(size=d) * scale).astype(np.float32)
+        b = (rng.normal(size=d) * scale).astype(np.float32)
+        if trial % 5 == 0:
+            b = (a * np.float32(1.0 + 1e-6)).astype(np.float32)  # near-duplicates: tiny terms
+        got = seq_rounding(a, b)
+        if got is not None:
+            used += 1
+            assert got == reference(a, b), (trial, got, reference(a, b))
+    assert used > 1500

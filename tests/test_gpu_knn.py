@@ -45,6 +45,23 @@ def test_find_d128_k10(form):
 
 
 @pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("d", [16, 32])
+def test_find_wide_exponent_span(form, d):
+    # features scaled from 1e-3 to 1e3: the squared terms of one distance span
+    # up to ~40 bits, so every path of the exact sequential f64 sum is taken
+    rng = np.random.default_rng(d)
+    scale = np.logspace(-3, 3, d)
+    train = (rng.normal(size=(6000, d)) * scale).astype(np.float32)
+    q = (rng.normal(size=(300, d)) * scale).astype(np.float32)
+    q[:40] = train[rng.integers(0, 6000, 40)] * np.float32(1.0 + 1e-6)  # near-duplicates
+    s = LinearKNNSearch(train, form=form)
+    idx, dist = s.find_batch(q, 7)
+    ridx, rdist = oracle.knn_find(train, q, 7)
+    assert np.array_equal(idx, ridx)
+    assert np.array_equal(dist, rdist)
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_find_ties_and_duplicates(form):
     # integer grid data: many exact distance ties, replay order matters
     rng = np.random.default_rng(0)
