@@ -109,8 +109,8 @@ struct AssignParams {
   int region;                // near-tie list entries reserved per CTA
   unsigned int *list_count;  // near-tie rows listed by each CTA
   int64_t *list_rows;        //   CTA b's rows at [b * region, ...)
-  uint32_t *cand4;           // [2 halves][n_pad]: up to 4 candidate columns of a listed row (bytes)
-  uint8_t *cmeta;            // [2 halves][n_pad]: bits 0-3 valid bytes of cand4, bit 4 list complete
+  uint2 *cand4;              // [2 halves][n_pad]: up to 4 candidate columns of a listed row (16 bits each)
+  uint8_t *cmeta;            // [2 halves][n_pad]: bits 0-3 valid columns of cand4, bit 4 list complete
   LloydState *st;
 };
 
@@ -357,13 +357,13 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
         // candidate; when every tracker's is, the maxima above the threshold
         // are this half's complete candidate list.
         const float thr = b1 - 1.05f * e;
-        uint32_t cw = 0u, meta = 16u;
+        uint32_t cw[2] = {0u, 0u}, meta = 16u;
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-          if (m1[r] >= thr) { cw |= (uint32_t)mi[r] << (8 * r); meta |= 1u << r; }
+          if (m1[r] >= thr) { cw[r >> 1] |= (uint32_t)mi[r] << (16 * (r & 1)); meta |= 1u << r; }
           if (m2[r] >= thr) meta &= ~16u;
         }
-        p.cand4[(size_t)h * p.n_pad + i] = cw;
+        p.cand4[(size_t)h * p.n_pad + i] = make_uint2(cw[0], cw[1]);
         p.cmeta[(size_t)h * p.n_pad + i] = (uint8_t)meta;
       }
     }
@@ -376,6 +376,256 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
   }
   if (threadIdx.x == 0) p.list_count[blockIdx.x] = *s_nlist;
   if (threadIdx.x == 0 && *s_abort && p.st) atomicExch(&p.st->err, kErrTimeout);
+}
+
+// ---------------------------------------------------------------------------
+// K5b: assignment for many centroids (k_pad > 256, or centroids too large to
+// stay resident).  The point tile (both BF16 halves) stays in shared memory
+// while the centroids stream through a TMA ring in blocks of kWN; two TMEM
+// accumulators alternate between blocks, and epilogue warpgroup g (4 warps,
+// one row per thread) folds blocks b = g (mod 2) into its four trackers.  At
+// the end of a tile the two warpgroups merge their trackers and hand near
+// ties over exactly as split_assign_kernel's column halves do.
+// ---------------------------------------------------------------------------
+constexpr int kWN = 128;  // centroids per block (UMMA N)
+constexpr int kWideThreads = 64 + 32 * 8;
+
+__global__ void __launch_bounds__(kWideThreads, 1)
+split_wide_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
+                  const __grid_constant__ CUtensorMap tm_ch, const __grid_constant__ CUtensorMap tm_cl,
+                  const __grid_constant__ CUtensorMap tm_ones, const __grid_constant__ CUtensorMap tm_cbx,
+                  const AssignParams p) {
+  if (p.st && p.st->done) return;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int nblk = p.k_pad / kWN;
+  const int a_blk = kBM * p.row_bytes;   // one (part, k-tile) block of the point tile
+  const int a_bytes = 2 * p.nkt * a_blk;
+  const int b_blk = kWN * p.row_bytes;  // one (part, k-tile) block of a centroid block
+  const int b_stage = (2 * p.nkt * b_blk + kWN * 32 + 1023) & ~1023;
+  uint8_t *sA = base;
+  uint8_t *sOnes = sA + a_bytes;
+  uint8_t *sB = sOnes + 4096;
+  float *s_xch = (float *)(sB + (size_t)p.stages * b_stage);  // [2 warpgroups][128 rows][12]
+  uint64_t *bars = (uint64_t *)(s_xch + 2 * kBM * 12);
+  uint64_t *bfull = bars, *bempty = bars + p.stages, *afull = bars + 2 * p.stages;
+  uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
+  uint32_t *s_tmem = (uint32_t *)(afull + 7);
+  int *s_abort = (int *)(s_tmem + 1);
+  unsigned int *s_nlist = (unsigned int *)(s_abort + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < p.stages; ++s) {
+      tc::mbar_init(&bfull[s], 1);
+      tc::mbar_init(&bempty[s], 1);
+    }
+    tc::mbar_init(afull, 1);
+    tc::mbar_init(aempty, 1);
+    tc::mbar_init(mma_done, 1);
+    for (int a = 0; a < 2; ++a) {
+      tc::mbar_init(&accfull[a], 1);
+      tc::mbar_init(&accempty[a], 128);  // one warpgroup
+    }
+    *s_abort = 0;
+    *s_nlist = 0u;
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&tm_xh);
+    tc::prefetch_tmap(&tm_xl);
+    tc::prefetch_tmap(&tm_ch);
+    tc::prefetch_tmap(&tm_cl);
+    tc::prefetch_tmap(&tm_ones);
+    tc::prefetch_tmap(&tm_cbx);
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(s_tmem, 2 * kWN);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *s_tmem;
+
+  if (warp == 0) {
+    if (lane == 0) {  // ---------------- TMA producer ----------------
+      int it = 0, ti = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < p.n_tiles; t += gridDim.x, ++ti) {
+        if (!tc::mbar_wait(aempty, (uint32_t)(ti & 1) ^ 1u, kWaitNs)) { ok = false; break; }
+        tc::mbar_expect_tx(afull, (uint32_t)(a_bytes + (ti == 0 ? kBM * 32 : 0)));
+        for (int part = 0; part < 2; ++part)
+          for (int kt = 0; kt < p.nkt; ++kt)
+            tc::tma_load_2d(sA + (part * p.nkt + kt) * a_blk, part ? &tm_xl : &tm_xh, afull, kt * p.kt_elems,
+                            t * kBM);
+        if (ti == 0) tc::tma_load_2d(sOnes, &tm_ones, afull, 0, 0);
+        for (int b = 0; b < nblk; ++b, ++it) {
+          const int s = it % p.stages;
+          const uint32_t ph = (uint32_t)(it / p.stages) & 1u;
+          if (!tc::mbar_wait(&bempty[s], ph ^ 1u, kWaitNs) || *(volatile int *)s_abort) { ok = false; break; }
+          tc::mbar_expect_tx(&bfull[s], (uint32_t)(2 * p.nkt * b_blk + kWN * 32));
+          uint8_t *dst = sB + (size_t)s * b_stage;
+          for (int part = 0; part < 2; ++part)
+            for (int kt = 0; kt < p.nkt; ++kt)
+              tc::tma_load_2d(dst + (part * p.nkt + kt) * b_blk, part ? &tm_cl : &tm_ch, &bfull[s],
+                              kt * p.kt_elems, b * kWN);
+          tc::tma_load_2d(dst + 2 * p.nkt * b_blk, &tm_cbx, &bfull[s], 0, b * kWN);
+        }
+      }
+      if (!ok) atomicExch(s_abort, 1);
+      for (int j = (it > p.stages ? it - p.stages : 0); j < it; ++j)  // drain in-flight copies
+        tc::mbar_wait(&bfull[j % p.stages], (uint32_t)(j / p.stages) & 1u, kWaitNs);
+      if (ti > 0) tc::mbar_wait(afull, (uint32_t)((ti - 1) & 1), kWaitNs);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // ---------------- MMA issuer ----------------
+      const uint32_t idesc = tc::idesc_bf16_f32(kBM, kWN);
+      const uint32_t sA0 = tc::smem_u32(sA), sB0 = tc::smem_u32(sB);
+      const uint64_t ones_desc = tc::smem_desc(tc::smem_u32(sOnes), 32);
+      int it = 0, ti = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < p.n_tiles; t += gridDim.x, ++ti) {
+        if (!tc::mbar_wait(afull, (uint32_t)(ti & 1), kWaitNs)) { ok = false; break; }
+        for (int b = 0; b < nblk; ++b, ++it) {
+          const int s = it % p.stages, acc = it & 1;
+          const uint32_t ph = (uint32_t)(it / p.stages) & 1u, aph = (uint32_t)(it >> 1) & 1u;
+          if (!tc::mbar_wait(&accempty[acc], aph ^ 1u, kWaitNs) || !tc::mbar_wait(&bfull[s], ph, kWaitNs) ||
+              *(volatile int *)s_abort) {
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint32_t d_tmem = tmem + (uint32_t)(acc * kWN);
+          const uint32_t b0 = sB0 + (uint32_t)(s * b_stage);
+          // -||c||^2 / 2 first, then x_h.c_h + x_h.c_l + x_l.c_h
+          tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(2 * p.nkt * b_blk), 32), idesc, 0u);
+          for (int prod = 0; prod < 3; ++prod) {
+            const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
+            for (int kt = 0; kt < p.nkt; ++kt)
+              for (int ks = 0; ks < p.kt_elems / 16; ++ks) {
+                const uint64_t ad = tc::smem_desc(sA0 + (uint32_t)((pa * p.nkt + kt) * a_blk + ks * 32), p.row_bytes);
+                const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((pb * p.nkt + kt) * b_blk + ks * 32), p.row_bytes);
+                tc::mma_f16(d_tmem, ad, bd, idesc, 1u);
+              }
+          }
+          tc::mma_commit(&bempty[s]);
+          tc::mma_commit(&accfull[acc]);
+        }
+        if (!ok) break;
+        tc::mma_commit(aempty);  // the point tile's smem is free once these MMAs complete
+      }
+      if (!ok) atomicExch(s_abort, 1);
+      tc::mma_commit(mma_done);
+      tc::mbar_wait(mma_done, 0, kWaitNs);
+    }
+  } else {
+    // ---------------- epilogue: 2 warpgroups x 4 lane quarters ----------------
+    const int g = (warp - 2) >> 2, lq = warp & 3;
+    const int row = lq * 32 + lane;
+    const uint32_t bar_id = 1u + (uint32_t)lq;  // the two warps of this lane quarter
+    const float cmax = __uint_as_float(*p.cmax);
+    const float ninf = -__int_as_float(0x7f800000);
+    int it = 0;
+    for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
+      const int64_t i = (int64_t)t * kBM + row;
+      const bool live = i < p.n;
+      const float xn = live ? __ldg(p.xnrm + i) : 0.f;
+      float m1[4] = {ninf, ninf, ninf, ninf}, m2[4] = {ninf, ninf, ninf, ninf};
+      int mi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+      bool stop = false;
+      for (int b = 0; b < nblk; ++b, ++it) {
+        if ((it & 1) != g || stop) continue;
+        const bool got = tc::mbar_wait(&accfull[g], (uint32_t)(it >> 1) & 1u, kWaitNs);
+        if (!__all_sync(0xffffffffu, got) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
+          atomicExch(s_abort, 1);
+          stop = true;
+          continue;
+        }
+        tc::fence_after_sync();
+        const uint32_t taddr = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(g * kWN);
+#pragma unroll
+        for (int c1 = 0; c1 < kWN; c1 += 64) {
+          uint32_t v[64];
+          tc::tmem_ld64(taddr + (uint32_t)c1, v);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int jj = 0; jj < 64; jj += 4) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              const float x = __uint_as_float(v[jj + r]);
+              const bool gt = x > m1[r];
+              m2[r] = gt ? m1[r] : fmaxf(m2[r], x);
+              mi[r] = gt ? b * kWN + c1 + jj + r : mi[r];
+              m1[r] = gt ? x : m1[r];
+            }
+          }
+        }
+        tc::fence_before_sync();
+        tc::mbar_arrive(&accempty[g]);
+      }
+      // merge the two warpgroups' trackers (warpgroup 0's first, in both)
+      float *mine = s_xch + ((size_t)g * kBM + row) * 12;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        mine[r] = m1[r];
+        mine[4 + r] = m2[r];
+        mine[8 + r] = __int_as_float(mi[r]);
+      }
+      if (tc::bar_red_or(stop || *(volatile int *)s_abort != 0, bar_id, 64)) break;  // uniform over the pair
+      const float *w0 = s_xch + (size_t)row * 12, *w1 = s_xch + ((size_t)kBM + row) * 12;
+      float b1 = w0[0], b2 = w0[4];
+      int ba = __float_as_int(w0[8]);
+#pragma unroll
+      for (int r = 1; r < 8; ++r) {
+        const float *src = r < 4 ? w0 : w1;
+        const float u1 = src[r & 3], u2 = src[4 + (r & 3)];
+        const int ua = __float_as_int(src[8 + (r & 3)]);
+        if (u1 > b1 || (u1 == b1 && ua < ba)) {
+          b2 = fmaxf(b1, u2);
+          b1 = u1;
+          ba = ua;
+        } else {
+          b2 = fmaxf(b2, u1);
+        }
+        b2 = fmaxf(b2, u2);
+      }
+      tc::bar_sync(bar_id, 64);  // both have read the exchange before the next tile writes it
+      // certification and near-tie hand-over: as in split_assign_kernel
+      const float e_acc = p.coef_xc * xn * cmax + p.coef_cc * cmax * cmax;
+      const float e = 2.f * e_acc + p.coef_ref * (xn + cmax) * (xn + cmax) + 1e-30f;
+      const bool flagged = live && !(2.f * (b1 - b2) > 2.1f * e);
+      if (g == 0) {
+        if (live) p.labels[i] = ba == 0x7fffffff ? 0 : ba;
+        const uint32_t fm = __ballot_sync(0xffffffffu, flagged);
+        if (fm) {
+          unsigned int first = 0;
+          if (lane == 0) first = atomicAdd(s_nlist, (unsigned int)__popc(fm));
+          first = __shfl_sync(0xffffffffu, first, 0);
+          if (flagged)
+            p.list_rows[(int64_t)blockIdx.x * p.region + first + __popc(fm & ((1u << lane) - 1u))] = i;
+        }
+      }
+      if (flagged) {
+        const float thr = b1 - 1.05f * e;
+        uint32_t cw[2] = {0u, 0u}, meta = 16u;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          if (m1[r] >= thr) { cw[r >> 1] |= (uint32_t)mi[r] << (16 * (r & 1)); meta |= 1u << r; }
+          if (m2[r] >= thr) meta &= ~16u;
+        }
+        p.cand4[(size_t)g * p.n_pad + i] = make_uint2(cw[0], cw[1]);
+        p.cmeta[(size_t)g * p.n_pad + i] = (uint8_t)meta;
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 2 * kWN);
+  }
+  if (threadIdx.x == 0) {
+    p.list_count[blockIdx.x] = *s_nlist;
+    if (*s_abort && p.st) atomicExch(&p.st->err, kErrTimeout);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -402,9 +652,9 @@ __device__ __forceinline__ double exact_sqd(const T *__restrict__ xr, const doub
   return s;
 }
 
-// Column of the u-th set bit (ascending) of an 8-word mask.
-__device__ __forceinline__ int nth_candidate(const uint32_t *mask, int u) {
-  for (int m = 0; m < 8; ++m) {
+// Column of the u-th set bit (ascending) of a mask of `words` words.
+__device__ __forceinline__ int nth_candidate(const uint32_t *mask, int words, int u) {
+  for (int m = 0; m < words; ++m) {
     uint32_t b = mask[m];
     const int c = __popc(b);
     if (u < c) {
@@ -427,12 +677,12 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
                const float *__restrict__ cT, const float *__restrict__ cn2,
                const unsigned int *__restrict__ cmax_bits, const float *__restrict__ xnrm,
                const int64_t *__restrict__ list_rows, const unsigned int *__restrict__ list_count, int region,
-               const uint32_t *__restrict__ cand4, const uint8_t *__restrict__ cmeta, int64_t n_pad,
+               const uint2 *__restrict__ cand4, const uint8_t *__restrict__ cmeta, int64_t n_pad,
                int32_t *__restrict__ labels, LloydState *st, int stage_ct) {
   if (st && st->done) return;
-  extern __shared__ __align__(16) float dyn[];  // [d x k_cols centroids^T when stage_ct] [d x kRsRows rows^T]
+  // dynamic: [d x k_cols centroids^T when stage_ct] [d x kRsRows rows^T] [kRsRows x mw survivor masks]
+  extern __shared__ __align__(16) float dyn[];
   __shared__ int64_t s_row[kRsRows];
-  __shared__ uint32_t s_mask[kRsRows][8];  // survivors per row
   __shared__ int s_cnt[kRsRows];           // survivors per row (0: resolved)
   __shared__ int s_pre[kRsRows + 1];
   __shared__ int s_full[kRsRows];          // rows whose candidate list is not complete
@@ -445,23 +695,23 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
   if (total == 0) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float *xs = dyn + (stage_ct ? d * k_cols : 0);  // xs[t * kRsRows + r]
+  const int mw = k_cols >> 5;                      // mask words per row
+  uint32_t *s_mask = (uint32_t *)(xs + d * kRsRows);  // s_mask[r * mw + word]
   if (stage_ct) {
     const int n_ct = d * k_cols;
     for (int t = threadIdx.x; t < n_ct; t += kRsThreads) dyn[t] = cT[t];
     cT = dyn;
   }
   const float cmax = __uint_as_float(*cmax_bits);
-  const int mchunks = k_cols >> 5;  // 32-centroid chunks present in cT (uniform)
   const int64_t *rows = list_rows + (int64_t)blockIdx.x * region;
   for (unsigned int base = 0; base < total; base += kRsRows) {
     const int nr = (int)min((unsigned int)kRsRows, total - base);
     if (threadIdx.x < kRsRows) {
       const int r = threadIdx.x;
       s_cnt[r] = 0;
-#pragma unroll
-      for (int m = 0; m < 8; ++m) s_mask[r][m] = 0u;
       if (r < nr) s_row[r] = rows[base + r];
     }
+    for (int e = threadIdx.x; e < kRsRows * mw; e += kRsThreads) s_mask[e] = 0u;
     if (threadIdx.x == 0) s_nfull = 0;
     __syncthreads();
     for (int e = threadIdx.x; e < kRsRows * d; e += kRsThreads) {
@@ -481,7 +731,8 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
       int j = -1;
       float a = __int_as_float(0x7f800000);
       if (listed && ((cmeta[(size_t)(u >> 2) * n_pad + i] >> (u & 3)) & 1u)) {
-        j = (int)((cand4[(size_t)(u >> 2) * n_pad + i] >> (8 * (u & 3))) & 0xffu);
+        const uint2 cw = cand4[(size_t)(u >> 2) * n_pad + i];
+        j = (int)((((u & 2) ? cw.y : cw.x) >> (16 * (u & 1))) & 0xffffu);
         float dot = 0.f;
         for (int t = 0; t < d; ++t) dot = fmaf(xs[t * kRsRows + r], cT[(int64_t)t * k_cols + j], dot);
         a = fmaf(-2.f, dot, cn2[j]);
@@ -493,55 +744,79 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
       const float lim = listed ? mn + 2.f * e32_bound(xnrm[i], cmax, d) : 0.f;
       const bool surv = j >= 0 && a <= lim;
       const uint32_t grp = (__ballot_sync(0xffffffffu, surv) >> (lane & 24)) & 0xffu;
-      if (surv) atomicOr(&s_mask[r][j >> 5], 1u << (j & 31));
+      if (surv) atomicOr(&s_mask[r * mw + (j >> 5)], 1u << (j & 31));
       if (listed && u == 0) s_cnt[r] = __popc(grp) > 1 ? __popc(grp) : 0;
       if (surv && __popc(grp) == 1) labels[i] = j;
     }
-    // ---- rows without a complete list: every centroid (warp = 2 rows)
+    // ---- rows without a complete list: every centroid (warp = 2 rows), in
+    // blocks of 256 columns: the minimum first, then the survivors
     const int nfull = s_nfull;
     for (int f0 = 2 * w; f0 < nfull; f0 += 2 * (kRsThreads / 32)) {
       const int r0 = s_full[f0], r1 = f0 + 1 < nfull ? s_full[f0 + 1] : r0;
+      const bool two = f0 + 1 < nfull;  // warp-uniform
+      auto scores = [&](int cb, float (&acc)[2][8]) {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) { acc[0][m] = 0.f; acc[1][m] = 0.f; }
+        const int mch = min(8, (k_cols - cb) >> 5);
+        for (int t = 0; t < d; ++t) {
+          const float x0 = xs[t * kRsRows + r0], x1 = xs[t * kRsRows + r1];
+          const float *crow = cT + (int64_t)t * k_cols + cb + lane;
+#pragma unroll
+          for (int m = 0; m < 8; ++m) {
+            if (m < mch) {
+              const float cv = crow[32 * m];
+              acc[0][m] = fmaf(x0, cv, acc[0][m]);
+              acc[1][m] = fmaf(x1, cv, acc[1][m]);
+            }
+          }
+        }
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+          for (int m = 0; m < 8; ++m) {
+            const int j = cb + lane + 32 * m;
+            acc[rr][m] = (m < mch && j < k) ? fmaf(-2.f, acc[rr][m], cn2[j]) : __int_as_float(0x7f800000);
+          }
+      };
       float acc[2][8];
+      float mn[2] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000)};
+      for (int cb = 0; cb < k_cols; cb += 256) {
+        scores(cb, acc);
 #pragma unroll
-      for (int m = 0; m < 8; ++m) { acc[0][m] = 0.f; acc[1][m] = 0.f; }
-      for (int t = 0; t < d; ++t) {
-        const float x0 = xs[t * kRsRows + r0], x1 = xs[t * kRsRows + r1];
-        const float *crow = cT + (int64_t)t * k_cols + lane;
+        for (int rr = 0; rr < 2; ++rr)
 #pragma unroll
-        for (int m = 0; m < 8; ++m) {
-          if (m < mchunks) {
-            const float cv = crow[32 * m];
-            acc[0][m] = fmaf(x0, cv, acc[0][m]);
-            acc[1][m] = fmaf(x1, cv, acc[1][m]);
+          for (int m = 0; m < 8; ++m) mn[rr] = fminf(mn[rr], acc[rr][m]);
+      }
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mn[rr] = fminf(mn[rr], __shfl_xor_sync(0xffffffffu, mn[rr], o));
+      const float lim0 = mn[0] + 2.f * e32_bound(xnrm[s_row[r0]], cmax, d);
+      const float lim1 = mn[1] + 2.f * e32_bound(xnrm[s_row[r1]], cmax, d);
+      int count[2] = {0, 0}, first[2] = {0x7fffffff, 0x7fffffff};
+      for (int cb = 0; cb < k_cols; cb += 256) {
+        if (k_cols > 256 || cb > 0) scores(cb, acc);  // one block: the scores are still in registers
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+          if (rr == 1 && !two) break;
+          const int r = rr ? r1 : r0;
+          const float lim = rr ? lim1 : lim0;
+#pragma unroll
+          for (int m = 0; m < 8; ++m) {
+            const uint32_t bm = __ballot_sync(0xffffffffu, acc[rr][m] <= lim);
+            count[rr] += __popc(bm);
+            if (bm && first[rr] == 0x7fffffff) first[rr] = cb + 32 * m + __ffs(bm) - 1;
+            if (lane == m && cb + 32 * m < k_cols) s_mask[r * mw + (cb >> 5) + m] = bm;
           }
         }
       }
 #pragma unroll
       for (int rr = 0; rr < 2; ++rr) {
-        if (rr == 1 && f0 + 1 >= nfull) break;  // warp-uniform
+        if (rr == 1 && !two) break;
         const int r = rr ? r1 : r0;
-        float mn = __int_as_float(0x7f800000);
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-          const int j = lane + 32 * m;
-          acc[rr][m] = (m < mchunks && j < k) ? fmaf(-2.f, acc[rr][m], cn2[j]) : __int_as_float(0x7f800000);
-          mn = fminf(mn, acc[rr][m]);
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        const int64_t i = s_row[r];
-        const float lim = mn + 2.f * e32_bound(xnrm[i], cmax, d);
-        int count = 0, first = 0x7fffffff;
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-          const uint32_t b = __ballot_sync(0xffffffffu, acc[rr][m] <= lim);
-          count += __popc(b);
-          if (b && first == 0x7fffffff) first = 32 * m + __ffs(b) - 1;
-          if (lane == m) s_mask[r][m] = b;
-        }
         if (lane == 0) {
-          s_cnt[r] = count > 1 ? count : 0;
-          if (count <= 1) labels[i] = first == 0x7fffffff ? 0 : first;
+          s_cnt[r] = count[rr] > 1 ? count[rr] : 0;
+          if (count[rr] <= 1) labels[s_row[r]] = first[rr] == 0x7fffffff ? 0 : first[rr];
         }
       }
     }
@@ -571,7 +846,7 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
           const int mid = (lo + hi + 1) >> 1;
           if (s_pre[mid] <= p) lo = mid; else hi = mid - 1;
         }
-        const int j = nth_candidate(s_mask[lo], p - s_pre[lo]);
+        const int j = nth_candidate(s_mask + lo * mw, mw, p - s_pre[lo]);
         q_j[p] = (int16_t)j;
         q_s[p] = exact_sqd(x + s_row[lo] * (int64_t)d, cent + (int64_t)j * d, d);
       }
@@ -585,19 +860,21 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
         labels[s_row[r]] = bj;
       }
     } else {
-      // ---- many survivors: one row at a time, one thread per survivor
+      // ---- many survivors: one row at a time, survivors spread over the threads
       for (int r = 0; r < kRsRows; ++r) {
-        const int c = s_cnt[r];  // <= k_cols <= kRsThreads
+        const int c = s_cnt[r];
         if (c == 0) continue;
         if (threadIdx.x == 0) { s_best = ~0ull; s_bj = 0x7fffffff; }
         __syncthreads();
-        double sv = 0.0;
-        int j = 0;
-        if ((int)threadIdx.x < c) {
-          j = nth_candidate(s_mask[r], threadIdx.x);
-          sv = exact_sqd(x + s_row[r] * (int64_t)d, cent + (int64_t)j * d, d);
-          atomicMin(&s_best, (unsigned long long)__double_as_longlong(sv));  // sv >= 0: bits order as values
+        double sv = DBL_MAX;
+        int j = 0x7fffffff;
+        for (int u = threadIdx.x; u < c; u += kRsThreads) {  // ascending j: strict < keeps the lowest
+          const int ju = nth_candidate(s_mask + r * mw, mw, u);
+          const double su = exact_sqd(x + s_row[r] * (int64_t)d, cent + (int64_t)ju * d, d);
+          if (su < sv) { sv = su; j = ju; }
         }
+        if ((int)threadIdx.x < c)
+          atomicMin(&s_best, (unsigned long long)__double_as_longlong(sv));  // sv >= 0: bits order as values
         __syncthreads();
         if ((int)threadIdx.x < c && (unsigned long long)__double_as_longlong(sv) == s_best) atomicMin(&s_bj, j);
         __syncthreads();
@@ -696,7 +973,7 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
   SC_TRY(dalloc(&s->part, (size_t)nb));
   SC_TRY(dalloc(&s->list_rows, (size_t)(s->n_pad + (int64_t)s->num_sms * kBM)));
   SC_TRY(dalloc(&s->list_count, (size_t)s->num_sms));
-  SC_TRY(dalloc(&s->cand4, (size_t)(2 * s->n_pad)));
+  SC_TRY(dalloc(&s->cand4, (size_t)(2 * s->n_pad)));  // uint2 each
   SC_TRY(dalloc(&s->cmeta, (size_t)(2 * s->n_pad)));
   SC_TRY(dalloc(&s->cmax, 1));
   if (dtype == SC_F32)
@@ -716,12 +993,25 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
   return SC_OK;
 }
 
+size_t wide_smem(const SplitState *s, int stages) {
+  const size_t a_bytes = (size_t)2 * s->nkt * kBM * s->row_bytes;
+  const size_t b_stage = ((size_t)2 * s->nkt * kWN * s->row_bytes + kWN * 32 + 1023) & ~(size_t)1023;
+  return 1024 + a_bytes + 4096 + (size_t)stages * b_stage + (size_t)2 * kBM * 12 * 4 + (size_t)(2 * stages + 7) * 8 + 16;
+}
+
 sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cudaStream_t st) {
   if (!s->ready) { set_error("split-BF16 state is not prepared"); return SC_ERR_INTERNAL; }
-  const int k_pad = (k + 15) / 16 * 16;
+  // up to 256 centroids resident in shared memory; more (or too large) stream in blocks of kWN
+  const int k_pad16 = (k + 15) / 16 * 16;
+  const bool wide = k_pad16 > 256 || assign_smem(s, 2, k_pad16) > 227 * 1024;
+  const int k_pad = wide ? (k + kWN - 1) / kWN * kWN : k_pad16;
   const int k_cols = (k_pad + 31) / 32 * 32;
-  if (k_pad > 256) {
-    set_error("k=%d exceeds the split-BF16 kernel's limit of 256 clusters", k);
+  if (k_pad > 65535) {
+    set_error("k=%d exceeds the split-BF16 kernel's limit of 65535 clusters", k);
+    return SC_ERR_INVALID;
+  }
+  if (wide && wide_smem(s, 2) > 227 * 1024) {
+    set_error("d=%d exceeds the split-BF16 kernel's shared memory for k=%d", s->d, k);
     return SC_ERR_INVALID;
   }
   if (k_cols > s->k_alloc) {
@@ -735,10 +1025,12 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
     s->k_pad = 0;
   }
   if (k_pad != s->k_pad) {
-    SC_TRY(make_map(&s->tm_ch, s->ch, k_pad, s->d_pad, s->kt_elems, k_pad, s->row_bytes));
-    SC_TRY(make_map(&s->tm_cl, s->cl, k_pad, s->d_pad, s->kt_elems, k_pad, s->row_bytes));
-    SC_TRY(make_map(&s->tm_cbx, s->cbx, k_pad, 16, 16, k_pad, 32));
+    const int box = wide ? kWN : k_pad;
+    SC_TRY(make_map(&s->tm_ch, s->ch, k_pad, s->d_pad, s->kt_elems, box, s->row_bytes));
+    SC_TRY(make_map(&s->tm_cl, s->cl, k_pad, s->d_pad, s->kt_elems, box, s->row_bytes));
+    SC_TRY(make_map(&s->tm_cbx, s->cbx, k_pad, 16, 16, box, 32));
   }
+  s->wide = wide ? 1 : 0;
   s->k = k;
   s->k_pad = k_pad;
   SC_CUDA(cudaMemsetAsync(s->cmax, 0, sizeof(unsigned int), st));
@@ -755,9 +1047,12 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   const int k_cols = (s->k_pad + 31) / 32 * 32;
   uint32_t tmem_cols = 32;
   while (tmem_cols < (uint32_t)(2 * k_cols)) tmem_cols <<= 1;
-  int stages = 6;
-  while (stages > 2 && assign_smem(s, stages, s->k_pad) > 227 * 1024) --stages;
-  const size_t smem = assign_smem(s, stages, s->k_pad);
+  int stages = s->wide ? 4 : 6;
+  if (s->wide)
+    while (stages > 2 && wide_smem(s, stages) > 227 * 1024) --stages;
+  else
+    while (stages > 2 && assign_smem(s, stages, s->k_pad) > 227 * 1024) --stages;
+  const size_t smem = s->wide ? wide_smem(s, stages) : assign_smem(s, stages, s->k_pad);
   if (smem > 227 * 1024) {
     set_error("d=%d, k=%d exceed the split-BF16 kernel's shared memory", d, k);
     return SC_ERR_INVALID;
@@ -792,15 +1087,22 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   p.cand4 = s->cand4;
   p.cmeta = s->cmeta;
   p.st = lst;
-  SC_CUDA(cudaFuncSetAttribute(split_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
-  split_assign_kernel<<<grid, kAssignThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, s->tm_ones,
-                                                          s->tm_cbx, p);
+  if (s->wide) {
+    SC_CUDA(cudaFuncSetAttribute(split_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
+    split_wide_kernel<<<grid, kWideThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, s->tm_ones,
+                                                        s->tm_cbx, p);
+  } else {
+    SC_CUDA(cudaFuncSetAttribute(split_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
+    split_assign_kernel<<<grid, kAssignThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, s->tm_ones,
+                                                            s->tm_cbx, p);
+  }
   SC_LAUNCHED();
   if (timing) SC_CUDA(cudaEventRecord(timing[1], st));
   // near ties: re-score the rows each CTA listed
   const size_t ct_bytes = (size_t)d * k_cols * sizeof(float);
-  const size_t xs_bytes = (size_t)d * kRsRows * sizeof(float);
+  const size_t xs_bytes = (size_t)d * kRsRows * sizeof(float) + (size_t)kRsRows * (k_cols / 32) * sizeof(uint32_t);
   const int stage = ct_bytes + xs_bytes <= 180 * 1024 ? 1 : 0;
   const size_t rsmem = xs_bytes + (stage ? ct_bytes : 0);
   if (dtype == SC_F32) {

@@ -18,6 +18,7 @@ struct SplitState {
   float *xnrm = nullptr;                        // n_pad: upper bound of ||x||
   double *part = nullptr;                       // block partials of ||x||^2
   int k = 0, k_pad = 0, k_alloc = 0;
+  int wide = 0;                                 // centroids streamed in blocks (split_wide_kernel)
   __nv_bfloat16 *ch = nullptr, *cl = nullptr;  // k_pad x d_pad
   __nv_bfloat16 *cbx = nullptr;                 // k_pad x 16: BF16 terms of -||c||^2/2
   __nv_bfloat16 *ones = nullptr;                // 128 x 16: [1, 1, 1, 0...] rows
@@ -27,8 +28,8 @@ struct SplitState {
   float *cT = nullptr;                          // d_pad x k_cols: centroids in f32, transposed
   unsigned int *list_count = nullptr;           // near ties of the last assignment: rows per CTA,
   int64_t *list_rows = nullptr;                 //   their rows (per-CTA regions),
-  uint32_t *cand4 = nullptr;                    //   [2][n_pad] candidate columns by row (bytes)
-  uint8_t *cmeta = nullptr;                     //   [2][n_pad] valid bytes, list complete
+  uint2 *cand4 = nullptr;                       //   [2][n_pad] candidate columns by row (4 x 16 bits)
+  uint8_t *cmeta = nullptr;                     //   [2][n_pad] valid columns, list complete
   CUtensorMap tm_xh, tm_xl, tm_ch, tm_cl;
   int num_sms = 0;
 };

@@ -129,6 +129,22 @@ def test_independent_small_problems(form):
 
 
 @pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("n,d,k", [(20000, 64, 300), (12000, 128, 1000), (8000, 128, 2048), (6000, 16, 500)])
+def test_predict_many_centroids(form, n, d, k):
+    # more centroids than stay resident in shared memory: streamed in blocks of 128
+    x, _ = blobs(n, d, 64, seed=n + k, dtype=np.float32, box=(-50.0, 50.0), std=2.0)
+    c = np.ascontiguousarray(x[np.random.default_rng(k).choice(n, k, replace=False)], np.float64)
+    km = KMeans(k, None, None, 0.0, c, 0, form)
+    assert np.array_equal(km.predict(x), oracle.kmeans_predict(x, c))
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_fit_many_centroids_d128(form):
+    x, _ = blobs(10000, 128, 40, seed=11, dtype=np.float32, box=(-50.0, 50.0), std=2.0)
+    assert_fit_parity(x, 300, 4, 5, form)
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_predict_many_tied_candidates(form):
     # 40 centroids drawn from the 16 vectors +-e_t (duplicates included), all
     # of norm 1: points at the origin tie with every centroid exactly, points
