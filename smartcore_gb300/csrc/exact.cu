@@ -151,8 +151,8 @@ pp_update_kernel(const T *__restrict__ x, int64_t n, int d, const LloydState *st
     const T *xr = x + i * (int64_t)d;
     double s = 0.0;
     bool exact = false;
-    // f32 rows: the same value from an integer exact sum when no partial sum rounds
-    if constexpr (sizeof(T) == 4) exact = sqd_exact_f32(xr, cen, d, lg_d, s);
+    // f32 rows: the same value from the integer reproduction of the sequential sum
+    if constexpr (sizeof(T) == 4) exact = sqd_seq_f32(xr, cen, d, lg_d, s);
     if (!exact) {
       s = 0.0;
       for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term(xr[j], cen[j]));
@@ -164,6 +164,79 @@ pp_update_kernel(const T *__restrict__ x, int64_t n, int d, const LloydState *st
     labels[i] = lab;
     v = cur;
   }
+  const double tot = block_sum_fixed<kPPThreads>(v);
+  if (threadIdx.x == 0 && part) part[blockIdx.x] = tot;
+}
+
+// f32 rows, d <= 128: the same update with each warp's 32 rows staged in
+// shared memory by coalesced loads (row stride d + 1: conflict-free when each
+// lane then walks its own row).  Thread t still handles row 256 b + t, so the
+// block partials are the same.
+__global__ void __launch_bounds__(kPPThreads)
+pp_update_staged_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *st,
+                        int32_t label_of_seed, double *__restrict__ dd, int32_t *__restrict__ labels,
+                        double *__restrict__ part, int first_pass, int lg_d) {
+  extern __shared__ float smf[];
+  float *cen = smf;                                                // d
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float *tile = smf + ((d + 3) & ~3) + (size_t)w * 32 * (d + 1);  // 32 rows x (d + 1)
+  const int64_t ci = st->pp_chosen;
+  for (int t = threadIdx.x; t < d; t += kPPThreads) cen[t] = x[ci * d + t];
+  const int64_t r0 = (int64_t)blockIdx.x * kPPThreads + w * 32;
+  // asynchronous 4-byte copies: every row of the warp in flight at once
+  for (int rr = 0; rr < 32; ++rr) {
+    const int64_t i = r0 + rr;
+    if (i < n)
+      for (int c = lane; c < d; c += 32) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(tile + rr * (d + 1) + c);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(x + i * d + c) : "memory");
+      }
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();
+  __shared__ int s_q[kPPThreads];  // block rows that need the exact distance
+  __shared__ double s_v[kPPThreads];
+  __shared__ int s_qn;
+  if (threadIdx.x == 0) s_qn = 0;
+  __syncthreads();
+  const int64_t i = r0 + lane;
+  double cur = DBL_MAX;
+  if (i < n) {
+    const float *xr = tile + lane * (d + 1);
+    cur = first_pass ? DBL_MAX : dd[i];
+    // The reference's terms q_t = fl32((x_t - c_t)^2) summed in f32 bound its
+    // f64 sum from below by s32 (1 - 1.05 d 2^-24): when that exceeds the
+    // current distance, the row keeps it and the exact sum is not needed.
+    float s32 = 0.f;
+    for (int j = 0; j < d; ++j) {
+      const float r = __fsub_rn(xr[j], cen[j]);
+      s32 = __fadd_rn(s32, __fmul_rn(r, r));
+    }
+    const bool keep = !first_pass && __fmul_rd(s32, 1.f - 1.05f * d * 0x1p-24f) > __double2float_ru(cur);
+    if (!keep) s_q[atomicAdd(&s_qn, 1)] = threadIdx.x;
+  }
+  s_v[threadIdx.x] = i < n ? cur : 0.0;
+  __syncthreads();
+  // the rows that need it, on contiguous threads (full warps)
+  const int qn = s_qn;
+  for (int qi = threadIdx.x; qi < qn; qi += kPPThreads) {
+    const int t = s_q[qi];
+    const int64_t row = (int64_t)blockIdx.x * kPPThreads + t;
+    const float *xr = smf + ((d + 3) & ~3) + (size_t)(t >> 5) * 32 * (d + 1) + (t & 31) * (d + 1);
+    double sq = 0.0;
+    if (!sqd_seq_f32(xr, cen, d, lg_d, sq)) {
+      sq = 0.0;
+      for (int j = 0; j < d; ++j) sq = __dadd_rn(sq, sq_term(xr[j], cen[j]));
+    }
+    double c = s_v[t];
+    int32_t lab = first_pass ? 0 : labels[row];
+    if (sq < c) { c = sq; lab = label_of_seed; }
+    dd[row] = c;
+    labels[row] = lab;
+    s_v[t] = c;
+  }
+  __syncthreads();
+  const double v = s_v[threadIdx.x];
   const double tot = block_sum_fixed<kPPThreads>(v);
   if (threadIdx.x == 0 && part) part[blockIdx.x] = tot;
 }
@@ -180,7 +253,12 @@ sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
   }
   int lg_d = 0;
   while ((1 << lg_d) < d) ++lg_d;
-  if (dtype == SC_F32)
+  if (dtype == SC_F32 && d <= 128) {
+    const size_t ssm = ((size_t)((d + 3) & ~3) + (size_t)kPPThreads * (d + 1)) * sizeof(float);
+    SC_CUDA(cudaFuncSetAttribute(pp_update_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    pp_update_staged_kernel<<<grid, kPPThreads, ssm, s>>>((const float *)x, n, d, st, label_of_seed, dd, labels,
+                                                          part, first_pass, lg_d);
+  } else if (dtype == SC_F32)
     pp_update_kernel<float><<<grid, kPPThreads, smem, s>>>((const float *)x, n, d, st, label_of_seed, dd, labels, part, first_pass, lg_d);
   else
     pp_update_kernel<double><<<grid, kPPThreads, smem, s>>>((const double *)x, n, d, st, label_of_seed, dd, labels, part, first_pass, lg_d);

@@ -352,7 +352,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
             if (p.d <= 32) {
               done = sqd_seq_f32_d32((const float *)qrow, (const float *)tr, p.d, p.lg_d, sq);
             } else {
-              done = sqd_exact_f32(qrow, tr, p.d, p.lg_d, sq);
+              done = sqd_seq_f32(qrow, tr, p.d, p.lg_d, sq);
             }
           }
           if (!done) {
