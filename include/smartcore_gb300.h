@@ -201,6 +201,19 @@ sc_status sc_knn_find(sc_knn *h, const void *queries, int32_t layout,
                       int32_t mem, int64_t m, int64_t ld, int64_t k,
                       int32_t form, int32_t out_mem, int64_t *idx_out,
                       double *dist_out);
+/* LinearKNNSearch::find_radius (linear_search.rs:89-108) for m query rows:
+ * every training row i with d = sqrt(D) <= radius, in index order.
+ * counts_out (host, m, may be NULL) receives each query's count and
+ * total_out (may be NULL) their sum.  With idx_out / dist_out (host) non-NULL
+ * and capacity >= total, they receive the rows of query 0, then of query 1,
+ * ...; with both NULL only the counts are computed (call again with enough
+ * capacity).  SC_ERR_INVALID with "radius should be > 0" (:90-95), or when
+ * capacity < total (total_out is still set). */
+sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout,
+                             int32_t mem, int64_t m, int64_t ld, double radius,
+                             int32_t form, int64_t *counts_out, int64_t capacity,
+                             int64_t *idx_out, double *dist_out,
+                             int64_t *total_out);
 /* KNNClassifier / KNNRegressor aggregation on the device over a find()
  * result already in idx/dist (device memory of this handle, m x k):
  * y_class = class index per training row (KNNClassifier::fit,

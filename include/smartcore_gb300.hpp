@@ -242,6 +242,25 @@ class LinearKNNSearch {
     return out;
   }
 
+  // find_radius() for one query (linear_search.rs:89-108): (index, distance)
+  // of every row with distance <= radius, in index order.
+  std::vector<std::pair<size_t, double>> find_radius(const std::vector<T> &from, double radius) const {
+    if (from.size() != d_) throw std::invalid_argument("Input vector sizes are different.");
+    int64_t count = 0, total = 0;
+    detail::check(sc_knn_find_radius(h_, from.data(), SC_ROW_MAJOR, SC_MEM_HOST, 1, (int64_t)d_, radius,
+                                     (int32_t)form_, &count, 0, nullptr, nullptr, &total),
+                  FailedError::FindFailed);
+    std::vector<int64_t> idx(total ? total : 1);
+    std::vector<double> dist(total ? total : 1);
+    if (total)
+      detail::check(sc_knn_find_radius(h_, from.data(), SC_ROW_MAJOR, SC_MEM_HOST, 1, (int64_t)d_, radius,
+                                       (int32_t)form_, &count, total, idx.data(), dist.data(), &total),
+                    FailedError::FindFailed);
+    std::vector<std::pair<size_t, double>> out;
+    for (int64_t s = 0; s < total; ++s) out.emplace_back((size_t)idx[s], dist[s]);
+    return out;
+  }
+
   sc_knn *handle() const { return h_; }
   Form form() const { return form_; }
   size_t len() const { return n_; }

@@ -46,6 +46,7 @@ SIGNATURES = {
     "sc_kmeans_destroy": ([_P], None),
     "sc_knn_create": ([_P, _I32, _I32, _I32, _I64, _I64, _I64, _P], _I32),
     "sc_knn_find": ([_P, _P, _I32, _I32, _I64, _I64, _I64, _I32, _I32, _P, _P], _I32),
+    "sc_knn_find_radius": ([_P, _P, _I32, _I32, _I64, _I64, _D, _I32, _P, _I64, _P, _P, _P], _I32),
     "sc_knn_classify": ([_P, _P, _I32, _I32, _I64, _I64, _I64, _I32, _I32, _P, _I64, _P], _I32),
     "sc_knn_regress": ([_P, _P, _I32, _I32, _I64, _I64, _I64, _I32, _I32, _P, _P], _I32),
     "sc_knn_stream": ([_P], _P),

@@ -539,6 +539,75 @@ sc_status sc_knn_find(sc_knn *h, const void *queries, int32_t layout, int32_t me
   return SC_OK;
 }
 
+sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout, int32_t mem, int64_t m,
+                             int64_t ld, double radius, int32_t form, int64_t *counts_out, int64_t capacity,
+                             int64_t *idx_out, double *dist_out, int64_t *total_out) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (!(radius > 0.0)) { set_error("radius should be > 0"); return SC_ERR_INVALID; }  // linear_search.rs:90-95
+  SC_TRY(check_matrix(queries, h->dtype, layout, mem, m, h->d, ld));
+  if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
+  if (total_out) *total_out = 0;
+  if (m == 0) return SC_OK;
+  SC_TRY(knn_reserve(h, m, 1));
+  SC_TRY(upload_matrix(queries, h->dtype, layout, mem, m, h->d, ld, h->q, h->stream));
+  int64_t *dcnt = nullptr, *doff = nullptr, *didx = nullptr;
+  double *ddist = nullptr;
+  sc_status r = SC_OK;
+  std::vector<int64_t> cnt((size_t)m);
+  int64_t total = 0;
+  do {
+    if ((r = dalloc(&dcnt, (size_t)m)) != SC_OK || (r = dalloc(&doff, (size_t)m)) != SC_OK) break;
+    // counting pass
+    r = form == SC_FORM_FP64
+            ? launch_knn_radius_fp64(h->dtype, h->train, h->n, (int)h->d, h->q, m, radius, dcnt, nullptr, nullptr,
+                                     nullptr, h->stream)
+            : split_knn_radius(&h->split, h->dtype, h->train, h->n, (int)h->d, h->q, m, radius, dcnt, nullptr,
+                               nullptr, nullptr, h->stream);
+    if (r != SC_OK) break;
+    if (cudaMemcpyAsync(cnt.data(), dcnt, (size_t)m * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "find_radius counts");
+      break;
+    }
+    std::vector<int64_t> off((size_t)m);
+    for (int64_t q = 0; q < m; ++q) { off[(size_t)q] = total; total += cnt[(size_t)q]; }
+    if (counts_out) memcpy(counts_out, cnt.data(), (size_t)m * sizeof(int64_t));
+    if (total_out) *total_out = total;
+    if (!idx_out && !dist_out) break;  // counts only
+    if (capacity < total) {
+      set_error("capacity %lld is smaller than the %lld neighbours found", (long long)capacity, (long long)total);
+      r = SC_ERR_INVALID;
+      break;
+    }
+    if (total == 0) break;
+    if ((r = dalloc(&didx, (size_t)total)) != SC_OK || (r = dalloc(&ddist, (size_t)total)) != SC_OK) break;
+    if (cudaMemcpyAsync(doff, off.data(), (size_t)m * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream) !=
+        cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "find_radius offsets");
+      break;
+    }
+    // filling pass
+    r = form == SC_FORM_FP64
+            ? launch_knn_radius_fp64(h->dtype, h->train, h->n, (int)h->d, h->q, m, radius, nullptr, doff, didx,
+                                     ddist, h->stream)
+            : split_knn_radius(&h->split, h->dtype, h->train, h->n, (int)h->d, h->q, m, radius, nullptr, doff,
+                               didx, ddist, h->stream);
+    if (r != SC_OK) break;
+    if ((idx_out && cudaMemcpyAsync(idx_out, didx, (size_t)total * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                    h->stream) != cudaSuccess) ||
+        (dist_out && cudaMemcpyAsync(dist_out, ddist, (size_t)total * sizeof(double), cudaMemcpyDeviceToHost,
+                                     h->stream) != cudaSuccess) ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "find_radius results");
+      break;
+    }
+  } while (0);
+  cudaStreamSynchronize(h->stream);
+  dfree(dcnt); dfree(doff); dfree(didx); dfree(ddist);
+  return r;
+}
+
 sc_status sc_knn_classify(sc_knn *h, const void *queries, int32_t layout, int32_t mem, int64_t m,
                           int64_t ld, int64_t k, int32_t form, int32_t weight,
                           const int64_t *y_class, int64_t n_classes, int64_t *classes_out) {

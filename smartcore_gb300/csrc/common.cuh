@@ -90,6 +90,9 @@ sc_status launch_pp_select(const double *dd, const double *part, int64_t n,
 sc_status launch_knn_fp64(int dtype, const void *train, int64_t n, int d,
                           const void *queries, int64_t m, int k, int64_t *idx,
                           double *dist, cudaStream_t s);
+sc_status launch_knn_radius_fp64(int dtype, const void *train, int64_t n, int d, const void *queries, int64_t m,
+                                 double radius, int64_t *counts, const int64_t *offsets, int64_t *idx,
+                                 double *dist, cudaStream_t s);
 sc_status launch_knn_vote(const int64_t *idx, const double *dist, int64_t m,
                           int k, int weight, const int64_t *y_class,
                           int64_t *out, cudaStream_t s);

@@ -103,6 +103,13 @@ struct KnnParams {
   double *dist_out;
   unsigned long long *evals;
   int *err;
+  // find_radius (linear_search.rs:89-108): rows with sqrt(D) <= radius, in
+  // index order; counts per query (counting pass, idx_out == nullptr) or the
+  // rows from offsets[q] on (filling pass)
+  int radius_mode;
+  double radius, r2up;  // r2up >= every D whose sqrt rounds to <= radius
+  int64_t *counts;
+  const int64_t *offsets;
 };
 
 // The reference keys its heap on d = sqrt(D) (f64).  The heap here holds D
@@ -336,6 +343,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       // row j can enter only if acc_j >= lo = -thr / 2 (thr = root^2 - ||q||^2 + e)
       float lo = live ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
       s_lo[row] = lo;
+      int64_t rc = 0, rpos = p.radius_mode && p.idx_out && live ? p.offsets[q] : 0;  // find_radius
       uint32_t qhead = 0, qtail = 0;  // warp-uniform queue cursors
       const int64_t qbase = (int64_t)qt * kQM + lq * 32;
       // one round: exact distances of up to 32 queued entries, then the owners' heap steps
@@ -374,6 +382,18 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         for (uint32_t mine = Rg[lane]; mine; mine &= mine - 1u) {
           const int r = __ffs(mine) - 1;
           const double sr = Rs[r];
+          if (p.radius_mode) {  // linear_search.rs:100-104: d <= radius, appended in index order
+            const double dist = __dsqrt_rn(sr);
+            if (dist <= p.radius) {
+              if (p.idx_out) {
+                p.idx_out[rpos] = Rj[r];
+                p.dist_out[rpos] = dist;
+                ++rpos;
+              }
+              ++rc;
+            }
+            continue;
+          }
           if (sqrt_less(sr, hD[0])) {  // sqrt(D) < root (linear_search.rs:72)
             hD[0] = sr;
             hi[0] = Rj[r];
@@ -454,7 +474,9 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         tc::mbar_arrive(&maskempty[slot]);  // tile replayed (queued entries only make lo staler)
       }
       while (!stop && qtail != qhead) round(min(32u, qtail - qhead));
-      if (live && !stop)
+      if (p.radius_mode) {
+        if (live && !stop && !p.idx_out) p.counts[q] = rc;
+      } else if (live && !stop)
         for (int s = 0; s < p.k; ++s) {
           p.idx_out[q * p.k + s] = hi[s * HS];
           p.dist_out[q * p.k + s] = __dsqrt_rn(hD[s * HS]);  // sqrt(+inf) = +inf for an empty slot
@@ -480,7 +502,21 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         // tt - 2.  Either wait also frees this tile's mask slot.
         const bool live_q = (int64_t)qt * kQM + row < p.m;
         float lo = live_q ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
-        if (tt >= 1) {
+        if (p.radius_mode) {
+          // a fixed threshold: D <= r2up; only the mask slot must be free
+          if (it >= kMaskSlots) {
+            const int u = it - kMaskSlots;
+            ok = ok && tc::mbar_wait(&maskempty[u % kMaskSlots], (uint32_t)(u / kMaskSlots) & 1u, kWaitNs);
+          }
+          if (live_q) {
+            const int64_t q = (int64_t)qt * kQM + row;
+            const float tmax = __uint_as_float(*p.tmax);
+            const float qn = p.qnrm[q];
+            const float eq = 1.05f * (2.f * (p.coef_xc * qn * tmax + p.coef_cc * tmax * tmax) +
+                                      p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
+            lo = -0.5f * knn_threshold(p.r2up, p.qn2[q], eq);
+          }
+        } else if (tt >= 1) {
           const int u = it - (tt == 1 ? 1 : 2);
           ok = ok && tc::mbar_wait(&maskempty[u % kMaskSlots], (uint32_t)(u / kMaskSlots) & 1u, kWaitNs);
           lo = *(volatile float *)&s_lo[row];
@@ -499,7 +535,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         uint32_t *mrow = sMask + ((size_t)slot * kQM + row) * kWords + c_lo / 32;
         const int64_t j0 = (int64_t)tt * TN + c_lo;
         float lo_rest = lo;  // threshold for the rows after the tile's first 32
-        if (tt == 0 && p.k <= 32) {
+        if (tt == 0 && !p.radius_mode && p.k <= 32) {
           // No heap yet.  Once any k rows have been seen the root is at most
           // the largest of their distances, so every row after the first 32
           // needs acc_j > (k-th largest acc of those 32) - e: |acc - (||q||^2 -
@@ -634,8 +670,16 @@ sc_status launch_knn_split(int grid, size_t smem, const CUtensorMap &tm_qh, cons
 
 }  // namespace
 
-sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
-                    int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, cudaStream_t st) {
+namespace {
+struct RadiusArgs {
+  double radius;
+  int64_t *counts;         // counting pass (idx == nullptr)
+  const int64_t *offsets;  // filling pass
+};
+
+sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
+                        int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, const RadiusArgs *rad,
+                        cudaStream_t st) {
   if (rescored) *rescored = 0;
   if (m == 0 || n == 0) return SC_OK;
   if (n >= ((int64_t)1 << kRowBits)) {
@@ -731,6 +775,13 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   p.coef_ref = (float)((d + 4) * 0x1p-52);
   p.idx_out = idx;
   p.dist_out = dist;
+  if (rad) {
+    p.radius_mode = 1;
+    p.radius = rad->radius;
+    p.r2up = rad->radius * rad->radius * (1.0 + 0x1p-48);  // covers every D with sqrt(D) rounding to <= radius
+    p.counts = rad->counts;
+    p.offsets = rad->offsets;
+  }
   p.evals = s->evals;
   p.err = (int *)(s->evals + 1);
   const int grid = p.n_tiles_q < s->num_sms ? p.n_tiles_q : s->num_sms;
@@ -753,6 +804,20 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
   }
   if (rescored) *rescored = (int64_t)host[0];
   return SC_OK;
+}
+
+}  // namespace
+
+sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
+                    int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, cudaStream_t st) {
+  return run_split_knn(s, dtype, train, n, d, queries, m, k, idx, dist, rescored, nullptr, st);
+}
+
+sc_status split_knn_radius(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
+                           int64_t m, double radius, int64_t *counts, const int64_t *offsets, int64_t *idx,
+                           double *dist, cudaStream_t st) {
+  const RadiusArgs rad{radius, counts, offsets};
+  return run_split_knn(s, dtype, train, n, d, queries, m, 0, idx, dist, nullptr, &rad, st);
 }
 
 void split_knn_free(SplitKnnState *s) {

@@ -62,6 +62,11 @@ void split_free(SplitState *s);
 sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
                     const void *queries, int64_t m, int k, int64_t *idx, double *dist,
                     int64_t *rescored, cudaStream_t st);
+// find_radius: counting pass when idx is null (counts[q]), else filling pass
+// (query q's rows from offsets[q] on); every pointer is device memory.
+sc_status split_knn_radius(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
+                           const void *queries, int64_t m, double radius, int64_t *counts,
+                           const int64_t *offsets, int64_t *idx, double *dist, cudaStream_t st);
 void split_knn_free(SplitKnnState *s);
 
 }  // namespace sc

@@ -71,6 +71,32 @@ class LinearKNNSearch:
         idx, dist = self.find_batch(np.asarray(from_)[None, :], k)
         return [(int(i), float(dd)) for i, dd in zip(idx[0], dist[0]) if i >= 0]
 
+    def find_radius_batch(self, queries, radius):
+        """find_radius() for every row of queries: (counts, idx, dist), the
+        rows of query 0 first, each query's rows in index order."""
+        a = self._q(queries)
+        m = a.shape[0]
+        lay, ld = layout_of(a)
+        counts = np.zeros(max(m, 1), np.int64)
+        total = np.zeros(1, np.int64)
+        _lib.check(self._L.sc_knn_find_radius(self.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, float(radius),
+                                              self.form, _lib.ptr(counts), 0, None, None, _lib.ptr(total)),
+                   FailedError.FindFailed)
+        t = int(total[0])
+        idx = np.zeros(max(t, 1), np.int64)
+        dist = np.zeros(max(t, 1), np.float64)
+        if t:
+            _lib.check(self._L.sc_knn_find_radius(self.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, float(radius),
+                                                  self.form, _lib.ptr(counts), t, _lib.ptr(idx), _lib.ptr(dist),
+                                                  _lib.ptr(total)), FailedError.FindFailed)
+        return counts[:m], idx[:t], dist[:t]
+
+    def find_radius(self, from_, radius):
+        """LinearKNNSearch::find_radius (linear_search.rs:89-108): list of
+        (index, distance) of the rows with distance <= radius, in index order."""
+        _, idx, dist = self.find_radius_batch(np.asarray(from_)[None, :], radius)
+        return [(int(i), float(dd)) for i, dd in zip(idx, dist)]
+
     def classify(self, queries, k, weight, y_class, n_classes):
         a = self._q(queries)
         m = a.shape[0]

@@ -80,6 +80,15 @@ static void knn_find(Form form) {
     threw = e.to_string() == "Find failed: k should be >= 1 and <= length(data)";
   }
   CHECK(threw);
+  // find_radius (linear_search.rs:166-174): the values within radius 3 of 5
+  std::vector<std::vector<double>> rows;
+  for (double v : kats::knn_scalar_data) rows.push_back({v});
+  LinearKNNSearch<double> s1(DenseMatrix<double>::from_2d_array(rows), form);
+  std::vector<int> vals;
+  for (auto &p : s1.find_radius({kats::knn_radius_query}, kats::knn_radius))
+    vals.push_back((int)kats::knn_scalar_data[p.first]);
+  std::sort(vals.begin(), vals.end());
+  CHECK(vals == kats::knn_radius_expect);
 }
 
 // src/neighbors/knn_classifier.rs:311-344

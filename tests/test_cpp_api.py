@@ -33,6 +33,10 @@ def write_kats(path):
         f"static const std::vector<std::vector<double>> iris_x = {_vec2(k['kmeans_fit_predict']['x'])};",
         f"static const std::vector<std::vector<double>> knn_euclid_data = {_vec2(e['data'])};",
         f"static const std::vector<double> knn_euclid_query = {_vec(e['query'])};",
+        f"static const std::vector<double> knn_scalar_data = {_vec(k['knn_find']['scalar']['data'])};",
+        f"static const double knn_radius_query = {float(k['knn_find']['scalar_radius']['query'])!r};",
+        f"static const double knn_radius = {float(k['knn_find']['scalar_radius']['radius'])!r};",
+        f"static const std::vector<int> knn_radius_expect = {_vec(k['knn_find']['scalar_radius']['expect_sorted_values'], 'int')};",
         f"static const std::vector<std::vector<double>> clf_x = {_vec2(k['knn_classifier_default']['x'])};",
         f"static const std::vector<int> clf_y = {_vec(k['knn_classifier_default']['y'], 'int')};",
         f"static const std::vector<std::vector<double>> clfw_x = {_vec2(k['knn_classifier_weighted']['x'])};",

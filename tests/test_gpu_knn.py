@@ -6,6 +6,7 @@ import pytest
 
 import oracle
 from smartcore_gb300 import _lib
+from smartcore_gb300.error import Failed
 from smartcore_gb300.neighbors import (KNNAlgorithmName, KNNClassifier, KNNClassifierParameters,
                                        KNNRegressor, KNNRegressorParameters, KNNWeightFunction,
                                        LinearKNNSearch)
@@ -62,6 +63,32 @@ def test_find_wide_exponent_span(form, d):
 
 
 @pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_find_radius_matches_oracle(form, dtype):
+    rng = np.random.default_rng(17)
+    train = rng.normal(size=(5000, 12)).astype(dtype)
+    q = rng.normal(size=(200, 12)).astype(dtype)
+    s = LinearKNNSearch(train, form=form)
+    for radius in (0.5, 1.5, 3.0):
+        counts, idx, dist = s.find_radius_batch(q, radius)
+        rc, ridx, rdist = oracle.knn_find_radius(train, q, radius)
+        assert np.array_equal(counts, rc)
+        assert np.array_equal(idx, ridx)
+        assert np.array_equal(dist, rdist)
+    # a radius that hits exact distances of integer grid data (d <= radius is inclusive)
+    g = rng.integers(-2, 3, size=(3000, 3)).astype(dtype)
+    s2 = LinearKNNSearch(g, form=form)
+    for radius in (1.0, 2.0, np.sqrt(2.0)):
+        counts, idx, dist = s2.find_radius_batch(g[:50], radius)
+        rc, ridx, rdist = oracle.knn_find_radius(g, g[:50], radius)
+        assert np.array_equal(counts, rc) and np.array_equal(idx, ridx) and np.array_equal(dist, rdist)
+    assert s.find_radius(q[0], 1.5) == [(int(i), float(d)) for i, d in
+                                        zip(*oracle.knn_find_radius(train, q[:1], 1.5)[1:])]
+    with pytest.raises(Failed, match="radius should be > 0"):
+        s.find_radius(q[0], 0.0)
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_find_ties_and_duplicates(form):
     # integer grid data: many exact distance ties, replay order matters
     rng = np.random.default_rng(0)
@@ -96,6 +123,11 @@ def test_reference_kats(kats):
     sc = kat["scalar"]
     s1 = LinearKNNSearch(np.array(sc["data"], np.float64)[:, None])
     assert sorted(i for i, _ in s1.find(np.array([float(sc["query"])]), sc["k"])) == sc["expect_sorted_idx"]
+    r = kat["scalar_radius"]  # linear_search.rs:166-174: the values within radius 3 of 5
+    for form in (_lib.FORM_FP64, _lib.FORM_SPLIT_BF16):
+        s2 = LinearKNNSearch(np.array(sc["data"], np.float64)[:, None], form=form)
+        got = s2.find_radius(np.array([float(r["query"])]), r["radius"])
+        assert sorted(int(sc["data"][i]) for i, _ in got) == r["expect_sorted_values"]
 
     w = kats["knn_classifier_weighted"]
     m = KNNClassifier.fit(np.array(w["x"]), np.array(w["y"], np.int64),
