@@ -212,6 +212,45 @@ def bench_knn(torch, local, reps=5, n_query=None, with_fp64=True):
                            "sample": f"C restatement of LinearKNNSearch::find + heap replay on the first "
                                      f"{KNN_CPU_QUERIES} of {KNN_M} queries against all {KNN_N} rows, single thread"}
     out["config"] = {"n_train": KNN_N, "n_query": KNN_M, "d": KNN_D, "k": KNN_K, "classes": 10, "dtype": "f32"}
+    out["find_radius"] = bench_radius(torch, local, xt, xq)
+    return out
+
+
+KNN_RADIUS = 8.0
+RADIUS_CPU_QUERIES = 200
+
+
+def bench_radius(torch, local, xt, xq):
+    """LinearKNNSearch::find_radius on the kNN workload (radius 8.0, ~56 rows per query): queries/s
+    of both forms through the C ABI with host queries and results (counting
+    and filling passes), agreement of the two forms on every query, and the
+    reference's CPU scan on a sample of the queries."""
+    import oracle
+    from smartcore_gb300 import _lib
+    from smartcore_gb300.neighbors import LinearKNNSearch
+    res, out = {}, {}
+    for name, form in (("split_bf16", _lib.FORM_SPLIT_BF16), ("fp64", _lib.FORM_FP64)):
+        s = LinearKNNSearch(xt, form=form)
+        s.find_radius_batch(xq[:1024], KNN_RADIUS)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res[name] = s.find_radius_batch(xq, KNN_RADIUS)
+        dt = time.perf_counter() - t0
+        out[name] = {"queries_per_s": len(xq) / dt, "ms": 1e3 * dt, "neighbours": int(res[name][0].sum())}
+        s.close()
+    out["forms_equal"] = bool(all(np.array_equal(a, b) for a, b in zip(res["split_bf16"], res["fp64"])))
+    t0 = time.perf_counter()
+    rc, ridx, rdist = oracle.knn_find_radius(xt, xq[:RADIUS_CPU_QUERIES], KNN_RADIUS)
+    cpu_s = time.perf_counter() - t0
+    c, idx, dist = res["split_bf16"]
+    nsamp = int(rc.sum())
+    out["oracle_sample_equal"] = bool(np.array_equal(c[:RADIUS_CPU_QUERIES], rc) and
+                                      np.array_equal(idx[:nsamp], ridx) and np.array_equal(dist[:nsamp], rdist))
+    out["cpu_baseline"] = {"value": RADIUS_CPU_QUERIES / cpu_s, "unit": "queries/s", "cores": 1, "kind": "port",
+                           "sample": f"C restatement of LinearKNNSearch::find_radius on the first "
+                                     f"{RADIUS_CPU_QUERIES} queries against all {KNN_N} rows, single thread"}
+    out["config"] = {"radius": KNN_RADIUS, "n_train": KNN_N, "n_query": len(xq), "d": KNN_D,
+                     "e2e": "host queries in, host rows out, both passes"}
     return out
 
 
