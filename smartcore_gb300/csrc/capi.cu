@@ -112,10 +112,13 @@ struct sc_kmeans {
   double *cent = nullptr;       // k x d
   int32_t *labels = nullptr;    // n
   double *dd = nullptr;         // n, k-means++ distances
+  float *dd32 = nullptr;        // n, k-means++ distances rounded up to f32
   double *part = nullptr;       // block partials
   int64_t *sizes = nullptr;     // k
   double *cterms = nullptr;     // k
   double *uniforms = nullptr;   // k - 1
+  void *seed_x = nullptr;       // k x d, k-means++ seed rows (element type)
+  float *seed_cc = nullptr;     // k, k-means++ seed-to-seed distance bounds
   double *xnorm_total = nullptr;
   LloydState *st = nullptr;
   unsigned long long *bits = nullptr;
@@ -145,10 +148,13 @@ static cudaEvent_t *next_timing(sc_kmeans *h) {
 static sc_status kmeans_alloc_k(sc_kmeans *h, int64_t k) {
   if (k == h->k_alloc) { h->k = k; return SC_OK; }
   dfree(h->cent); dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
+  dfree(h->seed_x); dfree(h->seed_cc);
   SC_TRY(dalloc(&h->cent, (size_t)(k * h->d)));
   SC_TRY(dalloc(&h->sizes, (size_t)k));
   SC_TRY(dalloc(&h->cterms, (size_t)(k * h->d)));
   SC_TRY(dalloc(&h->uniforms, (size_t)k));
+  SC_TRY(dalloc((char **)&h->seed_x, (size_t)(k * h->d) * esize(h->dtype)));
+  SC_TRY(dalloc(&h->seed_cc, (size_t)k));
   SC_CUDA(cudaStreamSynchronize(h->stream));
   SC_TRY(update_alloc(&h->upd, h->dtype, h->n, (int)h->d, (int)k, h->absmax, h->num_sms));
   h->k_alloc = k;
@@ -183,8 +189,8 @@ int32_t sc_device_ok(void) {
 void sc_kmeans_destroy(sc_kmeans *h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  dfree(h->x); dfree(h->cent); dfree(h->labels); dfree(h->dd); dfree(h->part);
-  dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
+  dfree(h->x); dfree(h->cent); dfree(h->labels); dfree(h->dd); dfree(h->dd32); dfree(h->part);
+  dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms); dfree(h->seed_x); dfree(h->seed_cc);
   update_free(&h->upd);
   dfree(h->xnorm_total); dfree(h->st); dfree(h->bits);
   split_free(&h->split);
@@ -214,6 +220,7 @@ sc_status sc_kmeans_create(const void *x, int32_t dtype, int32_t layout, int32_t
     if ((r = dalloc((char **)&h->x, (size_t)(n * d) * esize(dtype))) != SC_OK) break;
     if ((r = dalloc(&h->labels, (size_t)n)) != SC_OK) break;
     if ((r = dalloc(&h->dd, (size_t)n)) != SC_OK) break;
+    if ((r = dalloc(&h->dd32, (size_t)n)) != SC_OK) break;
     if ((r = dalloc(&h->part, (size_t)nparts)) != SC_OK) break;
     if ((r = dalloc(&h->st, 1)) != SC_OK) break;
     if ((r = dalloc(&h->bits, 1)) != SC_OK) break;
@@ -266,12 +273,18 @@ sc_status sc_kmeans_seed(sc_kmeans *h, int64_t k, int64_t first_index, const dou
   cudaStream_t s = h->stream;
   if (k > 1) SC_CUDA(cudaMemcpyAsync(h->uniforms, uniforms, (size_t)(k - 1) * sizeof(double), cudaMemcpyHostToDevice, s));
   SC_CUDA(cudaMemcpyAsync(&h->st->pp_chosen, &first_index, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  const size_t row_bytes = (size_t)h->d * esize(h->dtype);
+  SC_CUDA(cudaMemcpyAsync(h->seed_x, (const char *)h->x + (size_t)first_index * row_bytes, row_bytes,
+                          cudaMemcpyDeviceToDevice, s));
   const int nb = pp_block_count(h->n);
   for (int64_t j = 1; j < k; ++j) {  // kmeans.rs:367-397
-    SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(j - 1), h->dd, h->labels, h->part, j == 1, s));
-    SC_TRY(launch_pp_select(h->dd, h->part, h->n, nb, h->uniforms + (j - 1), h->st, s));
+    SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(j - 1), h->dd, h->dd32, h->labels,
+                            h->part, j == 1, h->seed_cc, s));
+    SC_TRY(launch_pp_select(h->dtype, h->x, (int)h->d, h->dd, h->part, h->n, nb, h->uniforms + (j - 1), h->st,
+                            h->seed_x, h->seed_cc, (int)j, s));
   }
-  SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(k - 1), h->dd, h->labels, nullptr, k == 1, s));  // :399-410
+  SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(k - 1), h->dd, h->dd32, h->labels,
+                          nullptr, k == 1, h->seed_cc, s));  // :399-410
   // initial centroids: means of the seeding partition (kmeans.rs:275-292)
   SC_TRY(launch_update(&h->upd, h->dtype, h->x, h->n, (int)h->d, h->labels, (int)k, nullptr, s));
   SC_TRY(launch_finalize(&h->upd, h->cent, h->sizes, (int)k, (int)h->d, nullptr, 1, nullptr, s));

@@ -43,7 +43,7 @@ struct LloydState {
   int32_t done;        // break rule taken (kmeans.rs:305-309)
   int32_t stop;        // 1: apply the break rule; 0: run every iteration
   int32_t err;         // device-side consistency failure code (0 = none)
-  int32_t pp_flag;     // k-means++: current draw needs the sequential replay
+  int32_t reserved;
   int64_t pp_chosen;   // k-means++: row index of the current seed
 };
 
@@ -80,13 +80,19 @@ sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
                              const double *cent, int k, int32_t *labels,
                              double *part, const LloydState *st,
                              cudaStream_t s);
+// seed_cc (k entries, may be null): lower bounds of the squared distances
+// from the current seed to the earlier ones, written by launch_pp_select;
+// dd32 (n entries, may be null): d rounded up to f32, the far test's copy
+// (f32 rows with d <= 128 only).
 sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
                            const LloydState *st, int32_t label_of_seed,
-                           double *dd, int32_t *labels, double *part,
-                           int first_pass, cudaStream_t s);
-sc_status launch_pp_select(const double *dd, const double *part, int64_t n,
-                           int nb, const double *uniform, LloydState *st,
-                           cudaStream_t s);
+                           double *dd, float *dd32, int32_t *labels, double *part,
+                           int first_pass, const float *seed_cc, cudaStream_t s);
+// Picks seed j into st->pp_chosen and its row into seed_x[j] (k x d, element
+// type); writes seed_cc[0..j).
+sc_status launch_pp_select(int dtype, const void *x, int d, const double *dd, const double *part,
+                           int64_t n, int nb, const double *uniform, LloydState *st,
+                           void *seed_x, float *seed_cc, int j, cudaStream_t s);
 sc_status launch_knn_fp64(int dtype, const void *train, int64_t n, int d,
                           const void *queries, int64_t m, int k, int64_t *idx,
                           double *dist, cudaStream_t s);

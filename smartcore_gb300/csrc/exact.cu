@@ -6,6 +6,9 @@
 // multiply-add is ever fused (rustc never fuses either).
 #include <float.h>
 
+#include <algorithm>
+#include <type_traits>
+
 #include "common.cuh"
 #include "exactsum.cuh"
 
@@ -129,17 +132,46 @@ sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
 // kmeans.rs:367-379 and :399-410).  The seed row is st->pp_chosen; the
 // distance uses the element type's arithmetic (a - b and its square in T,
 // summed in f64).  first_pass initialises d = f64::MAX and y = 0 (:357, :364).
+//
+// Rows far from the new seed are not read.  A row whose current seed a
+// (labels[i]) and the new seed c satisfy |c - c_a| >= 2 |x - c_a| has
+// |x - c| >= |x - c_a| (triangle inequality), so the reference's strict
+// `dist < d[i]` test keeps d[i].  The test is made rigorous against the
+// computed values: the reference's D = computed |x - c|^2 satisfies
+//   (1 - eta) r^2 - A <= D <= (1 + eta) r^2 + A
+// for the real r = |x - c| (terms in T, f64 sum of d terms; eta and A below),
+// so with cc_lo <= |c - c_a|^2 (pp_seed_gaps) the row keeps its distance when
+//   cc_lo >= 4 (1 + 3 eta) (D + A)                     (pp_far, pp_far32)
+// since then the new seed's computed distance is >= D.
 // ---------------------------------------------------------------------------
 constexpr int kPPThreads = 256;
 
 int pp_block_count(int64_t n) { return (int)((n + kPPThreads - 1) / kPPThreads); }
+
+// f32 terms: fl32(fl32(x - c)^2) is within (1 +- 2^-24)^3 of (x - c)^2, or
+// within 2^-149 on underflow; the f64 sum adds d 2^-53 relative.  eta =
+// 2^-22 covers d <= 2^25, A = d 2^-140.  f64 terms: eta = (d + 4) 2^-52,
+// A = d 2^-1070.
+struct PPFar {
+  double mul, abs_;  // keep when cc_lo >= mul (D + abs_)
+};
+
+PPFar pp_far_bound(int dtype, int d) {
+  const double eta = dtype == SC_F32 ? 0x1p-22 : (double)(d + 4) * 0x1p-52;
+  const double a = dtype == SC_F32 ? (double)d * 0x1p-140 : (double)d * 0x1p-1070;
+  return PPFar{4.0 * (1.0 + 3.0 * eta), a};
+}
+
+__device__ __forceinline__ bool pp_far(double cc_lo, double D, PPFar f) {
+  return cc_lo >= __dmul_rn(f.mul, __dadd_rn(D, f.abs_));
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kPPThreads)
 pp_update_kernel(const T *__restrict__ x, int64_t n, int d, const LloydState *st,
                  int32_t label_of_seed, double *__restrict__ dd,
                  int32_t *__restrict__ labels, double *__restrict__ part,
-                 int first_pass, int lg_d) {
+                 int first_pass, int lg_d, const float *__restrict__ seed_cc, PPFar far) {
   extern __shared__ unsigned char smraw[];
   T *cen = reinterpret_cast<T *>(smraw);
   const int64_t ci = st->pp_chosen;
@@ -148,103 +180,275 @@ pp_update_kernel(const T *__restrict__ x, int64_t n, int d, const LloydState *st
   const int64_t i = (int64_t)blockIdx.x * kPPThreads + threadIdx.x;
   double v = 0.0;
   if (i < n) {
-    const T *xr = x + i * (int64_t)d;
-    double s = 0.0;
-    bool exact = false;
-    // f32 rows: the same value from the integer reproduction of the sequential sum
-    if constexpr (sizeof(T) == 4) exact = sqd_seq_f32(xr, cen, d, lg_d, s);
-    if (!exact) {
-      s = 0.0;
-      for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term(xr[j], cen[j]));
-    }
     double cur = first_pass ? DBL_MAX : dd[i];
     int32_t lab = first_pass ? 0 : labels[i];
-    if (s < cur) { cur = s; lab = label_of_seed; }
-    dd[i] = cur;
-    labels[i] = lab;
+    if (first_pass || !seed_cc || !pp_far((double)seed_cc[lab], cur, far)) {
+      const T *xr = x + i * (int64_t)d;
+      double s = 0.0;
+      bool exact = false;
+      // f32 rows: the same value from the integer reproduction of the sequential sum
+      if constexpr (sizeof(T) == 4) exact = sqd_seq_f32(xr, cen, d, lg_d, s);
+      if (!exact) {
+        s = 0.0;
+        for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term(xr[j], cen[j]));
+      }
+      if (s < cur) { cur = s; lab = label_of_seed; }
+      dd[i] = cur;
+      labels[i] = lab;
+    }
     v = cur;
   }
   const double tot = block_sum_fixed<kPPThreads>(v);
   if (threadIdx.x == 0 && part) part[blockIdx.x] = tot;
 }
 
-// f32 rows, d <= 128: the same update with each warp's 32 rows staged in
-// shared memory by coalesced loads (row stride d + 1: conflict-free when each
-// lane then walks its own row).  Thread t still handles row 256 b + t, so the
-// block partials are the same.
+// Row stride (floats) of the staged tiles.  vec4: a multiple of 4 with an odd
+// number of 16-byte units, so 8 lanes reading float4s of 8 rows hit 8
+// different 4-bank groups; scalar: d + 1.
+__host__ __device__ __forceinline__ int pp_stage_ld(int d, int vec4) {
+  return vec4 ? (((d >> 2) & 1) ? d + 8 : d + 4) : d + 1;
+}
+
+// ---- f32 rows, d <= 128: one launch per draw ----
+// pp_draw_kernel: one warp per 256-row block of d.  The far test runs in f32
+// from (d32 = d rounded up, y, seed_cc) and reads no row; the rows it leaves
+// are listed and read coalesced (whole rows per warp instruction, four
+// instructions in flight) for the f32 lower bound; the rows that bound cannot
+// settle either (the rows whose distance may drop) are listed again and get
+// the reference's exact sequential sum, one row per lane.  The warp then writes the block's fixed-order partial sum
+// of d for the selection.  The first draw (every row exact) runs
+// pp_first_kernel, which stages the rows in shared memory, and then
+// pp_partials_kernel.
+constexpr int kPPWarps = kPPThreads / 32;
+
+// f32 form of the far test: keep when cc >= mul (D32 + abs_), both roundings
+// upward, with D32 >= D.
+struct PPFar32 {
+  float mul, abs_;
+};
+
+PPFar32 pp_far_bound32(int d) {
+  // eta = 2^-22: 4 (1 + 3 eta) is exact in f32; A = d 2^-140 is an f32 subnormal
+  return PPFar32{4.0f * (1.0f + 3.0f * 0x1p-22f), (float)d * 0x1p-140f};
+}
+
+__device__ __forceinline__ bool pp_far32(float cc, float D32, PPFar32 f) {
+  return cc >= __fmul_ru(f.mul, __fadd_ru(D32, f.abs_));
+}
+
+// Fixed-order sum of the 256 values of block b: lane l adds rows 32 g + l for
+// g = 0..7 in order, then the lanes by a shuffle tree (depth 8 + 5).
+__device__ __forceinline__ double pp_block_partial(const double *__restrict__ dd, int64_t n, int64_t b) {
+  const int lane = threadIdx.x & 31;
+  double t = 0.0;
+#pragma unroll
+  for (int g = 0; g < kPPWarps; ++g) {
+    const int64_t i = b * kPPThreads + g * 32 + lane;
+    t = __dadd_rn(t, i < n ? dd[i] : 0.0);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t = __dadd_rn(t, __shfl_down_sync(0xffffffffu, t, o));
+  return t;
+}
+
+template <int VEC>
 __global__ void __launch_bounds__(kPPThreads)
-pp_update_staged_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *st,
-                        int32_t label_of_seed, double *__restrict__ dd, int32_t *__restrict__ labels,
-                        double *__restrict__ part, int first_pass, int lg_d) {
-  extern __shared__ float smf[];
-  float *cen = smf;                                                // d
+pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *st, int32_t label_of_seed,
+               double *__restrict__ dd, float *__restrict__ dd32, int32_t *__restrict__ labels,
+               double *__restrict__ part, int64_t nb, int lg_d, const float *__restrict__ seed_cc,
+               PPFar32 far) {
+  using V = typename std::conditional<VEC == 4, float4, float>::type;
+  constexpr int NP = 4;                 // row passes with loads in flight together
+  constexpr int UM = VEC == 4 ? 1 : 4;  // loads per lane per row (d <= 128)
+  __shared__ __align__(16) float s_cen[128];
+  __shared__ uint8_t s_need[kPPWarps][kPPThreads];  // the warp's rows left by the far test
+  __shared__ float s_cur[kPPWarps][kPPThreads];     // and their d32
+  __shared__ uint8_t s_ex[kPPWarps][kPPThreads];    // rows that need the exact sum
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float *tile = smf + ((d + 3) & ~3) + (size_t)w * 32 * (d + 1);  // 32 rows x (d + 1)
+  const int64_t ci = st->pp_chosen;
+  for (int t = threadIdx.x; t < d; t += kPPThreads) s_cen[t] = x[ci * d + t];
+  __syncthreads();
+  // a row is `units` loads of VEC floats; p lanes per row (a power of two),
+  // R = 32 / p rows per warp instruction
+  const int units = d / VEC;
+  int p = 1;
+  while (p < units && p < 32) p <<= 1;
+  const int R = 32 / p, seg = lane / p, unit = lane - seg * p;
+  const float lbf = 1.f - 1.05f * d * 0x1p-24f;
+  const unsigned lt = (1u << lane) - 1u;
+  const int64_t nw = (int64_t)gridDim.x * kPPWarps;
+  for (int64_t b = (int64_t)blockIdx.x * kPPWarps + w; b < nb; b += nw) {
+    const int64_t rb = b * kPPThreads;  // first row of the block
+    // far test of the block's 8 groups, loads issued together
+    float c32[kPPWarps];
+    int32_t lb[kPPWarps];
+#pragma unroll
+    for (int g = 0; g < kPPWarps; ++g) {
+      const int64_t i = rb + g * 32 + lane;
+      c32[g] = i < n ? dd32[i] : 0.f;
+      lb[g] = i < n ? labels[i] : 0;
+    }
+    int cnt = 0;  // rows listed in s_need
+#pragma unroll
+    for (int g = 0; g < kPPWarps; ++g) {
+      const int64_t i = rb + g * 32 + lane;
+      const bool need = i < n && !pp_far32(seed_cc[lb[g]], c32[g], far);
+      const unsigned m = __ballot_sync(0xffffffffu, need);
+      if (need) {
+        const int pos = cnt + __popc(m & lt);
+        s_need[w][pos] = (uint8_t)(g * 32 + lane);
+        s_cur[w][pos] = c32[g];
+      }
+      cnt += __popc(m);
+    }
+    __syncwarp();
+    // f32 lower bound of the listed rows, R rows per load, NP loads in flight
+    int exn = 0;  // rows listed in s_ex
+    for (int it = 0; it < cnt; it += R * NP) {
+      int rq[NP];
+      V val[NP][UM];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const int idx = it + q * R + seg;
+        rq[q] = idx < cnt ? (int)s_need[w][idx] : -1;
+#pragma unroll
+        for (int k = 0; k < UM; ++k) {
+          const int uu = unit + k * p;
+          if (rq[q] >= 0 && uu < units) val[q][k] = reinterpret_cast<const V *>(x + (rb + rq[q]) * d)[uu];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        // The reference's terms q_t = fl32((x_t - c_t)^2) summed in f32 (any
+        // order, depth <= d) bound its f64 sum from below by s32 (1 - 1.05 d
+        // 2^-24): when that exceeds the current distance the row keeps it.
+        float s32 = 0.f;
+#pragma unroll
+        for (int k = 0; k < UM; ++k) {
+          const int uu = unit + k * p;
+          if (rq[q] >= 0 && uu < units) {
+            if constexpr (VEC == 4) {
+              const float4 a = val[q][k];
+              const float4 c = reinterpret_cast<const float4 *>(s_cen)[uu];
+              float r = __fsub_rn(a.x, c.x);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+              r = __fsub_rn(a.y, c.y);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+              r = __fsub_rn(a.z, c.z);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+              r = __fsub_rn(a.w, c.w);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+            } else {
+              const float r = __fsub_rn(val[q][k], s_cen[uu]);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+            }
+          }
+        }
+        for (int o = p >> 1; o > 0; o >>= 1) s32 = __fadd_rn(s32, __shfl_xor_sync(0xffffffffu, s32, o));
+        const int idx = it + q * R + seg;
+        const bool ex = rq[q] >= 0 && unit == 0 && !(__fmul_rd(s32, lbf) > s_cur[w][idx]);
+        const unsigned em = __ballot_sync(0xffffffffu, ex);
+        if (ex) s_ex[w][exn + __popc(em & lt)] = (uint8_t)rq[q];
+        exn += __popc(em);
+      }
+    }
+    __syncwarp();
+    // the rows whose distance may drop: the exact value, one row per lane
+    for (int e = lane; e < exn; e += 32) {
+      const int64_t i = rb + s_ex[w][e];
+      const float *xr = x + i * d;
+      double sq = 0.0;
+      if (!sqd_seq_f32(xr, s_cen, d, lg_d, sq)) {
+        sq = 0.0;
+        for (int j = 0; j < d; ++j) sq = __dadd_rn(sq, sq_term(xr[j], s_cen[j]));
+      }
+      if (sq < dd[i]) {
+        dd[i] = sq;
+        dd32[i] = __double2float_ru(sq);
+        labels[i] = label_of_seed;
+      }
+    }
+    __syncwarp();
+    if (part) {
+      const double t = pp_block_partial(dd, n, b);
+      if (lane == 0) part[b] = t;
+    }
+    __syncwarp();  // s_need / s_ex are refilled for the next block
+  }
+}
+
+// First draw: every row's exact distance to the first seed (d = f64::MAX and
+// y = 0 before it, kmeans.rs:357, :364), rows staged in shared memory by
+// asynchronous copies (16 bytes when d % 4 == 0, else 4), one row per lane.
+__global__ void __launch_bounds__(kPPThreads)
+pp_first_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *st,
+                double *__restrict__ dd, float *__restrict__ dd32, int32_t *__restrict__ labels,
+                int lg_d, int vec4) {
+  extern __shared__ __align__(16) float smf[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ld = pp_stage_ld(d, vec4);
+  float *cen = smf;                                          // d (padded to 4)
+  float *tile = smf + ((d + 3) & ~3) + (size_t)w * 32 * ld;  // 32 rows x ld
   const int64_t ci = st->pp_chosen;
   for (int t = threadIdx.x; t < d; t += kPPThreads) cen[t] = x[ci * d + t];
-  const int64_t r0 = (int64_t)blockIdx.x * kPPThreads + w * 32;
-  // asynchronous 4-byte copies: every row of the warp in flight at once
-  for (int rr = 0; rr < 32; ++rr) {
-    const int64_t i = r0 + rr;
-    if (i < n)
-      for (int c = lane; c < d; c += 32) {
-        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(tile + rr * (d + 1) + c);
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(x + i * d + c) : "memory");
+  __syncthreads();
+  const int64_t groups = (n + 31) / 32;
+  const int64_t nw = (int64_t)gridDim.x * kPPWarps;
+  const int units = vec4 ? d >> 2 : d;
+  for (int64_t g = (int64_t)blockIdx.x * kPPWarps + w; g < groups; g += nw) {
+    const int64_t r0 = g * 32, row = r0 + lane;
+    const int nrows = n - r0 < 32 ? (int)(n - r0) : 32;
+    // (row, unit) pairs of the warp's rows spread over the lanes
+    int rr = lane / units, c = lane - rr * units;
+    while (rr < nrows) {
+      if (vec4) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(tile + rr * ld + 4 * c);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(x + (r0 + rr) * d + 4 * c) : "memory");
+      } else {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(tile + rr * ld + c);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(x + (r0 + rr) * d + c) : "memory");
       }
-  }
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  __syncthreads();
-  __shared__ int s_q[kPPThreads];  // block rows that need the exact distance
-  __shared__ double s_v[kPPThreads];
-  __shared__ int s_qn;
-  if (threadIdx.x == 0) s_qn = 0;
-  __syncthreads();
-  const int64_t i = r0 + lane;
-  double cur = DBL_MAX;
-  if (i < n) {
-    const float *xr = tile + lane * (d + 1);
-    cur = first_pass ? DBL_MAX : dd[i];
-    // The reference's terms q_t = fl32((x_t - c_t)^2) summed in f32 bound its
-    // f64 sum from below by s32 (1 - 1.05 d 2^-24): when that exceeds the
-    // current distance, the row keeps it and the exact sum is not needed.
-    float s32 = 0.f;
-    for (int j = 0; j < d; ++j) {
-      const float r = __fsub_rn(xr[j], cen[j]);
-      s32 = __fadd_rn(s32, __fmul_rn(r, r));
+      c += 32;
+      while (c >= units) { c -= units; ++rr; }
     }
-    const bool keep = !first_pass && __fmul_rd(s32, 1.f - 1.05f * d * 0x1p-24f) > __double2float_ru(cur);
-    if (!keep) s_q[atomicAdd(&s_qn, 1)] = threadIdx.x;
-  }
-  s_v[threadIdx.x] = i < n ? cur : 0.0;
-  __syncthreads();
-  // the rows that need it, on contiguous threads (full warps)
-  const int qn = s_qn;
-  for (int qi = threadIdx.x; qi < qn; qi += kPPThreads) {
-    const int t = s_q[qi];
-    const int64_t row = (int64_t)blockIdx.x * kPPThreads + t;
-    const float *xr = smf + ((d + 3) & ~3) + (size_t)(t >> 5) * 32 * (d + 1) + (t & 31) * (d + 1);
-    double sq = 0.0;
-    if (!sqd_seq_f32(xr, cen, d, lg_d, sq)) {
-      sq = 0.0;
-      for (int j = 0; j < d; ++j) sq = __dadd_rn(sq, sq_term(xr[j], cen[j]));
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncwarp();
+    if (lane < nrows) {
+      const float *xr = tile + lane * ld;
+      double sq = 0.0;
+      if (!sqd_seq_f32(xr, cen, d, lg_d, sq)) {
+        sq = 0.0;
+        for (int j = 0; j < d; ++j) sq = __dadd_rn(sq, sq_term(xr[j], cen[j]));
+      }
+      const double v = sq < DBL_MAX ? sq : DBL_MAX;
+      dd[row] = v;
+      dd32[row] = __double2float_ru(v);
+      labels[row] = 0;
     }
-    double c = s_v[t];
-    int32_t lab = first_pass ? 0 : labels[row];
-    if (sq < c) { c = sq; lab = label_of_seed; }
-    dd[row] = c;
-    labels[row] = lab;
-    s_v[t] = c;
+    __syncwarp();  // the tile is refilled by the next group
   }
-  __syncthreads();
-  const double v = s_v[threadIdx.x];
-  const double tot = block_sum_fixed<kPPThreads>(v);
-  if (threadIdx.x == 0 && part) part[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kPPThreads)
+pp_partials_kernel(const double *__restrict__ dd, int64_t n, int64_t nb, double *__restrict__ part) {
+  const int64_t b = (int64_t)blockIdx.x * kPPWarps + (threadIdx.x >> 5);
+  if (b >= nb) return;
+  const double t = pp_block_partial(dd, n, b);
+  if ((threadIdx.x & 31) == 0) part[b] = t;
+}
+
+int device_sms() {
+  static int sms[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 132;
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms[dev] = 132;
+  return sms[dev];
 }
 
 sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
                            const LloydState *st, int32_t label_of_seed,
-                           double *dd, int32_t *labels, double *part,
-                           int first_pass, cudaStream_t s) {
+                           double *dd, float *dd32, int32_t *labels, double *part,
+                           int first_pass, const float *seed_cc, cudaStream_t s) {
   const int grid = pp_block_count(n);
   const size_t smem = (size_t)d * (dtype == SC_F32 ? 4 : 8);
   if (smem > 48 * 1024) {
@@ -253,16 +457,42 @@ sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
   }
   int lg_d = 0;
   while ((1 << lg_d) < d) ++lg_d;
-  if (dtype == SC_F32 && d <= 128) {
-    const size_t ssm = ((size_t)((d + 3) & ~3) + (size_t)kPPThreads * (d + 1)) * sizeof(float);
-    SC_CUDA(cudaFuncSetAttribute(pp_update_staged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
-    pp_update_staged_kernel<<<grid, kPPThreads, ssm, s>>>((const float *)x, n, d, st, label_of_seed, dd, labels,
-                                                          part, first_pass, lg_d);
-  } else if (dtype == SC_F32)
-    pp_update_kernel<float><<<grid, kPPThreads, smem, s>>>((const float *)x, n, d, st, label_of_seed, dd, labels, part, first_pass, lg_d);
-  else
-    pp_update_kernel<double><<<grid, kPPThreads, smem, s>>>((const double *)x, n, d, st, label_of_seed, dd, labels, part, first_pass, lg_d);
-  SC_LAUNCHED();
+  if (dtype == SC_F32 && d <= 128 && dd32) {
+    const float *xf = (const float *)x;
+    const int sms = device_sms();
+    const int vec4 = (d % 4 == 0 && ((uintptr_t)x & 15) == 0) ? 1 : 0;
+    const int warp_blocks = (grid + kPPWarps - 1) / kPPWarps;
+    if (first_pass) {
+      const size_t ssm = ((size_t)((d + 3) & ~3) + (size_t)kPPThreads * pp_stage_ld(d, vec4)) * sizeof(float);
+      SC_CUDA(cudaFuncSetAttribute(pp_first_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+      const int per_sm = std::max(1, std::min(8, (int)((225 * 1024) / (ssm + 1024))));
+      const int g1 = (int)std::min<int64_t>((int64_t)sms * per_sm, (int64_t)warp_blocks);
+      pp_first_kernel<<<g1, kPPThreads, ssm, s>>>(xf, n, d, st, dd, dd32, labels, lg_d, vec4);
+      SC_LAUNCHED();
+      if (part) {
+        pp_partials_kernel<<<warp_blocks, kPPThreads, 0, s>>>(dd, n, grid, part);
+        SC_LAUNCHED();
+      }
+    } else {
+      const int g1 = std::min(warp_blocks, sms * 8);
+      const PPFar32 far = pp_far_bound32(d);
+      if (vec4)
+        pp_draw_kernel<4><<<g1, kPPThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
+                                                    lg_d, seed_cc, far);
+      else
+        pp_draw_kernel<1><<<g1, kPPThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
+                                                    lg_d, seed_cc, far);
+      SC_LAUNCHED();
+    }
+  } else if (dtype == SC_F32) {
+    pp_update_kernel<float><<<grid, kPPThreads, smem, s>>>((const float *)x, n, d, st, label_of_seed, dd, labels,
+                                                           part, first_pass, lg_d, seed_cc, pp_far_bound(dtype, d));
+    SC_LAUNCHED();
+  } else {
+    pp_update_kernel<double><<<grid, kPPThreads, smem, s>>>((const double *)x, n, d, st, label_of_seed, dd, labels,
+                                                            part, first_pass, lg_d, seed_cc, pp_far_bound(dtype, d));
+    SC_LAUNCHED();
+  }
   return SC_OK;
 }
 
@@ -271,13 +501,17 @@ sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
 // d, cutoff = u * sum, index = first i whose sequential prefix >= cutoff.
 //
 // The sequential prefix S_i is inherently serial.  Here a parallel prefix
-// Q_i (block partials, then a chunked scan) locates the candidate, and the
-// choice is certified with a rigorous bound: all d_i >= 0, so
-// |S_i - P_i| <= gamma_i P_i (Higham) for the exact prefix P_i, and Q_i obeys
-// the same bound with the depth of its own summation tree.  Only when the
-// cutoff falls inside the uncertainty band of the crossing is the draw
-// resolved by pp_replay_kernel, which recomputes S exactly as the reference
-// does, on one thread.
+// Q_i (block partials, a block-wide scan of chunk sums, then warp walks over
+// the crossing chunk's partials and the crossing block's rows) locates the
+// candidate, and the choice is certified with a rigorous bound: all d_i >= 0,
+// so |S_i - P_i| <= gamma_i P_i (Higham) for the exact prefix P_i, and Q_i
+// obeys the same bound with the depth of its own summation tree.  Only when
+// the cutoff falls inside the uncertainty band of the crossing does the
+// kernel recompute S exactly as the reference does, on one thread.
+//
+// The same launch then copies the seed's row to seed_x[j] and writes the
+// lower bounds seed_cc[a] of |x_pick - seed_x[a]|^2 for a < j, which the next
+// update uses for its far test.
 // ---------------------------------------------------------------------------
 constexpr int kSelThreads = 1024;
 
@@ -286,101 +520,210 @@ __device__ __forceinline__ double pp_tol(double q, double depth) {
   return depth * 1.1102230246251565e-16 * 1.01 * q;
 }
 
+__device__ __forceinline__ double warp_incl_scan(double v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double y = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v = __dadd_rn(v, y);
+  }
+  return v;
+}
+
+struct Crossing {
+  int t;         // first index whose prefix reaches the cutoff (len: none)
+  double q;      // prefix through t (the total when none)
+  double qprev;  // prefix before t
+};
+
+// Whole warp: prefixes base + v[0] + ... + v[t] of len values, 8 consecutive
+// values per lane (sequential within the lane, a shuffle scan across lanes,
+// summation depth <= 8 + 5 + 2 per 256 values).
+__device__ Crossing warp_first_crossing(const double *__restrict__ v, int len, double base, double cutoff) {
+  constexpr int E = 8;
+  const int lane = threadIdx.x & 31;
+  for (int r0 = 0; r0 < len; r0 += 32 * E) {
+    const int s0 = r0 + lane * E;
+    double a[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) a[e] = s0 + e < len ? v[s0 + e] : 0.0;
+    double run = 0.0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      run = __dadd_rn(run, a[e]);
+      a[e] = run;
+    }
+    const double incl = warp_incl_scan(run);
+    const double prev = __shfl_up_sync(0xffffffffu, incl, 1);
+    const double off = lane ? __dadd_rn(base, prev) : base;
+    int first = E;
+    double q = 0.0, qp = 0.0;
+#pragma unroll
+    for (int e = E - 1; e >= 0; --e) {
+      const double qe = __dadd_rn(off, a[e]);
+      if (s0 + e < len && qe >= cutoff) {
+        first = e;
+        q = qe;
+        qp = e ? __dadd_rn(off, a[e - 1]) : off;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, first < E);
+    if (m) {
+      const int L = __ffs(m) - 1;
+      Crossing r;
+      r.t = __shfl_sync(0xffffffffu, s0 + first, L);
+      r.q = __shfl_sync(0xffffffffu, q, L);
+      r.qprev = __shfl_sync(0xffffffffu, qp, L);
+      return r;
+    }
+    base = __dadd_rn(base, __shfl_sync(0xffffffffu, incl, 31));
+  }
+  return Crossing{len, base, base};
+}
+
+// Lower bound (an f32 value) of the real |x_p - x_a|^2 for every earlier seed
+// a < j (rows seed_x[a]), one warp per seed, four seeds per pass; each lane
+// sums its strided terms in order, then a shuffle tree (depth m <= d + 5).
+//   f32 rows, f32 arithmetic: g = fl(x_p - x_a) is within 2^-24 |x_p - x_a|
+//     (exact when subnormal), fl(g^2) within 2^-24 relative or 2^-150, and each
+//     addition of nonnegative terms within 2^-24, so the real value is at least
+//     (s - d 2^-149)(1 - (d + 10) 2^-23), evaluated with downward rounding.
+//   f64 rows, f64 arithmetic: at least s (1 - (d + 16) 2^-52) - d 2^-1068,
+//     rounded down to f32.
+template <typename T>
+__device__ void pp_seed_gaps(const T *__restrict__ xp, int d, const T *__restrict__ seed_x, int j,
+                             float *__restrict__ seed_cc) {
+  constexpr int kW = kSelThreads / 32, kQ = 4;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int a0 = w; a0 < j; a0 += kW * kQ) {
+    T s[kQ];
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) s[q] = (T)0;
+    for (int t = lane; t < d; t += 32) {
+      const T xv = xp[t];
+#pragma unroll
+      for (int q = 0; q < kQ; ++q) {
+        const int a = a0 + q * kW;
+        if (a < j) {
+          if constexpr (sizeof(T) == 4) {
+            const float g = __fsub_rn(xv, seed_x[(int64_t)a * d + t]);
+            s[q] = __fadd_rn(s[q], __fmul_rn(g, g));
+          } else {
+            const double g = __dsub_rn(xv, seed_x[(int64_t)a * d + t]);
+            s[q] = __dadd_rn(s[q], __dmul_rn(g, g));
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+      T v = s[q];
+      float lo;
+      if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+        const float rel = 1.0f - (float)(d + 10) * 0x1p-23f;  // exact for d <= 2^13
+        lo = __fmul_rd(__fsub_rd(v, (float)d * 0x1p-149f), rel);
+      } else {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+        lo = __double2float_rd(__dsub_rn(__dmul_rn(v, 1.0 - (double)(d + 16) * 0x1p-52), (double)d * 0x1p-1068));
+      }
+      const int a = a0 + q * kW;
+      if (lane == 0 && a < j) seed_cc[a] = fmaxf(0.f, lo);
+    }
+  }
+}
+
+template <typename T>
 __global__ void __launch_bounds__(kSelThreads)
-pp_select_kernel(const double *__restrict__ dd, const double *__restrict__ part,
-                 int64_t n, int nb, const double *__restrict__ uniform,
-                 LloydState *st) {
-  __shared__ double scan[kSelThreads];
+pp_select_kernel(const T *__restrict__ x, int d, const double *__restrict__ dd,
+                 const double *__restrict__ part, int64_t n, int nb,
+                 const double *__restrict__ uniform, LloydState *st,
+                 T *__restrict__ seed_x, float *__restrict__ seed_cc, int j) {
+  __shared__ double s_incl[kSelThreads];  // inclusive prefix of the chunk sums
+  __shared__ double s_wtot[32];
   __shared__ int s_chunk;
-  const int t = threadIdx.x;
+  __shared__ long long s_pick;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int chunk = (nb + kSelThreads - 1) / kSelThreads;
   const int b0 = min(nb, t * chunk), b1 = min(nb, b0 + chunk);
   double loc = 0.0;
   for (int b = b0; b < b1; ++b) loc = __dadd_rn(loc, part[b]);
-  scan[t] = loc;
+  // block-wide inclusive scan: warp scans, then a scan of the warp totals
+  double v = warp_incl_scan(loc);
+  if (lane == 31) s_wtot[w] = v;
   if (t == 0) s_chunk = kSelThreads;
   __syncthreads();
-  for (int o = 1; o < kSelThreads; o <<= 1) {  // inclusive Hillis-Steele scan
-    double add = t >= o ? scan[t - o] : 0.0;
-    __syncthreads();
-    scan[t] = __dadd_rn(scan[t], add);
-    __syncthreads();
-  }
-  const double total = scan[kSelThreads - 1];
+  if (w == 0) s_wtot[lane] = warp_incl_scan(s_wtot[lane]);
+  __syncthreads();
+  if (w > 0) v = __dadd_rn(v, s_wtot[w - 1]);
+  s_incl[t] = v;
+  __syncthreads();
+  const double total = s_incl[kSelThreads - 1];
   const double u = *uniform;
   const double cutoff = __dmul_rn(u, total);
   const double depth_q = (double)chunk + 2.0 * kSelThreads + 2.0 * kPPThreads + 64.0;
-  const double excl = t > 0 ? scan[t - 1] : 0.0;
-  if (b1 > b0 && scan[t] >= cutoff && !(excl >= cutoff)) atomicMin(&s_chunk, t);
+  const double excl = t > 0 ? s_incl[t - 1] : 0.0;
+  if (b1 > b0 && v >= cutoff && !(excl >= cutoff)) atomicMin(&s_chunk, t);
   __syncthreads();
-  if (t != 0) return;
-  const bool finite = isfinite(total) && total < DBL_MAX;
-  const double tol_tot = pp_tol(total, (double)n + depth_q);
-  const double cut_lo = __dmul_rn(u, __dsub_rn(total, tol_tot));
-  const double cut_hi = __dmul_rn(u, __dadd_rn(total, tol_tot));
-  int64_t pick = -1;
-  if (finite && s_chunk < kSelThreads) {
-    const int c = s_chunk;
-    const int cb0 = c * chunk, cb1 = min(nb, cb0 + chunk);
-    double base = c > 0 ? scan[c - 1] : 0.0;
-    int b = cb0;
-    for (; b < cb1; ++b) {
-      const double nxt = __dadd_rn(base, part[b]);
-      if (nxt >= cutoff) break;
-      base = nxt;
-    }
-    if (b < cb1) {
-      const int64_t i0 = (int64_t)b * kPPThreads, i1 = min(n, i0 + kPPThreads);
-      double q = base, qprev = base;
-      int64_t i = i0;
-      for (; i < i1; ++i) {
-        qprev = q;
-        q = __dadd_rn(q, dd[i]);
-        if (q >= cutoff) break;
-      }
-      if (i < i1) {
-        const bool above = __dsub_rn(q, pp_tol(q, (double)i + depth_q)) >= cut_hi;
-        const bool below = i == 0 ? (0.0 < cut_lo)
-                                  : (__dadd_rn(qprev, pp_tol(qprev, (double)i + depth_q)) < cut_lo);
-        if (above && below) pick = i;
+  if (w == 0) {
+    const bool finite = isfinite(total) && total < DBL_MAX;
+    const double tol_tot = pp_tol(total, (double)n + depth_q);
+    const double cut_lo = __dmul_rn(u, __dsub_rn(total, tol_tot));
+    const double cut_hi = __dmul_rn(u, __dadd_rn(total, tol_tot));
+    int64_t pick = -1;
+    if (finite && s_chunk < kSelThreads) {
+      const int c = s_chunk;
+      const int cb0 = c * chunk, cb1 = min(nb, cb0 + chunk);
+      const Crossing cb = warp_first_crossing(part + cb0, cb1 - cb0, c > 0 ? s_incl[c - 1] : 0.0, cutoff);
+      if (cb.t < cb1 - cb0) {
+        const int64_t i0 = (int64_t)(cb0 + cb.t) * kPPThreads, i1 = min(n, i0 + kPPThreads);
+        const Crossing ci = warp_first_crossing(dd + i0, (int)(i1 - i0), cb.qprev, cutoff);
+        if (ci.t < i1 - i0) {
+          const int64_t i = i0 + ci.t;
+          const bool above = __dsub_rn(ci.q, pp_tol(ci.q, (double)i + depth_q)) >= cut_hi;
+          const bool below = i == 0 ? (0.0 < cut_lo)
+                                    : (__dadd_rn(ci.qprev, pp_tol(ci.qprev, (double)i + depth_q)) < cut_lo);
+          if (above && below) pick = i;
+        }
       }
     }
+    if (lane == 0) {
+      if (pick < 0) {  // the exact serial computation of kmeans.rs:381-396
+        double sum = 0.0;
+        for (int64_t r = 0; r < n; ++r) sum = __dadd_rn(sum, dd[r]);
+        const double cut = __dmul_rn(u, sum);
+        double cost = 0.0;
+        int64_t index = 0;
+        while (index < n) {
+          cost = __dadd_rn(cost, dd[index]);
+          if (cost >= cut) break;
+          ++index;
+        }
+        pick = index < n ? index : n - 1;
+        st->pp_replays += 1;
+      }
+      st->pp_chosen = pick;
+      s_pick = pick;
+    }
+    __syncwarp();
   }
-  if (pick >= 0) {
-    st->pp_chosen = pick;
-    st->pp_flag = 0;
-  } else {
-    st->pp_flag = 1;
-  }
+  __syncthreads();
+  const T *xp = x + (int64_t)s_pick * d;
+  for (int c = t; c < d; c += kSelThreads) seed_x[(int64_t)j * d + c] = xp[c];
+  pp_seed_gaps(xp, d, seed_x, j, seed_cc);
 }
 
-// The exact serial computation of kmeans.rs:381-396, used only when the
-// certified parallel selection could not decide.
-__global__ void pp_replay_kernel(const double *__restrict__ dd, int64_t n,
-                                 const double *__restrict__ uniform,
-                                 LloydState *st) {
-  if (!st->pp_flag) return;
-  double sum = 0.0;
-  for (int64_t i = 0; i < n; ++i) sum = __dadd_rn(sum, dd[i]);
-  const double cutoff = __dmul_rn(*uniform, sum);
-  double cost = 0.0;
-  int64_t index = 0;
-  while (index < n) {
-    cost = __dadd_rn(cost, dd[index]);
-    if (cost >= cutoff) break;
-    ++index;
-  }
-  st->pp_chosen = index < n ? index : n - 1;
-  st->pp_flag = 0;
-  st->pp_replays += 1;
-}
-
-sc_status launch_pp_select(const double *dd, const double *part, int64_t n,
-                           int nb, const double *uniform, LloydState *st,
-                           cudaStream_t s) {
-  pp_select_kernel<<<1, kSelThreads, 0, s>>>(dd, part, n, nb, uniform, st);
-  SC_LAUNCHED();
-  pp_replay_kernel<<<1, 1, 0, s>>>(dd, n, uniform, st);
+sc_status launch_pp_select(int dtype, const void *x, int d, const double *dd, const double *part,
+                           int64_t n, int nb, const double *uniform, LloydState *st,
+                           void *seed_x, float *seed_cc, int j, cudaStream_t s) {
+  if (dtype == SC_F32)
+    pp_select_kernel<float><<<1, kSelThreads, 0, s>>>((const float *)x, d, dd, part, n, nb, uniform, st,
+                                                      (float *)seed_x, seed_cc, j);
+  else
+    pp_select_kernel<double><<<1, kSelThreads, 0, s>>>((const double *)x, d, dd, part, n, nb, uniform, st,
+                                                       (double *)seed_x, seed_cc, j);
   SC_LAUNCHED();
   return SC_OK;
 }

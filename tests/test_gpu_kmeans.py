@@ -82,16 +82,39 @@ def test_bbdtree_iris_step(kats):
     h.close()
 
 
+# (n, d, blobs, k): d % 4 == 0 f32 rows take the 16-byte staged copies, other
+# f32 rows up to d = 128 the 4-byte ones, f64 rows and d > 128 the plain
+# kernel; well separated blobs let most rows skip the distance (far test).
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-def test_kmeanspp_labels(dtype):
-    x, _ = blobs(20_000, 8, 16, seed=12, dtype=dtype)
-    first, u = kmeanspp_draws(len(x), 16, 5)
+@pytest.mark.parametrize("n,d,c,k", [(20_000, 8, 16, 16), (30_000, 7, 40, 48), (20_000, 64, 64, 64),
+                                     (5_000, 200, 8, 12), (3_001, 1, 5, 9)])
+def test_kmeanspp_labels(dtype, n, d, c, k):
+    x, _ = blobs(n, d, c, seed=12, dtype=dtype)
+    first, u = kmeanspp_draws(len(x), k, 5)
     h = KMeansHandle(x)
-    h.seed(16, first, u)
+    h.seed(k, first, u)
     _, sizes, labels, _, _ = h.get()
-    y, _ = oracle.kmeanspp(x, 16, first, u)
+    y, _ = oracle.kmeanspp(x, k, first, u)
     assert np.array_equal(labels, y)
-    assert np.array_equal(sizes, np.bincount(y, minlength=16))
+    assert np.array_equal(sizes, np.bincount(y, minlength=k))
+    h.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_kmeanspp_uncertified_draw_replays(dtype):
+    """A cutoff a hair below the total lands inside the rounding band of the
+    parallel prefix: the draw is resolved by the exact sequential replay."""
+    rng = np.random.default_rng(4)
+    x = rng.normal(0.0, 1e-6, size=(2000, 4))
+    x[0] = 1e3
+    x = x.astype(dtype)
+    u = np.array([1.0 - 2.0 ** -53, 0.3, 0.999, 0.5, 0.01])
+    h = KMeansHandle(x)
+    h.seed(6, 1, u)
+    _, _, labels, _, _ = h.get()
+    assert h.stats()[1] >= 1
+    y, _ = oracle.kmeanspp(x, 6, 1, u)
+    assert np.array_equal(labels, y)
     h.close()
 
 
