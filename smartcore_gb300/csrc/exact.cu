@@ -212,10 +212,12 @@ __host__ __device__ __forceinline__ int pp_stage_ld(int d, int vec4) {
 // ---- f32 rows, d <= 128: one launch per draw ----
 // pp_draw_kernel: one warp per 256-row block of d.  The far test runs in f32
 // from (d32 = d rounded up, y, seed_cc) and reads no row; the rows it leaves
-// are listed and read coalesced (whole rows per warp instruction, four
+// are listed and read coalesced (whole rows per warp instruction, six
 // instructions in flight) for the f32 lower bound; the rows that bound cannot
-// settle either (the rows whose distance may drop) are listed again and get
-// the reference's exact sequential sum, one row per lane.  The warp then writes the block's fixed-order partial sum
+// settle either (the rows whose distance may drop) get the reference's exact
+// value, from the integer sum of their terms across the row's lanes when no
+// addition of the sequential f64 sum can round (almost every row), else from
+// the sequential reproduction, one row per lane.  The warp then writes the block's fixed-order partial sum
 // of d for the selection.  The first draw (every row exact) runs
 // pp_first_kernel, which stages the rows in shared memory, and then
 // pp_partials_kernel.
@@ -252,18 +254,20 @@ __device__ __forceinline__ double pp_block_partial(const double *__restrict__ dd
 }
 
 template <int VEC>
-__global__ void __launch_bounds__(kPPThreads)
+__global__ void __launch_bounds__(kPPThreads, 4)
 pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *st, int32_t label_of_seed,
                double *__restrict__ dd, float *__restrict__ dd32, int32_t *__restrict__ labels,
                double *__restrict__ part, int64_t nb, int lg_d, const float *__restrict__ seed_cc,
                PPFar32 far) {
   using V = typename std::conditional<VEC == 4, float4, float>::type;
-  constexpr int NP = 4;                 // row passes with loads in flight together
+  constexpr int NP = VEC == 4 ? 6 : 2;  // row passes with loads in flight together
   constexpr int UM = VEC == 4 ? 1 : 4;  // loads per lane per row (d <= 128)
   __shared__ __align__(16) float s_cen[128];
   __shared__ uint8_t s_need[kPPWarps][kPPThreads];  // the warp's rows left by the far test
   __shared__ float s_cur[kPPWarps][kPPThreads];     // and their d32
-  __shared__ uint8_t s_ex[kPPWarps][kPPThreads];    // rows that need the exact sum
+  __shared__ uint8_t s_ex[kPPWarps][kPPThreads];    // rows that need the sequential exact sum
+  __shared__ uint8_t s_valr[kPPWarps][kPPThreads];  // rows whose exact value is known
+  __shared__ double s_valv[kPPWarps][kPPThreads];   // and that value
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t ci = st->pp_chosen;
   for (int t = threadIdx.x; t < d; t += kPPThreads) s_cen[t] = x[ci * d + t];
@@ -279,31 +283,36 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
   const int64_t nw = (int64_t)gridDim.x * kPPWarps;
   for (int64_t b = (int64_t)blockIdx.x * kPPWarps + w; b < nb; b += nw) {
     const int64_t rb = b * kPPThreads;  // first row of the block
-    // far test of the block's 8 groups, loads issued together
-    float c32[kPPWarps];
-    int32_t lb[kPPWarps];
-#pragma unroll
-    for (int g = 0; g < kPPWarps; ++g) {
-      const int64_t i = rb + g * 32 + lane;
-      c32[g] = i < n ? dd32[i] : 0.f;
-      lb[g] = i < n ? labels[i] : 0;
-    }
+    // far test of the block's 8 groups, four groups' loads issued together
     int cnt = 0;  // rows listed in s_need
 #pragma unroll
-    for (int g = 0; g < kPPWarps; ++g) {
-      const int64_t i = rb + g * 32 + lane;
-      const bool need = i < n && !pp_far32(seed_cc[lb[g]], c32[g], far);
-      const unsigned m = __ballot_sync(0xffffffffu, need);
-      if (need) {
-        const int pos = cnt + __popc(m & lt);
-        s_need[w][pos] = (uint8_t)(g * 32 + lane);
-        s_cur[w][pos] = c32[g];
+    for (int h = 0; h < kPPWarps; h += 4) {
+      float c32[4];
+      int32_t lb[4];
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        const int64_t i = rb + (h + g) * 32 + lane;
+        c32[g] = i < n ? dd32[i] : 0.f;
+        lb[g] = i < n ? labels[i] : 0;
       }
-      cnt += __popc(m);
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        const int64_t i = rb + (h + g) * 32 + lane;
+        const bool need = i < n && !pp_far32(seed_cc[lb[g]], c32[g], far);
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (need) {
+          const int pos = cnt + __popc(m & lt);
+          s_need[w][pos] = (uint8_t)((h + g) * 32 + lane);
+          s_cur[w][pos] = c32[g];
+        }
+        cnt += __popc(m);
+      }
     }
     __syncwarp();
     // f32 lower bound of the listed rows, R rows per load, NP loads in flight
-    int exn = 0;  // rows listed in s_ex
+    const V *xb = reinterpret_cast<const V *>(x + rb * d);
+    int exn = 0;   // rows listed in s_ex
+    int nval = 0;  // rows listed in s_valr / s_valv
     for (int it = 0; it < cnt; it += R * NP) {
       int rq[NP];
       V val[NP][UM];
@@ -314,46 +323,102 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
 #pragma unroll
         for (int k = 0; k < UM; ++k) {
           const int uu = unit + k * p;
-          if (rq[q] >= 0 && uu < units) val[q][k] = reinterpret_cast<const V *>(x + (rb + rq[q]) * d)[uu];
+          if (rq[q] >= 0 && uu < units) val[q][k] = xb[rq[q] * units + uu];
         }
       }
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
-        // The reference's terms q_t = fl32((x_t - c_t)^2) summed in f32 (any
-        // order, depth <= d) bound its f64 sum from below by s32 (1 - 1.05 d
-        // 2^-24): when that exceeds the current distance the row keeps it.
-        float s32 = 0.f;
+        // The reference's terms q_t = fl32((x_t - c_t)^2).  Summed in f32 (any
+        // order, depth <= d) they bound its f64 sum from below by s32 (1 - 1.05
+        // d 2^-24): when that exceeds the current distance the row keeps it.
+        float tq[4 * UM];
 #pragma unroll
         for (int k = 0; k < UM; ++k) {
           const int uu = unit + k * p;
-          if (rq[q] >= 0 && uu < units) {
-            if constexpr (VEC == 4) {
-              const float4 a = val[q][k];
-              const float4 c = reinterpret_cast<const float4 *>(s_cen)[uu];
-              float r = __fsub_rn(a.x, c.x);
-              s32 = __fadd_rn(s32, __fmul_rn(r, r));
-              r = __fsub_rn(a.y, c.y);
-              s32 = __fadd_rn(s32, __fmul_rn(r, r));
-              r = __fsub_rn(a.z, c.z);
-              s32 = __fadd_rn(s32, __fmul_rn(r, r));
-              r = __fsub_rn(a.w, c.w);
-              s32 = __fadd_rn(s32, __fmul_rn(r, r));
-            } else {
-              const float r = __fsub_rn(val[q][k], s_cen[uu]);
-              s32 = __fadd_rn(s32, __fmul_rn(r, r));
-            }
+          const bool live = rq[q] >= 0 && uu < units;
+          if constexpr (VEC == 4) {
+            const float4 a = val[q][k];
+            const float4 c = reinterpret_cast<const float4 *>(s_cen)[live ? uu : 0];
+            float r = __fsub_rn(a.x, c.x);
+            tq[4 * k] = live ? __fmul_rn(r, r) : 0.f;
+            r = __fsub_rn(a.y, c.y);
+            tq[4 * k + 1] = live ? __fmul_rn(r, r) : 0.f;
+            r = __fsub_rn(a.z, c.z);
+            tq[4 * k + 2] = live ? __fmul_rn(r, r) : 0.f;
+            r = __fsub_rn(a.w, c.w);
+            tq[4 * k + 3] = live ? __fmul_rn(r, r) : 0.f;
+          } else {
+            const float r = __fsub_rn(val[q][k], s_cen[live ? uu : 0]);
+            tq[4 * k] = live ? __fmul_rn(r, r) : 0.f;
+            tq[4 * k + 1] = tq[4 * k + 2] = tq[4 * k + 3] = 0.f;
           }
         }
+        float s32 = 0.f;
+#pragma unroll
+        for (int t = 0; t < 4 * UM; ++t) s32 = __fadd_rn(s32, tq[t]);
         for (int o = p >> 1; o > 0; o >>= 1) s32 = __fadd_rn(s32, __shfl_xor_sync(0xffffffffu, s32, o));
         const int idx = it + q * R + seg;
         const bool ex = rq[q] >= 0 && unit == 0 && !(__fmul_rd(s32, lbf) > s_cur[w][idx]);
-        const unsigned em = __ballot_sync(0xffffffffu, ex);
-        if (ex) s_ex[w][exn + __popc(em & lt)] = (uint8_t)rq[q];
-        exn += __popc(em);
+        if (__any_sync(0xffffffffu, ex)) {
+          // The exact value without the sequential sum: in units of
+          // 2^(emin - 150) every term is an integer below 2^(24 + span); while
+          // span <= 29 - ceil(log2 d) every partial sum stays below 2^53, so
+          // no addition of the reference's f64 sequence rounds and its result
+          // is the integer sum, in any order (here: across the row's lanes).
+          int emn = 255, emx = 0;
+#pragma unroll
+          for (int t = 0; t < 4 * UM; ++t) {
+            const uint32_t u = __float_as_uint(tq[t]);
+            if (u) {
+              const int e = max((int)(u >> 23), 1);
+              emn = min(emn, e);
+              emx = max(emx, e);
+            }
+          }
+          for (int o = p >> 1; o > 0; o >>= 1) {
+            emn = min(emn, __shfl_xor_sync(0xffffffffu, emn, o));
+            emx = max(emx, __shfl_xor_sync(0xffffffffu, emx, o));
+          }
+          const bool fits = emx < 255 && (emn == 255 || emx - emn <= 29 - lg_d);
+          unsigned long long S = 0ull;
+          if (fits && emn < 255) {
+#pragma unroll
+            for (int t = 0; t < 4 * UM; ++t) {
+              const uint32_t u = __float_as_uint(tq[t]);
+              const int e = (int)(u >> 23);
+              const uint32_t m = (u & 0x7fffffu) | (e ? 0x800000u : 0u);
+              S += u ? (unsigned long long)m << (max(e, 1) - emn) : 0ull;
+            }
+          }
+          for (int o = p >> 1; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+          const unsigned fm = __ballot_sync(0xffffffffu, ex && fits);
+          const unsigned sm = __ballot_sync(0xffffffffu, ex && !fits);
+          if (ex && fits) {
+            const int pos = nval + __popc(fm & lt);
+            s_valr[w][pos] = (uint8_t)rq[q];
+            s_valv[w][pos] = emn == 255 ? 0.0
+                                        : __dmul_rn(__ull2double_rn(S),
+                                                    __longlong_as_double((long long)(emn - 150 + 1023) << 52));
+          }
+          if (ex && !fits) s_ex[w][exn + __popc(sm & lt)] = (uint8_t)rq[q];
+          nval += __popc(fm);
+          exn += __popc(sm);
+        }
       }
     }
     __syncwarp();
-    // the rows whose distance may drop: the exact value, one row per lane
+    // rows whose exact value is known: keep the smaller distance
+    for (int e = lane; e < nval; e += 32) {
+      const int64_t i = rb + s_valr[w][e];
+      const double v = s_valv[w][e];
+      if (v < dd[i]) {
+        dd[i] = v;
+        dd32[i] = __double2float_ru(v);
+        labels[i] = label_of_seed;
+      }
+    }
+    // the other rows whose distance may drop: the sequential exact sum, one
+    // row per lane
     for (int e = lane; e < exn; e += 32) {
       const int64_t i = rb + s_ex[w][e];
       const float *xr = x + i * d;
