@@ -212,8 +212,8 @@ __host__ __device__ __forceinline__ int pp_stage_ld(int d, int vec4) {
 // ---- f32 rows, d <= 128: one launch per draw ----
 // pp_draw_kernel: one warp per 256-row block of d.  The far test runs in f32
 // from (d32 = d rounded up, y, seed_cc) and reads no row; the rows it leaves
-// are listed and read coalesced (whole rows per warp instruction, six
-// instructions in flight) for the f32 lower bound; the rows that bound cannot
+// are listed and read coalesced (up to four 16-byte units per lane, two
+// passes of whole rows in flight) for the f32 lower bound; the rows that bound cannot
 // settle either (the rows whose distance may drop) get the reference's exact
 // value, from the integer sum of their terms across the row's lanes when no
 // addition of the sequential f64 sum can round (almost every row), else from
@@ -221,7 +221,8 @@ __host__ __device__ __forceinline__ int pp_stage_ld(int d, int vec4) {
 // of d for the selection.  The first draw (every row exact) runs
 // pp_first_kernel, which stages the rows in shared memory, and then
 // pp_partials_kernel.
-constexpr int kPPWarps = kPPThreads / 32;
+constexpr int kPPWarps = kPPThreads / 32;  // 32-row groups per 256-row block
+constexpr int kDrawWarps = 4, kDrawThreads = 32 * kDrawWarps;
 
 // f32 form of the far test: keep when cc >= mul (D32 + abs_), both roundings
 // upward, with D32 >= D.
@@ -253,35 +254,48 @@ __device__ __forceinline__ double pp_block_partial(const double *__restrict__ dd
   return t;
 }
 
+// Component c4 of unit uu's term fl32((x - c)^2).
 template <int VEC>
-__global__ void __launch_bounds__(kPPThreads, 4)
+__device__ __forceinline__ float pp_term(float4 v, const float *cen, int uu, int c4) {
+  const float a = c4 == 0 ? v.x : c4 == 1 ? v.y : c4 == 2 ? v.z : v.w;
+  const float r = __fsub_rn(a, cen[uu * 4 + c4]);
+  return __fmul_rn(r, r);
+}
+template <int VEC>
+__device__ __forceinline__ float pp_term(float v, const float *cen, int uu, int) {
+  const float r = __fsub_rn(v, cen[uu]);
+  return __fmul_rn(r, r);
+}
+
+template <int VEC>
+__global__ void __launch_bounds__(kDrawThreads, 7)
 pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *st, int32_t label_of_seed,
                double *__restrict__ dd, float *__restrict__ dd32, int32_t *__restrict__ labels,
                double *__restrict__ part, int64_t nb, int lg_d, const float *__restrict__ seed_cc,
                PPFar32 far) {
   using V = typename std::conditional<VEC == 4, float4, float>::type;
-  constexpr int NP = VEC == 4 ? 6 : 2;  // row passes with loads in flight together
-  constexpr int UM = VEC == 4 ? 1 : 4;  // loads per lane per row (d <= 128)
+  constexpr int NP = VEC == 4 ? 1 : 4;  // row passes with loads in flight together
+  constexpr int UM = 4;                 // loads per lane per row (d <= 128)
   __shared__ __align__(16) float s_cen[128];
-  __shared__ uint8_t s_need[kPPWarps][kPPThreads];  // the warp's rows left by the far test
-  __shared__ float s_cur[kPPWarps][kPPThreads];     // and their d32
-  __shared__ uint8_t s_ex[kPPWarps][kPPThreads];    // rows that need the sequential exact sum
-  __shared__ uint8_t s_valr[kPPWarps][kPPThreads];  // rows whose exact value is known
-  __shared__ double s_valv[kPPWarps][kPPThreads];   // and that value
+  __shared__ uint8_t s_need[kDrawWarps][kPPThreads];  // the warp's rows left by the far test
+  __shared__ float s_cur[kDrawWarps][kPPThreads];     // and their d32
+  __shared__ uint8_t s_ex[kDrawWarps][kPPThreads];    // rows that need the sequential exact sum
+  __shared__ uint8_t s_valr[kDrawWarps][kPPThreads];  // rows whose exact value is known
+  __shared__ double s_valv[kDrawWarps][kPPThreads];   // and that value
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t ci = st->pp_chosen;
-  for (int t = threadIdx.x; t < d; t += kPPThreads) s_cen[t] = x[ci * d + t];
+  for (int t = threadIdx.x; t < d; t += kDrawThreads) s_cen[t] = x[ci * d + t];
   __syncthreads();
-  // a row is `units` loads of VEC floats; p lanes per row (a power of two),
-  // R = 32 / p rows per warp instruction
+  // a row is `units` loads of VEC floats; p lanes per row (a power of two,
+  // at most UM units per lane), R = 32 / p rows per pass
   const int units = d / VEC;
   int p = 1;
-  while (p < units && p < 32) p <<= 1;
+  while (p * UM < units) p <<= 1;
   const int R = 32 / p, seg = lane / p, unit = lane - seg * p;
   const float lbf = 1.f - 1.05f * d * 0x1p-24f;
   const unsigned lt = (1u << lane) - 1u;
-  const int64_t nw = (int64_t)gridDim.x * kPPWarps;
-  for (int64_t b = (int64_t)blockIdx.x * kPPWarps + w; b < nb; b += nw) {
+  const int64_t nw = (int64_t)gridDim.x * kDrawWarps;
+  for (int64_t b = (int64_t)blockIdx.x * kDrawWarps + w; b < nb; b += nw) {
     const int64_t rb = b * kPPThreads;  // first row of the block
     // far test of the block's 8 groups, four groups' loads issued together
     int cnt = 0;  // rows listed in s_need
@@ -331,31 +345,28 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
         // The reference's terms q_t = fl32((x_t - c_t)^2).  Summed in f32 (any
         // order, depth <= d) they bound its f64 sum from below by s32 (1 - 1.05
         // d 2^-24): when that exceeds the current distance the row keeps it.
-        float tq[4 * UM];
+        float s32 = 0.f;
 #pragma unroll
         for (int k = 0; k < UM; ++k) {
           const int uu = unit + k * p;
-          const bool live = rq[q] >= 0 && uu < units;
-          if constexpr (VEC == 4) {
-            const float4 a = val[q][k];
-            const float4 c = reinterpret_cast<const float4 *>(s_cen)[live ? uu : 0];
-            float r = __fsub_rn(a.x, c.x);
-            tq[4 * k] = live ? __fmul_rn(r, r) : 0.f;
-            r = __fsub_rn(a.y, c.y);
-            tq[4 * k + 1] = live ? __fmul_rn(r, r) : 0.f;
-            r = __fsub_rn(a.z, c.z);
-            tq[4 * k + 2] = live ? __fmul_rn(r, r) : 0.f;
-            r = __fsub_rn(a.w, c.w);
-            tq[4 * k + 3] = live ? __fmul_rn(r, r) : 0.f;
-          } else {
-            const float r = __fsub_rn(val[q][k], s_cen[live ? uu : 0]);
-            tq[4 * k] = live ? __fmul_rn(r, r) : 0.f;
-            tq[4 * k + 1] = tq[4 * k + 2] = tq[4 * k + 3] = 0.f;
+          if (rq[q] >= 0 && uu < units) {
+            if constexpr (VEC == 4) {
+              const float4 a = val[q][k];
+              const float4 c = reinterpret_cast<const float4 *>(s_cen)[uu];
+              float r = __fsub_rn(a.x, c.x);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+              r = __fsub_rn(a.y, c.y);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+              r = __fsub_rn(a.z, c.z);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+              r = __fsub_rn(a.w, c.w);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+            } else {
+              const float r = __fsub_rn(val[q][k], s_cen[uu]);
+              s32 = __fadd_rn(s32, __fmul_rn(r, r));
+            }
           }
         }
-        float s32 = 0.f;
-#pragma unroll
-        for (int t = 0; t < 4 * UM; ++t) s32 = __fadd_rn(s32, tq[t]);
         for (int o = p >> 1; o > 0; o >>= 1) s32 = __fadd_rn(s32, __shfl_xor_sync(0xffffffffu, s32, o));
         const int idx = it + q * R + seg;
         const bool ex = rq[q] >= 0 && unit == 0 && !(__fmul_rd(s32, lbf) > s_cur[w][idx]);
@@ -367,12 +378,18 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
           // is the integer sum, in any order (here: across the row's lanes).
           int emn = 255, emx = 0;
 #pragma unroll
-          for (int t = 0; t < 4 * UM; ++t) {
-            const uint32_t u = __float_as_uint(tq[t]);
-            if (u) {
-              const int e = max((int)(u >> 23), 1);
-              emn = min(emn, e);
-              emx = max(emx, e);
+          for (int k = 0; k < UM; ++k) {
+            const int uu = unit + k * p;
+            if (rq[q] >= 0 && uu < units) {
+#pragma unroll
+              for (int c4 = 0; c4 < VEC; ++c4) {
+                const uint32_t u = __float_as_uint(pp_term<VEC>(val[q][k], s_cen, uu, c4));
+                if (u) {
+                  const int e = max((int)(u >> 23), 1);
+                  emn = min(emn, e);
+                  emx = max(emx, e);
+                }
+              }
             }
           }
           for (int o = p >> 1; o > 0; o >>= 1) {
@@ -383,11 +400,17 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
           unsigned long long S = 0ull;
           if (fits && emn < 255) {
 #pragma unroll
-            for (int t = 0; t < 4 * UM; ++t) {
-              const uint32_t u = __float_as_uint(tq[t]);
-              const int e = (int)(u >> 23);
-              const uint32_t m = (u & 0x7fffffu) | (e ? 0x800000u : 0u);
-              S += u ? (unsigned long long)m << (max(e, 1) - emn) : 0ull;
+            for (int k = 0; k < UM; ++k) {
+              const int uu = unit + k * p;
+              if (rq[q] >= 0 && uu < units) {
+#pragma unroll
+                for (int c4 = 0; c4 < VEC; ++c4) {
+                  const uint32_t u = __float_as_uint(pp_term<VEC>(val[q][k], s_cen, uu, c4));
+                  const int e = (int)(u >> 23);
+                  const uint32_t m = (u & 0x7fffffu) | (e ? 0x800000u : 0u);
+                  S += u ? (unsigned long long)m << (max(e, 1) - emn) : 0ull;
+                }
+              }
             }
           }
           for (int o = p >> 1; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
@@ -539,14 +562,15 @@ sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
         SC_LAUNCHED();
       }
     } else {
-      const int g1 = std::min(warp_blocks, sms * 8);
+      // one warp per 256-row block, every warp resident at once when they fit
+      const int g1 = std::min((grid + kDrawWarps - 1) / kDrawWarps, sms * 7);
       const PPFar32 far = pp_far_bound32(d);
       if (vec4)
-        pp_draw_kernel<4><<<g1, kPPThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
-                                                    lg_d, seed_cc, far);
+        pp_draw_kernel<4><<<g1, kDrawThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
+                                                      lg_d, seed_cc, far);
       else
-        pp_draw_kernel<1><<<g1, kPPThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
-                                                    lg_d, seed_cc, far);
+        pp_draw_kernel<1><<<g1, kDrawThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
+                                                      lg_d, seed_cc, far);
       SC_LAUNCHED();
     }
   } else if (dtype == SC_F32) {
