@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -37,21 +38,32 @@ sc_status cuda_fail(cudaError_t e, const char *what) {
   return SC_ERR_CUDA;
 }
 
-namespace {
+std::mutex g_pool_mutex;
+bool g_pool_ready[64] = {};
 
-template <class T>
-sc_status dalloc(T **p, size_t count) {
+sc_status dev_alloc(void **p, size_t bytes, cudaStream_t s) {
   *p = nullptr;
-  if (count == 0) count = 1;
-  SC_CUDA(cudaMalloc((void **)p, count * sizeof(T)));
+  int dev = 0;
+  SC_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64) {
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pool_ready[dev]) {
+      cudaMemPool_t pool;
+      SC_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+      uint64_t keep = UINT64_MAX;
+      SC_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+      g_pool_ready[dev] = true;
+    }
+  }
+  SC_CUDA(cudaMallocAsync(p, bytes ? bytes : 1, s));
   return SC_OK;
 }
 
-template <class T>
-void dfree(T *&p) {
-  if (p) cudaFree((void *)p);
-  p = nullptr;
+void dev_free(void *p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
 }
+
+namespace {
 
 size_t esize(int dtype) { return dtype == SC_F32 ? 4 : 8; }
 
@@ -147,16 +159,17 @@ static cudaEvent_t *next_timing(sc_kmeans *h) {
 
 static sc_status kmeans_alloc_k(sc_kmeans *h, int64_t k) {
   if (k == h->k_alloc) { h->k = k; return SC_OK; }
-  dfree(h->cent); dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms);
-  dfree(h->seed_x); dfree(h->seed_cc);
-  SC_TRY(dalloc(&h->cent, (size_t)(k * h->d)));
-  SC_TRY(dalloc(&h->sizes, (size_t)k));
-  SC_TRY(dalloc(&h->cterms, (size_t)(k * h->d)));
-  SC_TRY(dalloc(&h->uniforms, (size_t)k));
-  SC_TRY(dalloc((char **)&h->seed_x, (size_t)(k * h->d) * esize(h->dtype)));
-  SC_TRY(dalloc(&h->seed_cc, (size_t)k));
+  cudaStream_t hs = h->stream;
+  dfree(h->cent, hs); dfree(h->sizes, hs); dfree(h->cterms, hs); dfree(h->uniforms, hs);
+  dfree(h->seed_x, hs); dfree(h->seed_cc, hs);
+  SC_TRY(dalloc(&h->cent, (size_t)(k * h->d), h->stream));
+  SC_TRY(dalloc(&h->sizes, (size_t)k, h->stream));
+  SC_TRY(dalloc(&h->cterms, (size_t)(k * h->d), h->stream));
+  SC_TRY(dalloc(&h->uniforms, (size_t)k, h->stream));
+  SC_TRY(dalloc((char **)&h->seed_x, (size_t)(k * h->d) * esize(h->dtype), h->stream));
+  SC_TRY(dalloc(&h->seed_cc, (size_t)k, h->stream));
   SC_CUDA(cudaStreamSynchronize(h->stream));
-  SC_TRY(update_alloc(&h->upd, h->dtype, h->n, (int)h->d, (int)k, h->absmax, h->num_sms));
+  SC_TRY(update_alloc(&h->upd, h->dtype, h->n, (int)h->d, (int)k, h->absmax, h->num_sms, h->stream));
   h->k_alloc = k;
   h->k = k;
   return SC_OK;
@@ -189,11 +202,13 @@ int32_t sc_device_ok(void) {
 void sc_kmeans_destroy(sc_kmeans *h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  dfree(h->x); dfree(h->cent); dfree(h->labels); dfree(h->dd); dfree(h->dd32); dfree(h->part);
-  dfree(h->sizes); dfree(h->cterms); dfree(h->uniforms); dfree(h->seed_x); dfree(h->seed_cc);
-  update_free(&h->upd);
-  dfree(h->xnorm_total); dfree(h->st); dfree(h->bits);
-  split_free(&h->split);
+  cudaStream_t hs = h->stream;  // frees in stream order: no device-wide synchronisation
+  dfree(h->x, hs); dfree(h->cent, hs); dfree(h->labels, hs); dfree(h->dd, hs); dfree(h->dd32, hs);
+  dfree(h->part, hs); dfree(h->sizes, hs); dfree(h->cterms, hs); dfree(h->uniforms, hs);
+  dfree(h->seed_x, hs); dfree(h->seed_cc, hs);
+  update_free(&h->upd, hs);
+  dfree(h->xnorm_total, hs); dfree(h->st, hs); dfree(h->bits, hs);
+  split_free(&h->split, hs);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -217,14 +232,14 @@ sc_status sc_kmeans_create(const void *x, int32_t dtype, int32_t layout, int32_t
       break;
     }
     const int nparts = std::max(assign_block_count(n), pp_block_count(n));
-    if ((r = dalloc((char **)&h->x, (size_t)(n * d) * esize(dtype))) != SC_OK) break;
-    if ((r = dalloc(&h->labels, (size_t)n)) != SC_OK) break;
-    if ((r = dalloc(&h->dd, (size_t)n)) != SC_OK) break;
-    if ((r = dalloc(&h->dd32, (size_t)n)) != SC_OK) break;
-    if ((r = dalloc(&h->part, (size_t)nparts)) != SC_OK) break;
-    if ((r = dalloc(&h->st, 1)) != SC_OK) break;
-    if ((r = dalloc(&h->bits, 1)) != SC_OK) break;
-    if ((r = dalloc(&h->xnorm_total, 1)) != SC_OK) break;
+    if ((r = dalloc((char **)&h->x, (size_t)(n * d) * esize(dtype), h->stream)) != SC_OK) break;
+    if ((r = dalloc(&h->labels, (size_t)n, h->stream)) != SC_OK) break;
+    if ((r = dalloc(&h->dd, (size_t)n, h->stream)) != SC_OK) break;
+    if ((r = dalloc(&h->dd32, (size_t)n, h->stream)) != SC_OK) break;
+    if ((r = dalloc(&h->part, (size_t)nparts, h->stream)) != SC_OK) break;
+    if ((r = dalloc(&h->st, 1, h->stream)) != SC_OK) break;
+    if ((r = dalloc(&h->bits, 1, h->stream)) != SC_OK) break;
+    if ((r = dalloc(&h->xnorm_total, 1, h->stream)) != SC_OK) break;
     if ((r = upload_matrix(x, dtype, layout, mem, n, d, ld, h->x, h->stream)) != SC_OK) break;
     if ((r = launch_absmax(dtype, h->x, n * d, h->bits, h->stream)) != SC_OK) break;
     unsigned long long bits = 0;
@@ -341,7 +356,8 @@ sc_status sc_kmeans_iterate(sc_kmeans *h, int64_t max_iter, int32_t stop_on_conv
     SC_CUDA(cudaMemcpyAsync(iters_done, &h->st->iters, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     SC_CUDA(cudaStreamSynchronize(s));
     int32_t err = 0;
-    SC_CUDA(cudaMemcpy(&err, &h->st->err, sizeof err, cudaMemcpyDeviceToHost));
+    SC_CUDA(cudaMemcpyAsync(&err, &h->st->err, sizeof err, cudaMemcpyDeviceToHost, s));
+    SC_CUDA(cudaStreamSynchronize(s));
     if (err) { set_error("device-side check failed (code %d)", err); return err == 4 ? SC_ERR_TIMEOUT : SC_ERR_INTERNAL; }
   }
   return SC_OK;
@@ -351,16 +367,19 @@ sc_status sc_kmeans_get(sc_kmeans *h, double *centroids, int64_t *sizes, int64_t
                         double *distortion, int64_t *iters) {
   if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
   cudaStream_t s = h->stream;
-  SC_CUDA(cudaStreamSynchronize(s));
-  if (centroids) SC_CUDA(cudaMemcpy(centroids, h->cent, (size_t)(h->k * h->d) * sizeof(double), cudaMemcpyDeviceToHost));
-  if (sizes) SC_CUDA(cudaMemcpy(sizes, h->sizes, (size_t)h->k * sizeof(int64_t), cudaMemcpyDeviceToHost));
-  if (labels && h->n > 0) {
-    std::vector<int32_t> tmp((size_t)h->n);
-    SC_CUDA(cudaMemcpy(tmp.data(), h->labels, (size_t)h->n * sizeof(int32_t), cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < h->n; ++i) labels[i] = tmp[(size_t)i];
+  if (centroids)
+    SC_CUDA(cudaMemcpyAsync(centroids, h->cent, (size_t)(h->k * h->d) * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (sizes) SC_CUDA(cudaMemcpyAsync(sizes, h->sizes, (size_t)h->k * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  int64_t *wide = nullptr;
+  if (labels && h->n > 0) {  // widened on the device, one copy straight into the caller's array
+    SC_TRY(dalloc(&wide, (size_t)h->n, s));
+    SC_TRY(launch_widen_labels(h->labels, wide, h->n, s));
+    SC_CUDA(cudaMemcpyAsync(labels, wide, (size_t)h->n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    dfree(wide, s);
   }
   LloydState st;
-  SC_CUDA(cudaMemcpy(&st, h->st, sizeof st, cudaMemcpyDeviceToHost));
+  SC_CUDA(cudaMemcpyAsync(&st, h->st, sizeof st, cudaMemcpyDeviceToHost, s));
+  SC_CUDA(cudaStreamSynchronize(s));
   if (distortion) *distortion = st.distortion;
   if (iters) *iters = st.iters;
   return SC_OK;
@@ -369,8 +388,8 @@ sc_status sc_kmeans_get(sc_kmeans *h, double *centroids, int64_t *sizes, int64_t
 sc_status sc_kmeans_stats(sc_kmeans *h, int64_t *rescored, int64_t *pp_replays) {
   if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
   LloydState st;
+  SC_CUDA(cudaMemcpyAsync(&st, h->st, sizeof st, cudaMemcpyDeviceToHost, h->stream));
   SC_CUDA(cudaStreamSynchronize(h->stream));
-  SC_CUDA(cudaMemcpy(&st, h->st, sizeof st, cudaMemcpyDeviceToHost));
   if (rescored) *rescored = st.rescored;
   if (pp_replays) *pp_replays = st.pp_replays;
   return SC_OK;
@@ -465,14 +484,14 @@ struct sc_knn {
 
 static sc_status knn_reserve(sc_knn *h, int64_t m, int64_t k) {
   if (m > h->q_cap) {
-    dfree(h->q);
-    SC_TRY(dalloc((char **)&h->q, (size_t)(m * h->d) * esize(h->dtype)));
+    dfree(h->q, h->stream);
+    SC_TRY(dalloc((char **)&h->q, (size_t)(m * h->d) * esize(h->dtype), h->stream));
     h->q_cap = m;
   }
   if (m * k > h->res_cap) {
-    dfree(h->idx); dfree(h->dist);
-    SC_TRY(dalloc(&h->idx, (size_t)(m * k)));
-    SC_TRY(dalloc(&h->dist, (size_t)(m * k)));
+    dfree(h->idx, h->stream); dfree(h->dist, h->stream);
+    SC_TRY(dalloc(&h->idx, (size_t)(m * k), h->stream));
+    SC_TRY(dalloc(&h->dist, (size_t)(m * k), h->stream));
     h->res_cap = m * k;
   }
   return SC_OK;
@@ -500,8 +519,10 @@ extern "C" {
 void sc_knn_destroy(sc_knn *h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  dfree(h->train); dfree(h->q); dfree(h->idx); dfree(h->dist); dfree(h->aux_i); dfree(h->aux_d);
-  split_knn_free(&h->split);
+  cudaStream_t hs = h->stream;
+  dfree(h->train, hs); dfree(h->q, hs); dfree(h->idx, hs); dfree(h->dist, hs);
+  dfree(h->aux_i, hs); dfree(h->aux_d, hs);
+  split_knn_free(&h->split, hs);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -521,7 +542,7 @@ sc_status sc_knn_create(const void *train, int32_t dtype, int32_t layout, int32_
       h->stream = nullptr;
       break;
     }
-    if ((r = dalloc((char **)&h->train, (size_t)(n * d) * esize(dtype))) != SC_OK) break;
+    if ((r = dalloc((char **)&h->train, (size_t)(n * d) * esize(dtype), h->stream)) != SC_OK) break;
     if ((r = upload_matrix(train, dtype, layout, mem, n, d, ld, h->train, h->stream)) != SC_OK) break;
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "upload"); break; }
   } while (0);
@@ -569,7 +590,7 @@ sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout, int
   std::vector<int64_t> cnt((size_t)m);
   int64_t total = 0;
   do {
-    if ((r = dalloc(&dcnt, (size_t)m)) != SC_OK || (r = dalloc(&doff, (size_t)m)) != SC_OK) break;
+    if ((r = dalloc(&dcnt, (size_t)m, h->stream)) != SC_OK || (r = dalloc(&doff, (size_t)m, h->stream)) != SC_OK) break;
     // counting pass
     r = form == SC_FORM_FP64
             ? launch_knn_radius_fp64(h->dtype, h->train, h->n, (int)h->d, h->q, m, radius, dcnt, nullptr, nullptr,
@@ -594,7 +615,7 @@ sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout, int
       break;
     }
     if (total == 0) break;
-    if ((r = dalloc(&didx, (size_t)total)) != SC_OK || (r = dalloc(&ddist, (size_t)total)) != SC_OK) break;
+    if ((r = dalloc(&didx, (size_t)total, h->stream)) != SC_OK || (r = dalloc(&ddist, (size_t)total, h->stream)) != SC_OK) break;
     if (cudaMemcpyAsync(doff, off.data(), (size_t)m * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream) !=
         cudaSuccess) {
       r = cuda_fail(cudaGetLastError(), "find_radius offsets");
@@ -617,7 +638,7 @@ sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout, int
     }
   } while (0);
   cudaStreamSynchronize(h->stream);
-  dfree(dcnt); dfree(doff); dfree(didx); dfree(ddist);
+  dfree(dcnt, h->stream); dfree(doff, h->stream); dfree(didx, h->stream); dfree(ddist, h->stream);
   return r;
 }
 
@@ -628,9 +649,9 @@ sc_status sc_knn_classify(sc_knn *h, const void *queries, int32_t layout, int32_
   if (!y_class || n_classes < 1) { set_error("invalid class labels"); return SC_ERR_INVALID; }
   SC_TRY(knn_run(h, queries, layout, mem, m, ld, k, form));
   if (h->aux_cap < std::max(h->n, m)) {
-    dfree(h->aux_i); dfree(h->aux_d);
-    SC_TRY(dalloc(&h->aux_i, (size_t)(h->n + m)));
-    SC_TRY(dalloc(&h->aux_d, (size_t)(h->n + m)));
+    dfree(h->aux_i, h->stream); dfree(h->aux_d, h->stream);
+    SC_TRY(dalloc(&h->aux_i, (size_t)(h->n + m), h->stream));
+    SC_TRY(dalloc(&h->aux_d, (size_t)(h->n + m), h->stream));
     h->aux_cap = std::max(h->n, m);
   }
   SC_CUDA(cudaMemcpyAsync(h->aux_i, y_class, (size_t)h->n * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
@@ -647,9 +668,9 @@ sc_status sc_knn_regress(sc_knn *h, const void *queries, int32_t layout, int32_t
   if (!y) { set_error("null targets"); return SC_ERR_INVALID; }
   SC_TRY(knn_run(h, queries, layout, mem, m, ld, k, form));
   if (h->aux_cap < std::max(h->n, m)) {
-    dfree(h->aux_i); dfree(h->aux_d);
-    SC_TRY(dalloc(&h->aux_i, (size_t)(h->n + m)));
-    SC_TRY(dalloc(&h->aux_d, (size_t)(h->n + m)));
+    dfree(h->aux_i, h->stream); dfree(h->aux_d, h->stream);
+    SC_TRY(dalloc(&h->aux_i, (size_t)(h->n + m), h->stream));
+    SC_TRY(dalloc(&h->aux_d, (size_t)(h->n + m), h->stream));
     h->aux_cap = std::max(h->n, m);
   }
   SC_CUDA(cudaMemcpyAsync(h->aux_d, y, (size_t)h->n * sizeof(double), cudaMemcpyHostToDevice, h->stream));

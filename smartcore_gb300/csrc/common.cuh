@@ -74,6 +74,23 @@ struct UpdateBuf {
   unsigned int *cpart = nullptr;    // mode 1: grid x k
 };
 
+// ---- device memory ----
+// Stream-ordered allocations from the device's default memory pool.  Its
+// release threshold is raised once per device, so blocks a destroyed handle
+// gave back serve the next handle without new driver mappings.  A block is
+// freed in the order of the stream that last used it.
+sc_status dev_alloc(void **p, size_t bytes, cudaStream_t s);
+void dev_free(void *p, cudaStream_t s);
+template <class T>
+sc_status dalloc(T **p, size_t count, cudaStream_t s) {
+  return dev_alloc((void **)p, (count ? count : 1) * sizeof(T), s);
+}
+template <class T>
+void dfree(T *&p, cudaStream_t s) {
+  dev_free((void *)p, s);
+  p = nullptr;
+}
+
 // ---- kernel launchers (defined in the .cu files) ----
 // exact.cu: FP64 forms with the reference's operation order.
 sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
@@ -99,6 +116,7 @@ sc_status launch_knn_fp64(int dtype, const void *train, int64_t n, int d,
 sc_status launch_knn_radius_fp64(int dtype, const void *train, int64_t n, int d, const void *queries, int64_t m,
                                  double radius, int64_t *counts, const int64_t *offsets, int64_t *idx,
                                  double *dist, cudaStream_t s);
+sc_status launch_widen_labels(const int32_t *in, int64_t *out, int64_t n, cudaStream_t s);
 sc_status launch_knn_vote(const int64_t *idx, const double *dist, int64_t m,
                           int k, int weight, const int64_t *y_class,
                           int64_t *out, cudaStream_t s);
@@ -123,13 +141,14 @@ sc_status launch_finalize_scalar(const double *part, int nparts,
                                  const double *xnorm_total, LloydState *st,
                                  cudaStream_t s);
 // Chooses the mode for (n, d, k) and allocates; absmax = max |x|.
-sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms);
+sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms,
+                       cudaStream_t s);
 // Number of distortion terms launch_finalize writes: one per cluster (mode 0)
 // or one per block of 32 (cluster, feature) elements (mode 1).
 inline int64_t update_nterms(const UpdateBuf *u, int k, int d) {
   return u->mode != 0 ? ((int64_t)k * d + 31) / 32 : k;
 }
-void update_free(UpdateBuf *u);
+void update_free(UpdateBuf *u, cudaStream_t s);
 sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n, int d,
                         const int32_t *labels, int k, const LloydState *st, cudaStream_t s);
 sc_status launch_finalize(const UpdateBuf *u, double *cent, int64_t *sizes, int k, int d,

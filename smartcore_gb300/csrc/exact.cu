@@ -730,31 +730,46 @@ pp_select_kernel(const T *__restrict__ x, int d, const double *__restrict__ dd,
                  const double *__restrict__ part, int64_t n, int nb,
                  const double *__restrict__ uniform, LloydState *st,
                  T *__restrict__ seed_x, float *__restrict__ seed_cc, int j) {
-  __shared__ double s_incl[kSelThreads];  // inclusive prefix of the chunk sums
+  constexpr int kScan = 256;  // threads that sum chunks of the partials
+  __shared__ double s_incl[kScan];  // inclusive prefix of the chunk sums
   __shared__ double s_wtot[32];
   __shared__ int s_chunk;
   __shared__ long long s_pick;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const int chunk = (nb + kSelThreads - 1) / kSelThreads;
+  const int chunk = (nb + kScan - 1) / kScan;
   const int b0 = min(nb, t * chunk), b1 = min(nb, b0 + chunk);
-  double loc = 0.0;
-  for (int b = b0; b < b1; ++b) loc = __dadd_rn(loc, part[b]);
-  // block-wide inclusive scan: warp scans, then a scan of the warp totals
-  double v = warp_incl_scan(loc);
-  if (lane == 31) s_wtot[w] = v;
-  if (t == 0) s_chunk = kSelThreads;
+  double v = 0.0;
+  if (t < kScan) {
+    double loc = 0.0;
+    for (int b = b0; b < b1; b += 8) {  // eight loads in flight, added in order
+      double pv[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) pv[e] = b + e < b1 ? part[b + e] : 0.0;
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        if (b + e < b1) loc = __dadd_rn(loc, pv[e]);
+    }
+    // inclusive scan: warp scans, then a scan of the warp totals
+    v = warp_incl_scan(loc);
+    if (lane == 31) s_wtot[w] = v;
+  }
+  if (t == 0) s_chunk = kScan;
   __syncthreads();
-  if (w == 0) s_wtot[lane] = warp_incl_scan(s_wtot[lane]);
+  if (w == 0) s_wtot[lane] = warp_incl_scan(lane < kScan / 32 ? s_wtot[lane] : 0.0);
   __syncthreads();
-  if (w > 0) v = __dadd_rn(v, s_wtot[w - 1]);
-  s_incl[t] = v;
+  if (t < kScan) {
+    if (w > 0) v = __dadd_rn(v, s_wtot[w - 1]);
+    s_incl[t] = v;
+  }
   __syncthreads();
-  const double total = s_incl[kSelThreads - 1];
+  const double total = s_incl[kScan - 1];
   const double u = *uniform;
   const double cutoff = __dmul_rn(u, total);
   const double depth_q = (double)chunk + 2.0 * kSelThreads + 2.0 * kPPThreads + 64.0;
-  const double excl = t > 0 ? s_incl[t - 1] : 0.0;
-  if (b1 > b0 && v >= cutoff && !(excl >= cutoff)) atomicMin(&s_chunk, t);
+  if (t < kScan) {
+    const double excl = t > 0 ? s_incl[t - 1] : 0.0;
+    if (b1 > b0 && v >= cutoff && !(excl >= cutoff)) atomicMin(&s_chunk, t);
+  }
   __syncthreads();
   if (w == 0) {
     const bool finite = isfinite(total) && total < DBL_MAX;
@@ -762,7 +777,7 @@ pp_select_kernel(const T *__restrict__ x, int d, const double *__restrict__ dd,
     const double cut_lo = __dmul_rn(u, __dsub_rn(total, tol_tot));
     const double cut_hi = __dmul_rn(u, __dadd_rn(total, tol_tot));
     int64_t pick = -1;
-    if (finite && s_chunk < kSelThreads) {
+    if (finite && s_chunk < kScan) {
       const int c = s_chunk;
       const int cb0 = c * chunk, cb1 = min(nb, cb0 + chunk);
       const Crossing cb = warp_first_crossing(part + cb0, cb1 - cb0, c > 0 ? s_incl[c - 1] : 0.0, cutoff);
@@ -1066,6 +1081,20 @@ __global__ void knn_regress_kernel(const int64_t *__restrict__ idx,
   for (int t = 0; t < c; ++t)
     r = __dadd_rn(r, __dmul_rn(y[idx[q * k + pos[t]]], __ddiv_rn(w[t], w_sum)));
   out[q] = r;
+}
+
+// Labels widened to the reference's usize-sized indices for the host copy.
+__global__ void widen_labels_kernel(const int32_t *__restrict__ in, int64_t *__restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = in[i];
+}
+
+sc_status launch_widen_labels(const int32_t *in, int64_t *out, int64_t n, cudaStream_t s) {
+  if (n == 0) return SC_OK;
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  widen_labels_kernel<<<grid, 256, 0, s>>>(in, out, n);
+  SC_LAUNCHED();
+  return SC_OK;
 }
 
 sc_status launch_knn_vote(const int64_t *idx, const double *dist, int64_t m,

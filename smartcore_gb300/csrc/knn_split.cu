@@ -631,17 +631,6 @@ sc_status map2d(CUtensorMap *m, void *ptr, int64_t rows, int cols, int box_cols,
   return SC_OK;
 }
 
-template <class T>
-sc_status dal(T **p, size_t count) {
-  *p = nullptr;
-  SC_CUDA(cudaMalloc((void **)p, (count ? count : 1) * sizeof(T)));
-  return SC_OK;
-}
-template <class T>
-void dfr(T *&p) {
-  if (p) cudaFree((void *)p);
-  p = nullptr;
-}
 
 int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
 
@@ -704,12 +693,12 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   if (!s->num_sms) SC_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t n_pad = (n + tn - 1) / tn * tn;
   if (!s->ready || s->train != train || s->n != n || s->d != d) {  // training operand, once per handle
-    dfr(s->th); dfr(s->tl); dfr(s->tbx); dfr(s->tmax); dfr(s->ones);
-    SC_TRY(dal(&s->th, (size_t)n_pad * d_pad));
-    SC_TRY(dal(&s->tl, (size_t)n_pad * d_pad));
-    SC_TRY(dal(&s->tbx, (size_t)n_pad * 16));
-    SC_TRY(dal(&s->tmax, 1));
-    SC_TRY(dal(&s->ones, (size_t)kQM * 16));
+    dfree(s->th, st); dfree(s->tl, st); dfree(s->tbx, st); dfree(s->tmax, st); dfree(s->ones, st);
+    SC_TRY(dalloc(&s->th, (size_t)n_pad * d_pad, st));
+    SC_TRY(dalloc(&s->tl, (size_t)n_pad * d_pad, st));
+    SC_TRY(dalloc(&s->tbx, (size_t)n_pad * 16, st));
+    SC_TRY(dalloc(&s->tmax, 1, st));
+    SC_TRY(dalloc(&s->ones, (size_t)kQM * 16, st));
     ones_tile_kernel<<<1, kQM, 0, st>>>(s->ones);
     SC_LAUNCHED();
     SC_TRY(map2d(&s->tm_ones, s->ones, kQM, 16, 16, kQM, 32));
@@ -732,14 +721,14 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   }
   const int64_t m_pad = (m + kQM - 1) / kQM * kQM;
   if (m_pad > s->m_cap) {
-    dfr(s->qh); dfr(s->ql); dfr(s->qnrm); dfr(s->qn2);
-    SC_TRY(dal(&s->qh, (size_t)m_pad * d_pad));
-    SC_TRY(dal(&s->ql, (size_t)m_pad * d_pad));
-    SC_TRY(dal(&s->qnrm, (size_t)m_pad));
-    SC_TRY(dal(&s->qn2, (size_t)m_pad));
+    dfree(s->qh, st); dfree(s->ql, st); dfree(s->qnrm, st); dfree(s->qn2, st);
+    SC_TRY(dalloc(&s->qh, (size_t)m_pad * d_pad, st));
+    SC_TRY(dalloc(&s->ql, (size_t)m_pad * d_pad, st));
+    SC_TRY(dalloc(&s->qnrm, (size_t)m_pad, st));
+    SC_TRY(dalloc(&s->qn2, (size_t)m_pad, st));
     s->m_cap = m_pad;
   }
-  if (!s->evals) SC_TRY(dal(&s->evals, 2));
+  if (!s->evals) SC_TRY(dalloc(&s->evals, 2, st));
   SC_CUDA(cudaMemsetAsync(s->evals, 0, 2 * sizeof(unsigned long long), st));
   const int nbq = (int)((m_pad + 7) / 8);
   if (dtype == SC_F32)
@@ -820,9 +809,9 @@ sc_status split_knn_radius(SplitKnnState *s, int dtype, const void *train, int64
   return run_split_knn(s, dtype, train, n, d, queries, m, 0, idx, dist, nullptr, &rad, st);
 }
 
-void split_knn_free(SplitKnnState *s) {
-  dfr(s->th); dfr(s->tl); dfr(s->tbx); dfr(s->tmax); dfr(s->ones);
-  dfr(s->qh); dfr(s->ql); dfr(s->qnrm); dfr(s->qn2); dfr(s->evals);
+void split_knn_free(SplitKnnState *s, cudaStream_t st) {
+  dfree(s->th, st); dfree(s->tl, st); dfree(s->tbx, st); dfree(s->tmax, st); dfree(s->ones, st);
+  dfree(s->qh, st); dfree(s->ql, st); dfree(s->qnrm, st); dfree(s->qn2, st); dfree(s->evals, st);
   s->ready = 0;
   s->m_cap = 0;
 }

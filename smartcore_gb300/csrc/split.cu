@@ -922,17 +922,6 @@ sc_status make_map(CUtensorMap *m, void *ptr, int64_t rows, int cols, int box_co
   return SC_OK;
 }
 
-template <class T>
-sc_status dalloc(T **p, size_t count) {
-  *p = nullptr;
-  SC_CUDA(cudaMalloc((void **)p, (count ? count : 1) * sizeof(T)));
-  return SC_OK;
-}
-template <class T>
-void dfree(T *&p) {
-  if (p) cudaFree((void *)p);
-  p = nullptr;
-}
 
 // Feature padding: rows of 32 B (d <= 16, 32-byte swizzle), 64 B (d <= 32,
 // 64-byte swizzle) or multiples of 128 B (128-byte swizzle, 64-feature tiles).
@@ -949,7 +938,7 @@ size_t assign_smem(const SplitState *s, int stages, int k_pad) {
 
 sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int d, double *xnorm_total,
                         cudaStream_t st) {
-  split_free(s);
+  split_free(s, st);
   s->dtype = dtype;
   s->n = n;
   s->n_pad = (n + kBM - 1) / kBM * kBM;
@@ -966,16 +955,16 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
   int dev = 0;
   SC_CUDA(cudaGetDevice(&dev));
   SC_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
-  SC_TRY(dalloc(&s->xh, (size_t)(s->n_pad * s->d_pad)));
-  SC_TRY(dalloc(&s->xl, (size_t)(s->n_pad * s->d_pad)));
-  SC_TRY(dalloc(&s->xnrm, (size_t)s->n_pad));
+  SC_TRY(dalloc(&s->xh, (size_t)(s->n_pad * s->d_pad), st));
+  SC_TRY(dalloc(&s->xl, (size_t)(s->n_pad * s->d_pad), st));
+  SC_TRY(dalloc(&s->xnrm, (size_t)s->n_pad, st));
   const int nb = (int)((s->n_pad + 7) / 8);
-  SC_TRY(dalloc(&s->part, (size_t)nb));
-  SC_TRY(dalloc(&s->list_rows, (size_t)(s->n_pad + (int64_t)s->num_sms * kBM)));
-  SC_TRY(dalloc(&s->list_count, (size_t)s->num_sms));
-  SC_TRY(dalloc(&s->cand4, (size_t)(2 * s->n_pad)));  // uint2 each
-  SC_TRY(dalloc(&s->cmeta, (size_t)(2 * s->n_pad)));
-  SC_TRY(dalloc(&s->cmax, 1));
+  SC_TRY(dalloc(&s->part, (size_t)nb, st));
+  SC_TRY(dalloc(&s->list_rows, (size_t)(s->n_pad + (int64_t)s->num_sms * kBM), st));
+  SC_TRY(dalloc(&s->list_count, (size_t)s->num_sms, st));
+  SC_TRY(dalloc(&s->cand4, (size_t)(2 * s->n_pad), st));  // uint2 each
+  SC_TRY(dalloc(&s->cmeta, (size_t)(2 * s->n_pad), st));
+  SC_TRY(dalloc(&s->cmax, 1, st));
   if (dtype == SC_F32)
     prep_x_kernel<float><<<nb, 256, 0, st>>>((const float *)x, n, s->n_pad, d, s->d_pad, s->xh, s->xl, s->xnrm, s->part);
   else
@@ -985,7 +974,7 @@ sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int 
   SC_LAUNCHED();
   SC_TRY(make_map(&s->tm_xh, s->xh, s->n_pad, s->d_pad, s->kt_elems, kBM, s->row_bytes));
   SC_TRY(make_map(&s->tm_xl, s->xl, s->n_pad, s->d_pad, s->kt_elems, kBM, s->row_bytes));
-  SC_TRY(dalloc(&s->ones, (size_t)kBM * 16));
+  SC_TRY(dalloc(&s->ones, (size_t)kBM * 16, st));
   ones_tile_kernel<<<1, kBM, 0, st>>>(s->ones);
   SC_LAUNCHED();
   SC_TRY(make_map(&s->tm_ones, s->ones, kBM, 16, 16, kBM, 32));
@@ -1015,12 +1004,12 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
     return SC_ERR_INVALID;
   }
   if (k_cols > s->k_alloc) {
-    dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cT); dfree(s->cbx);
-    SC_TRY(dalloc(&s->ch, (size_t)k_cols * s->d_pad));
-    SC_TRY(dalloc(&s->cl, (size_t)k_cols * s->d_pad));
-    SC_TRY(dalloc(&s->cbx, (size_t)k_cols * 16));
-    SC_TRY(dalloc(&s->cn2, (size_t)k_cols));
-    SC_TRY(dalloc(&s->cT, (size_t)k_cols * s->d_pad));
+    dfree(s->ch, st); dfree(s->cl, st); dfree(s->cn2, st); dfree(s->cT, st); dfree(s->cbx, st);
+    SC_TRY(dalloc(&s->ch, (size_t)k_cols * s->d_pad, st));
+    SC_TRY(dalloc(&s->cl, (size_t)k_cols * s->d_pad, st));
+    SC_TRY(dalloc(&s->cbx, (size_t)k_cols * 16, st));
+    SC_TRY(dalloc(&s->cn2, (size_t)k_cols, st));
+    SC_TRY(dalloc(&s->cT, (size_t)k_cols * s->d_pad, st));
     s->k_alloc = k_cols;
     s->k_pad = 0;
   }
@@ -1122,10 +1111,10 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   return SC_OK;
 }
 
-void split_free(SplitState *s) {
-  dfree(s->xh); dfree(s->xl); dfree(s->xnrm); dfree(s->part);
-  dfree(s->ch); dfree(s->cl); dfree(s->cn2); dfree(s->cmax); dfree(s->cbx); dfree(s->ones);
-  dfree(s->cT); dfree(s->list_rows); dfree(s->list_count); dfree(s->cand4); dfree(s->cmeta);
+void split_free(SplitState *s, cudaStream_t st) {
+  dfree(s->xh, st); dfree(s->xl, st); dfree(s->xnrm, st); dfree(s->part, st);
+  dfree(s->ch, st); dfree(s->cl, st); dfree(s->cn2, st); dfree(s->cmax, st); dfree(s->cbx, st); dfree(s->ones, st);
+  dfree(s->cT, st); dfree(s->list_rows, st); dfree(s->list_count, st); dfree(s->cand4, st); dfree(s->cmeta, st);
   s->ready = 0;
   s->k_alloc = 0;
   s->k_pad = 0;

@@ -57,7 +57,7 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
 sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d,
                        const double *cent, int k, int32_t *labels, LloydState *lst,
                        cudaStream_t st, cudaEvent_t *timing = nullptr);
-void split_free(SplitState *s);
+void split_free(SplitState *s, cudaStream_t st);
 
 sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
                     const void *queries, int64_t m, int k, int64_t *idx, double *dist,
@@ -67,6 +67,6 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
 sc_status split_knn_radius(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
                            const void *queries, int64_t m, double radius, int64_t *counts,
                            const int64_t *offsets, int64_t *idx, double *dist, cudaStream_t st);
-void split_knn_free(SplitKnnState *s);
+void split_knn_free(SplitKnnState *s, cudaStream_t st);
 
 }  // namespace sc

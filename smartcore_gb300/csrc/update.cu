@@ -560,8 +560,9 @@ static int ceil_log2(int64_t v) {
   return l;
 }
 
-sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms) {
-  update_free(u);
+sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms,
+                       cudaStream_t s) {
+  update_free(u, s);
   int e = 0;
   if (absmax > 0) frexp(absmax, &e);  // |x| < 2^e
   int grid = num_sms;
@@ -581,26 +582,24 @@ sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double 
     if (u->scale > 160) u->scale = 160;  // values below 2^-160 contribute 0
     const size_t bal = smem + (size_t)k * d * sizeof(long long);
     u->balanced_smem = (d <= 128 && bal <= 200 * 1024) ? bal : 0;
-    if (cudaMalloc((void **)&u->part, part_bytes) != cudaSuccess ||
-        cudaMalloc((void **)&u->cpart, (size_t)grid * k * sizeof(unsigned int)) != cudaSuccess)
-      return cuda_fail(cudaErrorMemoryAllocation, "update partials");
+    SC_TRY(dalloc(&u->part, (size_t)grid * k * d, s));
+    SC_TRY(dalloc(&u->cpart, (size_t)grid * k, s));
     return SC_OK;
   }
   u->mode = 0;
   u->scale = 125 - e - ceil_log2(n + 1);
-  if (cudaMalloc((void **)&u->acc, (size_t)k * d * sizeof(Acc128)) != cudaSuccess ||
-      cudaMalloc((void **)&u->cnt, (size_t)k * sizeof(unsigned long long)) != cudaSuccess)
-    return cuda_fail(cudaErrorMemoryAllocation, "update accumulators");
-  SC_CUDA(cudaMemset(u->acc, 0, (size_t)k * d * sizeof(Acc128)));
-  SC_CUDA(cudaMemset(u->cnt, 0, (size_t)k * sizeof(unsigned long long)));
+  SC_TRY(dalloc(&u->acc, (size_t)k * d, s));
+  SC_TRY(dalloc(&u->cnt, (size_t)k, s));
+  SC_CUDA(cudaMemsetAsync(u->acc, 0, (size_t)k * d * sizeof(Acc128), s));
+  SC_CUDA(cudaMemsetAsync(u->cnt, 0, (size_t)k * sizeof(unsigned long long), s));
   return SC_OK;
 }
 
-void update_free(UpdateBuf *u) {
-  if (u->acc) cudaFree(u->acc);
-  if (u->cnt) cudaFree(u->cnt);
-  if (u->part) cudaFree(u->part);
-  if (u->cpart) cudaFree(u->cpart);
+void update_free(UpdateBuf *u, cudaStream_t s) {
+  dfree(u->acc, s);
+  dfree(u->cnt, s);
+  dfree(u->part, s);
+  dfree(u->cpart, s);
   *u = UpdateBuf();
 }
 
