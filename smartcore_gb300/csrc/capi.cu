@@ -292,14 +292,16 @@ sc_status sc_kmeans_seed(sc_kmeans *h, int64_t k, int64_t first_index, const dou
   SC_CUDA(cudaMemcpyAsync(h->seed_x, (const char *)h->x + (size_t)first_index * row_bytes, row_bytes,
                           cudaMemcpyDeviceToDevice, s));
   const int nb = pp_block_count(h->n);
+  // the split form's BF16 rows serve the update's first bound
+  const __nv_bfloat16 *xh = h->form == SC_FORM_SPLIT_BF16 && h->split.ready ? h->split.xh : nullptr;
   for (int64_t j = 1; j < k; ++j) {  // kmeans.rs:367-397
     SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(j - 1), h->dd, h->dd32, h->labels,
-                            h->part, j == 1, h->seed_cc, s));
+                            h->part, j == 1, h->seed_cc, xh, h->split.d_pad, h->split.xnrm, s));
     SC_TRY(launch_pp_select(h->dtype, h->x, (int)h->d, h->dd, h->part, h->n, nb, h->uniforms + (j - 1), h->st,
                             h->seed_x, h->seed_cc, (int)j, s));
   }
   SC_TRY(launch_pp_update(h->dtype, h->x, h->n, (int)h->d, h->st, (int32_t)(k - 1), h->dd, h->dd32, h->labels,
-                          nullptr, k == 1, h->seed_cc, s));  // :399-410
+                          nullptr, k == 1, h->seed_cc, xh, h->split.d_pad, h->split.xnrm, s));  // :399-410
   // initial centroids: means of the seeding partition (kmeans.rs:275-292)
   SC_TRY(launch_update(&h->upd, h->dtype, h->x, h->n, (int)h->d, h->labels, (int)k, nullptr, s));
   SC_TRY(launch_finalize(&h->upd, h->cent, h->sizes, (int)k, (int)h->d, nullptr, 1, nullptr, s));

@@ -1,6 +1,7 @@
 // Shared declarations of the smartcore_gb300 CUDA library.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -100,11 +101,13 @@ sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
 // seed_cc (k entries, may be null): lower bounds of the squared distances
 // from the current seed to the earlier ones, written by launch_pp_select;
 // dd32 (n entries, may be null): d rounded up to f32, the far test's copy
-// (f32 rows with d <= 128 only).
+// (f32 rows with d <= 128 only); xh (may be null): the BF16 high halves of
+// the rows (n_pad x d_pad, split form) with xnrm >= |x| per row.
 sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
                            const LloydState *st, int32_t label_of_seed,
                            double *dd, float *dd32, int32_t *labels, double *part,
-                           int first_pass, const float *seed_cc, cudaStream_t s);
+                           int first_pass, const float *seed_cc, const __nv_bfloat16 *xh, int d_pad,
+                           const float *xnrm, cudaStream_t s);
 // Picks seed j into st->pp_chosen and its row into seed_x[j] (k x d, element
 // type); writes seed_cc[0..j).
 sc_status launch_pp_select(int dtype, const void *x, int d, const double *dd, const double *part,

@@ -9,6 +9,8 @@
 #include <algorithm>
 #include <type_traits>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 #include "exactsum.cuh"
 
@@ -272,19 +274,20 @@ __global__ void __launch_bounds__(kDrawThreads, 7)
 pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *st, int32_t label_of_seed,
                double *__restrict__ dd, float *__restrict__ dd32, int32_t *__restrict__ labels,
                double *__restrict__ part, int64_t nb, int lg_d, const float *__restrict__ seed_cc,
-               PPFar32 far) {
+               PPFar32 far, const __nv_bfloat16 *__restrict__ xh, int d_pad, const float *__restrict__ xnrm) {
   using V = typename std::conditional<VEC == 4, float4, float>::type;
   constexpr int NP = VEC == 4 ? 1 : 4;  // row passes with loads in flight together
   constexpr int UM = 4;                 // loads per lane per row (d <= 128)
   __shared__ __align__(16) float s_cen[128];
   __shared__ uint8_t s_need[kDrawWarps][kPPThreads];  // the warp's rows left by the far test
-  __shared__ float s_cur[kDrawWarps][kPPThreads];     // and their d32
+  __shared__ uint8_t s_need2[kDrawWarps][kPPThreads];  // ... and by the BF16 bound
+  __shared__ float s_cur[kDrawWarps][kPPThreads];     // d32 of the block's rows
   __shared__ uint8_t s_ex[kDrawWarps][kPPThreads];    // rows that need the sequential exact sum
   __shared__ uint8_t s_valr[kDrawWarps][kPPThreads];  // rows whose exact value is known
   __shared__ double s_valv[kDrawWarps][kPPThreads];   // and that value
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t ci = st->pp_chosen;
-  for (int t = threadIdx.x; t < d; t += kDrawThreads) s_cen[t] = x[ci * d + t];
+  for (int t = threadIdx.x; t < 128; t += kDrawThreads) s_cen[t] = t < d ? x[ci * d + t] : 0.f;
   __syncthreads();
   // a row is `units` loads of VEC floats; p lanes per row (a power of two,
   // at most UM units per lane), R = 32 / p rows per pass
@@ -314,15 +317,70 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
         const int64_t i = rb + (h + g) * 32 + lane;
         const bool need = i < n && !pp_far32(seed_cc[lb[g]], c32[g], far);
         const unsigned m = __ballot_sync(0xffffffffu, need);
-        if (need) {
-          const int pos = cnt + __popc(m & lt);
-          s_need[w][pos] = (uint8_t)((h + g) * 32 + lane);
-          s_cur[w][pos] = c32[g];
-        }
+        if (need) s_need[w][cnt + __popc(m & lt)] = (uint8_t)((h + g) * 32 + lane);
+        s_cur[w][(h + g) * 32 + lane] = c32[g];
         cnt += __popc(m);
       }
     }
     __syncwarp();
+    const uint8_t *need_list = s_need[w];
+    if (xh) {
+      // Split form: the BF16 high half x_h of the row (half the bytes) bounds
+      // the real distance from below: |x - c| >= |x_h - c| - |x - x_h|, with
+      // |x - x_h| <= 2^-8 |x| + sqrt(d) 2^-133 (round to nearest BF16) and
+      // xnrm >= |x|.  With the f32 sum s_h of fl(fl(x_h - c)^2) (depth <= d),
+      // |x_h - c|^2 >= (s_h - d 2^-147)(1 - (d + 8) 2^-23); the row keeps its
+      // distance when (1 - eta) r_lo^2 - A >= d32, as in the far test.
+      const int units_h = d_pad >> 3;  // 16-byte units (8 BF16) per row
+      constexpr int UH = 2;  // 16-byte units per lane
+      int ph = 1;
+      while (ph * UH < units_h) ph <<= 1;
+      const int Rh = 32 / ph, segh = lane / ph, unith = lane - segh * ph;
+      const uint4 *xbh = reinterpret_cast<const uint4 *>(xh + rb * d_pad);
+      const float relh = 1.f - (float)(d + 8) * 0x1p-23f, sqd = sqrtf((float)d) * 0x1p-133f;
+      int cnt2 = 0;
+      for (int it = 0; it < cnt; it += Rh) {
+        const int idx = it + segh;
+        const int rr = idx < cnt ? (int)need_list[idx] : -1;
+        uint4 hv[UH];
+#pragma unroll
+        for (int k = 0; k < UH; ++k) {
+          const int uu = unith + k * ph;
+          if (rr >= 0 && uu < units_h) hv[k] = xbh[rr * units_h + uu];
+        }
+        const float xn = rr >= 0 && unith == 0 ? xnrm[rb + rr] : 0.f;
+        float sh = 0.f;
+#pragma unroll
+        for (int k = 0; k < UH; ++k) {
+          const int uu = unith + k * ph;
+          if (rr >= 0 && uu < units_h) {
+            const uint32_t wv[4] = {hv[k].x, hv[k].y, hv[k].z, hv[k].w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const float lo = __uint_as_float(wv[e] << 16), hi = __uint_as_float(wv[e] & 0xffff0000u);
+              float r = __fsub_rn(lo, s_cen[uu * 8 + 2 * e]);
+              sh = __fadd_rn(sh, __fmul_rn(r, r));
+              r = __fsub_rn(hi, s_cen[uu * 8 + 2 * e + 1]);
+              sh = __fadd_rn(sh, __fmul_rn(r, r));
+            }
+          }
+        }
+        for (int o = ph >> 1; o > 0; o >>= 1) sh = __fadd_rn(sh, __shfl_xor_sync(0xffffffffu, sh, o));
+        bool left = false;
+        if (rr >= 0 && unith == 0) {
+          const float L = fmaxf(0.f, __fmul_rd(__fsub_rd(sh, (float)d * 0x1p-147f), relh));
+          const float rlo = __fsub_rd(__fsqrt_rd(L), __fadd_ru(__fmul_ru(xn, 0x1p-8f), sqd));
+          left = !(rlo > 0.f &&
+                   __fsub_rd(__fmul_rd(__fmul_rd(rlo, rlo), 1.f - 0x1p-22f), far.abs_) >= s_cur[w][rr]);
+        }
+        const unsigned lm = __ballot_sync(0xffffffffu, left);
+        if (left) s_need2[w][cnt2 + __popc(lm & lt)] = (uint8_t)rr;
+        cnt2 += __popc(lm);
+      }
+      __syncwarp();
+      need_list = s_need2[w];
+      cnt = cnt2;
+    }
     // f32 lower bound of the listed rows, R rows per load, NP loads in flight
     const V *xb = reinterpret_cast<const V *>(x + rb * d);
     int exn = 0;   // rows listed in s_ex
@@ -333,7 +391,7 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         const int idx = it + q * R + seg;
-        rq[q] = idx < cnt ? (int)s_need[w][idx] : -1;
+        rq[q] = idx < cnt ? (int)need_list[idx] : -1;
 #pragma unroll
         for (int k = 0; k < UM; ++k) {
           const int uu = unit + k * p;
@@ -369,7 +427,7 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
         }
         for (int o = p >> 1; o > 0; o >>= 1) s32 = __fadd_rn(s32, __shfl_xor_sync(0xffffffffu, s32, o));
         const int idx = it + q * R + seg;
-        const bool ex = rq[q] >= 0 && unit == 0 && !(__fmul_rd(s32, lbf) > s_cur[w][idx]);
+        const bool ex = rq[q] >= 0 && unit == 0 && !(__fmul_rd(s32, lbf) > s_cur[w][rq[q] >= 0 ? rq[q] : 0]);
         if (__any_sync(0xffffffffu, ex)) {
           // The exact value without the sequential sum: in units of
           // 2^(emin - 150) every term is an integer below 2^(24 + span); while
@@ -536,7 +594,8 @@ int device_sms() {
 sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
                            const LloydState *st, int32_t label_of_seed,
                            double *dd, float *dd32, int32_t *labels, double *part,
-                           int first_pass, const float *seed_cc, cudaStream_t s) {
+                           int first_pass, const float *seed_cc, const __nv_bfloat16 *xh, int d_pad,
+                           const float *xnrm, cudaStream_t s) {
   const int grid = pp_block_count(n);
   const size_t smem = (size_t)d * (dtype == SC_F32 ? 4 : 8);
   if (smem > 48 * 1024) {
@@ -567,10 +626,10 @@ sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
       const PPFar32 far = pp_far_bound32(d);
       if (vec4)
         pp_draw_kernel<4><<<g1, kDrawThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
-                                                      lg_d, seed_cc, far);
+                                                      lg_d, seed_cc, far, xh, d_pad, xnrm);
       else
         pp_draw_kernel<1><<<g1, kDrawThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
-                                                      lg_d, seed_cc, far);
+                                                      lg_d, seed_cc, far, xh, d_pad, xnrm);
       SC_LAUNCHED();
     }
   } else if (dtype == SC_F32) {

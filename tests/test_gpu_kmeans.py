@@ -85,13 +85,17 @@ def test_bbdtree_iris_step(kats):
 # (n, d, blobs, k): d % 4 == 0 f32 rows take the 16-byte staged copies, other
 # f32 rows up to d = 128 the 4-byte ones, f64 rows and d > 128 the plain
 # kernel; well separated blobs let most rows skip the distance (far test).
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("n,d,c,k", [(20_000, 8, 16, 16), (30_000, 7, 40, 48), (20_000, 64, 64, 64),
-                                     (5_000, 200, 8, 12), (3_001, 1, 5, 9)])
-def test_kmeanspp_labels(dtype, n, d, c, k):
+                                     (9_000, 100, 30, 40), (5_000, 200, 8, 12), (3_001, 1, 5, 9)])
+def test_kmeanspp_labels(form, dtype, n, d, c, k):
+    # the split form's update also bounds rows through their BF16 high halves
+    if form == _lib.FORM_SPLIT_BF16 and d > 128:
+        pytest.skip("the split form's tiles hold d <= 128")
     x, _ = blobs(n, d, c, seed=12, dtype=dtype)
     first, u = kmeanspp_draws(len(x), k, 5)
-    h = KMeansHandle(x)
+    h = KMeansHandle(x, form=form)
     h.seed(k, first, u)
     _, sizes, labels, _, _ = h.get()
     y, _ = oracle.kmeanspp(x, k, first, u)
