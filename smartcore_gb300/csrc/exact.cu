@@ -217,9 +217,9 @@ __host__ __device__ __forceinline__ int pp_stage_ld(int d, int vec4) {
 // are listed and read coalesced (up to four 16-byte units per lane, two
 // passes of whole rows in flight) for the f32 lower bound; the rows that bound cannot
 // settle either (the rows whose distance may drop) get the reference's exact
-// value, from the integer sum of their terms across the row's lanes when no
-// addition of the sequential f64 sum can round (almost every row), else from
-// the sequential reproduction, one row per lane.  The warp then writes the block's fixed-order partial sum
+// value, from the integer sum of their terms across the row's lanes when that
+// sum shows that no addition of the sequential f64 sum can round (almost every
+// row), else from the sequential reproduction, one row per lane.  The warp then writes the block's fixed-order partial sum
 // of d for the selection.  The first draw (every row exact) runs
 // pp_first_kernel, which stages the rows in shared memory, and then
 // pp_partials_kernel.
@@ -430,10 +430,12 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
         const bool ex = rq[q] >= 0 && unit == 0 && !(__fmul_rd(s32, lbf) > s_cur[w][rq[q] >= 0 ? rq[q] : 0]);
         if (__any_sync(0xffffffffu, ex)) {
           // The exact value without the sequential sum: in units of
-          // 2^(emin - 150) every term is an integer below 2^(24 + span); while
-          // span <= 29 - ceil(log2 d) every partial sum stays below 2^53, so
-          // no addition of the reference's f64 sequence rounds and its result
-          // is the integer sum, in any order (here: across the row's lanes).
+          // 2^(emin - 150) every term is an integer below 2^(24 + span), so
+          // while span <= 38 - ceil(log2 d) the integer sum S of the terms
+          // (in any order; here across the row's lanes) is below 2^62.  The
+          // terms are nonnegative, so when S < 2^53 every partial sum of the
+          // reference's f64 sequence is an integer below 2^53 as well: no
+          // addition rounds and its result is S.
           int emn = 255, emx = 0;
 #pragma unroll
           for (int k = 0; k < UM; ++k) {
@@ -454,9 +456,9 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
             emn = min(emn, __shfl_xor_sync(0xffffffffu, emn, o));
             emx = max(emx, __shfl_xor_sync(0xffffffffu, emx, o));
           }
-          const bool fits = emx < 255 && (emn == 255 || emx - emn <= 29 - lg_d);
+          const bool span_ok = emx < 255 && (emn == 255 || emx - emn <= 38 - lg_d);
           unsigned long long S = 0ull;
-          if (fits && emn < 255) {
+          if (span_ok && emn < 255) {
 #pragma unroll
             for (int k = 0; k < UM; ++k) {
               const int uu = unit + k * p;
@@ -472,6 +474,7 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
             }
           }
           for (int o = p >> 1; o > 0; o >>= 1) S += __shfl_xor_sync(0xffffffffu, S, o);
+          const bool fits = span_ok && (S >> 53) == 0ull;
           const unsigned fm = __ballot_sync(0xffffffffu, ex && fits);
           const unsigned sm = __ballot_sync(0xffffffffu, ex && !fits);
           if (ex && fits) {
