@@ -63,6 +63,27 @@ void dev_free(void *p, cudaStream_t s) {
   if (p) cudaFreeAsync(p, s);
 }
 
+// Pinned host staging buffer for results copied into caller memory (grows,
+// never shrinks; callers hold g_stage_mutex while they use it).  A device
+// copy into pageable memory that the caller has just allocated pays for the
+// first touch of every page inside the driver's copy; a copy into pinned
+// memory and a CPU memcpy do not.
+std::mutex g_stage_mutex;
+void *g_stage = nullptr;
+size_t g_stage_bytes = 0;
+
+sc_status host_stage(size_t bytes, void **out) {
+  if (bytes > g_stage_bytes) {
+    if (g_stage) cudaFreeHost(g_stage);
+    g_stage = nullptr;
+    g_stage_bytes = 0;
+    SC_CUDA(cudaHostAlloc(&g_stage, bytes, cudaHostAllocDefault));
+    g_stage_bytes = bytes;
+  }
+  *out = g_stage;
+  return SC_OK;
+}
+
 namespace {
 
 size_t esize(int dtype) { return dtype == SC_F32 ? 4 : 8; }
@@ -170,6 +191,7 @@ static sc_status kmeans_alloc_k(sc_kmeans *h, int64_t k) {
   SC_TRY(dalloc(&h->seed_cc, (size_t)k, h->stream));
   SC_CUDA(cudaStreamSynchronize(h->stream));
   SC_TRY(update_alloc(&h->upd, h->dtype, h->n, (int)h->d, (int)k, h->absmax, h->num_sms, h->stream));
+  if (h->dtype == SC_F32) SC_TRY(update_pack(&h->upd, (const float *)h->x, h->n, (int)h->d, h->stream));
   h->k_alloc = k;
   h->k = k;
   return SC_OK;
@@ -210,7 +232,12 @@ void sc_kmeans_destroy(sc_kmeans *h) {
   dfree(h->xnorm_total, hs); dfree(h->st, hs); dfree(h->bits, hs);
   split_free(&h->split, hs);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  // the frees complete before the stream goes away, so the pool hands the
+  // blocks to the next handle's stream without waiting on a dead one
+  if (h->stream) {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+  }
   delete h;
 }
 
@@ -373,15 +400,21 @@ sc_status sc_kmeans_get(sc_kmeans *h, double *centroids, int64_t *sizes, int64_t
     SC_CUDA(cudaMemcpyAsync(centroids, h->cent, (size_t)(h->k * h->d) * sizeof(double), cudaMemcpyDeviceToHost, s));
   if (sizes) SC_CUDA(cudaMemcpyAsync(sizes, h->sizes, (size_t)h->k * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   int64_t *wide = nullptr;
-  if (labels && h->n > 0) {  // widened on the device, one copy straight into the caller's array
+  std::unique_lock<std::mutex> stage_lock(g_stage_mutex, std::defer_lock);
+  void *stage = nullptr;
+  const size_t label_bytes = (size_t)h->n * sizeof(int64_t);
+  if (labels && h->n > 0) {  // widened on the device, copied through the pinned staging buffer
     SC_TRY(dalloc(&wide, (size_t)h->n, s));
     SC_TRY(launch_widen_labels(h->labels, wide, h->n, s));
-    SC_CUDA(cudaMemcpyAsync(labels, wide, (size_t)h->n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    stage_lock.lock();
+    SC_TRY(host_stage(label_bytes, &stage));
+    SC_CUDA(cudaMemcpyAsync(stage, wide, label_bytes, cudaMemcpyDeviceToHost, s));
     dfree(wide, s);
   }
   LloydState st;
   SC_CUDA(cudaMemcpyAsync(&st, h->st, sizeof st, cudaMemcpyDeviceToHost, s));
   SC_CUDA(cudaStreamSynchronize(s));
+  if (stage) memcpy(labels, stage, label_bytes);
   if (distortion) *distortion = st.distortion;
   if (iters) *iters = st.iters;
   return SC_OK;
@@ -525,7 +558,10 @@ void sc_knn_destroy(sc_knn *h) {
   dfree(h->train, hs); dfree(h->q, hs); dfree(h->idx, hs); dfree(h->dist, hs);
   dfree(h->aux_i, hs); dfree(h->aux_d, hs);
   split_knn_free(&h->split, hs);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->stream) {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+  }
   delete h;
 }
 

@@ -73,6 +73,8 @@ struct UpdateBuf {
   unsigned long long *cnt = nullptr;  // mode 0: k
   long long *part = nullptr;        // mode 1: grid x k x d
   unsigned int *cpart = nullptr;    // mode 1: grid x k
+  uint32_t *xq = nullptr;           // mode 1: the points in the packed fixed-point form of `scale`
+  const void *xq_src = nullptr;     // the points xq was made from
 };
 
 // ---- device memory ----
@@ -152,6 +154,8 @@ inline int64_t update_nterms(const UpdateBuf *u, int k, int d) {
   return u->mode != 0 ? ((int64_t)k * d + 31) / 32 : k;
 }
 void update_free(UpdateBuf *u, cudaStream_t s);
+// Packs the points for the balanced partial form (once per dataset and scale).
+sc_status update_pack(UpdateBuf *u, const float *x, int64_t n, int d, cudaStream_t s);
 sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n, int d,
                         const int32_t *labels, int k, const LloydState *st, cudaStream_t s);
 sc_status launch_finalize(const UpdateBuf *u, double *cent, int64_t *sizes, int k, int d,

@@ -12,6 +12,9 @@
 #include <float.h>
 #include <math.h>
 
+#include <algorithm>
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace sc {
@@ -173,6 +176,45 @@ __device__ __forceinline__ void add_fixed64(long long &acc, float v, const Fixed
   acc += to_fixed64_slow(b, f.scale);  // subnormal, below the integer grid, or sh > 30: rare
 }
 
+// Packed fixed-point form of an f32 value for a given scale, made once per
+// dataset: bits 25..31 hold sh = e - 150 + scale in [0, 30] and bits 0..24 the
+// signed 25-bit mantissa, so v * 2^scale = mantissa * 2^sh.  sh = 31 marks a
+// value outside that form (subnormal, below the integer grid, or sh > 30),
+// converted from the f32 value itself.  +-0 packs to 0.
+constexpr uint32_t kPackSlow = 31u << 25;
+
+__global__ void pack_fixed_kernel(const float *__restrict__ x, int64_t count, uint32_t *__restrict__ xq, int scale) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t b = __float_as_uint(x[i]);
+    const int e = (int)((b >> 23) & 0xffu);
+    uint32_t q;
+    if (e == 0) {
+      q = (b << 1) == 0u ? 0u : kPackSlow;
+    } else {
+      const int sh = e - 150 + scale;
+      if (sh < 0 || sh > 30) {
+        q = kPackSlow;
+      } else {
+        const int m = (int)((b & 0x7fffffu) | 0x800000u);
+        q = ((uint32_t)sh << 25) | ((uint32_t)((int)b < 0 ? -m : m) & 0x1ffffffu);
+      }
+    }
+    xq[i] = q;
+  }
+}
+
+// The same sum as add_fixed64 from the packed form: one shift pair and one
+// 32 x 32 -> 64-bit multiply-add per value.
+__device__ __forceinline__ void add_packed64(long long &acc, uint32_t q, const float *xe, int scale) {
+  const uint32_t sh = q >> 25;
+  if (sh != 31u) {
+    const int sm = ((int)(q << 7)) >> 7;
+    asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(acc) : "r"(sm), "r"(1 << sh));
+  } else {
+    acc += to_fixed64_slow(__float_as_uint(*xe), scale);
+  }
+}
+
 // Counting sort of a CTA's chunk by label (shared memory): cnt[c] points of
 // cluster c, off[c] .. off[c + 1] their positions in idx (chunk-relative rows).
 __device__ __forceinline__ void sort_chunk_by_label(const int32_t *__restrict__ labels, int64_t i0, int len, int k,
@@ -206,11 +248,11 @@ __device__ __forceinline__ void sort_chunk_by_label(const int32_t *__restrict__ 
 // and flushes them into a k x d shared accumulator whenever the cluster
 // changes, so every warp gathers the same number of rows whatever the
 // cluster sizes.  Same partials as update_sorted_kernel.
-template <int MAXJ>
+template <int MAXJ, bool PACKED>
 __global__ void __launch_bounds__(1024)
-update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int32_t *__restrict__ labels, int k,
-                       long long *__restrict__ part, unsigned int *__restrict__ cpart, int scale,
-                       const LloydState *st) {
+update_balanced_kernel(const float *__restrict__ x, const uint32_t *__restrict__ xq, int64_t n, int d,
+                       const int32_t *__restrict__ labels, int k, long long *__restrict__ part,
+                       unsigned int *__restrict__ cpart, int scale, const LloydState *st) {
   if (st && st->done) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   unsigned long long *acc = reinterpret_cast<unsigned long long *>(smraw);  // k x d
@@ -227,7 +269,7 @@ update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int3
   for (int t = threadIdx.x; t < k; t += blockDim.x) cpart[(size_t)blockIdx.x * k + t] = (unsigned int)cnt[t];
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  constexpr int kRows = 16 / MAXJ;  // rows in flight per warp
+  constexpr int kRows = (PACKED && MAXJ == 1) ? 12 : 16 / MAXJ;  // rows in flight per warp
   const FixedConv fc = fixed_conv(scale);
   const int seg = (len + nw - 1) / nw;
   const int s_begin = min(len, w * seg), s_end = min(len, s_begin + seg);
@@ -242,15 +284,21 @@ update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int3
 #pragma unroll
     for (int q = 0; q < MAXJ; ++q) a[q] = 0;
     for (int s = s_begin; s < s_end; s += kRows) {
-      float v[kRows][MAXJ];
+      using E = typename std::conditional<PACKED, uint32_t, float>::type;
+      E v[kRows][MAXJ];
+      int rt[kRows];  // chunk-relative rows
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         const bool ok = s + r < s_end;
-        const float *xr = x + (i0 + (ok ? idx[s + r] : 0)) * (int64_t)d;
+        rt[r] = ok ? idx[s + r] : 0;
+        const int64_t ro = (i0 + rt[r]) * (int64_t)d;
 #pragma unroll
         for (int q = 0; q < MAXJ; ++q) {
           const int j = lane + 32 * q;
-          v[r][q] = (ok && j < d) ? __ldg(xr + j) : 0.f;
+          if constexpr (PACKED)
+            v[r][q] = (ok && j < d) ? __ldg(xq + ro + j) : 0u;
+          else
+            v[r][q] = (ok && j < d) ? __ldg(x + ro + j) : 0.f;
         }
       }
 #pragma unroll
@@ -267,7 +315,12 @@ update_balanced_kernel(const float *__restrict__ x, int64_t n, int d, const int3
           next = off[c + 1];
         }
 #pragma unroll
-        for (int q = 0; q < MAXJ; ++q) add_fixed64(a[q], v[r][q], fc);
+        for (int q = 0; q < MAXJ; ++q) {
+          if constexpr (PACKED)
+            add_packed64(a[q], v[r][q], x + (i0 + rt[r]) * (int64_t)d + lane + 32 * q, scale);
+          else
+            add_fixed64(a[q], v[r][q], fc);
+        }
       }
     }
 #pragma unroll
@@ -596,6 +649,7 @@ sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double 
 }
 
 void update_free(UpdateBuf *u, cudaStream_t s) {
+  dfree(u->xq, s);
   dfree(u->acc, s);
   dfree(u->cnt, s);
   dfree(u->part, s);
@@ -606,10 +660,21 @@ void update_free(UpdateBuf *u, cudaStream_t s) {
 template <int MAXJ>
 static sc_status launch_balanced(const UpdateBuf *u, const float *x, int64_t n, int d, const int32_t *labels, int k,
                                  const LloydState *st, cudaStream_t s) {
-  auto kern = update_balanced_kernel<MAXJ>;
+  const bool packed = u->xq && u->xq_src == (const void *)x;
+  auto kern = packed ? update_balanced_kernel<MAXJ, true> : update_balanced_kernel<MAXJ, false>;
   SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->balanced_smem));
-  kern<<<u->grid, 1024, u->balanced_smem, s>>>(x, n, d, labels, k, u->part, u->cpart, u->scale, st);
+  kern<<<u->grid, 1024, u->balanced_smem, s>>>(x, u->xq, n, d, labels, k, u->part, u->cpart, u->scale, st);
   SC_LAUNCHED();
+  return SC_OK;
+}
+
+sc_status update_pack(UpdateBuf *u, const float *x, int64_t n, int d, cudaStream_t s) {
+  if (u->mode != 1 || !u->balanced_smem || n == 0) return SC_OK;
+  if (!u->xq) SC_TRY(dalloc(&u->xq, (size_t)n * d, s));
+  const int64_t count = n * d;
+  pack_fixed_kernel<<<(int)std::min<int64_t>((count + 255) / 256, 65536), 256, 0, s>>>(x, count, u->xq, u->scale);
+  SC_LAUNCHED();
+  u->xq_src = x;
   return SC_OK;
 }
 
