@@ -213,6 +213,7 @@ def bench_knn(torch, local, reps=5, n_query=None, with_fp64=True):
                                      f"{KNN_CPU_QUERIES} of {KNN_M} queries against all {KNN_N} rows, single thread"}
     out["config"] = {"n_train": KNN_N, "n_query": KNN_M, "d": KNN_D, "k": KNN_K, "classes": 10, "dtype": "f32"}
     out["find_radius"] = bench_radius(torch, local, xt, xq)
+    out["dbscan"] = bench_dbscan(torch, xt)
     return out
 
 
@@ -251,6 +252,47 @@ def bench_radius(torch, local, xt, xq):
                                      f"{RADIUS_CPU_QUERIES} queries against all {KNN_N} rows, single thread"}
     out["config"] = {"radius": KNN_RADIUS, "n_train": KNN_N, "n_query": len(xq), "d": KNN_D,
                      "e2e": "host queries in, host rows out, both passes"}
+    return out
+
+
+DBSCAN_EPS = 8.0
+DBSCAN_MIN_SAMPLES = 10
+DBSCAN_SAMPLE = 20_000
+
+
+def bench_dbscan(torch, xt):
+    """DBSCAN::fit on the kNN training rows (eps 8.0, min_samples 10): points/s
+    of the split form with host input (every neighbourhood on the device, the
+    reference's expansion loop on the host), and on the first 20,000 rows both
+    forms and the reference's CPU algorithm (its own find_radius calls),
+    whose labels must agree; the CPU rate is scaled by 20,000 / n because each
+    neighbourhood query scans all n rows."""
+    import oracle
+    from smartcore_gb300 import _lib
+    from smartcore_gb300.cluster import DBSCAN, DBSCANParameters
+    par = lambda form: DBSCANParameters(form=form).with_eps(DBSCAN_EPS).with_min_samples(DBSCAN_MIN_SAMPLES)
+    DBSCAN.fit(xt[:4096], par(_lib.FORM_SPLIT_BF16))  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m = DBSCAN.fit(xt, par(_lib.FORM_SPLIT_BF16))
+    dt = time.perf_counter() - t0
+    out = {"split_bf16": {"points_per_s": len(xt) / dt, "ms": 1e3 * dt, "clusters": m.num_classes,
+                          "noise": int((m.cluster_labels < 0).sum())}}
+    sub = np.ascontiguousarray(xt[:DBSCAN_SAMPLE])
+    ms = DBSCAN.fit(sub, par(_lib.FORM_SPLIT_BF16))
+    mf = DBSCAN.fit(sub, par(_lib.FORM_FP64))
+    t0 = time.perf_counter()
+    y, k = oracle.dbscan_fit(sub, DBSCAN_EPS, DBSCAN_MIN_SAMPLES)
+    cpu_s = time.perf_counter() - t0
+    out["sample_forms_equal"] = bool(np.array_equal(ms.cluster_labels, mf.cluster_labels))
+    out["sample_oracle_equal"] = bool(np.array_equal(ms.cluster_labels, y) and ms.num_classes == k)
+    out["cpu_baseline"] = {"value": DBSCAN_SAMPLE / cpu_s * (DBSCAN_SAMPLE / len(xt)), "unit": "points/s",
+                           "cores": 1, "kind": "port",
+                           "sample": f"C restatement of DBSCAN::fit with LinearKNNSearch on the first "
+                                     f"{DBSCAN_SAMPLE} rows ({cpu_s:.1f} s), rate scaled by "
+                                     f"{DBSCAN_SAMPLE}/{len(xt)}, single thread"}
+    out["config"] = {"eps": DBSCAN_EPS, "min_samples": DBSCAN_MIN_SAMPLES, "n": len(xt), "d": KNN_D,
+                     "e2e": "host rows in, host labels out"}
     return out
 
 

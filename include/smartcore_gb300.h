@@ -214,6 +214,23 @@ sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout,
                              int32_t form, int64_t *counts_out, int64_t capacity,
                              int64_t *idx_out, double *dist_out,
                              int64_t *total_out);
+/* DBSCAN::fit (src/cluster/dbscan.rs:274-366) over the handle's training
+ * rows with the linear search: every row's find_radius(eps) neighbourhood on
+ * the device, then the reference's expansion loop on the host in its own visit
+ * order.  labels_out (host, n): the cluster index of each row, or -1 for
+ * noise; n_clusters_out (may be NULL): the number of clusters.
+ * SC_ERR_INVALID with "Invalid minPts" (min_samples < 1) or "Invalid radius: "
+ * (eps <= 0), the reference's messages. */
+sc_status sc_dbscan_fit(sc_knn *h, double eps, int64_t min_samples, int32_t form,
+                        int64_t *labels_out, int64_t *n_clusters_out);
+/* DBSCAN::predict (dbscan.rs:370-398) for m query rows against the handle's
+ * training rows labelled by sc_dbscan_fit: the cluster with the most
+ * neighbours within eps (first maximum; noise counted last), as cluster + 1,
+ * or 0 when noise wins.  out: host, m. */
+sc_status sc_dbscan_predict(sc_knn *h, const void *queries, int32_t layout,
+                            int32_t mem, int64_t m, int64_t ld, double eps,
+                            int32_t form, const int64_t *train_labels,
+                            int64_t n_clusters, int64_t *out);
 /* KNNClassifier / KNNRegressor aggregation on the device over a find()
  * result already in idx/dist (device memory of this handle, m x k):
  * y_class = class index per training row (KNNClassifier::fit,

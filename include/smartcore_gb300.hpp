@@ -364,4 +364,57 @@ class KNNRegressor {
   std::shared_ptr<LinearKNNSearch<TX>> knn_;
 };
 
+// DBSCANParameters (src/cluster/dbscan.rs:79-96, defaults :239-249); the
+// device always searches linearly (neighbourhoods in index order).
+struct DBSCANParameters {
+  size_t min_samples = 5;
+  double eps = 0.5;
+  Form form = Form::SplitBF16;
+  DBSCANParameters &with_min_samples(size_t v) { min_samples = v; return *this; }
+  DBSCANParameters &with_eps(double v) { eps = v; return *this; }
+};
+
+// DBSCAN::fit / predict (src/cluster/dbscan.rs:274-398).
+template <typename T>
+class DBSCAN {
+ public:
+  static DBSCAN fit(const DenseMatrix<T> &x, const DBSCANParameters &p = DBSCANParameters()) {
+    if (p.min_samples < 1) throw Failed::fit("Invalid minPts");
+    if (!(p.eps > 0)) throw Failed::fit("Invalid radius: ");
+    DBSCAN m(x, p);
+    const size_t n = m.search_->len();
+    m.labels_.assign(n ? n : 1, 0);
+    int64_t k = 0;
+    detail::check(sc_dbscan_fit(m.search_->handle(), p.eps, (int64_t)p.min_samples, (int32_t)p.form,
+                                m.labels_.data(), &k),
+                  FailedError::FitFailed);
+    m.labels_.resize(n);
+    m.k_ = k;
+    return m;
+  }
+
+  // cluster + 1 per row, 0 for noise
+  std::vector<int64_t> predict(const DenseMatrix<T> &x) const {
+    const auto [m, d] = x.shape();
+    std::vector<int64_t> out(m ? m : 1);
+    detail::check(sc_dbscan_predict(search_->handle(), x.data(), x.layout(), SC_MEM_HOST, (int64_t)m, x.ld(),
+                                    eps_, (int32_t)form_, labels_.data(), k_, out.data()),
+                  FailedError::PredictFailed);
+    out.resize(m);
+    return out;
+  }
+
+  const std::vector<int64_t> &cluster_labels() const { return labels_; }
+  size_t num_classes() const { return (size_t)k_; }
+
+ private:
+  DBSCAN(const DenseMatrix<T> &x, const DBSCANParameters &p)
+      : search_(std::make_shared<LinearKNNSearch<T>>(x, p.form)), eps_(p.eps), form_(p.form) {}
+  std::shared_ptr<LinearKNNSearch<T>> search_;
+  std::vector<int64_t> labels_;
+  int64_t k_ = 0;
+  double eps_;
+  Form form_;
+};
+
 }  // namespace smartcore

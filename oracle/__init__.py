@@ -67,6 +67,9 @@ def lib():
             L.orc_knn_find.restype = I
             L.orc_knn_find_radius.argtypes = [I, P, I64, I64, P, I64, D, P, P, P, I64]
             L.orc_knn_find_radius.restype = I64
+            L.orc_dbscan_fit.argtypes = [I, P, I64, I64, D, I64, P]
+            L.orc_dbscan_fit.restype = I64
+            L.orc_dbscan_predict.argtypes = [I, P, I64, I64, P, I64, P, I64, D, P]
             L.orc_knn_vote.argtypes = [P, P, I64, I64, P, I64, I, P]
             L.orc_knn_regress.argtypes = [P, P, I64, I64, P, I, P]
             L.orc_last_error.restype = C.c_char_p
@@ -225,6 +228,35 @@ def knn_find_radius(train, queries, radius, cap=None):
     if tot == -1:
         raise ValueError("Find failed: radius should be > 0")
     return counts, idx[:tot], dist[:tot]
+
+
+def dbscan_fit(x, eps, min_samples):
+    """DBSCAN::fit with the linear search: (cluster labels with -1 for noise, number of clusters)."""
+    x = np.ascontiguousarray(x)
+    if x.dtype not in (np.float32, np.float64):
+        x = x.astype(np.float64)
+    dt = F32 if x.dtype == np.float32 else F64
+    n, d = x.shape
+    y = np.zeros(n, np.int64)
+    k = lib().orc_dbscan_fit(dt, _ptr(x), n, d, float(eps), int(min_samples), _ptr(y))
+    if k == -1:
+        raise ValueError("Fit failed: Invalid minPts")
+    if k == -2:
+        raise ValueError("Fit failed: Invalid radius: ")
+    return y, int(k)
+
+
+def dbscan_predict(x, y, k, queries, eps):
+    x = np.ascontiguousarray(x)
+    if x.dtype not in (np.float32, np.float64):
+        x = x.astype(np.float64)
+    queries = np.ascontiguousarray(queries, dtype=x.dtype)
+    dt = F32 if x.dtype == np.float32 else F64
+    n, d = x.shape
+    out = np.zeros(queries.shape[0], np.int64)
+    lib().orc_dbscan_predict(dt, _ptr(x), n, d, _ptr(np.ascontiguousarray(y, np.int64)), int(k),
+                             _ptr(queries), queries.shape[0], float(eps), _ptr(out))
+    return out
 
 
 def knn_vote(idx, dist, y_index, n_classes, weight=0):

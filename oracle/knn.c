@@ -1,7 +1,8 @@
 /*
  * Oracle restatement of smartcore's brute-force kNN path: HeapSelection,
- * LinearKNNSearch::find / find_radius and the classifier / regressor
- * aggregation.  TEST INFRASTRUCTURE ONLY (see oracle.h).
+ * LinearKNNSearch::find / find_radius, the classifier / regressor
+ * aggregation, and DBSCAN over find_radius.  TEST INFRASTRUCTURE ONLY (see
+ * oracle.h).
  */
 #include "oracle.h"
 
@@ -196,4 +197,89 @@ void orc_knn_regress(const int64_t *idx, const double *dist, int64_t m,
     out[q] = r;
   }
   free(w); free(pos);
+}
+
+/* find_radius of row `from` as a growing index list (linear_search.rs:89-108) */
+static int64_t radius_list(int dtype, const void *x, int64_t n, int64_t d, const void *from, double eps,
+                           int64_t **buf, int64_t *cap) {
+  int64_t c = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (dist_row(dtype, from, row_at(dtype, x, i, d), d) <= eps) {
+      if (c == *cap) {
+        *cap = *cap ? 2 * *cap : 64;
+        *buf = realloc(*buf, (size_t)*cap * sizeof(int64_t));
+      }
+      (*buf)[c++] = i;
+    }
+  }
+  return c;
+}
+
+/* DBSCAN::fit (src/cluster/dbscan.rs:274-366) with LinearKNNSearch: y[i] is
+ * the cluster of row i or -1 (outlier).  Returns the number of clusters, -1
+ * for min_samples < 1 ("Invalid minPts"), -2 for eps <= 0 ("Invalid radius").
+ * find_radius is called exactly where the reference calls it. */
+int64_t orc_dbscan_fit(int dtype, const void *x, int64_t n, int64_t d, double eps, int64_t min_samples,
+                       int64_t *y) {
+  if (min_samples < 1) return -1;
+  if (!(eps > 0.0)) return -2;
+  const int64_t queued = -2, outlier = -1, undefined = -3;
+  for (int64_t i = 0; i < n; ++i) y[i] = undefined;
+  int64_t *nb = NULL, *sec = NULL, nb_cap = 0, sec_cap = 0;
+  int64_t k = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (y[i] != undefined) continue;
+    int64_t len = radius_list(dtype, x, n, d, row_at(dtype, x, i, d), eps, &nb, &nb_cap);
+    if (len < min_samples) {
+      y[i] = outlier;
+      continue;
+    }
+    y[i] = k;
+    for (int64_t j = 0; j < len; ++j)
+      if (y[nb[j]] == undefined) y[nb[j]] = queued;
+    while (len > 0) { /* neighbors.pop(): last element first */
+      const int64_t index = nb[--len];
+      if (y[index] == outlier) y[index] = k;
+      if (y[index] == undefined || y[index] == queued) {
+        y[index] = k;
+        const int64_t ns = radius_list(dtype, x, n, d, row_at(dtype, x, index, d), eps, &sec, &sec_cap);
+        if (ns >= min_samples) {
+          for (int64_t j = 0; j < ns; ++j) {
+            const int64_t label = y[sec[j]];
+            if (label == undefined) y[sec[j]] = queued;
+            if (label == undefined || label == outlier) {
+              if (len == nb_cap) {
+                nb_cap = nb_cap ? 2 * nb_cap : 64;
+                nb = realloc(nb, (size_t)nb_cap * sizeof(int64_t));
+              }
+              nb[len++] = sec[j];
+            }
+          }
+        }
+      }
+    }
+    ++k;
+  }
+  free(nb);
+  free(sec);
+  return k;
+}
+
+/* DBSCAN::predict (dbscan.rs:370-398): per query, votes over the training
+ * rows within eps (noise last); which_max keeps the first maximum
+ * (src/tree/decision_tree_classifier.rs:490-502); class + 1, or 0 for noise. */
+void orc_dbscan_predict(int dtype, const void *x, int64_t n, int64_t d, const int64_t *y, int64_t k,
+                        const void *q, int64_t m, double eps, int64_t *out) {
+  int64_t *votes = malloc((size_t)(k + 1) * sizeof(int64_t));
+  for (int64_t r = 0; r < m; ++r) {
+    const void *from = row_at(dtype, q, r, d);
+    for (int64_t c = 0; c <= k; ++c) votes[c] = 0;
+    for (int64_t i = 0; i < n; ++i)
+      if (dist_row(dtype, from, row_at(dtype, x, i, d), d) <= eps) ++votes[y[i] < 0 ? k : y[i]];
+    int64_t which = 0;
+    for (int64_t c = 1; c <= k; ++c)
+      if (votes[c] > votes[which]) which = c;
+    out[r] = which != k ? which + 1 : 0;
+  }
+  free(votes);
 }

@@ -104,6 +104,10 @@ int64_t orc_knn_find_radius(int dtype, const void *train, int64_t n, int64_t d,
 /* KNNClassifier::predict_for_row (src/neighbors/knn_classifier.rs:279-299)
  * over find() output.  y = class index per train row (fit, :229-235);
  * weight 0 = Uniform, 1 = Distance (src/neighbors/mod.rs:62-78). */
+int64_t orc_dbscan_fit(int dtype, const void *x, int64_t n, int64_t d, double eps, int64_t min_samples,
+                       int64_t *y);
+void orc_dbscan_predict(int dtype, const void *x, int64_t n, int64_t d, const int64_t *y, int64_t k,
+                        const void *q, int64_t m, double eps, int64_t *out);
 void orc_knn_vote(const int64_t *idx, const double *dist, int64_t m, int64_t k,
                   const int64_t *y, int64_t n_classes, int weight,
                   int64_t *class_out);

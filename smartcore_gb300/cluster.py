@@ -187,3 +187,65 @@ class KMeansHandle:
             self.close()
         except Exception:
             pass
+
+
+@dataclass
+class DBSCANParameters:
+    """DBSCANParameters (src/cluster/dbscan.rs:79-96, defaults :239-249).
+
+    `algorithm` keeps the reference's default (CoverTree); the device always
+    searches linearly, whose neighbourhoods come in index order.  The cluster
+    of a point that borders two clusters can depend on that order."""
+    min_samples: int = 5
+    eps: float = 0.5
+    algorithm: "object" = None
+    form: int = _lib.FORM_SPLIT_BF16
+
+    def with_min_samples(self, v):
+        self.min_samples = v
+        return self
+
+    def with_eps(self, v):
+        self.eps = v
+        return self
+
+    def with_algorithm(self, v):
+        self.algorithm = v
+        return self
+
+
+class DBSCAN:
+    """DBSCAN::fit / predict (src/cluster/dbscan.rs:274-398) on the device."""
+
+    def __init__(self, search, cluster_labels, num_classes, eps, form):
+        self._search = search
+        self.cluster_labels = cluster_labels
+        self.num_classes = num_classes
+        self.eps = eps
+        self.form = form
+
+    @staticmethod
+    def fit(x, parameters: DBSCANParameters = None) -> "DBSCAN":
+        from .neighbors import LinearKNNSearch
+        p = parameters or DBSCANParameters()
+        if p.min_samples < 1:
+            raise Failed(FailedError.FitFailed, "Invalid minPts")
+        if not p.eps > 0:
+            raise Failed(FailedError.FitFailed, "Invalid radius: ")
+        search = LinearKNNSearch(x, form=p.form)
+        labels = np.zeros(search.n, np.int64)
+        k = np.zeros(1, np.int64)
+        _lib.check(search._L.sc_dbscan_fit(search.h, float(p.eps), int(p.min_samples), p.form,
+                                           _lib.ptr(labels), _lib.ptr(k)))
+        return DBSCAN(search, labels, int(k[0]), float(p.eps), p.form)
+
+    def predict(self, x) -> np.ndarray:
+        s = self._search
+        a = s._q(x)
+        m = a.shape[0]
+        lay, ld = layout_of(a)
+        out = np.zeros(m, np.int64)
+        _lib.check(s._L.sc_dbscan_predict(s.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, self.eps, self.form,
+                                          _lib.ptr(self.cluster_labels), self.num_classes, _lib.ptr(out)),
+                   FailedError.PredictFailed)
+        return out

@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <vector>
@@ -608,6 +609,151 @@ sc_status sc_knn_find(sc_knn *h, const void *queries, int32_t layout, int32_t me
     if (dist_out) SC_CUDA(cudaMemcpyAsync(dist_out, h->dist, (size_t)(m * k) * sizeof(double), kind, h->stream));
   }
   SC_CUDA(cudaStreamSynchronize(h->stream));
+  return SC_OK;
+}
+
+}  // extern "C"
+
+// Rows of the handle's training set within `radius` of each of m device
+// query rows (row-major), in index order: CSR lists off (m + 1) and idx.
+static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double radius, int32_t form,
+                              std::vector<int64_t> &off, std::vector<int64_t> &idx) {
+  off.assign((size_t)m + 1, 0);
+  idx.clear();
+  if (m == 0) return SC_OK;
+  int64_t *dcnt = nullptr, *doff = nullptr, *didx = nullptr;
+  double *ddist = nullptr;
+  sc_status r = SC_OK;
+  do {
+    if ((r = dalloc(&dcnt, (size_t)m, h->stream)) != SC_OK || (r = dalloc(&doff, (size_t)m, h->stream)) != SC_OK) break;
+    r = form == SC_FORM_FP64
+            ? launch_knn_radius_fp64(h->dtype, h->train, h->n, (int)h->d, q_dev, m, radius, dcnt, nullptr, nullptr,
+                                     nullptr, h->stream)
+            : split_knn_radius(&h->split, h->dtype, h->train, h->n, (int)h->d, q_dev, m, radius, dcnt, nullptr,
+                               nullptr, nullptr, h->stream);
+    if (r != SC_OK) break;
+    if (cudaMemcpyAsync(off.data() + 1, dcnt, (size_t)m * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "radius counts");
+      break;
+    }
+    for (int64_t q = 0; q < m; ++q) off[(size_t)q + 1] += off[(size_t)q];
+    const int64_t total = off[(size_t)m];
+    if (total == 0) break;
+    idx.resize((size_t)total);
+    if ((r = dalloc(&didx, (size_t)total, h->stream)) != SC_OK || (r = dalloc(&ddist, (size_t)total, h->stream)) != SC_OK) break;
+    if (cudaMemcpyAsync(doff, off.data(), (size_t)m * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream) !=
+        cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "radius offsets");
+      break;
+    }
+    r = form == SC_FORM_FP64
+            ? launch_knn_radius_fp64(h->dtype, h->train, h->n, (int)h->d, q_dev, m, radius, nullptr, doff, didx,
+                                     ddist, h->stream)
+            : split_knn_radius(&h->split, h->dtype, h->train, h->n, (int)h->d, q_dev, m, radius, nullptr, doff,
+                               didx, ddist, h->stream);
+    if (r != SC_OK) break;
+    if (cudaMemcpyAsync(idx.data(), didx, (size_t)total * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "radius lists");
+      break;
+    }
+  } while (0);
+  cudaStreamSynchronize(h->stream);
+  dfree(dcnt, h->stream); dfree(doff, h->stream); dfree(didx, h->stream); dfree(ddist, h->stream);
+  return r;
+}
+
+// The expansion loop of DBSCAN::fit (src/cluster/dbscan.rs:299-360) over
+// precomputed neighbourhoods (each find_radius result is fixed by its query
+// row, so computing all of them first changes nothing): the same marks
+// (undefined -3, queued -2, outlier -1), the same LIFO stack of neighbours and
+// the same order of visits.  Returns the number of clusters.
+static int64_t dbscan_expand(int64_t n, const std::vector<int64_t> &off, const std::vector<int64_t> &idx,
+                             int64_t min_samples, int64_t *y) {
+  const int64_t queued = -2, outlier = -1, undefined = -3;
+  for (int64_t i = 0; i < n; ++i) y[i] = undefined;
+  int64_t k = 0;
+  std::vector<int64_t> stack;
+  for (int64_t i = 0; i < n; ++i) {
+    if (y[i] != undefined) continue;
+    const int64_t *nb = idx.data() + off[(size_t)i];
+    const int64_t nn = off[(size_t)i + 1] - off[(size_t)i];
+    if (nn < min_samples) {
+      y[i] = outlier;
+      continue;
+    }
+    y[i] = k;
+    for (int64_t j = 0; j < nn; ++j)
+      if (y[nb[j]] == undefined) y[nb[j]] = queued;
+    stack.assign(nb, nb + nn);
+    while (!stack.empty()) {
+      const int64_t index = stack.back();
+      stack.pop_back();
+      if (y[index] == outlier) y[index] = k;
+      if (y[index] == undefined || y[index] == queued) {
+        y[index] = k;
+        const int64_t *sec = idx.data() + off[(size_t)index];
+        const int64_t ns = off[(size_t)index + 1] - off[(size_t)index];
+        if (ns >= min_samples) {
+          for (int64_t j = 0; j < ns; ++j) {
+            const int64_t label = y[sec[j]];
+            if (label == undefined) y[sec[j]] = queued;
+            if (label == undefined || label == outlier) stack.push_back(sec[j]);
+          }
+        }
+      }
+    }
+    ++k;
+  }
+  return k;
+}
+
+extern "C" {
+
+sc_status sc_dbscan_fit(sc_knn *h, double eps, int64_t min_samples, int32_t form, int64_t *labels_out,
+                        int64_t *n_clusters_out) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (min_samples < 1) { set_error("Invalid minPts"); return SC_ERR_INVALID; }  // dbscan.rs:278-280
+  if (!(eps > 0.0)) { set_error("Invalid radius: "); return SC_ERR_INVALID; }   // dbscan.rs:282-284
+  if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
+  if (!labels_out && h->n > 0) { set_error("null labels"); return SC_ERR_INVALID; }
+  std::vector<int64_t> off, idx;
+  SC_TRY(radius_lists(h, h->train, h->n, eps, form, off, idx));  // every row's neighbourhood
+  const int64_t k = dbscan_expand(h->n, off, idx, min_samples, labels_out);
+  if (n_clusters_out) *n_clusters_out = k;
+  return SC_OK;
+}
+
+sc_status sc_dbscan_predict(sc_knn *h, const void *queries, int32_t layout, int32_t mem, int64_t m, int64_t ld,
+                            double eps, int32_t form, const int64_t *train_labels, int64_t n_clusters,
+                            int64_t *out) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (!(eps > 0.0)) { set_error("radius should be > 0"); return SC_ERR_INVALID; }  // linear_search.rs:90-95
+  SC_TRY(check_matrix(queries, h->dtype, layout, mem, m, h->d, ld));
+  if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
+  if (n_clusters < 0 || (!train_labels && h->n > 0) || (!out && m > 0)) { set_error("invalid labels"); return SC_ERR_INVALID; }
+  if (m == 0) return SC_OK;
+  SC_TRY(knn_reserve(h, m, 1));
+  SC_TRY(upload_matrix(queries, h->dtype, layout, mem, m, h->d, ld, h->q, h->stream));
+  std::vector<int64_t> off, idx;
+  SC_TRY(radius_lists(h, h->q, m, eps, form, off, idx));
+  // dbscan.rs:378-397: votes per cluster, noise counted last; the first
+  // maximum wins (which_max, src/tree/decision_tree_classifier.rs:490-502)
+  std::vector<int64_t> votes((size_t)n_clusters + 1);
+  for (int64_t q = 0; q < m; ++q) {
+    std::fill(votes.begin(), votes.end(), 0);
+    for (int64_t e = off[(size_t)q]; e < off[(size_t)q + 1]; ++e) {
+      const int64_t yi = train_labels[idx[(size_t)e]];
+      ++votes[yi < 0 ? (size_t)n_clusters : (size_t)yi];
+    }
+    size_t which = 0;
+    for (size_t c = 1; c < votes.size(); ++c)
+      if (votes[c] > votes[which]) which = c;
+    out[q] = which != (size_t)n_clusters ? (int64_t)which + 1 : 0;
+  }
   return SC_OK;
 }
 

@@ -124,6 +124,17 @@ static void knn_regressor(Form form) {
   for (size_t i = 0; i < yu.size(); ++i) CHECK(std::abs(yu[i] - kats::reg_u_expect[i]) < 1e-7);
 }
 
+static void dbscan(Form form) {
+  // dbscan.rs:427-461 (fit_predict_dbscan)
+  const auto x = DenseMatrix<double>::from_2d_array(kats::dbscan_x);
+  DBSCANParameters p;
+  p.form = form;
+  const auto m = DBSCAN<double>::fit(x, p.with_eps(kats::dbscan_eps).with_min_samples(kats::dbscan_min_samples));
+  const auto y = m.predict(x);
+  CHECK(y.size() == kats::dbscan_expect.size());
+  for (size_t i = 0; i < y.size(); ++i) CHECK(y[i] == kats::dbscan_expect[i]);
+}
+
 int main(int argc, char **argv) {
   const bool cpu_only = argc > 1 && std::strcmp(argv[1], "--cpu-only") == 0;
   invalid_k();
@@ -133,6 +144,7 @@ int main(int argc, char **argv) {
       knn_find(f);
       knn_classifier(f);
       knn_regressor(f);
+      dbscan(f);
     }
   }
   std::printf("%s: %d failure(s)\n", cpu_only ? "cpu-only" : "all", failures);

@@ -169,6 +169,17 @@ def main(root):
                      "expect": yexp,
                      "tol": 2.220446049250313e-16 if "EPSILON" in tol else float(tol)}
 
+    src = read(root, "src/cluster/dbscan.rs")
+    body = fn_body(src, "fit_predict_dbscan")
+    kats["dbscan_fit_predict"] = {
+        "cite": "src/cluster/dbscan.rs:427-461",
+        "x": rows(body[body.index("from_2d_array"):body.index(".unwrap()")]),
+        "eps": float(re.search(r"with_eps\(([0-9.]+)\)", body).group(1)),
+        "min_samples": int(re.search(r"with_min_samples\((\d+)\)", body).group(1)),
+        "expect": [int(v) for v in re.search(r"let expected_labels = vec!\[(.*?)\];", body).group(1).split(",")],
+        "errors": re.findall(r'Failed::fit\("(Invalid [^"]*)"\)', src),
+    }
+
     out = os.path.join(HERE, "reference_kats.json")
     with open(out, "w") as f:
         json.dump(kats, f, indent=1)

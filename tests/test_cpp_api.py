@@ -46,6 +46,10 @@ def write_kats(path):
         f"static const std::vector<double> reg_y = {_vec(k['knn_regressor_weighted']['y'])};",
         f"static const std::vector<double> reg_w_expect = {_vec(k['knn_regressor_weighted']['expect'])};",
         f"static const std::vector<double> reg_u_expect = {_vec(k['knn_regressor_uniform']['expect'])};",
+        f"static const std::vector<std::vector<double>> dbscan_x = {_vec2(k['dbscan_fit_predict']['x'])};",
+        f"static const double dbscan_eps = {float(k['dbscan_fit_predict']['eps'])!r};",
+        f"static const int dbscan_min_samples = {int(k['dbscan_fit_predict']['min_samples'])};",
+        f"static const std::vector<long> dbscan_expect = {_vec(k['dbscan_fit_predict']['expect'], 'long')};",
         "}",
     ]
     with open(os.path.join(path, "kats.inc"), "w") as f:

@@ -126,3 +126,13 @@ def test_rng_std_straddle():
     # next_u64 across the 64-word block buffer reads the same words as u32 pairs
     many = oracle.rng_u64(40, seed=3, rng=oracle.RNG_STD)
     assert len(set(many.tolist())) == 40
+
+
+def test_dbscan_fit_predict(kats):
+    c = kats["dbscan_fit_predict"]
+    x = np.array(c["x"])
+    y, k = oracle.dbscan_fit(x, c["eps"], c["min_samples"])
+    assert oracle.dbscan_predict(x, y, k, x, c["eps"]).tolist() == c["expect"]
+    for bad, msg in (((c["eps"], 0), c["errors"][0]), ((0.0, 2), c["errors"][1])):
+        with pytest.raises(ValueError, match=msg.strip()):
+            oracle.dbscan_fit(x, *bad)
