@@ -75,6 +75,7 @@ struct UpdateBuf {
   unsigned int *cpart = nullptr;    // mode 1: grid x k
   uint32_t *xq = nullptr;           // mode 1: the points in the packed fixed-point form of `scale`
   const void *xq_src = nullptr;     // the points xq was made from
+  bool xq_slow = false;             // some value of xq needs the conversion from f32
 };
 
 // ---- device memory ----

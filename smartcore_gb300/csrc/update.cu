@@ -183,7 +183,8 @@ __device__ __forceinline__ void add_fixed64(long long &acc, float v, const Fixed
 // converted from the f32 value itself.  +-0 packs to 0.
 constexpr uint32_t kPackSlow = 31u << 25;
 
-__global__ void pack_fixed_kernel(const float *__restrict__ x, int64_t count, uint32_t *__restrict__ xq, int scale) {
+__global__ void pack_fixed_kernel(const float *__restrict__ x, int64_t count, uint32_t *__restrict__ xq, int scale,
+                                  unsigned int *__restrict__ slow) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t b = __float_as_uint(x[i]);
     const int e = (int)((b >> 23) & 0xffu);
@@ -199,15 +200,19 @@ __global__ void pack_fixed_kernel(const float *__restrict__ x, int64_t count, ui
         q = ((uint32_t)sh << 25) | ((uint32_t)((int)b < 0 ? -m : m) & 0x1ffffffu);
       }
     }
+    if (q == kPackSlow) atomicAdd(slow, 1u);
     xq[i] = q;
   }
 }
 
 // The same sum as add_fixed64 from the packed form: one shift pair and one
 // 32 x 32 -> 64-bit multiply-add per value.
+// SLOW = false: the dataset has no value outside the packed form (counted
+// when it was packed), so no value needs the check.
+template <bool SLOW>
 __device__ __forceinline__ void add_packed64(long long &acc, uint32_t q, const float *xe, int scale) {
   const uint32_t sh = q >> 25;
-  if (sh != 31u) {
+  if (!SLOW || sh != 31u) {
     const int sm = ((int)(q << 7)) >> 7;
     asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(acc) : "r"(sm), "r"(1 << sh));
   } else {
@@ -248,7 +253,7 @@ __device__ __forceinline__ void sort_chunk_by_label(const int32_t *__restrict__ 
 // and flushes them into a k x d shared accumulator whenever the cluster
 // changes, so every warp gathers the same number of rows whatever the
 // cluster sizes.  Same partials as update_sorted_kernel.
-template <int MAXJ, bool PACKED>
+template <int MAXJ, bool PACKED, bool SLOW>
 __global__ void __launch_bounds__(1024)
 update_balanced_kernel(const float *__restrict__ x, const uint32_t *__restrict__ xq, int64_t n, int d,
                        const int32_t *__restrict__ labels, int k, long long *__restrict__ part,
@@ -292,13 +297,23 @@ update_balanced_kernel(const float *__restrict__ x, const uint32_t *__restrict__
         const bool ok = s + r < s_end;
         rt[r] = ok ? idx[s + r] : 0;
         const int64_t ro = (i0 + rt[r]) * (int64_t)d;
+        if constexpr (PACKED) {  // lane = features MAXJ * lane ... + MAXJ - 1, one vector load
+          const bool live = ok && lane * MAXJ < d;
+          if constexpr (MAXJ == 4) {
+            const uint4 t = live ? __ldg(reinterpret_cast<const uint4 *>(xq + ro) + lane) : make_uint4(0, 0, 0, 0);
+            v[r][0] = t.x; v[r][1] = t.y; v[r][2] = t.z; v[r][3] = t.w;
+          } else if constexpr (MAXJ == 2) {
+            const uint2 t = live ? __ldg(reinterpret_cast<const uint2 *>(xq + ro) + lane) : make_uint2(0, 0);
+            v[r][0] = t.x; v[r][1] = t.y;
+          } else {
+            v[r][0] = live ? __ldg(xq + ro + lane) : 0u;
+          }
+        } else {
 #pragma unroll
-        for (int q = 0; q < MAXJ; ++q) {
-          const int j = lane + 32 * q;
-          if constexpr (PACKED)
-            v[r][q] = (ok && j < d) ? __ldg(xq + ro + j) : 0u;
-          else
+          for (int q = 0; q < MAXJ; ++q) {
+            const int j = lane + 32 * q;
             v[r][q] = (ok && j < d) ? __ldg(x + ro + j) : 0.f;
+          }
         }
       }
 #pragma unroll
@@ -307,7 +322,7 @@ update_balanced_kernel(const float *__restrict__ x, const uint32_t *__restrict__
         while (s + r >= next) {  // cluster boundary: flush
 #pragma unroll
           for (int q = 0; q < MAXJ; ++q) {
-            const int j = lane + 32 * q;
+            const int j = PACKED ? lane * MAXJ + q : lane + 32 * q;
             if (j < d && a[q] != 0) atomicAdd(acc + c * d + j, (unsigned long long)a[q]);
             a[q] = 0;
           }
@@ -317,7 +332,7 @@ update_balanced_kernel(const float *__restrict__ x, const uint32_t *__restrict__
 #pragma unroll
         for (int q = 0; q < MAXJ; ++q) {
           if constexpr (PACKED)
-            add_packed64(a[q], v[r][q], x + (i0 + rt[r]) * (int64_t)d + lane + 32 * q, scale);
+            add_packed64<SLOW>(a[q], v[r][q], x + (i0 + rt[r]) * (int64_t)d + lane * MAXJ + q, scale);
           else
             add_fixed64(a[q], v[r][q], fc);
         }
@@ -325,7 +340,7 @@ update_balanced_kernel(const float *__restrict__ x, const uint32_t *__restrict__
     }
 #pragma unroll
     for (int q = 0; q < MAXJ; ++q) {
-      const int j = lane + 32 * q;
+      const int j = PACKED ? lane * MAXJ + q : lane + 32 * q;
       if (j < d && a[q] != 0) atomicAdd(acc + c * d + j, (unsigned long long)a[q]);
     }
   }
@@ -660,8 +675,9 @@ void update_free(UpdateBuf *u, cudaStream_t s) {
 template <int MAXJ>
 static sc_status launch_balanced(const UpdateBuf *u, const float *x, int64_t n, int d, const int32_t *labels, int k,
                                  const LloydState *st, cudaStream_t s) {
-  const bool packed = u->xq && u->xq_src == (const void *)x;
-  auto kern = packed ? update_balanced_kernel<MAXJ, true> : update_balanced_kernel<MAXJ, false>;
+  const bool packed = u->xq && u->xq_src == (const void *)x && d % MAXJ == 0;
+  auto kern = !packed ? update_balanced_kernel<MAXJ, false, false>
+              : u->xq_slow ? update_balanced_kernel<MAXJ, true, true> : update_balanced_kernel<MAXJ, true, false>;
   SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->balanced_smem));
   kern<<<u->grid, 1024, u->balanced_smem, s>>>(x, u->xq, n, d, labels, k, u->part, u->cpart, u->scale, st);
   SC_LAUNCHED();
@@ -672,8 +688,17 @@ sc_status update_pack(UpdateBuf *u, const float *x, int64_t n, int d, cudaStream
   if (u->mode != 1 || !u->balanced_smem || n == 0) return SC_OK;
   if (!u->xq) SC_TRY(dalloc(&u->xq, (size_t)n * d, s));
   const int64_t count = n * d;
-  pack_fixed_kernel<<<(int)std::min<int64_t>((count + 255) / 256, 65536), 256, 0, s>>>(x, count, u->xq, u->scale);
+  unsigned int *slow = nullptr;
+  SC_TRY(dalloc(&slow, 1, s));
+  SC_CUDA(cudaMemsetAsync(slow, 0, sizeof(unsigned int), s));
+  pack_fixed_kernel<<<(int)std::min<int64_t>((count + 255) / 256, 65536), 256, 0, s>>>(x, count, u->xq, u->scale,
+                                                                                     slow);
   SC_LAUNCHED();
+  unsigned int hs = 0;
+  SC_CUDA(cudaMemcpyAsync(&hs, slow, sizeof hs, cudaMemcpyDeviceToHost, s));
+  SC_CUDA(cudaStreamSynchronize(s));
+  dfree(slow, s);
+  u->xq_slow = hs != 0;
   u->xq_src = x;
   return SC_OK;
 }

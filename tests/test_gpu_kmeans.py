@@ -206,3 +206,15 @@ def test_throughput_mode_runs_all_iterations():
     h.seed(4, first, u)
     assert h.iterate(17, stop_on_converge=False) == 17
     h.close()
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_values_below_the_sum_grid(form):
+    """f32 points whose features span ~60 binades: the tiny ones fall outside
+    the packed fixed-point form of the centroid sums and take the exact
+    conversion from f32 (subnormals included)."""
+    x, _ = blobs(6000, 8, 5, seed=31, dtype=np.float32)
+    x[:, 3] *= np.float32(1e-18)
+    x[::7, 5] = np.float32(3e-39)  # subnormal
+    x = np.ascontiguousarray(x)
+    assert_fit_parity(x, 5, 20, 6, form)
