@@ -792,7 +792,7 @@ pp_select_kernel(const T *__restrict__ x, int d, const double *__restrict__ dd,
                  const double *__restrict__ part, int64_t n, int nb,
                  const double *__restrict__ uniform, LloydState *st,
                  T *__restrict__ seed_x, float *__restrict__ seed_cc, int j) {
-  constexpr int kScan = 256;  // threads that sum chunks of the partials
+  constexpr int kScan = kSelThreads;  // threads that sum chunks of the partials
   __shared__ double s_incl[kScan];  // inclusive prefix of the chunk sums
   __shared__ double s_wtot[32];
   __shared__ int s_chunk;
