@@ -111,6 +111,35 @@ class KMeans:
                                        _lib.ptr(labels)), FailedError.PredictFailed)
         return labels
 
+    # serde form of the reference's struct (kmeans.rs:71-83, `derive(Serialize,
+    # Deserialize)`): its fields in declaration order, the four PhantomData
+    # fields as unit (null).
+    _SERDE_FIELDS = ("k", "_y", "size", "_distortion", "centroids",
+                     "_phantom_tx", "_phantom_ty", "_phantom_x", "_phantom_y")
+
+    def to_serde(self) -> dict:
+        return {"k": int(self.k), "_y": [int(v) for v in self._y], "size": [int(v) for v in self.size],
+                "_distortion": float(self._distortion),
+                "centroids": [[float(v) for v in row] for row in np.asarray(self.centroids)],
+                "_phantom_tx": None, "_phantom_ty": None, "_phantom_x": None, "_phantom_y": None}
+
+    def to_json(self) -> str:
+        """The model as serde_json writes the reference's KMeans (compact, fields in order)."""
+        import json
+        return json.dumps(self.to_serde(), separators=(",", ":"), allow_nan=False)
+
+    @staticmethod
+    def from_json(text: str, form=_lib.FORM_SPLIT_BF16) -> "KMeans":
+        """A model written by serde_json from the reference's KMeans (or by to_json)."""
+        import json
+        d = json.loads(text)
+        missing = [f for f in KMeans._SERDE_FIELDS if f not in d]
+        if missing:
+            raise ValueError(f"missing field `{missing[0]}`")
+        cent = np.asarray(d["centroids"], np.float64).reshape(len(d["centroids"]), -1)
+        return KMeans(int(d["k"]), np.asarray(d["_y"], np.int64), np.asarray(d["size"], np.int64),
+                      float(d["_distortion"]), cent, 0, form)
+
     def __eq__(self, other):
         """PartialEq of kmeans.rs:85-107: k, size and centroids within f64::EPSILON."""
         if self.k != other.k or not np.array_equal(self.size, other.size):

@@ -218,3 +218,17 @@ def test_values_below_the_sum_grid(form):
     x[::7, 5] = np.float32(3e-39)  # subnormal
     x = np.ascontiguousarray(x)
     assert_fit_parity(x, 5, 20, 6, form)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_serde_round_trip(kats, form):
+    """kmeans.rs:512-546: a fitted model survives serialisation unchanged
+    (PartialEq), in the reference's serde layout."""
+    import json
+    x = np.array(kats["kmeans_fit_predict"]["x"], np.float32)
+    km = KMeans.fit(x, KMeansParameters(k=2, max_iter=100, seed=3, form=form))
+    text = km.to_json()
+    assert list(json.loads(text).keys()) == list(KMeans._SERDE_FIELDS)
+    back = KMeans.from_json(text, form=form)
+    assert back == km
+    assert np.array_equal(back.predict(x), km.predict(x))
