@@ -255,6 +255,48 @@ def bench_radius(torch, local, xt, xq):
     return out
 
 
+MANY_PROBLEMS = 512
+MANY_MAX_ITER = 30
+MANY_CPU_SAMPLE = 4
+
+
+def bench_many_problems(torch):
+    """512 independent k-means problems (n log-uniform in [1e3, 1e5], d in
+    {8, 16, 32, 64}, k in [4, 64], max_iter 30), each through KMeans.fit with
+    host input and output, one after another: problem-iterations per second of
+    the whole batch.  On the first four problems the same fits run through the
+    reference's CPU algorithm (BBD tree), whose labels must agree."""
+    import oracle
+    from smartcore_gb300 import _lib
+    from smartcore_gb300.cluster import KMeans, KMeansParameters
+    from smartcore_gb300.synthetic import batched_problems
+    probs = batched_problems(count=MANY_PROBLEMS)
+    par = lambda k, seed: KMeansParameters(k=k, max_iter=MANY_MAX_ITER, seed=seed, form=_lib.FORM_SPLIT_BF16)
+    KMeans.fit(probs[0][0], par(probs[0][1], probs[0][2]))  # warm-up
+    torch.cuda.synchronize()
+    iters, fits, t0 = 0, [], time.perf_counter()
+    for x, k, seed in probs:
+        km = KMeans.fit(x, par(k, seed))
+        iters += km.iters
+        fits.append(km)
+    dt = time.perf_counter() - t0
+    sample_iters, cpu_s, labels_equal = 0, 0.0, True
+    for (x, k, seed), km in zip(probs[:MANY_CPU_SAMPLE], fits):
+        t1 = time.perf_counter()
+        ref = oracle.kmeans_fit(x, k, MANY_MAX_ITER, seed=seed)
+        cpu_s += time.perf_counter() - t1
+        sample_iters += ref.iters
+        labels_equal &= bool(np.array_equal(km._y, ref.labels))
+    return {"problem_iters_per_s": iters / dt, "problems": len(probs), "iterations": iters, "ms": 1e3 * dt,
+            "points": int(sum(len(p[0]) for p in probs)), "sample_labels_equal": labels_equal,
+            "cpu_baseline": {"value": sample_iters / cpu_s, "unit": "problem-iterations/s", "cores": 1,
+                             "kind": "port",
+                             "sample": f"C restatement of KMeans::fit (k-means++ and BBD-tree Lloyd) on the "
+                                       f"first {MANY_CPU_SAMPLE} problems, single thread"},
+            "config": {"n": "log-uniform [1e3, 1e5]", "d": [8, 16, 32, 64], "k": "[4, 64]",
+                       "max_iter": MANY_MAX_ITER, "e2e": "KMeans.fit per problem, host data in and out"}}
+
+
 DBSCAN_EPS = 8.0
 DBSCAN_MIN_SAMPLES = 10
 DBSCAN_SAMPLE = 20_000
@@ -453,6 +495,7 @@ def run_ours(args):
                 traffic = float(line.split(":", 1)[1])
 
     knn = bench_knn(torch, local) if not args.no_knn else None
+    many = bench_many_problems(torch) if not args.no_knn else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -479,6 +522,7 @@ def run_ours(args):
         "parity_vs_fp64_form": agree,
         "rescored_points": int(rescored),
         "knn": knn,
+        "many_problems": many,
     }
     print(json.dumps(line), flush=True)
     h.close()
