@@ -472,13 +472,14 @@ def run_ours(args):
     e2e_steps = max(1, min(3, args.steps))
     e2e_iters, e2e_time = 0, 0.0
     xh = x_pinned.numpy()
-    for s in range(e2e_steps + 1):
+    e2e_warm = 2  # the first fits grow the device memory pool and the pinned staging buffer
+    for s in range(e2e_steps + e2e_warm):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         km = KMeans.fit(xh, KMeansParameters(k=K_CLUSTERS, max_iter=MAX_ITER, seed=SEED_KMEANS,
                                              form=_lib.FORM_SPLIT_BF16))
         dt = time.perf_counter() - t0
-        if s > 0:  # first call warms the allocator and the module
+        if s >= e2e_warm:
             e2e_iters += km.iters
             e2e_time += dt
     h2d = N * D * 4 + 8 * K_CLUSTERS
