@@ -214,6 +214,7 @@ def bench_knn(torch, local, reps=5, n_query=None, with_fp64=True):
     out["config"] = {"n_train": KNN_N, "n_query": KNN_M, "d": KNN_D, "k": KNN_K, "classes": 10, "dtype": "f32"}
     out["find_radius"] = bench_radius(torch, local, xt, xq)
     out["dbscan"] = bench_dbscan(torch, xt)
+    out["fastpair"] = bench_fastpair(torch, xt)
     return out
 
 
@@ -253,6 +254,37 @@ def bench_radius(torch, local, xt, xq):
     out["config"] = {"radius": KNN_RADIUS, "n_train": KNN_N, "n_query": len(xq), "d": KNN_D,
                      "e2e": "host queries in, host rows out, both passes"}
     return out
+
+
+FASTPAIR_N = 20_000
+
+
+def bench_fastpair(torch, xt):
+    """FastPair::new + closest_pair on the first 20,000 kNN training rows:
+    rows/s on the device (every row's nearest later row, exact reference
+    distances) and the reference's CPU algorithm on the same rows, whose
+    entries must agree."""
+    import oracle
+    from smartcore_gb300.neighbors import FastPair
+    x = np.ascontiguousarray(xt[:FASTPAIR_N])
+    FastPair(x[:1024])  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fp = FastPair(x)
+    dt = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    nb, dist, closest = oracle.fastpair(x)
+    cpu_s = time.perf_counter() - t0
+    c = fp.closest_pair()
+    equal = bool([fp.distances[i].neighbour for i in range(len(x))] == nb.tolist() and
+                 np.array_equal(np.array([fp.distances[i].distance for i in range(len(x))]), dist) and
+                 (c.node, c.neighbour, c.distance) == closest)
+    return {"rows_per_s": len(x) / dt, "ms": 1e3 * dt, "closest_pair": [c.node, c.neighbour, c.distance],
+            "oracle_equal": equal,
+            "cpu_baseline": {"value": len(x) / cpu_s, "unit": "rows/s", "cores": 1, "kind": "port",
+                             "sample": f"C restatement of FastPair::init on the same {len(x)} rows "
+                                       f"({cpu_s:.1f} s), single thread"},
+            "config": {"n": len(x), "d": KNN_D, "e2e": "host rows in, host map out"}}
 
 
 MANY_PROBLEMS = 512

@@ -231,6 +231,15 @@ sc_status sc_dbscan_predict(sc_knn *h, const void *queries, int32_t layout,
                             int32_t mem, int64_t m, int64_t ld, double eps,
                             int32_t form, const int64_t *train_labels,
                             int64_t n_clusters, int64_t *out);
+/* FastPair::new / closest_pair (src/algorithm/neighbour/fastpair.rs:59-182)
+ * over the handle's training rows: neighbour_out[i] / distance_out[i] (host,
+ * n, may be NULL) are the entry `distances[i]` of the reference, the nearest
+ * later row j > i by squared distance (first minimum, the running best kept in
+ * the element type), and for row n - 1 itself and the element type's maximum;
+ * closest_out (2) and closest_distance_out: closest_pair().
+ * SC_ERR_INVALID with "min number of rows should be 3" below three rows. */
+sc_status sc_fastpair(sc_knn *h, int64_t *neighbour_out, double *distance_out,
+                      int64_t *closest_out, double *closest_distance_out);
 /* KNNClassifier / KNNRegressor aggregation on the device over a find()
  * result already in idx/dist (device memory of this handle, m x k):
  * y_class = class index per training row (KNNClassifier::fit,

@@ -70,6 +70,8 @@ def lib():
             L.orc_dbscan_fit.argtypes = [I, P, I64, I64, D, I64, P]
             L.orc_dbscan_fit.restype = I64
             L.orc_dbscan_predict.argtypes = [I, P, I64, I64, P, I64, P, I64, D, P]
+            L.orc_fastpair.argtypes = [I, P, I64, I64, P, P]
+            L.orc_fastpair.restype = I
             L.orc_knn_vote.argtypes = [P, P, I64, I64, P, I64, I, P]
             L.orc_knn_regress.argtypes = [P, P, I64, I64, P, I, P]
             L.orc_last_error.restype = C.c_char_p
@@ -257,6 +259,24 @@ def dbscan_predict(x, y, k, queries, eps):
     lib().orc_dbscan_predict(dt, _ptr(x), n, d, _ptr(np.ascontiguousarray(y, np.int64)), int(k),
                              _ptr(queries), queries.shape[0], float(eps), _ptr(out))
     return out
+
+
+def fastpair(x):
+    """FastPair::new + closest_pair: (neighbour per row, distance per row, (a, b, d))."""
+    x = np.ascontiguousarray(x)
+    if x.dtype not in (np.float32, np.float64):
+        x = x.astype(np.float64)
+    dt = F32 if x.dtype == np.float32 else F64
+    n, d = x.shape
+    nb = np.zeros(max(n, 1), np.int64)
+    dist = np.zeros(max(n, 1), np.float64)
+    if lib().orc_fastpair(dt, _ptr(x), n, d, _ptr(nb), _ptr(dist)) != 0:
+        raise ValueError("Find failed: min number of rows should be 3")
+    a = 0
+    for p in range(n):  # closest_pair (fastpair.rs:165-182)
+        if dist[p] < dist[a]:
+            a = p
+    return nb[:n], dist[:n], (a, int(nb[a]), float(dist[a]))
 
 
 def knn_vote(idx, dist, y_index, n_classes, weight=0):

@@ -1,11 +1,12 @@
 /*
  * Oracle restatement of smartcore's brute-force kNN path: HeapSelection,
  * LinearKNNSearch::find / find_radius, the classifier / regressor
- * aggregation, and DBSCAN over find_radius.  TEST INFRASTRUCTURE ONLY (see
- * oracle.h).
+ * aggregation, DBSCAN over find_radius, and FastPair's initial closest
+ * pairs.  TEST INFRASTRUCTURE ONLY (see oracle.h).
  */
 #include "oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 
@@ -282,4 +283,32 @@ void orc_dbscan_predict(int dtype, const void *x, int64_t n, int64_t d, const in
     out[r] = which != k ? which + 1 : 0;
   }
   free(votes);
+}
+
+/* FastPair::init (src/algorithm/neighbour/fastpair.rs:82-150) step by step:
+ * the map `distances` as arrays nb / dist (nb = -1 for None), `insert` and
+ * `and_modify` as overwrites, the running best nbd kept in the element type
+ * (T::from(d)).  Row n - 1 ends with neighbour n - 1 and T::MAX. */
+int orc_fastpair(int dtype, const void *x, int64_t n, int64_t d, int64_t *nb, double *dist) {
+  if (n < 3) return -1; /* "min number of rows should be 3" */
+  const double tmax = dtype == ORC_F32 ? (double)FLT_MAX : DBL_MAX;
+  for (int64_t i = 0; i < n - 1; ++i) { nb[i] = -1; dist[i] = tmax; }
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t index_closest = i + 1;
+    double nbd = dist[i];
+    for (int64_t j = i + 1; j < n; ++j) {
+      nb[j] = i;
+      dist[j] = nbd;
+      const double dd = orc_sqdist(dtype, row_at(dtype, x, i, d), row_at(dtype, x, j, d), d);
+      if (dd < nbd) {
+        index_closest = j;
+        nbd = dtype == ORC_F32 ? (double)(float)dd : dd;
+      }
+    }
+    dist[i] = nbd;
+    nb[i] = index_closest;
+  }
+  nb[n - 1] = n - 1;
+  dist[n - 1] = tmax;
+  return 0;
 }

@@ -108,6 +108,7 @@ int64_t orc_dbscan_fit(int dtype, const void *x, int64_t n, int64_t d, double ep
                        int64_t *y);
 void orc_dbscan_predict(int dtype, const void *x, int64_t n, int64_t d, const int64_t *y, int64_t k,
                         const void *q, int64_t m, double eps, int64_t *out);
+int orc_fastpair(int dtype, const void *x, int64_t n, int64_t d, int64_t *nb, double *dist);
 void orc_knn_vote(const int64_t *idx, const double *dist, int64_t m, int64_t k,
                   const int64_t *y, int64_t n_classes, int weight,
                   int64_t *class_out);

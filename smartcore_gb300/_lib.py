@@ -47,6 +47,7 @@ SIGNATURES = {
     "sc_knn_create": ([_P, _I32, _I32, _I32, _I64, _I64, _I64, _P], _I32),
     "sc_knn_find": ([_P, _P, _I32, _I32, _I64, _I64, _I64, _I32, _I32, _P, _P], _I32),
     "sc_knn_find_radius": ([_P, _P, _I32, _I32, _I64, _I64, _D, _I32, _P, _I64, _P, _P, _P], _I32),
+    "sc_fastpair": ([_P, _P, _P, _P, _P], _I32),
     "sc_dbscan_fit": ([_P, _D, _I64, _I32, _P, _P], _I32),
     "sc_dbscan_predict": ([_P, _P, _I32, _I32, _I64, _I64, _D, _I32, _P, _I64, _P], _I32),
     "sc_knn_classify": ([_P, _P, _I32, _I32, _I64, _I64, _I64, _I32, _I32, _P, _I64, _P], _I32),

@@ -757,6 +757,43 @@ sc_status sc_dbscan_predict(sc_knn *h, const void *queries, int32_t layout, int3
   return SC_OK;
 }
 
+sc_status sc_fastpair(sc_knn *h, int64_t *neighbour_out, double *distance_out, int64_t *closest_out,
+                      double *closest_distance_out) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (h->n < 3) { set_error("min number of rows should be 3"); return SC_ERR_INVALID; }  // fastpair.rs:60-65
+  const int64_t n = h->n;
+  std::vector<int64_t> nb((size_t)n);
+  std::vector<double> dist((size_t)n);
+  int64_t *dnb = nullptr;
+  double *ddist = nullptr;
+  sc_status r = SC_OK;
+  do {
+    if ((r = dalloc(&dnb, (size_t)n, h->stream)) != SC_OK || (r = dalloc(&ddist, (size_t)n, h->stream)) != SC_OK) break;
+    if ((r = launch_fastpair(h->dtype, h->train, n, (int)h->d, dnb, ddist, h->stream)) != SC_OK) break;
+    if (cudaMemcpyAsync(nb.data(), dnb, (size_t)n * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(dist.data(), ddist, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "fastpair");
+      break;
+    }
+  } while (0);
+  cudaStreamSynchronize(h->stream);
+  dfree(dnb, h->stream); dfree(ddist, h->stream);
+  if (r != SC_OK) return r;
+  if (neighbour_out) memcpy(neighbour_out, nb.data(), (size_t)n * sizeof(int64_t));
+  if (distance_out) memcpy(distance_out, dist.data(), (size_t)n * sizeof(double));
+  // closest_pair (fastpair.rs:165-182): the first smallest distance along the
+  // neighbours list 0, 1, ..., n - 1
+  int64_t a = 0;
+  for (int64_t p = 0; p < n; ++p)
+    if (dist[(size_t)p] < dist[(size_t)a]) a = p;
+  if (closest_out) { closest_out[0] = a; closest_out[1] = nb[(size_t)a]; }
+  if (closest_distance_out) *closest_distance_out = dist[(size_t)a];
+  return SC_OK;
+}
+
 sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout, int32_t mem, int64_t m,
                              int64_t ld, double radius, int32_t form, int64_t *counts_out, int64_t capacity,
                              int64_t *idx_out, double *dist_out, int64_t *total_out) {

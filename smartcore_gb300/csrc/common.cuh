@@ -123,6 +123,8 @@ sc_status launch_knn_radius_fp64(int dtype, const void *train, int64_t n, int d,
                                  double radius, int64_t *counts, const int64_t *offsets, int64_t *idx,
                                  double *dist, cudaStream_t s);
 sc_status launch_widen_labels(const int32_t *in, int64_t *out, int64_t n, cudaStream_t s);
+sc_status launch_fastpair(int dtype, const void *x, int64_t n, int d, int64_t *nb, double *dist,
+                          cudaStream_t s);
 sc_status launch_knn_vote(const int64_t *idx, const double *dist, int64_t m,
                           int k, int weight, const int64_t *y_class,
                           int64_t *out, cudaStream_t s);

@@ -426,7 +426,6 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
           }
         }
         for (int o = p >> 1; o > 0; o >>= 1) s32 = __fadd_rn(s32, __shfl_xor_sync(0xffffffffu, s32, o));
-        const int idx = it + q * R + seg;
         const bool ex = rq[q] >= 0 && unit == 0 && !(__fmul_rd(s32, lbf) > s_cur[w][rq[q] >= 0 ? rq[q] : 0]);
         if (__any_sync(0xffffffffu, ex)) {
           // The exact value without the sequential sum: in units of
@@ -970,6 +969,83 @@ __global__ void knn_fp64_kernel(const T *__restrict__ train, int64_t n, int d,
     idx_out[q * k + s] = mi[s * nt];
     dist_out[q * k + s] = mh[s * nt];
   }
+}
+
+// ---------------------------------------------------------------------------
+// FastPair::init (src/algorithm/neighbour/fastpair.rs:82-150): for each row i
+// the nearest later row j > i by the reference's squared distance, scanned in
+// index order with the strict `d < nbd`, where nbd is the running best kept in
+// the element type (T::from(d)) and starting at T::MAX.  One thread per row;
+// the later rows stream through shared memory in tiles.  Row n - 1 keeps
+// neighbour n - 1 and distance T::MAX (fastpair.rs:141-143).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void fastpair_kernel(const T *__restrict__ x, int64_t n, int d, int64_t *__restrict__ nb_out,
+                                double *__restrict__ dist_out) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nt = blockDim.x;
+  T *qs = reinterpret_cast<T *>(smraw);  // d x nt: this block's rows, transposed
+  T *ts = qs + (size_t)d * nt;           // kKnnTile x d
+  const int tid = threadIdx.x;
+  const int64_t i = (int64_t)blockIdx.x * nt + tid;
+  const bool live = i < n;
+  for (int j = 0; j < d; ++j) qs[j * nt + tid] = live ? x[i * d + j] : T(0);
+  const T tmax = sizeof(T) == 4 ? (T)FLT_MAX : (T)DBL_MAX;
+  T best = tmax;
+  int64_t idx = i + 1;
+  const int64_t first = (int64_t)blockIdx.x * nt + 1;  // the block's smallest j
+  for (int64_t r0 = first - (first % kKnnTile); r0 < n; r0 += kKnnTile) {
+    const int rt = (int)min((int64_t)kKnnTile, n - r0);
+    __syncthreads();
+    for (int t = tid; t < rt * d; t += nt) ts[t] = x[r0 * d + t];
+    __syncthreads();
+    if (!live) continue;
+    for (int r = 0; r < rt; ++r) {
+      const int64_t j = r0 + r;
+      if (j <= i) continue;
+      const T *tr = ts + r * d;
+      // Euclidian::squared_distance (euclidian.rs:51-63) in the reference's order
+      double s = 0.0;
+      for (int c = 0; c < d; ++c) s = __dadd_rn(s, sq_term(qs[c * nt + tid], tr[c]));
+      if (s < (double)best) {
+        best = (T)s;  // T::from(d): round to nearest
+        idx = j;
+      }
+    }
+  }
+  if (!live) return;
+  if (i == n - 1) {
+    nb_out[i] = n - 1;
+    dist_out[i] = (double)tmax;
+  } else {
+    nb_out[i] = idx;
+    dist_out[i] = (double)best;
+  }
+}
+
+sc_status launch_fastpair(int dtype, const void *x, int64_t n, int d, int64_t *nb, double *dist, cudaStream_t s) {
+  if (n == 0) return SC_OK;
+  const int es = dtype == SC_F32 ? 4 : 8;
+  int nt = 128;
+  size_t smem = 0;
+  for (; nt >= 32; nt >>= 1) {
+    smem = (size_t)d * nt * es + (size_t)kKnnTile * d * es;
+    if (smem <= 200 * 1024) break;
+  }
+  if (nt < 32) {
+    set_error("d=%d exceeds the FastPair kernel's shared memory", d);
+    return SC_ERR_INVALID;
+  }
+  const int grid = (int)((n + nt - 1) / nt);
+  if (dtype == SC_F32) {
+    SC_CUDA(cudaFuncSetAttribute(fastpair_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fastpair_kernel<float><<<grid, nt, smem, s>>>((const float *)x, n, d, nb, dist);
+  } else {
+    SC_CUDA(cudaFuncSetAttribute(fastpair_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fastpair_kernel<double><<<grid, nt, smem, s>>>((const double *)x, n, d, nb, dist);
+  }
+  SC_LAUNCHED();
+  return SC_OK;
 }
 
 sc_status launch_knn_fp64(int dtype, const void *train, int64_t n, int d,

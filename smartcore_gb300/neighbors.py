@@ -209,3 +209,46 @@ class KNNRegressor:
 
     def predict(self, x) -> np.ndarray:
         return self.knn.regress(x, self.k, self.weight, self.y)
+
+
+@dataclass(frozen=True)
+class PairwiseDistance:
+    """PairwiseDistance (src/metrics/distance/mod.rs:84-110)."""
+    node: int
+    neighbour: Optional[int]
+    distance: Optional[float]
+
+
+class FastPair:
+    """FastPair::new / closest_pair (src/algorithm/neighbour/fastpair.rs:59-182).
+
+    `distances[i]` is the reference's entry for row i: the nearest later row
+    by squared distance (the running best kept in the element type), and for
+    the last row itself with the element type's maximum; `neighbours` is the
+    list 0 .. n - 1.  The scan runs on the device."""
+
+    def __init__(self, x):
+        a = as_matrix(x)
+        n = a.shape[0]
+        if n < 3:
+            raise Failed(FailedError.FindFailed, "min number of rows should be 3")
+        s = LinearKNNSearch(a)
+        nb = np.zeros(n, np.int64)
+        dist = np.zeros(n, np.float64)
+        pair = np.zeros(2, np.int64)
+        pd = np.zeros(1, np.float64)
+        try:
+            _lib.check(s._L.sc_fastpair(s.h, _lib.ptr(nb), _lib.ptr(dist), _lib.ptr(pair), _lib.ptr(pd)),
+                       FailedError.FindFailed)
+        finally:
+            s.close()
+        self.distances = {i: PairwiseDistance(i, int(nb[i]), float(dist[i])) for i in range(n)}
+        self.neighbours = list(range(n))
+        self._closest = PairwiseDistance(int(pair[0]), int(pair[1]), float(pd[0]))
+
+    @staticmethod
+    def new(x) -> "FastPair":
+        return FastPair(x)
+
+    def closest_pair(self) -> PairwiseDistance:
+        return self._closest

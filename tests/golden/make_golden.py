@@ -180,6 +180,25 @@ def main(root):
         "errors": re.findall(r'Failed::fit\("(Invalid [^"]*)"\)', src),
     }
 
+    src = read(root, "src/algorithm/neighbour/fastpair.rs")
+    body = fn_body(src, "fastpair_new")
+    entries = re.findall(r"\(\s*(\d+),\s*PairwiseDistance\s*\{\s*node:\s*(\d+),\s*neighbour:\s*Some\((\d+)\),"
+                         r"\s*distance:\s*Some\(([^)]*)\),", body)
+    closest = {}
+    for name in ("fastpair_closest_pair", "one_dimensional_dataset_minimal", "one_dimensional_dataset_2"):
+        b = fn_body(src, name)
+        m = re.search(r"node:\s*(\d+),\s*neighbour:\s*Some\((\d+)\),\s*distance:\s*Some\(([^)]*)\)", b)
+        closest[name] = {"x": rows(b[b.index("from_2d_array"):b.index(".unwrap()")]),
+                         "expect": [int(m.group(1)), int(m.group(2)), num(m.group(3))]}
+    kats["fastpair"] = {
+        "cite": "src/algorithm/neighbour/fastpair.rs:270-510",
+        "x": rows(body[body.index("from_2d_array"):body.index(".unwrap()")]),
+        "distances": {int(k): [int(nd), int(nb), float("inf") if "MAX" in dv else num(dv)]
+                      for k, nd, nb, dv in entries},
+        "closest": closest,
+        "error": re.search(r'"(min number of rows should be \d+)"', src).group(1),
+    }
+
     out = os.path.join(HERE, "reference_kats.json")
     with open(out, "w") as f:
         json.dump(kats, f, indent=1)

@@ -136,3 +136,16 @@ def test_dbscan_fit_predict(kats):
     for bad, msg in (((c["eps"], 0), c["errors"][0]), ((0.0, 2), c["errors"][1])):
         with pytest.raises(ValueError, match=msg.strip()):
             oracle.dbscan_fit(x, *bad)
+
+
+def test_fastpair(kats):
+    c = kats["fastpair"]
+    nb, dist, closest = oracle.fastpair(np.array(c["x"]))
+    for i, (node, neighbour, d) in c["distances"].items():
+        i = int(i)
+        assert nb[i] == neighbour
+        assert dist[i] == (np.finfo(np.float64).max if d == float("inf") else d)
+    for case in c["closest"].values():
+        assert list(oracle.fastpair(np.array(case["x"]))[2]) == case["expect"]
+    with pytest.raises(ValueError, match=c["error"]):
+        oracle.fastpair(np.zeros((2, 2)))
