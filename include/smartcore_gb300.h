@@ -153,7 +153,7 @@ void sc_kmeans_destroy(sc_kmeans *h);
  * For callers that cannot allocate device memory during the call: a process
  * whose device memory is already reserved by its own pool allocator (a
  * cudaMalloc would fail or fragment that pool), or a loop that re-clusters
- * at a high rate, where cudaMalloc / cudaFree would take the driver's
+ * at a high rate, where cudaMalloc / cudaFree would take the CUDA driver's
  * allocation lock and cudaFree would synchronise the whole device.
  *
  * x          n x d row-major (ld = d) SC_F32 / SC_F64 matrix, device memory.

@@ -1,7 +1,7 @@
 """CPU oracle for smartcore's distance-argmin path (test infrastructure).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may import this package: it is the checker, never the product.
+``bench.py`` may import this package: it checks the product and is never part of it.
 The C sources (``rng.c``, ``kmeans.c``, ``knn.c``) restate the reference
 algorithm function by function, each citing the smartcore file:line it
 follows; this module only loads them through ctypes and converts arrays.

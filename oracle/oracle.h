@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the distance-argmin path of smartcore 0.4.0.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * TEST INFRASTRUCTURE ONLY.  This library checks the product: the parity tests,
  * the smoke check and the CPU-baseline leg of the benchmark call it.  The
  * product library (libsmartcore_gb300.so) never links or calls it.
  *

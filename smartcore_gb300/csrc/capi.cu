@@ -67,7 +67,7 @@ void dev_free(void *p, cudaStream_t s) {
 // Pinned host staging buffer for results copied into caller memory (grows,
 // never shrinks; callers hold g_stage_mutex while they use it).  A device
 // copy into pageable memory that the caller has just allocated pays for the
-// first touch of every page inside the driver's copy; a copy into pinned
+// first touch of every page inside the CUDA copy; a copy into pinned
 // memory and a CPU memcpy do not.
 std::mutex g_stage_mutex;
 void *g_stage = nullptr;

@@ -6,7 +6,7 @@ smartcore sources are available:
 
     python tests/golden/make_golden.py /root/reference
 
-The tests that run on the GPU machine only read the JSON it wrote.
+The GPU tests only read the JSON it wrote.
 """
 from __future__ import annotations
 

@@ -1,8 +1,8 @@
 """Pin the CPU oracle to the reference's own known-answer tests.
 
 Each test restates one smartcore test (the fixture names its file:line) and
-runs it against the oracle.  These are the pins that make the oracle a
-trustworthy checker for the GPU parity tests.
+runs it against the oracle.  These pins are what make the oracle a trustworthy
+reference for the GPU parity tests.
 """
 import math
 
