@@ -979,8 +979,15 @@ __global__ void knn_fp64_kernel(const T *__restrict__ train, int64_t n, int d,
 // the later rows stream through shared memory in tiles.  Row n - 1 keeps
 // neighbour n - 1 and distance T::MAX (fastpair.rs:141-143).
 // ---------------------------------------------------------------------------
+// Element c of a row stored with stride s (a column of a transposed tile).
+struct StridedRow {
+  const float *p;
+  int s;
+  __device__ __forceinline__ float operator[](int c) const { return p[c * s]; }
+};
+
 template <typename T>
-__global__ void fastpair_kernel(const T *__restrict__ x, int64_t n, int d, int64_t *__restrict__ nb_out,
+__global__ void fastpair_kernel(const T *__restrict__ x, int64_t n, int d, int lg_d, int64_t *__restrict__ nb_out,
                                 double *__restrict__ dist_out) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nt = blockDim.x;
@@ -1004,9 +1011,15 @@ __global__ void fastpair_kernel(const T *__restrict__ x, int64_t n, int d, int64
       const int64_t j = r0 + r;
       if (j <= i) continue;
       const T *tr = ts + r * d;
-      // Euclidian::squared_distance (euclidian.rs:51-63) in the reference's order
+      // Euclidian::squared_distance (euclidian.rs:51-63) in the reference's
+      // order; f32 rows by the integer reproduction of the sequential sum
       double s = 0.0;
-      for (int c = 0; c < d; ++c) s = __dadd_rn(s, sq_term(qs[c * nt + tid], tr[c]));
+      bool done = false;
+      if constexpr (sizeof(T) == 4) done = sqd_seq_f32(StridedRow{qs + tid, nt}, tr, d, lg_d, s);
+      if (!done) {
+        s = 0.0;
+        for (int c = 0; c < d; ++c) s = __dadd_rn(s, sq_term(qs[c * nt + tid], tr[c]));
+      }
       if (s < (double)best) {
         best = (T)s;  // T::from(d): round to nearest
         idx = j;
@@ -1036,13 +1049,15 @@ sc_status launch_fastpair(int dtype, const void *x, int64_t n, int d, int64_t *n
     set_error("d=%d exceeds the FastPair kernel's shared memory", d);
     return SC_ERR_INVALID;
   }
+  int lg_d = 0;
+  while ((1 << lg_d) < d) ++lg_d;
   const int grid = (int)((n + nt - 1) / nt);
   if (dtype == SC_F32) {
     SC_CUDA(cudaFuncSetAttribute(fastpair_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    fastpair_kernel<float><<<grid, nt, smem, s>>>((const float *)x, n, d, nb, dist);
+    fastpair_kernel<float><<<grid, nt, smem, s>>>((const float *)x, n, d, lg_d, nb, dist);
   } else {
     SC_CUDA(cudaFuncSetAttribute(fastpair_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    fastpair_kernel<double><<<grid, nt, smem, s>>>((const double *)x, n, d, nb, dist);
+    fastpair_kernel<double><<<grid, nt, smem, s>>>((const double *)x, n, d, lg_d, nb, dist);
   }
   SC_LAUNCHED();
   return SC_OK;
