@@ -86,3 +86,16 @@ def test_draws_match_oracle(rng, n, k, seed):
 def test_draws_reject_empty(L):
     a = np.zeros(2, np.int64)
     assert L.sc_kmeanspp_draws(0, 0, 0, 2, _lib.ptr(a), _lib.ptr(a)) == _lib.SC_ERR_INVALID
+
+
+def test_null_handles_rejected_before_any_device_call(L):
+    """The entry points added after find check their handle and arguments on
+    the host first; these calls touch no GPU."""
+    out = np.zeros(4, np.int64)
+    dist = np.zeros(4)
+    k = np.zeros(1, np.int64)
+    assert L.sc_dbscan_fit(None, 0.5, 5, 1, _lib.ptr(out), _lib.ptr(k)) == _lib.SC_ERR_INVALID
+    assert L.sc_dbscan_predict(None, None, 0, 0, 0, 0, 0.5, 1, None, 0, None) == _lib.SC_ERR_INVALID
+    assert L.sc_fastpair(None, _lib.ptr(out), _lib.ptr(dist), None, None) == _lib.SC_ERR_INVALID
+    assert L.sc_knn_find_radius(None, None, 0, 0, 0, 0, 1.0, 1, None, 0, None, None, None) == _lib.SC_ERR_INVALID
+    assert "null handle" in _lib.last_error()
