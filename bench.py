@@ -572,6 +572,8 @@ def main():
                     help="time the device-resident Lloyd loop only (for profiler runs)")
     ap.add_argument("--knn-only", type=int, default=0, metavar="QUERIES",
                     help="time only the split-BF16 kNN find with this many queries (for profiler runs)")
+    ap.add_argument("--neighbours-only", action="store_true",
+                    help="time only the find_radius, DBSCAN and FastPair blocks (for profiler runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -579,6 +581,14 @@ def main():
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(bench_knn(torch, 0, reps=2, n_query=args.knn_only, with_fp64=False)), flush=True)
+        return
+    if args.neighbours_only:
+        import torch
+        from smartcore_gb300.synthetic import knn_blobs_f32
+        torch.cuda.set_device(0)
+        xt, _, xq, _ = knn_blobs_f32(KNN_N, KNN_M, KNN_D)
+        print(json.dumps({"find_radius": bench_radius(torch, 0, xt, xq), "dbscan": bench_dbscan(torch, xt),
+                          "fastpair": bench_fastpair(torch, xt)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)
