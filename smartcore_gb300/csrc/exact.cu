@@ -212,17 +212,19 @@ __host__ __device__ __forceinline__ int pp_stage_ld(int d, int vec4) {
 }
 
 // ---- f32 rows, d <= 128: one launch per draw ----
-// pp_draw_kernel: one warp per 256-row block of d.  The far test runs in f32
-// from (d32 = d rounded up, y, seed_cc) and reads no row; the rows it leaves
-// are listed and read coalesced (up to four 16-byte units per lane, two
-// passes of whole rows in flight) for the f32 lower bound; the rows that bound cannot
-// settle either (the rows whose distance may drop) get the reference's exact
-// value, from the integer sum of their terms across the row's lanes when that
-// sum shows that no addition of the sequential f64 sum can round (almost every
-// row), else from the sequential reproduction, one row per lane.  The warp then writes the block's fixed-order partial sum
-// of d for the selection.  The first draw (every row exact) runs
-// pp_first_kernel, which stages the rows in shared memory, and then
-// pp_partials_kernel.
+// pp_draw_kernel: one warp per 256-row block of d, in three stages.
+//  1. The far test, in f32 from (d32 = d rounded up, y, seed_cc): reads no row.
+//  2. Split form only: the rows it leaves are bounded through their BF16 high
+//     halves (half the bytes of the f32 row).
+//  3. The rows still left are read coalesced (up to four 16-byte units per
+//     lane) for the f32 lower bound; the rows that bound cannot settle either
+//     (the rows whose distance may drop) get the reference's exact value: from
+//     the integer sum of their terms across the row's lanes when that sum
+//     shows that no addition of the sequential f64 sum can round (almost every
+//     row), else from the sequential reproduction, one row per lane.
+// The warp then writes the block's fixed-order partial sum of d for the
+// selection.  The first draw (every row exact) runs pp_first_kernel, which
+// stages the rows in shared memory, and then pp_partials_kernel.
 constexpr int kPPWarps = kPPThreads / 32;  // 32-row groups per 256-row block
 constexpr int kDrawWarps = 4, kDrawThreads = 32 * kDrawWarps;
 
