@@ -175,9 +175,11 @@ void sc_kmeans_destroy(sc_kmeans *h);
  * them.  Every call in the process shares that array: overlapping calls on
  * one device would race on it, so calls are serialised by a process-wide
  * lock and each returns only after its work on the stream has finished.
- * The first call on each device looks the array's address up with
- * cudaGetSymbolAddress (which may load the library's device code): make it
- * outside any stream capture. */
+ * The first call on each device (and CUDA context) looks the array's address
+ * up with cudaGetSymbolAddress, which may load the library's device code.
+ * Every call synchronises the stream twice (it reads max |x| back to pick
+ * the fixed-point scale of the sums, and waits for its results), so it
+ * cannot be used inside stream capture. */
 sc_status sc_kmeans_step_noalloc(const void *x, int32_t dtype, int64_t n,
                                  int64_t d, double *centroids, int64_t k,
                                  int32_t *labels, int64_t *sizes,

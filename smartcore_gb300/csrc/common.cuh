@@ -148,6 +148,15 @@ sc_status launch_finalize_scalar(const double *part, int nparts,
                                  const double *cluster_terms, int64_t nterms,
                                  const double *xnorm_total, LloydState *st,
                                  cudaStream_t s);
+// Mode, fixed-point scale and partial count that update_alloc picks for
+// (n, d, k); absmax = max |x|.  Every path that sums at the returned scale
+// rounds each value to the same fixed-point integer, so equal inputs give
+// equal centroids whichever buffers hold the sums.
+struct UpdatePlan {
+  int mode = 0, grid = 0, scale = 0;
+  size_t smem = 0;
+};
+UpdatePlan update_plan(int dtype, int64_t n, int d, int k, double absmax, int num_sms);
 // Chooses the mode for (n, d, k) and allocates; absmax = max |x|.
 sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms,
                        cudaStream_t s);

@@ -24,6 +24,8 @@
 
 #include <mutex>
 
+#include <cuda.h>
+
 #include "common.cuh"
 
 namespace sc {
@@ -44,14 +46,27 @@ constexpr size_t kScratchBytes = align256(kOffBits + sizeof(unsigned long long))
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
-std::mutex g_mutex;                      // serialises calls: the scratch is shared
-unsigned char *g_addr[kMaxDevices] = {};  // device address of g_scratch, per device
+std::mutex g_mutex;  // serialises calls: the scratch is shared
+// Device address of g_scratch, looked up once per device and CUDA context: a
+// __device__ symbol's address belongs to the context that loaded the module,
+// so a new context on the same device (after cudaDeviceReset, or a caller's
+// own driver-API context) gets its own lookup.
+struct ScratchAddr {
+  CUcontext ctx = nullptr;
+  unsigned char *addr = nullptr;
+};
+ScratchAddr g_addr[kMaxDevices];
 
-int ceil_log2_i64(int64_t v) {
-  int r = 0;
-  while (((int64_t)1 << r) < v) ++r;
-  return r;
-}
+// Waits for the call's work on the stream before the lock is released, on
+// every return path: a call that fails after its first launch must not leave
+// kernels writing the shared scratch while the next call clears it.
+struct DrainOnExit {
+  cudaStream_t s;
+  bool armed = false;
+  ~DrainOnExit() {
+    if (armed) cudaStreamSynchronize(s);
+  }
+};
 
 }  // namespace
 }  // namespace sc
@@ -78,27 +93,38 @@ extern "C" sc_status sc_kmeans_step_noalloc(const void *x, int32_t dtype, int64_
   const int nparts = assign_block_count(n);  // one partial per 128 points
 
   std::lock_guard<std::mutex> lock(g_mutex);
-  int dev = 0;
+  int dev = 0, num_sms = 0;
   SC_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) { set_error("device ordinal %d is not supported", dev); return SC_ERR_INVALID; }
-  if (!g_addr[dev]) {
+  SC_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+  CUcontext ctx = nullptr;
+  if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+  if (!ctx || g_addr[dev].ctx != ctx || !g_addr[dev].addr) {
+    // Set-up for this device and context.  The lookup also makes the
+    // device's primary context current when no context is.
     void *p = nullptr;
     SC_CUDA(cudaGetSymbolAddress(&p, g_scratch));
-    g_addr[dev] = (unsigned char *)p;
+    if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS || !ctx) { set_error("no current CUDA context"); return SC_ERR_CUDA; }
+    g_addr[dev].ctx = ctx;
+    g_addr[dev].addr = (unsigned char *)p;
   }
-  unsigned char *base = g_addr[dev];
+  unsigned char *base = g_addr[dev].addr;
   Acc128 *acc = (Acc128 *)(base + kOffAcc);
   unsigned long long *cnt = (unsigned long long *)(base + kOffCnt);
   double *part = (double *)(base + kOffPart);
   LloydState *st = (LloydState *)(base + kOffSt);
   unsigned long long *bits = (unsigned long long *)(base + kOffBits);
   cudaStream_t s = (cudaStream_t)stream;
+  DrainOnExit drain{s};
+  drain.armed = true;
 
   SC_CUDA(cudaMemsetAsync(acc, 0, (size_t)(k * d) * sizeof(Acc128), s));
   SC_CUDA(cudaMemsetAsync(cnt, 0, (size_t)k * sizeof(unsigned long long), s));
   SC_CUDA(cudaMemsetAsync(st, 0, sizeof(LloydState), s));
 
-  // Fixed-point scale of the 128-bit sums: |x| < 2^e, n points.
+  // Fixed-point scale of the 128-bit sums: the scale the handle API picks for
+  // the same (n, d, k) and max |x|, so every value rounds to the same integer
+  // and the centroids equal the handle's bit for bit.
   SC_TRY(launch_absmax(dtype, x, n * d, bits, s));
   unsigned long long hb = 0;
   SC_CUDA(cudaMemcpyAsync(&hb, bits, sizeof hb, cudaMemcpyDeviceToHost, s));
@@ -106,9 +132,7 @@ extern "C" sc_status sc_kmeans_step_noalloc(const void *x, int32_t dtype, int64_
   double amax;
   memcpy(&amax, &hb, sizeof amax);
   if (!(amax <= DBL_MAX)) { set_error("x contains NaN or infinity; the GPU path requires finite input"); return SC_ERR_INVALID; }
-  int e = 0;
-  if (amax > 0) frexp(amax, &e);
-  const int scale = 125 - e - ceil_log2_i64(n + 1);
+  const int scale = update_plan(dtype, n, (int)d, (int)k, amax, num_sms).scale;
 
   SC_TRY(launch_assign_fp64(dtype, x, n, (int)d, centroids, (int)k, labels, part, st, s));
   SC_TRY(launch_update_fixed(dtype, x, n, (int)d, labels, acc, cnt, scale, st, s));
@@ -116,5 +140,6 @@ extern "C" sc_status sc_kmeans_step_noalloc(const void *x, int32_t dtype, int64_
   SC_TRY(launch_finalize_scalar(part, nparts, nullptr, k, nullptr, st, s));
   if (distortion) SC_CUDA(cudaMemcpyAsync(distortion, &st->last_dist, sizeof(double), cudaMemcpyDeviceToHost, s));
   SC_CUDA(cudaStreamSynchronize(s));
+  drain.armed = false;
   return SC_OK;
 }

@@ -628,9 +628,8 @@ static int ceil_log2(int64_t v) {
   return l;
 }
 
-sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms,
-                       cudaStream_t s) {
-  update_free(u, s);
+UpdatePlan update_plan(int dtype, int64_t n, int d, int k, double absmax, int num_sms) {
+  UpdatePlan p;
   int e = 0;
   if (absmax > 0) frexp(absmax, &e);  // |x| < 2^e
   int grid = num_sms;
@@ -642,20 +641,34 @@ sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double 
   const size_t smem = (size_t)(3 * k + 1 + chunk) * 4;
   const size_t part_bytes = (size_t)grid * k * d * sizeof(long long);
   if (dtype == SC_F32 && d <= 256 && smem <= 200 * 1024 && part_bytes <= ((size_t)512 << 20) && n > 0) {
-    u->mode = 1;
-    u->grid = grid;
+    p.mode = 1;
+    p.grid = grid;
+    p.smem = smem;
+    p.scale = 62 - e - ceil_log2(chunk + 1);
+    if (p.scale > 160) p.scale = 160;  // values below 2^-160 contribute 0
+    return p;
+  }
+  p.mode = 0;
+  p.scale = 125 - e - ceil_log2(n + 1);
+  return p;
+}
+
+sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double absmax, int num_sms,
+                       cudaStream_t s) {
+  update_free(u, s);
+  const UpdatePlan p = update_plan(dtype, n, d, k, absmax, num_sms);
+  u->mode = p.mode;
+  u->scale = p.scale;
+  if (p.mode == 1) {
+    u->grid = p.grid;
     u->threads = 1024;
-    u->smem = smem;
-    u->scale = 62 - e - ceil_log2(chunk + 1);
-    if (u->scale > 160) u->scale = 160;  // values below 2^-160 contribute 0
-    const size_t bal = smem + (size_t)k * d * sizeof(long long);
+    u->smem = p.smem;
+    const size_t bal = p.smem + (size_t)k * d * sizeof(long long);
     u->balanced_smem = (d <= 128 && bal <= 200 * 1024) ? bal : 0;
-    SC_TRY(dalloc(&u->part, (size_t)grid * k * d, s));
-    SC_TRY(dalloc(&u->cpart, (size_t)grid * k, s));
+    SC_TRY(dalloc(&u->part, (size_t)p.grid * k * d, s));
+    SC_TRY(dalloc(&u->cpart, (size_t)p.grid * k, s));
     return SC_OK;
   }
-  u->mode = 0;
-  u->scale = 125 - e - ceil_log2(n + 1);
   SC_TRY(dalloc(&u->acc, (size_t)k * d, s));
   SC_TRY(dalloc(&u->cnt, (size_t)k, s));
   SC_CUDA(cudaMemsetAsync(u->acc, 0, (size_t)k * d * sizeof(Acc128), s));

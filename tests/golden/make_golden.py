@@ -4,7 +4,7 @@ Reads the reference's own Rust test bodies (inputs and asserted answers) as
 text and writes ``reference_kats.json`` beside this script.  Run it where the
 smartcore sources are available:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the smartcore source tree>
 
 The GPU tests only read the JSON it wrote.
 """
@@ -206,4 +206,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path to the smartcore source tree>")
+    main(sys.argv[1])

@@ -64,6 +64,37 @@ def test_step_matches_handle_two_calls(L, n, d, k, np_dtype):
 
 
 @pytest.mark.gpu
+def test_step_matches_handle_values_below_the_sum_grid(L):
+    """f32 points with a column scaled by 1e-18 and subnormal entries: their
+    fixed-point roundings depend on the scale of the sums, which must be the
+    one the handle API picks for the same data."""
+    torch = pytest.importorskip("torch")
+    n, d, k = 6000, 8, 5
+    x, _ = blobs(n, d, k, seed=31, dtype=np.float32)
+    x[:, 3] *= np.float32(1e-18)
+    x[::7, 5] = np.float32(3e-39)
+    x = np.ascontiguousarray(x)
+    c0 = np.ascontiguousarray(x[np.random.default_rng(5).choice(n, k, replace=False)], np.float64)
+    ref = KMeansHandle(x, form=_lib.FORM_FP64)
+    ref.set_centroids(c0)
+    x_dev = torch.from_numpy(x).cuda()
+    cent_dev = torch.from_numpy(c0.copy()).cuda()
+    labels_dev = torch.zeros(n, dtype=torch.int32, device="cuda")
+    sizes_dev = torch.zeros(k, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(2):
+        ref.iterate(1, stop_on_converge=False)
+        r_cent, r_sizes, r_labels, r_dist, _ = ref.get()
+        dist = step(L, x_dev.data_ptr(), _lib.F32, n, d, cent_dev.data_ptr(), k, labels_dev.data_ptr(),
+                    sizes_dev.data_ptr())
+        assert np.array_equal(labels_dev.cpu().numpy().astype(np.int64), r_labels)
+        assert np.array_equal(sizes_dev.cpu().numpy(), r_sizes)
+        assert np.array_equal(cent_dev.cpu().numpy(), r_cent)
+        assert dist == r_dist
+    ref.close()
+
+
+@pytest.mark.gpu
 def test_step_null_sizes_and_distortion(L):
     torch = pytest.importorskip("torch")
     n, d, k = 2000, 8, 5
