@@ -186,6 +186,55 @@ sc_status sc_kmeans_step_noalloc(const void *x, int32_t dtype, int64_t n,
                                  double *distortion, void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Many independent KMeans::fit problems in one call                    */
+/* ------------------------------------------------------------------ */
+/* One problem of sc_kmeans_fit_batched: the arguments of sc_kmeans_fit
+ * (inputs in host memory) plus its outputs and counters. */
+typedef struct sc_kmeans_problem {
+  const void *x;           /* n x d, host memory */
+  int32_t layout;          /* SC_ROW_MAJOR or SC_COL_MAJOR */
+  int32_t status;          /* out: SC_OK, or the error of this problem */
+  int64_t n, d, ld;
+  int64_t k, max_iter;
+  int64_t first_index;     /* k-means++ draws, as for sc_kmeans_fit */
+  const double *uniforms;  /* k - 1 entries */
+  double *centroids_out;   /* k * d row-major, may be NULL */
+  int64_t *sizes_out;      /* k, may be NULL */
+  int64_t *labels_out;     /* n, may be NULL */
+  double *distortion_out;  /* 1, may be NULL */
+  int64_t *iters_out;      /* 1, may be NULL */
+  int64_t rescored;        /* out: rows re-scored in FP64 */
+  int64_t pp_replays;      /* out: k-means++ draws resolved by the replay */
+} sc_kmeans_problem;
+
+/* KMeans::fit (src/cluster/kmeans.rs:254-323) for `count` independent
+ * problems of uneven n, d and k (all of element type dtype) in one call, each
+ * with the results sc_kmeans_fit gives it alone (labels, sizes and iteration
+ * count equal; centroids equal up to the rounding of the exact sums, within
+ * 1e-15 relative).  Problems with d <= 64 and k <= 128 run together: every
+ * problem's k-means++ draw j in one pair of launches, then a persistent
+ * assignment kernel fed by a device work queue of (problem, rows) items and a
+ * per-problem finalize, the Lloyd loop captured as a CUDA graph.  The others
+ * run one after another through sc_kmeans_fit in `form`.
+ * Every problem is validated first, with KMeans::fit's messages
+ * (kmeans.rs:257-269) prefixed by "problem <i>: "; on a validation error
+ * nothing runs and no output is written. */
+sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count,
+                                int32_t dtype, int32_t form);
+/* Tuning of the batched assignment kernel: times its variants (centroids per
+ * inner pass, rows per work item) on one synthetic problem per (d class,
+ * k class) on the current device and keeps the fastest for this process;
+ * with path non-NULL also writes the table there.  Without a table the
+ * batched call uses fixed defaults. */
+sc_status sc_batch_tune(const char *path);
+/* Loads a table written by sc_batch_tune; SC_ERR_INVALID when the file is
+ * not one, is incomplete, or was made on another kind of device. */
+sc_status sc_batch_tune_load(const char *path);
+/* The variant the batched call uses for a problem of d features and k
+ * clusters (centroids per inner pass, rows per work item). */
+sc_status sc_batch_tune_get(int32_t d, int32_t k, int32_t *cu_out, int32_t *rows_out);
+
+/* ------------------------------------------------------------------ */
 /* Brute-force kNN (LinearKNNSearch)                                   */
 /* ------------------------------------------------------------------ */
 typedef struct sc_knn sc_knn;

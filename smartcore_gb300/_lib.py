@@ -44,6 +44,10 @@ SIGNATURES = {
     "sc_kmeans_sync": ([_P], _I32),
     "sc_kmeans_step_noalloc": ([_P, _I32, _I64, _I64, _P, _I64, _P, _P, _P, _P], _I32),
     "sc_kmeans_destroy": ([_P], None),
+    "sc_kmeans_fit_batched": ([_P, _I64, _I32, _I32], _I32),
+    "sc_batch_tune": ([C.c_char_p], _I32),
+    "sc_batch_tune_load": ([C.c_char_p], _I32),
+    "sc_batch_tune_get": ([_I32, _I32, _P, _P], _I32),
     "sc_knn_create": ([_P, _I32, _I32, _I32, _I64, _I64, _I64, _P], _I32),
     "sc_knn_find": ([_P, _P, _I32, _I32, _I64, _I64, _I64, _I32, _I32, _P, _P], _I32),
     "sc_knn_find_radius": ([_P, _P, _I32, _I32, _I64, _I64, _D, _I32, _P, _I64, _P, _P, _P], _I32),
@@ -56,6 +60,16 @@ SIGNATURES = {
     "sc_knn_stats": ([_P, _P], _I32),
     "sc_knn_destroy": ([_P], None),
 }
+
+
+
+class KMeansProblem(C.Structure):
+    """sc_kmeans_problem of include/smartcore_gb300.h."""
+    _fields_ = [("x", _P), ("layout", _I32), ("status", _I32), ("n", _I64), ("d", _I64), ("ld", _I64),
+                ("k", _I64), ("max_iter", _I64), ("first_index", _I64), ("uniforms", _P),
+                ("centroids_out", _P), ("sizes_out", _P), ("labels_out", _P), ("distortion_out", _P),
+                ("iters_out", _P), ("rescored", _I64), ("pp_replays", _I64)]
+
 
 _lib = None
 _lock = threading.Lock()

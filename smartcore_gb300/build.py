@@ -4,8 +4,8 @@
 
 Each source is compiled in parallel with nvcc (one -gencode: compute_103a /
 sm_103a), then linked into smartcore_gb300/_build/libsmartcore_gb300.so.
-exact.cu is compiled with -fmad=false: its kernels reproduce the reference's
-unfused operation order bit for bit.
+exact.cu and batch.cu are compiled with -fmad=false: their FP64 kernels
+reproduce the reference's unfused operation order bit for bit.
 """
 from __future__ import annotations
 
@@ -29,6 +29,7 @@ SOURCES = {
     "split.cu": [],
     "knn_split.cu": [],
     "noalloc.cu": [],
+    "batch.cu": ["-fmad=false"],
     "host_rng.cpp": None,  # host compiler
 }
 

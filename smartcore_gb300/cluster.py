@@ -99,6 +99,53 @@ class KMeans:
                                    _lib.ptr(dist), _lib.ptr(iters)))
         return KMeans(p.k, labels, sizes, float(dist[0]), cent, int(iters[0]), p.form)
 
+    @staticmethod
+    def fit_many(problems, form=_lib.FORM_SPLIT_BF16, stats=None) -> List["KMeans"]:
+        """KMeans::fit for many independent problems in one call
+        (sc_kmeans_fit_batched): `problems` is a list of (x, KMeansParameters),
+        every x of the same element type.  Each result equals KMeans.fit of
+        its problem alone.  `form` serves the problems beyond the batched
+        kernels' limits (d > 64 or k > 128).  With a list `stats`, one
+        (rescored rows, k-means++ replays) pair per problem is appended."""
+        if not problems:
+            return []
+        L = _lib.load()
+        mats = [as_matrix(x) for x, _ in problems]
+        dts = {a.dtype for a in mats}
+        if len(dts) != 1:
+            raise ValueError("every problem of one call must have the same element type")
+        dt = _lib.F32 if mats[0].dtype == np.float32 else _lib.F64
+        arr = (_lib.KMeansProblem * len(problems))()
+        keep = []
+        outs = []
+        for i, ((_, p), a) in enumerate(zip(problems, mats)):
+            p = p or KMeansParameters()
+            n, d = a.shape
+            if p.k < 2:
+                raise Failed(FailedError.FitFailed, f"invalid number of clusters: {p.k}")
+            if p.max_iter == 0:
+                raise Failed(FailedError.FitFailed, f"invalid maximum number of iterations: {p.max_iter}")
+            first, u = kmeanspp_draws(n, p.k, p.seed, p.rng)
+            uu = np.ascontiguousarray(u, np.float64) if len(u) else np.zeros(1)
+            lay, ld = layout_of(a)
+            cent = np.zeros((p.k, d), np.float64)
+            sizes = np.zeros(p.k, np.int64)
+            labels = np.zeros(n, np.int64)
+            dist = np.zeros(1, np.float64)
+            iters = np.zeros(1, np.int64)
+            keep += [a, uu]
+            outs.append((p, cent, sizes, labels, dist, iters))
+            q = arr[i]
+            q.x, q.layout, q.n, q.d, q.ld = a.ctypes.data, lay, n, d, ld
+            q.k, q.max_iter, q.first_index, q.uniforms = p.k, p.max_iter, first, uu.ctypes.data
+            q.centroids_out, q.sizes_out, q.labels_out = cent.ctypes.data, sizes.ctypes.data, labels.ctypes.data
+            q.distortion_out, q.iters_out = dist.ctypes.data, iters.ctypes.data
+        _lib.check(L.sc_kmeans_fit_batched(C.cast(arr, C.c_void_p), len(problems), dt, form))
+        if stats is not None:
+            stats.extend((int(arr[i].rescored), int(arr[i].pp_replays)) for i in range(len(problems)))
+        return [KMeans(p.k, labels, sizes, float(dist[0]), cent, int(iters[0]), form)
+                for p, cent, sizes, labels, dist, iters in outs]
+
     def predict(self, x) -> np.ndarray:
         a = as_matrix(x)
         n, d = a.shape
@@ -147,6 +194,30 @@ class KMeans:
         if self.centroids.shape != other.centroids.shape:
             return False
         return bool(np.all(np.abs(self.centroids - other.centroids) <= np.finfo(np.float64).eps))
+
+
+def batch_tune(path=None, force=False):
+    """Tuning table of the batched assignment kernel on the current device:
+    loaded from `path` when it holds one made on this kind of device, else
+    measured (about a second) and written there.  The default path is in the
+    package's build folder.  Returns the path."""
+    import os
+    from . import build as _build
+    L = _lib.load()
+    path = path or os.path.join(_build.BUILD, "batch_tune.txt")
+    if not force and os.path.exists(path) and L.sc_batch_tune_load(path.encode()) == _lib.SC_OK:
+        return path
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    _lib.check(L.sc_batch_tune(path.encode()))
+    return path
+
+
+def batch_variant(d, k):
+    """(centroids per inner pass, rows per work item) the batched call uses for (d, k)."""
+    L = _lib.load()
+    a = np.zeros(2, np.int32)
+    _lib.check(L.sc_batch_tune_get(d, k, _lib.ptr(a[:1]), _lib.ptr(a[1:])))
+    return int(a[0]), int(a[1])
 
 
 class KMeansHandle:

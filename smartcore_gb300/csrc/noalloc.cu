@@ -57,6 +57,22 @@ struct ScratchAddr {
 };
 ScratchAddr g_addr[kMaxDevices];
 
+// cuCtxGetCurrent through the runtime's driver entry point (the library does
+// not link the driver library itself).
+CUresult current_context(CUcontext *ctx) {
+  using Fn = CUresult (*)(CUcontext *);
+  static Fn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &p, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+      return CUDA_ERROR_NOT_FOUND;
+    fn = (Fn)p;
+  }
+  return fn(ctx);
+}
+
 // Waits for the call's work on the stream before the lock is released, on
 // every return path: a call that fails after its first launch must not leave
 // kernels writing the shared scratch while the next call clears it.
@@ -98,13 +114,13 @@ extern "C" sc_status sc_kmeans_step_noalloc(const void *x, int32_t dtype, int64_
   if (dev < 0 || dev >= kMaxDevices) { set_error("device ordinal %d is not supported", dev); return SC_ERR_INVALID; }
   SC_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   CUcontext ctx = nullptr;
-  if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+  if (current_context(&ctx) != CUDA_SUCCESS) ctx = nullptr;
   if (!ctx || g_addr[dev].ctx != ctx || !g_addr[dev].addr) {
     // Set-up for this device and context.  The lookup also makes the
     // device's primary context current when no context is.
     void *p = nullptr;
     SC_CUDA(cudaGetSymbolAddress(&p, g_scratch));
-    if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS || !ctx) { set_error("no current CUDA context"); return SC_ERR_CUDA; }
+    if (current_context(&ctx) != CUDA_SUCCESS || !ctx) { set_error("no current CUDA context"); return SC_ERR_CUDA; }
     g_addr[dev].ctx = ctx;
     g_addr[dev].addr = (unsigned char *)p;
   }

@@ -66,18 +66,20 @@ def anisotropic_dirichlet_f32(n=1_000_000, d=64, k=256, seed=3, chunk=1 << 17):
     return np.ascontiguousarray(x[p]), lab[p]
 
 
+def batched_problem(p, seed0=0, n_range=(1_000, 100_000), ds=(8, 16, 32, 64), k_range=(4, 64)):
+    """Problem p of the batched k-means workload: n log-uniform in n_range, d
+    from ds, k uniform in k_range, blobs with centres U[-10,10]^d and std
+    U[0.5, 2.0], generated from seed seed0 + p.  Returns (x, k, seed)."""
+    rng = np.random.default_rng(seed0 + p)
+    n = int(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
+    d = int(rng.choice(ds))
+    k = int(rng.integers(k_range[0], k_range[1] + 1))
+    std = float(rng.uniform(0.5, 2.0))
+    x, _ = blobs(n, d, k, seed=seed0 + p + 100_000, dtype=np.float32, std=std)
+    return x, k, seed0 + p
+
+
 def batched_problems(count=512, seed0=0, n_range=(1_000, 100_000), ds=(8, 16, 32, 64),
                      k_range=(4, 64)):
-    """Independent k-means problems: n log-uniform in n_range, d from ds,
-    k uniform in k_range, blobs with centres U[-10,10]^d and per-problem std
-    U[0.5, 2.0]; problem p is generated from seed seed0 + p."""
-    probs = []
-    for p in range(count):
-        rng = np.random.default_rng(seed0 + p)
-        n = int(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
-        d = int(rng.choice(ds))
-        k = int(rng.integers(k_range[0], k_range[1] + 1))
-        std = float(rng.uniform(0.5, 2.0))
-        x, _ = blobs(n, d, k, seed=seed0 + p + 100_000, dtype=np.float32, std=std)
-        probs.append((x, k, seed0 + p))
-    return probs
+    """Independent k-means problems 0 .. count-1 of batched_problem."""
+    return [batched_problem(p, seed0, n_range, ds, k_range) for p in range(count)]

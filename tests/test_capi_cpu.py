@@ -99,3 +99,30 @@ def test_null_handles_rejected_before_any_device_call(L):
     assert L.sc_fastpair(None, _lib.ptr(out), _lib.ptr(dist), None, None) == _lib.SC_ERR_INVALID
     assert L.sc_knn_find_radius(None, None, 0, 0, 0, 0, 1.0, 1, None, 0, None, None, None) == _lib.SC_ERR_INVALID
     assert "null handle" in _lib.last_error()
+
+
+def test_batched_validation_before_any_device_call(L):
+    """sc_kmeans_fit_batched validates every problem first, with KMeans::fit's
+    messages prefixed by the problem's index; an empty batch is a no-op."""
+    x = np.zeros((5, 2))
+    u = np.zeros(4)
+    arr = (_lib.KMeansProblem * 2)()
+    for i, k in enumerate((3, 1)):
+        q = arr[i]
+        q.x, q.layout, q.n, q.d, q.ld = x.ctypes.data, _lib.ROW_MAJOR, 5, 2, 2
+        q.k, q.max_iter, q.first_index, q.uniforms = k, 10, 0, u.ctypes.data
+    rc = L.sc_kmeans_fit_batched(C.cast(arr, C.c_void_p), 2, _lib.F64, _lib.FORM_FP64)
+    assert rc == _lib.SC_ERR_INVALID
+    assert _lib.last_error() == "problem 1: invalid number of clusters: 1"
+    arr[1].k, arr[1].max_iter = 2, 0
+    assert L.sc_kmeans_fit_batched(C.cast(arr, C.c_void_p), 2, _lib.F64, _lib.FORM_FP64) == _lib.SC_ERR_INVALID
+    assert _lib.last_error() == "problem 1: invalid maximum number of iterations: 0"
+    assert L.sc_kmeans_fit_batched(None, 0, _lib.F32, _lib.FORM_FP64) == _lib.SC_OK
+
+
+def test_batch_tune_rejects_foreign_files(L, tmp_path):
+    p = tmp_path / "t.txt"
+    p.write_text("not a table\n")
+    assert L.sc_batch_tune_load(str(p).encode()) == _lib.SC_ERR_INVALID
+    assert L.sc_batch_tune_load(str(tmp_path / "missing.txt").encode()) == _lib.SC_ERR_INVALID
+    assert L.sc_batch_tune_get(200, 5, None, None) == _lib.SC_ERR_INVALID

@@ -1,0 +1,135 @@
+"""GPU parity of the batched KMeans::fit (sc_kmeans_fit_batched) against the
+CPU oracle and against single-problem fits.
+
+Bar, per problem: labels, sizes and iteration count equal to the oracle's
+KMeans::fit (src/cluster/kmeans.rs:254-323), centroids within 1e-12
+relative, distortion within 1e-12 relative plus the identity's cancellation
+term 1e-14 sum ||x||^2 (the batched distortion is sum ||x||^2 - 2 c.S +
+n ||c||^2 from exact sums).
+"""
+import multiprocessing as mp
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle
+from smartcore_gb300 import _lib
+from smartcore_gb300.cluster import KMeans, KMeansParameters, batch_tune, batch_variant
+from tests.datagen import batched_problems, blobs
+from tests.oracle_jobs import fit_batched_problem
+
+pytestmark = pytest.mark.gpu
+
+CENT_RTOL = 1e-12
+
+
+def rel_err(a, b):
+    scale = np.maximum(np.abs(b).max(axis=-1, keepdims=True), 1e-300)
+    with np.errstate(invalid="ignore"):
+        e = np.abs(a - b) / scale
+    both_nan = np.isnan(a) & np.isnan(b)
+    return float(np.where(both_nan, 0.0, e).max())
+
+
+def check_against_oracle(x, km, labels, sizes, cent, iters, dist):
+    assert np.array_equal(km._y, labels)
+    assert np.array_equal(km.size, sizes)
+    assert km.iters == iters
+    assert rel_err(km.centroids, cent) <= CENT_RTOL
+    xx = float((np.asarray(x, np.float64) ** 2).sum())
+    assert abs(km._distortion - dist) <= 1e-12 * abs(dist) + 1e-14 * xx
+
+
+def test_512_problems_match_oracle():
+    """The batched k-means workload (512 problems, n log-uniform in [1e3,
+    1e5], d in {8, 16, 32, 64}, k in [4, 64], max_iter 30) in one call, every
+    problem against the oracle (a spawn pool of CPU workers)."""
+    count, max_iter = 512, 30
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(16, os.cpu_count() or 1)) as pool:
+        jobs = pool.imap_unordered(fit_batched_problem, [(i, count, max_iter) for i in range(count)], chunksize=4)
+        probs = batched_problems(count=count)
+        stats = []
+        fits = KMeans.fit_many([(x, KMeansParameters(k=k, max_iter=max_iter, seed=s)) for x, k, s in probs],
+                               stats=stats)
+        for i, labels, sizes, cent, iters, dist in jobs:
+            check_against_oracle(probs[i][0], fits[i], labels, sizes, cent, iters, dist)
+    assert sum(r for r, _ in stats) < 0.01 * sum(len(p[0]) for p in probs) * max_iter
+
+
+def test_batched_equals_single_fits():
+    """Each problem's result equals KMeans.fit of that problem alone (FP64
+    form): labels, sizes, iterations; centroids to the rounding of the sums."""
+    probs = batched_problems(count=24, seed0=900)
+    fits = KMeans.fit_many([(x, KMeansParameters(k=k, max_iter=40, seed=s)) for x, k, s in probs])
+    for (x, k, s), km in zip(probs, fits):
+        one = KMeans.fit(x, KMeansParameters(k=k, max_iter=40, seed=s, form=_lib.FORM_FP64))
+        assert np.array_equal(km._y, one._y)
+        assert np.array_equal(km.size, one.size)
+        assert km.iters == one.iters
+        assert rel_err(km.centroids, one.centroids) <= 1e-14
+
+
+def edge_problems(dtype):
+    rng = np.random.default_rng(5)
+    out = []
+    for n, d, k, it, seed in [(500, 1, 2, 50, 1), (777, 3, 5, 30, 2), (1500, 5, 17, 30, 3), (2049, 13, 33, 20, 4),
+                              (900, 50, 100, 15, 5), (4100, 64, 128, 10, 6), (300, 7, 64, 25, 7),
+                              (3000, 16, 2, 1, 8), (5000, 8, 9, 100, 9)]:
+        x, _ = blobs(n, d, max(2, k // 2), seed=seed, dtype=dtype)
+        out.append((x, KMeansParameters(k=k, max_iter=it, seed=seed)))
+    # duplicated points: k-means++ picks equal rows, empty clusters keep NaN centroids
+    base = rng.normal(size=(6, 4)).astype(dtype)
+    out.append((np.ascontiguousarray(np.repeat(base, 50, axis=0)), KMeansParameters(k=9, max_iter=20, seed=11)))
+    # k = n
+    xs, _ = blobs(12, 6, 3, seed=12, dtype=dtype)
+    out.append((xs, KMeansParameters(k=12, max_iter=10, seed=12)))
+    # column-major
+    xf, _ = blobs(1200, 10, 6, seed=13, dtype=dtype)
+    out.append((np.asfortranarray(xf), KMeansParameters(k=6, max_iter=30, seed=13)))
+    # beyond the batched kernels' limits: served one by one
+    xw, _ = blobs(800, 100, 5, seed=14, dtype=dtype)
+    out.append((xw, KMeansParameters(k=5, max_iter=20, seed=14)))
+    xk, _ = blobs(1000, 4, 80, seed=15, dtype=dtype)
+    out.append((xk, KMeansParameters(k=200, max_iter=10, seed=15)))
+    return out
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_edge_problems_match_oracle(dtype):
+    probs = edge_problems(dtype)
+    fits = KMeans.fit_many(probs)
+    for (x, p), km in zip(probs, fits):
+        r = oracle.kmeans_fit(x, p.k, p.max_iter, seed=p.seed)
+        check_against_oracle(x, km, r.labels, r.sizes, r.centroids, r.iters, r.distortion)
+
+
+def test_validation_writes_nothing():
+    x, _ = blobs(100, 4, 3, seed=1, dtype=np.float32)
+    from smartcore_gb300.error import Failed
+    with pytest.raises(Failed) as e:
+        KMeans.fit_many([(x, KMeansParameters(k=3)), (x, KMeansParameters(k=1))])
+    assert "invalid number of clusters: 1" in str(e.value)
+
+
+def test_tuner_table_round_trip():
+    """The tuner measures every (d class, k class), writes its table, and a
+    load of that file gives the same choices; the batched fit then uses them."""
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "tune.txt")
+        batch_tune(path, force=True)
+        chosen = {(d, k): batch_variant(d, k) for d in (8, 16, 32, 64) for k in (8, 16, 32, 64, 128)}
+        for cu, rows in chosen.values():
+            assert cu in (2, 4, 8) and rows in (1024, 2048, 4096)
+        with open(path) as f:
+            lines = f.read().splitlines()
+        assert lines[0].startswith("smartcore_gb300") and len(lines) == 22
+        batch_tune(path)  # loads the file
+        assert {(d, k): batch_variant(d, k) for d, k in chosen} == chosen
+    probs = batched_problems(count=6, seed0=50)
+    fits = KMeans.fit_many([(x, KMeansParameters(k=k, max_iter=30, seed=s)) for x, k, s in probs])
+    for (x, k, s), km in zip(probs, fits):
+        r = oracle.kmeans_fit(x, k, 30, seed=s)
+        check_against_oracle(x, km, r.labels, r.sizes, r.centroids, r.iters, r.distortion)
