@@ -250,6 +250,9 @@ sc_status sc_kmeans_create(const void *x, int32_t dtype, int32_t layout, int32_t
   SC_TRY(check_matrix(x, dtype, layout, mem, n, d, ld));
   if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
   if (n > ((int64_t)1 << 40)) { set_error("n=%lld is too large", (long long)n); return SC_ERR_INVALID; }
+  // the split-BF16 k-means kernels serve rows of up to 128 features; wider
+  // data runs the FP64 form, whose results are the same
+  if (form == SC_FORM_SPLIT_BF16 && d > kSplitKMeansMaxD) form = SC_FORM_FP64;
   sc_kmeans *h = new sc_kmeans();
   h->dtype = dtype; h->form = form; h->n = n; h->d = d;
   sc_status r = SC_OK;
@@ -486,7 +489,7 @@ sc_status sc_kmeans_predict(const void *x, int32_t dtype, int32_t layout, int64_
   SC_TRY(sc_kmeans_create(x, dtype, layout, SC_MEM_HOST, n, d, ld, form, &h));
   sc_status r = sc_kmeans_set_centroids(h, k, centroids);
   if (r == SC_OK) {
-    if (form == SC_FORM_FP64)
+    if (h->form == SC_FORM_FP64)
       r = launch_assign_fp64(h->dtype, h->x, h->n, (int)h->d, h->cent, (int)k, h->labels, nullptr, nullptr, h->stream);
     else
       r = split_assign(&h->split, h->dtype, h->x, h->n, (int)h->d, h->cent, (int)k, h->labels, h->st, h->stream);
@@ -540,8 +543,10 @@ static sc_status knn_run(sc_knn *h, const void *queries, int32_t layout, int32_t
     set_error("k should be >= 1 and <= length(data)");
     return SC_ERR_INVALID;
   }
-  if (k > kMaxKnnK) { set_error("k=%lld exceeds the supported maximum %d", (long long)k, kMaxKnnK); return SC_ERR_INVALID; }
+  if (k > (1 << 24)) { set_error("k=%lld is too large", (long long)k); return SC_ERR_INVALID; }
   if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
+  // beyond the split kernel's heaps and tiles the FP64 kernel serves the call (same results)
+  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, (int)k)) form = SC_FORM_FP64;
   SC_TRY(knn_reserve(h, m, k));
   SC_TRY(upload_matrix(queries, h->dtype, layout, mem, m, h->d, ld, h->q, h->stream));
   if (form == SC_FORM_FP64)
@@ -618,6 +623,7 @@ sc_status sc_knn_find(sc_knn *h, const void *queries, int32_t layout, int32_t me
 // query rows (row-major), in index order: CSR lists off (m + 1) and idx.
 static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double radius, int32_t form,
                               std::vector<int64_t> &off, std::vector<int64_t> &idx) {
+  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, 1)) form = SC_FORM_FP64;
   off.assign((size_t)m + 1, 0);
   idx.clear();
   if (m == 0) return SC_OK;
@@ -801,6 +807,7 @@ sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout, int
   if (!(radius > 0.0)) { set_error("radius should be > 0"); return SC_ERR_INVALID; }  // linear_search.rs:90-95
   SC_TRY(check_matrix(queries, h->dtype, layout, mem, m, h->d, ld));
   if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
+  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, 1)) form = SC_FORM_FP64;
   if (total_out) *total_out = 0;
   if (m == 0) return SC_OK;
   SC_TRY(knn_reserve(h, m, 1));

@@ -766,49 +766,65 @@ __device__ __forceinline__ void heap_heapify(double *hd, int32_t *hi, int k, int
   for (int s = k / 2 - 1; s >= 0; --s) heap_sift_down(hd, hi, s, k - 1, stride);
 }
 
-template <typename T>
+// SHQ: the block's queries (transposed) and each training tile are staged in
+// shared memory (else read from global memory, for wide rows).  SHH: the
+// heaps live in shared memory (else in global memory, slot s of local query
+// t at gh*[s * gstride + t], for large k).
+template <typename T, bool SHQ, bool SHH>
 __global__ void knn_fp64_kernel(const T *__restrict__ train, int64_t n, int d,
                                 const T *__restrict__ queries, int64_t m, int k,
                                 int64_t *__restrict__ idx_out,
-                                double *__restrict__ dist_out) {
+                                double *__restrict__ dist_out,
+                                double *__restrict__ ghd, int32_t *__restrict__ ghi, int64_t gstride) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nt = blockDim.x;
-  double *hd = reinterpret_cast<double *>(smraw);                // k x nt
-  int32_t *hi = reinterpret_cast<int32_t *>(hd + (size_t)k * nt);  // k x nt
-  T *qs = reinterpret_cast<T *>(hi + (size_t)k * nt + ((k * nt) & 1));  // d x nt
-  T *ts = qs + (size_t)d * nt;                                   // kKnnTile x d
+  double *hd = reinterpret_cast<double *>(smraw);                          // k x nt (SHH)
+  int32_t *hi = reinterpret_cast<int32_t *>(hd + (SHH ? (size_t)k * nt : 0));  // k x nt (SHH)
+  T *qs = reinterpret_cast<T *>(hi + (SHH ? (size_t)k * nt + ((k * nt) & 1) : 0));  // d x nt (SHQ)
+  T *ts = qs + (SHQ ? (size_t)d * nt : 0);                                  // kKnnTile x d (SHQ)
   const int tid = threadIdx.x;
   const int64_t q = (int64_t)blockIdx.x * nt + tid;
   const bool live = q < m;
-  for (int j = 0; j < d; ++j) qs[j * nt + tid] = live ? queries[q * d + j] : T(0);
-  for (int s = 0; s < k; ++s) {
-    hd[s * nt + tid] = __longlong_as_double(0x7ff0000000000000ll);  // +inf
-    hi[s * nt + tid] = -1;
-  }
-  double *mh = hd + tid;
-  int32_t *mi = hi + tid;
+  if (SHQ)
+    for (int j = 0; j < d; ++j) qs[j * nt + tid] = live ? queries[q * d + j] : T(0);
+  double *mh = SHH ? hd + tid : ghd + (live ? q : 0);
+  int32_t *mi = SHH ? hi + tid : ghi + (live ? q : 0);
+  const int hs = SHH ? nt : (int)gstride;
+  if (SHH || live)
+    for (int s = 0; s < k; ++s) {
+      mh[s * hs] = __longlong_as_double(0x7ff0000000000000ll);  // +inf
+      mi[s * hs] = -1;
+    }
+  const T *qg = queries + (live ? q : 0) * d;
   for (int64_t r0 = 0; r0 < n; r0 += kKnnTile) {
     const int rt = (int)min((int64_t)kKnnTile, n - r0);
-    __syncthreads();
-    for (int t = tid; t < rt * d; t += nt) ts[t] = train[r0 * d + t];
-    __syncthreads();
+    if (SHQ) {
+      __syncthreads();
+      for (int t = tid; t < rt * d; t += nt) ts[t] = train[r0 * d + t];
+      __syncthreads();
+    }
     if (!live) continue;
     for (int r = 0; r < rt; ++r) {
-      const T *tr = ts + r * d;
       double s = 0.0;
-      for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term(qs[j * nt + tid], tr[j]));
+      if (SHQ) {
+        const T *tr = ts + r * d;
+        for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term(qs[j * nt + tid], tr[j]));
+      } else {
+        const T *tr = train + (r0 + r) * d;
+        for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term(qg[j], tr[j]));
+      }
       const double dist = __dsqrt_rn(s);
       if (dist < mh[0]) {
         mh[0] = dist;
         mi[0] = (int32_t)(r0 + r);
-        heap_heapify(mh, mi, k, nt);
+        heap_heapify(mh, mi, k, hs);
       }
     }
   }
   if (!live) return;
   for (int s = 0; s < k; ++s) {
-    idx_out[q * k + s] = mi[s * nt];
-    dist_out[q * k + s] = mh[s * nt];
+    idx_out[q * k + s] = mi[s * hs];
+    dist_out[q * k + s] = mh[s * hs];
   }
 }
 
@@ -904,33 +920,57 @@ sc_status launch_fastpair(int dtype, const void *x, int64_t n, int d, int64_t *n
   return SC_OK;
 }
 
+template <typename T, bool SHQ, bool SHH>
+static sc_status knn_fp64_launch(const T *train, int64_t n, int d, const T *queries, int64_t m, int k,
+                                 int64_t *idx, double *dist, int nt, size_t smem, double *ghd, int32_t *ghi,
+                                 int64_t gstride, cudaStream_t s) {
+  auto kern = knn_fp64_kernel<T, SHQ, SHH>;
+  SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)((m + nt - 1) / nt), nt, smem, s>>>(train, n, d, queries, m, k, idx, dist, ghd, ghi, gstride);
+  SC_LAUNCHED();
+  return SC_OK;
+}
+
+template <typename T>
+static sc_status knn_fp64_typed(const T *train, int64_t n, int d, const T *queries, int64_t m, int k,
+                                int64_t *idx, double *dist, cudaStream_t s) {
+  constexpr size_t es = sizeof(T), kLimit = 200 * 1024;
+  const size_t rows = (size_t)kKnnTile * d * es + 16;
+  // everything in shared memory, widest block first
+  for (int nt = 128; nt >= 32; nt >>= 1) {
+    const size_t smem = (size_t)k * nt * 12 + 8 + (size_t)d * nt * es + rows;
+    if (smem <= kLimit) return knn_fp64_launch<T, true, true>(train, n, d, queries, m, k, idx, dist, nt, smem,
+                                                               nullptr, nullptr, 0, s);
+  }
+  // Heaps in global memory, queries in chunks of bounded heap storage.
+  const bool shq = (size_t)d * 64 * es + rows <= kLimit;
+  const int nt = shq ? 64 : 128;
+  const size_t smem = shq ? (size_t)d * nt * es + rows : 0;
+  int64_t chunk = std::max<int64_t>(nt, (int64_t)(((size_t)256 << 20) / ((size_t)k * 12)) / nt * nt);
+  chunk = std::min<int64_t>(chunk, (m + nt - 1) / nt * nt);
+  double *ghd = nullptr;
+  int32_t *ghi = nullptr;
+  SC_TRY(dalloc(&ghd, (size_t)chunk * k, s));
+  sc_status r = dalloc(&ghi, (size_t)chunk * k, s);
+  for (int64_t q0 = 0; r == SC_OK && q0 < m; q0 += chunk) {
+    const int64_t mc = std::min(chunk, m - q0);
+    r = shq ? knn_fp64_launch<T, true, false>(train, n, d, queries + q0 * d, mc, k, idx + q0 * k, dist + q0 * k, nt,
+                                              smem, ghd, ghi, chunk, s)
+            : knn_fp64_launch<T, false, false>(train, n, d, queries + q0 * d, mc, k, idx + q0 * k, dist + q0 * k,
+                                               nt, 0, ghd, ghi, chunk, s);
+  }
+  dfree(ghd, s);
+  dfree(ghi, s);
+  return r;
+}
+
 sc_status launch_knn_fp64(int dtype, const void *train, int64_t n, int d,
                           const void *queries, int64_t m, int k, int64_t *idx,
                           double *dist, cudaStream_t s) {
   if (m == 0) return SC_OK;
-  const int es = dtype == SC_F32 ? 4 : 8;
-  int nt = 128;
-  size_t smem = 0;
-  for (; nt >= 32; nt >>= 1) {
-    smem = (size_t)k * nt * 12 + 8 + (size_t)d * nt * es + (size_t)kKnnTile * d * es + 16;
-    if (smem <= 200 * 1024) break;
-  }
-  if (nt < 32) {
-    set_error("d=%d, k=%d exceed the FP64 kNN kernel's shared memory", d, k);
-    return SC_ERR_INVALID;
-  }
-  const int grid = (int)((m + nt - 1) / nt);
-  if (dtype == SC_F32) {
-    auto kern = knn_fp64_kernel<float>;
-    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, nt, smem, s>>>((const float *)train, n, d, (const float *)queries, m, k, idx, dist);
-  } else {
-    auto kern = knn_fp64_kernel<double>;
-    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, nt, smem, s>>>((const double *)train, n, d, (const double *)queries, m, k, idx, dist);
-  }
-  SC_LAUNCHED();
-  return SC_OK;
+  if (dtype == SC_F32)
+    return knn_fp64_typed<float>((const float *)train, n, d, (const float *)queries, m, k, idx, dist, s);
+  return knn_fp64_typed<double>((const double *)train, n, d, (const double *)queries, m, k, idx, dist, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1031,16 +1071,28 @@ __device__ __forceinline__ int knn_weights(const int64_t *qi, const double *qd,
   return c;
 }
 
+// Per-query work arrays of the aggregation: in local memory for k <= 64,
+// else slices of a global scratch (k entries per query of the launch).
+struct VoteScratch {
+  double *w = nullptr, *cv = nullptr;
+  int *pos = nullptr;
+  int64_t *cls = nullptr;
+};
+
+template <bool LOCAL>
 __global__ void knn_vote_kernel(const int64_t *__restrict__ idx,
                                 const double *__restrict__ dist, int64_t m,
                                 int k, int weight,
                                 const int64_t *__restrict__ y_class,
-                                int64_t *__restrict__ out) {
+                                int64_t *__restrict__ out, VoteScratch sc) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= m) return;
-  double w[kMaxKnnK], cv[kMaxKnnK];
-  int pos[kMaxKnnK];
-  int64_t cls[kMaxKnnK];
+  double wl[LOCAL ? kMaxKnnK : 1], cvl[LOCAL ? kMaxKnnK : 1];
+  int posl[LOCAL ? kMaxKnnK : 1];
+  int64_t clsl[LOCAL ? kMaxKnnK : 1];
+  double *w = LOCAL ? wl : sc.w + q * k, *cv = LOCAL ? cvl : sc.cv + q * k;
+  int *pos = LOCAL ? posl : sc.pos + q * k;
+  int64_t *cls = LOCAL ? clsl : sc.cls + q * k;
   const int c = knn_weights(idx + q * k, dist + q * k, k, weight, w, pos);
   double w_sum = 0.0;
   for (int t = 0; t < c; ++t) w_sum = __dadd_rn(w_sum, w[t]);
@@ -1059,15 +1111,18 @@ __global__ void knn_vote_kernel(const int64_t *__restrict__ idx,
 }
 
 // KNNRegressor::predict_for_row (src/neighbors/knn_regressor.rs:268-282).
+template <bool LOCAL>
 __global__ void knn_regress_kernel(const int64_t *__restrict__ idx,
                                    const double *__restrict__ dist, int64_t m,
                                    int k, int weight,
                                    const double *__restrict__ y,
-                                   double *__restrict__ out) {
+                                   double *__restrict__ out, VoteScratch sc) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= m) return;
-  double w[kMaxKnnK];
-  int pos[kMaxKnnK];
+  double wl[LOCAL ? kMaxKnnK : 1];
+  int posl[LOCAL ? kMaxKnnK : 1];
+  double *w = LOCAL ? wl : sc.w + q * k;
+  int *pos = LOCAL ? posl : sc.pos + q * k;
   const int c = knn_weights(idx + q * k, dist + q * k, k, weight, w, pos);
   double w_sum = 0.0;
   for (int t = 0; t < c; ++t) w_sum = __dadd_rn(w_sum, w[t]);
@@ -1091,22 +1146,63 @@ sc_status launch_widen_labels(const int32_t *in, int64_t *out, int64_t n, cudaSt
   return SC_OK;
 }
 
+// Queries per launch of the scratch form: at most 256 MB of work arrays.
+static int64_t vote_chunk(int64_t m, int k) {
+  return std::min<int64_t>(m, std::max<int64_t>(128, (int64_t)(((size_t)256 << 20) / ((size_t)k * 28))));
+}
+
 sc_status launch_knn_vote(const int64_t *idx, const double *dist, int64_t m,
                           int k, int weight, const int64_t *y_class,
                           int64_t *out, cudaStream_t s) {
   if (m == 0) return SC_OK;
-  knn_vote_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(idx, dist, m, k, weight, y_class, out);
-  SC_LAUNCHED();
-  return SC_OK;
+  if (k <= kMaxKnnK) {
+    knn_vote_kernel<true><<<(unsigned)((m + 127) / 128), 128, 0, s>>>(idx, dist, m, k, weight, y_class, out,
+                                                                       VoteScratch());
+    SC_LAUNCHED();
+    return SC_OK;
+  }
+  const int64_t chunk = vote_chunk(m, k);
+  VoteScratch sc;
+  sc_status r = dalloc(&sc.w, (size_t)chunk * k, s);
+  if (r == SC_OK) r = dalloc(&sc.cv, (size_t)chunk * k, s);
+  if (r == SC_OK) r = dalloc(&sc.pos, (size_t)chunk * k, s);
+  if (r == SC_OK) r = dalloc(&sc.cls, (size_t)chunk * k, s);
+  for (int64_t q0 = 0; r == SC_OK && q0 < m; q0 += chunk) {
+    const int64_t mc = std::min(chunk, m - q0);
+    knn_vote_kernel<false><<<(unsigned)((mc + 127) / 128), 128, 0, s>>>(idx + q0 * k, dist + q0 * k, mc, k, weight,
+                                                                         y_class, out + q0, sc);
+    note_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) r = cuda_fail(e, "knn_vote_kernel");
+  }
+  dfree(sc.w, s); dfree(sc.cv, s); dfree(sc.pos, s); dfree(sc.cls, s);
+  return r;
 }
 
 sc_status launch_knn_regress(const int64_t *idx, const double *dist,
                              int64_t m, int k, int weight, const double *y,
                              double *out, cudaStream_t s) {
   if (m == 0) return SC_OK;
-  knn_regress_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(idx, dist, m, k, weight, y, out);
-  SC_LAUNCHED();
-  return SC_OK;
+  if (k <= kMaxKnnK) {
+    knn_regress_kernel<true><<<(unsigned)((m + 127) / 128), 128, 0, s>>>(idx, dist, m, k, weight, y, out,
+                                                                         VoteScratch());
+    SC_LAUNCHED();
+    return SC_OK;
+  }
+  const int64_t chunk = vote_chunk(m, k);
+  VoteScratch sc;
+  sc_status r = dalloc(&sc.w, (size_t)chunk * k, s);
+  if (r == SC_OK) r = dalloc(&sc.pos, (size_t)chunk * k, s);
+  for (int64_t q0 = 0; r == SC_OK && q0 < m; q0 += chunk) {
+    const int64_t mc = std::min(chunk, m - q0);
+    knn_regress_kernel<false><<<(unsigned)((mc + 127) / 128), 128, 0, s>>>(idx + q0 * k, dist + q0 * k, mc, k,
+                                                                           weight, y, out + q0, sc);
+    note_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) r = cuda_fail(e, "knn_regress_kernel");
+  }
+  dfree(sc.w, s); dfree(sc.pos, s);
+  return r;
 }
 
 }  // namespace sc

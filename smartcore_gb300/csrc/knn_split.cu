@@ -797,6 +797,14 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
 
 }  // namespace
 
+bool split_knn_serves(int d, int k) {
+  const int d_pad = knn_pad_d(d);
+  if (d_pad > 256 || k > kMaxKnnK) return false;
+  const int kt = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt, rb = kt * 2, tn = knn_tile_n(d_pad);
+  const bool sh = knn_smem(nkt, rb, 2, tn, k) <= 227 * 1024;
+  return knn_smem(nkt, rb, 2, tn, sh ? k : 0) <= 227 * 1024;
+}
+
 sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
                     int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, cudaStream_t st) {
   return run_split_knn(s, dtype, train, n, d, queries, m, k, idx, dist, rescored, nullptr, st);

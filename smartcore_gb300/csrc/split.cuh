@@ -62,6 +62,12 @@ void split_free(SplitState *s, cudaStream_t st);
 sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
                     const void *queries, int64_t m, int k, int64_t *idx, double *dist,
                     int64_t *rescored, cudaStream_t st);
+// Whether the split-BF16 kNN kernel serves d features and k neighbours (its
+// heaps hold at most 64 entries, its tiles at most 256 features); the entry
+// points run the FP64 kernels, with the same results, otherwise.
+bool split_knn_serves(int d, int k);
+// Widest rows the split-BF16 k-means kernels serve.
+constexpr int kSplitKMeansMaxD = 128;
 // find_radius: counting pass when idx is null (counts[q]), else filling pass
 // (query q's rows from offsets[q] on); every pointer is device memory.
 sc_status split_knn_radius(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,

@@ -90,9 +90,8 @@ def test_bbdtree_iris_step(kats):
 @pytest.mark.parametrize("n,d,c,k", [(20_000, 8, 16, 16), (30_000, 7, 40, 48), (20_000, 64, 64, 64),
                                      (9_000, 100, 30, 40), (5_000, 200, 8, 12), (3_001, 1, 5, 9)])
 def test_kmeanspp_labels(form, dtype, n, d, c, k):
-    # the split form's update also bounds rows through their BF16 high halves
-    if form == _lib.FORM_SPLIT_BF16 and d > 128:
-        pytest.skip("the split form's tiles hold d <= 128")
+    # the split form's update also bounds rows through their BF16 high halves;
+    # a split-form handle of d > 128 runs the FP64 form
     x, _ = blobs(n, d, c, seed=12, dtype=dtype)
     first, u = kmeanspp_draws(len(x), k, 5)
     h = KMeansHandle(x, form=form)
@@ -232,3 +231,13 @@ def test_serde_round_trip(kats, form):
     back = KMeans.from_json(text, form=form)
     assert back == km
     assert np.array_equal(back.predict(x), km.predict(x))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_split_form_wide_rows_fit(dtype):
+    """KMeans::fit on d = 200 asked for in the split form: rows wider than its
+    128-feature tiles run the FP64 form, with the oracle's results."""
+    x, _ = blobs(4000, 200, 10, seed=21, dtype=dtype)
+    assert_fit_parity(x, 10, 30, 3, _lib.FORM_SPLIT_BF16)
+    km = KMeans.fit(x, KMeansParameters(k=10, max_iter=30, seed=3, form=_lib.FORM_SPLIT_BF16))
+    assert np.array_equal(km.predict(x), km._y)

@@ -174,3 +174,54 @@ def test_regressor_matches_oracle(weight):
     got = m.predict(xq)
     idx, dist = oracle.knn_find(xt, xq, 4)
     assert np.array_equal(got, oracle.knn_regress(idx, dist, y, weight=weight))
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("k", [65, 100, 700])
+def test_find_large_k(form, dtype, k):
+    """LinearKNNSearch::find accepts any 1 <= k <= n (linear_search.rs:53-58):
+    k beyond the split kernel's 64-entry heaps runs the FP64 kernel (shared-
+    memory heaps up to its limit, then heaps in global memory)."""
+    rng = np.random.default_rng(k)
+    train = rng.normal(size=(2500, 9)).astype(dtype)
+    q = rng.normal(size=(150, 9)).astype(dtype)
+    s = LinearKNNSearch(train, form=form)
+    idx, dist = s.find_batch(q, k)
+    ridx, rdist = oracle.knn_find(train, q, k)
+    assert np.array_equal(idx, ridx)
+    assert np.array_equal(dist, rdist)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("d", [200, 1000])
+def test_find_wide_rows(form, d):
+    """Rows wider than the split kernel's 256-feature tiles (and, at d = 1000,
+    wider than the FP64 kernel's shared-memory staging) are served."""
+    rng = np.random.default_rng(d)
+    train = rng.normal(size=(1500, d)).astype(np.float32)
+    q = rng.normal(size=(64, d)).astype(np.float32)
+    s = LinearKNNSearch(train, form=form)
+    idx, dist = s.find_batch(q, 100)
+    ridx, rdist = oracle.knn_find(train, q, 100)
+    assert np.array_equal(idx, ridx)
+    assert np.array_equal(dist, rdist)
+    counts, ridxs, _ = s.find_radius_batch(q, float(np.median(rdist)))
+    rc, rr, _ = oracle.knn_find_radius(train, q, float(np.median(rdist)))
+    assert np.array_equal(counts, rc) and np.array_equal(ridxs, rr)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("weight", [0, 1])
+def test_classifier_regressor_large_k(form, weight):
+    """Vote and regression over 100 neighbours (the aggregation's work arrays
+    in global memory)."""
+    xt, yt, xq, _ = knn_blobs_f32(n_train=4000, n_query=300, d=8, classes=6, seed=3)
+    m = KNNClassifier.fit(xt, yt, KNNClassifierParameters(k=100, algorithm=KNNAlgorithmName.LinearSearch,
+                                                         weight=KNNWeightFunction(weight), form=form))
+    idx, dist = oracle.knn_find(xt, xq, 100)
+    assert np.array_equal(m.predict(xq), oracle.knn_vote(idx, dist, yt, 6, weight=weight))
+    yr = yt.astype(np.float64) * 0.5
+    r = KNNRegressor.fit(xt, yr, KNNRegressorParameters(k=100, algorithm=KNNAlgorithmName.LinearSearch,
+                                                        weight=KNNWeightFunction(weight), form=form))
+    assert np.array_equal(r.predict(xq), oracle.knn_regress(idx, dist, yr, weight=weight))
