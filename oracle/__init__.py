@@ -50,6 +50,11 @@ def lib():
             P, I64, D, I = C.c_void_p, C.c_int64, C.c_double, C.c_int
             L.orc_kmeanspp_draws.argtypes = [I, C.c_uint64, I64, I64, P, P]
             L.orc_rng_u64.argtypes = [I, C.c_uint64, I64, P]
+            L.orc_xoshiro256pp.argtypes = [P, I64, P]
+            L.orc_splitmix64.argtypes = [C.c_uint64, I64, P]
+            L.orc_chacha_block.argtypes = [P, P, I, P]
+            L.orc_chacha_quarter_round.argtypes = [P]
+            L.orc_pcg32.argtypes = [C.c_uint64, C.c_uint64, I, I64, P]
             L.orc_sqdist.argtypes = [I, P, P, I64]
             L.orc_sqdist.restype = D
             L.orc_kmeans_fit.argtypes = [I, I, P, I64, I64, I64, I64, I64, I64, P, P, P, P, P, P, P]
@@ -107,6 +112,42 @@ def kmeanspp_draws(n, k, seed=0, rng=RNG_SMALL):
 def rng_u64(count, seed=0, rng=RNG_SMALL):
     out = np.zeros(count, np.uint64)
     lib().orc_rng_u64(rng, C.c_uint64(seed), count, _ptr(out))
+    return out
+
+
+def xoshiro256pp(state, count):
+    """count outputs of xoshiro256++ from the 4-word state."""
+    st = np.ascontiguousarray(state, np.uint64)
+    out = np.zeros(count, np.uint64)
+    lib().orc_xoshiro256pp(_ptr(st), count, _ptr(out))
+    return out
+
+
+def splitmix64(seed, count):
+    out = np.zeros(count, np.uint64)
+    lib().orc_splitmix64(C.c_uint64(seed), count, _ptr(out))
+    return out
+
+
+def chacha_block(key, words12_15, rounds):
+    """The ChaCha block function: 16 output words of the given key (8 words),
+    words 12..15 (counter / nonce) and round count."""
+    k = np.ascontiguousarray(key, np.uint32)
+    w = np.ascontiguousarray(words12_15, np.uint32)
+    out = np.zeros(16, np.uint32)
+    lib().orc_chacha_block(_ptr(k), _ptr(w), rounds, _ptr(out))
+    return out
+
+
+def chacha_quarter_round(a, b, c, d):
+    v = np.array([a, b, c, d], np.uint32)
+    lib().orc_chacha_quarter_round(_ptr(v))
+    return [int(t) for t in v]
+
+
+def pcg32(state, inc, count, after_step=False):
+    out = np.zeros(count, np.uint32)
+    lib().orc_pcg32(C.c_uint64(state), C.c_uint64(inc), 1 if after_step else 0, count, _ptr(out))
     return out
 
 

@@ -38,6 +38,13 @@ void orc_kmeanspp_draws(int rng_kind, uint64_t seed, int64_t n, int64_t k,
                         int64_t *first_index, double *uniforms /* k-1 */);
 /* Raw next_u64 stream, for cross-checking two independent restatements. */
 void orc_rng_u64(int rng_kind, uint64_t seed, int64_t count, uint64_t *out);
+/* The primitives under the draws, exposed to be checked one by one against
+ * the published algorithms' own known answers. */
+void orc_xoshiro256pp(const uint64_t state[4], int64_t count, uint64_t *out);
+void orc_splitmix64(uint64_t seed, int64_t count, uint64_t *out);
+void orc_chacha_block(const uint32_t key[8], const uint32_t w12_15[4], int rounds, uint32_t out[16]);
+void orc_chacha_quarter_round(uint32_t v[4]);
+void orc_pcg32(uint64_t state, uint64_t inc, int after_step, int64_t count, uint32_t *out);
 
 /* ---- Euclidian::squared_distance (src/metrics/distance/euclidian.rs:51-67) ---- */
 double orc_sqdist(int dtype, const void *a, const void *b, int64_t d);

@@ -39,25 +39,91 @@ static uint32_t rotr32(uint32_t v, unsigned r) {
   return r ? (v >> r) | (v << (32 - r)) : v;
 }
 
-static void chacha_block(const uint32_t key[8], uint64_t ctr, uint32_t out[16]) {
+/* The ChaCha block function (Bernstein; RFC 7539 section 2.3 for 20 rounds):
+ * state = the four constants, the 256-bit key, words 12..15 as given;
+ * `rounds` rounds (column and diagonal rounds alternating), then the input
+ * added word by word. */
+void orc_chacha_block(const uint32_t key[8], const uint32_t w12_15[4], int rounds, uint32_t out[16]) {
   uint32_t in[16], w[16];
   in[0] = 0x61707865u; in[1] = 0x3320646eu; in[2] = 0x79622d32u; in[3] = 0x6b206574u;
   for (int i = 0; i < 8; ++i) in[4 + i] = key[i];
-  in[12] = (uint32_t)ctr;
-  in[13] = (uint32_t)(ctr >> 32);
-  in[14] = 0; in[15] = 0;
+  for (int i = 0; i < 4; ++i) in[12 + i] = w12_15[i];
   memcpy(w, in, sizeof w);
 #define QR(a, b, c, d)                                   \
   w[a] += w[b]; w[d] ^= w[a]; w[d] = rotl32(w[d], 16);   \
   w[c] += w[d]; w[b] ^= w[c]; w[b] = rotl32(w[b], 12);   \
   w[a] += w[b]; w[d] ^= w[a]; w[d] = rotl32(w[d], 8);    \
   w[c] += w[d]; w[b] ^= w[c]; w[b] = rotl32(w[b], 7);
-  for (int r = 0; r < 6; ++r) { /* 12 rounds = 6 column+diagonal pairs */
+  for (int r = 0; r < rounds; r += 2) { /* a column round and a diagonal round */
     QR(0, 4, 8, 12) QR(1, 5, 9, 13) QR(2, 6, 10, 14) QR(3, 7, 11, 15)
     QR(0, 5, 10, 15) QR(1, 6, 11, 12) QR(2, 7, 8, 13) QR(3, 4, 9, 14)
   }
 #undef QR
   for (int i = 0; i < 16; ++i) out[i] = w[i] + in[i];
+}
+
+/* One ChaCha quarter round on (a, b, c, d) (RFC 7539 section 2.1). */
+void orc_chacha_quarter_round(uint32_t v[4]) {
+  v[0] += v[1]; v[3] ^= v[0]; v[3] = rotl32(v[3], 16);
+  v[2] += v[3]; v[1] ^= v[2]; v[1] = rotl32(v[1], 12);
+  v[0] += v[1]; v[3] ^= v[0]; v[3] = rotl32(v[3], 8);
+  v[2] += v[3]; v[1] ^= v[2]; v[1] = rotl32(v[1], 7);
+}
+
+/* rand's ChaCha12 block: 64-bit block counter in words 12-13, stream id 0. */
+static void chacha_block(const uint32_t key[8], uint64_t ctr, uint32_t out[16]) {
+  const uint32_t w[4] = {(uint32_t)ctr, (uint32_t)(ctr >> 32), 0u, 0u};
+  orc_chacha_block(key, w, 12, out);
+}
+
+/* xoshiro256++ (Blackman & Vigna): output rotl(s0 + s3, 23) + s0, then the
+ * state update. */
+static uint64_t xoshiro_next(uint64_t s[4]) {
+  uint64_t r = rotl64(s[0] + s[3], 23) + s[0];
+  uint64_t t = s[1] << 17;
+  s[2] ^= s[0];
+  s[3] ^= s[1];
+  s[1] ^= s[2];
+  s[0] ^= s[3];
+  s[2] ^= t;
+  s[3] = rotl64(s[3], 45);
+  return r;
+}
+
+void orc_xoshiro256pp(const uint64_t state[4], int64_t count, uint64_t *out) {
+  uint64_t s[4] = {state[0], state[1], state[2], state[3]};
+  for (int64_t i = 0; i < count; ++i) out[i] = xoshiro_next(s);
+}
+
+/* SplitMix64 (Steele, Lea & Flood): state += golden gamma, then the mix. */
+static uint64_t splitmix_next(uint64_t *st) {
+  *st += 0x9e3779b97f4a7c15ull;
+  uint64_t z = *st;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+void orc_splitmix64(uint64_t seed, int64_t count, uint64_t *out) {
+  uint64_t st = seed;
+  for (int64_t i = 0; i < count; ++i) out[i] = splitmix_next(&st);
+}
+
+/* PCG32 output function XSH-RR (O'Neill) of a 64-bit LCG state. */
+static uint32_t pcg_xsh_rr(uint64_t st) {
+  uint32_t xs = (uint32_t)(((st >> 18) ^ st) >> 27);
+  return rotr32(xs, (unsigned)(st >> 59));
+}
+
+/* count outputs of the LCG state' = state * 6364136223846793005 + inc with
+ * the XSH-RR output of the state before the step (after_step = 0, the PCG
+ * paper's pcg32) or after it (after_step = 1, rand_core's seed filler). */
+void orc_pcg32(uint64_t state, uint64_t inc, int after_step, int64_t count, uint32_t *out) {
+  for (int64_t i = 0; i < count; ++i) {
+    const uint64_t old = state;
+    state = state * 6364136223846793005ull + inc;
+    out[i] = pcg_xsh_rr(after_step ? state : old);
+  }
 }
 
 static void chacha_refill(orc_rng *g) {
@@ -71,39 +137,17 @@ static void rng_seed(orc_rng *g, int kind, uint64_t seed) {
   g->kind = kind;
   if (kind == ORC_RNG_SMALL) {
     uint64_t st = seed;
-    for (int i = 0; i < 4; ++i) {
-      st += 0x9e3779b97f4a7c15ull;
-      uint64_t z = st;
-      z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-      z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-      g->s[i] = z ^ (z >> 31);
-    }
+    for (int i = 0; i < 4; ++i) g->s[i] = splitmix_next(&st);
     /* an all-zero state would be reseeded from 0; SplitMix64 never yields it */
   } else {
-    uint64_t st = seed;
-    for (int i = 0; i < 8; ++i) {
-      st = st * 6364136223846793005ull + 11634580456548205067ull;
-      uint32_t xs = (uint32_t)(((st >> 18) ^ st) >> 27);
-      g->key[i] = rotr32(xs, (unsigned)(st >> 59));
-    }
+    orc_pcg32(seed, 11634580456548205067ull, 1, 8, g->key);
     g->counter = 0;
     g->idx = 64; /* empty: first read generates */
   }
 }
 
 static uint64_t rng_next_u64(orc_rng *g) {
-  if (g->kind == ORC_RNG_SMALL) {
-    uint64_t *s = g->s;
-    uint64_t r = rotl64(s[0] + s[3], 23) + s[0];
-    uint64_t t = s[1] << 17;
-    s[2] ^= s[0];
-    s[3] ^= s[1];
-    s[1] ^= s[2];
-    s[0] ^= s[3];
-    s[2] ^= t;
-    s[3] = rotl64(s[3], 45);
-    return r;
-  }
+  if (g->kind == ORC_RNG_SMALL) return xoshiro_next(g->s);
   if (g->idx >= 64) chacha_refill(g);
   if (g->idx == 63) { /* a u64 straddling two refills: low word first */
     uint64_t lo = g->buf[63];
