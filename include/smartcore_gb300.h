@@ -310,6 +310,23 @@ void *sc_knn_stream(sc_knn *h);
 sc_status sc_knn_stats(sc_knn *h, int64_t *rescored);
 void sc_knn_destroy(sc_knn *h);
 
+/* ------------------------------------------------------------------ */
+/* Testing hooks (no counterpart in the reference)                     */
+/* ------------------------------------------------------------------ */
+/* Bound (ns) of the pipeline waits of this handle's split-form assignment
+ * kernel (0: the default 2 s).  Every wait of the kernel is bounded; when one
+ * runs out the kernel stops, waits (with the default bound) for the copies
+ * and tensor-core work it has issued, frees its tensor memory, and marks the
+ * step void: the next sc_kmeans_iterate returns SC_ERR_TIMEOUT and the handle
+ * runs no further iteration.  A tiny bound makes that path run on purpose. */
+sc_status sc_kmeans_set_wait_limit(sc_kmeans *h, int64_t ns);
+/* After `after` more successful device allocations of the library, every
+ * allocation fails with SC_ERR_OOM until the hook is reset (after < 0). */
+sc_status sc_debug_fail_alloc_after(int64_t after);
+/* Device allocations of the library not yet freed (stream-ordered frees
+ * count as freed when issued). */
+int64_t sc_debug_live_allocations(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,6 +61,7 @@ constexpr int kCUs[kNumCU] = {2, 4, 8};
 constexpr int kNumRows = 3;       // rows per work item
 constexpr int kRowsOpts[kNumRows] = {1024, 2048, 4096};
 constexpr int kGraphIters = 32;  // Lloyd iterations per graph launch
+constexpr int kNumD = 4;         // padded widths 8, 16, 32, 64
 
 struct BProb {
   int64_t x_off;   // element offset of row 0 in X
@@ -237,87 +238,103 @@ __device__ __forceinline__ void load_row(const T *__restrict__ xr, float (&x)[D]
   }
 }
 
-// One work item of rows, one row per thread.  mode 0: assign + sums;
-// mode 1: sums of the given labels (the seeding partition).
+// One work item of rows in passes of 256, one row per thread for the
+// distances.  mode 0: assign + sums; mode 1: sums of the given labels (the
+// seeding partition).  The sums are taken warp by warp afterwards: for each
+// of its 32 rows the warp adds the row's values, lane j feature j, into the
+// cluster's shared accumulators, so the 64-bit shared atomics of one
+// instruction hit consecutive words (no bank conflicts); the rows are read
+// again from global memory, where the distance pass has just brought them
+// into L1.
 template <typename T, int D, int CU>
 __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BState *st, const T *__restrict__ X,
                                             const double *__restrict__ cent64, const float *s_c, float cdelta,
-                                            unsigned long long *s_acc, unsigned *s_cnt,
+                                            unsigned long long *s_acc, unsigned *s_cnt, int *s_lab,
                                             int32_t *__restrict__ labels, int mode) {
   const int d = P.d, k = P.k, kpad = (k + 7) & ~7;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   long long rescored = 0;
-  for (int r = it.r0 + (int)threadIdx.x; r < it.r1; r += kAsgThreads) {
-    const T *xr = X + P.x_off + (int64_t)r * D;
-    float x[D];
-    load_row<T, D>(xr, x);
-    int bi = 0;
-    if (mode == 1) {
-      bi = labels[P.row0 + r];
-    } else {
-      float best = __int_as_float(0x7f800000), second = best;
+  for (int base = it.r0; base < it.r1; base += kAsgThreads) {
+    const int r = base + (int)threadIdx.x;
+    int bi = -1;
+    if (r < it.r1) {
+      const T *xr = X + P.x_off + (int64_t)r * D;
+      if (mode == 1) {
+        bi = labels[P.row0 + r];
+      } else {
+        float x[D];
+        load_row<T, D>(xr, x);
+        float best = __int_as_float(0x7f800000), second = best;
+        bi = 0;
 #pragma unroll 1
-      for (int c0 = 0; c0 < kpad; c0 += CU) {
-        float a[CU];
+        for (int c0 = 0; c0 < kpad; c0 += CU) {
+          float a[CU];
 #pragma unroll
-        for (int u = 0; u < CU; ++u) a[u] = dist32<D>(x, s_c + (c0 + u) * D);
+          for (int u = 0; u < CU; ++u) a[u] = dist32<D>(x, s_c + (c0 + u) * D);
 #pragma unroll
-        for (int u = 0; u < CU; ++u) {
-          const float v = a[u];  // NaN (padding, empty clusters) never wins
-          if (v < best) {
-            second = best;
-            best = v;
-            bi = c0 + u;
-          } else if (v < second) {
-            second = v;
+          for (int u = 0; u < CU; ++u) {
+            const float v = a[u];  // NaN (padding, empty clusters) never wins
+            if (v < best) {
+              second = best;
+              best = v;
+              bi = c0 + u;
+            } else if (v < second) {
+              second = v;
+            }
           }
         }
-      }
-      float del = cdelta;
-      if constexpr (sizeof(T) == 8) {  // ||x - fl32(x)|| <= 2^-24 ||x~|| (1 + 2^-20)
-        float xn = 0.f;
+        float del = cdelta;
+        if constexpr (sizeof(T) == 8) {  // ||x - fl32(x)|| <= 2^-24 ||x~|| (1 + 2^-20)
+          float xn = 0.f;
 #pragma unroll
-        for (int j = 0; j < D; ++j) xn = __fmaf_ru(x[j], x[j], xn);
-        del = __fadd_ru(del, __fmul_ru(__fsqrt_ru(xn), 0x1.00001p-24f));
-      }
-      const Bound bd = make_bound(d, del);
-      const bool certain = second >= bd.floor16 &&
-                           __fsub_rd(second, err_bound(second, bd)) > __fadd_ru(best, err_bound(best, bd));
-      if (!certain) {
-        // Near tie (or a non-finite value): every centroid whose FP32 distance
-        // cannot be shown to exceed the best one's is scored with the
-        // reference's FP64 distance (src/metrics/distance/euclidian.rs:51-63
-        // on f64 rows, kmeans.rs:338-346), strict <, lowest index first.
-        const float thr = __fadd_ru(best, err_bound(best, bd));
-        double bdist = DBL_MAX;
-        int b = 0;
-        for (int c = 0; c < k; ++c) {
-          const float a = dist32<D>(x, s_c + c * D);
-          if (__fsub_rd(a, err_bound(a, bd)) > thr) continue;
-          const double *cr = cent64 + P.c_off + (int64_t)c * d;
-          double s = 0.0;
-          for (int j = 0; j < d; ++j) s = __dadd_rn(s, sq_term((double)xr[j], cr[j]));
-          if (s < bdist) {
-            bdist = s;
-            b = c;
-          }
+          for (int j = 0; j < D; ++j) xn = __fmaf_ru(x[j], x[j], xn);
+          del = __fadd_ru(del, __fmul_ru(__fsqrt_ru(xn), 0x1.00001p-24f));
         }
-        bi = b;
-        ++rescored;
+        const Bound bd = make_bound(d, del);
+        const bool certain = second >= bd.floor16 &&
+                             __fsub_rd(second, err_bound(second, bd)) > __fadd_ru(best, err_bound(best, bd));
+        if (!certain) {
+          // Near tie (or a non-finite value): every centroid whose FP32
+          // distance cannot be shown to exceed the best one's is scored with
+          // the reference's FP64 distance (src/metrics/distance/
+          // euclidian.rs:51-63 on f64 rows, kmeans.rs:338-346), strict <,
+          // lowest index first.
+          const float thr = __fadd_ru(best, err_bound(best, bd));
+          double bdist = DBL_MAX;
+          int b = 0;
+          for (int c = 0; c < k; ++c) {
+            const float a = dist32<D>(x, s_c + c * D);
+            if (__fsub_rd(a, err_bound(a, bd)) > thr) continue;
+            const double *cr = cent64 + P.c_off + (int64_t)c * d;
+            double sd = 0.0;
+            for (int j = 0; j < d; ++j) sd = __dadd_rn(sd, sq_term((double)xr[j], cr[j]));
+            if (sd < bdist) {
+              bdist = sd;
+              b = c;
+            }
+          }
+          bi = b;
+          ++rescored;
+        }
+        labels[P.row0 + r] = bi;
       }
-      labels[P.row0 + r] = bi;
     }
-    // exact fixed-point sums of the row into its cluster's shared accumulators
-    atomicAdd(&s_cnt[bi], 1u);
-    unsigned long long *ar = s_acc + (int64_t)bi * d;
-#pragma unroll
-    for (int j = 0; j < D; ++j) {
-      if (j < d) {
-        long long v;
-        if constexpr (sizeof(T) == 4) v = fixed64(x[j], P.scale);
-        else v = fixed64(xr[j], P.scale);
+    s_lab[threadIdx.x] = bi;
+    __syncwarp();
+    // exact fixed-point sums of the warp's rows, one row at a time
+    const int rw = base + w * 32;
+    for (int q = 0; q < 32; ++q) {
+      const int lab = s_lab[w * 32 + q];
+      if (lab < 0) break;  // rows past the item's end (uniform over the warp)
+      const T *xr = X + P.x_off + (int64_t)(rw + q) * D;
+      unsigned long long *ar = s_acc + (int64_t)lab * d;
+      for (int j = lane; j < d; j += 32) {
+        const long long v = fixed64(xr[j], P.scale);
         if (v) atomicAdd(ar + j, (unsigned long long)v);
       }
+      if (lane == 0) atomicAdd(&s_cnt[lab], 1u);
     }
+    __syncwarp();  // s_lab is rewritten by the next pass
   }
   if (rescored) atomicAdd((unsigned long long *)&st->rescored, (unsigned long long)rescored);
 }
@@ -325,22 +342,30 @@ __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BSt
 template <typename T, int D>
 __device__ __forceinline__ void assign_rows_cu(int cu, const BItem &it, const BProb &P, BState *st, const T *X,
                                                const double *cent64, const float *s_c, float cdelta,
-                                               unsigned long long *s_acc, unsigned *s_cnt, int32_t *labels,
-                                               int mode) {
-  if (cu == 2) assign_rows<T, D, 2>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, labels, mode);
-  else if (cu == 8) assign_rows<T, D, 8>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, labels, mode);
-  else assign_rows<T, D, 4>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, labels, mode);
+                                               unsigned long long *s_acc, unsigned *s_cnt, int *s_lab,
+                                               int32_t *labels, int mode) {
+  if (cu == 2) assign_rows<T, D, 2>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, s_lab, labels, mode);
+  else if (cu == 8) assign_rows<T, D, 8>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, s_lab, labels, mode);
+  else assign_rows<T, D, 4>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, s_lab, labels, mode);
 }
 
-// Persistent assignment (+ sums) kernel fed by the device work queue `head`.
-template <typename T>
-__global__ void __launch_bounds__(kAsgThreads, 2)
+// Resident CTAs per SM the compiler plans registers for, by row width.
+template <int D>
+struct AsgOcc {
+  static constexpr int value = D <= 16 ? 4 : D <= 32 ? 3 : 2;
+};
+
+// Persistent assignment (+ sums) kernel of the problems of padded width D,
+// fed by the device work queue `head` over their items.
+template <typename T, int D>
+__global__ void __launch_bounds__(kAsgThreads, AsgOcc<D>::value)
 batch_assign_kernel(const BItem *__restrict__ items, int nitems, const BProb *__restrict__ probs, BState *st,
                     const T *__restrict__ X, const float *__restrict__ cent32, const double *__restrict__ cent64,
                     int32_t *__restrict__ labels, Acc128 *__restrict__ acc, unsigned long long *__restrict__ cnt,
                     unsigned *head, const int *active, int mode) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_item, s_prob;
+  __shared__ int s_lab[kAsgThreads];
   if (mode == 0 && *active == 0) return;
   if (threadIdx.x == 0) s_prob = -1;
   for (;;) {
@@ -352,7 +377,7 @@ batch_assign_kernel(const BItem *__restrict__ items, int nitems, const BProb *__
     const BItem it = items[iti];
     if (mode == 0 && st[it.prob].done) continue;
     const BProb P = probs[it.prob];
-    const int k = P.k, d = P.d, D = P.D, kpad = (k + 7) & ~7;
+    const int k = P.k, d = P.d, kpad = (k + 7) & ~7;
     float *s_c = reinterpret_cast<float *>(smraw);
     unsigned long long *s_acc = reinterpret_cast<unsigned long long *>(smraw + (size_t)kpad * D * 4);
     unsigned *s_cnt = reinterpret_cast<unsigned *>(s_acc + (size_t)k * d);
@@ -366,14 +391,8 @@ batch_assign_kernel(const BItem *__restrict__ items, int nitems, const BProb *__
     for (int t = threadIdx.x; t < k * d; t += kAsgThreads) s_acc[t] = 0ull;
     for (int t = threadIdx.x; t < k; t += kAsgThreads) s_cnt[t] = 0u;
     __syncthreads();
-    const float cdelta = st[it.prob].cdelta;
-    const int cu = it.variant;
-    switch (D) {
-      case 8: assign_rows_cu<T, 8>(cu, it, P, st + it.prob, X, cent64, s_c, cdelta, s_acc, s_cnt, labels, mode); break;
-      case 16: assign_rows_cu<T, 16>(cu, it, P, st + it.prob, X, cent64, s_c, cdelta, s_acc, s_cnt, labels, mode); break;
-      case 32: assign_rows_cu<T, 32>(cu, it, P, st + it.prob, X, cent64, s_c, cdelta, s_acc, s_cnt, labels, mode); break;
-      default: assign_rows_cu<T, 64>(cu, it, P, st + it.prob, X, cent64, s_c, cdelta, s_acc, s_cnt, labels, mode); break;
-    }
+    assign_rows_cu<T, D>(it.variant, it, P, st + it.prob, X, cent64, s_c, st[it.prob].cdelta, s_acc, s_cnt, s_lab,
+                         labels, mode);
     __syncthreads();
     for (int t = threadIdx.x; t < k * d; t += kAsgThreads) {
       const long long v = (long long)s_acc[t];
@@ -689,7 +708,7 @@ batch_pp_select_kernel(const BProb *__restrict__ probs, BState *st, const T *__r
 // Tuning table: per (padded width D, cluster class) the centroids per inner
 // pass (CU) and rows per work item of the assignment kernel.
 // ---------------------------------------------------------------------------
-constexpr int kNumD = 4, kNumKC = 5;
+constexpr int kNumKC = 5;
 struct Tune {
   bool ready = false;
   int cu[kNumD][kNumKC];
@@ -742,13 +761,15 @@ struct Batch {
   std::vector<BProb> probs;       // internal order (k descending)
   std::vector<int> order;         // internal index -> caller's index
   std::vector<int32_t> block_prob;
-  std::vector<BItem> items;
+  std::vector<BItem> items;         // grouped by padded width, each group largest first
+  int item_off[kNumD + 1] = {};     // group dc = items [item_off[dc], item_off[dc + 1])
+  size_t smem_d[kNumD] = {};        // dynamic shared memory of each width's kernel
+  int grid_d[kNumD] = {};           // persistent CTAs of each width's kernel
   std::vector<double> uniforms;
   std::vector<int64_t> first;
   int64_t rows = 0, xelems = 0, kd = 0, k32 = 0, ksum = 0;
   int blocks = 0, kmax = 0, max_iter = 0;
   bool needs_pad = false;
-  size_t smem = 0;
   // device
   cudaStream_t s = nullptr;
   void *mem = nullptr;
@@ -762,9 +783,8 @@ struct Batch {
   BProb *d_probs = nullptr;
   BState *st = nullptr;
   BItem *d_items = nullptr;
-  unsigned *heads = nullptr;
+  unsigned *heads = nullptr;  // one queue head per (graph iteration, width), then the seeding pass's
   int *active = nullptr;
-  int grid_asg = 0;
 };
 
 // Work items of problem q with the given rows per item and variant.
@@ -816,23 +836,33 @@ void plan_batch(Batch &B, const std::vector<int64_t> &n, const std::vector<int64
     B.kmax = std::max(B.kmax, P.k);
     B.max_iter = std::max(B.max_iter, P.max_iter);
     const size_t sm = (size_t)((P.k + 7) & ~7) * P.D * 4 + (size_t)P.k * P.d * 8 + (size_t)P.k * 4 + 64;
-    B.smem = std::max(B.smem, sm);
+    B.smem_d[dclass(P.D)] = std::max(B.smem_d[dclass(P.D)], sm);
     int cu, rows;
     tune_choice(P.D, P.k, &cu, &rows);
     P.rows = rows;
-    add_items(B.items, q, P.n, rows, cu);
   }
+  // work items grouped by width, largest cost (rows x k) first in each group
+  std::vector<BItem> groups[kNumD];
+  for (int q = 0; q < m; ++q) {
+    const BProb &P = B.probs[q];
+    int cu, rows;
+    tune_choice(P.D, P.k, &cu, &rows);
+    add_items(groups[dclass(P.D)], q, P.n, P.rows, cu);
+  }
+  for (int dc = 0; dc < kNumD; ++dc) {
+    std::stable_sort(groups[dc].begin(), groups[dc].end(), [&](const BItem &a, const BItem &b) {
+      return (int64_t)(a.r1 - a.r0) * B.probs[a.prob].k > (int64_t)(b.r1 - b.r0) * B.probs[b.prob].k;
+    });
+    B.item_off[dc] = (int)B.items.size();
+    B.items.insert(B.items.end(), groups[dc].begin(), groups[dc].end());
+  }
+  B.item_off[kNumD] = (int)B.items.size();
   B.xelems = xo;
   B.rows = row;
   B.kd = co;
   B.k32 = c32;
   B.ksum = ko;
   B.blocks = blk;
-  // largest items first (cost ~ rows x k x D), ties in problem order
-  std::stable_sort(B.items.begin(), B.items.end(), [&](const BItem &a, const BItem &b) {
-    const BProb &pa = B.probs[a.prob], &pb = B.probs[b.prob];
-    return (int64_t)(a.r1 - a.r0) * pa.k * pa.D > (int64_t)(b.r1 - b.r0) * pb.k * pb.D;
-  });
 }
 
 sc_status alloc_batch(Batch &B) {
@@ -858,7 +888,7 @@ sc_status alloc_batch(Batch &B) {
     B.st = a.take<BState>(B.count);
     B.d_block_prob = a.take<int32_t>(B.blocks);
     B.d_items = a.take<BItem>(B.items.size());
-    B.heads = a.take<unsigned>((size_t)kGraphIters + 1);
+    B.heads = a.take<unsigned>((size_t)(kGraphIters + 1) * kNumD);
     B.active = a.take<int>(1);
   };
   layout(A);  // sizes only (base = null)
@@ -881,30 +911,66 @@ sc_status upload_tables(Batch &B) {
   return SC_OK;
 }
 
-template <typename T>
-sc_status launch_assign(Batch &B, unsigned *head, int nitems, const BItem *items, int mode) {
-  auto kern = batch_assign_kernel<T>;  // shared-memory attribute set by assign_grid
-  kern<<<B.grid_asg, kAsgThreads, B.smem, B.s>>>(items, nitems, B.d_probs, B.st, (const T *)B.X, B.cent32,
-                                                 B.cent64, B.labels, B.acc, B.cnt, head, B.active, mode);
+template <typename T, int D>
+sc_status launch_assign_d(Batch &B, int dc, unsigned *head, int nitems, const BItem *items, int mode) {
+  if (nitems == 0) return SC_OK;
+  // shared-memory attribute set by assign_grid
+  batch_assign_kernel<T, D><<<B.grid_d[dc], kAsgThreads, B.smem_d[dc], B.s>>>(
+      items, nitems, B.d_probs, B.st, (const T *)B.X, B.cent32, B.cent64, B.labels, B.acc, B.cnt, head, B.active,
+      mode);
   SC_LAUNCHED();
   return SC_OK;
 }
 
+// One assignment pass over the item groups of every width; heads[dc] is the
+// queue head of width dc (cleared beforehand).
+template <typename T>
+sc_status launch_assign(Batch &B, unsigned *heads, int mode) {
+  const BItem *it = B.d_items;
+  const int *o = B.item_off;
+  SC_TRY((launch_assign_d<T, 8>(B, 0, heads + 0, o[1] - o[0], it + o[0], mode)));
+  SC_TRY((launch_assign_d<T, 16>(B, 1, heads + 1, o[2] - o[1], it + o[1], mode)));
+  SC_TRY((launch_assign_d<T, 32>(B, 2, heads + 2, o[3] - o[2], it + o[2], mode)));
+  SC_TRY((launch_assign_d<T, 64>(B, 3, heads + 3, o[4] - o[3], it + o[3], mode)));
+  return SC_OK;
+}
+
+// The items of one width class only (the tuner's single-problem passes).
+template <typename T>
+sc_status launch_assign_class(Batch &B, int dc, unsigned *head, int nitems, const BItem *items, int mode) {
+  switch (dc) {
+    case 0: return launch_assign_d<T, 8>(B, 0, head, nitems, items, mode);
+    case 1: return launch_assign_d<T, 16>(B, 1, head, nitems, items, mode);
+    case 2: return launch_assign_d<T, 32>(B, 2, head, nitems, items, mode);
+    default: return launch_assign_d<T, 64>(B, 3, head, nitems, items, mode);
+  }
+}
+
+template <typename T, int D>
+sc_status assign_grid_d(Batch &B, int dc, int sms) {
+  if (B.item_off[dc + 1] == B.item_off[dc]) return SC_OK;
+  int per = 0;
+  SC_CUDA(cudaFuncSetAttribute(batch_assign_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)B.smem_d[dc]));
+  SC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_assign_kernel<T, D>, kAsgThreads, B.smem_d[dc]));
+  B.grid_d[dc] = sms * std::max(1, per);
+  return SC_OK;
+}
+
+template <typename T>
+sc_status assign_grid_t(Batch &B, int sms) {
+  SC_TRY((assign_grid_d<T, 8>(B, 0, sms)));
+  SC_TRY((assign_grid_d<T, 16>(B, 1, sms)));
+  SC_TRY((assign_grid_d<T, 32>(B, 2, sms)));
+  SC_TRY((assign_grid_d<T, 64>(B, 3, sms)));
+  return SC_OK;
+}
+
 sc_status assign_grid(Batch &B, int dtype) {
-  int dev = 0, sms = 0, per = 0;
+  int dev = 0, sms = 0;
   SC_CUDA(cudaGetDevice(&dev));
   SC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  if (dtype == SC_F32) {
-    SC_CUDA(cudaFuncSetAttribute(batch_assign_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)B.smem));
-    SC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_assign_kernel<float>, kAsgThreads, B.smem));
-  } else {
-    SC_CUDA(cudaFuncSetAttribute(batch_assign_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)B.smem));
-    SC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_assign_kernel<double>, kAsgThreads, B.smem));
-  }
-  B.grid_asg = sms * std::max(1, per);
-  return SC_OK;
+  return dtype == SC_F32 ? assign_grid_t<float>(B, sms) : assign_grid_t<double>(B, sms);
 }
 
 // Device phases of a batch: scan, scales, k-means++, initial means.
@@ -958,8 +1024,9 @@ sc_status run_setup(Batch &B) {
   // initial means of the seeding partition
   SC_CUDA(cudaMemsetAsync(B.acc, 0, (size_t)B.kd * sizeof(Acc128), s));
   SC_CUDA(cudaMemsetAsync(B.cnt, 0, (size_t)B.ksum * sizeof(unsigned long long), s));
-  SC_CUDA(cudaMemsetAsync(B.heads + kGraphIters, 0, sizeof(unsigned), s));
-  SC_TRY(launch_assign<T>(B, B.heads + kGraphIters, (int)B.items.size(), B.d_items, 1));
+  unsigned *seed_heads = B.heads + (size_t)kGraphIters * kNumD;
+  SC_CUDA(cudaMemsetAsync(seed_heads, 0, kNumD * sizeof(unsigned), s));
+  SC_TRY(launch_assign<T>(B, seed_heads, 1));
   batch_finalize_kernel<<<B.count, kFinT, 0, s>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 1,
                                                   B.active);
   SC_LAUNCHED();
@@ -980,9 +1047,10 @@ sc_status run_lloyd(Batch &B) {
   cudaGraphExec_t exec = nullptr;
   SC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   sc_status r = SC_OK;
-  if (cudaMemsetAsync(B.heads, 0, (size_t)G * sizeof(unsigned), s) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "memset");
+  if (cudaMemsetAsync(B.heads, 0, (size_t)G * kNumD * sizeof(unsigned), s) != cudaSuccess)
+    r = cuda_fail(cudaGetLastError(), "memset");
   for (int t = 0; t < G && r == SC_OK; ++t) {
-    r = launch_assign<T>(B, B.heads + t, (int)B.items.size(), B.d_items, 0);
+    r = launch_assign<T>(B, B.heads + (size_t)t * kNumD, 0);
     if (r != SC_OK) break;
     batch_finalize_kernel<<<B.count, kFinT, 0, s>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 0,
                                                     B.active);
@@ -1252,7 +1320,7 @@ sc_status sc_batch_tune(const char *path) {
           for (int rep = 0; rep < 4 && r == SC_OK; ++rep) {
             if (cudaMemsetAsync(B.heads, 0, sizeof(unsigned), B.s) != cudaSuccess ||
                 cudaEventRecord(e0, B.s) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "tuning"); break; }
-            if ((r = launch_assign<float>(B, B.heads, (int)items.size(), d_items, 0)) != SC_OK) break;
+            if ((r = launch_assign_class<float>(B, dc, B.heads, (int)items.size(), d_items, 0)) != SC_OK) break;
             float ms = 0.f;
             if (cudaEventRecord(e1, B.s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
                 cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "tuning"); break; }

@@ -41,9 +41,18 @@ sc_status cuda_fail(cudaError_t e, const char *what) {
 
 std::mutex g_pool_mutex;
 bool g_pool_ready[64] = {};
+// Testing hooks: allocations left before injected failures (-1: none), and
+// the number of live device allocations made through dev_alloc.
+std::atomic<long long> g_fail_after{-1};
+std::atomic<long long> g_live_allocs{0};
 
 sc_status dev_alloc(void **p, size_t bytes, cudaStream_t s) {
   *p = nullptr;
+  if (g_fail_after.load() >= 0 && g_fail_after.fetch_sub(1) <= 0) {
+    g_fail_after.store(0);
+    set_error("device allocation of %zu bytes failed (injected)", bytes);
+    return SC_ERR_OOM;
+  }
   int dev = 0;
   SC_CUDA(cudaGetDevice(&dev));
   if (dev >= 0 && dev < 64) {
@@ -57,11 +66,15 @@ sc_status dev_alloc(void **p, size_t bytes, cudaStream_t s) {
     }
   }
   SC_CUDA(cudaMallocAsync(p, bytes ? bytes : 1, s));
+  g_live_allocs.fetch_add(1);
   return SC_OK;
 }
 
 void dev_free(void *p, cudaStream_t s) {
-  if (p) cudaFreeAsync(p, s);
+  if (p) {
+    cudaFreeAsync(p, s);
+    g_live_allocs.fetch_sub(1);
+  }
 }
 
 // Pinned host staging buffer for results copied into caller memory (grows,
@@ -117,12 +130,15 @@ sc_status upload_matrix(const void *x, int32_t dtype, int32_t layout, int32_t me
   const size_t span = (size_t)((d - 1) * ld + n);
   const void *src = x;
   if (mem == SC_MEM_HOST) {
-    SC_CUDA(cudaMallocAsync(&tmp, span * es, s));
-    SC_CUDA(cudaMemcpyAsync(tmp, x, span * es, cudaMemcpyHostToDevice, s));
+    SC_TRY(dev_alloc(&tmp, span * es, s));
+    if (cudaMemcpyAsync(tmp, x, span * es, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      dev_free(tmp, s);
+      return cuda_fail(cudaGetLastError(), "upload");
+    }
     src = tmp;
   }
   sc_status r = launch_to_row_major(dtype, src, n, d, ld, dst, s);
-  if (tmp) cudaFreeAsync(tmp, s);
+  dev_free(tmp, s);
   return r;
 }
 
@@ -181,6 +197,9 @@ static cudaEvent_t *next_timing(sc_kmeans *h) {
 
 static sc_status kmeans_alloc_k(sc_kmeans *h, int64_t k) {
   if (k == h->k_alloc) { h->k = k; return SC_OK; }
+  // until every buffer of the new k exists the handle has no centroids
+  h->k_alloc = 0;
+  h->k = 0;
   cudaStream_t hs = h->stream;
   dfree(h->cent, hs); dfree(h->sizes, hs); dfree(h->cterms, hs); dfree(h->uniforms, hs);
   dfree(h->seed_x, hs); dfree(h->seed_cc, hs);
@@ -307,13 +326,7 @@ sc_status sc_kmeans_create(const void *x, int32_t dtype, int32_t layout, int32_t
 
 void *sc_kmeans_stream(sc_kmeans *h) { return h ? (void *)h->stream : nullptr; }
 
-sc_status sc_kmeans_seed(sc_kmeans *h, int64_t k, int64_t first_index, const double *uniforms) {
-  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
-  if (k < 1) { set_error("invalid number of clusters: %lld", (long long)k); return SC_ERR_INVALID; }
-  if (h->n < 1) { set_error("cannot seed an empty dataset"); return SC_ERR_INVALID; }
-  if (first_index < 0 || first_index >= h->n) { set_error("first seed index %lld out of range", (long long)first_index); return SC_ERR_INVALID; }
-  if (k > 1 && !uniforms) { set_error("null uniforms"); return SC_ERR_INVALID; }
-  if (k > (1 << 20)) { set_error("k=%lld is too large", (long long)k); return SC_ERR_INVALID; }
+static sc_status seed_impl(sc_kmeans *h, int64_t k, int64_t first_index, const double *uniforms) {
   SC_TRY(kmeans_alloc_k(h, k));
   SC_TRY(reset_state(h));
   cudaStream_t s = h->stream;
@@ -341,15 +354,33 @@ sc_status sc_kmeans_seed(sc_kmeans *h, int64_t k, int64_t first_index, const dou
   return SC_OK;
 }
 
-sc_status sc_kmeans_set_centroids(sc_kmeans *h, int64_t k, const double *centroids) {
+sc_status sc_kmeans_seed(sc_kmeans *h, int64_t k, int64_t first_index, const double *uniforms) {
   if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
-  if (k < 1 || !centroids) { set_error("invalid number of clusters: %lld", (long long)k); return SC_ERR_INVALID; }
+  if (k < 1) { set_error("invalid number of clusters: %lld", (long long)k); return SC_ERR_INVALID; }
+  if (h->n < 1) { set_error("cannot seed an empty dataset"); return SC_ERR_INVALID; }
+  if (first_index < 0 || first_index >= h->n) { set_error("first seed index %lld out of range", (long long)first_index); return SC_ERR_INVALID; }
+  if (k > 1 && !uniforms) { set_error("null uniforms"); return SC_ERR_INVALID; }
+  if (k > (1 << 20)) { set_error("k=%lld is too large", (long long)k); return SC_ERR_INVALID; }
+  sc_status r = seed_impl(h, k, first_index, uniforms);
+  if (r != SC_OK) h->k = 0;  // the handle has no usable centroids after a failed seeding
+  return r;
+}
+
+static sc_status set_centroids_impl(sc_kmeans *h, int64_t k, const double *centroids) {
   SC_TRY(kmeans_alloc_k(h, k));
   SC_TRY(reset_state(h));
   SC_CUDA(cudaMemcpyAsync(h->cent, centroids, (size_t)(k * h->d) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   if (h->form == SC_FORM_SPLIT_BF16) SC_TRY(split_centroids_changed(&h->split, h->cent, (int)k, h->stream));
   SC_CUDA(cudaStreamSynchronize(h->stream));
   return SC_OK;
+}
+
+sc_status sc_kmeans_set_centroids(sc_kmeans *h, int64_t k, const double *centroids) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (k < 1 || !centroids) { set_error("invalid number of clusters: %lld", (long long)k); return SC_ERR_INVALID; }
+  sc_status r = set_centroids_impl(h, k, centroids);
+  if (r != SC_OK) h->k = 0;  // no usable centroids after a failed update
+  return r;
 }
 
 // One Lloyd iteration: assignment, sums, new centroids, distortion + break.
@@ -458,6 +489,20 @@ sc_status sc_kmeans_profile_read(sc_kmeans *h, double *total_ms, int64_t *launch
 
 int64_t sc_kernel_launches(void) { return (int64_t)g_launches.load(); }
 
+sc_status sc_kmeans_set_wait_limit(sc_kmeans *h, int64_t ns) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  if (ns < 0) { set_error("invalid wait limit %lld", (long long)ns); return SC_ERR_INVALID; }
+  h->split.wait_ns = (uint64_t)ns;
+  return SC_OK;
+}
+
+sc_status sc_debug_fail_alloc_after(int64_t after) {
+  g_fail_after.store(after < 0 ? -1 : after);
+  return SC_OK;
+}
+
+int64_t sc_debug_live_allocations(void) { return (int64_t)g_live_allocs.load(); }
+
 sc_status sc_kmeans_sync(sc_kmeans *h) {
   if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
   SC_CUDA(cudaStreamSynchronize(h->stream));
@@ -523,11 +568,13 @@ struct sc_knn {
 
 static sc_status knn_reserve(sc_knn *h, int64_t m, int64_t k) {
   if (m > h->q_cap) {
+    h->q_cap = 0;  // a failed allocation leaves no stale capacity
     dfree(h->q, h->stream);
     SC_TRY(dalloc((char **)&h->q, (size_t)(m * h->d) * esize(h->dtype), h->stream));
     h->q_cap = m;
   }
   if (m * k > h->res_cap) {
+    h->res_cap = 0;
     dfree(h->idx, h->stream); dfree(h->dist, h->stream);
     SC_TRY(dalloc(&h->idx, (size_t)(m * k), h->stream));
     SC_TRY(dalloc(&h->dist, (size_t)(m * k), h->stream));
@@ -877,6 +924,7 @@ sc_status sc_knn_classify(sc_knn *h, const void *queries, int32_t layout, int32_
   if (!y_class || n_classes < 1) { set_error("invalid class labels"); return SC_ERR_INVALID; }
   SC_TRY(knn_run(h, queries, layout, mem, m, ld, k, form));
   if (h->aux_cap < std::max(h->n, m)) {
+    h->aux_cap = 0;
     dfree(h->aux_i, h->stream); dfree(h->aux_d, h->stream);
     SC_TRY(dalloc(&h->aux_i, (size_t)(h->n + m), h->stream));
     SC_TRY(dalloc(&h->aux_d, (size_t)(h->n + m), h->stream));
@@ -896,6 +944,7 @@ sc_status sc_knn_regress(sc_knn *h, const void *queries, int32_t layout, int32_t
   if (!y) { set_error("null targets"); return SC_ERR_INVALID; }
   SC_TRY(knn_run(h, queries, layout, mem, m, ld, k, form));
   if (h->aux_cap < std::max(h->n, m)) {
+    h->aux_cap = 0;
     dfree(h->aux_i, h->stream); dfree(h->aux_d, h->stream);
     SC_TRY(dalloc(&h->aux_i, (size_t)(h->n + m), h->stream));
     SC_TRY(dalloc(&h->aux_d, (size_t)(h->n + m), h->stream));

@@ -979,30 +979,41 @@ sc_status launch_knn_fp64(int dtype, const void *train, int64_t n, int d,
 // with d = sqrt(D) <= radius.  Pass 1 (out == nullptr) counts per query; pass
 // 2 writes each query's rows from offsets[q] on.
 // ---------------------------------------------------------------------------
-template <typename T>
+// SHQ: queries and training tiles staged in shared memory (else read from
+// global memory, for rows too wide to stage).
+template <typename T, bool SHQ>
 __global__ void knn_radius_fp64_kernel(const T *__restrict__ train, int64_t n, int d,
                                        const T *__restrict__ queries, int64_t m, double radius,
                                        int64_t *__restrict__ counts, const int64_t *__restrict__ offsets,
                                        int64_t *__restrict__ idx_out, double *__restrict__ dist_out) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nt = blockDim.x;
-  T *qs = reinterpret_cast<T *>(smraw);  // d x nt
-  T *ts = qs + (size_t)d * nt;           // kKnnTile x d
+  T *qs = reinterpret_cast<T *>(smraw);  // d x nt (SHQ)
+  T *ts = qs + (SHQ ? (size_t)d * nt : 0);  // kKnnTile x d (SHQ)
   const int tid = threadIdx.x;
   const int64_t q = (int64_t)blockIdx.x * nt + tid;
   const bool live = q < m;
-  for (int j = 0; j < d; ++j) qs[j * nt + tid] = live ? queries[q * d + j] : T(0);
+  if (SHQ)
+    for (int j = 0; j < d; ++j) qs[j * nt + tid] = live ? queries[q * d + j] : T(0);
+  const T *qg = queries + (live ? q : 0) * d;
   int64_t c = 0, pos = live && idx_out ? offsets[q] : 0;
   for (int64_t r0 = 0; r0 < n; r0 += kKnnTile) {
     const int rt = (int)min((int64_t)kKnnTile, n - r0);
-    __syncthreads();
-    for (int t = tid; t < rt * d; t += nt) ts[t] = train[r0 * d + t];
-    __syncthreads();
+    if (SHQ) {
+      __syncthreads();
+      for (int t = tid; t < rt * d; t += nt) ts[t] = train[r0 * d + t];
+      __syncthreads();
+    }
     if (!live) continue;
     for (int r = 0; r < rt; ++r) {
-      const T *tr = ts + r * d;
       double sq = 0.0;
-      for (int j = 0; j < d; ++j) sq = __dadd_rn(sq, sq_term(qs[j * nt + tid], tr[j]));
+      if (SHQ) {
+        const T *tr = ts + r * d;
+        for (int j = 0; j < d; ++j) sq = __dadd_rn(sq, sq_term(qs[j * nt + tid], tr[j]));
+      } else {
+        const T *tr = train + (r0 + r) * d;
+        for (int j = 0; j < d; ++j) sq = __dadd_rn(sq, sq_term(qg[j], tr[j]));
+      }
       const double dist = __dsqrt_rn(sq);
       if (dist <= radius) {
         if (idx_out) {
@@ -1017,35 +1028,36 @@ __global__ void knn_radius_fp64_kernel(const T *__restrict__ train, int64_t n, i
   if (live && !idx_out) counts[q] = c;
 }
 
+template <typename T>
+static sc_status knn_radius_typed(const T *train, int64_t n, int d, const T *queries, int64_t m, double radius,
+                                  int64_t *counts, const int64_t *offsets, int64_t *idx, double *dist,
+                                  cudaStream_t s) {
+  constexpr size_t es = sizeof(T);
+  for (int nt = 128; nt >= 32; nt >>= 1) {
+    const size_t smem = (size_t)d * nt * es + (size_t)kKnnTile * d * es + 16;
+    if (smem > 200 * 1024) continue;
+    auto kern = knn_radius_fp64_kernel<T, true>;
+    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<(unsigned)((m + nt - 1) / nt), nt, smem, s>>>(train, n, d, queries, m, radius, counts, offsets, idx,
+                                                         dist);
+    SC_LAUNCHED();
+    return SC_OK;
+  }
+  knn_radius_fp64_kernel<T, false><<<(unsigned)((m + 127) / 128), 128, 0, s>>>(train, n, d, queries, m, radius,
+                                                                                counts, offsets, idx, dist);
+  SC_LAUNCHED();
+  return SC_OK;
+}
+
 sc_status launch_knn_radius_fp64(int dtype, const void *train, int64_t n, int d, const void *queries, int64_t m,
                                  double radius, int64_t *counts, const int64_t *offsets, int64_t *idx,
                                  double *dist, cudaStream_t s) {
   if (m == 0) return SC_OK;
-  const int es = dtype == SC_F32 ? 4 : 8;
-  int nt = 128;
-  size_t smem = 0;
-  for (; nt >= 32; nt >>= 1) {
-    smem = (size_t)d * nt * es + (size_t)kKnnTile * d * es + 16;
-    if (smem <= 200 * 1024) break;
-  }
-  if (nt < 32) {
-    set_error("d=%d exceeds the FP64 radius kernel's shared memory", d);
-    return SC_ERR_INVALID;
-  }
-  const int grid = (int)((m + nt - 1) / nt);
-  if (dtype == SC_F32) {
-    auto kern = knn_radius_fp64_kernel<float>;
-    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, nt, smem, s>>>((const float *)train, n, d, (const float *)queries, m, radius, counts, offsets,
-                                idx, dist);
-  } else {
-    auto kern = knn_radius_fp64_kernel<double>;
-    SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<grid, nt, smem, s>>>((const double *)train, n, d, (const double *)queries, m, radius, counts, offsets,
-                                idx, dist);
-  }
-  SC_LAUNCHED();
-  return SC_OK;
+  if (dtype == SC_F32)
+    return knn_radius_typed<float>((const float *)train, n, d, (const float *)queries, m, radius, counts, offsets,
+                                   idx, dist, s);
+  return knn_radius_typed<double>((const double *)train, n, d, (const double *)queries, m, radius, counts, offsets,
+                                  idx, dist, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -693,6 +693,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   if (!s->num_sms) SC_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t n_pad = (n + tn - 1) / tn * tn;
   if (!s->ready || s->train != train || s->n != n || s->d != d) {  // training operand, once per handle
+    s->ready = 0;  // until every buffer below exists
     dfree(s->th, st); dfree(s->tl, st); dfree(s->tbx, st); dfree(s->tmax, st); dfree(s->ones, st);
     SC_TRY(dalloc(&s->th, (size_t)n_pad * d_pad, st));
     SC_TRY(dalloc(&s->tl, (size_t)n_pad * d_pad, st));
@@ -721,6 +722,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   }
   const int64_t m_pad = (m + kQM - 1) / kQM * kQM;
   if (m_pad > s->m_cap) {
+    s->m_cap = 0;  // a failed allocation leaves no stale capacity
     dfree(s->qh, st); dfree(s->ql, st); dfree(s->qnrm, st); dfree(s->qn2, st);
     SC_TRY(dalloc(&s->qh, (size_t)m_pad * d_pad, st));
     SC_TRY(dalloc(&s->ql, (size_t)m_pad * d_pad, st));

@@ -112,6 +112,7 @@ struct AssignParams {
   uint2 *cand4;              // [2 halves][n_pad]: up to 4 candidate columns of a listed row (16 bits each)
   uint8_t *cmeta;            // [2 halves][n_pad]: bits 0-3 valid columns of cand4, bit 4 list complete
   LloydState *st;
+  uint64_t wait_ns;  // bound of the pipeline waits (the drains keep kWaitNs)
 };
 
 __global__ void __launch_bounds__(kAssignThreads, 1)
@@ -183,7 +184,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x, ++it) {
         const int s = it % p.stages;
         const uint32_t ph = (uint32_t)(it / p.stages) & 1u;
-        if (!tc::mbar_wait(&empty[s], ph ^ 1u, kWaitNs)) { atomicExch(s_abort, 1); break; }
+        if (!tc::mbar_wait(&empty[s], ph ^ 1u, p.wait_ns)) { atomicExch(s_abort, 1); break; }
         if (*(volatile int *)s_abort) break;
         tc::mbar_expect_tx(&full[s], (uint32_t)a_stage);
         uint8_t *dst = sA + (size_t)s * a_stage;
@@ -202,7 +203,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t idesc = tc::idesc_bf16_f32(kBM, p.k_pad);
-      bool ok = tc::mbar_wait(bfull, 0, kWaitNs);
+      bool ok = tc::mbar_wait(bfull, 0, p.wait_ns);
       const uint32_t sA0 = tc::smem_u32(sA), sB0 = tc::smem_u32(sB);
       const uint64_t ones_desc = tc::smem_desc(tc::smem_u32(sOnes), 32);
       const uint64_t bx_desc = tc::smem_desc(tc::smem_u32(sBx), 32);
@@ -210,7 +211,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       for (int t = blockIdx.x; ok && t < p.n_tiles; t += gridDim.x, ++it) {
         const int s = it % p.stages, acc = it & 1;
         const uint32_t ph = (uint32_t)(it / p.stages) & 1u, aph = (uint32_t)(it >> 1) & 1u;
-        if (!tc::mbar_wait(&accempty[acc], aph ^ 1u, kWaitNs) || !tc::mbar_wait(&full[s], ph, kWaitNs)) {
+        if (!tc::mbar_wait(&accempty[acc], aph ^ 1u, p.wait_ns) || !tc::mbar_wait(&full[s], ph, p.wait_ns)) {
           ok = false;
           break;
         }
@@ -259,7 +260,7 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
       const bool live = i < p.n;
       const float xn = live ? __ldg(p.xnrm + i) : 0.f;
       const uint32_t aph = (uint32_t)(it >> 1) & 1u;
-      const bool got = tc::mbar_wait(&accfull[g], aph, kWaitNs);
+      const bool got = tc::mbar_wait(&accfull[g], aph, p.wait_ns);
       if (tc::bar_red_or(!got || *(volatile int *)s_abort != 0, bar_id, 64)) {  // uniform over the pair
         atomicExch(s_abort, 1);
         break;
@@ -375,7 +376,11 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
     tc::tmem_dealloc(tmem, p.tmem_cols);
   }
   if (threadIdx.x == 0) p.list_count[blockIdx.x] = *s_nlist;
-  if (threadIdx.x == 0 && *s_abort && p.st) atomicExch(&p.st->err, kErrTimeout);
+  if (threadIdx.x == 0 && *s_abort && p.st) {
+    // the step is void: the kernels after this one return at once
+    atomicExch(&p.st->err, kErrTimeout);
+    atomicExch(&p.st->done, 1);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1004,6 +1009,8 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
     return SC_ERR_INVALID;
   }
   if (k_cols > s->k_alloc) {
+    s->k_alloc = 0;  // a failed allocation leaves no stale capacity
+    s->k_pad = 0;
     dfree(s->ch, st); dfree(s->cl, st); dfree(s->cn2, st); dfree(s->cT, st); dfree(s->cbx, st);
     SC_TRY(dalloc(&s->ch, (size_t)k_cols * s->d_pad, st));
     SC_TRY(dalloc(&s->cl, (size_t)k_cols * s->d_pad, st));
@@ -1076,6 +1083,7 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   p.cand4 = s->cand4;
   p.cmeta = s->cmeta;
   p.st = lst;
+  p.wait_ns = s->wait_ns ? s->wait_ns : kWaitNs;
   if (s->wide) {
     SC_CUDA(cudaFuncSetAttribute(split_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (timing) SC_CUDA(cudaEventRecord(timing[0], st));

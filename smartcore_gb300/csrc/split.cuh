@@ -32,6 +32,7 @@ struct SplitState {
   uint8_t *cmeta = nullptr;                     //   [2][n_pad] valid columns, list complete
   CUtensorMap tm_xh, tm_xl, tm_ch, tm_cl;
   int num_sms = 0;
+  uint64_t wait_ns = 0;                         // bound of the assignment's pipeline waits (0: 2 s)
 };
 
 struct SplitKnnState {
