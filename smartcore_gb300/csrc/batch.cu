@@ -202,23 +202,25 @@ __device__ __forceinline__ float err_bound(float v, const Bound &b) {
   return __fadd_ru(__fmul_ru(2.f, e), b.A);
 }
 
-// FP32 difference-form distance of the row x (registers) to centroid c.
+// FP32 difference-form distance of the row x (registers) to centroid c, in
+// two interleaved FMA chains (even and odd feature pairs) added at the end:
+// every term passes through at most D / 2 + 1 roundings, within the bound.
 template <int D>
 __device__ __forceinline__ float dist32(const float (&x)[D], const float *__restrict__ c) {
-  float a = 0.f;
+  float a = 0.f, b = 0.f;
 #pragma unroll
   for (int j = 0; j < D; j += 4) {
     const float4 cc = *reinterpret_cast<const float4 *>(c + j);
     float t = __fsub_rn(x[j], cc.x);
     a = __fmaf_rn(t, t, a);
     t = __fsub_rn(x[j + 1], cc.y);
-    a = __fmaf_rn(t, t, a);
+    b = __fmaf_rn(t, t, b);
     t = __fsub_rn(x[j + 2], cc.z);
     a = __fmaf_rn(t, t, a);
     t = __fsub_rn(x[j + 3], cc.w);
-    a = __fmaf_rn(t, t, a);
+    b = __fmaf_rn(t, t, b);
   }
-  return a;
+  return __fadd_rn(a, b);
 }
 
 template <typename T, int D>
@@ -513,6 +515,41 @@ batch_scan_kernel(const int32_t *__restrict__ block_prob, const BProb *__restric
   if ((threadIdx.x & 31) == 0) atomicMax(&absmax_bits[p], (unsigned long long)__double_as_longlong(m));
 }
 
+// The same scan for f32 rows of padded width D, the row read with 16-byte
+// loads (pad columns are zero).
+template <int D>
+__global__ void __launch_bounds__(kBlk)
+batch_scan32_kernel(const int32_t *__restrict__ cls_blocks, const int32_t *__restrict__ block_prob,
+                    const BProb *__restrict__ probs, const float *__restrict__ X, double *__restrict__ part,
+                    unsigned long long *__restrict__ absmax_bits) {
+  const int b = cls_blocks[blockIdx.x];
+  const int p = block_prob[b];
+  const BProb P = probs[p];
+  const int64_t il = (int64_t)(b - P.b0) * kBlk + threadIdx.x;
+  double s = 0.0;
+  float m = 0.f;
+  if (il < P.n) {
+    float x[D];
+    load_row<float, D>(X + P.x_off + il * D, x);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      const double v = (double)x[j];
+      s = __fma_rn(v, v, s);
+      const float a = fabsf(x[j]);
+      m = (a > m || a != a) ? a : m;  // NaN propagates
+    }
+  }
+  const double tot = block_sum_fixed<kBlk>(s);
+  if (threadIdx.x == 0) part[b] = tot;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (y > m || y != y) ? y : m;
+  }
+  if ((threadIdx.x & 31) == 0)
+    atomicMax(&absmax_bits[p], (unsigned long long)__double_as_longlong((double)m));
+}
+
 // Per problem: xnorm2 = sum of its block partials in order, the state's start
 // values, and the first seed (row first_index) as seed 0.
 template <typename T>
@@ -601,6 +638,71 @@ batch_pp_update_kernel(const int32_t *__restrict__ block_prob, const BProb *__re
       dd[gi] = cur;
       dd32[gi] = __double2float_ru(cur);
       labels[gi] = lab;
+    }
+  }
+  const double tot = block_sum_fixed<kBlk>(live ? cur : 0.0);
+  if (threadIdx.x == 0) part[b] = tot;
+}
+
+// The same update for f32 rows of padded width D: the row comes into
+// registers with 16-byte loads only when the far test leaves it, its terms
+// fl32((x_t - c_t)^2) give the f32 lower bound and, when needed, the exact
+// value by the integer reproduction of the sequential f64 sum.  One CTA per
+// 256-row block of the width's problems with k >= j (cls_blocks lists them,
+// largest k first).
+template <int D>
+__global__ void __launch_bounds__(kBlk)
+batch_pp_update32_kernel(const int32_t *__restrict__ cls_blocks, const int32_t *__restrict__ block_prob,
+                         const BProb *__restrict__ probs, const BState *__restrict__ st,
+                         const float *__restrict__ X, double *__restrict__ dd, float *__restrict__ dd32,
+                         int32_t *__restrict__ labels, double *__restrict__ part,
+                         const float *__restrict__ seed_cc, int j, PPFar32 far) {
+  __shared__ __align__(16) float s_seed[D];
+  const int b = cls_blocks[blockIdx.x];
+  const int p = block_prob[b];
+  const BProb P = probs[p];
+  const int64_t ci = st[p].pp_chosen;
+  if (threadIdx.x < D) s_seed[threadIdx.x] = X[P.x_off + ci * D + threadIdx.x];
+  __syncthreads();
+  const int64_t il = (int64_t)(b - P.b0) * kBlk + threadIdx.x;
+  const bool live = il < P.n;
+  const int64_t gi = P.row0 + il;
+  const bool first = j == 1;
+  double cur = 0.0;
+  if (live) {
+    cur = first ? DBL_MAX : dd[gi];
+    int32_t lab = first ? 0 : labels[gi];
+    const int d = P.d;
+    const float c32 = first ? 0.f : dd32[gi];
+    if (first || !pp_far32(seed_cc[P.k_off + lab], c32, far)) {
+      float x[D];
+      load_row<float, D>(X + P.x_off + il * D, x);
+      float q[D];
+      float s32 = 0.f;
+#pragma unroll
+      for (int t = 0; t < D; ++t) {
+        const float r = __fsub_rn(x[t], s_seed[t]);
+        q[t] = __fmul_rn(r, r);
+        if (t < d) s32 = __fadd_rn(s32, q[t]);
+      }
+      // the terms summed in f32 bound the reference's f64 sum from below by
+      // s32 (1 - 1.05 d 2^-24): above the current distance, the row keeps it
+      if (first || !(__fmul_rd(s32, 1.f - 1.05f * d * 0x1p-24f) > c32)) {
+        double s = 0.0;
+        if (!sqd_seq_terms<D>(q, d, P.lg_d, s)) {
+          s = 0.0;
+#pragma unroll
+          for (int t = 0; t < D; ++t)
+            if (t < d) s = __dadd_rn(s, (double)q[t]);
+        }
+        if (s < cur) {
+          cur = s;
+          lab = j - 1;
+        }
+        dd[gi] = cur;
+        dd32[gi] = __double2float_ru(cur);
+        labels[gi] = lab;
+      }
     }
   }
   const double tot = block_sum_fixed<kBlk>(live ? cur : 0.0);
@@ -761,6 +863,9 @@ struct Batch {
   std::vector<BProb> probs;       // internal order (k descending)
   std::vector<int> order;         // internal index -> caller's index
   std::vector<int32_t> block_prob;
+  std::vector<int32_t> cls_blocks;  // blocks of each width's problems (largest k first), classes in order
+  int cls_off[kNumD + 1] = {};
+  int32_t *d_cls_blocks = nullptr;
   std::vector<BItem> items;         // grouped by padded width, each group largest first
   int item_off[kNumD + 1] = {};     // group dc = items [item_off[dc], item_off[dc + 1])
   size_t smem_d[kNumD] = {};        // dynamic shared memory of each width's kernel
@@ -857,6 +962,13 @@ void plan_batch(Batch &B, const std::vector<int64_t> &n, const std::vector<int64
     B.items.insert(B.items.end(), groups[dc].begin(), groups[dc].end());
   }
   B.item_off[kNumD] = (int)B.items.size();
+  for (int dc = 0; dc < kNumD; ++dc) {
+    B.cls_off[dc] = (int)B.cls_blocks.size();
+    for (int q = 0; q < m; ++q)
+      if (dclass(B.probs[q].D) == dc)
+        for (int b = 0; b < B.probs[q].nb; ++b) B.cls_blocks.push_back(B.probs[q].b0 + b);
+  }
+  B.cls_off[kNumD] = (int)B.cls_blocks.size();
   B.xelems = xo;
   B.rows = row;
   B.kd = co;
@@ -887,6 +999,7 @@ sc_status alloc_batch(Batch &B) {
     B.d_probs = a.take<BProb>(B.count);
     B.st = a.take<BState>(B.count);
     B.d_block_prob = a.take<int32_t>(B.blocks);
+    B.d_cls_blocks = a.take<int32_t>(B.cls_blocks.size());
     B.d_items = a.take<BItem>(B.items.size());
     B.heads = a.take<unsigned>((size_t)(kGraphIters + 1) * kNumD);
     B.active = a.take<int>(1);
@@ -904,6 +1017,8 @@ sc_status upload_tables(Batch &B) {
   SC_CUDA(cudaMemcpyAsync(B.d_block_prob, B.block_prob.data(), B.block_prob.size() * sizeof(int32_t),
                           cudaMemcpyHostToDevice, B.s));
   SC_CUDA(cudaMemcpyAsync(B.d_items, B.items.data(), B.items.size() * sizeof(BItem), cudaMemcpyHostToDevice, B.s));
+  SC_CUDA(cudaMemcpyAsync(B.d_cls_blocks, B.cls_blocks.data(), B.cls_blocks.size() * sizeof(int32_t),
+                          cudaMemcpyHostToDevice, B.s));
   if (!B.uniforms.empty())
     SC_CUDA(cudaMemcpyAsync(B.d_uniforms, B.uniforms.data(), B.uniforms.size() * sizeof(double),
                             cudaMemcpyHostToDevice, B.s));
@@ -978,8 +1093,24 @@ template <typename T>
 sc_status run_setup(Batch &B) {
   cudaStream_t s = B.s;
   SC_CUDA(cudaMemsetAsync(B.absmax, 0, (size_t)B.count * sizeof(unsigned long long), s));
-  batch_scan_kernel<T><<<B.blocks, kBlk, 0, s>>>(B.d_block_prob, B.d_probs, (const T *)B.X, B.part, B.absmax);
-  SC_LAUNCHED();
+  if constexpr (sizeof(T) == 4) {
+    for (int dc = 0; dc < kNumD; ++dc) {
+      const int nb = B.cls_off[dc + 1] - B.cls_off[dc];
+      if (nb == 0) continue;
+      const int32_t *cb = B.d_cls_blocks + B.cls_off[dc];
+      const float *xf = (const float *)B.X;
+      switch (dc) {
+        case 0: batch_scan32_kernel<8><<<nb, kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
+        case 1: batch_scan32_kernel<16><<<nb, kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
+        case 2: batch_scan32_kernel<32><<<nb, kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
+        default: batch_scan32_kernel<64><<<nb, kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
+      }
+      SC_LAUNCHED();
+    }
+  } else {
+    batch_scan_kernel<T><<<B.blocks, kBlk, 0, s>>>(B.d_block_prob, B.d_probs, (const T *)B.X, B.part, B.absmax);
+    SC_LAUNCHED();
+  }
   batch_init_kernel<T><<<B.count, 64, 0, s>>>(B.d_probs, B.count, B.st, B.part, B.d_first, (const T *)B.X,
                                              (T *)B.seed_x, B.seed_idx);
   SC_LAUNCHED();
@@ -1001,18 +1132,43 @@ sc_status run_setup(Batch &B) {
   }
   SC_CUDA(cudaMemcpyAsync(B.d_probs, B.probs.data(), B.probs.size() * sizeof(BProb), cudaMemcpyHostToDevice, s));
   // k-means++: problems sorted by k descending, so those still drawing at
-  // step j are a prefix of the problems and their blocks a prefix of the blocks
+  // step j are a prefix of the problems and their blocks a prefix of the
+  // blocks (of each width's list too)
   std::vector<int> blocks_upto(B.count + 1, 0);
   for (int q = 0; q < B.count; ++q) blocks_upto[q + 1] = blocks_upto[q] + B.probs[q].nb;
+  std::vector<int> cls_probs[kNumD];  // each width's problems, largest k first
+  for (int q = 0; q < B.count; ++q) cls_probs[dclass(B.probs[q].D)].push_back(q);
   int q_ge = B.count, q_gt = B.count;
+  int cls_ge[kNumD], cls_nb[kNumD];
+  for (int dc = 0; dc < kNumD; ++dc) {
+    cls_ge[dc] = (int)cls_probs[dc].size();
+    cls_nb[dc] = B.cls_off[dc + 1] - B.cls_off[dc];
+  }
+  const PPFar32 far = pp_far_bound32(kMaxBD);  // d = 64 bounds the far test of every width
   for (int j = 1; j <= B.kmax; ++j) {
     while (q_ge > 0 && B.probs[q_ge - 1].k < j) --q_ge;
     while (q_gt > 0 && B.probs[q_gt - 1].k <= j) --q_gt;
-    if (q_ge > 0) {
-      // d of the far test: the largest d among the problems (a safe bound)
+    if constexpr (sizeof(T) == 4) {
+      for (int dc = 0; dc < kNumD; ++dc) {
+        while (cls_ge[dc] > 0 && B.probs[cls_probs[dc][cls_ge[dc] - 1]].k < j) {
+          --cls_ge[dc];
+          cls_nb[dc] -= B.probs[cls_probs[dc][cls_ge[dc]]].nb;
+        }
+        if (cls_nb[dc] == 0) continue;
+        const int32_t *cb = B.d_cls_blocks + B.cls_off[dc];
+        const float *xf = (const float *)B.X;
+        switch (dc) {
+          case 0: batch_pp_update32_kernel<8><<<cls_nb[dc], kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+          case 1: batch_pp_update32_kernel<16><<<cls_nb[dc], kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+          case 2: batch_pp_update32_kernel<32><<<cls_nb[dc], kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+          default: batch_pp_update32_kernel<64><<<cls_nb[dc], kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+        }
+        SC_LAUNCHED();
+      }
+    } else if (q_ge > 0) {
       batch_pp_update_kernel<T><<<blocks_upto[q_ge], kBlk, 0, s>>>(B.d_block_prob, B.d_probs, B.st, (const T *)B.X,
                                                                    B.dd, B.dd32, B.labels, B.part, B.seed_cc, j,
-                                                                   pp_far_bound32(kMaxBD));
+                                                                   far);
       SC_LAUNCHED();
     }
     if (q_gt > 0) {

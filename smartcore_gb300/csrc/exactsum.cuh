@@ -125,3 +125,48 @@ __device__ __forceinline__ bool sqd_seq_f32(PA a, PB b, int d, int lg_d, double 
 }
 
 }  // namespace sc
+
+namespace sc {
+
+// The same reproduction from terms already in registers: q[t] =
+// fl32((a_t - b_t)^2) for t < d (entries t >= d are ignored), D a compile-
+// time bound so that q stays in registers.
+template <int D>
+__device__ __forceinline__ bool sqd_seq_terms(const float (&q)[D], int d, int lg_d, double &out) {
+  int emin = 256, emax = 0;
+#pragma unroll
+  for (int t = 0; t < D; ++t) {
+    const uint32_t u = __float_as_uint(q[t]);
+    if (t < d && u != 0u) {
+      const int e = max((int)(u >> 23), 1);
+      emin = min(emin, e);
+      emax = max(emax, e);
+    }
+  }
+  if (emin == 256) { out = 0.0; return true; }
+  if (emax >= 255 || emax - emin > 38 - lg_d) return false;
+  unsigned long long S = 0;
+#pragma unroll
+  for (int t = 0; t < D; ++t) {
+    const uint32_t u = __float_as_uint(q[t]);
+    if (t < d && u != 0u) {
+      const int e = (int)(u >> 23);
+      const uint32_t m = (u & 0x7fffffu) | (e ? 0x800000u : 0u);
+      S += (unsigned long long)m << (max(e, 1) - emin);  // stays below 2^63
+      if (S >> 53) {  // more than 53 significant bits: round as the f64 addition does
+        const int drop = 11 - __clzll((long long)S);
+        const unsigned long long half = 1ull << (drop - 1), rem = S & ((half << 1) - 1ull);
+        unsigned long long qv = S >> drop;
+        if (rem > half || (rem == half && (qv & 1ull))) ++qv;
+        S = qv << drop;
+      }
+    }
+  }
+  const int pbit = 63 - __clzll((long long)S);
+  const unsigned long long mant = pbit <= 52 ? S << (52 - pbit) : S >> (pbit - 52);
+  const int ex = pbit + emin - 150 + 1023;
+  out = __longlong_as_double((long long)(((unsigned long long)ex << 52) | (mant & 0xfffffffffffffull)));
+  return true;
+}
+
+}  // namespace sc
