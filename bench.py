@@ -307,7 +307,9 @@ def bench_many_problems(torch):
     from smartcore_gb300.synthetic import batched_problems
     L = _lib.load()
     probs = batched_problems(count=MANY_PROBLEMS)
-    par = [(x, KMeansParameters(k=k, max_iter=MANY_MAX_ITER, seed=seed)) for x, k, seed in probs]
+    # the host rows live in pinned memory, as an application feeding a GPU keeps them
+    pinned = [torch.from_numpy(x).pin_memory().numpy() for x, _, _ in probs]
+    par = [(xp, KMeansParameters(k=k, max_iter=MANY_MAX_ITER, seed=seed)) for xp, (_, k, seed) in zip(pinned, probs)]
     t0 = time.perf_counter()
     batch_tune()
     tune_s = time.perf_counter() - t0
@@ -341,7 +343,149 @@ def bench_many_problems(torch):
                                        f"first {MANY_CPU_SAMPLE} problems, single thread"},
             "config": {"n": "log-uniform [1e3, 1e5]", "d": [8, 16, 32, 64], "k": "[4, 64]",
                        "max_iter": MANY_MAX_ITER, "h2d_bytes": int(sum(p[0].nbytes for p in probs)),
-                       "e2e": "one sc_kmeans_fit_batched call, host data in and out"}}
+                       "e2e": "one sc_kmeans_fit_batched call, host data (pinned) in and results out"}}
+
+
+LARGE_N, LARGE_D, LARGE_K, LARGE_MAX_ITER = 16_000_000, 128, 4096, 20
+LARGE_Q, LARGE_KNN_K = 1_000_000, 10
+LARGE_PREDICT_SAMPLE, LARGE_KNN_FP64_SAMPLE, LARGE_KNN_ORACLE_SAMPLE = 10_000, 512, 8
+
+
+def large_data(torch, dev, n_query):
+    """16,000,000 x 128 f32 points in 4,096 isotropic Gaussian blobs (centres
+    U[-50,50]^128, std 2.0, equal sizes, rows shuffled) and n_query queries
+    from the same mixture, generated on the device from seeded generators."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    centers = torch.rand((LARGE_K, LARGE_D), generator=g, device=dev, dtype=torch.float32) * 100.0 - 50.0
+    lab = torch.arange(LARGE_N, device=dev) % LARGE_K
+    lab = lab[torch.randperm(LARGE_N, generator=g, device=dev)]
+    x = torch.empty((LARGE_N, LARGE_D), device=dev, dtype=torch.float32)
+    for r0 in range(0, LARGE_N, 1 << 20):
+        r1 = min(LARGE_N, r0 + (1 << 20))
+        x[r0:r1] = centers[lab[r0:r1]] + 2.0 * torch.randn((r1 - r0, LARGE_D), generator=g, device=dev)
+    qlab = torch.randint(0, LARGE_K, (n_query,), generator=g, device=dev)
+    q = centers[qlab] + 2.0 * torch.randn((n_query, LARGE_D), generator=g, device=dev)
+    return x, q.contiguous()
+
+
+def bench_large(torch, local, n_query=LARGE_Q):
+    """The large workload: KMeans::fit on 16M x 128 f32 points, k = 4,096,
+    max_iter 20 (k-means++ and the Lloyd loop on device-resident data, split-
+    BF16 form: the streamed-centroid assignment kernel), then brute-force kNN
+    (k = 10) of n_query queries from the same mixture against the 16M rows.
+    Checks: the split form's predict with the final centroids against the
+    oracle on 10,000 sample rows; the kNN heaps against the FP64 GPU form on
+    512 queries and against the oracle on 8."""
+    import oracle
+    from smartcore_gb300 import _lib
+    from smartcore_gb300.cluster import KMeans, KMeansHandle, kmeanspp_draws
+    L = _lib.load()
+    dev = torch.device(f"cuda:{local}")
+    t0 = time.perf_counter()
+    x, q = large_data(torch, dev, n_query)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    out = {"config": {"n": LARGE_N, "d": LARGE_D, "k": LARGE_K, "max_iter": LARGE_MAX_ITER, "dtype": "f32",
+                      "data": f"4096 blobs, centres U[-50,50]^128, std 2 (generated on the device, {gen_s:.1f} s)",
+                      "knn_queries": n_query, "knn_k": LARGE_KNN_K}}
+    pk, pk_kind = peaks()
+    # ---- KMeans::fit, device-resident ----
+    h = KMeansHandle(None, form=_lib.FORM_SPLIT_BF16, device_ptr=x.data_ptr(), dtype=np.float32,
+                     shape=(LARGE_N, LARGE_D))
+    first, u = kmeanspp_draws(LARGE_N, LARGE_K, SEED_KMEANS)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h.seed(LARGE_K, first, u)
+    seed_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(h.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    L.sc_kmeans_profile(h.h, 1)
+    e0.record(stream)
+    iters = h.iterate(LARGE_MAX_ITER, stop_on_converge=True)
+    e1.record(stream)
+    e1.synchronize()
+    lloyd_ms = e0.elapsed_time(e1)
+    kms = np.zeros(1)
+    kl = np.zeros(1, np.int64)
+    L.sc_kmeans_profile_read(h.h, _lib.ptr(kms), _lib.ptr(kl))
+    rescored, replays = h.stats()
+    cent, sizes, _, dist, _ = h.get()
+    h.close()
+    assign_ms = float(kms[0]) / max(int(kl[0]), 1)
+    flop = 2.0 * LARGE_N * LARGE_K * LARGE_D
+    rs = np.random.default_rng(0).choice(LARGE_N, LARGE_PREDICT_SAMPLE, replace=False)
+    xs = x[torch.from_numpy(rs).to(dev)].cpu().numpy()
+    km = KMeans(LARGE_K, None, sizes, dist, cent, iters, _lib.FORM_SPLIT_BF16)
+    t0 = time.perf_counter()
+    ref = oracle.kmeans_predict(xs, cent)
+    cpu_pred_s = time.perf_counter() - t0
+    achieved = flop / (assign_ms / 1e3) / 1e12
+    out["kmeans"] = {
+        "lloyd_iters_per_s": iters / (lloyd_ms / 1e3), "iterations": iters, "lloyd_ms": lloyd_ms,
+        "seeding_s": seed_s, "assign_kernel_ms": assign_ms, "rescored_points_per_iter": rescored / max(iters, 1),
+        "pp_replays": replays, "distortion": dist,
+        "roofline": {"bound": "tensor", "kernel": "split_wide_kernel", "achieved": achieved,
+                     "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"],
+                     "peak_kind": f"{pk_kind} bf16 burst", "algorithmic_flop_per_launch": flop},
+        "predict_sample_oracle_equal": bool(np.array_equal(km.predict(xs), ref)),
+        "cpu_baseline": {"value": (LARGE_PREDICT_SAMPLE / LARGE_N) / cpu_pred_s,
+                         "unit": "assignment passes/s", "cores": 1, "kind": "port",
+                         "sample": f"C restatement of KMeans::predict (the brute-force assignment a BBD-tree step "
+                                   f"reduces to at d = 128) on {LARGE_PREDICT_SAMPLE} rows ({cpu_pred_s:.1f} s), "
+                                   f"scaled by {LARGE_PREDICT_SAMPLE}/{LARGE_N}, single thread"},
+    }
+    # ---- kNN: the queries against the 16M rows ----
+    hk = C.c_void_p()
+    _lib.check(L.sc_knn_create(C.c_void_p(x.data_ptr()), _lib.F32, _lib.ROW_MAJOR, _lib.MEM_DEVICE, LARGE_N,
+                               LARGE_D, LARGE_D, C.byref(hk)))
+    kstream = torch.cuda.ExternalStream(L.sc_knn_stream(hk))
+    idx = torch.empty((n_query, LARGE_KNN_K), dtype=torch.int64, device=dev)
+    dst = torch.empty((n_query, LARGE_KNN_K), dtype=torch.float64, device=dev)
+
+    def find(form, m):
+        _lib.check(L.sc_knn_find(hk, C.c_void_p(q.data_ptr()), _lib.ROW_MAJOR, _lib.MEM_DEVICE, m, LARGE_D,
+                                 LARGE_KNN_K, form, _lib.MEM_DEVICE, C.c_void_p(idx.data_ptr()),
+                                 C.c_void_p(dst.data_ptr())))
+    find(_lib.FORM_SPLIT_BF16, min(1024, n_query))  # warm-up: builds the training operand
+    torch.cuda.synchronize()
+    e0.record(kstream)
+    find(_lib.FORM_SPLIT_BF16, n_query)
+    e1.record(kstream)
+    e1.synchronize()
+    knn_ms = e0.elapsed_time(e1)
+    ev = np.zeros(1, np.int64)
+    L.sc_knn_stats(hk, _lib.ptr(ev))
+    ns = min(LARGE_KNN_FP64_SAMPLE, n_query)
+    si, sd = idx[:ns].cpu().numpy(), dst[:ns].cpu().numpy()
+    t0 = time.perf_counter()
+    find(_lib.FORM_FP64, ns)
+    torch.cuda.synchronize()
+    fp64_s = time.perf_counter() - t0
+    fi, fd = idx[:ns].cpu().numpy(), dst[:ns].cpu().numpy()
+    L.sc_knn_destroy(hk)
+    xt = x.cpu().numpy()
+    no = min(LARGE_KNN_ORACLE_SAMPLE, n_query)
+    t0 = time.perf_counter()
+    ridx, rdist = oracle.knn_find(xt, q[:no].cpu().numpy(), LARGE_KNN_K)
+    cpu_s = time.perf_counter() - t0
+    kflop = 2.0 * n_query * LARGE_N * LARGE_D
+    kach = kflop / (knn_ms / 1e3) / 1e12
+    out["knn"] = {
+        "queries_per_s": n_query / (knn_ms / 1e3), "ms": knn_ms, "exact_distance_evals": int(ev[0]),
+        "roofline": {"bound": "tensor", "kernel": "knn_split_kernel", "achieved": kach,
+                     "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": kach / pk["bf16_tflops"],
+                     "peak_kind": f"{pk_kind} bf16 burst"},
+        "heaps_equal_fp64_form": bool(np.array_equal(si, fi) and np.array_equal(sd, fd)),
+        "fp64_form_queries_per_s": ns / fp64_s,
+        "oracle_sample_equal": bool(np.array_equal(ridx, si[:no]) and np.array_equal(rdist, sd[:no])),
+        "cpu_baseline": {"value": no / cpu_s, "unit": "queries/s", "cores": 1, "kind": "port",
+                         "sample": f"C restatement of LinearKNNSearch::find on {no} queries "
+                                   f"against all {LARGE_N} rows ({cpu_s:.1f} s), single thread"},
+    }
+    del x, q, idx, dst, xt
+    torch.cuda.empty_cache()
+    return out
 
 
 DBSCAN_EPS = 8.0
@@ -544,6 +688,7 @@ def run_ours(args):
 
     knn = bench_knn(torch, local) if not args.no_knn else None
     many = bench_many_problems(torch) if not args.no_knn else None
+    large = bench_large(torch, local) if not (args.no_knn or args.no_large) else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -571,6 +716,7 @@ def run_ours(args):
         "rescored_points": int(rescored),
         "knn": knn,
         "many_problems": many,
+        "large": large,
     }
     print(json.dumps(line), flush=True)
     h.close()
@@ -589,6 +735,10 @@ def main():
                     help="time only the split-BF16 kNN find with this many queries (for profiler runs)")
     ap.add_argument("--neighbours-only", action="store_true",
                     help="time only the find_radius, DBSCAN and FastPair blocks (for profiler runs)")
+    ap.add_argument("--no-large", action="store_true", help="skip the 16M x 128 block")
+    ap.add_argument("--large-only", type=int, default=0, metavar="QUERIES",
+                    help="run only the 16M x 128 block, with this many kNN queries")
+    ap.add_argument("--many-only", action="store_true", help="run only the 512-problem block")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -604,6 +754,16 @@ def main():
         xt, _, xq, _ = knn_blobs_f32(KNN_N, KNN_M, KNN_D)
         print(json.dumps({"find_radius": bench_radius(torch, 0, xt, xq), "dbscan": bench_dbscan(torch, xt),
                           "fastpair": bench_fastpair(torch, xt)}), flush=True)
+        return
+    if args.large_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(bench_large(torch, 0, n_query=args.large_only)), flush=True)
+        return
+    if args.many_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(bench_many_problems(torch)), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

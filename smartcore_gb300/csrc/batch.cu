@@ -33,6 +33,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
+#include <cstdlib>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -67,7 +69,7 @@ struct BProb {
   int64_t x_off;   // element offset of row 0 in X
   int64_t row0;    // global index of row 0 (labels, dd, dd32)
   int64_t c_off;   // offset of the k x d arrays (cent64, acc, seed_x)
-  int64_t c32_off; // offset of the k_pad x D f32 centroid copies
+  int64_t c32_off; // offset of the f32 centroid copies: k_pad x D values, then k_pad ||c||^2
   int32_t n, d, D, k;
   int32_t k_off;   // offset of the per-cluster arrays
   int32_t b0, nb;  // 256-row blocks of the problem
@@ -87,7 +89,9 @@ struct BState {
   int64_t rescored;   // rows re-scored in FP64
   int64_t pp_replays; // draws resolved by the sequential replay
   float cdelta;       // >= max over centroids of ||c - fl32(c)||
+  float cmax;         // >= max over centroids of ||fl32(c)||
   int32_t done;
+  int32_t pad;
 };
 
 struct BItem {
@@ -223,6 +227,28 @@ __device__ __forceinline__ float dist32(const float (&x)[D], const float *__rest
   return __fadd_rn(a, b);
 }
 
+// Expansion-form score of the row x to centroid c: ||c~||^2 - 2 x~.c~ (the
+// row's own ||x~||^2, common to every centroid, is left out), the dot product
+// in two FMA chains.  Against ||c~||^2 - 2 S for the exact S = x~.c~:
+//   |score - (||c~||^2 - 2 S)| <= E_s = (2 g + 2u) ||x~|| cmax + 2.01 u cmax^2 + A
+// with g = (D/2 + 1) u (1.02) (the roundings a product passes through),
+// u = 2^-24, cn2 within 1.01 u of ||c~||^2, and A the underflow of the
+// products.  Differences of two scores then bound differences of the
+// D~ = ||x~ - c~||^2 within 2 E_s.
+template <int D>
+__device__ __forceinline__ float score32(const float (&x)[D], const float *__restrict__ c, float cn2) {
+  float a = 0.f, b = 0.f;
+#pragma unroll
+  for (int j = 0; j < D; j += 4) {
+    const float4 cc = *reinterpret_cast<const float4 *>(c + j);
+    a = __fmaf_rn(x[j], cc.x, a);
+    b = __fmaf_rn(x[j + 1], cc.y, b);
+    a = __fmaf_rn(x[j + 2], cc.z, a);
+    b = __fmaf_rn(x[j + 3], cc.w, b);
+  }
+  return __fmaf_rn(-2.f, __fadd_rn(a, b), cn2);
+}
+
 template <typename T, int D>
 __device__ __forceinline__ void load_row(const T *__restrict__ xr, float (&x)[D]) {
   if constexpr (sizeof(T) == 4) {
@@ -251,7 +277,7 @@ __device__ __forceinline__ void load_row(const T *__restrict__ xr, float (&x)[D]
 template <typename T, int D, int CU>
 __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BState *st, const T *__restrict__ X,
                                             const double *__restrict__ cent64, const float *s_c, float cdelta,
-                                            unsigned long long *s_acc, unsigned *s_cnt, int *s_lab,
+                                            float cmax, unsigned long long *s_acc, unsigned *s_cnt, int *s_lab,
                                             int32_t *__restrict__ labels, int mode) {
   const int d = P.d, k = P.k, kpad = (k + 7) & ~7;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -268,11 +294,12 @@ __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BSt
         load_row<T, D>(xr, x);
         float best = __int_as_float(0x7f800000), second = best;
         bi = 0;
+        const float *s_cn2 = s_c + kpad * D;
 #pragma unroll 1
         for (int c0 = 0; c0 < kpad; c0 += CU) {
           float a[CU];
 #pragma unroll
-          for (int u = 0; u < CU; ++u) a[u] = dist32<D>(x, s_c + (c0 + u) * D);
+          for (int u = 0; u < CU; ++u) a[u] = score32<D>(x, s_c + (c0 + u) * D, s_cn2[c0 + u]);
 #pragma unroll
           for (int u = 0; u < CU; ++u) {
             const float v = a[u];  // NaN (padding, empty clusters) never wins
@@ -285,23 +312,40 @@ __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BSt
             }
           }
         }
-        float del = cdelta;
-        if constexpr (sizeof(T) == 8) {  // ||x - fl32(x)|| <= 2^-24 ||x~|| (1 + 2^-20)
-          float xn = 0.f;
+        // ||x~|| from above; for f64 rows also ||x - fl32(x)|| <= 2^-24 ||x~|| (1 + 2^-20)
+        float xn = 0.f;
 #pragma unroll
-          for (int j = 0; j < D; ++j) xn = __fmaf_ru(x[j], x[j], xn);
-          del = __fadd_ru(del, __fmul_ru(__fsqrt_ru(xn), 0x1.00001p-24f));
+        for (int j = 0; j < D; ++j) xn = __fmaf_ru(x[j], x[j], xn);
+        const float rn = __fsqrt_ru(xn);
+        float del = cdelta;
+        if constexpr (sizeof(T) == 8) del = __fadd_ru(del, __fmul_ru(rn, 0x1.00001p-24f));
+        // The label is certain when the two best scores differ by more than
+        // 2 (2 E_s + 2 E_d): E_s bounds each score (score32), E_d >= |D - D~|
+        // for every centroid, 2 (||x~|| + cmax) del + del^2, plus the
+        // reference's own FP64 rounding of D; any other centroid's D then
+        // exceeds the best one's (a factor 2 of slack).
+        bool certain;
+        {
+          const float g2 = __fadd_ru(__fmul_ru((float)(D / 2 + 1), 0x1.06p-23f), 0x1p-23f);  // 2 g + 2 u
+          const float rc = __fmul_ru(rn, cmax);
+          float es = __fadd_ru(__fmul_ru(g2, rc), __fmul_ru(0x1.02p-23f, __fmul_ru(cmax, cmax)));
+          es = __fadd_ru(es, __fmul_ru((float)(D + 4), 0x1p-138f));
+          const float rs = __fadd_ru(rn, cmax);
+          float ed = __fadd_ru(__fmul_ru(__fmul_ru(2.f, rs), del), __fmul_ru(del, del));
+          ed = __fadd_ru(ed, __fmul_ru(__fmul_ru((float)(d + 2), 0x1p-52f), __fmul_ru(rs, rs)));
+          const float margin = __fmul_ru(4.f, __fadd_ru(es, ed));
+          certain = __fsub_rd(second, best) > margin;
         }
-        const Bound bd = make_bound(d, del);
-        const bool certain = second >= bd.floor16 &&
-                             __fsub_rd(second, err_bound(second, bd)) > __fadd_ru(best, err_bound(best, bd));
         if (!certain) {
-          // Near tie (or a non-finite value): every centroid whose FP32
-          // distance cannot be shown to exceed the best one's is scored with
-          // the reference's FP64 distance (src/metrics/distance/
-          // euclidian.rs:51-63 on f64 rows, kmeans.rs:338-346), strict <,
-          // lowest index first.
-          const float thr = __fadd_ru(best, err_bound(best, bd));
+          // Near tie (or a non-finite value): the difference form bounds each
+          // centroid's D on its own; every centroid whose FP32 distance cannot
+          // be shown to exceed the best one's is scored with the reference's
+          // FP64 distance (src/metrics/distance/euclidian.rs:51-63 on f64 rows,
+          // kmeans.rs:338-346), strict <, lowest index first.
+          const Bound bd = make_bound(d, del);
+          float best32 = __int_as_float(0x7f800000);
+          for (int c = 0; c < k; ++c) best32 = fminf(best32, dist32<D>(x, s_c + c * D));
+          const float thr = __fadd_ru(best32, err_bound(best32, bd));
           double bdist = DBL_MAX;
           int b = 0;
           for (int c = 0; c < k; ++c) {
@@ -343,12 +387,12 @@ __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BSt
 
 template <typename T, int D>
 __device__ __forceinline__ void assign_rows_cu(int cu, const BItem &it, const BProb &P, BState *st, const T *X,
-                                               const double *cent64, const float *s_c, float cdelta,
+                                               const double *cent64, const float *s_c, float cdelta, float cmax,
                                                unsigned long long *s_acc, unsigned *s_cnt, int *s_lab,
                                                int32_t *labels, int mode) {
-  if (cu == 2) assign_rows<T, D, 2>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, s_lab, labels, mode);
-  else if (cu == 8) assign_rows<T, D, 8>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, s_lab, labels, mode);
-  else assign_rows<T, D, 4>(it, P, st, X, cent64, s_c, cdelta, s_acc, s_cnt, s_lab, labels, mode);
+  if (cu == 2) assign_rows<T, D, 2>(it, P, st, X, cent64, s_c, cdelta, cmax, s_acc, s_cnt, s_lab, labels, mode);
+  else if (cu == 8) assign_rows<T, D, 8>(it, P, st, X, cent64, s_c, cdelta, cmax, s_acc, s_cnt, s_lab, labels, mode);
+  else assign_rows<T, D, 4>(it, P, st, X, cent64, s_c, cdelta, cmax, s_acc, s_cnt, s_lab, labels, mode);
 }
 
 // Resident CTAs per SM the compiler plans registers for, by row width.
@@ -380,21 +424,21 @@ batch_assign_kernel(const BItem *__restrict__ items, int nitems, const BProb *__
     if (mode == 0 && st[it.prob].done) continue;
     const BProb P = probs[it.prob];
     const int k = P.k, d = P.d, kpad = (k + 7) & ~7;
-    float *s_c = reinterpret_cast<float *>(smraw);
-    unsigned long long *s_acc = reinterpret_cast<unsigned long long *>(smraw + (size_t)kpad * D * 4);
+    float *s_c = reinterpret_cast<float *>(smraw);  // kpad x D values, then kpad ||c||^2
+    unsigned long long *s_acc = reinterpret_cast<unsigned long long *>(smraw + (size_t)kpad * (D + 1) * 4);
     unsigned *s_cnt = reinterpret_cast<unsigned *>(s_acc + (size_t)k * d);
     const bool reload = mode == 0 && s_prob != it.prob;
     __syncthreads();  // every thread has read s_prob
     if (reload) {
       const float4 *src = reinterpret_cast<const float4 *>(cent32 + P.c32_off);
-      for (int t = threadIdx.x; t < kpad * D / 4; t += kAsgThreads) reinterpret_cast<float4 *>(s_c)[t] = src[t];
+      for (int t = threadIdx.x; t < kpad * (D + 1) / 4; t += kAsgThreads) reinterpret_cast<float4 *>(s_c)[t] = src[t];
       if (threadIdx.x == 0) s_prob = it.prob;
     }
     for (int t = threadIdx.x; t < k * d; t += kAsgThreads) s_acc[t] = 0ull;
     for (int t = threadIdx.x; t < k; t += kAsgThreads) s_cnt[t] = 0u;
     __syncthreads();
-    assign_rows_cu<T, D>(it.variant, it, P, st + it.prob, X, cent64, s_c, st[it.prob].cdelta, s_acc, s_cnt, s_lab,
-                         labels, mode);
+    assign_rows_cu<T, D>(it.variant, it, P, st + it.prob, X, cent64, s_c, st[it.prob].cdelta, st[it.prob].cmax,
+                         s_acc, s_cnt, s_lab, labels, mode);
     __syncthreads();
     for (int t = threadIdx.x; t < k * d; t += kAsgThreads) {
       const long long v = (long long)s_acc[t];
@@ -414,7 +458,7 @@ __global__ void __launch_bounds__(kFinT)
 batch_finalize_kernel(const BProb *__restrict__ probs, BState *st, Acc128 *__restrict__ acc,
                       unsigned long long *__restrict__ cnt, double *__restrict__ cent64, float *__restrict__ cent32,
                       int64_t *__restrict__ sizes, int init, int *active) {
-  __shared__ float wd[kFinT / 32];
+  __shared__ float wd[kFinT / 32], wc[kFinT / 32];
   const int p = blockIdx.x;
   const BProb P = probs[p];
   BState *S = st + p;
@@ -463,25 +507,41 @@ batch_finalize_kernel(const BProb *__restrict__ probs, BState *st, Acc128 *__res
     if (c < k) v = j < d ? __double2float_rn(cent64[P.c_off + (int64_t)c * d + j]) : 0.f;
     cent32[P.c32_off + t] = v;
   }
-  // cdelta >= max_c ||c - fl32(c)|| (NaN centroids skipped)
-  float mx = 0.f;
-  for (int c = threadIdx.x; c < k; c += kFinT) {
-    double s = 0.0;
-    for (int j = 0; j < d; ++j) {
+  // per centroid: ||c~||^2 rounded to f32 (the f64 sum of the exact squares
+  // is within d 2^-53 of it), cdelta >= ||c - c~||, cmax >= ||c~|| (NaN
+  // centroids skipped in both maxima)
+  float mx = 0.f, mc = 0.f;
+  for (int c = threadIdx.x; c < kpad; c += kFinT) {
+    double s = 0.0, n2 = 0.0;
+    for (int j = 0; c < k && j < d; ++j) {
       const double v = cent64[P.c_off + (int64_t)c * d + j];
-      const double e = __dsub_rn(v, (double)__double2float_rn(v));
+      const double vf = (double)__double2float_rn(v);
+      const double e = __dsub_rn(v, vf);
       s = __fma_rn(e, e, s);
+      n2 = __fma_rn(vf, vf, n2);
     }
-    if (s == s) mx = fmaxf(mx, __fmul_ru(__fsqrt_ru(__double2float_ru(s)), 1.0001f));
+    cent32[P.c32_off + (int64_t)kpad * D + c] = c < k ? __double2float_rn(n2) : __int_as_float(0x7fc00000);
+    if (c < k && s == s) mx = fmaxf(mx, __fmul_ru(__fsqrt_ru(__double2float_ru(s)), 1.0001f));
+    if (c < k && n2 == n2) mc = fmaxf(mc, __fmul_ru(__fsqrt_ru(__double2float_ru(n2)), 1.0001f));
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) wd[threadIdx.x >> 5] = mx;
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mc = fmaxf(mc, __shfl_xor_sync(0xffffffffu, mc, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    wd[threadIdx.x >> 5] = mx;
+    wc[threadIdx.x >> 5] = mc;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    float m = 0.f;
-    for (int w = 0; w < kFinT / 32; ++w) m = fmaxf(m, wd[w]);
+    float m = 0.f, m2 = 0.f;
+    for (int w = 0; w < kFinT / 32; ++w) {
+      m = fmaxf(m, wd[w]);
+      m2 = fmaxf(m2, wc[w]);
+    }
     S->cdelta = m;
+    S->cmax = m2;
   }
 }
 
@@ -651,7 +711,7 @@ batch_pp_update_kernel(const int32_t *__restrict__ block_prob, const BProb *__re
 // 256-row block of the width's problems with k >= j (cls_blocks lists them,
 // largest k first).
 template <int D>
-__global__ void __launch_bounds__(kBlk)
+__global__ void __launch_bounds__(kBlk, AsgOcc<D>::value)
 batch_pp_update32_kernel(const int32_t *__restrict__ cls_blocks, const int32_t *__restrict__ block_prob,
                          const BProb *__restrict__ probs, const BState *__restrict__ st,
                          const float *__restrict__ X, double *__restrict__ dd, float *__restrict__ dd32,
@@ -677,23 +737,25 @@ batch_pp_update32_kernel(const int32_t *__restrict__ cls_blocks, const int32_t *
     if (first || !pp_far32(seed_cc[P.k_off + lab], c32, far)) {
       float x[D];
       load_row<float, D>(X + P.x_off + il * D, x);
-      float q[D];
-      float s32 = 0.f;
+      // the row's terms fl32((x_t - c_t)^2) overwrite the row (no second array)
 #pragma unroll
       for (int t = 0; t < D; ++t) {
         const float r = __fsub_rn(x[t], s_seed[t]);
-        q[t] = __fmul_rn(r, r);
-        if (t < d) s32 = __fadd_rn(s32, q[t]);
+        x[t] = __fmul_rn(r, r);
       }
+      float s32 = 0.f;
+#pragma unroll
+      for (int t = 0; t < D; ++t)
+        if (t < d) s32 = __fadd_rn(s32, x[t]);
       // the terms summed in f32 bound the reference's f64 sum from below by
       // s32 (1 - 1.05 d 2^-24): above the current distance, the row keeps it
       if (first || !(__fmul_rd(s32, 1.f - 1.05f * d * 0x1p-24f) > c32)) {
         double s = 0.0;
-        if (!sqd_seq_terms<D>(q, d, P.lg_d, s)) {
+        if (!sqd_seq_terms<D>(x, d, P.lg_d, s)) {
           s = 0.0;
 #pragma unroll
           for (int t = 0; t < D; ++t)
-            if (t < d) s = __dadd_rn(s, (double)q[t]);
+            if (t < d) s = __dadd_rn(s, (double)x[t]);
         }
         if (s < cur) {
           cur = s;
@@ -892,6 +954,27 @@ struct Batch {
   int *active = nullptr;
 };
 
+// Phase times of one batched call, printed to stderr when the environment
+// variable SMARTCORE_GB300_TRACE is set (each mark waits for the stream, so
+// tracing itself serialises the phases).
+struct PhaseTrace {
+  bool on = std::getenv("SMARTCORE_GB300_TRACE") != nullptr;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  std::string line;
+  void mark(const char *name, cudaStream_t s) {
+    if (!on) return;
+    if (s) cudaStreamSynchronize(s);
+    const auto t = std::chrono::steady_clock::now();
+    char buf[96];
+    snprintf(buf, sizeof buf, " %s %.2f ms", name, std::chrono::duration<double, std::milli>(t - t0).count());
+    line += buf;
+    t0 = t;
+  }
+  ~PhaseTrace() {
+    if (on) fprintf(stderr, "[smartcore_gb300] sc_kmeans_fit_batched:%s\n", line.c_str());
+  }
+};
+
 // Work items of problem q with the given rows per item and variant.
 void add_items(std::vector<BItem> &items, int q, int n, int rows, int cu) {
   for (int r0 = 0; r0 < n; r0 += rows) items.push_back(BItem{q, r0, std::min(n, r0 + rows), cu});
@@ -932,7 +1015,7 @@ void plan_batch(Batch &B, const std::vector<int64_t> &n, const std::vector<int64
     xo += ((int64_t)P.n * P.D + align - 1) / align * align;
     row += P.n;
     co += (int64_t)P.k * P.d;
-    c32 += (int64_t)((P.k + 7) & ~7) * P.D;
+    c32 += (int64_t)((P.k + 7) & ~7) * (P.D + 1);
     ko += P.k;
     uo += P.k - 1;
     blk += P.nb;
@@ -940,7 +1023,7 @@ void plan_batch(Batch &B, const std::vector<int64_t> &n, const std::vector<int64
     B.order[q] = caller_index[i];
     B.kmax = std::max(B.kmax, P.k);
     B.max_iter = std::max(B.max_iter, P.max_iter);
-    const size_t sm = (size_t)((P.k + 7) & ~7) * P.D * 4 + (size_t)P.k * P.d * 8 + (size_t)P.k * 4 + 64;
+    const size_t sm = (size_t)((P.k + 7) & ~7) * (P.D + 1) * 4 + (size_t)P.k * P.d * 8 + (size_t)P.k * 4 + 64;
     B.smem_d[dclass(P.D)] = std::max(B.smem_d[dclass(P.D)], sm);
     int cu, rows;
     tune_choice(P.D, P.k, &cu, &rows);
@@ -1307,6 +1390,7 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
   }
   if (who.empty()) return SC_OK;
 
+  PhaseTrace trace;
   Batch B;
   B.dtype = dtype;
   plan_batch(B, n, d, k, mi, who);
@@ -1318,9 +1402,11 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
   if (cudaStreamCreateWithFlags(&B.s, cudaStreamNonBlocking) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaStreamCreate");
   sc_status r = SC_OK;
   do {
+    trace.mark("plan", nullptr);
     if ((r = alloc_batch(B)) != SC_OK) break;
     if ((r = assign_grid(B, dtype)) != SC_OK) break;
     if ((r = upload_tables(B)) != SC_OK) break;
+    trace.mark("alloc", B.s);
     // rows into the padded layout
     const size_t es = esz(dtype);
     if (B.needs_pad && cudaMemsetAsync(B.X, 0, (size_t)B.xelems * es, B.s) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "memset"); break; }
@@ -1360,10 +1446,13 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
     }
     if (tmp) dev_free(tmp, B.s);
     if (r != SC_OK) break;
+    trace.mark("upload", B.s);
     r = dtype == SC_F32 ? run_setup<float>(B) : run_setup<double>(B);
     if (r != SC_OK) break;
+    trace.mark("seeding", B.s);
     r = dtype == SC_F32 ? run_lloyd<float>(B) : run_lloyd<double>(B);
     if (r != SC_OK) break;
+    trace.mark("lloyd", B.s);
     // results back to the callers' buffers
     std::vector<double> cent((size_t)B.kd);
     std::vector<int64_t> sizes((size_t)B.ksum);
@@ -1395,8 +1484,10 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
       pr.rescored = st[q].rescored;
       pr.pp_replays = st[q].pp_replays;
     }
+    trace.mark("results", nullptr);
   } while (0);
   free_batch(B);
+  trace.mark("free", nullptr);
   return r;
 }
 
