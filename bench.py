@@ -346,6 +346,62 @@ def bench_many_problems(torch):
                        "e2e": "one sc_kmeans_fit_batched call, host data (pinned) in and results out"}}
 
 
+def measure_pipe_peaks(torch, local):
+    """FP64 and FP32 (no TF32) GEMM rates of this GPU through cuBLAS (torch
+    matmul, 8192^3 for FP32, 4096^3 for FP64, best of 5 after a warm-up):
+    the denominators of the FP64 form's roofline, which the driver's peak
+    file does not record."""
+    dev = torch.device(f"cuda:{local}")
+    old_tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    out = {}
+    try:
+        for name, dt, n in (("fp64_tflops", torch.float64, 4096), ("fp32_tflops", torch.float32, 8192)):
+            a = torch.randn((n, n), device=dev, dtype=dt)
+            b = torch.randn((n, n), device=dev, dtype=dt)
+            torch.matmul(a, b)
+            torch.cuda.synchronize()
+            best = 1e30
+            for _ in range(5):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                torch.matmul(a, b)
+                e1.record()
+                e1.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            out[name] = 2.0 * n ** 3 / (best / 1e3) / 1e12
+            del a, b
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old_tf32
+    out["how"] = "cuBLAS via torch.matmul, FP64 4096^3 and FP32 8192^3 (TF32 off), best of 5, CUDA events"
+    return out
+
+
+def bench_fp64_kernels(torch, local):
+    """The FP64 form's kernels alone (for profiler runs): one Lloyd step of
+    the 1M x 64, k = 256 workload and a kNN find of 2,000 queries of the
+    200,000 x 32 training rows."""
+    from smartcore_gb300 import _lib
+    from smartcore_gb300.cluster import KMeansHandle, kmeanspp_draws
+    from smartcore_gb300.neighbors import LinearKNNSearch
+    from smartcore_gb300.synthetic import anisotropic_dirichlet_f32, knn_blobs_f32
+    x, _ = anisotropic_dirichlet_f32(N, D, K_CLUSTERS, seed=SEED_DATA)
+    h = KMeansHandle(x, form=_lib.FORM_FP64)
+    first, u = kmeanspp_draws(N, K_CLUSTERS, SEED_KMEANS)
+    h.seed(K_CLUSTERS, first, u)
+    t0 = time.perf_counter()
+    h.iterate(1, stop_on_converge=False)
+    lloyd_ms = 1e3 * (time.perf_counter() - t0)
+    h.close()
+    xt, _, xq, _ = knn_blobs_f32(KNN_N, 2000, KNN_D)
+    s = LinearKNNSearch(xt, form=_lib.FORM_FP64)
+    t0 = time.perf_counter()
+    s.find_batch(xq, KNN_K)
+    knn_ms = 1e3 * (time.perf_counter() - t0)
+    s.close()
+    return {"fp64_lloyd_step_ms": lloyd_ms, "fp64_knn_2000_queries_ms": knn_ms}
+
+
 LARGE_N, LARGE_D, LARGE_K, LARGE_MAX_ITER = 16_000_000, 128, 4096, 20
 LARGE_Q, LARGE_KNN_K = 1_000_000, 10
 LARGE_PREDICT_SAMPLE, LARGE_KNN_FP64_SAMPLE, LARGE_KNN_ORACLE_SAMPLE = 10_000, 512, 8
@@ -689,6 +745,7 @@ def run_ours(args):
     knn = bench_knn(torch, local) if not args.no_knn else None
     many = bench_many_problems(torch) if not args.no_knn else None
     large = bench_large(torch, local) if not (args.no_knn or args.no_large) else None
+    pipes = measure_pipe_peaks(torch, local)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -711,7 +768,15 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "fp64_form": {"value": 1e3 / float(np.median(fp64_ms)), "unit": UNIT,
-                      "split_speedup": value / ws / (1e3 / float(np.median(fp64_ms)))},
+                      "split_speedup": value / ws / (1e3 / float(np.median(fp64_ms))),
+                      "roofline": {"bound": "fp64", "kernel": "assign_fp64_kernel",
+                                   "achieved": 1.5 * flop / (float(np.median(fp64_ms)) / 1e3) / 1e12,
+                                   "peak": pipes["fp64_tflops"], "unit": "TFLOP/s",
+                                   "frac": 1.5 * flop / (float(np.median(fp64_ms)) / 1e3) / 1e12 / pipes["fp64_tflops"],
+                                   "note": "3 n k d FP64 operations (subtract, multiply, add: the reference's "
+                                           "unfused order) per step over the whole step's time, against cuBLAS "
+                                           "DGEMM's FMA rate"}},
+        "pipe_peaks": pipes,
         "parity_vs_fp64_form": agree,
         "rescored_points": int(rescored),
         "knn": knn,
@@ -739,6 +804,9 @@ def main():
     ap.add_argument("--large-only", type=int, default=0, metavar="QUERIES",
                     help="run only the 16M x 128 block, with this many kNN queries")
     ap.add_argument("--many-only", action="store_true", help="run only the 512-problem block")
+    ap.add_argument("--fp64-kernels", action="store_true",
+                    help="run the FP64 form's assignment and kNN kernels once each (for profiler runs)")
+    ap.add_argument("--peaks-only", action="store_true", help="measure the FP64 and FP32 GEMM rates only")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -759,6 +827,16 @@ def main():
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(bench_large(torch, 0, n_query=args.large_only)), flush=True)
+        return
+    if args.fp64_kernels:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(bench_fp64_kernels(torch, 0)), flush=True)
+        return
+    if args.peaks_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(measure_pipe_peaks(torch, 0)), flush=True)
         return
     if args.many_only:
         import torch

@@ -136,6 +136,12 @@ void *sc_kmeans_stream(sc_kmeans *h);
 /* Counters of the last sc_kmeans_iterate: near-tie points re-scored in FP64
  * (split form) and k-means++ draws that needed the sequential replay. */
 sc_status sc_kmeans_stats(sc_kmeans *h, int64_t *rescored, int64_t *pp_replays);
+/* Steps of the last sc_kmeans_iterate whose cluster sums were updated from
+ * the rows that changed label alone.  The sums are exact fixed-point
+ * integers, so moving a row's values from its old cluster's sum to its new
+ * one gives the same sums as summing every row again; a step takes that path
+ * when at most 1/32 of the rows changed label (f32 data). */
+sc_status sc_kmeans_sum_stats(sc_kmeans *h, int64_t *incremental_steps);
 /* Timing of the assignment kernel: with profiling enabled, every Lloyd
  * iteration records a CUDA event pair on the handle's stream around its
  * assignment kernel; profile_read returns the summed elapsed time and the

@@ -38,6 +38,7 @@ SIGNATURES = {
     "sc_kmeans_get": ([_P, _P, _P, _P, _P, _P], _I32),
     "sc_kmeans_stream": ([_P], _P),
     "sc_kmeans_stats": ([_P, _P, _P], _I32),
+    "sc_kmeans_sum_stats": ([_P, _P], _I32),
     "sc_kmeans_profile": ([_P, _I32], _I32),
     "sc_kmeans_profile_read": ([_P, _P, _P], _I32),
     "sc_kernel_launches": ([], _I64),

@@ -271,6 +271,12 @@ class KMeansHandle:
         _lib.check(self._L.sc_kmeans_stats(self.h, _lib.ptr(a[:1]), _lib.ptr(a[1:])))
         return int(a[0]), int(a[1])
 
+    def incremental_steps(self):
+        """Steps of the last iterate() whose sums moved only the relabelled rows."""
+        a = np.zeros(1, np.int64)
+        _lib.check(self._L.sc_kmeans_sum_stats(self.h, _lib.ptr(a)))
+        return int(a[0])
+
     def stream(self):
         return self._L.sc_kmeans_stream(self.h)
 

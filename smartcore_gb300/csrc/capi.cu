@@ -349,6 +349,7 @@ static sc_status seed_impl(sc_kmeans *h, int64_t k, int64_t first_index, const d
   // initial centroids: means of the seeding partition (kmeans.rs:275-292)
   SC_TRY(launch_update(&h->upd, h->dtype, h->x, h->n, (int)h->d, h->labels, (int)k, nullptr, s));
   SC_TRY(launch_finalize(&h->upd, h->cent, h->sizes, (int)k, (int)h->d, nullptr, 1, nullptr, s));
+  SC_TRY(update_mark_sums(&h->upd, h->labels, h->n, h->st, s));  // the first step may move rows alone
   if (h->form == SC_FORM_SPLIT_BF16) SC_TRY(split_centroids_changed(&h->split, h->cent, (int)k, s));
   SC_CUDA(cudaStreamSynchronize(s));
   return SC_OK;
@@ -415,6 +416,7 @@ sc_status sc_kmeans_iterate(sc_kmeans *h, int64_t max_iter, int32_t stop_on_conv
   const int64_t zero = 0;
   SC_CUDA(cudaMemcpyAsync(&h->st->iters, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
   SC_CUDA(cudaMemcpyAsync(&h->st->rescored, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
+  SC_CUDA(cudaMemcpyAsync(&h->st->incremental_steps, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
   for (int64_t t = 0; t < max_iter; ++t) SC_TRY(lloyd_step(h));
   if (iters_done) {
     SC_CUDA(cudaMemcpyAsync(iters_done, &h->st->iters, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -462,6 +464,15 @@ sc_status sc_kmeans_stats(sc_kmeans *h, int64_t *rescored, int64_t *pp_replays) 
   SC_CUDA(cudaStreamSynchronize(h->stream));
   if (rescored) *rescored = st.rescored;
   if (pp_replays) *pp_replays = st.pp_replays;
+  return SC_OK;
+}
+
+sc_status sc_kmeans_sum_stats(sc_kmeans *h, int64_t *incremental_steps) {
+  if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
+  LloydState st;
+  SC_CUDA(cudaMemcpyAsync(&st, h->st, sizeof st, cudaMemcpyDeviceToHost, h->stream));
+  SC_CUDA(cudaStreamSynchronize(h->stream));
+  if (incremental_steps) *incremental_steps = st.incremental_steps;
   return SC_OK;
 }
 

@@ -44,8 +44,10 @@ struct LloydState {
   int32_t done;        // break rule taken (kmeans.rs:305-309)
   int32_t stop;        // 1: apply the break rule; 0: run every iteration
   int32_t err;         // device-side consistency failure code (0 = none)
-  int32_t reserved;
+  int32_t sums_valid;  // the persistent cluster sums hold the sums of the previous labels
   int64_t pp_chosen;   // k-means++: row index of the current seed
+  int64_t moved;       // rows whose label changed in the current step
+  int64_t incremental_steps;  // steps whose sums were updated from the moved rows alone
 };
 
 // 128-bit fixed-point accumulator word pair (lo, hi), two's complement.
@@ -76,6 +78,15 @@ struct UpdateBuf {
   uint32_t *xq = nullptr;           // mode 1: the points in the packed fixed-point form of `scale`
   const void *xq_src = nullptr;     // the points xq was made from
   bool xq_slow = false;             // some value of xq needs the conversion from f32
+  // mode 1, incremental sums: the exact totals of the last step's labels
+  // persist, and a step in which few labels change moves only those rows'
+  // values between clusters (integer sums: the same totals as a full pass)
+  Acc128 *tot = nullptr;            // k x d
+  unsigned long long *tcnt = nullptr;  // k
+  int32_t *prev = nullptr;          // n: the labels the totals were summed for
+  int64_t *mrows = nullptr;         // moved rows of the step (at most mcap)
+  int32_t *mold = nullptr;          //   and their previous labels
+  int64_t mcap = 0;                 // moved rows above which the step runs the full pass
 };
 
 // ---- device memory ----
@@ -166,6 +177,10 @@ inline int64_t update_nterms(const UpdateBuf *u, int k, int d) {
   return u->mode != 0 ? ((int64_t)k * d + 31) / 32 : k;
 }
 void update_free(UpdateBuf *u, cudaStream_t s);
+// After a full pass outside the Lloyd loop (the seeding's initial means):
+// the labels the totals now hold and the flag that makes the next step's
+// incremental path available.
+sc_status update_mark_sums(const UpdateBuf *u, const int32_t *labels, int64_t n, LloydState *st, cudaStream_t s);
 // Packs the points for the balanced partial form (once per dataset and scale).
 sc_status update_pack(UpdateBuf *u, const float *x, int64_t n, int d, cudaStream_t s);
 sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n, int d,

@@ -220,6 +220,13 @@ __device__ __forceinline__ void add_packed64(long long &acc, uint32_t q, const f
   }
 }
 
+// The step updates the persistent totals from its moved rows alone when they
+// hold the previous labels' sums and at most mcap rows changed label; else
+// the full pass runs.  Every kernel of the step reads the same two values.
+__device__ __forceinline__ bool incremental_step(const LloydState *st, int64_t mcap) {
+  return st && st->sums_valid && st->moved <= mcap;
+}
+
 // Counting sort of a CTA's chunk by label (shared memory): cnt[c] points of
 // cluster c, off[c] .. off[c + 1] their positions in idx (chunk-relative rows).
 __device__ __forceinline__ void sort_chunk_by_label(const int32_t *__restrict__ labels, int64_t i0, int len, int k,
@@ -257,8 +264,8 @@ template <int MAXJ, bool PACKED, bool SLOW>
 __global__ void __launch_bounds__(1024)
 update_balanced_kernel(const float *__restrict__ x, const uint32_t *__restrict__ xq, int64_t n, int d,
                        const int32_t *__restrict__ labels, int k, long long *__restrict__ part,
-                       unsigned int *__restrict__ cpart, int scale, const LloydState *st) {
-  if (st && st->done) return;
+                       unsigned int *__restrict__ cpart, int scale, const LloydState *st, int64_t mcap) {
+  if (st && (st->done || incremental_step(st, mcap))) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   unsigned long long *acc = reinterpret_cast<unsigned long long *>(smraw);  // k x d
   const int kd = k * d;
@@ -353,8 +360,8 @@ template <typename T, int MAXJ>
 __global__ void __launch_bounds__(1024)
 update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *__restrict__ labels, int k,
                      long long *__restrict__ part, unsigned int *__restrict__ cpart, int scale,
-                     const LloydState *st) {
-  if (st && st->done) return;
+                     const LloydState *st, int64_t mcap) {
+  if (st && (st->done || incremental_step(st, mcap))) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   int *cnt = reinterpret_cast<int *>(smraw);  // k
   int *off = cnt + k;                         // k + 1
@@ -408,8 +415,9 @@ update_sorted_kernel(const T *__restrict__ x, int64_t n, int d, const int32_t *_
 __global__ void __launch_bounds__(256)
 finalize_partials_kernel(const long long *__restrict__ part, const unsigned int *__restrict__ cpart,
                          int nparts, int k, double *__restrict__ cent, int64_t *__restrict__ sizes, int d,
-                         int scale, double *__restrict__ terms, int empty_nan, const LloydState *st) {
-  if (st && st->done) return;
+                         int scale, double *__restrict__ terms, int empty_nan, const LloydState *st,
+                         Acc128 *__restrict__ tot, unsigned long long *__restrict__ tcnt, int64_t mcap) {
+  if (st && (st->done || incremental_step(st, mcap))) return;
   __shared__ unsigned long long s_lo[8][32], s_hi[8][32];
   __shared__ unsigned long long s_cn[8][32];
   const int64_t kd = (int64_t)k * d;
@@ -436,6 +444,11 @@ finalize_partials_kernel(const long long *__restrict__ part, const unsigned int 
       cn += s_cn[q][e];
     }
     const int c = (int)(t / d);
+    if (tot) {  // the totals of these labels, for the next step's incremental path
+      tot[t].lo = (unsigned long long)v;
+      tot[t].hi = (unsigned long long)(v >> 64);
+      if (t % d == 0) tcnt[c] = cn;
+    }
     const double sum = fixed_to_double((unsigned long long)v, (unsigned long long)(v >> 64), scale);
     const double dn = (double)cn;
     const double old = cent[t];
@@ -449,6 +462,103 @@ finalize_partials_kernel(const long long *__restrict__ part, const unsigned int 
     for (int o = 16; o > 0; o >>= 1) term += __shfl_down_sync(0xffffffffu, term, o);
     if (e == 0) terms[blockIdx.x] = term;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Incremental path of a step.  label_diff_kernel lists the rows whose label
+// differs from the one the totals were summed for (and records the new one);
+// moved_rows_kernel moves each listed row's fixed-point values from its old
+// cluster's totals to its new one's; finalize_total_kernel makes the
+// centroids and the distortion terms from the totals, element for element
+// and block for block as finalize_partials_kernel does, so both paths give
+// the same bits.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+label_diff_kernel(const int32_t *__restrict__ labels, int32_t *__restrict__ prev, int64_t n,
+                  int64_t *__restrict__ mrows, int32_t *__restrict__ mold, int64_t mcap, LloydState *st) {
+  if (st->done) return;
+  const int lane = threadIdx.x & 31;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;
+    int32_t l = 0, p = 0;
+    if (i < n) {
+      l = labels[i];
+      p = prev[i];
+    }
+    const bool moved = i < n && l != p;
+    const unsigned m = __ballot_sync(0xffffffffu, moved);
+    if (!m) continue;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd((unsigned long long *)&st->moved, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (moved) {
+      prev[i] = l;
+      const int64_t pos = (int64_t)base + __popc(m & ((1u << lane) - 1u));
+      if (pos < mcap) {
+        mrows[pos] = i;
+        mold[pos] = p;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void atomic_sub128(Acc128 *a, unsigned __int128 v) {
+  atomic_add128(a, (unsigned __int128)0 - v);
+}
+
+// One warp per moved row, lane = feature.
+__global__ void __launch_bounds__(256)
+moved_rows_kernel(const float *__restrict__ x, int d, const int32_t *__restrict__ labels,
+                  const int64_t *__restrict__ mrows, const int32_t *__restrict__ mold, int64_t mcap,
+                  Acc128 *__restrict__ tot, unsigned long long *__restrict__ tcnt, int scale, const LloydState *st) {
+  if (st->done || !incremental_step(st, mcap)) return;
+  const int64_t nm = st->moved;
+  const int lane = threadIdx.x & 31;
+  for (int64_t m = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < nm;
+       m += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t i = mrows[m];
+    const int cn = labels[i], co = mold[m];
+    const float *xr = x + i * (int64_t)d;
+    for (int j = lane; j < d; j += 32) {
+      const long long v = to_fixed64_slow(__float_as_uint(xr[j]), scale);
+      if (v) {
+        const unsigned __int128 w = (unsigned __int128)(__int128)v;
+        atomic_add128(&tot[(int64_t)cn * d + j], w);
+        atomic_sub128(&tot[(int64_t)co * d + j], w);
+      }
+    }
+    if (lane == 0) {
+      atomicAdd(&tcnt[cn], 1ull);
+      atomicAdd(&tcnt[co], ~0ull);  // minus one
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32)
+finalize_total_kernel(const Acc128 *__restrict__ tot, const unsigned long long *__restrict__ tcnt, int k,
+                      double *__restrict__ cent, int64_t *__restrict__ sizes, int d, int scale,
+                      double *__restrict__ terms, LloydState *st, int64_t mcap) {
+  if (st->done || !incremental_step(st, mcap)) return;
+  const int64_t kd = (int64_t)k * d;
+  const int e = threadIdx.x;
+  const int64_t t = (int64_t)blockIdx.x * 32 + e;
+  double term = 0.0;
+  if (t < kd) {
+    const int c = (int)(t / d);
+    const unsigned long long cn = tcnt[c];
+    const double sum = fixed_to_double(tot[t].lo, tot[t].hi, scale);
+    const double dn = (double)cn;
+    const double old = cent[t];
+    term = __fma_rn(old, __fma_rn(dn, old, -2.0 * sum), 0.0);
+    if (cn > 0) cent[t] = __ddiv_rn(sum, dn);
+    if (sizes && t % d == 0) sizes[c] = (int64_t)cn;
+  }
+  if (terms) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) term += __shfl_down_sync(0xffffffffu, term, o);
+    if (e == 0) terms[blockIdx.x] = term;
+  }
+  if (blockIdx.x == 0 && e == 0) st->incremental_steps += 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -542,6 +652,8 @@ finalize_scalar_kernel(const double *__restrict__ part, int nparts,
   st->last_dist = dist;
   if (st->stop && st->distortion <= dist) st->done = 1;
   else st->distortion = dist;
+  st->sums_valid = 1;  // either path left the totals of this step's labels
+  st->moved = 0;
 }
 
 sc_status launch_finalize_scalar(const double *part, int nparts,
@@ -667,6 +779,13 @@ sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double 
     u->balanced_smem = (d <= 128 && bal <= 200 * 1024) ? bal : 0;
     SC_TRY(dalloc(&u->part, (size_t)p.grid * k * d, s));
     SC_TRY(dalloc(&u->cpart, (size_t)p.grid * k, s));
+    // incremental sums: totals, the labels they hold, the moved-row list
+    u->mcap = std::min<int64_t>(n, n / 32 + 1);
+    SC_TRY(dalloc(&u->tot, (size_t)k * d, s));
+    SC_TRY(dalloc(&u->tcnt, (size_t)k, s));
+    SC_TRY(dalloc(&u->prev, (size_t)n, s));
+    SC_TRY(dalloc(&u->mrows, (size_t)u->mcap, s));
+    SC_TRY(dalloc(&u->mold, (size_t)u->mcap, s));
     return SC_OK;
   }
   SC_TRY(dalloc(&u->acc, (size_t)k * d, s));
@@ -677,6 +796,11 @@ sc_status update_alloc(UpdateBuf *u, int dtype, int64_t n, int d, int k, double 
 }
 
 void update_free(UpdateBuf *u, cudaStream_t s) {
+  dfree(u->tot, s);
+  dfree(u->tcnt, s);
+  dfree(u->prev, s);
+  dfree(u->mrows, s);
+  dfree(u->mold, s);
   dfree(u->xq, s);
   dfree(u->acc, s);
   dfree(u->cnt, s);
@@ -692,7 +816,7 @@ static sc_status launch_balanced(const UpdateBuf *u, const float *x, int64_t n, 
   auto kern = !packed ? update_balanced_kernel<MAXJ, false, false>
               : u->xq_slow ? update_balanced_kernel<MAXJ, true, true> : update_balanced_kernel<MAXJ, true, false>;
   SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->balanced_smem));
-  kern<<<u->grid, 1024, u->balanced_smem, s>>>(x, u->xq, n, d, labels, k, u->part, u->cpart, u->scale, st);
+  kern<<<u->grid, 1024, u->balanced_smem, s>>>(x, u->xq, n, d, labels, k, u->part, u->cpart, u->scale, st, u->mcap);
   SC_LAUNCHED();
   return SC_OK;
 }
@@ -721,7 +845,7 @@ static sc_status launch_sorted(const UpdateBuf *u, const float *x, int64_t n, in
                                const LloydState *st, cudaStream_t s) {
   auto kern = update_sorted_kernel<float, MAXJ>;
   SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->smem));
-  kern<<<u->grid, u->threads, u->smem, s>>>(x, n, d, labels, k, u->part, u->cpart, u->scale, st);
+  kern<<<u->grid, u->threads, u->smem, s>>>(x, n, d, labels, k, u->part, u->cpart, u->scale, st, u->mcap);
   SC_LAUNCHED();
   return SC_OK;
 }
@@ -735,15 +859,40 @@ sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n,
     return SC_ERR_INTERNAL;
   }
   const float *xf = (const float *)x;
-  if (u->balanced_smem) {
-    if (d <= 32) return launch_balanced<1>(u, xf, n, d, labels, k, st, s);
-    if (d <= 64) return launch_balanced<2>(u, xf, n, d, labels, k, st, s);
-    return launch_balanced<4>(u, xf, n, d, labels, k, st, s);
+  // a Lloyd step (st set): the rows that changed label, then the full pass or
+  // the moved rows, whichever the step's count selects on the device
+  LloydState *ms = const_cast<LloydState *>(st);
+  const int sms = u->grid > 0 ? u->grid : 1;
+  if (ms) {
+    label_diff_kernel<<<sms * 8, 256, 0, s>>>(labels, u->prev, n, u->mrows, u->mold, u->mcap, ms);
+    SC_LAUNCHED();
   }
-  if (d <= 32) return launch_sorted<1>(u, xf, n, d, labels, k, st, s);
-  if (d <= 64) return launch_sorted<2>(u, xf, n, d, labels, k, st, s);
-  if (d <= 128) return launch_sorted<4>(u, xf, n, d, labels, k, st, s);
-  return launch_sorted<8>(u, xf, n, d, labels, k, st, s);
+  if (u->balanced_smem) {
+    if (d <= 32) SC_TRY(launch_balanced<1>(u, xf, n, d, labels, k, st, s));
+    else if (d <= 64) SC_TRY(launch_balanced<2>(u, xf, n, d, labels, k, st, s));
+    else SC_TRY(launch_balanced<4>(u, xf, n, d, labels, k, st, s));
+  } else {
+    if (d <= 32) SC_TRY(launch_sorted<1>(u, xf, n, d, labels, k, st, s));
+    else if (d <= 64) SC_TRY(launch_sorted<2>(u, xf, n, d, labels, k, st, s));
+    else if (d <= 128) SC_TRY(launch_sorted<4>(u, xf, n, d, labels, k, st, s));
+    else SC_TRY(launch_sorted<8>(u, xf, n, d, labels, k, st, s));
+  }
+  if (ms) {
+    moved_rows_kernel<<<sms * 4, 256, 0, s>>>(xf, d, labels, u->mrows, u->mold, u->mcap, u->tot, u->tcnt, u->scale,
+                                             ms);
+    SC_LAUNCHED();
+  }
+  return SC_OK;
+}
+
+sc_status update_mark_sums(const UpdateBuf *u, const int32_t *labels, int64_t n, LloydState *st, cudaStream_t s) {
+  if (u->mode != 1 || !u->prev || n == 0) return SC_OK;
+  SC_CUDA(cudaMemcpyAsync(u->prev, labels, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+  static const int32_t one = 1;
+  static const int64_t zero = 0;
+  SC_CUDA(cudaMemcpyAsync(&st->sums_valid, &one, sizeof one, cudaMemcpyHostToDevice, s));
+  SC_CUDA(cudaMemcpyAsync(&st->moved, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
+  return SC_OK;
 }
 
 sc_status launch_finalize(const UpdateBuf *u, double *cent, int64_t *sizes, int k, int d,
@@ -753,8 +902,13 @@ sc_status launch_finalize(const UpdateBuf *u, double *cent, int64_t *sizes, int 
   const int64_t kd = (int64_t)k * d;
   const int blocks = (int)((kd + 31) / 32);
   finalize_partials_kernel<<<blocks, 256, 0, s>>>(u->part, u->cpart, u->grid, k, cent, sizes, d, u->scale, terms,
-                                                  empty_nan, st);
+                                                  empty_nan, st, u->tot, u->tcnt, u->mcap);
   SC_LAUNCHED();
+  if (st) {
+    finalize_total_kernel<<<blocks, 32, 0, s>>>(u->tot, u->tcnt, k, cent, sizes, d, u->scale, terms,
+                                                const_cast<LloydState *>(st), u->mcap);
+    SC_LAUNCHED();
+  }
   return SC_OK;
 }
 

@@ -241,3 +241,33 @@ def test_split_form_wide_rows_fit(dtype):
     assert_fit_parity(x, 10, 30, 3, _lib.FORM_SPLIT_BF16)
     km = KMeans.fit(x, KMeansParameters(k=10, max_iter=30, seed=3, form=_lib.FORM_SPLIT_BF16))
     assert np.array_equal(km.predict(x), km._y)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_incremental_sums_equal_full_pass(form):
+    """Steps whose sums move only the relabelled rows (few rows change label)
+    give the same bits as steps that sum every row: one handle iterates on
+    its own, the other is re-set to the same centroids before each step
+    (which forces the full pass)."""
+    x, _ = blobs(60_000, 24, 20, seed=8, dtype=np.float32)
+    c0 = np.ascontiguousarray(x[np.random.default_rng(3).choice(len(x), 20, replace=False)], np.float64)
+    a = KMeansHandle(x, form=form)
+    b = KMeansHandle(x, form=form)
+    a.set_centroids(c0)
+    inc = 0
+    cent = c0
+    for step in range(12):
+        b.set_centroids(cent)
+        a.iterate(1, stop_on_converge=False)
+        inc += a.incremental_steps()
+        b.iterate(1, stop_on_converge=False)
+        ca, sa, la, da, _ = a.get()
+        cb, sb, lb, db, _ = b.get()
+        assert np.array_equal(la, lb) and np.array_equal(sa, sb)
+        assert np.array_equal(ca, cb)
+        assert da == db
+        assert b.incremental_steps() == 0
+        cent = ca
+    assert inc >= 6  # the later steps move few rows
+    a.close()
+    b.close()
