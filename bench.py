@@ -404,7 +404,7 @@ def bench_fp64_kernels(torch, local):
 
 LARGE_N, LARGE_D, LARGE_K, LARGE_MAX_ITER = 16_000_000, 128, 4096, 20
 LARGE_Q, LARGE_KNN_K = 1_000_000, 10
-LARGE_PREDICT_SAMPLE, LARGE_KNN_FP64_SAMPLE, LARGE_KNN_ORACLE_SAMPLE = 10_000, 512, 8
+LARGE_PREDICT_SAMPLE, LARGE_KNN_FP64_SAMPLE, LARGE_KNN_ORACLE_SAMPLE = 10_000, 32, 8
 
 
 def large_data(torch, dev, n_query):
@@ -432,7 +432,7 @@ def bench_large(torch, local, n_query=LARGE_Q):
     (k = 10) of n_query queries from the same mixture against the 16M rows.
     Checks: the split form's predict with the final centroids against the
     oracle on 10,000 sample rows; the kNN heaps against the FP64 GPU form on
-    512 queries and against the oracle on 8."""
+    32 queries and against the oracle on 8."""
     import oracle
     from smartcore_gb300 import _lib
     from smartcore_gb300.cluster import KMeans, KMeansHandle, kmeanspp_draws

@@ -841,28 +841,25 @@ batch_pp_select_kernel(const BProb *__restrict__ probs, BState *st, const T *__r
         }
       }
     }
-    if (lane == 0) {
-      if (pick < 0) {  // the exact serial computation of kmeans.rs:381-396
-        double sum = 0.0;
-        for (int64_t r = 0; r < n; ++r) sum = __dadd_rn(sum, dd[r]);
-        const double cut = __dmul_rn(u, sum);
-        double cost = 0.0;
-        int64_t index = 0;
-        while (index < n) {
-          cost = __dadd_rn(cost, dd[index]);
-          if (cost >= cut) break;
-          ++index;
-        }
-        pick = index < n ? index : n - 1;
-        S->pp_replays += 1;
-      }
-      S->pp_chosen = pick;
-      seed_idx[P.k_off + j] = pick;
-      s_pick = pick;
-    }
+    if (lane == 0) s_pick = pick;
     __syncwarp();
   }
   __syncthreads();
+  if (s_pick < 0) {  // inside the rounding band: the exact sequential sum and prefix, by the CTA
+    double sum = 0.0;
+    int64_t index = n;
+    seq_exact_pass<kSelT>(dd, n, false, 0.0, &sum, nullptr);
+    seq_exact_pass<kSelT>(dd, n, true, __dmul_rn(u, sum), nullptr, &index);
+    if (t == 0) {
+      s_pick = index < n ? index : n - 1;
+      S->pp_replays += 1;
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    S->pp_chosen = s_pick;
+    seed_idx[P.k_off + j] = s_pick;
+  }
   const T *xp = X + P.x_off + (int64_t)s_pick * P.D;
   for (int c = t; c < P.d; c += kSelT) seed_x[P.c_off + (int64_t)j * P.d + c] = xp[c];
   if constexpr (sizeof(T) == 4) pp_seed_gaps<kSelT>(xp, P.d, seed_x + P.c_off, j, seed_cc + P.k_off);

@@ -695,27 +695,24 @@ pp_select_kernel(const T *__restrict__ x, int d, const double *__restrict__ dd,
         }
       }
     }
-    if (lane == 0) {
-      if (pick < 0) {  // the exact serial computation of kmeans.rs:381-396
-        double sum = 0.0;
-        for (int64_t r = 0; r < n; ++r) sum = __dadd_rn(sum, dd[r]);
-        const double cut = __dmul_rn(u, sum);
-        double cost = 0.0;
-        int64_t index = 0;
-        while (index < n) {
-          cost = __dadd_rn(cost, dd[index]);
-          if (cost >= cut) break;
-          ++index;
-        }
-        pick = index < n ? index : n - 1;
-        st->pp_replays += 1;
-      }
-      st->pp_chosen = pick;
-      s_pick = pick;
-    }
+    if (lane == 0) s_pick = pick;
     __syncwarp();
   }
   __syncthreads();
+  if (s_pick < 0) {
+    // The cutoff is inside the rounding band: the exact values of the
+    // sequential sum and prefix of kmeans.rs:381-396, by the whole CTA.
+    double sum = 0.0;
+    int64_t index = n;
+    seq_exact_pass<kSelThreads>(dd, n, false, 0.0, &sum, nullptr);
+    seq_exact_pass<kSelThreads>(dd, n, true, __dmul_rn(u, sum), nullptr, &index);
+    if (t == 0) {
+      s_pick = index < n ? index : n - 1;
+      st->pp_replays += 1;
+    }
+    __syncthreads();
+  }
+  if (t == 0) st->pp_chosen = s_pick;
   const T *xp = x + (int64_t)s_pick * d;
   for (int c = t; c < d; c += kSelThreads) seed_x[(int64_t)j * d + c] = xp[c];
   pp_seed_gaps<kSelThreads>(xp, d, seed_x, j, seed_cc);

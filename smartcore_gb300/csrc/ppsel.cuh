@@ -4,6 +4,9 @@
 // seed selection.  Both translation units are compiled with -fmad=false.
 #pragma once
 
+#include <cfloat>
+#include <climits>
+
 #include <cuda_runtime.h>
 
 namespace sc {
@@ -169,6 +172,195 @@ __device__ void pp_seed_gaps(const T *__restrict__ xp, int d, const T *__restric
       if (lane == 0 && a < j) seed_cc[a] = fmaxf(0.f, lo);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Exact sequential f64 sum of nonnegative doubles by a whole CTA: the values
+// the reference's loops `sum += d[i]` and `cost += d[index]` take, bit for
+// bit, in parallel.  While the running sum S stays inside one binade, every
+// addition rounds to the same grid q (the binade's ulp): with S = N q,
+// S + v rounds to (N + r) q, where r is v / q rounded to an integer; only
+// an exact tie depends on S, through the parity of N (ties to even).  So an
+// addend is a function of the parity: (grid steps added, parity after), and
+// these compose associatively: a CTA scan gives every prefix's N.  The first
+// element whose sum leaves the binade (N reaches 2^53) is added with one real
+// f64 addition, and the scan resumes after it on the new grid.  Binades only
+// grow, so a pass rescans at most one chunk per binade change.
+// ---------------------------------------------------------------------------
+struct SeqFn {
+  unsigned long long d0, d1;  // grid steps added for parity 0 / 1 of N (saturating at 2^62)
+  int f0, f1;                 // parity of N after the addend, for parity 0 / 1 before
+};
+constexpr unsigned long long kSeqCap = 1ull << 62;
+
+__device__ __forceinline__ SeqFn seq_identity() { return SeqFn{0ull, 0ull, 0, 1}; }
+
+__device__ __forceinline__ SeqFn seq_compose(const SeqFn &a, const SeqFn &b) {  // a, then b
+  SeqFn r;
+  r.d0 = min(a.d0 + (a.f0 ? b.d1 : b.d0), kSeqCap);
+  r.d1 = min(a.d1 + (a.f1 ? b.d1 : b.d0), kSeqCap);
+  r.f0 = a.f0 ? b.f1 : b.f0;
+  r.f1 = a.f1 ? b.f1 : b.f0;
+  return r;
+}
+
+// The addend v >= 0 on the grid 2^qe.
+__device__ __forceinline__ SeqFn seq_elem(double v, int qe) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int ef = (int)((b >> 52) & 0x7ff);
+  const unsigned long long M = (b & 0xfffffffffffffull) | (ef ? (1ull << 52) : 0ull);
+  const int e = (ef ? ef : 1) - 1075;  // v = M 2^e
+  unsigned long long m = 0;
+  int cls = 1;  // 0 below half, 1 exact, 2 above half, 3 tie
+  if (M != 0) {
+    const int s = qe - e;
+    if (s <= 0) {
+      const int sh = -s;
+      m = (sh >= 62 || (M >> (62 - sh)) != 0ull) ? kSeqCap : (M << sh);
+    } else if (s >= 64) {
+      cls = 0;
+    } else {
+      m = M >> s;
+      const unsigned long long rem = M & ((1ull << s) - 1ull), half = 1ull << (s - 1);
+      cls = rem == 0ull ? 1 : (rem < half ? 0 : (rem > half ? 2 : 3));
+    }
+  }
+  SeqFn f;
+  if (cls == 3) {  // the result is even whatever the parity before
+    f.d0 = m + (m & 1ull);
+    f.d1 = m + ((m + 1ull) & 1ull);
+    f.f0 = 0;
+    f.f1 = 0;
+  } else {
+    const unsigned long long r = m + (cls == 2 ? 1ull : 0ull);
+    f.d0 = r;
+    f.d1 = r;
+    f.f0 = (int)(r & 1ull);
+    f.f1 = (int)((r + 1ull) & 1ull);
+  }
+  return f;
+}
+
+__device__ __forceinline__ SeqFn seq_shfl_up(const SeqFn &f, int o) {
+  SeqFn r;
+  r.d0 = __shfl_up_sync(0xffffffffu, f.d0, o);
+  r.d1 = __shfl_up_sync(0xffffffffu, f.d1, o);
+  r.f0 = __shfl_up_sync(0xffffffffu, f.f0, o);
+  r.f1 = __shfl_up_sync(0xffffffffu, f.f1, o);
+  return r;
+}
+
+// Whole CTA of NT threads.  find = false: *sum_out = the sequential sum of
+// v[0..n).  find = true: *index_out = the first i whose sequential prefix
+// through v[i] is >= cutoff (n when none).
+template <int NT>
+__device__ void seq_exact_pass(const double *__restrict__ v, int64_t n, bool find, double cutoff, double *sum_out,
+                               int64_t *index_out) {
+  constexpr int E = 4, NW = NT / 32;
+  constexpr int64_t CH = (int64_t)NT * E;
+  constexpr unsigned long long kTop = 1ull << 53;
+  __shared__ unsigned long long s_d0[NW], s_d1[NW];
+  __shared__ int s_f0[NW], s_f1[NW];
+  __shared__ double s_S, s_Snew;
+  __shared__ long long s_j, s_ovf, s_crs;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) {
+    s_S = 0.0;
+    s_j = 0;
+  }
+  __syncthreads();
+  int64_t found = -1;
+  for (;;) {
+    const double S = s_S;
+    const int64_t j = s_j;
+    if (j >= n) break;
+    if (t == 0) {
+      s_ovf = LLONG_MAX;
+      s_crs = LLONG_MAX;
+    }
+    const unsigned long long sb = (unsigned long long)__double_as_longlong(S);
+    const int ef = (int)((sb >> 52) & 0x7ff);
+    const int qe = (ef ? ef : 1) - 1075;
+    const unsigned long long N0 = (sb & 0xfffffffffffffull) | (ef ? (1ull << 52) : 0ull);
+    const int p0 = (int)(N0 & 1ull);
+    const int64_t e0 = j + (int64_t)t * E;
+    SeqFn fe[E];
+    SeqFn F = seq_identity();
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      fe[e] = e0 + e < n ? seq_elem(v[e0 + e], qe) : seq_identity();
+      F = seq_compose(F, fe[e]);
+    }
+    // inclusive warp scan, then the warps' totals in order
+    SeqFn G = F;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const SeqFn y = seq_shfl_up(G, o);
+      if (lane >= o) G = seq_compose(y, G);
+    }
+    if (lane == 31) {
+      s_d0[w] = G.d0;
+      s_d1[w] = G.d1;
+      s_f0[w] = G.f0;
+      s_f1[w] = G.f1;
+    }
+    __syncthreads();
+    SeqFn P = seq_identity();  // everything before this warp
+    for (int q = 0; q < w; ++q) P = seq_compose(P, SeqFn{s_d0[q], s_d1[q], s_f0[q], s_f1[q]});
+    SeqFn Gx = seq_shfl_up(G, 1);  // exclusive within the warp
+    if (lane == 0) Gx = seq_identity();
+    P = seq_compose(P, Gx);
+    unsigned long long N = min(N0 + (p0 ? P.d1 : P.d0), kSeqCap);
+    int par = p0 ? P.f1 : P.f0;
+    long long my_ovf = LLONG_MAX, my_crs = LLONG_MAX;
+    unsigned long long n_before = N;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      if (e0 + e >= n) break;
+      const unsigned long long Ne = min(N + (par ? fe[e].d1 : fe[e].d0), kSeqCap);
+      if (Ne >= kTop) {  // this addend leaves the binade
+        my_ovf = e0 + e;
+        n_before = N;
+        break;
+      }
+      if (find && my_crs == LLONG_MAX && ldexp((double)Ne, qe) >= cutoff) my_crs = e0 + e;
+      N = Ne;
+      par = par ? fe[e].f1 : fe[e].f0;
+    }
+    if (my_ovf != LLONG_MAX) atomicMin(&s_ovf, my_ovf);
+    if (my_crs != LLONG_MAX) atomicMin(&s_crs, my_crs);
+    __syncthreads();
+    const long long ovf = s_ovf, crs = s_crs;
+    if (ovf != LLONG_MAX && my_ovf == ovf)  // the one real addition of the segment
+      s_Snew = __dadd_rn(ldexp((double)n_before, qe), v[ovf]);
+    // the sum after the chunk when nothing left the binade
+    const int64_t last = min(n, j + CH) - 1;
+    if (ovf == LLONG_MAX && e0 <= last && last < e0 + E) s_Snew = ldexp((double)N, qe);
+    __syncthreads();
+    const double Sn = s_Snew;
+    __syncthreads();
+    if (find && crs != LLONG_MAX && crs < ovf) { found = crs; break; }
+    if (ovf != LLONG_MAX && !(Sn <= DBL_MAX)) {  // the sum overflowed: it stays +inf from here on
+      if (find) found = Sn >= cutoff ? ovf : n;
+      else if (t == 0) s_S = Sn;
+      __syncthreads();
+      break;
+    }
+    if (ovf != LLONG_MAX) {
+      if (find && Sn >= cutoff) { found = ovf; break; }
+      if (t == 0) {
+        s_S = Sn;
+        s_j = ovf + 1;
+      }
+    } else if (t == 0) {
+      s_S = Sn;
+      s_j = j + CH;
+    }
+    __syncthreads();
+  }
+  if (sum_out) *sum_out = s_S;
+  if (index_out) *index_out = found < 0 ? n : found;
+  __syncthreads();
 }
 
 }  // namespace sc

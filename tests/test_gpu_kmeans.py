@@ -271,3 +271,59 @@ def test_incremental_sums_equal_full_pass(form):
     assert inc >= 6  # the later steps move few rows
     a.close()
     b.close()
+
+
+def replay_cases():
+    rng = np.random.default_rng(11)
+    # rows spanning 32 decades: the sequential f64 sum absorbs the small terms
+    wide = rng.normal(size=(40_000, 3)) * (10.0 ** rng.uniform(-8, 8, size=(40_000, 1)))
+    # integer rows far apart: squared distances are integers whose running sum
+    # passes 2^53, where additions round and ties go to even
+    grid = rng.integers(-2 ** 12, 2 ** 12, size=(60_000, 4)).astype(np.float64) * 2.0 ** 10
+    u = np.array([1.0 - 2.0 ** -53, 1.0 - 2.0 ** -52, 0.5, 1.0 - 2.0 ** -50, 0.25, 1.0 - 2.0 ** -53, 0.75])
+    return [(wide, u), (grid, u)]
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["wide_span", "integer_grid"])
+def test_kmeanspp_exact_replay_adversarial(case):
+    """Draws whose cutoff is inside the rounding band take the CTA-wide exact
+    reproduction of the sequential sum and prefix (binade by binade, ties to
+    even): the chosen seeds equal the oracle's sequential loop."""
+    x, u = replay_cases()[case]
+    k = len(u) + 1
+    h = KMeansHandle(x)
+    h.seed(k, 3, u)
+    _, _, labels, _, _ = h.get()
+    assert h.stats()[1] >= 2
+    y, chosen = oracle.kmeanspp(x, k, 3, u)
+    assert np.array_equal(labels, y)
+    h.close()
+
+
+def test_batched_exact_replay_adversarial():
+    """The batched selection takes the same exact reproduction: problems with
+    hand-set draws whose cutoffs fall inside the rounding band."""
+    import ctypes as C
+    L = _lib.load()
+    cases = replay_cases()
+    arr = (_lib.KMeansProblem * len(cases))()
+    keep, outs = [], []
+    for i, (x, u) in enumerate(cases):
+        x = np.ascontiguousarray(x)
+        k = len(u) + 1
+        n, d = x.shape
+        labels = np.zeros(n, np.int64)
+        cent = np.zeros((k, d))
+        iters = np.zeros(1, np.int64)
+        keep += [x, u, labels, cent, iters]
+        outs.append((x, u, labels, cent, iters))
+        q = arr[i]
+        q.x, q.layout, q.n, q.d, q.ld = x.ctypes.data, _lib.ROW_MAJOR, n, d, d
+        q.k, q.max_iter, q.first_index, q.uniforms = k, 5, 3, u.ctypes.data
+        q.labels_out, q.centroids_out, q.iters_out = labels.ctypes.data, cent.ctypes.data, iters.ctypes.data
+    _lib.check(L.sc_kmeans_fit_batched(C.cast(arr, C.c_void_p), len(cases), _lib.F64, _lib.FORM_FP64))
+    assert sum(arr[i].pp_replays for i in range(len(cases))) >= 2
+    for x, u, labels, cent, iters in outs:
+        ref = oracle.kmeans_fit(x, len(u) + 1, 5, first=3, uniforms=u)
+        assert np.array_equal(labels, ref.labels)
+        assert int(iters[0]) == ref.iters
