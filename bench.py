@@ -675,6 +675,7 @@ def run_ours(args):
     L.sc_kmeans_profile_read(h.h, _lib.ptr(kms), _lib.ptr(kl))
     L.sc_kmeans_profile(h.h, 0)
     rescored, _ = h.stats()
+    incremental = h.incremental_steps()
     kernel_ms = float(kms[0]) / max(int(kl[0]), 1)
     value = job_rate(args.steps, ws, ms)
 
@@ -772,6 +773,7 @@ def run_ours(args):
         "pipe_peaks": pipes,
         "parity_vs_fp64_form": agree,
         "rescored_points": int(rescored),
+        "incremental_sum_steps": int(incremental),
         "knn": knn,
         "many_problems": many,
         "large": large,
