@@ -367,18 +367,35 @@ __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BSt
     }
     s_lab[threadIdx.x] = bi;
     __syncwarp();
-    // exact fixed-point sums of the warp's rows, one row at a time
+    // exact fixed-point sums of the warp's rows, four rows' loads in flight
     const int rw = base + w * 32;
-    for (int q = 0; q < 32; ++q) {
-      const int lab = s_lab[w * 32 + q];
-      if (lab < 0) break;  // rows past the item's end (uniform over the warp)
-      const T *xr = X + P.x_off + (int64_t)(rw + q) * D;
-      unsigned long long *ar = s_acc + (int64_t)lab * d;
-      for (int j = lane; j < d; j += 32) {
-        const long long v = fixed64(xr[j], P.scale);
-        if (v) atomicAdd(ar + j, (unsigned long long)v);
+    constexpr int JW = D > 32 ? 2 : 1;  // features per lane
+    for (int q0 = 0; q0 < 32; q0 += 4) {
+      int lab[4];
+      T v[4][JW];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        lab[u] = s_lab[w * 32 + q0 + u];  // -1: past the item's end (uniform over the warp)
+        const T *xr = X + P.x_off + (int64_t)(rw + q0 + u) * D;
+#pragma unroll
+        for (int h = 0; h < JW; ++h) {
+          const int j = lane + 32 * h;
+          v[u][h] = (lab[u] >= 0 && j < d) ? xr[j] : T(0);
+        }
       }
-      if (lane == 0) atomicAdd(&s_cnt[lab], 1u);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (lab[u] < 0) break;
+        unsigned long long *ar = s_acc + (int64_t)lab[u] * d;
+#pragma unroll
+        for (int h = 0; h < JW; ++h) {
+          const int j = lane + 32 * h;
+          const long long fv = j < d ? fixed64(v[u][h], P.scale) : 0ll;
+          if (fv) atomicAdd(ar + j, (unsigned long long)fv);
+        }
+        if (lane == 0) atomicAdd(&s_cnt[lab[u]], 1u);
+      }
+      if (lab[3] < 0) break;
     }
     __syncwarp();  // s_lab is rewritten by the next pass
   }
