@@ -297,9 +297,30 @@ __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BSt
         const float *s_cn2 = s_c + kpad * D;
 #pragma unroll 1
         for (int c0 = 0; c0 < kpad; c0 += CU) {
-          float a[CU];
+          // the CU centroids' dot products in 2 CU independent FMA chains,
+          // interleaved feature group by feature group (score32's order per
+          // centroid, so the same roundings)
+          float a[CU], b[CU];
 #pragma unroll
-          for (int u = 0; u < CU; ++u) a[u] = score32<D>(x, s_c + (c0 + u) * D, s_cn2[c0 + u]);
+          for (int u = 0; u < CU; ++u) {
+            a[u] = 0.f;
+            b[u] = 0.f;
+          }
+#pragma unroll
+          for (int j = 0; j < D; j += 4) {
+            float4 cc[CU];
+#pragma unroll
+            for (int u = 0; u < CU; ++u) cc[u] = *reinterpret_cast<const float4 *>(s_c + (c0 + u) * D + j);
+#pragma unroll
+            for (int u = 0; u < CU; ++u) {
+              a[u] = __fmaf_rn(x[j], cc[u].x, a[u]);
+              b[u] = __fmaf_rn(x[j + 1], cc[u].y, b[u]);
+              a[u] = __fmaf_rn(x[j + 2], cc[u].z, a[u]);
+              b[u] = __fmaf_rn(x[j + 3], cc[u].w, b[u]);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < CU; ++u) a[u] = __fmaf_rn(-2.f, __fadd_rn(a[u], b[u]), s_cn2[c0 + u]);
 #pragma unroll
           for (int u = 0; u < CU; ++u) {
             const float v = a[u];  // NaN (padding, empty clusters) never wins
