@@ -332,6 +332,10 @@ sc_status sc_debug_fail_alloc_after(int64_t after);
 /* Device allocations of the library not yet freed (stream-ordered frees
  * count as freed when issued). */
 int64_t sc_debug_live_allocations(void);
+/* Candidate slots per query of the split-BF16 find (cap <= 0 restores the
+ * default, about 4 k (1 + ln(n / k))); queries with more candidates are
+ * served by the FP64 kernel.  A small cap exercises that path. */
+sc_status sc_debug_knn_candidate_cap(int64_t cap);
 
 #ifdef __cplusplus
 }

@@ -514,6 +514,11 @@ sc_status sc_debug_fail_alloc_after(int64_t after) {
 
 int64_t sc_debug_live_allocations(void) { return (int64_t)g_live_allocs.load(); }
 
+sc_status sc_debug_knn_candidate_cap(int64_t cap) {
+  split_knn_set_candidate_cap(cap);
+  return SC_OK;
+}
+
 sc_status sc_kmeans_sync(sc_kmeans *h) {
   if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
   SC_CUDA(cudaStreamSynchronize(h->stream));
@@ -604,7 +609,7 @@ static sc_status knn_run(sc_knn *h, const void *queries, int32_t layout, int32_t
   if (k > (1 << 24)) { set_error("k=%lld is too large", (long long)k); return SC_ERR_INVALID; }
   if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
   // beyond the split kernel's heaps and tiles the FP64 kernel serves the call (same results)
-  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, (int)k)) form = SC_FORM_FP64;
+  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, (int)k, h->dtype, false)) form = SC_FORM_FP64;
   SC_TRY(knn_reserve(h, m, k));
   SC_TRY(upload_matrix(queries, h->dtype, layout, mem, m, h->d, ld, h->q, h->stream));
   if (form == SC_FORM_FP64)
@@ -681,7 +686,7 @@ sc_status sc_knn_find(sc_knn *h, const void *queries, int32_t layout, int32_t me
 // query rows (row-major), in index order: CSR lists off (m + 1) and idx.
 static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double radius, int32_t form,
                               std::vector<int64_t> &off, std::vector<int64_t> &idx) {
-  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, 1)) form = SC_FORM_FP64;
+  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, 1, h->dtype, true)) form = SC_FORM_FP64;
   off.assign((size_t)m + 1, 0);
   idx.clear();
   if (m == 0) return SC_OK;
@@ -865,7 +870,7 @@ sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout, int
   if (!(radius > 0.0)) { set_error("radius should be > 0"); return SC_ERR_INVALID; }  // linear_search.rs:90-95
   SC_TRY(check_matrix(queries, h->dtype, layout, mem, m, h->d, ld));
   if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
-  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, 1)) form = SC_FORM_FP64;
+  if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, 1, h->dtype, true)) form = SC_FORM_FP64;
   if (total_out) *total_out = 0;
   if (m == 0) return SC_OK;
   SC_TRY(knn_reserve(h, m, 1));

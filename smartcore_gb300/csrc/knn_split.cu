@@ -31,8 +31,10 @@ constexpr int kFilterWarps = 8;  // 2 accumulator buffers x 4 TMEM lane quarters
 constexpr int kKnnThreads = 32 * (2 + kOwnerWarps + kFilterWarps);  // + warp 0 TMA, warp 1 MMA
 constexpr int kMaskSlots = 4;    // candidate-mask tiles between the filters and the owners
 constexpr uint64_t kWaitNs = 2000000000ull;
-constexpr int kQueue = 1024;     // per owner warp: ring of pending candidates (owner lane << 27 | row)
+constexpr int kQueue = 64;       // per owner warp: ring of pending candidates (owner lane << 27 | row);
+                                 // a round runs once 32 are pending, and a column adds at most 32
 constexpr int kRowBits = 27;     // training rows per handle < 2^27
+constexpr int kStageFloats = 1056;  // per owner warp (f32 data): training rows, then query rows (528 floats each)
 
 // One term of Euclidian::squared_distance (src/metrics/distance/
 // euclidian.rs:56-62): r = a - b and r * r in the element type, then to_f64.
@@ -144,23 +146,198 @@ __device__ __forceinline__ void heap_sift(double *hD, int32_t *hi, int kk, int n
   }
 }
 
-// Pulls training row j toward L1 when it is queued, tiles before its exact
-// distance is computed.
+// Pulls training row j into L2 when it is queued, tiles before its exact
+// distance is computed (L1 is almost all shared memory in this kernel).
 template <typename T>
 __device__ __forceinline__ void prefetch_row(const T *train, int64_t j, int d) {
   const char *a = (const char *)(train + j * (int64_t)d);
   const char *b = a + (size_t)d * sizeof(T) - 1;
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
-  if (((uintptr_t)a >> 7) != ((uintptr_t)b >> 7)) asm volatile("prefetch.global.L1 [%0];" ::"l"(b));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+  if (((uintptr_t)a >> 7) != ((uintptr_t)b >> 7)) asm volatile("prefetch.global.L2 [%0];" ::"l"(b));
+}
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool in) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(in ? 4 : 0)
+               : "memory");
+}
+
+// Exact reference squared distances of up to 32 queued f32 entries (lane r:
+// entry r).  Groups of entries are staged by asynchronous copies, coalesced
+// (lane l copies features l, l + 32, ...), into the warp's slice of shared
+// memory (Sx: training rows, Sq: query rows; zeros past d), so that all of a
+// group's loads are in flight at once without holding registers.
+//  - d <= 32 (KC = 1): 16 entries a group at a row stride of 33 floats; lane r
+//    then sums its own entry from shared memory (conflict-free): branch-free
+//    where no running sum can round, else the sequential form, FP64 only
+//    where the exponent span is too wide for that.
+//  - wider rows (KC = 2 or 8 features a lane): 16 / KC entries a group, each
+//    summed across the warp by warp_sqd_terms (a lane reads back only what it
+//    copied itself); fb is set where a running sum may round and the caller
+//    runs the sequential form.
+// Lane r gets entry r's distance in sq.
+template <int KC>
+__device__ __forceinline__ void round_dist_f32(const float *__restrict__ train, const float *__restrict__ queries,
+                                               uint32_t e, uint32_t cnt, int64_t qbase, int64_t m, int d, int lg_d,
+                                               int lane, float *Sx, float *Sq, double &sq, bool &fb) {
+  constexpr int G = 16 / KC, W = KC == 1 ? 33 : 32 * KC;
+  const bool live = (uint32_t)lane < cnt && qbase + (int)(e >> kRowBits) < m;
+  unsigned long long S = 0ull;
+  uint32_t emin = 256u;
+  bool ok = true;
+  for (uint32_t b0 = 0; b0 < cnt; b0 += G) {
+#pragma unroll
+    for (int r = 0; r < G; ++r) {
+      const uint32_t er = __shfl_sync(0xffffffffu, e, (int)((b0 + r) & 31u));
+      const int64_t qr = qbase + (int)(er >> kRowBits);
+      const bool in_r = b0 + r < cnt && qr < m;
+      const float *tr = train + (int64_t)(er & ((1u << kRowBits) - 1u)) * d;
+      const float *qrow = queries + qr * d;
+#pragma unroll
+      for (int c = 0; c < KC; ++c) {
+        const int f = 32 * c + lane;
+        const bool in = in_r && f < d;
+        cp_async4(Sx + r * W + f, in ? tr + f : train, in);
+        cp_async4(Sq + r * W + f, in ? qrow + f : queries, in);
+      }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    if constexpr (KC == 1) {
+      __syncwarp();  // every lane's copies have landed
+      const int r = lane - (int)b0;
+      if (live && r >= 0 && r < G) {
+        if (!sqd_f32_d32(Sq + r * W, Sx + r * W, d, lg_d, sq)) {
+          sq = 0.0;
+          for (int t = 0; t < d; ++t) sq = __dadd_rn(sq, ref_term(Sq[r * W + t], Sx[r * W + t]));
+        }
+      }
+      __syncwarp();  // before the next group's copies
+    } else {
+      constexpr int NB = KC == 2 ? 2 : 1;
+#pragma unroll
+      for (int r0 = 0; r0 < G; r0 += NB) {
+        if (b0 + r0 >= cnt) break;
+        float t[NB][KC];
+#pragma unroll
+        for (int r = 0; r < NB; ++r)
+#pragma unroll
+          for (int c = 0; c < KC; ++c) {
+            const int o = (r0 + r) * W + 32 * c + lane;
+            const float df = __fsub_rn(Sq[o], Sx[o]);
+            t[r][c] = __fmul_rn(df, df);
+          }
+        warp_sqd_terms<KC, NB>(t, lg_d, lane, (int)(b0 + r0), S, emin, ok);
+      }
+    }
+  }
+  if constexpr (KC != 1) {
+    if (live) {
+      fb = !ok;
+      if (ok) sq = sqd_from_units(S, emin);
+    }
+  }
 }
 
 // Threshold on a_j below which a row may enter the heap: D_root - ||q||^2 + E,
 // rounded up (a larger threshold only admits more rows to the exact test),
 // in f32 with a margin of 2^-22 (D_root + ||q||^2) for the f32 roundings.
-__device__ __forceinline__ float knn_threshold(double droot, double qn2, float eq) {
-  if (!(droot < DBL_MAX)) return __int_as_float(0x7f800000);
-  const float r = __double2float_ru(droot), qf = __double2float_rd(qn2);
+// qf is ||q||^2 rounded down to f32 (once per query).
+__device__ __forceinline__ float knn_threshold(double droot, float qf, float eq) {
+  const long long b = __double_as_longlong(droot);  // droot >= 0 or +inf: integer tests, no FP64 pipe
+  if (b >= 0x7ff0000000000000ll) return __int_as_float(0x7f800000);
+  // an f32 upper bound of droot: its top 23 fraction bits plus one ulp
+  const int e = (int)(b >> 52) - 1023;
+  const float r = e > 127 ? __int_as_float(0x7f800000)
+                  : e < -126 ? 0x1p-126f
+                             : __uint_as_float((((uint32_t)(e + 127) << 23) | (uint32_t)((b >> 29) & 0x7fffff)) + 1u);
   return __fadd_ru(__fadd_ru(__fsub_ru(r, qf), eq), __fmul_ru(0x1p-22f, __fadd_ru(r, qf)));
+}
+
+// The shared-memory pipeline of the split kNN kernels: the query tile (A,
+// resident per query tile), training tiles (B, `stages` deep) and the two
+// TMEM accumulators, with their barriers.
+struct KnnPipe {
+  uint8_t *sA, *sOnes, *sB;
+  uint64_t *full, *empty, *afull, *aempty, *accfull, *accempty, *mma_done;
+  int *s_abort;
+  int a_blk, a_bytes, b_blk, b_stage;
+  int n_tiles_q, n_tiles_t, nkt, kt_elems, row_bytes, stages;
+};
+
+// TMA producer (one thread): per query tile its split halves once (and the
+// ones tile on the first), then the training tiles in index order.
+template <int TN>
+__device__ void knn_tma_role(const KnnPipe &P, const CUtensorMap *tm_qh, const CUtensorMap *tm_ql,
+                             const CUtensorMap *tm_th, const CUtensorMap *tm_tl, const CUtensorMap *tm_ones,
+                             const CUtensorMap *tm_tbx) {
+  int it = 0, ql = 0;
+  bool ok = true;
+  for (int qt = blockIdx.x; ok && qt < P.n_tiles_q; qt += gridDim.x, ++ql) {
+    if (!tc::mbar_wait(P.aempty, (uint32_t)(ql & 1) ^ 1u, kWaitNs)) { ok = false; break; }
+    tc::mbar_expect_tx(P.afull, (uint32_t)(P.a_bytes + (ql == 0 ? kQM * 32 : 0)));
+    for (int part = 0; part < 2; ++part)
+      for (int kt = 0; kt < P.nkt; ++kt)
+        tc::tma_load_2d(P.sA + (part * P.nkt + kt) * P.a_blk, part ? tm_ql : tm_qh, P.afull, kt * P.kt_elems,
+                        qt * kQM);
+    if (ql == 0) tc::tma_load_2d(P.sOnes, tm_ones, P.afull, 0, 0);
+    for (int tt = 0; tt < P.n_tiles_t; ++tt, ++it) {
+      const int s = it % P.stages;
+      const uint32_t ph = (uint32_t)(it / P.stages) & 1u;
+      if (!tc::mbar_wait(&P.empty[s], ph ^ 1u, kWaitNs) || *(volatile int *)P.s_abort) { ok = false; break; }
+      tc::mbar_expect_tx(&P.full[s], (uint32_t)P.b_stage);
+      uint8_t *dst = P.sB + (size_t)s * P.b_stage;
+      for (int part = 0; part < 2; ++part)
+        for (int kt = 0; kt < P.nkt; ++kt)
+          tc::tma_load_2d(dst + (part * P.nkt + kt) * P.b_blk, part ? tm_tl : tm_th, &P.full[s], kt * P.kt_elems,
+                          tt * TN);
+      tc::tma_load_2d(dst + 2 * P.nkt * P.b_blk, tm_tbx, &P.full[s], 0, tt * TN);
+    }
+  }
+  if (!ok) atomicExch(P.s_abort, 1);
+  for (int j = (it > P.stages ? it - P.stages : 0); j < it; ++j)  // drain in-flight copies
+    tc::mbar_wait(&P.full[j % P.stages], (uint32_t)(j / P.stages) & 1u, kWaitNs);
+  if (ql > 0) tc::mbar_wait(P.afull, (uint32_t)((ql - 1) & 1), kWaitNs);
+}
+
+// MMA issuer (one thread): per training tile, into accumulator it & 1,
+// -||t||^2 / 2 (ones x norm-folding rows) then q_h.t_h + q_h.t_l + q_l.t_h.
+template <int TN>
+__device__ void knn_mma_role(const KnnPipe &P, uint32_t tmem) {
+  const uint32_t idesc = tc::idesc_bf16_f32(kQM, TN);
+  const uint32_t sA0 = tc::smem_u32(P.sA), sB0 = tc::smem_u32(P.sB);
+  const uint64_t ones_desc = tc::smem_desc(tc::smem_u32(P.sOnes), 32);
+  int it = 0, ql = 0;
+  bool ok = true;
+  for (int qt = blockIdx.x; ok && qt < P.n_tiles_q; qt += gridDim.x, ++ql) {
+    if (!tc::mbar_wait(P.afull, (uint32_t)(ql & 1), kWaitNs)) { ok = false; break; }
+    for (int tt = 0; tt < P.n_tiles_t; ++tt, ++it) {
+      const int s = it % P.stages, acc = it & 1;
+      const uint32_t ph = (uint32_t)(it / P.stages) & 1u, aph = (uint32_t)(it >> 1) & 1u;
+      if (!tc::mbar_wait(&P.accempty[acc], aph ^ 1u, kWaitNs) || !tc::mbar_wait(&P.full[s], ph, kWaitNs) ||
+          *(volatile int *)P.s_abort) {
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+      const uint32_t d_tmem = tmem + (uint32_t)(acc * TN);
+      const uint32_t b0 = sB0 + (uint32_t)(s * P.b_stage);
+      tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(2 * P.nkt * P.b_blk), 32), idesc, 0u);
+      for (int prod = 0; prod < 3; ++prod) {
+        const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
+        for (int kt = 0; kt < P.nkt; ++kt)
+          for (int ks = 0; ks < P.kt_elems / 16; ++ks) {
+            const uint64_t ad = tc::smem_desc(sA0 + (uint32_t)((pa * P.nkt + kt) * P.a_blk + ks * 32), P.row_bytes);
+            const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((pb * P.nkt + kt) * P.b_blk + ks * 32), P.row_bytes);
+            tc::mma_f16(d_tmem, ad, bd, idesc, 1u);
+          }
+      }
+      tc::mma_commit(&P.empty[s]);
+      tc::mma_commit(&P.accfull[acc]);
+    }
+    tc::mma_commit(P.aempty);  // the query tile's smem is free once these MMAs complete
+  }
+  if (!ok) atomicExch(P.s_abort, 1);
+  tc::mma_commit(P.mma_done);
+  tc::mbar_wait(P.mma_done, 0, kWaitNs);
 }
 
 // Roles: warp 0 TMA (query tile once, training tiles in index order), warp 1
@@ -189,8 +366,9 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   uint8_t *sOnes = base + a_bytes;                   // 128 x 32 B
   uint8_t *sB = sOnes + kQM * 32;
   uint32_t *sQ = (uint32_t *)(sB + (size_t)p.stages * b_stage);  // owner warps x kQueue entries
-  uint32_t *sMask = sQ + kOwnerWarps * kQueue;                   // [slot][query][word]
-  float *s_lo = (float *)(sMask + kMaskSlots * kQM * kWords);    // per query: filter threshold on acc
+  uint32_t *sMask = sQ + kOwnerWarps * kQueue;                   // [slot][word][query]
+  float *s_stage = (float *)(sMask + kMaskSlots * kQM * kWords);  // f32: owner warps x kStageFloats
+  float *s_lo = s_stage + (sizeof(T) == 4 ? kOwnerWarps * kStageFloats : 0);  // per query: filter threshold on acc
   double *s_rs = (double *)(s_lo + kQM);                          // owner warps x 32: round distances
   int32_t *s_rj = (int32_t *)(s_rs + kOwnerWarps * 32);            //   rows
   uint32_t *s_rg = (uint32_t *)(s_rj + kOwnerWarps * 32);          //   entries per owner lane
@@ -237,76 +415,13 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   tc::fence_after_sync();
   const uint32_t tmem = *s_tmem;
 
+  const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
+                  a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
+                  p.stages};
   if (warp == 0) {
-    if (lane == 0) {  // ---------------- TMA producer ----------------
-      int it = 0, ql = 0;
-      bool ok = true;
-      for (int qt = blockIdx.x; ok && qt < p.n_tiles_q; qt += gridDim.x, ++ql) {
-        if (!tc::mbar_wait(aempty, (uint32_t)(ql & 1) ^ 1u, kWaitNs)) { ok = false; break; }
-        tc::mbar_expect_tx(afull, (uint32_t)(a_bytes + (ql == 0 ? kQM * 32 : 0)));
-        for (int part = 0; part < 2; ++part)
-          for (int kt = 0; kt < p.nkt; ++kt)
-            tc::tma_load_2d(sA + (part * p.nkt + kt) * a_blk, part ? &tm_ql : &tm_qh, afull, kt * p.kt_elems,
-                            qt * kQM);
-        if (ql == 0) tc::tma_load_2d(sOnes, &tm_ones, afull, 0, 0);
-        for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
-          const int s = it % p.stages;
-          const uint32_t ph = (uint32_t)(it / p.stages) & 1u;
-          if (!tc::mbar_wait(&empty[s], ph ^ 1u, kWaitNs) || *(volatile int *)s_abort) { ok = false; break; }
-          tc::mbar_expect_tx(&full[s], (uint32_t)b_stage);
-          uint8_t *dst = sB + (size_t)s * b_stage;
-          for (int part = 0; part < 2; ++part)
-            for (int kt = 0; kt < p.nkt; ++kt)
-              tc::tma_load_2d(dst + (part * p.nkt + kt) * b_blk, part ? &tm_tl : &tm_th, &full[s],
-                              kt * p.kt_elems, tt * TN);
-          tc::tma_load_2d(dst + 2 * p.nkt * b_blk, &tm_tbx, &full[s], 0, tt * TN);
-        }
-      }
-      if (!ok) atomicExch(s_abort, 1);
-      for (int j = (it > p.stages ? it - p.stages : 0); j < it; ++j)  // drain in-flight copies
-        tc::mbar_wait(&full[j % p.stages], (uint32_t)(j / p.stages) & 1u, kWaitNs);
-      if (ql > 0) tc::mbar_wait(afull, (uint32_t)((ql - 1) & 1), kWaitNs);
-    }
+    if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
   } else if (warp == 1) {
-    if (lane == 0) {  // ---------------- MMA issuer ----------------
-      const uint32_t idesc = tc::idesc_bf16_f32(kQM, TN);
-      const uint32_t sA0 = tc::smem_u32(sA), sB0 = tc::smem_u32(sB);
-      const uint64_t ones_desc = tc::smem_desc(tc::smem_u32(sOnes), 32);
-      int it = 0, ql = 0;
-      bool ok = true;
-      for (int qt = blockIdx.x; ok && qt < p.n_tiles_q; qt += gridDim.x, ++ql) {
-        if (!tc::mbar_wait(afull, (uint32_t)(ql & 1), kWaitNs)) { ok = false; break; }
-        for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
-          const int s = it % p.stages, acc = it & 1;
-          const uint32_t ph = (uint32_t)(it / p.stages) & 1u, aph = (uint32_t)(it >> 1) & 1u;
-          if (!tc::mbar_wait(&accempty[acc], aph ^ 1u, kWaitNs) || !tc::mbar_wait(&full[s], ph, kWaitNs) ||
-              *(volatile int *)s_abort) {
-            ok = false;
-            break;
-          }
-          tc::fence_after_sync();
-          const uint32_t d_tmem = tmem + (uint32_t)(acc * TN);
-          const uint32_t b0 = sB0 + (uint32_t)(s * b_stage);
-          // -||t||^2 / 2 first, then q_h.t_h + q_h.t_l + q_l.t_h
-          tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(2 * p.nkt * b_blk), 32), idesc, 0u);
-          for (int prod = 0; prod < 3; ++prod) {
-            const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
-            for (int kt = 0; kt < p.nkt; ++kt)
-              for (int ks = 0; ks < p.kt_elems / 16; ++ks) {
-                const uint64_t ad = tc::smem_desc(sA0 + (uint32_t)((pa * p.nkt + kt) * a_blk + ks * 32), p.row_bytes);
-                const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((pb * p.nkt + kt) * b_blk + ks * 32), p.row_bytes);
-                tc::mma_f16(d_tmem, ad, bd, idesc, 1u);
-              }
-          }
-          tc::mma_commit(&empty[s]);
-          tc::mma_commit(&accfull[acc]);
-        }
-        tc::mma_commit(aempty);  // the query tile's smem is free once these MMAs complete
-      }
-      if (!ok) atomicExch(s_abort, 1);
-      tc::mma_commit(mma_done);
-      tc::mbar_wait(mma_done, 0, kWaitNs);
-    }
+    if (lane == 0) knn_mma_role<TN>(P, tmem);
   } else if (warp < 2 + kOwnerWarps) {
     // ---------------- owners: one query per thread ----------------
     // The candidates of a tile arrive as bit masks in index order; they are
@@ -336,7 +451,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         hi[s * HS] = -1;
       }
       const float qn = live ? p.qnrm[q] : 0.f;
-      const double qn2 = live ? p.qn2[q] : 0.0;
+      const float qn2f = live ? __double2float_rd(p.qn2[q]) : 0.f;
       // |a_j - (D_j - ||q||^2)| <= e, a_j = -2 acc_j (see split.cu for the terms)
       const float eq = 1.05f * (2.f * (p.coef_xc * qn * tmax + p.coef_cc * tmax * tmax) +
                                 p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
@@ -352,7 +467,16 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         const int owner = (int)(e >> kRowBits);
         const int64_t j = (int64_t)(e & ((1u << kRowBits) - 1u));
         double sq = __longlong_as_double(0x7ff0000000000000ll);
-        if ((uint32_t)lane < cnt && qbase + owner < p.m) {
+        bool seq = (uint32_t)lane < cnt && qbase + owner < p.m;  // this lane's entry needs the sequential form
+        if constexpr (sizeof(T) == 4) {
+          constexpr int KC = TN == 256 ? 1 : TN == 128 ? 2 : 8;  // d_pad <= 32, 64, 256
+          bool fb = false;
+          float *Sx = s_stage + (warp - 2) * kStageFloats;
+          round_dist_f32<KC>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane,
+                             Sx, Sx + kStageFloats / 2, sq, fb);
+          seq = seq && fb;
+        }
+        if (seq) {
           const T *tr = train + j * (int64_t)p.d;
           const T *qrow = queries + (qbase + owner) * (int64_t)p.d;
           bool done = false;
@@ -399,9 +523,10 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
             hi[0] = Rj[r];
             if (p.k > 1)
               for (int s2 = p.k / 2 - 1; s2 >= 0; --s2) heap_sift<HS>(hD, hi, s2, p.k - 1);
-            lo = -0.5f * knn_threshold(hD[0], qn2, eq);
+            lo = -0.5f * knn_threshold(hD[0], qn2f, eq);
           }
         }
+        if (!p.radius_mode) s_lo[row] = lo;
         __syncwarp();
         qhead += cnt;
         evals += (uint32_t)lane < cnt ? 1u : 0u;
@@ -410,68 +535,58 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
         const int slot = it % kMaskSlots;
         const bool got = tc::mbar_wait(&maskfull[slot], (uint32_t)(it / kMaskSlots) & 1u, kWaitNs);
-        if (!__all_sync(0xffffffffu, got) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
+        // (A stopped filter shows up here as a wait that runs out.)
+        if (!__all_sync(0xffffffffu, got)) {
           atomicExch(s_abort, 1);
           stop = true;
           break;
         }
-        const uint32_t *mrow = sMask + ((size_t)slot * kQM + row) * kWords;
+        const uint32_t *mcol = sMask + (size_t)slot * kWords * kQM + row;
         const int64_t j0 = (int64_t)tt * TN;
-        uint32_t mw[kWords], mcnt = 0u;
+        uint32_t nzw = 0u;  // this query's words with an entry
 #pragma unroll
-        for (int w = 0; w < kWords; ++w) {
-          mw[w] = mrow[w];
-          mcnt += __popc(mw[w]);
+        for (int w = 0; w < kWords; ++w) nzw |= (mcol[w * kQM] != 0u ? 1u : 0u) << w;
+        // Once the tile's mask is in registers the slot is free, and the
+        // filters may take the current threshold (entries still queued only
+        // make it staler).  Tile 0 is released after its replay instead: the
+        // thresholds of tiles 1 and 2 come from it.
+        const bool early = tt != 0 || p.radius_mode;
+        if (early) {
+          s_lo[row] = lo;
+          tc::mbar_arrive(&maskempty[slot]);
         }
-        const uint32_t mtotal = __reduce_add_sync(0xffffffffu, mcnt);
-        if (mtotal != 0u && mtotal <= (uint32_t)(kQueue - 32)) {
-          // the whole tile at once: one scan, entries in index order per owner
-          uint32_t incl = mcnt;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-          }
-          uint32_t pos = qtail + incl - mcnt;
-#pragma unroll
-          for (int w = 0; w < kWords; ++w)
-            for (uint32_t m = mw[w]; m; m &= m - 1) {
-              const int64_t jr = j0 + 32 * w + __ffs(m) - 1;
-              prefetch_row(train, jr, p.d);
-              Q[(pos++) & (kQueue - 1)] = ((uint32_t)lane << kRowBits) | (uint32_t)jr;
+        // Entries in row order, and within a row in owner order: each owner
+        // still sees its rows in index order, and a round spreads over many
+        // owners, so their heap replays run side by side.
+        // (The filters refill this slot only after this owner has taken the
+        // mask of tile tt + 2, so its words are read again here.)
+        for (uint32_t words = __reduce_or_sync(0xffffffffu, nzw); words; words &= words - 1u) {
+          {
+            const int w = __ffs(words) - 1;
+            const uint32_t mword = mcol[w * kQM];
+            uint32_t cols = __reduce_or_sync(0xffffffffu, mword);  // rows of this word with an entry
+            while (cols) {
+              const int b = __ffs(cols) - 1;
+              cols &= cols - 1u;
+              const bool mine = (mword >> b) & 1u;
+              const uint32_t own = __ballot_sync(0xffffffffu, mine);
+              const int64_t jr = j0 + 32 * w + b;
+              if (mine)
+                Q[(qtail + __popc(own & ((1u << lane) - 1u))) & (kQueue - 1)] =
+                    ((uint32_t)lane << kRowBits) | (uint32_t)jr;
+              if (lane == __ffs(own) - 1) prefetch_row(train, jr, p.d);
+              qtail += __popc(own);
+              if (qtail - qhead >= 32) {
+                __syncwarp();
+                round(32);
+              }
             }
-          qtail += mtotal;
-          __syncwarp();
-          while (qtail - qhead >= 32) round(32);
-        }
-#pragma unroll
-        for (int w = 0; w < kWords && mtotal > (uint32_t)(kQueue - 32); ++w) {  // rare: a tile too large for the ring
-          if (!__any_sync(0xffffffffu, mw[w] != 0u)) continue;
-#pragma unroll
-          for (int half = 0; half < 2; ++half) {  // <= 32 x 16 new entries per step: the ring never overflows
-            const uint32_t mask = (mw[w] >> (16 * half)) & 0xffffu;
-            const uint32_t cnt = __popc(mask);
-            const uint32_t total = __reduce_add_sync(0xffffffffu, cnt);
-            if (total == 0) continue;
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-              if (lane >= o) incl += y;
-            }
-            uint32_t pos = qtail + incl - cnt;
-            for (uint32_t m = mask; m; m &= m - 1) {
-              const int64_t jr = j0 + 32 * w + 16 * half + __ffs(m) - 1;
-              prefetch_row(train, jr, p.d);
-              Q[(pos++) & (kQueue - 1)] = ((uint32_t)lane << kRowBits) | (uint32_t)jr;
-            }
-            qtail += total;
-            __syncwarp();
-            while (qtail - qhead >= 32) round(32);
           }
         }
-        s_lo[row] = lo;                     // threshold for the filters, published before the release
-        tc::mbar_arrive(&maskempty[slot]);  // tile replayed (queued entries only make lo staler)
+        if (!early) {
+          s_lo[row] = lo;
+          tc::mbar_arrive(&maskempty[slot]);
+        }
       }
       while (!stop && qtail != qhead) round(min(32u, qtail - qhead));
       if (p.radius_mode) {
@@ -493,37 +608,33 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     int it = 0;
     bool stop = false;
     for (int qt = blockIdx.x; !stop && qt < p.n_tiles_q; qt += gridDim.x) {
+      const bool live_q = (int64_t)qt * kQM + row < p.m;
+      float rad_lo = __int_as_float(0x7f800000);  // find_radius: a fixed threshold, D <= r2up
+      if (p.radius_mode && live_q) {
+        const int64_t q = (int64_t)qt * kQM + row;
+        const float tmax = __uint_as_float(*p.tmax);
+        const float qn = p.qnrm[q];
+        const float eq = 1.05f * (2.f * (p.coef_xc * qn * tmax + p.coef_cc * tmax * tmax) +
+                                  p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
+        rad_lo = -0.5f * knn_threshold(p.r2up, __double2float_rd(p.qn2[q]), eq);
+      }
       for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
         if ((it & 1) != g) continue;
         const int slot = it % kMaskSlots;
         bool ok = tc::mbar_wait(&accfull[g], (uint32_t)(it >> 1) & 1u, kWaitNs);
-        // threshold: tile 0 of a query tile admits every row; tile 1 waits for
-        // the owners' replay of tile 0; later tiles use the replay of tile
-        // tt - 2.  Either wait also frees this tile's mask slot.
-        const bool live_q = (int64_t)qt * kQM + row < p.m;
+        // Every tile waits until the owners have taken the mask of tile it - 2
+        // (tile 0 of the query tile for tile 1): by then they have finished
+        // with tile it - 4, the slot's previous contents.  Threshold: tile 0
+        // of a query tile admits every row; tile 1 uses the owners' replay of
+        // tile 0; later tiles whatever the owners have published by now.
         float lo = live_q ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
-        if (p.radius_mode) {
-          // a fixed threshold: D <= r2up; only the mask slot must be free
-          if (it >= kMaskSlots) {
-            const int u = it - kMaskSlots;
-            ok = ok && tc::mbar_wait(&maskempty[u % kMaskSlots], (uint32_t)(u / kMaskSlots) & 1u, kWaitNs);
-          }
-          if (live_q) {
-            const int64_t q = (int64_t)qt * kQM + row;
-            const float tmax = __uint_as_float(*p.tmax);
-            const float qn = p.qnrm[q];
-            const float eq = 1.05f * (2.f * (p.coef_xc * qn * tmax + p.coef_cc * tmax * tmax) +
-                                      p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
-            lo = -0.5f * knn_threshold(p.r2up, p.qn2[q], eq);
-          }
-        } else if (tt >= 1) {
-          const int u = it - (tt == 1 ? 1 : 2);
+        const int u = p.radius_mode || tt != 1 ? it - 2 : it - 1;
+        if (u >= 0)
           ok = ok && tc::mbar_wait(&maskempty[u % kMaskSlots], (uint32_t)(u / kMaskSlots) & 1u, kWaitNs);
+        if (p.radius_mode)
+          lo = rad_lo;
+        else if (tt >= 1)
           lo = *(volatile float *)&s_lo[row];
-        } else if (it >= kMaskSlots) {
-          const int u = it - kMaskSlots;
-          ok = ok && tc::mbar_wait(&maskempty[u % kMaskSlots], (uint32_t)(u / kMaskSlots) & 1u, kWaitNs);
-        }
         if (!__all_sync(0xffffffffu, ok) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
           atomicExch(s_abort, 1);
           stop = true;
@@ -532,7 +643,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         tc::fence_after_sync();
         const uint32_t tbase = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(g * TN);
         const uint32_t taddr = tbase + (uint32_t)c_lo;
-        uint32_t *mrow = sMask + ((size_t)slot * kQM + row) * kWords + c_lo / 32;
+        uint32_t *mcol = sMask + (size_t)slot * kWords * kQM + row;
         const int64_t j0 = (int64_t)tt * TN + c_lo;
         float lo_rest = lo;  // threshold for the rows after the tile's first 32
         if (tt == 0 && !p.radius_mode && p.k <= 32) {
@@ -561,7 +672,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
                                     p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
           lo_rest = live_q && p.n >= 32 ? top[p.k - 1] - 1.01f * eq - 1e-30f : lo;
         }
-#pragma unroll
+#pragma unroll 1
         for (int c1 = 0; c1 < kCols; c1 += 64) {  // 64 columns per TMEM round trip
           uint32_t v[64];
           tc::tmem_ld64(taddr + (uint32_t)c1, v);
@@ -570,17 +681,21 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
           for (int c2 = 0; c2 < 64; c2 += 32) {
             const int c0 = c1 + c2;
             if (c_lo + c0 >= 32) lo = lo_rest;
-            float mx = __uint_as_float(v[c2]);
+            float mx[16];  // max of the 32 columns as a tree (depth 5, not a chain of 31)
 #pragma unroll
-            for (int jj = 1; jj < 32; ++jj) mx = fmaxf(mx, __uint_as_float(v[c2 + jj]));
+            for (int jj = 0; jj < 16; ++jj) mx[jj] = fmaxf(__uint_as_float(v[c2 + jj]), __uint_as_float(v[c2 + jj + 16]));
+#pragma unroll
+            for (int w2 = 8; w2 > 0; w2 >>= 1)
+#pragma unroll
+              for (int jj = 0; jj < w2; ++jj) mx[jj] = fmaxf(mx[jj], mx[jj + w2]);
             uint32_t mask = 0u;
-            if (__any_sync(0xffffffffu, mx >= lo)) {
+            if (__any_sync(0xffffffffu, mx[0] >= lo)) {
 #pragma unroll
               for (int jj = 0; jj < 32; ++jj) mask |= (__uint_as_float(v[c2 + jj]) >= lo ? 1u : 0u) << jj;
               const int64_t rem = p.n - (j0 + c0);  // rows past the end of the training set
               if (rem < 32) mask &= rem <= 0 ? 0u : ((1u << rem) - 1u);
             }
-            mrow[c0 / 32] = mask;
+            mcol[(c_lo + c0) / 32 * kQM] = mask;
           }
         }
         tc::fence_before_sync();
@@ -596,6 +711,362 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
     tc::tmem_dealloc(tmem, 2 * TN);
   }
   if (threadIdx.x == 0 && *s_abort) atomicExch(p.err, 4);
+}
+
+// ---------------------------------------------------------------------------
+// find: a certified candidate filter on the tensor cores, then the exact
+// replay per query on the CUDA cores
+// ---------------------------------------------------------------------------
+// The reference inserts row j exactly when D_j < root_j, the largest of the
+// k smallest distances among rows 0..j-1 (+inf before k rows).  With acc_i
+// the split-BF16 score, |acc_i - (||q||^2 - D_i) / 2| <= e / 2, so if T is the
+// k-th largest acc among any prefix of rows 0..j-1 (-inf before k rows),
+// T <= (||q||^2 - root_j) / 2 + e / 2 and D_j < root_j implies acc_j > T - e.
+// Each filter lane keeps the k largest acc of its query (a min-heap in shared
+// memory) and lists every row with acc_j >= T - e, in index order: a superset
+// of the rows the reference inserts, found without any exact distance.  The
+// refine kernel then computes the reference distances of the listed rows and
+// replays the heap exactly.
+constexpr int kFiltWarps = 4;                        // one per TMEM lane quarter, every tile
+constexpr int kFiltThreads = 32 * (2 + kFiltWarps);  // + warp 0 TMA, warp 1 MMA
+
+struct FilterParams {
+  int64_t n, m;
+  int n_tiles_t, n_tiles_q;
+  int nkt, kt_elems, row_bytes;
+  int stages;
+  int k;
+  const float *qnrm;
+  const unsigned int *tmax;
+  float coef_xc, coef_cc, coef_ref;
+  int64_t cap;                 // candidate slots per query
+  int32_t *cand;               // [m_pad][cap]: rows in index order
+  int32_t *count;              // per query: candidates, or -1 past cap
+  int32_t *over;               // the queries past cap
+  unsigned long long *stats;   // [1] wait timed out, [2] queries past cap
+};
+
+// Inserts x (> the root) into a lane's min-heap of its k largest scores
+// (entries at stride kQM) and returns the new root, the k-th largest.
+__device__ __noinline__ float topk_push(float *h, int k, float x) {
+  int i = 0;
+  while (true) {
+    int c = 2 * i + 1;
+    if (c >= k) break;
+    float cv = h[c * kQM];
+    if (c + 1 < k) {
+      const float c2 = h[(c + 1) * kQM];
+      if (c2 < cv) {
+        cv = c2;
+        ++c;
+      }
+    }
+    if (!(cv < x)) break;
+    h[i * kQM] = cv;
+    i = c;
+  }
+  h[i * kQM] = x;
+  return h[0];
+}
+
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+// A filter lane's state for its query: candidates listed, the k-th largest
+// score (its heap root) and the threshold root - e.
+struct FiltLane {
+  int64_t cnt;
+  float root, lo;
+};
+
+// The rows of one 8-column group of a lane with a score at or above the
+// threshold (rare after the first tiles): listed in index order, and pushed
+// into the lane's top-k when above its root.
+__device__ __noinline__ FiltLane filt_group(FiltLane st, float x0, float x1, float x2, float x3, float x4, float x5,
+                                            float x6, float x7, int64_t row0, int64_t n, int32_t *cq, int64_t cap,
+                                            float *top, int k, float marg) {
+  const float xs[8] = {x0, x1, x2, x3, x4, x5, x6, x7};
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    if (xs[jj] >= st.lo && row0 + jj < n) {
+      if (st.cnt < cap) cq[st.cnt] = (int32_t)(row0 + jj);
+      ++st.cnt;
+      if (xs[jj] > st.root) {
+        st.root = topk_push(top, k, xs[jj]);
+        st.lo = __fsub_rd(st.root, marg);
+      }
+    }
+  }
+  return st;
+}
+
+// One 64-column chunk of a lane's scores: the maxima of its 8-column groups
+// against the threshold at the start of the chunk give each lane a mask of
+// groups to look at (a staler threshold only admits more), and one warp-wide
+// OR the groups any lane needs; those are scanned column by column.
+__device__ __forceinline__ FiltLane filt_chunk(FiltLane st, const uint32_t (&v)[64], int64_t jb, int64_t n,
+                                               int32_t *cq, int64_t cap, float *top, int k, float marg) {
+  uint32_t lm = 0u;
+#pragma unroll
+  for (int g = 0; g < 8; ++g) {
+    const float *x = (const float *)&v[8 * g];
+    const float gm = fmax3(fmax3(x[0], x[1], x[2]), fmax3(x[3], x[4], x[5]), fmaxf(x[6], x[7]));
+    lm |= (gm >= st.lo ? 1u : 0u) << g;
+  }
+  for (uint32_t um = __reduce_or_sync(0xffffffffu, lm); um; um &= um - 1u) {
+    const int g = __ffs(um) - 1;
+    if (!((lm >> g) & 1u)) continue;
+#define SC_FILT_GROUP(G)                                                                                          \
+  case G:                                                                                                         \
+    st = filt_group(st, __uint_as_float(v[8 * G]), __uint_as_float(v[8 * G + 1]), __uint_as_float(v[8 * G + 2]), \
+                    __uint_as_float(v[8 * G + 3]), __uint_as_float(v[8 * G + 4]), __uint_as_float(v[8 * G + 5]), \
+                    __uint_as_float(v[8 * G + 6]), __uint_as_float(v[8 * G + 7]), jb + 8 * G, n, cq, cap, top, k,  \
+                    marg);                                                                                        \
+    break;
+    switch (g) {
+      SC_FILT_GROUP(0)
+      SC_FILT_GROUP(1)
+      SC_FILT_GROUP(2)
+      SC_FILT_GROUP(3)
+      SC_FILT_GROUP(4)
+      SC_FILT_GROUP(5)
+      SC_FILT_GROUP(6)
+      SC_FILT_GROUP(7)
+    }
+#undef SC_FILT_GROUP
+  }
+  return st;
+}
+
+// Roles: warp 0 TMA, warp 1 MMA (one elected thread each), warps 2-5 filters:
+// warp w reads TMEM lane quarter w % 4 (32 queries), every column of every
+// tile, so each query's running top-k stays with one lane and is never stale.
+template <int TN>
+__global__ void __launch_bounds__(kFiltThreads, 1)
+knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constant__ CUtensorMap tm_ql,
+                  const __grid_constant__ CUtensorMap tm_th, const __grid_constant__ CUtensorMap tm_tl,
+                  const __grid_constant__ CUtensorMap tm_ones, const __grid_constant__ CUtensorMap tm_tbx,
+                  const FilterParams p) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int a_blk = kQM * p.row_bytes;
+  const int a_bytes = 2 * p.nkt * a_blk;
+  const int b_blk = TN * p.row_bytes;
+  const int b_stage = 2 * p.nkt * b_blk + TN * 32;
+  uint8_t *sA = base;
+  uint8_t *sOnes = base + a_bytes;
+  uint8_t *sB = sOnes + kQM * 32;
+  float *s_top = (float *)(sB + (size_t)p.stages * b_stage);  // [k][query]: min-heaps of the k largest scores
+  uint64_t *bars = (uint64_t *)(s_top + ((p.k * kQM + 1) & ~1));
+  uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
+  uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
+  uint32_t *s_tmem = (uint32_t *)(afull + 7);
+  int *s_abort = (int *)(s_tmem + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < p.stages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(afull, 1);
+    tc::mbar_init(aempty, 1);
+    tc::mbar_init(mma_done, 1);
+    for (int a = 0; a < 2; ++a) {
+      tc::mbar_init(&accfull[a], 1);
+      tc::mbar_init(&accempty[a], 32 * kFiltWarps);
+    }
+    *s_abort = 0;
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&tm_qh);
+    tc::prefetch_tmap(&tm_ql);
+    tc::prefetch_tmap(&tm_th);
+    tc::prefetch_tmap(&tm_tl);
+    tc::prefetch_tmap(&tm_ones);
+    tc::prefetch_tmap(&tm_tbx);
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(s_tmem, 2 * TN);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *s_tmem;
+  const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
+                  a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
+                  p.stages};
+  if (warp == 0) {
+    if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
+  } else if (warp == 1) {
+    if (lane == 0) knn_mma_role<TN>(P, tmem);
+  } else {
+    const int lq = warp & 3;
+    const int row = lq * 32 + lane;
+    const float tmax = __uint_as_float(*p.tmax);
+    float *top = s_top + row;
+    int it = 0;
+    bool stop = false;
+    for (int qt = blockIdx.x; !stop && qt < p.n_tiles_q; qt += gridDim.x) {
+      const int64_t q = (int64_t)qt * kQM + row;
+      const bool live = q < p.m;
+      for (int s = 0; s < p.k; ++s) top[s * kQM] = -__int_as_float(0x7f800000);
+      float root = -__int_as_float(0x7f800000);
+      const float qn = live ? p.qnrm[q] : 0.f;
+      // e bounds |a_j - (D_j - ||q||^2)| for a_j = -2 acc_j (see split.cu for
+      // the terms); the 1% covers the f32 roundings of the comparison
+      const float eq = 1.05f * (2.f * (p.coef_xc * qn * tmax + p.coef_cc * tmax * tmax) +
+                                p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
+      const float marg = __fadd_ru(__fmul_ru(1.01f, eq), 1e-30f);
+      FiltLane st{0, root, live ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000)};
+      int32_t *cq = p.cand + (live ? q : 0) * p.cap;
+      for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
+        const int acc = it & 1;
+        const bool got = tc::mbar_wait(&accfull[acc], (uint32_t)(it >> 1) & 1u, kWaitNs);
+        if (!__all_sync(0xffffffffu, got) || __any_sync(0xffffffffu, *(volatile int *)s_abort != 0)) {
+          atomicExch(s_abort, 1);
+          stop = true;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t taddr = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(acc * TN);
+        const int64_t j0 = (int64_t)tt * TN;
+        // 64 columns per TMEM load, the next load in flight while a chunk is scanned
+        uint32_t va[64], vb[64];
+        tc::tmem_ld64(taddr, va);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < TN / 64; ++c) {
+          if (c + 1 < TN / 64) tc::tmem_ld64(taddr + (uint32_t)(64 * (c + 1)), (c & 1) ? va : vb);
+          st = filt_chunk(st, (c & 1) ? vb : va, j0 + 64 * c, p.n, cq, p.cap, top, p.k, marg);
+          if (c + 1 < TN / 64) tc::tmem_wait_ld();
+        }
+        tc::fence_before_sync();
+        tc::mbar_arrive(&accempty[acc]);
+      }
+      const int64_t cnt = st.cnt;
+      if (live && !stop) {
+        if (cnt <= p.cap) {
+          p.count[q] = (int32_t)cnt;
+        } else {
+          p.count[q] = -1;
+          p.over[atomicAdd(&p.stats[2], 1ull)] = (int32_t)q;
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 2 * TN);
+  }
+  if (threadIdx.x == 0 && *s_abort) atomicExch(&p.stats[1], 1ull);
+}
+
+// The reference's squared distance of a query row and a training row.
+template <typename T>
+__device__ __forceinline__ double knn_exact_sqd(const T *__restrict__ a, const T *__restrict__ b, int d, int lg_d) {
+  double sq;
+  if constexpr (sizeof(T) == 4) {
+    if (d <= 32 ? sqd_f32_d32(a, b, d, lg_d, sq) : sqd_seq_f32(a, b, d, lg_d, sq)) return sq;
+  }
+  sq = 0.0;
+  for (int t = 0; t < d; ++t) sq = __dadd_rn(sq, ref_term(a[t], b[t]));
+  return sq;
+}
+
+// One warp per query: the exact distances of its candidates, 32 at a time
+// (one per lane), then the reference's insertion test and heapify
+// (linear_search.rs:72-77, heap_select.rs:42-50, :71-86) on lane 0, in index
+// order.  The reference's heapify after a replaced root runs sift_down from
+// every internal node; all of them but the root's find their (unchanged)
+// subtrees already in heap order and stop at once (the heap never holds a NaN:
+// a NaN distance fails the insertion test), so one sift_down from the root
+// leaves the same array.  Queries past the candidate capacity (count -1) are
+// left to the FP64 kernel.
+constexpr int kRefineWarps = 8;
+template <typename T>
+__global__ void __launch_bounds__(32 * kRefineWarps, 3)
+knn_refine_kernel(const T *__restrict__ train, const T *__restrict__ queries, int64_t m, int d, int lg_d, int k,
+                  int64_t cap, const int32_t *__restrict__ cand, const int32_t *__restrict__ count,
+                  int64_t *__restrict__ idx_out, double *__restrict__ dist_out, unsigned long long *evals) {
+  __shared__ double s_hD[kRefineWarps][kMaxKnnK];
+  __shared__ int32_t s_hi[kRefineWarps][kMaxKnnK];
+  __shared__ double s_D[kRefineWarps][32];
+  __shared__ int32_t s_j[kRefineWarps][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *hD = s_hD[warp], *D = s_D[warp];
+  int32_t *hi = s_hi[warp], *J = s_j[warp];
+  unsigned long long ev = 0;
+  for (int64_t q = (int64_t)blockIdx.x * kRefineWarps + warp; q < m; q += (int64_t)gridDim.x * kRefineWarps) {
+    const int c = count[q];
+    if (c < 0) continue;
+    for (int s = lane; s < k; s += 32) {
+      hD[s] = __longlong_as_double(0x7ff0000000000000ll);
+      hi[s] = -1;
+    }
+    const T *qrow = queries + q * d;
+    const int32_t *cq = cand + q * cap;
+    for (int b = 0; b < c; b += 32) {
+      const int r = b + lane;
+      double sq = __longlong_as_double(0x7ff0000000000000ll);
+      int32_t j = -1;
+      if (r < c) {
+        j = cq[r];
+        sq = knn_exact_sqd<T>(qrow, train + (int64_t)j * d, d, lg_d);
+        ++ev;
+      }
+      D[lane] = sq;
+      J[lane] = j;
+      __syncwarp();
+      // only rows below the root at the start of the batch can enter
+      uint32_t in = __ballot_sync(0xffffffffu, sqrt_less(sq, hD[0]));
+      if (lane == 0) {
+        double root = hD[0];
+        for (; in; in &= in - 1u) {
+          const int rr = __ffs(in) - 1;
+          const double sr = D[rr];
+          if (sqrt_less(sr, root)) {  // sqrt(D) < root (linear_search.rs:72)
+            hD[0] = sr;
+            hi[0] = J[rr];
+            if (k > 1) heap_sift<1>(hD, hi, 0, k - 1);
+            root = hD[0];
+          }
+        }
+      }
+      __syncwarp();
+    }
+    for (int s = lane; s < k; s += 32) {
+      idx_out[q * k + s] = hi[s];
+      dist_out[q * k + s] = __dsqrt_rn(hD[s]);  // sqrt(+inf) = +inf for an empty slot
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ev += __shfl_xor_sync(0xffffffffu, ev, o);
+  if (lane == 0 && ev) atomicAdd(evals, ev);
+}
+
+// Queries past the candidate capacity: their rows gathered for the FP64
+// kernel, and its heaps scattered back.
+template <typename T>
+__global__ void gather_rows_kernel(const T *__restrict__ src, const int32_t *__restrict__ rows, int64_t nr, int d,
+                                   T *__restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nr * d) return;
+  dst[i] = src[(int64_t)rows[i / d] * d + i % d];
+}
+__global__ void scatter_heaps_kernel(const int32_t *__restrict__ rows, int64_t nr, int k,
+                                     const int64_t *__restrict__ isub, const double *__restrict__ dsub,
+                                     int64_t *__restrict__ idx, double *__restrict__ dist) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nr * k) return;
+  const int64_t q = rows[i / k];
+  idx[q * k + i % k] = isub[i];
+  dist[q * k + i % k] = dsub[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -638,11 +1109,47 @@ int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; 
 // resident query tile and two or more training stages fit in shared memory.
 int knn_tile_n(int d_pad) { return d_pad <= 32 ? 256 : d_pad <= 64 ? 128 : 64; }
 
-size_t knn_smem(int nkt, int row_bytes, int stages, int tn, int heap_k) {
+size_t knn_smem(int nkt, int row_bytes, int stages, int tn, int heap_k, int dtype) {
   return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * tn * row_bytes + tn * 32) +
-         (size_t)kOwnerWarps * kQueue * 4 + (size_t)kMaskSlots * kQM * (tn / 32) * 4 + kQM * 4 +
+         (size_t)kOwnerWarps * kQueue * 4 + (size_t)kMaskSlots * kQM * (tn / 32) * 4 +
+         (dtype == SC_F32 ? (size_t)kOwnerWarps * kStageFloats * 4 : 0) + kQM * 4 +
          (size_t)kOwnerWarps * 32 * 16 + (size_t)heap_k * kQM * 12 + 8 +
          (size_t)(2 * stages + 7 + 2 * kMaskSlots) * 8 + 16;
+}
+
+size_t filt_smem(int nkt, int row_bytes, int stages, int tn, int k) {
+  return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * tn * row_bytes + tn * 32) +
+         (size_t)((k * kQM + 1) & ~1) * 4 + (size_t)(2 * stages + 7) * 8 + 16;
+}
+
+// Training stages of the filter kernel: as many as fit, up to 6 (deeper
+// queues hide DRAM latency when the training rows exceed L2).
+int filt_stages(int nkt, int row_bytes, int tn, int k) {
+  int st = 6;
+  while (st > 2 && filt_smem(nkt, row_bytes, st, tn, k) > 227 * 1024) --st;
+  return st;
+}
+
+// Candidate slots per query: about 4 k (1 + ln(n / k)), the expected number
+// of heap insertions k (1 + ln(n / k)) with room for ties and the bound's
+// slack; a query past it is served by the FP64 kernel.
+int64_t g_knn_cap_override = 0;
+int64_t knn_candidate_cap(int64_t n, int k) {
+  if (g_knn_cap_override > 0) return g_knn_cap_override;
+  const double r = (double)n / k > 1.0 ? (double)n / k : 1.0;
+  int64_t c = (int64_t)(4.0 * k * (1.0 + log(r))) + 32;
+  c = (c + 31) / 32 * 32;
+  return c < 256 ? 256 : c;
+}
+
+template <int TN>
+sc_status launch_knn_filter(int grid, size_t smem, const CUtensorMap &tm_qh, const CUtensorMap &tm_ql,
+                            const SplitKnnState *s, const FilterParams &p, cudaStream_t st) {
+  auto kern = knn_filter_kernel<TN>;
+  SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<grid, kFiltThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, p);
+  SC_LAUNCHED();
+  return SC_OK;
 }
 
 template <typename T, int TN, bool SH>
@@ -666,6 +1173,113 @@ struct RadiusArgs {
   const int64_t *offsets;  // filling pass
 };
 
+// find: the candidate filter, the exact replay per query, and the FP64
+// kernel for the queries past the candidate capacity.
+sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, int lg_d,
+                         const void *queries, int64_t m, int64_t m_pad, int k, int64_t *idx, double *dist,
+                         int64_t *rescored, const CUtensorMap &tm_qh, const CUtensorMap &tm_ql, int nkt, int kt_elems,
+                         int row_bytes, int tn, float coef_xc, float coef_cc, float coef_ref, cudaStream_t st) {
+  const int stages = filt_stages(nkt, row_bytes, tn, k);
+  const size_t smem = filt_smem(nkt, row_bytes, stages, tn, k);
+  if (smem > 227 * 1024) {
+    set_error("d=%d exceeds the split-BF16 kNN kernel's shared memory", d);
+    return SC_ERR_INVALID;
+  }
+  const int64_t cap = knn_candidate_cap(n, k);
+  if ((size_t)(m_pad * cap) > s->cand_cap || m_pad > s->count_cap) {
+    s->cand_cap = 0;
+    s->count_cap = 0;
+    dfree(s->cand, st); dfree(s->count, st); dfree(s->over, st);
+    SC_TRY(dalloc(&s->cand, (size_t)(m_pad * cap), st));
+    SC_TRY(dalloc(&s->count, (size_t)m_pad, st));
+    SC_TRY(dalloc(&s->over, (size_t)m_pad, st));
+    s->cand_cap = (size_t)(m_pad * cap);
+    s->count_cap = m_pad;
+  }
+  FilterParams fp;
+  memset(&fp, 0, sizeof fp);
+  fp.n = n;
+  fp.m = m;
+  fp.n_tiles_t = (int)((n + tn - 1) / tn);
+  fp.n_tiles_q = (int)(m_pad / kQM);
+  fp.nkt = nkt;
+  fp.kt_elems = kt_elems;
+  fp.row_bytes = row_bytes;
+  fp.stages = stages;
+  fp.k = k;
+  fp.qnrm = s->qnrm;
+  fp.tmax = s->tmax;
+  fp.coef_xc = coef_xc;
+  fp.coef_cc = coef_cc;
+  fp.coef_ref = coef_ref;
+  fp.cap = cap;
+  fp.cand = s->cand;
+  fp.count = s->count;
+  fp.over = s->over;
+  fp.stats = s->evals;
+  const int grid = fp.n_tiles_q < s->num_sms ? fp.n_tiles_q : s->num_sms;
+  SC_TRY(tn == 256   ? launch_knn_filter<256>(grid, smem, tm_qh, tm_ql, s, fp, st)
+         : tn == 128 ? launch_knn_filter<128>(grid, smem, tm_qh, tm_ql, s, fp, st)
+                     : launch_knn_filter<64>(grid, smem, tm_qh, tm_ql, s, fp, st));
+  const int64_t rwarps = (int64_t)s->num_sms * 64;
+  const int rgrid = (int)((m < rwarps ? m : rwarps) + kRefineWarps - 1) / kRefineWarps;
+  if (dtype == SC_F32)
+    knn_refine_kernel<float><<<rgrid, 32 * kRefineWarps, 0, st>>>((const float *)train, (const float *)queries, m, d,
+                                                                   lg_d, k, cap, s->cand, s->count, idx, dist,
+                                                                   s->evals);
+  else
+    knn_refine_kernel<double><<<rgrid, 32 * kRefineWarps, 0, st>>>((const double *)train, (const double *)queries, m,
+                                                                    d, lg_d, k, cap, s->cand, s->count, idx, dist,
+                                                                    s->evals);
+  SC_LAUNCHED();
+  unsigned long long host[3];
+  SC_CUDA(cudaMemcpyAsync(host, s->evals, sizeof host, cudaMemcpyDeviceToHost, st));
+  SC_CUDA(cudaStreamSynchronize(st));
+  if (host[1]) {
+    set_error("split-BF16 kNN kernel: a bounded wait timed out");
+    return SC_ERR_TIMEOUT;
+  }
+  int64_t evals = (int64_t)host[0];
+  const int64_t nover = (int64_t)host[2];
+  if (nover > 0) {  // past the candidate capacity: the FP64 kernel on those queries
+    const size_t es = dtype == SC_F32 ? 4 : 8;
+    char *qsub = nullptr;
+    int64_t *isub = nullptr;
+    double *dsub = nullptr;
+    sc_status r = dalloc(&qsub, (size_t)nover * d * es, st);
+    if (r == SC_OK) r = dalloc(&isub, (size_t)(nover * k), st);
+    if (r == SC_OK) r = dalloc(&dsub, (size_t)(nover * k), st);
+    if (r == SC_OK) {
+      const int64_t tot = nover * d;
+      const int gb = (int)((tot + 255) / 256);
+      if (dtype == SC_F32)
+        gather_rows_kernel<float><<<gb, 256, 0, st>>>((const float *)queries, s->over, nover, d, (float *)qsub);
+      else
+        gather_rows_kernel<double><<<gb, 256, 0, st>>>((const double *)queries, s->over, nover, d, (double *)qsub);
+      if (cudaGetLastError() != cudaSuccess) r = SC_ERR_CUDA;
+      note_launch();
+    }
+    if (r == SC_OK) r = launch_knn_fp64(dtype, train, n, d, qsub, nover, k, isub, dsub, st);
+    if (r == SC_OK) {
+      scatter_heaps_kernel<<<(int)((nover * k + 255) / 256), 256, 0, st>>>(s->over, nover, k, isub, dsub, idx, dist);
+      if (cudaGetLastError() != cudaSuccess) r = SC_ERR_CUDA;
+      note_launch();
+    }
+    if (r == SC_OK && cudaStreamSynchronize(st) != cudaSuccess) r = SC_ERR_CUDA;
+    dfree(qsub, st);
+    dfree(isub, st);
+    dfree(dsub, st);
+    if (r != SC_OK) {
+      if (r == SC_ERR_CUDA) set_error("kNN: the FP64 pass over %lld queries past the candidate capacity failed",
+                                      (long long)nover);
+      return r;
+    }
+    evals += nover * n;
+  }
+  if (rescored) *rescored = evals;
+  return SC_OK;
+}
+
 sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
                         int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, const RadiusArgs *rad,
                         cudaStream_t st) {
@@ -679,11 +1293,11 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   const int kt_elems = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt_elems, row_bytes = kt_elems * 2;
   const int tn = knn_tile_n(d_pad);
   // heaps in shared memory when they fit beside at least two training stages
-  bool sh = knn_smem(nkt, row_bytes, 2, tn, k) <= 227 * 1024;
+  bool sh = knn_smem(nkt, row_bytes, 2, tn, k, dtype) <= 227 * 1024;
   const int heap_k = sh ? k : 0;
   int stages = 4;
-  while (stages > 2 && knn_smem(nkt, row_bytes, stages, tn, heap_k) > 227 * 1024) --stages;
-  const size_t smem = knn_smem(nkt, row_bytes, stages, tn, heap_k);
+  while (stages > 2 && knn_smem(nkt, row_bytes, stages, tn, heap_k, dtype) > 227 * 1024) --stages;
+  const size_t smem = knn_smem(nkt, row_bytes, stages, tn, heap_k, dtype);
   if (d_pad > 256 || smem > 227 * 1024) {
     set_error("d=%d exceeds the split-BF16 kNN kernel's shared memory", d);
     return SC_ERR_INVALID;
@@ -730,8 +1344,8 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
     SC_TRY(dalloc(&s->qn2, (size_t)m_pad, st));
     s->m_cap = m_pad;
   }
-  if (!s->evals) SC_TRY(dalloc(&s->evals, 2, st));
-  SC_CUDA(cudaMemsetAsync(s->evals, 0, 2 * sizeof(unsigned long long), st));
+  if (!s->evals) SC_TRY(dalloc(&s->evals, 3, st));
+  SC_CUDA(cudaMemsetAsync(s->evals, 0, 3 * sizeof(unsigned long long), st));
   const int nbq = (int)((m_pad + 7) / 8);
   if (dtype == SC_F32)
     knn_prep_kernel<float><<<nbq, 256, 0, st>>>((const float *)queries, m, m_pad, d, d_pad, s->qh, s->ql, s->qnrm,
@@ -743,6 +1357,14 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   CUtensorMap tm_qh, tm_ql;
   SC_TRY(map2d(&tm_qh, s->qh, m_pad, d_pad, kt_elems, kQM, row_bytes));
   SC_TRY(map2d(&tm_ql, s->ql, m_pad, d_pad, kt_elems, kQM, row_bytes));
+  const double nacc = 3.0 * d_pad + 3.0;
+  const float coef_xc = (float)(3.02 * 0x1p-16 + 1.02 * nacc * 0x1p-22);
+  const float coef_cc = (float)(1.01 * 0x1p-25 + 0.51 * nacc * 0x1p-22);
+  const float coef_ref = (float)((d + 4) * 0x1p-52);
+  int lg_d = 0;
+  while ((1 << lg_d) < d) ++lg_d;
+  if (!rad) return run_split_find(s, dtype, train, n, d, lg_d, queries, m, m_pad, k, idx, dist, rescored, tm_qh, tm_ql,
+                                  nkt, kt_elems, row_bytes, tn, coef_xc, coef_cc, coef_ref, st);
   KnnParams p;
   memset(&p, 0, sizeof p);
   p.n = n;
@@ -755,15 +1377,13 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   p.stages = stages;
   p.k = k;
   p.d = d;
-  p.lg_d = 0;
-  while ((1 << p.lg_d) < d) ++p.lg_d;
+  p.lg_d = lg_d;
   p.qnrm = s->qnrm;
   p.qn2 = s->qn2;
   p.tmax = s->tmax;
-  const double nacc = 3.0 * d_pad + 3.0;
-  p.coef_xc = (float)(3.02 * 0x1p-16 + 1.02 * nacc * 0x1p-22);
-  p.coef_cc = (float)(1.01 * 0x1p-25 + 0.51 * nacc * 0x1p-22);
-  p.coef_ref = (float)((d + 4) * 0x1p-52);
+  p.coef_xc = coef_xc;
+  p.coef_cc = coef_cc;
+  p.coef_ref = coef_ref;
   p.idx_out = idx;
   p.dist_out = dist;
   if (rad) {
@@ -799,12 +1419,15 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
 
 }  // namespace
 
-bool split_knn_serves(int d, int k) {
+void split_knn_set_candidate_cap(int64_t cap) { g_knn_cap_override = cap > 0 ? cap : 0; }
+
+bool split_knn_serves(int d, int k, int dtype, bool radius) {
   const int d_pad = knn_pad_d(d);
   if (d_pad > 256 || k > kMaxKnnK) return false;
   const int kt = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt, rb = kt * 2, tn = knn_tile_n(d_pad);
-  const bool sh = knn_smem(nkt, rb, 2, tn, k) <= 227 * 1024;
-  return knn_smem(nkt, rb, 2, tn, sh ? k : 0) <= 227 * 1024;
+  if (!radius) return filt_smem(nkt, rb, 2, tn, k) <= 227 * 1024;
+  const bool sh = knn_smem(nkt, rb, 2, tn, k, dtype) <= 227 * 1024;
+  return knn_smem(nkt, rb, 2, tn, sh ? k : 0, dtype) <= 227 * 1024;
 }
 
 sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
@@ -822,8 +1445,11 @@ sc_status split_knn_radius(SplitKnnState *s, int dtype, const void *train, int64
 void split_knn_free(SplitKnnState *s, cudaStream_t st) {
   dfree(s->th, st); dfree(s->tl, st); dfree(s->tbx, st); dfree(s->tmax, st); dfree(s->ones, st);
   dfree(s->qh, st); dfree(s->ql, st); dfree(s->qnrm, st); dfree(s->qn2, st); dfree(s->evals, st);
+  dfree(s->cand, st); dfree(s->count, st); dfree(s->over, st);
   s->ready = 0;
   s->m_cap = 0;
+  s->cand_cap = 0;
+  s->count_cap = 0;
 }
 
 }  // namespace sc

@@ -49,7 +49,11 @@ struct SplitKnnState {
   float *qnrm = nullptr;
   double *qn2 = nullptr;
   int64_t m_cap = 0;
-  unsigned long long *evals = nullptr;          // [0] exact evaluations, [1] error flag
+  int32_t *cand = nullptr;                      // find: candidate rows, m_pad x cap
+  int32_t *count = nullptr, *over = nullptr;    //   per query: candidates; queries past cap
+  size_t cand_cap = 0;
+  int64_t count_cap = 0;
+  unsigned long long *evals = nullptr;          // [0] exact evaluations, [1] error flag, [2] queries past cap
 };
 
 sc_status split_prepare(SplitState *s, int dtype, const void *x, int64_t n, int d,
@@ -63,10 +67,13 @@ void split_free(SplitState *s, cudaStream_t st);
 sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
                     const void *queries, int64_t m, int k, int64_t *idx, double *dist,
                     int64_t *rescored, cudaStream_t st);
-// Whether the split-BF16 kNN kernel serves d features and k neighbours (its
-// heaps hold at most 64 entries, its tiles at most 256 features); the entry
-// points run the FP64 kernels, with the same results, otherwise.
-bool split_knn_serves(int d, int k);
+// Whether the split-BF16 kNN kernels serve d features and k neighbours for
+// find (heaps of at most 64 entries) or for find_radius (its tiles at most
+// 256 features); the entry points run the FP64 kernels, with the same
+// results, otherwise.
+bool split_knn_serves(int d, int k, int dtype, bool radius);
+// Testing: candidate slots per query of split find (0: the default).
+void split_knn_set_candidate_cap(int64_t cap);
 // Widest rows the split-BF16 k-means kernels serve.
 constexpr int kSplitKMeansMaxD = 128;
 // find_radius: counting pass when idx is null (counts[q]), else filling pass

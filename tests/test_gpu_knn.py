@@ -46,10 +46,12 @@ def test_find_d128_k10(form):
 
 
 @pytest.mark.parametrize("form", FORMS)
-@pytest.mark.parametrize("d", [16, 32])
+@pytest.mark.parametrize("d", [16, 32, 64, 200])
 def test_find_wide_exponent_span(form, d):
     # features scaled from 1e-3 to 1e3: the squared terms of one distance span
     # up to ~40 bits, so every path of the exact sequential f64 sum is taken
+    # (the warp's exact integer total, its 64-bit form, and the sequential
+    # form where a running sum rounds), at one, two and eight features a lane
     rng = np.random.default_rng(d)
     scale = np.logspace(-3, 3, d)
     train = (rng.normal(size=(6000, d)) * scale).astype(np.float32)
@@ -225,3 +227,42 @@ def test_classifier_regressor_large_k(form, weight):
     r = KNNRegressor.fit(xt, yr, KNNRegressorParameters(k=100, algorithm=KNNAlgorithmName.LinearSearch,
                                                         weight=KNNWeightFunction(weight), form=form))
     assert np.array_equal(r.predict(xq), oracle.knn_regress(idx, dist, yr, weight=weight))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("cap", [8, 64])
+def test_find_candidate_overflow(dtype, cap):
+    """Split find lists each query's candidate rows (a certified superset of
+    the rows the reference inserts) before the exact replay; a query with more
+    candidates than its slots is served by the FP64 kernel.  A small cap sends
+    most (8) or some (64) queries down that path, with the same heaps."""
+    L = _lib.load()
+    rng = np.random.default_rng(cap)
+    train = rng.normal(size=(4000, 24)).astype(dtype)
+    q = rng.normal(size=(300, 24)).astype(dtype)
+    s = LinearKNNSearch(train, form=_lib.FORM_SPLIT_BF16)
+    ridx, rdist = oracle.knn_find(train, q, 10)
+    try:
+        _lib.check(L.sc_debug_knn_candidate_cap(cap))
+        idx, dist = s.find_batch(q, 10)
+    finally:
+        L.sc_debug_knn_candidate_cap(0)
+    assert np.array_equal(idx, ridx)
+    assert np.array_equal(dist, rdist)
+    idx, dist = s.find_batch(q, 10)
+    assert np.array_equal(idx, ridx) and np.array_equal(dist, rdist)
+
+
+def test_find_sorted_training_rows():
+    """Training rows sorted by decreasing distance to the queries make every
+    row a heap insertion: the candidate lists overflow and the FP64 kernel
+    serves those queries."""
+    rng = np.random.default_rng(11)
+    q = rng.normal(size=(40, 8)).astype(np.float32)
+    t = rng.normal(size=(3000, 8)).astype(np.float32)
+    order = np.argsort(-((t - q[0]) ** 2).sum(axis=1))
+    train = np.ascontiguousarray(t[order])
+    s = LinearKNNSearch(train, form=_lib.FORM_SPLIT_BF16)
+    idx, dist = s.find_batch(q, 5)
+    ridx, rdist = oracle.knn_find(train, q, 5)
+    assert np.array_equal(idx, ridx) and np.array_equal(dist, rdist)
