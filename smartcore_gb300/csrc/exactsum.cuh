@@ -305,4 +305,36 @@ __device__ __forceinline__ bool sqd_seq_terms(const float (&q)[D], int d, int lg
   return true;
 }
 
+// Register terms of d <= 32 features (zero past d), branch-free where no
+// running sum can round (the span test of sqd_f32_d32), else sqd_seq_terms.
+__device__ __forceinline__ bool sqd_terms32(const float (&q)[32], int d, int lg_d, double &out) {
+  uint32_t emn0 = 256u, emn1 = 256u, emx0 = 0u, emx1 = 0u;
+#pragma unroll
+  for (int t = 0; t < 32; t += 2) {
+    const uint32_t u0 = __float_as_uint(q[t]), u1 = __float_as_uint(q[t + 1]);
+    const uint32_t e0 = max(u0 >> 23, 1u), e1 = max(u1 >> 23, 1u);
+    emn0 = min(emn0, u0 ? e0 : 256u);
+    emn1 = min(emn1, u1 ? e1 : 256u);
+    emx0 = max(emx0, u0 ? e0 : 0u);
+    emx1 = max(emx1, u1 ? e1 : 0u);
+  }
+  const uint32_t emn = min(emn0, emn1), emx = max(emx0, emx1);
+  if (emn == 256u) { out = 0.0; return true; }
+  if (emx >= 255u || emx - emn > 24u || (int)(emx - emn) > 29 - lg_d) return sqd_seq_terms<32>(q, d, lg_d, out);
+  uint32_t lo[4] = {0u, 0u, 0u, 0u}, hi[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int t = 0; t < 32; ++t) {
+    const uint32_t u = __float_as_uint(q[t]);
+    const uint32_t e = u >> 23;
+    const uint32_t m = u ? (u & 0x7fffffu) | (e ? 0x800000u : 0u) : 0u;
+    const uint32_t sh = max(e, 1u) - emn;  // <= 24 for every nonzero term (0 terms add nothing)
+    lo[t & 3] += (m << (sh & 31u)) & 0xffffffu;
+    hi[t & 3] += sh ? m >> (24u - sh) : 0u;
+  }
+  const unsigned long long S = ((unsigned long long)(hi[0] + hi[1] + hi[2] + hi[3]) << 24) +
+                               (unsigned long long)(lo[0] + lo[1] + lo[2] + lo[3]);
+  out = sqd_from_units(S, emn);
+  return true;
+}
+
 }  // namespace sc

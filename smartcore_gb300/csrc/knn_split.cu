@@ -259,12 +259,15 @@ struct KnnPipe {
   uint8_t *sA, *sOnes, *sB;
   uint64_t *full, *empty, *afull, *aempty, *accfull, *accempty, *mma_done;
   int *s_abort;
-  int a_blk, a_bytes, b_blk, b_stage;
+  int a_blk, a_bytes, b_blk, b_stage;  // a_bytes: one 128-query half
   int n_tiles_q, n_tiles_t, nkt, kt_elems, row_bytes, stages;
+  int qh;     // 128-query halves per query tile, each with its accumulator pair
+  int b_box;  // training rows per TMA box (a tile of TN rows takes TN / b_box boxes)
 };
 
 // TMA producer (one thread): per query tile its split halves once (and the
-// ones tile on the first), then the training tiles in index order.
+// ones tile on the first), then the training tiles in index order.  A query
+// tile is qh x 128 queries; each training tile serves all of them.
 template <int TN>
 __device__ void knn_tma_role(const KnnPipe &P, const CUtensorMap *tm_qh, const CUtensorMap *tm_ql,
                              const CUtensorMap *tm_th, const CUtensorMap *tm_tl, const CUtensorMap *tm_ones,
@@ -273,11 +276,12 @@ __device__ void knn_tma_role(const KnnPipe &P, const CUtensorMap *tm_qh, const C
   bool ok = true;
   for (int qt = blockIdx.x; ok && qt < P.n_tiles_q; qt += gridDim.x, ++ql) {
     if (!tc::mbar_wait(P.aempty, (uint32_t)(ql & 1) ^ 1u, kWaitNs)) { ok = false; break; }
-    tc::mbar_expect_tx(P.afull, (uint32_t)(P.a_bytes + (ql == 0 ? kQM * 32 : 0)));
-    for (int part = 0; part < 2; ++part)
-      for (int kt = 0; kt < P.nkt; ++kt)
-        tc::tma_load_2d(P.sA + (part * P.nkt + kt) * P.a_blk, part ? tm_ql : tm_qh, P.afull, kt * P.kt_elems,
-                        qt * kQM);
+    tc::mbar_expect_tx(P.afull, (uint32_t)(P.qh * P.a_bytes + (ql == 0 ? kQM * 32 : 0)));
+    for (int h = 0; h < P.qh; ++h)
+      for (int part = 0; part < 2; ++part)
+        for (int kt = 0; kt < P.nkt; ++kt)
+          tc::tma_load_2d(P.sA + h * P.a_bytes + (part * P.nkt + kt) * P.a_blk, part ? tm_ql : tm_qh, P.afull,
+                          kt * P.kt_elems, (qt * P.qh + h) * kQM);
     if (ql == 0) tc::tma_load_2d(P.sOnes, tm_ones, P.afull, 0, 0);
     for (int tt = 0; tt < P.n_tiles_t; ++tt, ++it) {
       const int s = it % P.stages;
@@ -285,11 +289,13 @@ __device__ void knn_tma_role(const KnnPipe &P, const CUtensorMap *tm_qh, const C
       if (!tc::mbar_wait(&P.empty[s], ph ^ 1u, kWaitNs) || *(volatile int *)P.s_abort) { ok = false; break; }
       tc::mbar_expect_tx(&P.full[s], (uint32_t)P.b_stage);
       uint8_t *dst = P.sB + (size_t)s * P.b_stage;
-      for (int part = 0; part < 2; ++part)
-        for (int kt = 0; kt < P.nkt; ++kt)
-          tc::tma_load_2d(dst + (part * P.nkt + kt) * P.b_blk, part ? tm_tl : tm_th, &P.full[s], kt * P.kt_elems,
-                          tt * TN);
-      tc::tma_load_2d(dst + 2 * P.nkt * P.b_blk, tm_tbx, &P.full[s], 0, tt * TN);
+      for (int r = 0; r < TN; r += P.b_box) {  // boxes stack rows in the K-major operand layout
+        for (int part = 0; part < 2; ++part)
+          for (int kt = 0; kt < P.nkt; ++kt)
+            tc::tma_load_2d(dst + (part * P.nkt + kt) * P.b_blk + r * P.row_bytes, part ? tm_tl : tm_th, &P.full[s],
+                            kt * P.kt_elems, tt * TN + r);
+        tc::tma_load_2d(dst + 2 * P.nkt * P.b_blk + r * 32, tm_tbx, &P.full[s], 0, tt * TN + r);
+      }
     }
   }
   if (!ok) atomicExch(P.s_abort, 1);
@@ -298,8 +304,9 @@ __device__ void knn_tma_role(const KnnPipe &P, const CUtensorMap *tm_qh, const C
   if (ql > 0) tc::mbar_wait(P.afull, (uint32_t)((ql - 1) & 1), kWaitNs);
 }
 
-// MMA issuer (one thread): per training tile, into accumulator it & 1,
-// -||t||^2 / 2 (ones x norm-folding rows) then q_h.t_h + q_h.t_l + q_l.t_h.
+// MMA issuer (one thread): per training tile and query half h, into
+// accumulator (h, it & 1) at TMEM column (2 h + (it & 1)) TN: -||t||^2 / 2
+// (ones x norm-folding rows), then q_h.t_h + q_h.t_l + q_l.t_h.
 template <int TN>
 __device__ void knn_mma_role(const KnnPipe &P, uint32_t tmem) {
   const uint32_t idesc = tc::idesc_bf16_f32(kQM, TN);
@@ -318,17 +325,20 @@ __device__ void knn_mma_role(const KnnPipe &P, uint32_t tmem) {
         break;
       }
       tc::fence_after_sync();
-      const uint32_t d_tmem = tmem + (uint32_t)(acc * TN);
       const uint32_t b0 = sB0 + (uint32_t)(s * P.b_stage);
-      tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(2 * P.nkt * P.b_blk), 32), idesc, 0u);
-      for (int prod = 0; prod < 3; ++prod) {
-        const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
-        for (int kt = 0; kt < P.nkt; ++kt)
-          for (int ks = 0; ks < P.kt_elems / 16; ++ks) {
-            const uint64_t ad = tc::smem_desc(sA0 + (uint32_t)((pa * P.nkt + kt) * P.a_blk + ks * 32), P.row_bytes);
-            const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((pb * P.nkt + kt) * P.b_blk + ks * 32), P.row_bytes);
-            tc::mma_f16(d_tmem, ad, bd, idesc, 1u);
-          }
+      for (int h = 0; h < P.qh; ++h) {
+        const uint32_t d_tmem = tmem + (uint32_t)((2 * h + acc) * TN);
+        const uint32_t a0 = sA0 + (uint32_t)(h * P.a_bytes);
+        tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(2 * P.nkt * P.b_blk), 32), idesc, 0u);
+        for (int prod = 0; prod < 3; ++prod) {
+          const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
+          for (int kt = 0; kt < P.nkt; ++kt)
+            for (int ks = 0; ks < P.kt_elems / 16; ++ks) {
+              const uint64_t ad = tc::smem_desc(a0 + (uint32_t)((pa * P.nkt + kt) * P.a_blk + ks * 32), P.row_bytes);
+              const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((pb * P.nkt + kt) * P.b_blk + ks * 32), P.row_bytes);
+              tc::mma_f16(d_tmem, ad, bd, idesc, 1u);
+            }
+        }
       }
       tc::mma_commit(&P.empty[s]);
       tc::mma_commit(&P.accfull[acc]);
@@ -417,7 +427,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
 
   const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
                   a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
-                  p.stages};
+                  p.stages, 1, TN};
   if (warp == 0) {
     if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
   } else if (warp == 1) {
@@ -469,11 +479,19 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         double sq = __longlong_as_double(0x7ff0000000000000ll);
         bool seq = (uint32_t)lane < cnt && qbase + owner < p.m;  // this lane's entry needs the sequential form
         if constexpr (sizeof(T) == 4) {
-          constexpr int KC = TN == 256 ? 1 : TN == 128 ? 2 : 8;  // d_pad <= 32, 64, 256
           bool fb = false;
           float *Sx = s_stage + (warp - 2) * kStageFloats;
-          round_dist_f32<KC>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane,
-                             Sx, Sx + kStageFloats / 2, sq, fb);
+          if constexpr (TN == 128) {  // d_pad <= 64
+            if (p.d <= 32)
+              round_dist_f32<1>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane,
+                                Sx, Sx + kStageFloats / 2, sq, fb);
+            else
+              round_dist_f32<2>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane,
+                                Sx, Sx + kStageFloats / 2, sq, fb);
+          } else {  // d_pad <= 256
+            round_dist_f32<8>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane, Sx,
+                              Sx + kStageFloats / 2, sq, fb);
+          }
           seq = seq && fb;
         }
         if (seq) {
@@ -727,11 +745,13 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
 // of the rows the reference inserts, found without any exact distance.  The
 // refine kernel then computes the reference distances of the listed rows and
 // replays the heap exactly.
-constexpr int kFiltWarps = 4;                        // one per TMEM lane quarter, every tile
-constexpr int kFiltThreads = 32 * (2 + kFiltWarps);  // + warp 0 TMA, warp 1 MMA
+// Filter CTA: warp 0 TMA, warp 1 MMA, then 4 filter warps per 128-query half.
+template <int QH>
+constexpr int filt_threads() { return 32 * (2 + 4 * QH); }
 
 struct FilterParams {
   int64_t n, m;
+  int b_box;
   int n_tiles_t, n_tiles_q;
   int nkt, kt_elems, row_bytes;
   int stages;
@@ -782,70 +802,54 @@ struct FiltLane {
   float root, lo;
 };
 
-// The rows of one 8-column group of a lane with a score at or above the
-// threshold (rare after the first tiles): listed in index order, and pushed
-// into the lane's top-k when above its root.
-__device__ __noinline__ FiltLane filt_group(FiltLane st, float x0, float x1, float x2, float x3, float x4, float x5,
-                                            float x6, float x7, int64_t row0, int64_t n, int32_t *cq, int64_t cap,
-                                            float *top, int k, float marg) {
-  const float xs[8] = {x0, x1, x2, x3, x4, x5, x6, x7};
-#pragma unroll
-  for (int jj = 0; jj < 8; ++jj) {
-    if (xs[jj] >= st.lo && row0 + jj < n) {
-      if (st.cnt < cap) cq[st.cnt] = (int32_t)(row0 + jj);
-      ++st.cnt;
-      if (xs[jj] > st.root) {
-        st.root = topk_push(top, k, xs[jj]);
-        st.lo = __fsub_rd(st.root, marg);
-      }
-    }
-  }
-  return st;
-}
-
-// One 64-column chunk of a lane's scores: the maxima of its 8-column groups
-// against the threshold at the start of the chunk give each lane a mask of
-// groups to look at (a staler threshold only admits more), and one warp-wide
-// OR the groups any lane needs; those are scanned column by column.
-__device__ __forceinline__ FiltLane filt_chunk(FiltLane st, const uint32_t (&v)[64], int64_t jb, int64_t n,
-                                               int32_t *cq, int64_t cap, float *top, int k, float marg) {
+// One block of W columns of a lane's scores (W / 8 <= 32 groups of 8), at
+// TMEM address ta: the maxima of its 8-column groups against the threshold at
+// the start of the block (a staler threshold only admits more) give each lane
+// a mask of groups, one warp-wide OR the groups any lane needs.  Those are
+// read again from TMEM, 8 columns at a time in a rolled loop (the per-column
+// code exists once), and scanned: rows at or above the threshold are listed
+// in index order and pushed into the top-k when above its root.
+template <int W>
+__device__ __forceinline__ void filt_block(FiltLane &st, const uint32_t (&v)[W], uint32_t ta, int64_t jb, int64_t n,
+                                           int32_t *cq, int64_t cap, float *top, int k, float marg) {
   uint32_t lm = 0u;
 #pragma unroll
-  for (int g = 0; g < 8; ++g) {
+  for (int g = 0; g < W / 8; ++g) {
     const float *x = (const float *)&v[8 * g];
     const float gm = fmax3(fmax3(x[0], x[1], x[2]), fmax3(x[3], x[4], x[5]), fmaxf(x[6], x[7]));
     lm |= (gm >= st.lo ? 1u : 0u) << g;
   }
+#pragma unroll 1
   for (uint32_t um = __reduce_or_sync(0xffffffffu, lm); um; um &= um - 1u) {
     const int g = __ffs(um) - 1;
-    if (!((lm >> g) & 1u)) continue;
-#define SC_FILT_GROUP(G)                                                                                          \
-  case G:                                                                                                         \
-    st = filt_group(st, __uint_as_float(v[8 * G]), __uint_as_float(v[8 * G + 1]), __uint_as_float(v[8 * G + 2]), \
-                    __uint_as_float(v[8 * G + 3]), __uint_as_float(v[8 * G + 4]), __uint_as_float(v[8 * G + 5]), \
-                    __uint_as_float(v[8 * G + 6]), __uint_as_float(v[8 * G + 7]), jb + 8 * G, n, cq, cap, top, k,  \
-                    marg);                                                                                        \
-    break;
-    switch (g) {
-      SC_FILT_GROUP(0)
-      SC_FILT_GROUP(1)
-      SC_FILT_GROUP(2)
-      SC_FILT_GROUP(3)
-      SC_FILT_GROUP(4)
-      SC_FILT_GROUP(5)
-      SC_FILT_GROUP(6)
-      SC_FILT_GROUP(7)
+    uint32_t x8[8];
+    tc::tmem_ld8(ta + (uint32_t)(8 * g), x8);
+    tc::tmem_wait_ld();
+    if ((lm >> g) & 1u) {
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        const float x = __uint_as_float(x8[jj]);
+        const int64_t row = jb + 8 * g + jj;
+        if (x >= st.lo && row < n) {
+          if (st.cnt < cap) cq[st.cnt] = (int32_t)row;
+          ++st.cnt;
+          if (x > st.root) {
+            st.root = topk_push(top, k, x);
+            st.lo = __fsub_rd(st.root, marg);
+          }
+        }
+      }
     }
-#undef SC_FILT_GROUP
   }
-  return st;
 }
 
-// Roles: warp 0 TMA, warp 1 MMA (one elected thread each), warps 2-5 filters:
-// warp w reads TMEM lane quarter w % 4 (32 queries), every column of every
-// tile, so each query's running top-k stays with one lane and is never stale.
-template <int TN>
-__global__ void __launch_bounds__(kFiltThreads, 1)
+// Roles: warp 0 TMA, warp 1 MMA (one elected thread each), warps 2 .. 4 QH + 1
+// filters: warp w reads TMEM lane quarter w % 4 (32 queries) of query half
+// (w - 2) / 4, every column of every tile, so each query's running top-k stays
+// with one lane and is never stale.  A query tile is QH x 128 queries: every
+// training tile brought on chip serves all of them.
+template <int TN, int QH>
+__global__ void __launch_bounds__(filt_threads<QH>(), 1)
 knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constant__ CUtensorMap tm_ql,
                   const __grid_constant__ CUtensorMap tm_th, const __grid_constant__ CUtensorMap tm_tl,
                   const __grid_constant__ CUtensorMap tm_ones, const __grid_constant__ CUtensorMap tm_tbx,
@@ -857,10 +861,10 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
   const int b_blk = TN * p.row_bytes;
   const int b_stage = 2 * p.nkt * b_blk + TN * 32;
   uint8_t *sA = base;
-  uint8_t *sOnes = base + a_bytes;
+  uint8_t *sOnes = base + QH * a_bytes;
   uint8_t *sB = sOnes + kQM * 32;
-  float *s_top = (float *)(sB + (size_t)p.stages * b_stage);  // [k][query]: min-heaps of the k largest scores
-  uint64_t *bars = (uint64_t *)(s_top + ((p.k * kQM + 1) & ~1));
+  float *s_top = (float *)(sB + (size_t)p.stages * b_stage);  // [half][k][query]: min-heaps of the k largest scores
+  uint64_t *bars = (uint64_t *)(s_top + QH * p.k * kQM);
   uint64_t *full = bars, *empty = bars + p.stages, *afull = bars + 2 * p.stages;
   uint64_t *aempty = afull + 1, *accfull = afull + 2, *accempty = afull + 4, *mma_done = afull + 6;
   uint32_t *s_tmem = (uint32_t *)(afull + 7);
@@ -876,7 +880,7 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
     tc::mbar_init(mma_done, 1);
     for (int a = 0; a < 2; ++a) {
       tc::mbar_init(&accfull[a], 1);
-      tc::mbar_init(&accempty[a], 32 * kFiltWarps);
+      tc::mbar_init(&accempty[a], 32 * 4 * QH);
     }
     *s_abort = 0;
     tc::fence_mbar_init();
@@ -888,7 +892,7 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
     tc::prefetch_tmap(&tm_tbx);
   }
   if (warp == 1) {
-    tc::tmem_alloc(s_tmem, 2 * TN);
+    tc::tmem_alloc(s_tmem, 2 * QH * TN);
     tc::tmem_relinquish();
   }
   tc::fence_before_sync();
@@ -897,20 +901,20 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
   const uint32_t tmem = *s_tmem;
   const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
                   a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
-                  p.stages};
+                  p.stages, QH, p.b_box};
   if (warp == 0) {
     if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
   } else if (warp == 1) {
     if (lane == 0) knn_mma_role<TN>(P, tmem);
   } else {
-    const int lq = warp & 3;
+    const int lq = warp & 3, half = (warp - 2) >> 2;
     const int row = lq * 32 + lane;
     const float tmax = __uint_as_float(*p.tmax);
-    float *top = s_top + row;
+    float *top = s_top + half * p.k * kQM + row;
     int it = 0;
     bool stop = false;
     for (int qt = blockIdx.x; !stop && qt < p.n_tiles_q; qt += gridDim.x) {
-      const int64_t q = (int64_t)qt * kQM + row;
+      const int64_t q = ((int64_t)qt * QH + half) * kQM + row;
       const bool live = q < p.m;
       for (int s = 0; s < p.k; ++s) top[s * kQM] = -__int_as_float(0x7f800000);
       float root = -__int_as_float(0x7f800000);
@@ -931,17 +935,19 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
           break;
         }
         tc::fence_after_sync();
-        const uint32_t taddr = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(acc * TN);
+        const uint32_t taddr = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)((2 * half + acc) * TN);
         const int64_t j0 = (int64_t)tt * TN;
-        // 64 columns per TMEM load, the next load in flight while a chunk is scanned
-        uint32_t va[64], vb[64];
-        tc::tmem_ld64(taddr, va);
-        tc::tmem_wait_ld();
+        // blocks of up to 128 columns: their TMEM loads issued together, then
+        // one scan (a rolled loop over the blocks keeps the code small)
+        constexpr int W = TN < 128 ? TN : 128;
+#pragma unroll 1
+        for (int c = 0; c < TN; c += W) {
+          uint32_t v[W];
 #pragma unroll
-        for (int c = 0; c < TN / 64; ++c) {
-          if (c + 1 < TN / 64) tc::tmem_ld64(taddr + (uint32_t)(64 * (c + 1)), (c & 1) ? va : vb);
-          st = filt_chunk(st, (c & 1) ? vb : va, j0 + 64 * c, p.n, cq, p.cap, top, p.k, marg);
-          if (c + 1 < TN / 64) tc::tmem_wait_ld();
+          for (int c2 = 0; c2 < W; c2 += 32)
+            tc::tmem_ld32(taddr + (uint32_t)(c + c2), *reinterpret_cast<uint32_t(*)[32]>(&v[c2]));
+          tc::tmem_wait_ld();
+          filt_block<W>(st, v, taddr + (uint32_t)c, j0 + c, p.n, cq, p.cap, top, p.k, marg);
         }
         tc::fence_before_sync();
         tc::mbar_arrive(&accempty[acc]);
@@ -961,7 +967,7 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
   __syncthreads();
   if (warp == 1) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tmem, 2 * TN);
+    tc::tmem_dealloc(tmem, 2 * QH * TN);
   }
   if (threadIdx.x == 0 && *s_abort) atomicExch(&p.stats[1], 1ull);
 }
@@ -978,76 +984,102 @@ __device__ __forceinline__ double knn_exact_sqd(const T *__restrict__ a, const T
   return sq;
 }
 
-// One warp per query: the exact distances of its candidates, 32 at a time
-// (one per lane), then the reference's insertion test and heapify
-// (linear_search.rs:72-77, heap_select.rs:42-50, :71-86) on lane 0, in index
-// order.  The reference's heapify after a replaced root runs sift_down from
-// every internal node; all of them but the root's find their (unchanged)
-// subtrees already in heap order and stop at once (the heap never holds a NaN:
-// a NaN distance fails the insertion test), so one sift_down from the root
-// leaves the same array.  Queries past the candidate capacity (count -1) are
-// left to the FP64 kernel.
-constexpr int kRefineWarps = 8;
+// A row of d <= 32 f32 features into registers, zeros past d: 16-byte loads
+// when d % 4 == 0 (rows then start on 16-byte boundaries), else scalar.
+__device__ __forceinline__ void load_row32(const float *__restrict__ p, int d, float (&x)[32]) {
+  if ((d & 3) == 0) {
+#pragma unroll
+    for (int t = 0; t < 32; t += 4) {
+      const float4 v = t < d ? __ldg(reinterpret_cast<const float4 *>(p + t)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      x[t] = v.x;
+      x[t + 1] = v.y;
+      x[t + 2] = v.z;
+      x[t + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < 32; ++t) x[t] = t < d ? __ldg(p + t) : 0.f;
+  }
+}
+
+// One lane per query: the reference distances of its candidates in index
+// order, each followed by the reference's insertion test and heapify
+// (linear_search.rs:72-77, heap_select.rs:42-50, :71-86).  The reference's
+// heapify after a replaced root runs sift_down from every internal node; all
+// of them but the root's find their (unchanged) subtrees already in heap order
+// and stop at once (the heap never holds a NaN: a NaN distance fails the
+// insertion test), so one sift_down from the root leaves the same array.
+// The heaps live in shared memory, entry e of lane l at [e][l].  Queries past
+// the candidate capacity (count -1) are left to the FP64 kernel.
+constexpr int kRefineThreads = 64;
 template <typename T>
-__global__ void __launch_bounds__(32 * kRefineWarps, 3)
+__global__ void __launch_bounds__(kRefineThreads)
 knn_refine_kernel(const T *__restrict__ train, const T *__restrict__ queries, int64_t m, int d, int lg_d, int k,
                   int64_t cap, const int32_t *__restrict__ cand, const int32_t *__restrict__ count,
                   int64_t *__restrict__ idx_out, double *__restrict__ dist_out, unsigned long long *evals) {
-  __shared__ double s_hD[kRefineWarps][kMaxKnnK];
-  __shared__ int32_t s_hi[kRefineWarps][kMaxKnnK];
-  __shared__ double s_D[kRefineWarps][32];
-  __shared__ int32_t s_j[kRefineWarps][32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double *hD = s_hD[warp], *D = s_D[warp];
-  int32_t *hi = s_hi[warp], *J = s_j[warp];
+  extern __shared__ __align__(8) uint8_t refine_smem[];
+  double *hD = (double *)refine_smem + threadIdx.x;
+  int32_t *hi = (int32_t *)((double *)refine_smem + (size_t)k * kRefineThreads) + threadIdx.x;
+  const int64_t q = (int64_t)blockIdx.x * kRefineThreads + threadIdx.x;
   unsigned long long ev = 0;
-  for (int64_t q = (int64_t)blockIdx.x * kRefineWarps + warp; q < m; q += (int64_t)gridDim.x * kRefineWarps) {
+  if (q < m) {
     const int c = count[q];
-    if (c < 0) continue;
-    for (int s = lane; s < k; s += 32) {
-      hD[s] = __longlong_as_double(0x7ff0000000000000ll);
-      hi[s] = -1;
-    }
-    const T *qrow = queries + q * d;
-    const int32_t *cq = cand + q * cap;
-    for (int b = 0; b < c; b += 32) {
-      const int r = b + lane;
-      double sq = __longlong_as_double(0x7ff0000000000000ll);
-      int32_t j = -1;
-      if (r < c) {
-        j = cq[r];
-        sq = knn_exact_sqd<T>(qrow, train + (int64_t)j * d, d, lg_d);
-        ++ev;
+    if (c >= 0) {
+      for (int s = 0; s < k; ++s) {
+        hD[s * kRefineThreads] = __longlong_as_double(0x7ff0000000000000ll);
+        hi[s * kRefineThreads] = -1;
       }
-      D[lane] = sq;
-      J[lane] = j;
-      __syncwarp();
-      // only rows below the root at the start of the batch can enter
-      uint32_t in = __ballot_sync(0xffffffffu, sqrt_less(sq, hD[0]));
-      if (lane == 0) {
-        double root = hD[0];
-        for (; in; in &= in - 1u) {
-          const int rr = __ffs(in) - 1;
-          const double sr = D[rr];
-          if (sqrt_less(sr, root)) {  // sqrt(D) < root (linear_search.rs:72)
-            hD[0] = sr;
-            hi[0] = J[rr];
-            if (k > 1) heap_sift<1>(hD, hi, 0, k - 1);
-            root = hD[0];
+      double root = __longlong_as_double(0x7ff0000000000000ll);
+      const T *qrow = queries + q * d;
+      const int32_t *cq = cand + q * cap;
+      // f32 rows of up to 32 features: the query row held in registers, each
+      // candidate row loaded whole (16-byte loads when d % 4 == 0)
+      float qv[32];
+      const bool regs = sizeof(T) == 4 && d <= 32;
+      if constexpr (sizeof(T) == 4) {
+        if (regs) load_row32((const float *)qrow, d, qv);
+      }
+      for (int r = 0; r < c; ++r) {
+        const int32_t j = cq[r];
+        double sr;
+        if constexpr (sizeof(T) == 4) {
+          if (regs) {
+            float xv[32];
+            load_row32((const float *)(train + (int64_t)j * d), d, xv);
+#pragma unroll
+            for (int t = 0; t < 32; ++t) {
+              const float df = __fsub_rn(qv[t], xv[t]);
+              xv[t] = __fmul_rn(df, df);
+            }
+            if (!sqd_terms32(xv, d, lg_d, sr)) {
+              sr = 0.0;
+#pragma unroll
+              for (int t = 0; t < 32; ++t)
+                if (t < d) sr = __dadd_rn(sr, (double)xv[t]);
+            }
+          } else {
+            sr = knn_exact_sqd<T>(qrow, train + (int64_t)j * d, d, lg_d);
           }
+        } else {
+          sr = knn_exact_sqd<T>(qrow, train + (int64_t)j * d, d, lg_d);
+        }
+        if (sqrt_less(sr, root)) {  // sqrt(D) < root (linear_search.rs:72)
+          hD[0] = sr;
+          hi[0] = j;
+          if (k > 1) heap_sift<kRefineThreads>(hD, hi, 0, k - 1);
+          root = hD[0];
         }
       }
-      __syncwarp();
+      ev = (unsigned long long)c;
+      for (int s = 0; s < k; ++s) {
+        idx_out[q * k + s] = hi[s * kRefineThreads];
+        dist_out[q * k + s] = __dsqrt_rn(hD[s * kRefineThreads]);  // sqrt(+inf) = +inf for an empty slot
+      }
     }
-    for (int s = lane; s < k; s += 32) {
-      idx_out[q * k + s] = hi[s];
-      dist_out[q * k + s] = __dsqrt_rn(hD[s]);  // sqrt(+inf) = +inf for an empty slot
-    }
-    __syncwarp();
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) ev += __shfl_xor_sync(0xffffffffu, ev, o);
-  if (lane == 0 && ev) atomicAdd(evals, ev);
+  if ((threadIdx.x & 31) == 0 && ev) atomicAdd(evals, ev);
 }
 
 // Queries past the candidate capacity: their rows gathered for the FP64
@@ -1105,9 +1137,9 @@ sc_status map2d(CUtensorMap *m, void *ptr, int64_t rows, int cols, int box_cols,
 
 int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
 
-// Training rows per tile: 256 up to d = 32, then narrower so that the
-// resident query tile and two or more training stages fit in shared memory.
-int knn_tile_n(int d_pad) { return d_pad <= 32 ? 256 : d_pad <= 64 ? 128 : 64; }
+// Training rows per tile: 128 up to d_pad = 64, then 64 so that the resident
+// query tile and two or more training stages fit in shared memory.
+int knn_tile_n(int d_pad) { return d_pad <= 64 ? 128 : 64; }
 
 size_t knn_smem(int nkt, int row_bytes, int stages, int tn, int heap_k, int dtype) {
   return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * tn * row_bytes + tn * 32) +
@@ -1117,16 +1149,23 @@ size_t knn_smem(int nkt, int row_bytes, int stages, int tn, int heap_k, int dtyp
          (size_t)(2 * stages + 7 + 2 * kMaskSlots) * 8 + 16;
 }
 
-size_t filt_smem(int nkt, int row_bytes, int stages, int tn, int k) {
-  return 1024 + (size_t)2 * nkt * kQM * row_bytes + kQM * 32 + (size_t)stages * (2 * nkt * tn * row_bytes + tn * 32) +
-         (size_t)((k * kQM + 1) & ~1) * 4 + (size_t)(2 * stages + 7) * 8 + 16;
+// Filter kernel tiles: 128 queries against 256 training rows up to d_pad = 32
+// (one 128 x 256 MMA per K step: the fewest MMA instructions per score), then
+// the training tiles of knn_tile_n.  One 128-query half per query tile.
+int filt_tile_n(int d_pad) { return d_pad <= 32 ? 256 : knn_tile_n(d_pad); }
+int filt_halves(int) { return 1; }
+
+size_t filt_smem(int nkt, int row_bytes, int stages, int tn, int k, int qh) {
+  return 1024 + (size_t)qh * 2 * nkt * kQM * row_bytes + kQM * 32 +
+         (size_t)stages * (2 * nkt * tn * row_bytes + tn * 32) + (size_t)qh * k * kQM * 4 +
+         (size_t)(2 * stages + 7) * 8 + 16;
 }
 
 // Training stages of the filter kernel: as many as fit, up to 6 (deeper
 // queues hide DRAM latency when the training rows exceed L2).
-int filt_stages(int nkt, int row_bytes, int tn, int k) {
+int filt_stages(int nkt, int row_bytes, int tn, int k, int qh) {
   int st = 6;
-  while (st > 2 && filt_smem(nkt, row_bytes, st, tn, k) > 227 * 1024) --st;
+  while (st > 2 && filt_smem(nkt, row_bytes, st, tn, k, qh) > 227 * 1024) --st;
   return st;
 }
 
@@ -1142,12 +1181,12 @@ int64_t knn_candidate_cap(int64_t n, int k) {
   return c < 256 ? 256 : c;
 }
 
-template <int TN>
+template <int TN, int QH>
 sc_status launch_knn_filter(int grid, size_t smem, const CUtensorMap &tm_qh, const CUtensorMap &tm_ql,
                             const SplitKnnState *s, const FilterParams &p, cudaStream_t st) {
-  auto kern = knn_filter_kernel<TN>;
+  auto kern = knn_filter_kernel<TN, QH>;
   SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<grid, kFiltThreads, smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, p);
+  kern<<<grid, filt_threads<QH>(), smem, st>>>(tm_qh, tm_ql, s->tm_th, s->tm_tl, s->tm_ones, s->tm_tbx, p);
   SC_LAUNCHED();
   return SC_OK;
 }
@@ -1179,8 +1218,11 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
                          const void *queries, int64_t m, int64_t m_pad, int k, int64_t *idx, double *dist,
                          int64_t *rescored, const CUtensorMap &tm_qh, const CUtensorMap &tm_ql, int nkt, int kt_elems,
                          int row_bytes, int tn, float coef_xc, float coef_cc, float coef_ref, cudaStream_t st) {
-  const int stages = filt_stages(nkt, row_bytes, tn, k);
-  const size_t smem = filt_smem(nkt, row_bytes, stages, tn, k);
+  const int qh = filt_halves(nkt * kt_elems);
+  const int b_box = tn;  // rows per box of the training maps
+  tn = filt_tile_n(nkt * kt_elems);
+  const int stages = filt_stages(nkt, row_bytes, tn, k, qh);
+  const size_t smem = filt_smem(nkt, row_bytes, stages, tn, k, qh);
   if (smem > 227 * 1024) {
     set_error("d=%d exceeds the split-BF16 kNN kernel's shared memory", d);
     return SC_ERR_INVALID;
@@ -1201,7 +1243,8 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
   fp.n = n;
   fp.m = m;
   fp.n_tiles_t = (int)((n + tn - 1) / tn);
-  fp.n_tiles_q = (int)(m_pad / kQM);
+  fp.b_box = b_box;
+  fp.n_tiles_q = (int)(m_pad / (kQM * qh));
   fp.nkt = nkt;
   fp.kt_elems = kt_elems;
   fp.row_bytes = row_bytes;
@@ -1218,19 +1261,22 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
   fp.over = s->over;
   fp.stats = s->evals;
   const int grid = fp.n_tiles_q < s->num_sms ? fp.n_tiles_q : s->num_sms;
-  SC_TRY(tn == 256   ? launch_knn_filter<256>(grid, smem, tm_qh, tm_ql, s, fp, st)
-         : tn == 128 ? launch_knn_filter<128>(grid, smem, tm_qh, tm_ql, s, fp, st)
-                     : launch_knn_filter<64>(grid, smem, tm_qh, tm_ql, s, fp, st));
-  const int64_t rwarps = (int64_t)s->num_sms * 64;
-  const int rgrid = (int)((m < rwarps ? m : rwarps) + kRefineWarps - 1) / kRefineWarps;
-  if (dtype == SC_F32)
-    knn_refine_kernel<float><<<rgrid, 32 * kRefineWarps, 0, st>>>((const float *)train, (const float *)queries, m, d,
-                                                                   lg_d, k, cap, s->cand, s->count, idx, dist,
-                                                                   s->evals);
+  if (tn == 256)
+    SC_TRY((launch_knn_filter<256, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
+  else if (tn == 128)
+    SC_TRY((launch_knn_filter<128, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
   else
-    knn_refine_kernel<double><<<rgrid, 32 * kRefineWarps, 0, st>>>((const double *)train, (const double *)queries, m,
+    SC_TRY((launch_knn_filter<64, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
+  const int rgrid = (int)((m + kRefineThreads - 1) / kRefineThreads);
+  const size_t rsmem = (size_t)k * kRefineThreads * 12;
+  if (dtype == SC_F32)
+    knn_refine_kernel<float><<<rgrid, kRefineThreads, rsmem, st>>>((const float *)train, (const float *)queries, m,
                                                                     d, lg_d, k, cap, s->cand, s->count, idx, dist,
                                                                     s->evals);
+  else
+    knn_refine_kernel<double><<<rgrid, kRefineThreads, rsmem, st>>>((const double *)train, (const double *)queries, m,
+                                                                     d, lg_d, k, cap, s->cand, s->count, idx, dist,
+                                                                     s->evals);
   SC_LAUNCHED();
   unsigned long long host[3];
   SC_CUDA(cudaMemcpyAsync(host, s->evals, sizeof host, cudaMemcpyDeviceToHost, st));
@@ -1305,7 +1351,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   int dev = 0;
   SC_CUDA(cudaGetDevice(&dev));
   if (!s->num_sms) SC_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev));
-  const int64_t n_pad = (n + tn - 1) / tn * tn;
+  const int64_t n_pad = (n + 255) / 256 * 256;  // whole tiles of every kernel (TMA boxes never leave the operand)
   if (!s->ready || s->train != train || s->n != n || s->d != d) {  // training operand, once per handle
     s->ready = 0;  // until every buffer below exists
     dfree(s->th, st); dfree(s->tl, st); dfree(s->tbx, st); dfree(s->tmax, st); dfree(s->ones, st);
@@ -1334,7 +1380,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
     s->d = d;
     s->ready = 1;
   }
-  const int64_t m_pad = (m + kQM - 1) / kQM * kQM;
+  const int64_t m_pad = (m + 2 * kQM - 1) / (2 * kQM) * (2 * kQM);  // whole 256-query tiles
   if (m_pad > s->m_cap) {
     s->m_cap = 0;  // a failed allocation leaves no stale capacity
     dfree(s->qh, st); dfree(s->ql, st); dfree(s->qnrm, st); dfree(s->qn2, st);
@@ -1401,9 +1447,9 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   (sh ? launch_knn_split<TT, NN, true>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)            \
       : launch_knn_split<TT, NN, false>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st))
   if (dtype == SC_F32)
-    r = tn == 256 ? SC_KNN_LAUNCH(float, 256) : tn == 128 ? SC_KNN_LAUNCH(float, 128) : SC_KNN_LAUNCH(float, 64);
+    r = tn == 128 ? SC_KNN_LAUNCH(float, 128) : SC_KNN_LAUNCH(float, 64);
   else
-    r = tn == 256 ? SC_KNN_LAUNCH(double, 256) : tn == 128 ? SC_KNN_LAUNCH(double, 128) : SC_KNN_LAUNCH(double, 64);
+    r = tn == 128 ? SC_KNN_LAUNCH(double, 128) : SC_KNN_LAUNCH(double, 64);
 #undef SC_KNN_LAUNCH
   SC_TRY(r);
   unsigned long long host[2];
@@ -1425,7 +1471,7 @@ bool split_knn_serves(int d, int k, int dtype, bool radius) {
   const int d_pad = knn_pad_d(d);
   if (d_pad > 256 || k > kMaxKnnK) return false;
   const int kt = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt, rb = kt * 2, tn = knn_tile_n(d_pad);
-  if (!radius) return filt_smem(nkt, rb, 2, tn, k) <= 227 * 1024;
+  if (!radius) return filt_smem(nkt, rb, 2, filt_tile_n(d_pad), k, filt_halves(d_pad)) <= 227 * 1024;
   const bool sh = knn_smem(nkt, rb, 2, tn, k, dtype) <= 227 * 1024;
   return knn_smem(nkt, rb, 2, tn, sh ? k : 0, dtype) <= 227 * 1024;
 }
