@@ -93,6 +93,7 @@ knn_prep_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_
 
 struct KnnParams {
   int64_t n, m;
+  int b_box;  // training rows per TMA box
   int n_tiles_t, n_tiles_q;
   int nkt, kt_elems, row_bytes;
   int stages;
@@ -427,7 +428,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
 
   const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
                   a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
-                  p.stages, 1, TN};
+                  p.stages, 1, p.b_box};
   if (warp == 0) {
     if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
   } else if (warp == 1) {
@@ -479,19 +480,11 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
         double sq = __longlong_as_double(0x7ff0000000000000ll);
         bool seq = (uint32_t)lane < cnt && qbase + owner < p.m;  // this lane's entry needs the sequential form
         if constexpr (sizeof(T) == 4) {
+          constexpr int KC = TN == 256 ? 1 : TN == 128 ? 2 : 8;  // d_pad <= 32, 64, 256
           bool fb = false;
           float *Sx = s_stage + (warp - 2) * kStageFloats;
-          if constexpr (TN == 128) {  // d_pad <= 64
-            if (p.d <= 32)
-              round_dist_f32<1>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane,
-                                Sx, Sx + kStageFloats / 2, sq, fb);
-            else
-              round_dist_f32<2>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane,
-                                Sx, Sx + kStageFloats / 2, sq, fb);
-          } else {  // d_pad <= 256
-            round_dist_f32<8>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane, Sx,
-                              Sx + kStageFloats / 2, sq, fb);
-          }
+          round_dist_f32<KC>((const float *)train, (const float *)queries, e, cnt, qbase, p.m, p.d, p.lg_d, lane, Sx,
+                             Sx + kStageFloats / 2, sq, fb);
           seq = seq && fb;
         }
         if (seq) {
@@ -1137,8 +1130,8 @@ sc_status map2d(CUtensorMap *m, void *ptr, int64_t rows, int cols, int box_cols,
 
 int knn_pad_d(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : (d + 63) / 64 * 64; }
 
-// Training rows per tile: 128 up to d_pad = 64, then 64 so that the resident
-// query tile and two or more training stages fit in shared memory.
+// Training rows per TMA box: 128 up to d_pad = 64, then 64 so that the
+// resident query tile and two or more training stages fit in shared memory.
 int knn_tile_n(int d_pad) { return d_pad <= 64 ? 128 : 64; }
 
 size_t knn_smem(int nkt, int row_bytes, int stages, int tn, int heap_k, int dtype) {
@@ -1149,9 +1142,9 @@ size_t knn_smem(int nkt, int row_bytes, int stages, int tn, int heap_k, int dtyp
          (size_t)(2 * stages + 7 + 2 * kMaskSlots) * 8 + 16;
 }
 
-// Filter kernel tiles: 128 queries against 256 training rows up to d_pad = 32
-// (one 128 x 256 MMA per K step: the fewest MMA instructions per score), then
-// the training tiles of knn_tile_n.  One 128-query half per query tile.
+// Training rows per tile of both kNN kernels: 256 up to d_pad = 32 (one
+// 128 x 256 MMA per K step: the fewest MMA instructions per score), then the
+// TMA box height of knn_tile_n.  One 128-query half per query tile.
 int filt_tile_n(int d_pad) { return d_pad <= 32 ? 256 : knn_tile_n(d_pad); }
 int filt_halves(int) { return 1; }
 
@@ -1169,14 +1162,15 @@ int filt_stages(int nkt, int row_bytes, int tn, int k, int qh) {
   return st;
 }
 
-// Candidate slots per query: about 4 k (1 + ln(n / k)), the expected number
-// of heap insertions k (1 + ln(n / k)) with room for ties and the bound's
-// slack; a query past it is served by the FP64 kernel.
+// Candidate slots per query: about 6 k (1 + ln(n / k)), the expected number
+// of heap insertions k (1 + ln(n / k)) of rows in random order with room for
+// ordered data, ties and the bound's slack; a query past it is served by the
+// streaming kernel (exact root feedback, no capacity).
 int64_t g_knn_cap_override = 0;
 int64_t knn_candidate_cap(int64_t n, int k) {
   if (g_knn_cap_override > 0) return g_knn_cap_override;
   const double r = (double)n / k > 1.0 ? (double)n / k : 1.0;
-  int64_t c = (int64_t)(4.0 * k * (1.0 + log(r))) + 32;
+  int64_t c = (int64_t)(6.0 * k * (1.0 + log(r))) + 64;
   c = (c + 31) / 32 * 32;
   return c < 256 ? 256 : c;
 }
@@ -1212,15 +1206,20 @@ struct RadiusArgs {
   const int64_t *offsets;  // filling pass
 };
 
-// find: the candidate filter, the exact replay per query, and the FP64
-// kernel for the queries past the candidate capacity.
+struct RadiusArgs;
+sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
+                        int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, const RadiusArgs *rad,
+                        cudaStream_t st, bool streaming = false);
+
+// find: the candidate filter, the exact replay per query, and for the queries
+// past the candidate capacity the streaming kernel (or, where its shared
+// memory does not fit, the FP64 kernel).
 sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, int lg_d,
                          const void *queries, int64_t m, int64_t m_pad, int k, int64_t *idx, double *dist,
                          int64_t *rescored, const CUtensorMap &tm_qh, const CUtensorMap &tm_ql, int nkt, int kt_elems,
                          int row_bytes, int tn, float coef_xc, float coef_cc, float coef_ref, cudaStream_t st) {
   const int qh = filt_halves(nkt * kt_elems);
-  const int b_box = tn;  // rows per box of the training maps
-  tn = filt_tile_n(nkt * kt_elems);
+  const int b_box = knn_tile_n(nkt * kt_elems);  // rows per box of the training maps
   const int stages = filt_stages(nkt, row_bytes, tn, k, qh);
   const size_t smem = filt_smem(nkt, row_bytes, stages, tn, k, qh);
   if (smem > 227 * 1024) {
@@ -1305,7 +1304,15 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
       if (cudaGetLastError() != cudaSuccess) r = SC_ERR_CUDA;
       note_launch();
     }
-    if (r == SC_OK) r = launch_knn_fp64(dtype, train, n, d, qsub, nover, k, isub, dsub, st);
+    int64_t ev2 = nover * n;
+    if (r == SC_OK) {
+      const int d_pad = nkt * kt_elems, stn = filt_tile_n(d_pad);
+      const bool sh = knn_smem(nkt, row_bytes, 2, stn, k, dtype) <= 227 * 1024;
+      if (knn_smem(nkt, row_bytes, 2, stn, sh ? k : 0, dtype) <= 227 * 1024)
+        r = run_split_knn(s, dtype, train, n, d, qsub, nover, k, isub, dsub, &ev2, nullptr, st, true);
+      else
+        r = launch_knn_fp64(dtype, train, n, d, qsub, nover, k, isub, dsub, st);
+    }
     if (r == SC_OK) {
       scatter_heaps_kernel<<<(int)((nover * k + 255) / 256), 256, 0, st>>>(s->over, nover, k, isub, dsub, idx, dist);
       if (cudaGetLastError() != cudaSuccess) r = SC_ERR_CUDA;
@@ -1316,19 +1323,21 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
     dfree(isub, st);
     dfree(dsub, st);
     if (r != SC_OK) {
-      if (r == SC_ERR_CUDA) set_error("kNN: the FP64 pass over %lld queries past the candidate capacity failed",
+      if (r == SC_ERR_CUDA) set_error("kNN: the pass over %lld queries past the candidate capacity failed",
                                       (long long)nover);
       return r;
     }
-    evals += nover * n;
+    evals += ev2;
   }
   if (rescored) *rescored = evals;
   return SC_OK;
 }
 
+// streaming: find through the streaming kernel (each query's heap replayed as
+// the tiles arrive; no candidate capacity) instead of filter + replay.
 sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
                         int64_t m, int k, int64_t *idx, double *dist, int64_t *rescored, const RadiusArgs *rad,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool streaming) {
   if (rescored) *rescored = 0;
   if (m == 0 || n == 0) return SC_OK;
   if (n >= ((int64_t)1 << kRowBits)) {
@@ -1337,7 +1346,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   }
   const int d_pad = knn_pad_d(d);
   const int kt_elems = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt_elems, row_bytes = kt_elems * 2;
-  const int tn = knn_tile_n(d_pad);
+  const int tn = filt_tile_n(d_pad), box = knn_tile_n(d_pad);
   // heaps in shared memory when they fit beside at least two training stages
   bool sh = knn_smem(nkt, row_bytes, 2, tn, k, dtype) <= 227 * 1024;
   const int heap_k = sh ? k : 0;
@@ -1372,9 +1381,9 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
       knn_prep_kernel<double><<<nb, 256, 0, st>>>((const double *)train, n, n_pad, d, d_pad, s->th, s->tl,
                                                  nullptr, nullptr, nullptr, s->tmax, s->tbx);
     SC_LAUNCHED();
-    SC_TRY(map2d(&s->tm_th, s->th, n_pad, d_pad, kt_elems, tn, row_bytes));
-    SC_TRY(map2d(&s->tm_tl, s->tl, n_pad, d_pad, kt_elems, tn, row_bytes));
-    SC_TRY(map2d(&s->tm_tbx, s->tbx, n_pad, 16, 16, tn, 32));
+    SC_TRY(map2d(&s->tm_th, s->th, n_pad, d_pad, kt_elems, box, row_bytes));
+    SC_TRY(map2d(&s->tm_tl, s->tl, n_pad, d_pad, kt_elems, box, row_bytes));
+    SC_TRY(map2d(&s->tm_tbx, s->tbx, n_pad, 16, 16, box, 32));
     s->train = train;
     s->n = n;
     s->d = d;
@@ -1409,7 +1418,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   const float coef_ref = (float)((d + 4) * 0x1p-52);
   int lg_d = 0;
   while ((1 << lg_d) < d) ++lg_d;
-  if (!rad) return run_split_find(s, dtype, train, n, d, lg_d, queries, m, m_pad, k, idx, dist, rescored, tm_qh, tm_ql,
+  if (!rad && !streaming) return run_split_find(s, dtype, train, n, d, lg_d, queries, m, m_pad, k, idx, dist, rescored, tm_qh, tm_ql,
                                   nkt, kt_elems, row_bytes, tn, coef_xc, coef_cc, coef_ref, st);
   KnnParams p;
   memset(&p, 0, sizeof p);
@@ -1417,6 +1426,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   p.m = m;
   p.n_tiles_t = (int)(n_pad / tn);
   p.n_tiles_q = (int)(m_pad / kQM);
+  p.b_box = box;
   p.nkt = nkt;
   p.kt_elems = kt_elems;
   p.row_bytes = row_bytes;
@@ -1447,9 +1457,9 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   (sh ? launch_knn_split<TT, NN, true>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st)            \
       : launch_knn_split<TT, NN, false>(grid, smem, tm_qh, tm_ql, s, train, queries, p, st))
   if (dtype == SC_F32)
-    r = tn == 128 ? SC_KNN_LAUNCH(float, 128) : SC_KNN_LAUNCH(float, 64);
+    r = tn == 256 ? SC_KNN_LAUNCH(float, 256) : tn == 128 ? SC_KNN_LAUNCH(float, 128) : SC_KNN_LAUNCH(float, 64);
   else
-    r = tn == 128 ? SC_KNN_LAUNCH(double, 128) : SC_KNN_LAUNCH(double, 64);
+    r = tn == 256 ? SC_KNN_LAUNCH(double, 256) : tn == 128 ? SC_KNN_LAUNCH(double, 128) : SC_KNN_LAUNCH(double, 64);
 #undef SC_KNN_LAUNCH
   SC_TRY(r);
   unsigned long long host[2];
@@ -1470,7 +1480,7 @@ void split_knn_set_candidate_cap(int64_t cap) { g_knn_cap_override = cap > 0 ? c
 bool split_knn_serves(int d, int k, int dtype, bool radius) {
   const int d_pad = knn_pad_d(d);
   if (d_pad > 256 || k > kMaxKnnK) return false;
-  const int kt = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt, rb = kt * 2, tn = knn_tile_n(d_pad);
+  const int kt = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt, rb = kt * 2, tn = filt_tile_n(d_pad);
   if (!radius) return filt_smem(nkt, rb, 2, filt_tile_n(d_pad), k, filt_halves(d_pad)) <= 227 * 1024;
   const bool sh = knn_smem(nkt, rb, 2, tn, k, dtype) <= 227 * 1024;
   return knn_smem(nkt, rb, 2, tn, sh ? k : 0, dtype) <= 227 * 1024;
