@@ -406,6 +406,44 @@ static sc_status lloyd_step(sc_kmeans *h) {
   return SC_OK;
 }
 
+// One Lloyd step captured as a CUDA graph (its kernels recorded, not run):
+// the later steps of an iterate call replay it, one launch instead of the
+// step's nine.  Every buffer exists after the call's first step and the
+// step's kernels take the same arguments each time (their state lives on the
+// device), so the replay runs exactly what lloyd_step would launch.
+// *kernels gets the step's kernel count; the capture itself launches nothing.
+static sc_status capture_step(sc_kmeans *h, cudaGraphExec_t *exec, int64_t *kernels) {
+  *exec = nullptr;
+  cudaStream_t s = h->stream;
+  const long long l0 = g_launches.load();
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return SC_ERR_CUDA;
+  }
+  const sc_status r = lloyd_step(h);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &g);
+  *kernels = g_launches.load() - l0;
+  g_launches.fetch_sub(*kernels);
+  if (r != SC_OK || e != cudaSuccess || !g || cudaGraphInstantiate(exec, g, 0) != cudaSuccess) {
+    *exec = nullptr;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return SC_ERR_CUDA;
+  }
+  cudaGraphDestroy(g);
+  return SC_OK;
+}
+
+namespace {
+struct GraphExecGuard {
+  cudaGraphExec_t exec = nullptr;
+  ~GraphExecGuard() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+}  // namespace
+
 sc_status sc_kmeans_iterate(sc_kmeans *h, int64_t max_iter, int32_t stop_on_converge, int64_t *iters_done) {
   if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
   if (h->k < 1) { set_error("centroids are not set"); return SC_ERR_INVALID; }
@@ -417,7 +455,20 @@ sc_status sc_kmeans_iterate(sc_kmeans *h, int64_t max_iter, int32_t stop_on_conv
   SC_CUDA(cudaMemcpyAsync(&h->st->iters, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
   SC_CUDA(cudaMemcpyAsync(&h->st->rescored, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
   SC_CUDA(cudaMemcpyAsync(&h->st->incremental_steps, &zero, sizeof zero, cudaMemcpyHostToDevice, s));
-  for (int64_t t = 0; t < max_iter; ++t) SC_TRY(lloyd_step(h));
+  GraphExecGuard graph;
+  int64_t per_step = 0;
+  for (int64_t t = 0; t < max_iter; ++t) {
+    if (graph.exec) {
+      SC_CUDA(cudaGraphLaunch(graph.exec, s));
+      g_launches.fetch_add(per_step, std::memory_order_relaxed);
+      continue;
+    }
+    SC_TRY(lloyd_step(h));
+    // per-step timing events stay outside graphs; a failed capture leaves
+    // the plain launches
+    if (t == 0 && max_iter > 2 && !h->profile && capture_step(h, &graph.exec, &per_step) != SC_OK)
+      graph.exec = nullptr;
+  }
   if (iters_done) {
     SC_CUDA(cudaMemcpyAsync(iters_done, &h->st->iters, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     SC_CUDA(cudaStreamSynchronize(s));
