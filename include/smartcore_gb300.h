@@ -125,7 +125,10 @@ sc_status sc_kmeans_set_centroids(sc_kmeans *h, int64_t k,
 /* Runs Lloyd iterations.  stop_on_converge = 1: the reference loop (at most
  * max_iter iterations, break rule of kmeans.rs:305-309).  0: exactly
  * max_iter full iterations with the break rule disabled (throughput runs).
- * iters_done may be NULL; otherwise the call waits for completion. */
+ * iters_done may be NULL; otherwise the call waits for completion.  With
+ * more than two iterations the later ones replay the second captured as a
+ * CUDA graph on the handle's stream (not when the caller is capturing that
+ * stream, or with per-step timing on). */
 sc_status sc_kmeans_iterate(sc_kmeans *h, int64_t max_iter,
                             int32_t stop_on_converge, int64_t *iters_done);
 /* Copies the state to host buffers (any may be NULL). */

@@ -464,9 +464,12 @@ sc_status sc_kmeans_iterate(sc_kmeans *h, int64_t max_iter, int32_t stop_on_conv
       continue;
     }
     SC_TRY(lloyd_step(h));
-    // per-step timing events stay outside graphs; a failed capture leaves
-    // the plain launches
-    if (t == 0 && max_iter > 2 && !h->profile && capture_step(h, &graph.exec, &per_step) != SC_OK)
+    // per-step timing events stay outside graphs, and a stream the caller is
+    // capturing into its own graph keeps plain launches; a failed capture
+    // leaves them too
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (t == 0 && max_iter > 2 && !h->profile && cudaStreamIsCapturing(s, &cs) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusNone && capture_step(h, &graph.exec, &per_step) != SC_OK)
       graph.exec = nullptr;
   }
   if (iters_done) {
