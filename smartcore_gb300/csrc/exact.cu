@@ -122,6 +122,14 @@ sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
 // ---------------------------------------------------------------------------
 constexpr int kPPThreads = 256;
 
+// Programmatic dependent launch (the draw and selection kernels of
+// k-means++ alternate 2 (k - 1) times): a kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may start while its
+// predecessor runs; it must wait for the predecessor's completion and memory
+// before reading its results.  Without that attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait_prerequisite() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 int pp_block_count(int64_t n) { return (int)((n + kPPThreads - 1) / kPPThreads); }
 
 // f32 terms: fl32(fl32(x - c)^2) is within (1 +- 2^-24)^3 of (x - c)^2, or
@@ -247,6 +255,10 @@ pp_draw_kernel(const float *__restrict__ x, int64_t n, int d, const LloydState *
   __shared__ uint8_t s_valr[kDrawWarps][kPPThreads];  // rows whose exact value is known
   __shared__ double s_valv[kDrawWarps][kPPThreads];   // and that value
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // launched as a programmatic dependent of the previous draw's selection:
+  // the CTAs come up while it runs and wait here for its results
+  pdl_release_dependents();
+  pdl_wait_prerequisite();
   const int64_t ci = st->pp_chosen;
   for (int t = threadIdx.x; t < 128; t += kDrawThreads) s_cen[t] = t < d ? x[ci * d + t] : 0.f;
   __syncthreads();
@@ -554,6 +566,24 @@ int device_sms() {
   return sms[dev];
 }
 
+// Launches kern as a programmatic dependent of the stream's previous kernel
+// (the kernel itself waits for its predecessor: pdl_wait_prerequisite).
+template <typename... KArgs, typename... Args>
+sc_status launch_pdl(void (*kern)(KArgs...), int grid, int threads, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  SC_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+  return SC_OK;
+}
+
 sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
                            const LloydState *st, int32_t label_of_seed,
                            double *dd, float *dd32, int32_t *labels, double *part,
@@ -588,11 +618,11 @@ sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,
       const int g1 = std::min((grid + kDrawWarps - 1) / kDrawWarps, sms * 7);
       const PPFar32 far = pp_far_bound32(d);
       if (vec4)
-        pp_draw_kernel<4><<<g1, kDrawThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
-                                                      lg_d, seed_cc, far, xh, d_pad, xnrm);
+        SC_TRY(launch_pdl(pp_draw_kernel<4>, g1, kDrawThreads, 0, s, xf, n, d, st, label_of_seed, dd, dd32, labels,
+                          part, (int64_t)grid, lg_d, seed_cc, far, xh, d_pad, xnrm));
       else
-        pp_draw_kernel<1><<<g1, kDrawThreads, 0, s>>>(xf, n, d, st, label_of_seed, dd, dd32, labels, part, grid,
-                                                      lg_d, seed_cc, far, xh, d_pad, xnrm);
+        SC_TRY(launch_pdl(pp_draw_kernel<1>, g1, kDrawThreads, 0, s, xf, n, d, st, label_of_seed, dd, dd32, labels,
+                          part, (int64_t)grid, lg_d, seed_cc, far, xh, d_pad, xnrm));
       SC_LAUNCHED();
     }
   } else if (dtype == SC_F32) {
@@ -638,6 +668,8 @@ pp_select_kernel(const T *__restrict__ x, int d, const double *__restrict__ dd,
   __shared__ int s_chunk;
   __shared__ long long s_pick;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  pdl_release_dependents();  // the next draw's CTAs may come up now; they wait for this kernel's results
+  pdl_wait_prerequisite();   // the draw's partial sums
   const int chunk = (nb + kScan - 1) / kScan;
   const int b0 = min(nb, t * chunk), b1 = min(nb, b0 + chunk);
   double v = 0.0;
@@ -722,11 +754,11 @@ sc_status launch_pp_select(int dtype, const void *x, int d, const double *dd, co
                            int64_t n, int nb, const double *uniform, LloydState *st,
                            void *seed_x, float *seed_cc, int j, cudaStream_t s) {
   if (dtype == SC_F32)
-    pp_select_kernel<float><<<1, kSelThreads, 0, s>>>((const float *)x, d, dd, part, n, nb, uniform, st,
-                                                      (float *)seed_x, seed_cc, j);
+    SC_TRY(launch_pdl(pp_select_kernel<float>, 1, kSelThreads, 0, s, (const float *)x, d, dd, part, n, nb, uniform,
+                      st, (float *)seed_x, seed_cc, j));
   else
-    pp_select_kernel<double><<<1, kSelThreads, 0, s>>>((const double *)x, d, dd, part, n, nb, uniform, st,
-                                                       (double *)seed_x, seed_cc, j);
+    SC_TRY(launch_pdl(pp_select_kernel<double>, 1, kSelThreads, 0, s, (const double *)x, d, dd, part, n, nb, uniform,
+                      st, (double *)seed_x, seed_cc, j));
   SC_LAUNCHED();
   return SC_OK;
 }
