@@ -34,6 +34,29 @@ void note_launch();
     if (s_ != SC_OK) return s_;                                              \
   } while (0)
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may start
+// while the stream's previous kernel runs; it calls pdl_wait_prerequisite()
+// before its first read of that kernel's results (and before any early
+// exit), and pdl_release_dependents() to let its own successor come up.
+// Launched the ordinary way, both are no-ops.
+__device__ __forceinline__ void pdl_wait_prerequisite() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+template <typename... KArgs, typename... Args>
+sc_status launch_pdl(void (*kern)(KArgs...), int64_t grid, int threads, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  SC_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+  return SC_OK;
+}
+
 // ---- device-resident state of one Lloyd loop ----
 struct LloydState {
   double distortion;   // the reference's `distortion` (starts at f64::MAX)

@@ -122,13 +122,8 @@ sc_status launch_assign_fp64(int dtype, const void *x, int64_t n, int d,
 // ---------------------------------------------------------------------------
 constexpr int kPPThreads = 256;
 
-// Programmatic dependent launch (the draw and selection kernels of
-// k-means++ alternate 2 (k - 1) times): a kernel launched with
-// cudaLaunchAttributeProgrammaticStreamSerialization may start while its
-// predecessor runs; it must wait for the predecessor's completion and memory
-// before reading its results.  Without that attribute both are no-ops.
-__device__ __forceinline__ void pdl_wait_prerequisite() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_release_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+// The draw and selection kernels of k-means++ alternate 2 (k - 1) times;
+// they are launched as programmatic dependents (launch_pdl, common.cuh).
 
 int pp_block_count(int64_t n) { return (int)((n + kPPThreads - 1) / kPPThreads); }
 
@@ -564,24 +559,6 @@ int device_sms() {
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 132;
   if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms[dev] = 132;
   return sms[dev];
-}
-
-// Launches kern as a programmatic dependent of the stream's previous kernel
-// (the kernel itself waits for its predecessor: pdl_wait_prerequisite).
-template <typename... KArgs, typename... Args>
-sc_status launch_pdl(void (*kern)(KArgs...), int grid, int threads, size_t smem, cudaStream_t s, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3((unsigned)threads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  SC_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
-  return SC_OK;
 }
 
 sc_status launch_pp_update(int dtype, const void *x, int64_t n, int d,

@@ -44,6 +44,8 @@ __global__ void __launch_bounds__(128)
 prep_c_kernel(const double *__restrict__ cent, int k, int d, int d_pad, int k_pad, int k_cols,
               __nv_bfloat16 *__restrict__ ch, __nv_bfloat16 *__restrict__ cl, __nv_bfloat16 *__restrict__ cbx,
               float *__restrict__ cn2, unsigned int *__restrict__ cmax, float *__restrict__ cT) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   __shared__ double ws[4];
   const int j = blockIdx.x;
   double s = 0.0;
@@ -120,6 +122,8 @@ split_assign_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_cons
                     const __grid_constant__ CUtensorMap tm_ch, const __grid_constant__ CUtensorMap tm_cl,
                     const __grid_constant__ CUtensorMap tm_ones, const __grid_constant__ CUtensorMap tm_cbx,
                     const AssignParams p) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (p.st && p.st->done) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -400,6 +404,8 @@ split_wide_kernel(const __grid_constant__ CUtensorMap tm_xh, const __grid_consta
                   const __grid_constant__ CUtensorMap tm_ch, const __grid_constant__ CUtensorMap tm_cl,
                   const __grid_constant__ CUtensorMap tm_ones, const __grid_constant__ CUtensorMap tm_cbx,
                   const AssignParams p) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (p.st && p.st->done) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -684,6 +690,8 @@ rescore_kernel(const T *__restrict__ x, int d, const double *__restrict__ cent, 
                const int64_t *__restrict__ list_rows, const unsigned int *__restrict__ list_count, int region,
                const uint2 *__restrict__ cand4, const uint8_t *__restrict__ cmeta, int64_t n_pad,
                int32_t *__restrict__ labels, LloydState *st, int stage_ct) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (st && st->done) return;
   // dynamic: [d x k_cols centroids^T when stage_ct] [d x kRsRows rows^T] [kRsRows x mw survivor masks]
   extern __shared__ __align__(16) float dyn[];
@@ -1030,8 +1038,8 @@ sc_status split_centroids_changed(SplitState *s, const double *cent, int k, cuda
   s->k = k;
   s->k_pad = k_pad;
   SC_CUDA(cudaMemsetAsync(s->cmax, 0, sizeof(unsigned int), st));
-  prep_c_kernel<<<k_cols, 128, 0, st>>>(cent, k, s->d, s->d_pad, k_pad, k_cols, s->ch, s->cl, s->cbx, s->cn2,
-                                        s->cmax, s->cT);
+  SC_TRY(launch_pdl(prep_c_kernel, k_cols, 128, 0, st, cent, k, s->d, s->d_pad, k_pad, k_cols, s->ch, s->cl, s->cbx,
+                    s->cn2, s->cmax, s->cT));
   SC_LAUNCHED();
   return SC_OK;
 }
@@ -1087,13 +1095,13 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   if (s->wide) {
     SC_CUDA(cudaFuncSetAttribute(split_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
-    split_wide_kernel<<<grid, kWideThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, s->tm_ones,
-                                                        s->tm_cbx, p);
+    SC_TRY(launch_pdl(split_wide_kernel, grid, kWideThreads, smem, st, s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl,
+                      s->tm_ones, s->tm_cbx, p));
   } else {
     SC_CUDA(cudaFuncSetAttribute(split_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (timing) SC_CUDA(cudaEventRecord(timing[0], st));
-    split_assign_kernel<<<grid, kAssignThreads, smem, st>>>(s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl, s->tm_ones,
-                                                            s->tm_cbx, p);
+    SC_TRY(launch_pdl(split_assign_kernel, grid, kAssignThreads, smem, st, s->tm_xh, s->tm_xl, s->tm_ch, s->tm_cl,
+                      s->tm_ones, s->tm_cbx, p));
   }
   SC_LAUNCHED();
   if (timing) SC_CUDA(cudaEventRecord(timing[1], st));
@@ -1105,15 +1113,13 @@ sc_status split_assign(SplitState *s, int dtype, const void *x, int64_t n, int d
   if (dtype == SC_F32) {
     auto kern = rescore_kernel<float>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
-    kern<<<grid, kRsThreads, rsmem, st>>>((const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax, s->xnrm,
-                                          s->list_rows, s->list_count, p.region, s->cand4, s->cmeta, s->n_pad,
-                                          labels, lst, stage);
+    SC_TRY(launch_pdl(kern, grid, kRsThreads, rsmem, st, (const float *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
+                      s->xnrm, s->list_rows, s->list_count, p.region, s->cand4, s->cmeta, s->n_pad, labels, lst, stage));
   } else {
     auto kern = rescore_kernel<double>;
     SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
-    kern<<<grid, kRsThreads, rsmem, st>>>((const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
-                                          s->xnrm, s->list_rows, s->list_count, p.region, s->cand4, s->cmeta,
-                                          s->n_pad, labels, lst, stage);
+    SC_TRY(launch_pdl(kern, grid, kRsThreads, rsmem, st, (const double *)x, d, cent, k, k_cols, s->cT, s->cn2, s->cmax,
+                      s->xnrm, s->list_rows, s->list_count, p.region, s->cand4, s->cmeta, s->n_pad, labels, lst, stage));
   }
   SC_LAUNCHED();
   return SC_OK;

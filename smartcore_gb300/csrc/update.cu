@@ -265,6 +265,8 @@ __global__ void __launch_bounds__(1024)
 update_balanced_kernel(const float *__restrict__ x, const uint32_t *__restrict__ xq, int64_t n, int d,
                        const int32_t *__restrict__ labels, int k, long long *__restrict__ part,
                        unsigned int *__restrict__ cpart, int scale, const LloydState *st, int64_t mcap) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (st && (st->done || incremental_step(st, mcap))) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   unsigned long long *acc = reinterpret_cast<unsigned long long *>(smraw);  // k x d
@@ -417,6 +419,8 @@ finalize_partials_kernel(const long long *__restrict__ part, const unsigned int 
                          int nparts, int k, double *__restrict__ cent, int64_t *__restrict__ sizes, int d,
                          int scale, double *__restrict__ terms, int empty_nan, const LloydState *st,
                          Acc128 *__restrict__ tot, unsigned long long *__restrict__ tcnt, int64_t mcap) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (st && (st->done || incremental_step(st, mcap))) return;
   __shared__ unsigned long long s_lo[8][32], s_hi[8][32];
   __shared__ unsigned long long s_cn[8][32];
@@ -476,6 +480,8 @@ finalize_partials_kernel(const long long *__restrict__ part, const unsigned int 
 __global__ void __launch_bounds__(256)
 label_diff_kernel(const int32_t *__restrict__ labels, int32_t *__restrict__ prev, int64_t n,
                   int64_t *__restrict__ mrows, int32_t *__restrict__ mold, int64_t mcap, LloydState *st) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (st->done) return;
   const int lane = threadIdx.x & 31;
   for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
@@ -511,6 +517,8 @@ __global__ void __launch_bounds__(256)
 moved_rows_kernel(const float *__restrict__ x, int d, const int32_t *__restrict__ labels,
                   const int64_t *__restrict__ mrows, const int32_t *__restrict__ mold, int64_t mcap,
                   Acc128 *__restrict__ tot, unsigned long long *__restrict__ tcnt, int scale, const LloydState *st) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (st->done || !incremental_step(st, mcap)) return;
   const int64_t nm = st->moved;
   const int lane = threadIdx.x & 31;
@@ -538,6 +546,8 @@ __global__ void __launch_bounds__(32)
 finalize_total_kernel(const Acc128 *__restrict__ tot, const unsigned long long *__restrict__ tcnt, int k,
                       double *__restrict__ cent, int64_t *__restrict__ sizes, int d, int scale,
                       double *__restrict__ terms, LloydState *st, int64_t mcap) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (st->done || !incremental_step(st, mcap)) return;
   const int64_t kd = (int64_t)k * d;
   const int e = threadIdx.x;
@@ -626,6 +636,8 @@ __global__ void __launch_bounds__(kScalarThreads)
 finalize_scalar_kernel(const double *__restrict__ part, int nparts,
                        const double *__restrict__ cluster_terms, int64_t k,
                        const double *__restrict__ xnorm_total, LloydState *st) {
+  pdl_release_dependents();  // launched as a programmatic dependent in the Lloyd step
+  pdl_wait_prerequisite();
   if (st->done) return;
   __shared__ double ws[kScalarThreads / 32];
   const double *a = part ? part : cluster_terms;
@@ -660,7 +672,7 @@ sc_status launch_finalize_scalar(const double *part, int nparts,
                                  const double *cluster_terms, int64_t k,
                                  const double *xnorm_total, LloydState *st,
                                  cudaStream_t s) {
-  finalize_scalar_kernel<<<1, kScalarThreads, 0, s>>>(part, nparts, cluster_terms, k, xnorm_total, st);
+  SC_TRY(launch_pdl(finalize_scalar_kernel, 1, kScalarThreads, 0, s, part, nparts, cluster_terms, k, xnorm_total, st));
   SC_LAUNCHED();
   return SC_OK;
 }
@@ -816,7 +828,8 @@ static sc_status launch_balanced(const UpdateBuf *u, const float *x, int64_t n, 
   auto kern = !packed ? update_balanced_kernel<MAXJ, false, false>
               : u->xq_slow ? update_balanced_kernel<MAXJ, true, true> : update_balanced_kernel<MAXJ, true, false>;
   SC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)u->balanced_smem));
-  kern<<<u->grid, 1024, u->balanced_smem, s>>>(x, u->xq, n, d, labels, k, u->part, u->cpart, u->scale, st, u->mcap);
+  SC_TRY(launch_pdl(kern, u->grid, 1024, u->balanced_smem, s, x, u->xq, n, d, labels, k, u->part, u->cpart, u->scale,
+                    st, u->mcap));
   SC_LAUNCHED();
   return SC_OK;
 }
@@ -864,7 +877,7 @@ sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n,
   LloydState *ms = const_cast<LloydState *>(st);
   const int sms = u->grid > 0 ? u->grid : 1;
   if (ms) {
-    label_diff_kernel<<<sms * 8, 256, 0, s>>>(labels, u->prev, n, u->mrows, u->mold, u->mcap, ms);
+    SC_TRY(launch_pdl(label_diff_kernel, sms * 8, 256, 0, s, labels, u->prev, n, u->mrows, u->mold, u->mcap, ms));
     SC_LAUNCHED();
   }
   if (u->balanced_smem) {
@@ -878,8 +891,8 @@ sc_status launch_update(const UpdateBuf *u, int dtype, const void *x, int64_t n,
     else SC_TRY(launch_sorted<8>(u, xf, n, d, labels, k, st, s));
   }
   if (ms) {
-    moved_rows_kernel<<<sms * 4, 256, 0, s>>>(xf, d, labels, u->mrows, u->mold, u->mcap, u->tot, u->tcnt, u->scale,
-                                             ms);
+    SC_TRY(launch_pdl(moved_rows_kernel, sms * 4, 256, 0, s, xf, d, labels, u->mrows, u->mold, u->mcap, u->tot,
+                      u->tcnt, u->scale, ms));
     SC_LAUNCHED();
   }
   return SC_OK;
@@ -901,12 +914,12 @@ sc_status launch_finalize(const UpdateBuf *u, double *cent, int64_t *sizes, int 
     return launch_finalize_centroids(u->acc, u->cnt, cent, sizes, k, d, u->scale, terms, empty_nan, st, s);
   const int64_t kd = (int64_t)k * d;
   const int blocks = (int)((kd + 31) / 32);
-  finalize_partials_kernel<<<blocks, 256, 0, s>>>(u->part, u->cpart, u->grid, k, cent, sizes, d, u->scale, terms,
-                                                  empty_nan, st, u->tot, u->tcnt, u->mcap);
+  SC_TRY(launch_pdl(finalize_partials_kernel, blocks, 256, 0, s, u->part, u->cpart, u->grid, k, cent, sizes, d,
+                    u->scale, terms, empty_nan, st, u->tot, u->tcnt, u->mcap));
   SC_LAUNCHED();
   if (st) {
-    finalize_total_kernel<<<blocks, 32, 0, s>>>(u->tot, u->tcnt, k, cent, sizes, d, u->scale, terms,
-                                                const_cast<LloydState *>(st), u->mcap);
+    SC_TRY(launch_pdl(finalize_total_kernel, blocks, 32, 0, s, u->tot, u->tcnt, k, cent, sizes, d, u->scale, terms,
+                      const_cast<LloydState *>(st), u->mcap));
     SC_LAUNCHED();
   }
   return SC_OK;
