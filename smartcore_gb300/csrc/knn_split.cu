@@ -47,11 +47,13 @@ __device__ __forceinline__ double ref_term(double a, double b) {
   return __dmul_rn(r, r);
 }
 
-// Rows of a matrix as split-BF16 operand: halves, f32 upper bound of the norm,
-// ||row||^2 rounded to f32 (+inf for padding rows) and in f64.
+// Rows of a matrix as split-BF16 operand: halves (row i of either at
+// [i * stride]: separate arrays, or both halves in one row when interleaved),
+// f32 upper bound of the norm, ||row||^2 rounded to f32 (+inf for padding
+// rows) and in f64.
 template <typename T>
 __global__ void __launch_bounds__(256)
-knn_prep_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_pad,
+knn_prep_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_pad, int stride,
                 __nv_bfloat16 *__restrict__ xh, __nv_bfloat16 *__restrict__ xl, float *__restrict__ nrm,
                 float *__restrict__ n2f, double *__restrict__ n2d, unsigned int *__restrict__ nmax,
                 __nv_bfloat16 *__restrict__ bx) {
@@ -66,8 +68,8 @@ knn_prep_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_
       split2<T>(v, h, l);
       s = fma((double)v, (double)v, s);
     }
-    xh[i * d_pad + j] = h;
-    xl[i * d_pad + j] = l;
+    xh[i * stride + j] = h;
+    xl[i * stride + j] = l;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -94,6 +96,7 @@ knn_prep_kernel(const T *__restrict__ x, int64_t n, int64_t n_pad, int d, int d_
 struct KnnParams {
   int64_t n, m;
   int b_box;  // training rows per TMA box
+  int il;     // interleaved halves (KnnPipe::il)
   int n_tiles_t, n_tiles_q;
   int nkt, kt_elems, row_bytes;
   int stages;
@@ -264,6 +267,8 @@ struct KnnPipe {
   int n_tiles_q, n_tiles_t, nkt, kt_elems, row_bytes, stages;
   int qh;     // 128-query halves per query tile, each with its accumulator pair
   int b_box;  // training rows per TMA box (a tile of TN rows takes TN / b_box boxes)
+  int il;     // interleaved halves: one row_bytes row holds the high then the low half (d_pad = 32:
+              // 128-byte rows, 128-byte swizzle); else the halves are separate nkt-block operands
 };
 
 // TMA producer (one thread): per query tile its split halves once (and the
@@ -279,7 +284,7 @@ __device__ void knn_tma_role(const KnnPipe &P, const CUtensorMap *tm_qh, const C
     if (!tc::mbar_wait(P.aempty, (uint32_t)(ql & 1) ^ 1u, kWaitNs)) { ok = false; break; }
     tc::mbar_expect_tx(P.afull, (uint32_t)(P.qh * P.a_bytes + (ql == 0 ? kQM * 32 : 0)));
     for (int h = 0; h < P.qh; ++h)
-      for (int part = 0; part < 2; ++part)
+      for (int part = 0; part < (P.il ? 1 : 2); ++part)
         for (int kt = 0; kt < P.nkt; ++kt)
           tc::tma_load_2d(P.sA + h * P.a_bytes + (part * P.nkt + kt) * P.a_blk, part ? tm_ql : tm_qh, P.afull,
                           kt * P.kt_elems, (qt * P.qh + h) * kQM);
@@ -290,12 +295,13 @@ __device__ void knn_tma_role(const KnnPipe &P, const CUtensorMap *tm_qh, const C
       if (!tc::mbar_wait(&P.empty[s], ph ^ 1u, kWaitNs) || *(volatile int *)P.s_abort) { ok = false; break; }
       tc::mbar_expect_tx(&P.full[s], (uint32_t)P.b_stage);
       uint8_t *dst = P.sB + (size_t)s * P.b_stage;
+      const int parts = P.il ? 1 : 2;
       for (int r = 0; r < TN; r += P.b_box) {  // boxes stack rows in the K-major operand layout
-        for (int part = 0; part < 2; ++part)
+        for (int part = 0; part < parts; ++part)
           for (int kt = 0; kt < P.nkt; ++kt)
             tc::tma_load_2d(dst + (part * P.nkt + kt) * P.b_blk + r * P.row_bytes, part ? tm_tl : tm_th, &P.full[s],
                             kt * P.kt_elems, tt * TN + r);
-        tc::tma_load_2d(dst + 2 * P.nkt * P.b_blk + r * 32, tm_tbx, &P.full[s], 0, tt * TN + r);
+        tc::tma_load_2d(dst + parts * P.nkt * P.b_blk + r * 32, tm_tbx, &P.full[s], 0, tt * TN + r);
       }
     }
   }
@@ -327,16 +333,21 @@ __device__ void knn_mma_role(const KnnPipe &P, uint32_t tmem) {
       }
       tc::fence_after_sync();
       const uint32_t b0 = sB0 + (uint32_t)(s * P.b_stage);
+      const int parts = P.il ? 1 : 2;
       for (int h = 0; h < P.qh; ++h) {
         const uint32_t d_tmem = tmem + (uint32_t)((2 * h + acc) * TN);
         const uint32_t a0 = sA0 + (uint32_t)(h * P.a_bytes);
-        tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(2 * P.nkt * P.b_blk), 32), idesc, 0u);
+        tc::mma_f16(d_tmem, ones_desc, tc::smem_desc(b0 + (uint32_t)(parts * P.nkt * P.b_blk), 32), idesc, 0u);
         for (int prod = 0; prod < 3; ++prod) {
           const int pa = prod == 2 ? 1 : 0, pb = prod == 1 ? 1 : 0;
+          // a half's K slices: its own nkt-block operand, or (interleaved) its
+          // 64-byte half of each 128-byte row
+          const int pa_off = P.il ? pa * P.kt_elems * 2 : pa * P.nkt * P.a_blk;
+          const int pb_off = P.il ? pb * P.kt_elems * 2 : pb * P.nkt * P.b_blk;
           for (int kt = 0; kt < P.nkt; ++kt)
             for (int ks = 0; ks < P.kt_elems / 16; ++ks) {
-              const uint64_t ad = tc::smem_desc(a0 + (uint32_t)((pa * P.nkt + kt) * P.a_blk + ks * 32), P.row_bytes);
-              const uint64_t bd = tc::smem_desc(b0 + (uint32_t)((pb * P.nkt + kt) * P.b_blk + ks * 32), P.row_bytes);
+              const uint64_t ad = tc::smem_desc(a0 + (uint32_t)(pa_off + kt * P.a_blk + ks * 32), P.row_bytes);
+              const uint64_t bd = tc::smem_desc(b0 + (uint32_t)(pb_off + kt * P.b_blk + ks * 32), P.row_bytes);
               tc::mma_f16(d_tmem, ad, bd, idesc, 1u);
             }
         }
@@ -370,9 +381,9 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int a_blk = kQM * p.row_bytes;
-  const int a_bytes = 2 * p.nkt * a_blk;
+  const int a_bytes = (p.il ? 1 : 2) * p.nkt * a_blk;
   const int b_blk = TN * p.row_bytes;
-  const int b_stage = 2 * p.nkt * b_blk + TN * 32;  // halves + norm-folding rows
+  const int b_stage = (p.il ? 1 : 2) * p.nkt * b_blk + TN * 32;  // halves + norm-folding rows
   uint8_t *sA = base;
   uint8_t *sOnes = base + a_bytes;                   // 128 x 32 B
   uint8_t *sB = sOnes + kQM * 32;
@@ -428,7 +439,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
 
   const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
                   a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
-                  p.stages, 1, p.b_box};
+                  p.stages, 1, p.b_box, p.il};
   if (warp == 0) {
     if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
   } else if (warp == 1) {
@@ -745,6 +756,7 @@ constexpr int filt_threads() { return 32 * (2 + 4 * QH); }
 struct FilterParams {
   int64_t n, m;
   int b_box;
+  int il;  // interleaved halves (KnnPipe::il)
   int n_tiles_t, n_tiles_q;
   int nkt, kt_elems, row_bytes;
   int stages;
@@ -850,9 +862,9 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int a_blk = kQM * p.row_bytes;
-  const int a_bytes = 2 * p.nkt * a_blk;
+  const int a_bytes = (p.il ? 1 : 2) * p.nkt * a_blk;
   const int b_blk = TN * p.row_bytes;
-  const int b_stage = 2 * p.nkt * b_blk + TN * 32;
+  const int b_stage = (p.il ? 1 : 2) * p.nkt * b_blk + TN * 32;
   uint8_t *sA = base;
   uint8_t *sOnes = base + QH * a_bytes;
   uint8_t *sB = sOnes + kQM * 32;
@@ -894,7 +906,7 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
   const uint32_t tmem = *s_tmem;
   const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
                   a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
-                  p.stages, QH, p.b_box};
+                  p.stages, QH, p.b_box, p.il};
   if (warp == 0) {
     if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
   } else if (warp == 1) {
@@ -1217,7 +1229,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
 sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, int lg_d,
                          const void *queries, int64_t m, int64_t m_pad, int k, int64_t *idx, double *dist,
                          int64_t *rescored, const CUtensorMap &tm_qh, const CUtensorMap &tm_ql, int nkt, int kt_elems,
-                         int row_bytes, int tn, float coef_xc, float coef_cc, float coef_ref, cudaStream_t st) {
+                         int row_bytes, int il, int tn, float coef_xc, float coef_cc, float coef_ref, cudaStream_t st) {
   const int qh = filt_halves(nkt * kt_elems);
   const int b_box = knn_tile_n(nkt * kt_elems);  // rows per box of the training maps
   const int stages = filt_stages(nkt, row_bytes, tn, k, qh);
@@ -1246,7 +1258,8 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
   fp.n_tiles_q = (int)(m_pad / (kQM * qh));
   fp.nkt = nkt;
   fp.kt_elems = kt_elems;
-  fp.row_bytes = row_bytes;
+  fp.row_bytes = il ? 2 * row_bytes : row_bytes;  // sizes above use the half width: the same bytes either way
+  fp.il = il;
   fp.stages = stages;
   fp.k = k;
   fp.qnrm = s->qnrm;
@@ -1346,6 +1359,9 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   }
   const int d_pad = knn_pad_d(d);
   const int kt_elems = d_pad >= 64 ? 64 : d_pad, nkt = d_pad / kt_elems, row_bytes = kt_elems * 2;
+  // d_pad = 32: both halves of a row in one 128-byte row (128-byte swizzle);
+  // the same bytes as two 64-byte operands, so the sizes keep row_bytes
+  const int il = d_pad == 32 ? 1 : 0, lay_bytes = il ? 2 * row_bytes : row_bytes;
   const int tn = filt_tile_n(d_pad), box = knn_tile_n(d_pad);
   // heaps in shared memory when they fit beside at least two training stages
   bool sh = knn_smem(nkt, row_bytes, 2, tn, k, dtype) <= 227 * 1024;
@@ -1364,8 +1380,8 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   if (!s->ready || s->train != train || s->n != n || s->d != d) {  // training operand, once per handle
     s->ready = 0;  // until every buffer below exists
     dfree(s->th, st); dfree(s->tl, st); dfree(s->tbx, st); dfree(s->tmax, st); dfree(s->ones, st);
-    SC_TRY(dalloc(&s->th, (size_t)n_pad * d_pad, st));
-    SC_TRY(dalloc(&s->tl, (size_t)n_pad * d_pad, st));
+    SC_TRY(dalloc(&s->th, (size_t)n_pad * d_pad * (il ? 2 : 1), st));
+    if (!il) SC_TRY(dalloc(&s->tl, (size_t)n_pad * d_pad, st));
     SC_TRY(dalloc(&s->tbx, (size_t)n_pad * 16, st));
     SC_TRY(dalloc(&s->tmax, 1, st));
     SC_TRY(dalloc(&s->ones, (size_t)kQM * 16, st));
@@ -1375,14 +1391,21 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
     SC_CUDA(cudaMemsetAsync(s->tmax, 0, sizeof(unsigned int), st));
     const int nb = (int)((n_pad + 7) / 8);
     if (dtype == SC_F32)
-      knn_prep_kernel<float><<<nb, 256, 0, st>>>((const float *)train, n, n_pad, d, d_pad, s->th, s->tl, nullptr,
+      knn_prep_kernel<float><<<nb, 256, 0, st>>>((const float *)train, n, n_pad, d, d_pad, il ? 2 * d_pad : d_pad,
+                                                s->th, il ? s->th + d_pad : s->tl, nullptr,
                                                 nullptr, nullptr, s->tmax, s->tbx);
     else
-      knn_prep_kernel<double><<<nb, 256, 0, st>>>((const double *)train, n, n_pad, d, d_pad, s->th, s->tl,
+      knn_prep_kernel<double><<<nb, 256, 0, st>>>((const double *)train, n, n_pad, d, d_pad, il ? 2 * d_pad : d_pad,
+                                                 s->th, il ? s->th + d_pad : s->tl,
                                                  nullptr, nullptr, nullptr, s->tmax, s->tbx);
     SC_LAUNCHED();
-    SC_TRY(map2d(&s->tm_th, s->th, n_pad, d_pad, kt_elems, box, row_bytes));
-    SC_TRY(map2d(&s->tm_tl, s->tl, n_pad, d_pad, kt_elems, box, row_bytes));
+    if (il) {
+      SC_TRY(map2d(&s->tm_th, s->th, n_pad, 2 * d_pad, 2 * kt_elems, box, lay_bytes));
+      s->tm_tl = s->tm_th;  // unused: one operand holds both halves
+    } else {
+      SC_TRY(map2d(&s->tm_th, s->th, n_pad, d_pad, kt_elems, box, row_bytes));
+      SC_TRY(map2d(&s->tm_tl, s->tl, n_pad, d_pad, kt_elems, box, row_bytes));
+    }
     SC_TRY(map2d(&s->tm_tbx, s->tbx, n_pad, 16, 16, box, 32));
     s->train = train;
     s->n = n;
@@ -1393,8 +1416,8 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   if (m_pad > s->m_cap) {
     s->m_cap = 0;  // a failed allocation leaves no stale capacity
     dfree(s->qh, st); dfree(s->ql, st); dfree(s->qnrm, st); dfree(s->qn2, st);
-    SC_TRY(dalloc(&s->qh, (size_t)m_pad * d_pad, st));
-    SC_TRY(dalloc(&s->ql, (size_t)m_pad * d_pad, st));
+    SC_TRY(dalloc(&s->qh, (size_t)m_pad * d_pad * (il ? 2 : 1), st));
+    if (!il) SC_TRY(dalloc(&s->ql, (size_t)m_pad * d_pad, st));
     SC_TRY(dalloc(&s->qnrm, (size_t)m_pad, st));
     SC_TRY(dalloc(&s->qn2, (size_t)m_pad, st));
     s->m_cap = m_pad;
@@ -1403,23 +1426,31 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   SC_CUDA(cudaMemsetAsync(s->evals, 0, 3 * sizeof(unsigned long long), st));
   const int nbq = (int)((m_pad + 7) / 8);
   if (dtype == SC_F32)
-    knn_prep_kernel<float><<<nbq, 256, 0, st>>>((const float *)queries, m, m_pad, d, d_pad, s->qh, s->ql, s->qnrm,
+    knn_prep_kernel<float><<<nbq, 256, 0, st>>>((const float *)queries, m, m_pad, d, d_pad, il ? 2 * d_pad : d_pad,
+                                               s->qh, il ? s->qh + d_pad : s->ql, s->qnrm,
                                                nullptr, s->qn2, nullptr, nullptr);
   else
-    knn_prep_kernel<double><<<nbq, 256, 0, st>>>((const double *)queries, m, m_pad, d, d_pad, s->qh, s->ql,
+    knn_prep_kernel<double><<<nbq, 256, 0, st>>>((const double *)queries, m, m_pad, d, d_pad, il ? 2 * d_pad : d_pad,
+                                                s->qh, il ? s->qh + d_pad : s->ql,
                                                 s->qnrm, nullptr, s->qn2, nullptr, nullptr);
   SC_LAUNCHED();
   CUtensorMap tm_qh, tm_ql;
-  SC_TRY(map2d(&tm_qh, s->qh, m_pad, d_pad, kt_elems, kQM, row_bytes));
-  SC_TRY(map2d(&tm_ql, s->ql, m_pad, d_pad, kt_elems, kQM, row_bytes));
+  if (il) {
+    SC_TRY(map2d(&tm_qh, s->qh, m_pad, 2 * d_pad, 2 * kt_elems, kQM, lay_bytes));
+    tm_ql = tm_qh;
+  } else {
+    SC_TRY(map2d(&tm_qh, s->qh, m_pad, d_pad, kt_elems, kQM, row_bytes));
+    SC_TRY(map2d(&tm_ql, s->ql, m_pad, d_pad, kt_elems, kQM, row_bytes));
+  }
   const double nacc = 3.0 * d_pad + 3.0;
   const float coef_xc = (float)(3.02 * 0x1p-16 + 1.02 * nacc * 0x1p-22);
   const float coef_cc = (float)(1.01 * 0x1p-25 + 0.51 * nacc * 0x1p-22);
   const float coef_ref = (float)((d + 4) * 0x1p-52);
   int lg_d = 0;
   while ((1 << lg_d) < d) ++lg_d;
-  if (!rad && !streaming) return run_split_find(s, dtype, train, n, d, lg_d, queries, m, m_pad, k, idx, dist, rescored, tm_qh, tm_ql,
-                                  nkt, kt_elems, row_bytes, tn, coef_xc, coef_cc, coef_ref, st);
+  if (!rad && !streaming)
+    return run_split_find(s, dtype, train, n, d, lg_d, queries, m, m_pad, k, idx, dist, rescored, tm_qh, tm_ql, nkt,
+                          kt_elems, row_bytes, il, tn, coef_xc, coef_cc, coef_ref, st);
   KnnParams p;
   memset(&p, 0, sizeof p);
   p.n = n;
@@ -1429,7 +1460,8 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
   p.b_box = box;
   p.nkt = nkt;
   p.kt_elems = kt_elems;
-  p.row_bytes = row_bytes;
+  p.row_bytes = lay_bytes;
+  p.il = il;
   p.stages = stages;
   p.k = k;
   p.d = d;
