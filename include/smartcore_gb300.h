@@ -336,9 +336,14 @@ sc_status sc_debug_fail_alloc_after(int64_t after);
  * count as freed when issued). */
 int64_t sc_debug_live_allocations(void);
 /* Candidate slots per query of the split-BF16 find (cap <= 0 restores the
- * default, about 4 k (1 + ln(n / k))); queries with more candidates are
- * served by the FP64 kernel.  A small cap exercises that path. */
+ * default, 6 k (1 + ln(n / k)) + 64 rounded up to 32, at least 256); queries
+ * with more candidates are served by the streaming kernel afterwards.  A small
+ * cap exercises that path. */
 sc_status sc_debug_knn_candidate_cap(int64_t cap);
+/* Queries per pass of the split-BF16 find (rounded down to whole query tiles
+ * of 128 or 256; q <= 0 restores the default, as many as keep the candidate
+ * lists within 2 GB).  A small value exercises the passes over query chunks. */
+sc_status sc_debug_knn_chunk_queries(int64_t q);
 
 #ifdef __cplusplus
 }

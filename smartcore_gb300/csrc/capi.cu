@@ -573,6 +573,11 @@ sc_status sc_debug_knn_candidate_cap(int64_t cap) {
   return SC_OK;
 }
 
+sc_status sc_debug_knn_chunk_queries(int64_t q) {
+  split_knn_set_chunk_queries(q);
+  return SC_OK;
+}
+
 sc_status sc_kmeans_sync(sc_kmeans *h) {
   if (!h) { set_error("null handle"); return SC_ERR_INVALID; }
   SC_CUDA(cudaStreamSynchronize(h->stream));

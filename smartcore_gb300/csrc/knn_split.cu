@@ -267,6 +267,7 @@ struct KnnPipe {
   int n_tiles_q, n_tiles_t, nkt, kt_elems, row_bytes, stages;
   int qh;     // 128-query halves per query tile, each with its accumulator pair
   int b_box;  // training rows per TMA box (a tile of TN rows takes TN / b_box boxes)
+  int qt0;    // first query tile (a chunk of the queries starts there)
   int il;     // interleaved halves: one row_bytes row holds the high then the low half (d_pad = 32:
               // 128-byte rows, 128-byte swizzle); else the halves are separate nkt-block operands
 };
@@ -287,7 +288,7 @@ __device__ void knn_tma_role(const KnnPipe &P, const CUtensorMap *tm_qh, const C
       for (int part = 0; part < (P.il ? 1 : 2); ++part)
         for (int kt = 0; kt < P.nkt; ++kt)
           tc::tma_load_2d(P.sA + h * P.a_bytes + (part * P.nkt + kt) * P.a_blk, part ? tm_ql : tm_qh, P.afull,
-                          kt * P.kt_elems, (qt * P.qh + h) * kQM);
+                          kt * P.kt_elems, ((P.qt0 + qt) * P.qh + h) * kQM);
     if (ql == 0) tc::tma_load_2d(P.sOnes, tm_ones, P.afull, 0, 0);
     for (int tt = 0; tt < P.n_tiles_t; ++tt, ++it) {
       const int s = it % P.stages;
@@ -439,7 +440,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
 
   const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
                   a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
-                  p.stages, 1, p.b_box, p.il};
+                  p.stages, 1, p.b_box, 0, p.il};
   if (warp == 0) {
     if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
   } else if (warp == 1) {
@@ -756,7 +757,8 @@ constexpr int filt_threads() { return 32 * (2 + 4 * QH); }
 struct FilterParams {
   int64_t n, m;
   int b_box;
-  int il;  // interleaved halves (KnnPipe::il)
+  int il;   // interleaved halves (KnnPipe::il)
+  int qt0;  // the chunk's first query tile: cand and count are indexed from its first query
   int n_tiles_t, n_tiles_q;
   int nkt, kt_elems, row_bytes;
   int stages;
@@ -765,8 +767,8 @@ struct FilterParams {
   const unsigned int *tmax;
   float coef_xc, coef_cc, coef_ref;
   int64_t cap;                 // candidate slots per query
-  int32_t *cand;               // [m_pad][cap]: rows in index order
-  int32_t *count;              // per query: candidates, or -1 past cap
+  int32_t *cand;               // [chunk queries][cap]: rows in index order
+  int32_t *count;              // per query of the chunk: candidates, or -1 past cap
   int32_t *over;               // the queries past cap
   unsigned long long *stats;   // [1] wait timed out, [2] queries past cap
 };
@@ -906,7 +908,7 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
   const uint32_t tmem = *s_tmem;
   const KnnPipe P{sA, sOnes, sB, full, empty, afull, aempty, accfull, accempty, mma_done, s_abort,
                   a_blk, a_bytes, b_blk, b_stage, p.n_tiles_q, p.n_tiles_t, p.nkt, p.kt_elems, p.row_bytes,
-                  p.stages, QH, p.b_box, p.il};
+                  p.stages, QH, p.b_box, p.qt0, p.il};
   if (warp == 0) {
     if (lane == 0) knn_tma_role<TN>(P, &tm_qh, &tm_ql, &tm_th, &tm_tl, &tm_ones, &tm_tbx);
   } else if (warp == 1) {
@@ -919,7 +921,8 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
     int it = 0;
     bool stop = false;
     for (int qt = blockIdx.x; !stop && qt < p.n_tiles_q; qt += gridDim.x) {
-      const int64_t q = ((int64_t)qt * QH + half) * kQM + row;
+      const int64_t ql = ((int64_t)qt * QH + half) * kQM + row;  // within the chunk
+      const int64_t q = (int64_t)p.qt0 * QH * kQM + ql;
       const bool live = q < p.m;
       for (int s = 0; s < p.k; ++s) top[s * kQM] = -__int_as_float(0x7f800000);
       float root = -__int_as_float(0x7f800000);
@@ -930,7 +933,7 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
                                 p.coef_ref * (qn + tmax) * (qn + tmax)) + 1e-30f;
       const float marg = __fadd_ru(__fmul_ru(1.01f, eq), 1e-30f);
       FiltLane st{0, root, live ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000)};
-      int32_t *cq = p.cand + (live ? q : 0) * p.cap;
+      int32_t *cq = p.cand + (live ? ql : 0) * p.cap;
       for (int tt = 0; tt < p.n_tiles_t; ++tt, ++it) {
         const int acc = it & 1;
         const bool got = tc::mbar_wait(&accfull[acc], (uint32_t)(it >> 1) & 1u, kWaitNs);
@@ -960,9 +963,9 @@ knn_filter_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_consta
       const int64_t cnt = st.cnt;
       if (live && !stop) {
         if (cnt <= p.cap) {
-          p.count[q] = (int32_t)cnt;
+          p.count[ql] = (int32_t)cnt;
         } else {
-          p.count[q] = -1;
+          p.count[ql] = -1;
           p.over[atomicAdd(&p.stats[2], 1ull)] = (int32_t)q;
         }
       }
@@ -1019,16 +1022,17 @@ __device__ __forceinline__ void load_row32(const float *__restrict__ p, int d, f
 constexpr int kRefineThreads = 64;
 template <typename T>
 __global__ void __launch_bounds__(kRefineThreads)
-knn_refine_kernel(const T *__restrict__ train, const T *__restrict__ queries, int64_t m, int d, int lg_d, int k,
-                  int64_t cap, const int32_t *__restrict__ cand, const int32_t *__restrict__ count,
+knn_refine_kernel(const T *__restrict__ train, const T *__restrict__ queries, int64_t q0, int64_t m, int d, int lg_d,
+                  int k, int64_t cap, const int32_t *__restrict__ cand, const int32_t *__restrict__ count,
                   int64_t *__restrict__ idx_out, double *__restrict__ dist_out, unsigned long long *evals) {
   extern __shared__ __align__(8) uint8_t refine_smem[];
   double *hD = (double *)refine_smem + threadIdx.x;
   int32_t *hi = (int32_t *)((double *)refine_smem + (size_t)k * kRefineThreads) + threadIdx.x;
-  const int64_t q = (int64_t)blockIdx.x * kRefineThreads + threadIdx.x;
+  const int64_t ql = (int64_t)blockIdx.x * kRefineThreads + threadIdx.x;  // within the chunk of m queries
+  const int64_t q = q0 + ql;
   unsigned long long ev = 0;
-  if (q < m) {
-    const int c = count[q];
+  if (ql < m) {
+    const int c = count[ql];
     if (c >= 0) {
       for (int s = 0; s < k; ++s) {
         hD[s * kRefineThreads] = __longlong_as_double(0x7ff0000000000000ll);
@@ -1036,7 +1040,7 @@ knn_refine_kernel(const T *__restrict__ train, const T *__restrict__ queries, in
       }
       double root = __longlong_as_double(0x7ff0000000000000ll);
       const T *qrow = queries + q * d;
-      const int32_t *cq = cand + q * cap;
+      const int32_t *cq = cand + ql * cap;
       // f32 rows of up to 32 features: the query row held in registers, each
       // candidate row loaded whole (16-byte loads when d % 4 == 0)
       float qv[32];
@@ -1179,6 +1183,7 @@ int filt_stages(int nkt, int row_bytes, int tn, int k, int qh) {
 // ordered data, ties and the bound's slack; a query past it is served by the
 // streaming kernel (exact root feedback, no capacity).
 int64_t g_knn_cap_override = 0;
+int64_t g_knn_chunk_override = 0;
 int64_t knn_candidate_cap(int64_t n, int k) {
   if (g_knn_cap_override > 0) return g_knn_cap_override;
   const double r = (double)n / k > 1.0 ? (double)n / k : 1.0;
@@ -1239,14 +1244,19 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
     return SC_ERR_INVALID;
   }
   const int64_t cap = knn_candidate_cap(n, k);
-  if ((size_t)(m_pad * cap) > s->cand_cap || m_pad > s->count_cap) {
+  // queries in chunks whose candidate lists take at most 2 GB, whole query tiles
+  const int64_t tile_q = (int64_t)kQM * qh;
+  int64_t chunk = (g_knn_chunk_override > 0 ? g_knn_chunk_override : ((int64_t)1 << 31) / (cap * 4)) / tile_q * tile_q;
+  if (chunk < tile_q) chunk = tile_q;
+  if (chunk > m_pad) chunk = m_pad;
+  if ((size_t)(chunk * cap) > s->cand_cap || m_pad > s->count_cap) {
     s->cand_cap = 0;
     s->count_cap = 0;
     dfree(s->cand, st); dfree(s->count, st); dfree(s->over, st);
-    SC_TRY(dalloc(&s->cand, (size_t)(m_pad * cap), st));
+    SC_TRY(dalloc(&s->cand, (size_t)(chunk * cap), st));
     SC_TRY(dalloc(&s->count, (size_t)m_pad, st));
     SC_TRY(dalloc(&s->over, (size_t)m_pad, st));
-    s->cand_cap = (size_t)(m_pad * cap);
+    s->cand_cap = (size_t)(chunk * cap);
     s->count_cap = m_pad;
   }
   FilterParams fp;
@@ -1255,7 +1265,7 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
   fp.m = m;
   fp.n_tiles_t = (int)((n + tn - 1) / tn);
   fp.b_box = b_box;
-  fp.n_tiles_q = (int)(m_pad / (kQM * qh));
+  fp.n_tiles_q = 0;  // per chunk, below
   fp.nkt = nkt;
   fp.kt_elems = kt_elems;
   fp.row_bytes = il ? 2 * row_bytes : row_bytes;  // sizes above use the half width: the same bytes either way
@@ -1272,24 +1282,29 @@ sc_status run_split_find(SplitKnnState *s, int dtype, const void *train, int64_t
   fp.count = s->count;
   fp.over = s->over;
   fp.stats = s->evals;
-  const int grid = fp.n_tiles_q < s->num_sms ? fp.n_tiles_q : s->num_sms;
-  if (tn == 256)
-    SC_TRY((launch_knn_filter<256, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
-  else if (tn == 128)
-    SC_TRY((launch_knn_filter<128, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
-  else
-    SC_TRY((launch_knn_filter<64, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
-  const int rgrid = (int)((m + kRefineThreads - 1) / kRefineThreads);
-  const size_t rsmem = (size_t)k * kRefineThreads * 12;
-  if (dtype == SC_F32)
-    knn_refine_kernel<float><<<rgrid, kRefineThreads, rsmem, st>>>((const float *)train, (const float *)queries, m,
-                                                                    d, lg_d, k, cap, s->cand, s->count, idx, dist,
-                                                                    s->evals);
-  else
-    knn_refine_kernel<double><<<rgrid, kRefineThreads, rsmem, st>>>((const double *)train, (const double *)queries, m,
-                                                                     d, lg_d, k, cap, s->cand, s->count, idx, dist,
-                                                                     s->evals);
-  SC_LAUNCHED();
+  for (int64_t q0 = 0; q0 < m; q0 += chunk) {
+    const int64_t mc = m - q0 < chunk ? m - q0 : chunk;
+    fp.qt0 = (int)(q0 / tile_q);
+    fp.n_tiles_q = (int)((mc + tile_q - 1) / tile_q);
+    const int grid = fp.n_tiles_q < s->num_sms ? fp.n_tiles_q : s->num_sms;
+    if (tn == 256)
+      SC_TRY((launch_knn_filter<256, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
+    else if (tn == 128)
+      SC_TRY((launch_knn_filter<128, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
+    else
+      SC_TRY((launch_knn_filter<64, 1>(grid, smem, tm_qh, tm_ql, s, fp, st)));
+    const int rgrid = (int)((mc + kRefineThreads - 1) / kRefineThreads);
+    const size_t rsmem = (size_t)k * kRefineThreads * 12;
+    if (dtype == SC_F32)
+      knn_refine_kernel<float><<<rgrid, kRefineThreads, rsmem, st>>>((const float *)train, (const float *)queries, q0,
+                                                                      mc, d, lg_d, k, cap, s->cand, s->count, idx,
+                                                                      dist, s->evals);
+    else
+      knn_refine_kernel<double><<<rgrid, kRefineThreads, rsmem, st>>>((const double *)train, (const double *)queries,
+                                                                       q0, mc, d, lg_d, k, cap, s->cand, s->count,
+                                                                       idx, dist, s->evals);
+    SC_LAUNCHED();
+  }
   unsigned long long host[3];
   SC_CUDA(cudaMemcpyAsync(host, s->evals, sizeof host, cudaMemcpyDeviceToHost, st));
   SC_CUDA(cudaStreamSynchronize(st));
@@ -1508,6 +1523,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
 }  // namespace
 
 void split_knn_set_candidate_cap(int64_t cap) { g_knn_cap_override = cap > 0 ? cap : 0; }
+void split_knn_set_chunk_queries(int64_t q) { g_knn_chunk_override = q > 0 ? q : 0; }
 
 bool split_knn_serves(int d, int k, int dtype, bool radius) {
   const int d_pad = knn_pad_d(d);

@@ -74,6 +74,7 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
 bool split_knn_serves(int d, int k, int dtype, bool radius);
 // Testing: candidate slots per query of split find (0: the default).
 void split_knn_set_candidate_cap(int64_t cap);
+void split_knn_set_chunk_queries(int64_t q);
 // Widest rows the split-BF16 k-means kernels serve.
 constexpr int kSplitKMeansMaxD = 128;
 // find_radius: counting pass when idx is null (counts[q]), else filling pass

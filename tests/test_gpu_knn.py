@@ -234,8 +234,9 @@ def test_classifier_regressor_large_k(form, weight):
 def test_find_candidate_overflow(dtype, cap):
     """Split find lists each query's candidate rows (a certified superset of
     the rows the reference inserts) before the exact replay; a query with more
-    candidates than its slots is served by the FP64 kernel.  A small cap sends
-    most (8) or some (64) queries down that path, with the same heaps."""
+    candidates than its slots is served by the streaming kernel afterwards.  A
+    small cap sends most (8) or some (64) queries down that path, with the same
+    heaps."""
     L = _lib.load()
     rng = np.random.default_rng(cap)
     train = rng.normal(size=(4000, 24)).astype(dtype)
@@ -253,10 +254,34 @@ def test_find_candidate_overflow(dtype, cap):
     assert np.array_equal(idx, ridx) and np.array_equal(dist, rdist)
 
 
+@pytest.mark.parametrize("d", [8, 32, 100])
+@pytest.mark.parametrize("cap", [0, 64])
+def test_find_query_chunks(d, cap):
+    """Split find runs its filter and replay over chunks of whole query tiles
+    (by default as many queries as keep the candidate lists within 2 GB).
+    Chunks of one tile, a ragged last chunk, and queries past the candidate
+    slots in several chunks give the same heaps."""
+    L = _lib.load()
+    rng = np.random.default_rng(d + cap)
+    train = rng.normal(size=(5000, d)).astype(np.float32)
+    q = rng.normal(size=(1000, d)).astype(np.float32)
+    s = LinearKNNSearch(train, form=_lib.FORM_SPLIT_BF16)
+    ridx, rdist = oracle.knn_find(train, q, 10)
+    try:
+        _lib.check(L.sc_debug_knn_chunk_queries(1))
+        _lib.check(L.sc_debug_knn_candidate_cap(cap))
+        idx, dist = s.find_batch(q, 10)
+    finally:
+        L.sc_debug_knn_chunk_queries(0)
+        L.sc_debug_knn_candidate_cap(0)
+    assert np.array_equal(idx, ridx)
+    assert np.array_equal(dist, rdist)
+
+
 def test_find_sorted_training_rows():
     """Training rows sorted by decreasing distance to the queries make every
-    row a heap insertion: the candidate lists overflow and the FP64 kernel
-    serves those queries."""
+    row a heap insertion: the candidate lists overflow and the streaming
+    kernel serves those queries."""
     rng = np.random.default_rng(11)
     q = rng.normal(size=(40, 8)).astype(np.float32)
     t = rng.normal(size=(3000, 8)).astype(np.float32)
