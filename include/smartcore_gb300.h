@@ -232,7 +232,8 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count,
                                 int32_t dtype, int32_t form);
 /* Tuning of the batched assignment kernel: times its variants (centroids per
  * inner pass, rows per work item) on one synthetic problem per (d class,
- * k class) on the current device and keeps the fastest for this process;
+ * k class), its items repeated so that every CTA has work, on the current
+ * device and keeps the fastest for this process;
  * with path non-NULL also writes the table there.  Without a table the
  * batched call uses fixed defaults. */
 sc_status sc_batch_tune(const char *path);
@@ -344,6 +345,10 @@ sc_status sc_debug_knn_candidate_cap(int64_t cap);
  * of 128 or 256; q <= 0 restores the default, as many as keep the candidate
  * lists within 2 GB).  A small value exercises the passes over query chunks. */
 sc_status sc_debug_knn_chunk_queries(int64_t q);
+/* Every problem of the batched call uses this assignment variant (2, 4 or
+ * 8 centroids per inner pass; a negative value restores the tuning table's
+ * choice). */
+sc_status sc_debug_batch_variant(int32_t variant);
 
 #ifdef __cplusplus
 }

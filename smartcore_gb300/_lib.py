@@ -54,6 +54,7 @@ SIGNATURES = {
     "sc_debug_live_allocations": ([], _I64),
     "sc_debug_knn_candidate_cap": ([_I64], _I32),
     "sc_debug_knn_chunk_queries": ([_I64], _I32),
+    "sc_debug_batch_variant": ([_I32], _I32),
     "sc_knn_create": ([_P, _I32, _I32, _I32, _I64, _I64, _I64, _P], _I32),
     "sc_knn_find": ([_P, _P, _I32, _I32, _I64, _I64, _I64, _I32, _I32, _P, _P], _I32),
     "sc_knn_find_radius": ([_P, _P, _I32, _I32, _I64, _I64, _D, _I32, _P, _I64, _P, _P, _P], _I32),

@@ -38,6 +38,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -266,6 +267,68 @@ __device__ __forceinline__ void load_row(const T *__restrict__ xr, float (&x)[D]
   }
 }
 
+// The label of a scored row: certain when the two best scores differ by more
+// than the bound, else settled among the centroids the difference form cannot
+// exclude with the reference's FP64 distance.  x: the row's f32 values, xr:
+// the row as given; best / second / bi from the scores in centroid order.
+template <typename T, int D>
+__device__ __forceinline__ int settle_row(const float (&x)[D], const T *__restrict__ xr, const BProb &P,
+                                          const double *__restrict__ cent64, const float *s_c, float best,
+                                          float second, int bi, float cdelta, float cmax, long long &rescored) {
+  const int d = P.d, k = P.k;
+  // ||x~|| from above; for f64 rows also ||x - fl32(x)|| <= 2^-24 ||x~|| (1 + 2^-20)
+  float xn = 0.f;
+#pragma unroll
+  for (int j = 0; j < D; ++j) xn = __fmaf_ru(x[j], x[j], xn);
+  const float rn = __fsqrt_ru(xn);
+  float del = cdelta;
+  if constexpr (sizeof(T) == 8) del = __fadd_ru(del, __fmul_ru(rn, 0x1.00001p-24f));
+  // The label is certain when the two best scores differ by more than
+  // 2 (2 E_s + 2 E_d): E_s bounds each score (score32), E_d >= |D - D~|
+  // for every centroid, 2 (||x~|| + cmax) del + del^2, plus the
+  // reference's own FP64 rounding of D; any other centroid's D then
+  // exceeds the best one's (a factor 2 of slack).
+  bool certain;
+  {
+    const float g2 = __fadd_ru(__fmul_ru((float)(D / 2 + 1), 0x1.06p-23f), 0x1p-23f);  // 2 g + 2 u
+    const float rc = __fmul_ru(rn, cmax);
+    float es = __fadd_ru(__fmul_ru(g2, rc), __fmul_ru(0x1.02p-23f, __fmul_ru(cmax, cmax)));
+    es = __fadd_ru(es, __fmul_ru((float)(D + 4), 0x1p-138f));
+    const float rs = __fadd_ru(rn, cmax);
+    float ed = __fadd_ru(__fmul_ru(__fmul_ru(2.f, rs), del), __fmul_ru(del, del));
+    ed = __fadd_ru(ed, __fmul_ru(__fmul_ru((float)(d + 2), 0x1p-52f), __fmul_ru(rs, rs)));
+    const float margin = __fmul_ru(4.f, __fadd_ru(es, ed));
+    certain = __fsub_rd(second, best) > margin;
+  }
+  if (!certain) {
+    // Near tie (or a non-finite value): the difference form bounds each
+    // centroid's D on its own; every centroid whose FP32 distance cannot
+    // be shown to exceed the best one's is scored with the reference's
+    // FP64 distance (src/metrics/distance/euclidian.rs:51-63 on f64 rows,
+    // kmeans.rs:338-346), strict <, lowest index first.
+    const Bound bd = make_bound(d, del);
+    float best32 = __int_as_float(0x7f800000);
+    for (int c = 0; c < k; ++c) best32 = fminf(best32, dist32<D>(x, s_c + c * D));
+    const float thr = __fadd_ru(best32, err_bound(best32, bd));
+    double bdist = DBL_MAX;
+    int b = 0;
+    for (int c = 0; c < k; ++c) {
+      const float a = dist32<D>(x, s_c + c * D);
+      if (__fsub_rd(a, err_bound(a, bd)) > thr) continue;
+      const double *cr = cent64 + P.c_off + (int64_t)c * d;
+      double sd = 0.0;
+      for (int j = 0; j < d; ++j) sd = __dadd_rn(sd, sq_term((double)xr[j], cr[j]));
+      if (sd < bdist) {
+        bdist = sd;
+        b = c;
+      }
+    }
+    ++rescored;
+    return b;
+  }
+  return bi;
+}
+
 // One work item of rows in passes of 256, one row per thread for the
 // distances.  mode 0: assign + sums; mode 1: sums of the given labels (the
 // seeding partition).  The sums are taken warp by warp afterwards: for each
@@ -333,56 +396,7 @@ __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BSt
             }
           }
         }
-        // ||x~|| from above; for f64 rows also ||x - fl32(x)|| <= 2^-24 ||x~|| (1 + 2^-20)
-        float xn = 0.f;
-#pragma unroll
-        for (int j = 0; j < D; ++j) xn = __fmaf_ru(x[j], x[j], xn);
-        const float rn = __fsqrt_ru(xn);
-        float del = cdelta;
-        if constexpr (sizeof(T) == 8) del = __fadd_ru(del, __fmul_ru(rn, 0x1.00001p-24f));
-        // The label is certain when the two best scores differ by more than
-        // 2 (2 E_s + 2 E_d): E_s bounds each score (score32), E_d >= |D - D~|
-        // for every centroid, 2 (||x~|| + cmax) del + del^2, plus the
-        // reference's own FP64 rounding of D; any other centroid's D then
-        // exceeds the best one's (a factor 2 of slack).
-        bool certain;
-        {
-          const float g2 = __fadd_ru(__fmul_ru((float)(D / 2 + 1), 0x1.06p-23f), 0x1p-23f);  // 2 g + 2 u
-          const float rc = __fmul_ru(rn, cmax);
-          float es = __fadd_ru(__fmul_ru(g2, rc), __fmul_ru(0x1.02p-23f, __fmul_ru(cmax, cmax)));
-          es = __fadd_ru(es, __fmul_ru((float)(D + 4), 0x1p-138f));
-          const float rs = __fadd_ru(rn, cmax);
-          float ed = __fadd_ru(__fmul_ru(__fmul_ru(2.f, rs), del), __fmul_ru(del, del));
-          ed = __fadd_ru(ed, __fmul_ru(__fmul_ru((float)(d + 2), 0x1p-52f), __fmul_ru(rs, rs)));
-          const float margin = __fmul_ru(4.f, __fadd_ru(es, ed));
-          certain = __fsub_rd(second, best) > margin;
-        }
-        if (!certain) {
-          // Near tie (or a non-finite value): the difference form bounds each
-          // centroid's D on its own; every centroid whose FP32 distance cannot
-          // be shown to exceed the best one's is scored with the reference's
-          // FP64 distance (src/metrics/distance/euclidian.rs:51-63 on f64 rows,
-          // kmeans.rs:338-346), strict <, lowest index first.
-          const Bound bd = make_bound(d, del);
-          float best32 = __int_as_float(0x7f800000);
-          for (int c = 0; c < k; ++c) best32 = fminf(best32, dist32<D>(x, s_c + c * D));
-          const float thr = __fadd_ru(best32, err_bound(best32, bd));
-          double bdist = DBL_MAX;
-          int b = 0;
-          for (int c = 0; c < k; ++c) {
-            const float a = dist32<D>(x, s_c + c * D);
-            if (__fsub_rd(a, err_bound(a, bd)) > thr) continue;
-            const double *cr = cent64 + P.c_off + (int64_t)c * d;
-            double sd = 0.0;
-            for (int j = 0; j < d; ++j) sd = __dadd_rn(sd, sq_term((double)xr[j], cr[j]));
-            if (sd < bdist) {
-              bdist = sd;
-              b = c;
-            }
-          }
-          bi = b;
-          ++rescored;
-        }
+        bi = settle_row<T, D>(x, xr, P, cent64, s_c, best, second, bi, cdelta, cmax, rescored);
         labels[P.row0 + r] = bi;
       }
     }
@@ -922,6 +936,8 @@ int kclass(int k) { return k <= 8 ? 0 : k <= 16 ? 1 : k <= 32 ? 2 : k <= 64 ? 3 
 const int kClassK[kNumKC] = {8, 16, 32, 64, 128};
 const int kClassD[kNumD] = {8, 16, 32, 64};
 
+int g_variant_override = -1;  // sc_debug_batch_variant
+
 void tune_choice(int D, int k, int *cu, int *rows) {
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   if (g_tune.ready) {
@@ -931,6 +947,7 @@ void tune_choice(int D, int k, int *cu, int *rows) {
     *cu = 4;
     *rows = 2048;
   }
+  if (g_variant_override >= 0) *cu = g_variant_override;
 }
 
 int ceil_log2i(int64_t v) {
@@ -1010,6 +1027,12 @@ struct PhaseTrace {
   }
 };
 
+// Dynamic shared memory of the assignment kernel for problem P: centroids
+// (f32 and ||c||^2), 64-bit sums and counts.
+size_t assign_smem(const BProb &P) {
+  return (size_t)((P.k + 7) & ~7) * (P.D + 1) * 4 + (size_t)P.k * P.d * 8 + (size_t)P.k * 4 + 64;
+}
+
 // Work items of problem q with the given rows per item and variant.
 void add_items(std::vector<BItem> &items, int q, int n, int rows, int cu) {
   for (int r0 = 0; r0 < n; r0 += rows) items.push_back(BItem{q, r0, std::min(n, r0 + rows), cu});
@@ -1058,11 +1081,10 @@ void plan_batch(Batch &B, const std::vector<int64_t> &n, const std::vector<int64
     B.order[q] = caller_index[i];
     B.kmax = std::max(B.kmax, P.k);
     B.max_iter = std::max(B.max_iter, P.max_iter);
-    const size_t sm = (size_t)((P.k + 7) & ~7) * (P.D + 1) * 4 + (size_t)P.k * P.d * 8 + (size_t)P.k * 4 + 64;
-    B.smem_d[dclass(P.D)] = std::max(B.smem_d[dclass(P.D)], sm);
     int cu, rows;
     tune_choice(P.D, P.k, &cu, &rows);
     P.rows = rows;
+    B.smem_d[dclass(P.D)] = std::max(B.smem_d[dclass(P.D)], assign_smem(P));
   }
   // work items grouped by width, largest cost (rows x k) first in each group
   std::vector<BItem> groups[kNumD];
@@ -1507,18 +1529,36 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
       break;
     }
     const int32_t *lab = (const int32_t *)stage;
-    for (int q = 0; q < B.count; ++q) {
-      sc_kmeans_problem &pr = problems[B.order[q]];
-      const BProb &P = B.probs[q];
-      if (pr.centroids_out) memcpy(pr.centroids_out, cent.data() + P.c_off, (size_t)P.k * P.d * sizeof(double));
-      if (pr.sizes_out) memcpy(pr.sizes_out, sizes.data() + P.k_off, (size_t)P.k * sizeof(int64_t));
-      if (pr.labels_out)
-        for (int64_t i = 0; i < P.n; ++i) pr.labels_out[i] = lab[P.row0 + i];
-      if (pr.distortion_out) *pr.distortion_out = st[q].distortion;
-      if (pr.iters_out) *pr.iters_out = st[q].iters;
-      pr.rescored = st[q].rescored;
-      pr.pp_replays = st[q].pp_replays;
+    // into the callers' buffers: problems split over host threads by row
+    // count (the labels widen to 64 bits on the way)
+    auto fill = [&](int q0, int q1) {
+      for (int q = q0; q < q1; ++q) {
+        sc_kmeans_problem &pr = problems[B.order[q]];
+        const BProb &P = B.probs[q];
+        if (pr.centroids_out) memcpy(pr.centroids_out, cent.data() + P.c_off, (size_t)P.k * P.d * sizeof(double));
+        if (pr.sizes_out) memcpy(pr.sizes_out, sizes.data() + P.k_off, (size_t)P.k * sizeof(int64_t));
+        if (pr.labels_out)
+          for (int64_t i = 0; i < P.n; ++i) pr.labels_out[i] = lab[P.row0 + i];
+        if (pr.distortion_out) *pr.distortion_out = st[q].distortion;
+        if (pr.iters_out) *pr.iters_out = st[q].iters;
+        pr.rescored = st[q].rescored;
+        pr.pp_replays = st[q].pp_replays;
+      }
+    };
+    const int nth = (int)std::min<int64_t>({(int64_t)std::max(1u, std::thread::hardware_concurrency()), 16,
+                                            (int64_t)B.count, B.rows / 65536 + 1});
+    std::vector<int> cut(nth + 1, B.count);  // thread t: problems [cut[t], cut[t + 1])
+    cut[0] = 0;
+    for (int q = 0, t = 1; q < B.count && t < nth; ++q)
+      if (B.probs[q].row0 + B.probs[q].n >= B.rows * t / nth) cut[t++] = q + 1;
+    std::vector<std::thread> pool;
+    try {
+      for (int t = 1; t < nth; ++t) pool.emplace_back(fill, cut[t], cut[t + 1]);
+    } catch (...) {  // no threads: the rest on this one
+      fill(cut[pool.size() + 1], B.count);
     }
+    fill(cut[0], cut[1]);
+    for (auto &th : pool) th.join();
     trace.mark("results", nullptr);
   } while (0);
   free_batch(B);
@@ -1539,7 +1579,7 @@ static std::string device_tag() {
   return buf;
 }
 
-static const char *kTuneHeader = "smartcore_gb300 batched-assignment tuning v1";
+static const char *kTuneHeader = "smartcore_gb300 batched-assignment tuning v2";  // v2: timed over repeated items
 
 sc_status sc_batch_tune(const char *path) {
   const std::string tag = device_tag();
@@ -1561,8 +1601,11 @@ sc_status sc_batch_tune(const char *path) {
     B.first.push_back((int64_t)q * 977 % kTuneRows);
     for (int a = 0; a + 1 < B.probs[q].k; ++a) B.uniforms.push_back((double)((a * 7919 + q * 104729) % 1000) / 1000.0);
   }
-  // room for the items of the smallest rows-per-item option
-  size_t item_cap = (size_t)kTuneRows / kRowsOpts[0] + 1;
+  // Each timed launch runs the problem's items kTuneRepeat times over, so that
+  // every persistent CTA has work, as in a full batch (the sums of the
+  // repeats only grow the 128-bit totals; the labels are rewritten alike).
+  constexpr int kTuneRepeat = 16;
+  size_t item_cap = ((size_t)kTuneRows / kRowsOpts[0] + 1) * kTuneRepeat;
   if (cudaStreamCreateWithFlags(&B.s, cudaStreamNonBlocking) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaStreamCreate");
   Tune T;
   sc_status r = SC_OK;
@@ -1589,7 +1632,7 @@ sc_status sc_batch_tune(const char *path) {
       for (int ci = 0; ci < kNumCU && r == SC_OK; ++ci)
         for (int ri = 0; ri < kNumRows && r == SC_OK; ++ri) {
           std::vector<BItem> items;
-          add_items(items, q, B.probs[q].n, kRowsOpts[ri], kCUs[ci]);
+          for (int rp = 0; rp < kTuneRepeat; ++rp) add_items(items, q, B.probs[q].n, kRowsOpts[ri], kCUs[ci]);
           std::vector<BProb> probs = B.probs;
           const int sc = 62 - 3 - ceil_log2i(kRowsOpts[ri] + 1);  // |x| < 2^3 here
           probs[q].scale = sc;
@@ -1675,6 +1718,15 @@ sc_status sc_batch_tune_load(const char *path) {
   T.ready = true;
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   g_tune = T;
+  return SC_OK;
+}
+
+sc_status sc_debug_batch_variant(int32_t variant) {
+  bool ok = variant < 0;
+  for (int i = 0; i < kNumCU; ++i) ok |= kCUs[i] == variant;
+  if (!ok) { set_error("unknown batched assignment variant %d", variant); return SC_ERR_INVALID; }
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_variant_override = variant < 0 ? -1 : variant;
   return SC_OK;
 }
 

@@ -101,15 +101,46 @@ def edge_problems(dtype):
     return out
 
 
+@pytest.fixture
+def force_variant():
+    L = _lib.load()
+    yield lambda v: _lib.check(L.sc_debug_batch_variant(v))
+    L.sc_debug_batch_variant(-1)
+
+
+@pytest.mark.parametrize("variant", [-1, 2], ids=["tuned", "cu2"])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
-def test_edge_problems_match_oracle(dtype):
+def test_edge_problems_match_oracle(dtype, variant, force_variant):
     probs = edge_problems(dtype)
+    force_variant(variant)
     fits = KMeans.fit_many(probs)
     for i, ((x, p), km) in enumerate(zip(probs, fits)):
         r = oracle.kmeans_fit(x, p.k, p.max_iter, seed=p.seed)
         duplicated = i == 9
         check_against_oracle(x, km, r.labels, r.sizes, r.centroids, r.iters, r.distortion,
                              iters_slack=1 if duplicated else 0)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_assignment_variants_agree(dtype, force_variant):
+    """The assignment variants (2, 4 or 8 centroids per inner pass) score every
+    (row, centroid) pair in the same order, so whole fits agree bit for bit:
+    labels, sizes, iterations, centroids, distortion and re-scored rows, for
+    every width class and k up to 128."""
+    probs = batched_problems(count=80, seed0=300, n_range=(300, 20_000))
+    probs += batched_problems(count=16, seed0=400, n_range=(300, 20_000), ds=(3, 13, 50, 64), k_range=(65, 128))
+    par = [(x.astype(dtype), KMeansParameters(k=k, max_iter=12, seed=s)) for x, k, s in probs]
+    out = {}
+    for v in (2, 4, 8):
+        force_variant(v)
+        stats = []
+        out[v] = (KMeans.fit_many(par, stats=stats), stats)
+    for v in (4, 8):
+        for a, b in zip(out[2][0], out[v][0]):
+            assert np.array_equal(a._y, b._y) and np.array_equal(a.size, b.size) and a.iters == b.iters
+            assert np.array_equal(a.centroids, b.centroids, equal_nan=True)
+            assert a._distortion == b._distortion
+        assert out[2][1] == out[v][1]
 
 
 def test_validation_writes_nothing():
