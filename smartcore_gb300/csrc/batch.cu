@@ -803,7 +803,7 @@ batch_pp_update32_kernel(const int32_t *__restrict__ cls_blocks, const int32_t *
       // s32 (1 - 1.05 d 2^-24): above the current distance, the row keeps it
       if (first || !(__fmul_rd(s32, 1.f - 1.05f * d * 0x1p-24f) > c32)) {
         double s = 0.0;
-        if (!sqd_seq_terms<D>(x, d, P.lg_d, s)) {
+        if (!sqd_terms<D>(x, d, P.lg_d, s)) {
           s = 0.0;
 #pragma unroll
           for (int t = 0; t < D; ++t)

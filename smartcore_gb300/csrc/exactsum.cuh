@@ -305,12 +305,16 @@ __device__ __forceinline__ bool sqd_seq_terms(const float (&q)[D], int d, int lg
   return true;
 }
 
-// Register terms of d <= 32 features (zero past d), branch-free where no
+// Register terms of d <= D features (zero past d), branch-free where no
 // running sum can round (the span test of sqd_f32_d32), else sqd_seq_terms.
-__device__ __forceinline__ bool sqd_terms32(const float (&q)[32], int d, int lg_d, double &out) {
+// Four 32-bit accumulator pairs: each takes D / 4 <= 16 terms of < 2^24, so
+// none can overflow.
+template <int D>
+__device__ __forceinline__ bool sqd_terms(const float (&q)[D], int d, int lg_d, double &out) {
+  static_assert(D % 4 == 0 && D <= 64, "four accumulators of at most 16 terms");
   uint32_t emn0 = 256u, emn1 = 256u, emx0 = 0u, emx1 = 0u;
 #pragma unroll
-  for (int t = 0; t < 32; t += 2) {
+  for (int t = 0; t < D; t += 2) {
     const uint32_t u0 = __float_as_uint(q[t]), u1 = __float_as_uint(q[t + 1]);
     const uint32_t e0 = max(u0 >> 23, 1u), e1 = max(u1 >> 23, 1u);
     emn0 = min(emn0, u0 ? e0 : 256u);
@@ -320,10 +324,10 @@ __device__ __forceinline__ bool sqd_terms32(const float (&q)[32], int d, int lg_
   }
   const uint32_t emn = min(emn0, emn1), emx = max(emx0, emx1);
   if (emn == 256u) { out = 0.0; return true; }
-  if (emx >= 255u || emx - emn > 24u || (int)(emx - emn) > 29 - lg_d) return sqd_seq_terms<32>(q, d, lg_d, out);
+  if (emx >= 255u || emx - emn > 24u || (int)(emx - emn) > 29 - lg_d) return sqd_seq_terms<D>(q, d, lg_d, out);
   uint32_t lo[4] = {0u, 0u, 0u, 0u}, hi[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-  for (int t = 0; t < 32; ++t) {
+  for (int t = 0; t < D; ++t) {
     const uint32_t u = __float_as_uint(q[t]);
     const uint32_t e = u >> 23;
     const uint32_t m = u ? (u & 0x7fffffu) | (e ? 0x800000u : 0u) : 0u;
@@ -335,6 +339,10 @@ __device__ __forceinline__ bool sqd_terms32(const float (&q)[32], int d, int lg_
                                (unsigned long long)(lo[0] + lo[1] + lo[2] + lo[3]);
   out = sqd_from_units(S, emn);
   return true;
+}
+
+__device__ __forceinline__ bool sqd_terms32(const float (&q)[32], int d, int lg_d, double &out) {
+  return sqd_terms<32>(q, d, lg_d, out);
 }
 
 }  // namespace sc
