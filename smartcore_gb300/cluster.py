@@ -63,6 +63,17 @@ def kmeanspp_draws(n, k, seed=None, rng=_lib.RNG_SMALL):
     return int(first[0]), u[: max(k - 1, 0)]
 
 
+# sc_kmeans_problem of include/smartcore_gb300.h as a NumPy record (the same
+# layout as _lib.KMeansProblem), so that a batch's fields fill as columns
+PROBLEM_DTYPE = np.dtype([("x", np.uint64), ("layout", np.int32), ("status", np.int32), ("n", np.int64),
+                          ("d", np.int64), ("ld", np.int64), ("k", np.int64), ("max_iter", np.int64),
+                          ("first_index", np.int64), ("uniforms", np.uint64), ("centroids_out", np.uint64),
+                          ("sizes_out", np.uint64), ("labels_out", np.uint64), ("distortion_out", np.uint64),
+                          ("iters_out", np.uint64), ("rescored", np.int64), ("pp_replays", np.int64)])
+assert PROBLEM_DTYPE.itemsize == C.sizeof(_lib.KMeansProblem)
+assert all(PROBLEM_DTYPE.fields[n][1] == getattr(_lib.KMeansProblem, n).offset for n in PROBLEM_DTYPE.names)
+
+
 class KMeans:
     """Fitted model: k, size, _y, _distortion, centroids (kmeans.rs:73-83)."""
 
@@ -115,36 +126,52 @@ class KMeans:
         if len(dts) != 1:
             raise ValueError("every problem of one call must have the same element type")
         dt = _lib.F32 if mats[0].dtype == np.float32 else _lib.F64
-        arr = (_lib.KMeansProblem * len(problems))()
-        keep = []
-        outs = []
-        for i, ((_, p), a) in enumerate(zip(problems, mats)):
-            p = p or KMeansParameters()
-            n, d = a.shape
+        pars = [p or KMeansParameters() for _, p in problems]
+        for p in pars:
             if p.k < 2:
                 raise Failed(FailedError.FitFailed, f"invalid number of clusters: {p.k}")
             if p.max_iter == 0:
                 raise Failed(FailedError.FitFailed, f"invalid maximum number of iterations: {p.max_iter}")
-            first, u = kmeanspp_draws(n, p.k, p.seed, p.rng)
-            uu = np.ascontiguousarray(u, np.float64) if len(u) else np.zeros(1)
-            lay, ld = layout_of(a)
-            cent = np.zeros((p.k, d), np.float64)
-            sizes = np.zeros(p.k, np.int64)
-            labels = np.zeros(n, np.int64)
-            dist = np.zeros(1, np.float64)
-            iters = np.zeros(1, np.int64)
-            keep += [a, uu]
-            outs.append((p, cent, sizes, labels, dist, iters))
-            q = arr[i]
-            q.x, q.layout, q.n, q.d, q.ld = a.ctypes.data, lay, n, d, ld
-            q.k, q.max_iter, q.first_index, q.uniforms = p.k, p.max_iter, first, uu.ctypes.data
-            q.centroids_out, q.sizes_out, q.labels_out = cent.ctypes.data, sizes.ctypes.data, labels.ctypes.data
-            q.distortion_out, q.iters_out = dist.ctypes.data, iters.ctypes.data
-        _lib.check(L.sc_kmeans_fit_batched(C.cast(arr, C.c_void_p), len(problems), dt, form))
+        m = len(problems)
+        ns = np.array([a.shape[0] for a in mats], np.int64)
+        ds = np.array([a.shape[1] for a in mats], np.int64)
+        ks = np.array([p.k for p in pars], np.int64)
+        # every output in one array per kind; each problem gets its slice
+        n_off = np.concatenate(([0], np.cumsum(ns)))
+        c_off = np.concatenate(([0], np.cumsum(ks * ds)))
+        k_off = np.concatenate(([0], np.cumsum(ks)))
+        u_off = np.concatenate(([0], np.cumsum(np.maximum(ks - 1, 1))))
+        labels = np.empty(int(n_off[-1]), np.int64)
+        cent = np.empty(int(c_off[-1]), np.float64)
+        sizes = np.empty(int(k_off[-1]), np.int64)
+        dist = np.empty(m, np.float64)
+        iters = np.empty(m, np.int64)
+        first = np.empty(m, np.int64)
+        uu = np.empty(int(u_off[-1]), np.float64)
+        fb, ub = first.ctypes.data, uu.ctypes.data
+        for i, (p, a) in enumerate(zip(pars, mats)):  # k-means++ draws of each problem (kmeanspp_draws)
+            _lib.check(L.sc_kmeanspp_draws(p.rng, 0 if p.seed is None else p.seed, int(ns[i]), p.k, fb + 8 * i,
+                                           ub + 8 * int(u_off[i])))
+        arr = np.zeros(m, PROBLEM_DTYPE)
+        lay = [layout_of(a) for a in mats]
+        arr["x"] = [a.ctypes.data for a in mats]
+        arr["layout"] = [l for l, _ in lay]
+        arr["ld"] = [ld for _, ld in lay]
+        arr["n"], arr["d"], arr["k"] = ns, ds, ks
+        arr["max_iter"] = [p.max_iter for p in pars]
+        arr["first_index"] = first
+        arr["uniforms"] = ub + 8 * u_off[:-1]
+        arr["centroids_out"] = cent.ctypes.data + 8 * c_off[:-1]
+        arr["sizes_out"] = sizes.ctypes.data + 8 * k_off[:-1]
+        arr["labels_out"] = labels.ctypes.data + 8 * n_off[:-1]
+        arr["distortion_out"] = dist.ctypes.data + 8 * np.arange(m)
+        arr["iters_out"] = iters.ctypes.data + 8 * np.arange(m)
+        _lib.check(L.sc_kmeans_fit_batched(arr.ctypes.data, m, dt, form))
         if stats is not None:
-            stats.extend((int(arr[i].rescored), int(arr[i].pp_replays)) for i in range(len(problems)))
-        return [KMeans(p.k, labels, sizes, float(dist[0]), cent, int(iters[0]), form)
-                for p, cent, sizes, labels, dist, iters in outs]
+            stats.extend(zip(arr["rescored"].tolist(), arr["pp_replays"].tolist()))
+        return [KMeans(p.k, labels[n_off[i]:n_off[i + 1]], sizes[k_off[i]:k_off[i + 1]], float(dist[i]),
+                       cent[c_off[i]:c_off[i + 1]].reshape(p.k, -1), int(iters[i]), form)
+                for i, p in enumerate(pars)]
 
     def predict(self, x) -> np.ndarray:
         a = as_matrix(x)
