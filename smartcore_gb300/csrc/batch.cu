@@ -756,14 +756,78 @@ batch_pp_update_kernel(const int32_t *__restrict__ block_prob, const BProb *__re
   if (threadIdx.x == 0) part[b] = tot;
 }
 
-// The same update for f32 rows of padded width D: the row comes into
-// registers with 16-byte loads only when the far test leaves it, its terms
-// fl32((x_t - c_t)^2) give the f32 lower bound and, when needed, the exact
-// value by the integer reproduction of the sequential f64 sum.  One CTA per
-// 256-row block of the width's problems with k >= j (cls_blocks lists them,
-// largest k first).
+// The reference's f64 sequential sum of the terms fl32((x_t - c_t)^2) of an
+// f32 row (zero past d, padded width D, 16-byte aligned) against the seed
+// c in shared memory, given emin / emax of its nonzero terms, recomputing the
+// terms from the row (a second read, from cache) instead of holding them:
+// the integer sum where no running sum can round, else the sequential
+// reproduction (both as sqd_terms), else the f64 additions themselves.
 template <int D>
-__global__ void __launch_bounds__(kBlk, AsgOcc<D>::value)
+__device__ __noinline__ double pp_exact_row(const float *__restrict__ xr, const float *s_seed, int d, int lg_d,
+                                            uint32_t emn, uint32_t emx) {
+  if (emn == 256u) return 0.0;
+  const float4 *x4 = reinterpret_cast<const float4 *>(xr);
+  if (emx < 255u && emx - emn <= 24u && (int)(emx - emn) <= 29 - lg_d) {
+    uint32_t lo[4] = {0u, 0u, 0u, 0u}, hi[4] = {0u, 0u, 0u, 0u};
+#pragma unroll 4
+    for (int q = 0; q < D / 4; ++q) {
+      const float4 v = x4[q];
+      const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float r = __fsub_rn(vv[c], s_seed[4 * q + c]);
+        const uint32_t u = __float_as_uint(__fmul_rn(r, r));
+        const uint32_t e = u >> 23;
+        const uint32_t m = u ? (u & 0x7fffffu) | (e ? 0x800000u : 0u) : 0u;
+        const uint32_t sh = max(e, 1u) - emn;  // <= 24 for every nonzero term (0 terms add nothing)
+        lo[c] += (m << (sh & 31u)) & 0xffffffu;
+        hi[c] += sh ? m >> (24u - sh) : 0u;
+      }
+    }
+    const unsigned long long S = ((unsigned long long)(hi[0] + hi[1] + hi[2] + hi[3]) << 24) +
+                                 (unsigned long long)(lo[0] + lo[1] + lo[2] + lo[3]);
+    return sqd_from_units(S, emn);
+  }
+  if (emx < 255u && (int)(emx - emn) <= 38 - lg_d) {
+    unsigned long long S = 0;
+    for (int t = 0; t < d; ++t) {
+      const float r = __fsub_rn(xr[t], s_seed[t]);
+      const uint32_t u = __float_as_uint(__fmul_rn(r, r));
+      if (u != 0u) {
+        const int e = (int)(u >> 23);
+        const uint32_t m = (u & 0x7fffffu) | (e ? 0x800000u : 0u);
+        S += (unsigned long long)m << (max(e, 1) - (int)emn);  // stays below 2^63
+        if (S >> 53) {  // more than 53 significant bits: round as the f64 addition does
+          const int drop = 11 - __clzll((long long)S);
+          const unsigned long long half = 1ull << (drop - 1), rem = S & ((half << 1) - 1ull);
+          unsigned long long qv = S >> drop;
+          if (rem > half || (rem == half && (qv & 1ull))) ++qv;
+          S = qv << drop;
+        }
+      }
+    }
+    const int pbit = 63 - __clzll((long long)S);
+    const unsigned long long mant = pbit <= 52 ? S << (52 - pbit) : S >> (pbit - 52);
+    const int ex = pbit + (int)emn - 150 + 1023;
+    return __longlong_as_double((long long)(((unsigned long long)ex << 52) | (mant & 0xfffffffffffffull)));
+  }
+  double s = 0.0;
+  for (int t = 0; t < d; ++t) {
+    const float r = __fsub_rn(xr[t], s_seed[t]);
+    s = __dadd_rn(s, (double)__fmul_rn(r, r));
+  }
+  return s;
+}
+
+// The same update for f32 rows of padded width D: the row is read with
+// 16-byte loads only when the far test leaves it, and streamed: its terms
+// fl32((x_t - c_t)^2) give the f32 lower bound and the exponent range of the
+// terms, and only when the bound cannot settle the row is it read again for
+// the exact value (pp_exact_row).  Holding no row in registers leaves room
+// for four CTAs per SM.  One CTA per 256-row block of the width's problems
+// with k >= j (cls_blocks lists them, largest k first).
+template <int D>
+__global__ void __launch_bounds__(kBlk, 4)
 batch_pp_update32_kernel(const int32_t *__restrict__ cls_blocks, const int32_t *__restrict__ block_prob,
                          const BProb *__restrict__ probs, const BState *__restrict__ st,
                          const float *__restrict__ X, double *__restrict__ dd, float *__restrict__ dd32,
@@ -787,28 +851,28 @@ batch_pp_update32_kernel(const int32_t *__restrict__ cls_blocks, const int32_t *
     const int d = P.d;
     const float c32 = first ? 0.f : dd32[gi];
     if (first || !pp_far32(seed_cc[P.k_off + lab], c32, far)) {
-      float x[D];
-      load_row<float, D>(X + P.x_off + il * D, x);
-      // the row's terms fl32((x_t - c_t)^2) overwrite the row (no second array)
-#pragma unroll
-      for (int t = 0; t < D; ++t) {
-        const float r = __fsub_rn(x[t], s_seed[t]);
-        x[t] = __fmul_rn(r, r);
-      }
+      const float *xr = X + P.x_off + il * D;
+      const float4 *x4 = reinterpret_cast<const float4 *>(xr);
       float s32 = 0.f;
+      uint32_t emn = 256u, emx = 0u;
+#pragma unroll 4
+      for (int q = 0; q < D / 4; ++q) {
+        const float4 v = __ldg(x4 + q);
+        const float vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-      for (int t = 0; t < D; ++t)
-        if (t < d) s32 = __fadd_rn(s32, x[t]);
+        for (int c = 0; c < 4; ++c) {
+          const float r = __fsub_rn(vv[c], s_seed[4 * q + c]);
+          const float tv = __fmul_rn(r, r);
+          if (4 * q + c < d) s32 = __fadd_rn(s32, tv);
+          const uint32_t u = __float_as_uint(tv), e = max(u >> 23, 1u);
+          emn = min(emn, u ? e : 256u);
+          emx = max(emx, u ? e : 0u);
+        }
+      }
       // the terms summed in f32 bound the reference's f64 sum from below by
       // s32 (1 - 1.05 d 2^-24): above the current distance, the row keeps it
       if (first || !(__fmul_rd(s32, 1.f - 1.05f * d * 0x1p-24f) > c32)) {
-        double s = 0.0;
-        if (!sqd_terms<D>(x, d, P.lg_d, s)) {
-          s = 0.0;
-#pragma unroll
-          for (int t = 0; t < D; ++t)
-            if (t < d) s = __dadd_rn(s, (double)x[t]);
-        }
+        const double s = pp_exact_row<D>(xr, s_seed, d, P.lg_d, emn, emx);
         if (s < cur) {
           cur = s;
           lab = j - 1;
