@@ -1055,6 +1055,7 @@ struct Batch {
   bool needs_pad = false;
   // device
   cudaStream_t s = nullptr;
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};  // the Lloyd graph's parallel assignment branches
   void *mem = nullptr;
   void *X = nullptr, *seed_x = nullptr;
   int32_t *labels = nullptr, *d_block_prob = nullptr;
@@ -1231,10 +1232,11 @@ sc_status upload_tables(Batch &B) {
 }
 
 template <typename T, int D>
-sc_status launch_assign_d(Batch &B, int dc, unsigned *head, int nitems, const BItem *items, int mode) {
+sc_status launch_assign_d(Batch &B, int dc, unsigned *head, int nitems, const BItem *items, int mode,
+                          cudaStream_t st = nullptr) {
   if (nitems == 0) return SC_OK;
   // shared-memory attribute set by assign_grid
-  batch_assign_kernel<T, D><<<B.grid_d[dc], kAsgThreads, B.smem_d[dc], B.s>>>(
+  batch_assign_kernel<T, D><<<B.grid_d[dc], kAsgThreads, B.smem_d[dc], st ? st : B.s>>>(
       items, nitems, B.d_probs, B.st, (const T *)B.X, B.cent32, B.cent64, B.labels, B.acc, B.cnt, head, B.active,
       mode);
   SC_LAUNCHED();
@@ -1242,15 +1244,30 @@ sc_status launch_assign_d(Batch &B, int dc, unsigned *head, int nitems, const BI
 }
 
 // One assignment pass over the item groups of every width; heads[dc] is the
-// queue head of width dc (cleared beforehand).
+// queue head of width dc (cleared beforehand).  With fork / join events the
+// four widths run on B.s and the three side streams at once, widest first,
+// so that each launch's tail overlaps the next one's work.
 template <typename T>
-sc_status launch_assign(Batch &B, unsigned *heads, int mode) {
+sc_status launch_assign(Batch &B, unsigned *heads, int mode, cudaEvent_t *ev = nullptr) {
   const BItem *it = B.d_items;
   const int *o = B.item_off;
-  SC_TRY((launch_assign_d<T, 8>(B, 0, heads + 0, o[1] - o[0], it + o[0], mode)));
-  SC_TRY((launch_assign_d<T, 16>(B, 1, heads + 1, o[2] - o[1], it + o[1], mode)));
-  SC_TRY((launch_assign_d<T, 32>(B, 2, heads + 2, o[3] - o[2], it + o[2], mode)));
-  SC_TRY((launch_assign_d<T, 64>(B, 3, heads + 3, o[4] - o[3], it + o[3], mode)));
+  cudaStream_t s3 = B.s, s2 = B.s, s1 = B.s, s0 = B.s;
+  if (ev) {
+    SC_CUDA(cudaEventRecord(ev[0], B.s));
+    for (int i = 0; i < 3; ++i) SC_CUDA(cudaStreamWaitEvent(B.side[i], ev[0], 0));
+    s2 = B.side[0];
+    s1 = B.side[1];
+    s0 = B.side[2];
+  }
+  SC_TRY((launch_assign_d<T, 64>(B, 3, heads + 3, o[4] - o[3], it + o[3], mode, s3)));
+  SC_TRY((launch_assign_d<T, 32>(B, 2, heads + 2, o[3] - o[2], it + o[2], mode, s2)));
+  SC_TRY((launch_assign_d<T, 16>(B, 1, heads + 1, o[2] - o[1], it + o[1], mode, s1)));
+  SC_TRY((launch_assign_d<T, 8>(B, 0, heads + 0, o[1] - o[0], it + o[0], mode, s0)));
+  if (ev)
+    for (int i = 0; i < 3; ++i) {
+      SC_CUDA(cudaEventRecord(ev[1 + i], B.side[i]));
+      SC_CUDA(cudaStreamWaitEvent(B.s, ev[1 + i], 0));
+    }
   return SC_OK;
 }
 
@@ -1405,12 +1422,23 @@ sc_status run_lloyd(Batch &B) {
   const int G = std::min(B.max_iter, kGraphIters);
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  SC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int i = 0; i < 3; ++i)
+    if (!B.side[i]) SC_CUDA(cudaStreamCreateWithFlags(&B.side[i], cudaStreamNonBlocking));
+  for (int i = 0; i < 4; ++i) {
+    const cudaError_t e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      for (int q = 0; q < i; ++q) cudaEventDestroy(ev[q]);
+      return cuda_fail(e, "cudaEventCreate");
+    }
+  }
   sc_status r = SC_OK;
-  if (cudaMemsetAsync(B.heads, 0, (size_t)G * kNumD * sizeof(unsigned), s) != cudaSuccess)
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    r = cuda_fail(cudaGetLastError(), "cudaStreamBeginCapture");
+  if (r == SC_OK && cudaMemsetAsync(B.heads, 0, (size_t)G * kNumD * sizeof(unsigned), s) != cudaSuccess)
     r = cuda_fail(cudaGetLastError(), "memset");
   for (int t = 0; t < G && r == SC_OK; ++t) {
-    r = launch_assign<T>(B, B.heads + (size_t)t * kNumD, 0);
+    r = launch_assign<T>(B, B.heads + (size_t)t * kNumD, 0, ev);
     if (r != SC_OK) break;
     batch_finalize_kernel<<<B.count, kFinT, 0, s>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 0,
                                                     B.active);
@@ -1418,8 +1446,12 @@ sc_status run_lloyd(Batch &B) {
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) r = cuda_fail(le, "batch_finalize_kernel");
   }
-  const cudaError_t ec = cudaStreamEndCapture(s, &graph);
-  if (r == SC_OK && ec != cudaSuccess) r = cuda_fail(ec, "cudaStreamEndCapture");
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+    const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+    if (r == SC_OK && ec != cudaSuccess) r = cuda_fail(ec, "cudaStreamEndCapture");
+  }
+  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
   if (r == SC_OK) {
     const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
     if (e != cudaSuccess) r = cuda_fail(e, "cudaGraphInstantiate");
@@ -1439,6 +1471,12 @@ sc_status run_lloyd(Batch &B) {
 void free_batch(Batch &B) {
   if (B.mem) dev_free(B.mem, B.s);
   B.mem = nullptr;
+  for (int i = 0; i < 3; ++i)
+    if (B.side[i]) {
+      cudaStreamSynchronize(B.side[i]);
+      cudaStreamDestroy(B.side[i]);
+      B.side[i] = nullptr;
+    }
   if (B.s) {
     cudaStreamSynchronize(B.s);
     cudaStreamDestroy(B.s);
