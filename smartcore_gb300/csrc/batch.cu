@@ -1309,6 +1309,26 @@ sc_status assign_grid(Batch &B, int dtype) {
   return dtype == SC_F32 ? assign_grid_t<float>(B, sms) : assign_grid_t<double>(B, sms);
 }
 
+// The side streams of a batch's parallel width-class launches.
+sc_status ensure_side_streams(Batch &B) {
+  for (int i = 0; i < 3; ++i)
+    if (!B.side[i]) SC_CUDA(cudaStreamCreateWithFlags(&B.side[i], cudaStreamNonBlocking));
+  return SC_OK;
+}
+
+// Fork / join events (no timing), destroyed with the set.
+struct EventSet {
+  cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+  sc_status create() {
+    for (int i = 0; i < 4; ++i) SC_CUDA(cudaEventCreateWithFlags(&e[i], cudaEventDisableTiming));
+    return SC_OK;
+  }
+  ~EventSet() {
+    for (int i = 0; i < 4; ++i)
+      if (e[i]) cudaEventDestroy(e[i]);
+  }
+};
+
 // Device phases of a batch: scan, scales, k-means++, initial means.
 template <typename T>
 sc_status run_setup(Batch &B) {
@@ -1366,11 +1386,18 @@ sc_status run_setup(Batch &B) {
     cls_nb[dc] = B.cls_off[dc + 1] - B.cls_off[dc];
   }
   const PPFar32 far = pp_far_bound32(kMaxBD);  // d = 64 bounds the far test of every width
+  // each draw's width classes run at once (B.s and the side streams, widest
+  // first), joined before the selection
+  SC_TRY(ensure_side_streams(B));
+  EventSet ev;
+  SC_TRY(ev.create());
   for (int j = 1; j <= B.kmax; ++j) {
     while (q_ge > 0 && B.probs[q_ge - 1].k < j) --q_ge;
     while (q_gt > 0 && B.probs[q_gt - 1].k <= j) --q_gt;
     if constexpr (sizeof(T) == 4) {
-      for (int dc = 0; dc < kNumD; ++dc) {
+      SC_CUDA(cudaEventRecord(ev.e[0], s));
+      for (int i = 0; i < 3; ++i) SC_CUDA(cudaStreamWaitEvent(B.side[i], ev.e[0], 0));
+      for (int dc = kNumD - 1; dc >= 0; --dc) {
         while (cls_ge[dc] > 0 && B.probs[cls_probs[dc][cls_ge[dc] - 1]].k < j) {
           --cls_ge[dc];
           cls_nb[dc] -= B.probs[cls_probs[dc][cls_ge[dc]]].nb;
@@ -1378,13 +1405,18 @@ sc_status run_setup(Batch &B) {
         if (cls_nb[dc] == 0) continue;
         const int32_t *cb = B.d_cls_blocks + B.cls_off[dc];
         const float *xf = (const float *)B.X;
+        cudaStream_t st = dc == kNumD - 1 ? s : B.side[kNumD - 2 - dc];
         switch (dc) {
-          case 0: batch_pp_update32_kernel<8><<<cls_nb[dc], kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
-          case 1: batch_pp_update32_kernel<16><<<cls_nb[dc], kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
-          case 2: batch_pp_update32_kernel<32><<<cls_nb[dc], kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
-          default: batch_pp_update32_kernel<64><<<cls_nb[dc], kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+          case 0: batch_pp_update32_kernel<8><<<cls_nb[dc], kBlk, 0, st>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+          case 1: batch_pp_update32_kernel<16><<<cls_nb[dc], kBlk, 0, st>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+          case 2: batch_pp_update32_kernel<32><<<cls_nb[dc], kBlk, 0, st>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+          default: batch_pp_update32_kernel<64><<<cls_nb[dc], kBlk, 0, st>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
         }
         SC_LAUNCHED();
+      }
+      for (int i = 0; i < 3; ++i) {
+        SC_CUDA(cudaEventRecord(ev.e[1 + i], B.side[i]));
+        SC_CUDA(cudaStreamWaitEvent(s, ev.e[1 + i], 0));
       }
     } else if (q_ge > 0) {
       batch_pp_update_kernel<T><<<blocks_upto[q_ge], kBlk, 0, s>>>(B.d_block_prob, B.d_probs, B.st, (const T *)B.X,
@@ -1422,16 +1454,10 @@ sc_status run_lloyd(Batch &B) {
   const int G = std::min(B.max_iter, kGraphIters);
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  for (int i = 0; i < 3; ++i)
-    if (!B.side[i]) SC_CUDA(cudaStreamCreateWithFlags(&B.side[i], cudaStreamNonBlocking));
-  for (int i = 0; i < 4; ++i) {
-    const cudaError_t e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
-    if (e != cudaSuccess) {
-      for (int q = 0; q < i; ++q) cudaEventDestroy(ev[q]);
-      return cuda_fail(e, "cudaEventCreate");
-    }
-  }
+  SC_TRY(ensure_side_streams(B));
+  EventSet evs;
+  SC_TRY(evs.create());
+  cudaEvent_t *ev = evs.e;
   sc_status r = SC_OK;
   if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     r = cuda_fail(cudaGetLastError(), "cudaStreamBeginCapture");
@@ -1451,7 +1477,6 @@ sc_status run_lloyd(Batch &B) {
     const cudaError_t ec = cudaStreamEndCapture(s, &graph);
     if (r == SC_OK && ec != cudaSuccess) r = cuda_fail(ec, "cudaStreamEndCapture");
   }
-  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
   if (r == SC_OK) {
     const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
     if (e != cudaSuccess) r = cuda_fail(e, "cudaGraphInstantiate");
