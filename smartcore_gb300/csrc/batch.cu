@@ -1309,6 +1309,30 @@ sc_status assign_grid(Batch &B, int dtype) {
   return dtype == SC_F32 ? assign_grid_t<float>(B, sms) : assign_grid_t<double>(B, sms);
 }
 
+// Rows the device can read where they are (pinned, mapped host memory):
+// copied by SM loads, 16 bytes each, every CTA striding over every job.
+struct CopyJob {
+  const uint4 *src;
+  uint4 *dst;
+  int64_t n16;
+};
+
+__global__ void __launch_bounds__(256) gather_host_rows_kernel(const CopyJob *__restrict__ jobs, int njobs) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int q = 0; q < njobs; ++q) {
+    const CopyJob jb = jobs[q];
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < jb.n16; i += 4 * stride) {  // four loads in flight
+      const uint4 a = jb.src[i], b = jb.src[i + stride], c = jb.src[i + 2 * stride], e = jb.src[i + 3 * stride];
+      jb.dst[i] = a;
+      jb.dst[i + stride] = b;
+      jb.dst[i + 2 * stride] = c;
+      jb.dst[i + 3 * stride] = e;
+    }
+    for (; i < jb.n16; i += stride) jb.dst[i] = jb.src[i];
+  }
+}
+
 // The side streams of a batch's parallel width-class launches.
 sc_status ensure_side_streams(Batch &B) {
   for (int i = 0; i < 3; ++i)
@@ -1596,6 +1620,7 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
     if (B.needs_pad && cudaMemsetAsync(B.X, 0, (size_t)B.xelems * es, B.s) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "memset"); break; }
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
+    std::vector<CopyJob> jobs;  // rows the device reads in place
     for (int q = 0; q < B.count && r == SC_OK; ++q) {
       const sc_kmeans_problem &pr = problems[B.order[q]];
       const BProb &P = B.probs[q];
@@ -1603,6 +1628,16 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
       const void *src = pr.x;
       size_t pitch = (size_t)pr.ld * es;
       cudaMemcpyKind kind = cudaMemcpyHostToDevice;
+      const size_t bytes = (size_t)P.n * P.d * es;
+      if (pr.layout == SC_ROW_MAJOR && P.D == P.d && pitch == (size_t)P.d * es && bytes % 16 == 0) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, pr.x) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer &&
+            ((uintptr_t)at.devicePointer & 15) == 0) {
+          jobs.push_back(CopyJob{(const uint4 *)at.devicePointer, (uint4 *)dst, (int64_t)(bytes / 16)});
+          continue;
+        }
+        cudaGetLastError();  // an unregistered pointer leaves an error behind on some drivers
+      }
       if (pr.layout == SC_COL_MAJOR) {
         // the columns as stored, then a transpose to rows on the device
         const size_t span = (size_t)((P.d - 1) * pr.ld + P.n) * es, span_al = (span + 255) & ~(size_t)255;
@@ -1629,6 +1664,24 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
       if (e != cudaSuccess) r = cuda_fail(e, "upload");
     }
     if (tmp) dev_free(tmp, B.s);
+    if (r == SC_OK && !jobs.empty()) {
+      CopyJob *d_jobs = nullptr;
+      if ((r = dev_alloc((void **)&d_jobs, jobs.size() * sizeof(CopyJob), B.s)) == SC_OK) {
+        int dev = 0, sms = 0;
+        if (cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(CopyJob), cudaMemcpyHostToDevice, B.s) !=
+                cudaSuccess ||
+            cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+          r = cuda_fail(cudaGetLastError(), "upload");
+        } else {
+          gather_host_rows_kernel<<<4 * sms, 256, 0, B.s>>>(d_jobs, (int)jobs.size());
+          note_launch();
+          const cudaError_t le = cudaGetLastError();
+          if (le != cudaSuccess) r = cuda_fail(le, "gather_host_rows_kernel");
+        }
+        dev_free(d_jobs, B.s);
+      }
+    }
     if (r != SC_OK) break;
     trace.mark("upload", B.s);
     r = dtype == SC_F32 ? run_setup<float>(B) : run_setup<double>(B);

@@ -143,6 +143,27 @@ def test_assignment_variants_agree(dtype, force_variant):
         assert out[2][1] == out[v][1]
 
 
+def test_pinned_host_rows():
+    """Rows in pinned host memory are read by the device in place (one gather
+    kernel for all of them); the fits equal those from pageable copies of the
+    same rows, in both element types, with misaligned and column-major
+    inputs in the same call taking the copy path."""
+    torch = pytest.importorskip("torch")
+    probs = batched_problems(count=24, seed0=500, n_range=(500, 20_000))
+    for dt in (np.float32, np.float64):
+        xs = [np.ascontiguousarray(x.astype(dt)) for x, _, _ in probs]
+        pinned = [torch.from_numpy(x).pin_memory().numpy() for x in xs]
+        # a pinned buffer offset by one element (not 16-byte aligned) and a column-major one
+        big = torch.from_numpy(np.concatenate([np.zeros(1, dt), xs[1].ravel()])).pin_memory().numpy()
+        pinned[1] = big[1:].reshape(xs[1].shape)
+        pinned[2] = np.asfortranarray(xs[2])
+        par_p = [(x, KMeansParameters(k=k, max_iter=15, seed=s)) for x, (_, k, s) in zip(pinned, probs)]
+        par_h = [(x, KMeansParameters(k=k, max_iter=15, seed=s)) for x, (_, k, s) in zip(xs, probs)]
+        for a, b in zip(KMeans.fit_many(par_p), KMeans.fit_many(par_h)):
+            assert np.array_equal(a._y, b._y) and np.array_equal(a.size, b.size) and a.iters == b.iters
+            assert np.array_equal(a.centroids, b.centroids, equal_nan=True)
+
+
 def test_validation_writes_nothing():
     x, _ = blobs(100, 4, 3, seed=1, dtype=np.float32)
     from smartcore_gb300.error import Failed
