@@ -363,27 +363,26 @@ __device__ __forceinline__ void assign_rows(const BItem &it, const BProb &P, BSt
           // the CU centroids' dot products in 2 CU independent FMA chains,
           // interleaved feature group by feature group (score32's order per
           // centroid, so the same roundings)
-          float a[CU], b[CU];
+          // (a, b) of a centroid as one pair: each paired FMA is the two
+          // chains' scalar FMAs, each rounded on its own
+          float2 ab[CU];
 #pragma unroll
-          for (int u = 0; u < CU; ++u) {
-            a[u] = 0.f;
-            b[u] = 0.f;
-          }
+          for (int u = 0; u < CU; ++u) ab[u] = make_float2(0.f, 0.f);
 #pragma unroll
           for (int j = 0; j < D; j += 4) {
             float4 cc[CU];
 #pragma unroll
             for (int u = 0; u < CU; ++u) cc[u] = *reinterpret_cast<const float4 *>(s_c + (c0 + u) * D + j);
+            const float2 x01 = make_float2(x[j], x[j + 1]), x23 = make_float2(x[j + 2], x[j + 3]);
 #pragma unroll
             for (int u = 0; u < CU; ++u) {
-              a[u] = __fmaf_rn(x[j], cc[u].x, a[u]);
-              b[u] = __fmaf_rn(x[j + 1], cc[u].y, b[u]);
-              a[u] = __fmaf_rn(x[j + 2], cc[u].z, a[u]);
-              b[u] = __fmaf_rn(x[j + 3], cc[u].w, b[u]);
+              ab[u] = __ffma2_rn(x01, make_float2(cc[u].x, cc[u].y), ab[u]);
+              ab[u] = __ffma2_rn(x23, make_float2(cc[u].z, cc[u].w), ab[u]);
             }
           }
+          float a[CU];
 #pragma unroll
-          for (int u = 0; u < CU; ++u) a[u] = __fmaf_rn(-2.f, __fadd_rn(a[u], b[u]), s_cn2[c0 + u]);
+          for (int u = 0; u < CU; ++u) a[u] = __fmaf_rn(-2.f, __fadd_rn(ab[u].x, ab[u].y), s_cn2[c0 + u]);
 #pragma unroll
           for (int u = 0; u < CU; ++u) {
             const float v = a[u];  // NaN (padding, empty clusters) never wins
