@@ -508,9 +508,9 @@ batch_assign_kernel(const BItem *__restrict__ items, int nitems, const BProb *__
 __global__ void __launch_bounds__(kFinT)
 batch_finalize_kernel(const BProb *__restrict__ probs, BState *st, Acc128 *__restrict__ acc,
                       unsigned long long *__restrict__ cnt, double *__restrict__ cent64, float *__restrict__ cent32,
-                      int64_t *__restrict__ sizes, int init, int *active) {
+                      int64_t *__restrict__ sizes, int init, int *active, const int32_t *__restrict__ plist) {
   __shared__ float wd[kFinT / 32], wc[kFinT / 32];
-  const int p = blockIdx.x;
+  const int p = plist ? plist[blockIdx.x] : (int)blockIdx.x;  // plist: one width class's problems
   const BProb P = probs[p];
   BState *S = st + p;
   if (!init && S->done) return;
@@ -1043,6 +1043,9 @@ struct Batch {
   std::vector<int32_t> cls_blocks;  // blocks of each width's problems (largest k first), classes in order
   int cls_off[kNumD + 1] = {};
   int32_t *d_cls_blocks = nullptr;
+  std::vector<int32_t> cls_probs;  // each width's problems, classes in order
+  int cls_poff[kNumD + 1] = {};
+  int32_t *d_cls_probs = nullptr;
   std::vector<BItem> items;         // grouped by padded width, each group largest first
   int item_off[kNumD + 1] = {};     // group dc = items [item_off[dc], item_off[dc + 1])
   size_t smem_d[kNumD] = {};        // dynamic shared memory of each width's kernel
@@ -1173,6 +1176,12 @@ void plan_batch(Batch &B, const std::vector<int64_t> &n, const std::vector<int64
         for (int b = 0; b < B.probs[q].nb; ++b) B.cls_blocks.push_back(B.probs[q].b0 + b);
   }
   B.cls_off[kNumD] = (int)B.cls_blocks.size();
+  for (int dc = 0; dc < kNumD; ++dc) {
+    B.cls_poff[dc] = (int)B.cls_probs.size();
+    for (int q = 0; q < m; ++q)
+      if (dclass(B.probs[q].D) == dc) B.cls_probs.push_back(q);
+  }
+  B.cls_poff[kNumD] = (int)B.cls_probs.size();
   B.xelems = xo;
   B.rows = row;
   B.kd = co;
@@ -1204,6 +1213,7 @@ sc_status alloc_batch(Batch &B) {
     B.st = a.take<BState>(B.count);
     B.d_block_prob = a.take<int32_t>(B.blocks);
     B.d_cls_blocks = a.take<int32_t>(B.cls_blocks.size());
+    B.d_cls_probs = a.take<int32_t>(B.cls_probs.size());
     B.d_items = a.take<BItem>(B.items.size());
     B.heads = a.take<unsigned>((size_t)(kGraphIters + 1) * kNumD);
     B.active = a.take<int>(1);
@@ -1222,6 +1232,8 @@ sc_status upload_tables(Batch &B) {
                           cudaMemcpyHostToDevice, B.s));
   SC_CUDA(cudaMemcpyAsync(B.d_items, B.items.data(), B.items.size() * sizeof(BItem), cudaMemcpyHostToDevice, B.s));
   SC_CUDA(cudaMemcpyAsync(B.d_cls_blocks, B.cls_blocks.data(), B.cls_blocks.size() * sizeof(int32_t),
+                          cudaMemcpyHostToDevice, B.s));
+  SC_CUDA(cudaMemcpyAsync(B.d_cls_probs, B.cls_probs.data(), B.cls_probs.size() * sizeof(int32_t),
                           cudaMemcpyHostToDevice, B.s));
   if (!B.uniforms.empty())
     SC_CUDA(cudaMemcpyAsync(B.d_uniforms, B.uniforms.data(), B.uniforms.size() * sizeof(double),
@@ -1243,30 +1255,15 @@ sc_status launch_assign_d(Batch &B, int dc, unsigned *head, int nitems, const BI
 }
 
 // One assignment pass over the item groups of every width; heads[dc] is the
-// queue head of width dc (cleared beforehand).  With fork / join events the
-// four widths run on B.s and the three side streams at once, widest first,
-// so that each launch's tail overlaps the next one's work.
+// queue head of width dc (cleared beforehand).
 template <typename T>
-sc_status launch_assign(Batch &B, unsigned *heads, int mode, cudaEvent_t *ev = nullptr) {
+sc_status launch_assign(Batch &B, unsigned *heads, int mode) {
   const BItem *it = B.d_items;
   const int *o = B.item_off;
-  cudaStream_t s3 = B.s, s2 = B.s, s1 = B.s, s0 = B.s;
-  if (ev) {
-    SC_CUDA(cudaEventRecord(ev[0], B.s));
-    for (int i = 0; i < 3; ++i) SC_CUDA(cudaStreamWaitEvent(B.side[i], ev[0], 0));
-    s2 = B.side[0];
-    s1 = B.side[1];
-    s0 = B.side[2];
-  }
-  SC_TRY((launch_assign_d<T, 64>(B, 3, heads + 3, o[4] - o[3], it + o[3], mode, s3)));
-  SC_TRY((launch_assign_d<T, 32>(B, 2, heads + 2, o[3] - o[2], it + o[2], mode, s2)));
-  SC_TRY((launch_assign_d<T, 16>(B, 1, heads + 1, o[2] - o[1], it + o[1], mode, s1)));
-  SC_TRY((launch_assign_d<T, 8>(B, 0, heads + 0, o[1] - o[0], it + o[0], mode, s0)));
-  if (ev)
-    for (int i = 0; i < 3; ++i) {
-      SC_CUDA(cudaEventRecord(ev[1 + i], B.side[i]));
-      SC_CUDA(cudaStreamWaitEvent(B.s, ev[1 + i], 0));
-    }
+  SC_TRY((launch_assign_d<T, 64>(B, 3, heads + 3, o[4] - o[3], it + o[3], mode)));
+  SC_TRY((launch_assign_d<T, 32>(B, 2, heads + 2, o[3] - o[2], it + o[2], mode)));
+  SC_TRY((launch_assign_d<T, 16>(B, 1, heads + 1, o[2] - o[1], it + o[1], mode)));
+  SC_TRY((launch_assign_d<T, 8>(B, 0, heads + 0, o[1] - o[0], it + o[0], mode)));
   return SC_OK;
 }
 
@@ -1460,7 +1457,7 @@ sc_status run_setup(Batch &B) {
   SC_CUDA(cudaMemsetAsync(seed_heads, 0, kNumD * sizeof(unsigned), s));
   SC_TRY(launch_assign<T>(B, seed_heads, 1));
   batch_finalize_kernel<<<B.count, kFinT, 0, s>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 1,
-                                                  B.active);
+                                                  B.active, nullptr);
   SC_LAUNCHED();
   return SC_OK;
 }
@@ -1486,15 +1483,35 @@ sc_status run_lloyd(Batch &B) {
     r = cuda_fail(cudaGetLastError(), "cudaStreamBeginCapture");
   if (r == SC_OK && cudaMemsetAsync(B.heads, 0, (size_t)G * kNumD * sizeof(unsigned), s) != cudaSuccess)
     r = cuda_fail(cudaGetLastError(), "memset");
-  for (int t = 0; t < G && r == SC_OK; ++t) {
-    r = launch_assign<T>(B, B.heads + (size_t)t * kNumD, 0, ev);
-    if (r != SC_OK) break;
-    batch_finalize_kernel<<<B.count, kFinT, 0, s>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 0,
-                                                    B.active);
-    note_launch();
-    const cudaError_t le = cudaGetLastError();
-    if (le != cudaSuccess) r = cuda_fail(le, "batch_finalize_kernel");
+  // one chain of G x (assignment, finalize) per width class, the classes'
+  // chains side by side (B.s and the side streams), joined at the end
+  if (r == SC_OK && cudaEventRecord(ev[0], s) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "fork");
+  for (int i = 0; i < 3 && r == SC_OK; ++i)
+    if (cudaStreamWaitEvent(B.side[i], ev[0], 0) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "fork");
+  for (int dc = kNumD - 1; dc >= 0 && r == SC_OK; --dc) {
+    const int np = B.cls_poff[dc + 1] - B.cls_poff[dc], ni = B.item_off[dc + 1] - B.item_off[dc];
+    if (np == 0) continue;
+    cudaStream_t cs = dc == kNumD - 1 ? s : B.side[kNumD - 2 - dc];
+    for (int t = 0; t < G && r == SC_OK; ++t) {
+      unsigned *head = B.heads + (size_t)t * kNumD + dc;
+      const BItem *it = B.d_items + B.item_off[dc];
+      switch (dc) {
+        case 0: r = launch_assign_d<T, 8>(B, 0, head, ni, it, 0, cs); break;
+        case 1: r = launch_assign_d<T, 16>(B, 1, head, ni, it, 0, cs); break;
+        case 2: r = launch_assign_d<T, 32>(B, 2, head, ni, it, 0, cs); break;
+        default: r = launch_assign_d<T, 64>(B, 3, head, ni, it, 0, cs); break;
+      }
+      if (r != SC_OK) break;
+      batch_finalize_kernel<<<np, kFinT, 0, cs>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 0,
+                                                  B.active, B.d_cls_probs + B.cls_poff[dc]);
+      note_launch();
+      const cudaError_t le = cudaGetLastError();
+      if (le != cudaSuccess) r = cuda_fail(le, "batch_finalize_kernel");
+    }
   }
+  for (int i = 0; i < 3 && r == SC_OK; ++i)
+    if (cudaEventRecord(ev[1 + i], B.side[i]) != cudaSuccess || cudaStreamWaitEvent(s, ev[1 + i], 0) != cudaSuccess)
+      r = cuda_fail(cudaGetLastError(), "join");
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
     const cudaError_t ec = cudaStreamEndCapture(s, &graph);
