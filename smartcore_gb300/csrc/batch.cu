@@ -899,12 +899,12 @@ __global__ void __launch_bounds__(kSelT)
 batch_pp_select_kernel(const BProb *__restrict__ probs, BState *st, const T *__restrict__ X,
                        const double *__restrict__ dd_all, const double *__restrict__ part_all,
                        const double *__restrict__ uniforms, int64_t *__restrict__ seed_idx, T *__restrict__ seed_x,
-                       float *__restrict__ seed_cc, int j) {
+                       float *__restrict__ seed_cc, int j, const int32_t *__restrict__ plist) {
   __shared__ double s_incl[kSelT];
   __shared__ double s_wtot[32];
   __shared__ int s_chunk;
   __shared__ long long s_pick;
-  const int p = blockIdx.x;
+  const int p = plist ? plist[blockIdx.x] : (int)blockIdx.x;  // plist: one width class's problems
   const BProb P = probs[p];
   BState *S = st + p;
   const double *part = part_all + P.b0;
@@ -1397,57 +1397,66 @@ sc_status run_setup(Batch &B) {
   // blocks (of each width's list too)
   std::vector<int> blocks_upto(B.count + 1, 0);
   for (int q = 0; q < B.count; ++q) blocks_upto[q + 1] = blocks_upto[q] + B.probs[q].nb;
-  std::vector<int> cls_probs[kNumD];  // each width's problems, largest k first
-  for (int q = 0; q < B.count; ++q) cls_probs[dclass(B.probs[q].D)].push_back(q);
-  int q_ge = B.count, q_gt = B.count;
-  int cls_ge[kNumD], cls_nb[kNumD];
-  for (int dc = 0; dc < kNumD; ++dc) {
-    cls_ge[dc] = (int)cls_probs[dc].size();
-    cls_nb[dc] = B.cls_off[dc + 1] - B.cls_off[dc];
-  }
   const PPFar32 far = pp_far_bound32(kMaxBD);  // d = 64 bounds the far test of every width
-  // each draw's width classes run at once (B.s and the side streams, widest
-  // first), joined before the selection
-  SC_TRY(ensure_side_streams(B));
-  EventSet ev;
-  SC_TRY(ev.create());
-  for (int j = 1; j <= B.kmax; ++j) {
-    while (q_ge > 0 && B.probs[q_ge - 1].k < j) --q_ge;
-    while (q_gt > 0 && B.probs[q_gt - 1].k <= j) --q_gt;
-    if constexpr (sizeof(T) == 4) {
-      SC_CUDA(cudaEventRecord(ev.e[0], s));
-      for (int i = 0; i < 3; ++i) SC_CUDA(cudaStreamWaitEvent(B.side[i], ev.e[0], 0));
-      for (int dc = kNumD - 1; dc >= 0; --dc) {
-        while (cls_ge[dc] > 0 && B.probs[cls_probs[dc][cls_ge[dc] - 1]].k < j) {
-          --cls_ge[dc];
-          cls_nb[dc] -= B.probs[cls_probs[dc][cls_ge[dc]]].nb;
+  if constexpr (sizeof(T) == 4) {
+    // One chain of draws per width class (its problems, largest k first, and
+    // their blocks are prefixes of the class's lists at every draw): update,
+    // then the class's selection; the chains run side by side on B.s and the
+    // side streams, widest first, joined after the last draw.
+    SC_TRY(ensure_side_streams(B));
+    EventSet ev;
+    SC_TRY(ev.create());
+    SC_CUDA(cudaEventRecord(ev.e[0], s));
+    for (int i = 0; i < 3; ++i) SC_CUDA(cudaStreamWaitEvent(B.side[i], ev.e[0], 0));
+    const float *xf = (const float *)B.X;
+    for (int dc = kNumD - 1; dc >= 0; --dc) {
+      const int np = B.cls_poff[dc + 1] - B.cls_poff[dc];
+      if (np == 0) continue;
+      const int32_t *pl = B.cls_probs.data() + B.cls_poff[dc];
+      const int32_t *cb = B.d_cls_blocks + B.cls_off[dc];
+      const int32_t *dpl = B.d_cls_probs + B.cls_poff[dc];
+      cudaStream_t cs = dc == kNumD - 1 ? s : B.side[kNumD - 2 - dc];
+      int ge = np, gt = np, nb = B.cls_off[dc + 1] - B.cls_off[dc];
+      for (int j = 1; j <= B.probs[pl[0]].k; ++j) {
+        while (ge > 0 && B.probs[pl[ge - 1]].k < j) nb -= B.probs[pl[--ge]].nb;
+        while (gt > 0 && B.probs[pl[gt - 1]].k <= j) --gt;
+        if (nb > 0) {
+          switch (dc) {
+            case 0: batch_pp_update32_kernel<8><<<nb, kBlk, 0, cs>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+            case 1: batch_pp_update32_kernel<16><<<nb, kBlk, 0, cs>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+            case 2: batch_pp_update32_kernel<32><<<nb, kBlk, 0, cs>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+            default: batch_pp_update32_kernel<64><<<nb, kBlk, 0, cs>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+          }
+          SC_LAUNCHED();
         }
-        if (cls_nb[dc] == 0) continue;
-        const int32_t *cb = B.d_cls_blocks + B.cls_off[dc];
-        const float *xf = (const float *)B.X;
-        cudaStream_t st = dc == kNumD - 1 ? s : B.side[kNumD - 2 - dc];
-        switch (dc) {
-          case 0: batch_pp_update32_kernel<8><<<cls_nb[dc], kBlk, 0, st>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
-          case 1: batch_pp_update32_kernel<16><<<cls_nb[dc], kBlk, 0, st>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
-          case 2: batch_pp_update32_kernel<32><<<cls_nb[dc], kBlk, 0, st>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
-          default: batch_pp_update32_kernel<64><<<cls_nb[dc], kBlk, 0, st>>>(cb, B.d_block_prob, B.d_probs, B.st, xf, B.dd, B.dd32, B.labels, B.part, B.seed_cc, j, far); break;
+        if (gt > 0) {
+          batch_pp_select_kernel<T><<<gt, kSelT, 0, cs>>>(B.d_probs, B.st, (const T *)B.X, B.dd, B.part, B.d_uniforms,
+                                                          B.seed_idx, (T *)B.seed_x, B.seed_cc, j, dpl);
+          SC_LAUNCHED();
         }
+      }
+    }
+    for (int i = 0; i < 3; ++i) {
+      SC_CUDA(cudaEventRecord(ev.e[1 + i], B.side[i]));
+      SC_CUDA(cudaStreamWaitEvent(s, ev.e[1 + i], 0));
+    }
+  } else {
+    int q_ge = B.count, q_gt = B.count;
+    for (int j = 1; j <= B.kmax; ++j) {
+      while (q_ge > 0 && B.probs[q_ge - 1].k < j) --q_ge;
+      while (q_gt > 0 && B.probs[q_gt - 1].k <= j) --q_gt;
+      if (q_ge > 0) {
+        batch_pp_update_kernel<T><<<blocks_upto[q_ge], kBlk, 0, s>>>(B.d_block_prob, B.d_probs, B.st,
+                                                                     (const T *)B.X, B.dd, B.dd32, B.labels, B.part,
+                                                                     B.seed_cc, j, far);
         SC_LAUNCHED();
       }
-      for (int i = 0; i < 3; ++i) {
-        SC_CUDA(cudaEventRecord(ev.e[1 + i], B.side[i]));
-        SC_CUDA(cudaStreamWaitEvent(s, ev.e[1 + i], 0));
+      if (q_gt > 0) {
+        batch_pp_select_kernel<T><<<q_gt, kSelT, 0, s>>>(B.d_probs, B.st, (const T *)B.X, B.dd, B.part,
+                                                         B.d_uniforms, B.seed_idx, (T *)B.seed_x, B.seed_cc, j,
+                                                         nullptr);
+        SC_LAUNCHED();
       }
-    } else if (q_ge > 0) {
-      batch_pp_update_kernel<T><<<blocks_upto[q_ge], kBlk, 0, s>>>(B.d_block_prob, B.d_probs, B.st, (const T *)B.X,
-                                                                   B.dd, B.dd32, B.labels, B.part, B.seed_cc, j,
-                                                                   far);
-      SC_LAUNCHED();
-    }
-    if (q_gt > 0) {
-      batch_pp_select_kernel<T><<<q_gt, kSelT, 0, s>>>(B.d_probs, B.st, (const T *)B.X, B.dd, B.part,
-                                                         B.d_uniforms, B.seed_idx, (T *)B.seed_x, B.seed_cc, j);
-      SC_LAUNCHED();
     }
   }
   // initial means of the seeding partition
