@@ -1057,7 +1057,8 @@ struct Batch {
   bool needs_pad = false;
   // device
   cudaStream_t s = nullptr;
-  cudaStream_t side[3] = {nullptr, nullptr, nullptr};  // the Lloyd graph's parallel assignment branches
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};  // streams of the width classes' parallel chains
+  bool chains_open = false;  // set-up left each class's work on its own stream (no join)
   void *mem = nullptr;
   void *X = nullptr, *seed_x = nullptr;
   int32_t *labels = nullptr, *d_block_prob = nullptr;
@@ -1336,6 +1337,10 @@ sc_status ensure_side_streams(Batch &B) {
   return SC_OK;
 }
 
+// Stream of width class dc's chain: the widest on B.s, the others on the side
+// streams.
+cudaStream_t class_stream(const Batch &B, int dc) { return dc == kNumD - 1 ? B.s : B.side[kNumD - 2 - dc]; }
+
 // Fork / join events (no timing), destroyed with the set.
 struct EventSet {
   cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -1398,11 +1403,22 @@ sc_status run_setup(Batch &B) {
   std::vector<int> blocks_upto(B.count + 1, 0);
   for (int q = 0; q < B.count; ++q) blocks_upto[q + 1] = blocks_upto[q] + B.probs[q].nb;
   const PPFar32 far = pp_far_bound32(kMaxBD);  // d = 64 bounds the far test of every width
+  // the initial means' sums and queue heads, and the Lloyd loop's count of
+  // running problems
+  SC_CUDA(cudaMemsetAsync(B.acc, 0, (size_t)B.kd * sizeof(Acc128), s));
+  SC_CUDA(cudaMemsetAsync(B.cnt, 0, (size_t)B.ksum * sizeof(unsigned long long), s));
+  unsigned *seed_heads = B.heads + (size_t)kGraphIters * kNumD;
+  SC_CUDA(cudaMemsetAsync(seed_heads, 0, kNumD * sizeof(unsigned), s));
+  const int act = B.count;
+  SC_CUDA(cudaMemcpyAsync(B.active, &act, sizeof act, cudaMemcpyHostToDevice, s));
+  B.chains_open = false;
   if constexpr (sizeof(T) == 4) {
-    // One chain of draws per width class (its problems, largest k first, and
-    // their blocks are prefixes of the class's lists at every draw): update,
-    // then the class's selection; the chains run side by side on B.s and the
-    // side streams, widest first, joined after the last draw.
+    // One chain per width class (its problems, largest k first, and their
+    // blocks are prefixes of the class's lists at every draw): each draw's
+    // update and the class's selection, then the initial means of the
+    // seeding partition.  The chains run side by side on the classes'
+    // streams, widest first, and stay open: the class's Lloyd loop follows
+    // on the same stream.
     SC_TRY(ensure_side_streams(B));
     EventSet ev;
     SC_TRY(ev.create());
@@ -1415,7 +1431,7 @@ sc_status run_setup(Batch &B) {
       const int32_t *pl = B.cls_probs.data() + B.cls_poff[dc];
       const int32_t *cb = B.d_cls_blocks + B.cls_off[dc];
       const int32_t *dpl = B.d_cls_probs + B.cls_poff[dc];
-      cudaStream_t cs = dc == kNumD - 1 ? s : B.side[kNumD - 2 - dc];
+      cudaStream_t cs = class_stream(B, dc);
       int ge = np, gt = np, nb = B.cls_off[dc + 1] - B.cls_off[dc];
       for (int j = 1; j <= B.probs[pl[0]].k; ++j) {
         while (ge > 0 && B.probs[pl[ge - 1]].k < j) nb -= B.probs[pl[--ge]].nb;
@@ -1435,11 +1451,20 @@ sc_status run_setup(Batch &B) {
           SC_LAUNCHED();
         }
       }
+      const int ni = B.item_off[dc + 1] - B.item_off[dc];
+      const BItem *it = B.d_items + B.item_off[dc];
+      switch (dc) {
+        case 0: SC_TRY((launch_assign_d<T, 8>(B, 0, seed_heads + 0, ni, it, 1, cs))); break;
+        case 1: SC_TRY((launch_assign_d<T, 16>(B, 1, seed_heads + 1, ni, it, 1, cs))); break;
+        case 2: SC_TRY((launch_assign_d<T, 32>(B, 2, seed_heads + 2, ni, it, 1, cs))); break;
+        default: SC_TRY((launch_assign_d<T, 64>(B, 3, seed_heads + 3, ni, it, 1, cs))); break;
+      }
+      batch_finalize_kernel<<<np, kFinT, 0, cs>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 1,
+                                                  B.active, dpl);
+      SC_LAUNCHED();
     }
-    for (int i = 0; i < 3; ++i) {
-      SC_CUDA(cudaEventRecord(ev.e[1 + i], B.side[i]));
-      SC_CUDA(cudaStreamWaitEvent(s, ev.e[1 + i], 0));
-    }
+    B.chains_open = true;
+    return SC_OK;
   } else {
     int q_ge = B.count, q_gt = B.count;
     for (int j = 1; j <= B.kmax; ++j) {
@@ -1460,10 +1485,6 @@ sc_status run_setup(Batch &B) {
     }
   }
   // initial means of the seeding partition
-  SC_CUDA(cudaMemsetAsync(B.acc, 0, (size_t)B.kd * sizeof(Acc128), s));
-  SC_CUDA(cudaMemsetAsync(B.cnt, 0, (size_t)B.ksum * sizeof(unsigned long long), s));
-  unsigned *seed_heads = B.heads + (size_t)kGraphIters * kNumD;
-  SC_CUDA(cudaMemsetAsync(seed_heads, 0, kNumD * sizeof(unsigned), s));
   SC_TRY(launch_assign<T>(B, seed_heads, 1));
   batch_finalize_kernel<<<B.count, kFinT, 0, s>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 1,
                                                   B.active, nullptr);
@@ -1471,44 +1492,46 @@ sc_status run_setup(Batch &B) {
   return SC_OK;
 }
 
-// The Lloyd loop: a graph of G = min(max_iter, 32) iterations (queue heads
-// cleared, then G x (assignment, finalize)), launched until every problem has
-// stopped; a stopped problem's items and finalize return at once.
+// The Lloyd loop: per width class a graph of G = min(max_iter, 32)
+// iterations (the class's queue heads cleared, then G x (assignment,
+// finalize)), launched on the class's stream so that it follows the class's
+// own set-up; the classes are joined after each round of graphs, which
+// repeats until every problem has stopped.  A stopped problem's items and
+// finalize return at once.
 template <typename T>
 sc_status run_lloyd(Batch &B) {
   cudaStream_t s = B.s;
-  int act = B.count;
-  SC_CUDA(cudaMemcpyAsync(B.active, &act, sizeof act, cudaMemcpyHostToDevice, s));
-  SC_CUDA(cudaStreamSynchronize(s));
   const int G = std::min(B.max_iter, kGraphIters);
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
   SC_TRY(ensure_side_streams(B));
   EventSet evs;
   SC_TRY(evs.create());
   cudaEvent_t *ev = evs.e;
+  if (!B.chains_open) {  // every class waits for the set-up on B.s
+    SC_CUDA(cudaEventRecord(ev[0], s));
+    for (int i = 0; i < 3; ++i) SC_CUDA(cudaStreamWaitEvent(B.side[i], ev[0], 0));
+  }
+  B.chains_open = false;
+  cudaGraph_t graph[kNumD] = {};
+  cudaGraphExec_t exec[kNumD] = {};
   sc_status r = SC_OK;
-  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-    r = cuda_fail(cudaGetLastError(), "cudaStreamBeginCapture");
-  if (r == SC_OK && cudaMemsetAsync(B.heads, 0, (size_t)G * kNumD * sizeof(unsigned), s) != cudaSuccess)
-    r = cuda_fail(cudaGetLastError(), "memset");
-  // one chain of G x (assignment, finalize) per width class, the classes'
-  // chains side by side (B.s and the side streams), joined at the end
-  if (r == SC_OK && cudaEventRecord(ev[0], s) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "fork");
-  for (int i = 0; i < 3 && r == SC_OK; ++i)
-    if (cudaStreamWaitEvent(B.side[i], ev[0], 0) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "fork");
   for (int dc = kNumD - 1; dc >= 0 && r == SC_OK; --dc) {
     const int np = B.cls_poff[dc + 1] - B.cls_poff[dc], ni = B.item_off[dc + 1] - B.item_off[dc];
     if (np == 0) continue;
-    cudaStream_t cs = dc == kNumD - 1 ? s : B.side[kNumD - 2 - dc];
+    cudaStream_t cs = class_stream(B, dc);
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "cudaStreamBeginCapture");
+      break;
+    }
+    unsigned *heads = B.heads + (size_t)dc * kGraphIters;
+    if (cudaMemsetAsync(heads, 0, (size_t)G * sizeof(unsigned), cs) != cudaSuccess)
+      r = cuda_fail(cudaGetLastError(), "memset");
+    const BItem *it = B.d_items + B.item_off[dc];
     for (int t = 0; t < G && r == SC_OK; ++t) {
-      unsigned *head = B.heads + (size_t)t * kNumD + dc;
-      const BItem *it = B.d_items + B.item_off[dc];
       switch (dc) {
-        case 0: r = launch_assign_d<T, 8>(B, 0, head, ni, it, 0, cs); break;
-        case 1: r = launch_assign_d<T, 16>(B, 1, head, ni, it, 0, cs); break;
-        case 2: r = launch_assign_d<T, 32>(B, 2, head, ni, it, 0, cs); break;
-        default: r = launch_assign_d<T, 64>(B, 3, head, ni, it, 0, cs); break;
+        case 0: r = launch_assign_d<T, 8>(B, 0, heads + t, ni, it, 0, cs); break;
+        case 1: r = launch_assign_d<T, 16>(B, 1, heads + t, ni, it, 0, cs); break;
+        case 2: r = launch_assign_d<T, 32>(B, 2, heads + t, ni, it, 0, cs); break;
+        default: r = launch_assign_d<T, 64>(B, 3, heads + t, ni, it, 0, cs); break;
       }
       if (r != SC_OK) break;
       batch_finalize_kernel<<<np, kFinT, 0, cs>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 0,
@@ -1517,40 +1540,45 @@ sc_status run_lloyd(Batch &B) {
       const cudaError_t le = cudaGetLastError();
       if (le != cudaSuccess) r = cuda_fail(le, "batch_finalize_kernel");
     }
-  }
-  for (int i = 0; i < 3 && r == SC_OK; ++i)
-    if (cudaEventRecord(ev[1 + i], B.side[i]) != cudaSuccess || cudaStreamWaitEvent(s, ev[1 + i], 0) != cudaSuccess)
-      r = cuda_fail(cudaGetLastError(), "join");
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
-    const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+    const cudaError_t ec = cudaStreamEndCapture(cs, &graph[dc]);
     if (r == SC_OK && ec != cudaSuccess) r = cuda_fail(ec, "cudaStreamEndCapture");
-  }
-  if (r == SC_OK) {
-    const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
-    if (e != cudaSuccess) r = cuda_fail(e, "cudaGraphInstantiate");
+    if (r == SC_OK) {
+      const cudaError_t e = cudaGraphInstantiate(&exec[dc], graph[dc], 0);
+      if (e != cudaSuccess) r = cuda_fail(e, "cudaGraphInstantiate");
+    }
   }
   for (int done = 0; r == SC_OK && done < B.max_iter; done += G) {
-    cudaError_t e = cudaGraphLaunch(exec, s);
+    cudaError_t e = cudaSuccess;
+    for (int dc = kNumD - 1; dc >= 0 && e == cudaSuccess; --dc)
+      if (exec[dc]) e = cudaGraphLaunch(exec[dc], class_stream(B, dc));
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+      e = cudaEventRecord(ev[1 + i], B.side[i]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev[1 + i], 0);
+    }
+    int act = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&act, B.active, sizeof act, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) r = cuda_fail(e, "Lloyd graph");
+    if (e != cudaSuccess) r = cuda_fail(e, "Lloyd graphs");
     else if (act == 0) break;
   }
-  if (exec) cudaGraphExecDestroy(exec);
-  if (graph) cudaGraphDestroy(graph);
+  for (int dc = 0; dc < kNumD; ++dc) {
+    if (exec[dc]) cudaGraphExecDestroy(exec[dc]);
+    if (graph[dc]) cudaGraphDestroy(graph[dc]);
+  }
   return r;
 }
 
 void free_batch(Batch &B) {
-  if (B.mem) dev_free(B.mem, B.s);
-  B.mem = nullptr;
+  // the side streams' work (an error may have left a chain unjoined) ends
+  // before the arena is released on B.s
   for (int i = 0; i < 3; ++i)
     if (B.side[i]) {
       cudaStreamSynchronize(B.side[i]);
       cudaStreamDestroy(B.side[i]);
       B.side[i] = nullptr;
     }
+  if (B.mem) dev_free(B.mem, B.s);
+  B.mem = nullptr;
   if (B.s) {
     cudaStreamSynchronize(B.s);
     cudaStreamDestroy(B.s);
@@ -1632,7 +1660,11 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
     B.first.push_back(pr.first_index);
     for (int64_t a = 0; a + 1 < pr.k; ++a) B.uniforms.push_back(pr.uniforms[a]);
   }
-  if (cudaStreamCreateWithFlags(&B.s, cudaStreamNonBlocking) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaStreamCreate");
+  // the widest class's chain (on B.s) is the longest: its blocks go first
+  int prio_lo = 0, prio_hi = 0;
+  if (cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&B.s, cudaStreamNonBlocking, prio_hi) != cudaSuccess)
+    return cuda_fail(cudaGetLastError(), "cudaStreamCreate");
   sc_status r = SC_OK;
   do {
     trace.mark("plan", nullptr);
@@ -1824,6 +1856,9 @@ sc_status sc_batch_tune(const char *path) {
     tune_fill_kernel<<<1024, 256, 0, B.s>>>((float *)B.X, B.xelems, 12345u);
     SC_LAUNCHED();
     if ((r = run_setup<float>(B)) != SC_OK) break;
+    for (int i = 0; i < 3; ++i)  // the classes' set-up chains, before any timing
+      if (B.side[i] && cudaStreamSynchronize(B.side[i]) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "tuning set-up");
+    if (r != SC_OK) break;
     const int act = B.count;
     if (cudaMemcpyAsync(B.active, &act, sizeof act, cudaMemcpyHostToDevice, B.s) != cudaSuccess ||
         cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
