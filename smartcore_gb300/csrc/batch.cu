@@ -662,15 +662,27 @@ batch_scan32_kernel(const int32_t *__restrict__ cls_blocks, const int32_t *__res
 }
 
 // Per problem: xnorm2 = sum of its block partials in order, the state's start
-// values, and the first seed (row first_index) as seed 0.
+// values, the first seed (row first_index) as seed 0, and the fixed-point
+// scale of the sums from max |x| < 2^e: an item's int64 partial of up to
+// `rows` values stays below 2^62 (at most 2^160; a non-finite max leaves a
+// scale that the call reports as an error before writing any output).
+// plist: one width class's problems (else problem = block).
 template <typename T>
-__global__ void batch_init_kernel(const BProb *__restrict__ probs, int count, BState *st,
-                                  const double *__restrict__ part, const int64_t *__restrict__ first,
-                                  const T *__restrict__ X, T *__restrict__ seed_x, int64_t *__restrict__ seed_idx) {
-  const int p = blockIdx.x;
-  if (p >= count) return;
+__global__ void batch_init_kernel(BProb *__restrict__ probs, int count, BState *st, const double *__restrict__ part,
+                                  const int64_t *__restrict__ first, const T *__restrict__ X, T *__restrict__ seed_x,
+                                  int64_t *__restrict__ seed_idx, const unsigned long long *__restrict__ absmax_bits,
+                                  const int32_t *__restrict__ plist) {
+  if ((int)blockIdx.x >= count) return;
+  const int p = plist ? plist[blockIdx.x] : (int)blockIdx.x;
   const BProb P = probs[p];
   if (threadIdx.x == 0) {
+    const double a = __longlong_as_double((long long)absmax_bits[p]);
+    int e = 0;
+    if (a > 0.0 && a <= DBL_MAX) frexp(a, &e);
+    int lg = 0;
+    while ((1ll << lg) < (long long)P.rows + 1) ++lg;
+    const int sc = 62 - e - lg;
+    probs[p].scale = sc > 160 ? 160 : sc;
     double s = 0.0;
     for (int b = 0; b < P.nb; ++b) s = __dadd_rn(s, part[P.b0 + b]);
     BState z;
@@ -1034,6 +1046,12 @@ struct Arena {
   }
 };
 
+struct CopyJob {
+  const uint4 *src;
+  uint4 *dst;
+  int64_t n16;
+};
+
 struct Batch {
   int dtype = SC_F32;
   int count = 0;
@@ -1072,6 +1090,7 @@ struct Batch {
   BItem *d_items = nullptr;
   unsigned *heads = nullptr;  // one queue head per (graph iteration, width), then the seeding pass's
   int *active = nullptr;
+  CopyJob *d_jobs = nullptr;  // gather table of rows read in place from host memory
 };
 
 // Phase times of one batched call, printed to stderr when the environment
@@ -1308,12 +1327,6 @@ sc_status assign_grid(Batch &B, int dtype) {
 
 // Rows the device can read where they are (pinned, mapped host memory):
 // copied by SM loads, 16 bytes each, every CTA striding over every job.
-struct CopyJob {
-  const uint4 *src;
-  uint4 *dst;
-  int64_t n16;
-};
-
 __global__ void __launch_bounds__(256) gather_host_rows_kernel(const CopyJob *__restrict__ jobs, int njobs) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int q = 0; q < njobs; ++q) {
@@ -1354,76 +1367,54 @@ struct EventSet {
   }
 };
 
+// Clears what the set-up accumulates (max |x|, the initial means' sums and
+// queue heads, the count of running problems), then forks the side streams
+// from B.s: each width class's work from here on runs on its own stream.
+sc_status begin_chains(Batch &B) {
+  cudaStream_t s = B.s;
+  SC_CUDA(cudaMemsetAsync(B.absmax, 0, (size_t)B.count * sizeof(unsigned long long), s));
+  SC_CUDA(cudaMemsetAsync(B.acc, 0, (size_t)B.kd * sizeof(Acc128), s));
+  SC_CUDA(cudaMemsetAsync(B.cnt, 0, (size_t)B.ksum * sizeof(unsigned long long), s));
+  SC_CUDA(cudaMemsetAsync(B.heads + (size_t)kGraphIters * kNumD, 0, kNumD * sizeof(unsigned), s));
+  const int act = B.count;
+  SC_CUDA(cudaMemcpyAsync(B.active, &act, sizeof act, cudaMemcpyHostToDevice, s));
+  SC_TRY(ensure_side_streams(B));
+  EventSet ev;
+  SC_TRY(ev.create());
+  SC_CUDA(cudaEventRecord(ev.e[0], s));
+  for (int i = 0; i < 3; ++i) SC_CUDA(cudaStreamWaitEvent(B.side[i], ev.e[0], 0));
+  B.chains_open = true;
+  return SC_OK;
+}
+
+// Joins the side streams into B.s.
+sc_status join_chains(Batch &B) {
+  EventSet ev;
+  SC_TRY(ev.create());
+  for (int i = 0; i < 3; ++i)
+    if (B.side[i]) {
+      SC_CUDA(cudaEventRecord(ev.e[1 + i], B.side[i]));
+      SC_CUDA(cudaStreamWaitEvent(B.s, ev.e[1 + i], 0));
+    }
+  B.chains_open = false;
+  return SC_OK;
+}
+
 // Device phases of a batch: scan, scales, k-means++, initial means.
 template <typename T>
 sc_status run_setup(Batch &B) {
   cudaStream_t s = B.s;
-  SC_CUDA(cudaMemsetAsync(B.absmax, 0, (size_t)B.count * sizeof(unsigned long long), s));
-  if constexpr (sizeof(T) == 4) {
-    for (int dc = 0; dc < kNumD; ++dc) {
-      const int nb = B.cls_off[dc + 1] - B.cls_off[dc];
-      if (nb == 0) continue;
-      const int32_t *cb = B.d_cls_blocks + B.cls_off[dc];
-      const float *xf = (const float *)B.X;
-      switch (dc) {
-        case 0: batch_scan32_kernel<8><<<nb, kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
-        case 1: batch_scan32_kernel<16><<<nb, kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
-        case 2: batch_scan32_kernel<32><<<nb, kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
-        default: batch_scan32_kernel<64><<<nb, kBlk, 0, s>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
-      }
-      SC_LAUNCHED();
-    }
-  } else {
-    batch_scan_kernel<T><<<B.blocks, kBlk, 0, s>>>(B.d_block_prob, B.d_probs, (const T *)B.X, B.part, B.absmax);
-    SC_LAUNCHED();
-  }
-  batch_init_kernel<T><<<B.count, 64, 0, s>>>(B.d_probs, B.count, B.st, B.part, B.d_first, (const T *)B.X,
-                                             (T *)B.seed_x, B.seed_idx);
-  SC_LAUNCHED();
-  std::vector<unsigned long long> am(B.count);
-  SC_CUDA(cudaMemcpyAsync(am.data(), B.absmax, am.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-  SC_CUDA(cudaStreamSynchronize(s));
-  for (int q = 0; q < B.count; ++q) {
-    double a;
-    memcpy(&a, &am[q], sizeof a);
-    if (!(a <= DBL_MAX)) {
-      set_error("problem %d: x contains NaN or infinity; the GPU path requires finite input", B.order[q]);
-      return SC_ERR_INVALID;
-    }
-    int e = 0;
-    if (a > 0) frexp(a, &e);  // |x| < 2^e
-    // an item's int64 partial of up to `rows` values stays below 2^62
-    int sc = 62 - e - ceil_log2i((int64_t)B.probs[q].rows + 1);
-    B.probs[q].scale = sc > 160 ? 160 : sc;
-  }
-  SC_CUDA(cudaMemcpyAsync(B.d_probs, B.probs.data(), B.probs.size() * sizeof(BProb), cudaMemcpyHostToDevice, s));
-  // k-means++: problems sorted by k descending, so those still drawing at
-  // step j are a prefix of the problems and their blocks a prefix of the
-  // blocks (of each width's list too)
-  std::vector<int> blocks_upto(B.count + 1, 0);
-  for (int q = 0; q < B.count; ++q) blocks_upto[q + 1] = blocks_upto[q] + B.probs[q].nb;
+  if (!B.chains_open) SC_TRY(begin_chains(B));
   const PPFar32 far = pp_far_bound32(kMaxBD);  // d = 64 bounds the far test of every width
-  // the initial means' sums and queue heads, and the Lloyd loop's count of
-  // running problems
-  SC_CUDA(cudaMemsetAsync(B.acc, 0, (size_t)B.kd * sizeof(Acc128), s));
-  SC_CUDA(cudaMemsetAsync(B.cnt, 0, (size_t)B.ksum * sizeof(unsigned long long), s));
   unsigned *seed_heads = B.heads + (size_t)kGraphIters * kNumD;
-  SC_CUDA(cudaMemsetAsync(seed_heads, 0, kNumD * sizeof(unsigned), s));
-  const int act = B.count;
-  SC_CUDA(cudaMemcpyAsync(B.active, &act, sizeof act, cudaMemcpyHostToDevice, s));
-  B.chains_open = false;
   if constexpr (sizeof(T) == 4) {
-    // One chain per width class (its problems, largest k first, and their
-    // blocks are prefixes of the class's lists at every draw): each draw's
-    // update and the class's selection, then the initial means of the
-    // seeding partition.  The chains run side by side on the classes'
-    // streams, widest first, and stay open: the class's Lloyd loop follows
+    // One chain per width class, on the class's stream after its rows (its
+    // problems, largest k first, and their blocks are prefixes of the
+    // class's lists at every draw): the scan of ||x||^2 and max |x|, the
+    // start values and scales, each draw's update and the class's
+    // selection, then the initial means of the seeding partition.  The
+    // chains run side by side and stay open: the class's Lloyd loop follows
     // on the same stream.
-    SC_TRY(ensure_side_streams(B));
-    EventSet ev;
-    SC_TRY(ev.create());
-    SC_CUDA(cudaEventRecord(ev.e[0], s));
-    for (int i = 0; i < 3; ++i) SC_CUDA(cudaStreamWaitEvent(B.side[i], ev.e[0], 0));
     const float *xf = (const float *)B.X;
     for (int dc = kNumD - 1; dc >= 0; --dc) {
       const int np = B.cls_poff[dc + 1] - B.cls_poff[dc];
@@ -1433,6 +1424,16 @@ sc_status run_setup(Batch &B) {
       const int32_t *dpl = B.d_cls_probs + B.cls_poff[dc];
       cudaStream_t cs = class_stream(B, dc);
       int ge = np, gt = np, nb = B.cls_off[dc + 1] - B.cls_off[dc];
+      switch (dc) {
+        case 0: batch_scan32_kernel<8><<<nb, kBlk, 0, cs>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
+        case 1: batch_scan32_kernel<16><<<nb, kBlk, 0, cs>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
+        case 2: batch_scan32_kernel<32><<<nb, kBlk, 0, cs>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
+        default: batch_scan32_kernel<64><<<nb, kBlk, 0, cs>>>(cb, B.d_block_prob, B.d_probs, xf, B.part, B.absmax); break;
+      }
+      SC_LAUNCHED();
+      batch_init_kernel<T><<<np, 64, 0, cs>>>(B.d_probs, np, B.st, B.part, B.d_first, (const T *)B.X,
+                                               (T *)B.seed_x, B.seed_idx, B.absmax, dpl);
+      SC_LAUNCHED();
       for (int j = 1; j <= B.probs[pl[0]].k; ++j) {
         while (ge > 0 && B.probs[pl[ge - 1]].k < j) nb -= B.probs[pl[--ge]].nb;
         while (gt > 0 && B.probs[pl[gt - 1]].k <= j) --gt;
@@ -1463,9 +1464,19 @@ sc_status run_setup(Batch &B) {
                                                   B.active, dpl);
       SC_LAUNCHED();
     }
-    B.chains_open = true;
     return SC_OK;
   } else {
+    SC_TRY(join_chains(B));  // the rows of every class, then the whole set-up on B.s
+    batch_scan_kernel<T><<<B.blocks, kBlk, 0, s>>>(B.d_block_prob, B.d_probs, (const T *)B.X, B.part, B.absmax);
+    SC_LAUNCHED();
+    batch_init_kernel<T><<<B.count, 64, 0, s>>>(B.d_probs, B.count, B.st, B.part, B.d_first, (const T *)B.X,
+                                               (T *)B.seed_x, B.seed_idx, B.absmax, nullptr);
+    SC_LAUNCHED();
+    // k-means++: problems sorted by k descending, so those still drawing at
+    // step j are a prefix of the problems and their blocks a prefix of the
+    // blocks
+    std::vector<int> blocks_upto(B.count + 1, 0);
+    for (int q = 0; q < B.count; ++q) blocks_upto[q + 1] = blocks_upto[q] + B.probs[q].nb;
     int q_ge = B.count, q_gt = B.count;
     for (int j = 1; j <= B.kmax; ++j) {
       while (q_ge > 0 && B.probs[q_ge - 1].k < j) --q_ge;
@@ -1483,13 +1494,13 @@ sc_status run_setup(Batch &B) {
         SC_LAUNCHED();
       }
     }
+    // initial means of the seeding partition
+    SC_TRY(launch_assign<T>(B, seed_heads, 1));
+    batch_finalize_kernel<<<B.count, kFinT, 0, s>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 1,
+                                                    B.active, nullptr);
+    SC_LAUNCHED();
+    return SC_OK;
   }
-  // initial means of the seeding partition
-  SC_TRY(launch_assign<T>(B, seed_heads, 1));
-  batch_finalize_kernel<<<B.count, kFinT, 0, s>>>(B.d_probs, B.st, B.acc, B.cnt, B.cent64, B.cent32, B.sizes, 1,
-                                                  B.active, nullptr);
-  SC_LAUNCHED();
-  return SC_OK;
 }
 
 // The Lloyd loop: per width class a graph of G = min(max_iter, 32)
@@ -1579,6 +1590,8 @@ void free_batch(Batch &B) {
     }
   if (B.mem) dev_free(B.mem, B.s);
   B.mem = nullptr;
+  if (B.d_jobs) dev_free(B.d_jobs, B.s);
+  B.d_jobs = nullptr;
   if (B.s) {
     cudaStreamSynchronize(B.s);
     cudaStreamDestroy(B.s);
@@ -1672,30 +1685,41 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
     if ((r = assign_grid(B, dtype)) != SC_OK) break;
     if ((r = upload_tables(B)) != SC_OK) break;
     trace.mark("alloc", B.s);
-    // rows into the padded layout
+    // Rows into the padded layout.  Column-major rows (a transpose through a
+    // staging buffer) go first on B.s; then, after the fork of the width
+    // classes' streams, each class's rows on its own stream, the widest
+    // class first and each class's copies after the previous class's, so
+    // that the widest class's set-up starts as soon as its rows are in.
+    // Rows in pinned, device-mapped host memory are read in place by one
+    // gather kernel per class; the others are copied.
     const size_t es = esz(dtype);
     if (B.needs_pad && cudaMemsetAsync(B.X, 0, (size_t)B.xelems * es, B.s) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "memset"); break; }
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
-    std::vector<CopyJob> jobs;  // rows the device reads in place
-    for (int q = 0; q < B.count && r == SC_OK; ++q) {
-      const sc_kmeans_problem &pr = problems[B.order[q]];
-      const BProb &P = B.probs[q];
-      char *dst = (char *)B.X + (size_t)P.x_off * es;
-      const void *src = pr.x;
-      size_t pitch = (size_t)pr.ld * es;
-      cudaMemcpyKind kind = cudaMemcpyHostToDevice;
-      const size_t bytes = (size_t)P.n * P.d * es;
-      if (pr.layout == SC_ROW_MAJOR && P.D == P.d && pitch == (size_t)P.d * es && bytes % 16 == 0) {
-        cudaPointerAttributes at;
-        if (cudaPointerGetAttributes(&at, pr.x) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer &&
-            ((uintptr_t)at.devicePointer & 15) == 0) {
-          jobs.push_back(CopyJob{(const uint4 *)at.devicePointer, (uint4 *)dst, (int64_t)(bytes / 16)});
+    std::vector<CopyJob> jobs;  // rows the device reads in place, by class
+    int jb[kNumD] = {}, je[kNumD] = {};  // class dc's jobs: [jb[dc], je[dc])
+    std::vector<char> copy_q(B.count, 0);  // row-major problems copied on their class's stream
+    for (int dc = kNumD - 1; dc >= 0 && r == SC_OK; --dc) {
+      jb[dc] = (int)jobs.size();
+      for (int i = B.cls_poff[dc]; i < B.cls_poff[dc + 1] && r == SC_OK; ++i) {
+        const int q = B.cls_probs[i];
+        const sc_kmeans_problem &pr = problems[B.order[q]];
+        const BProb &P = B.probs[q];
+        char *dst = (char *)B.X + (size_t)P.x_off * es;
+        const size_t pitch = (size_t)pr.ld * es, bytes = (size_t)P.n * P.d * es;
+        if (pr.layout == SC_ROW_MAJOR) {
+          if (P.D == P.d && pitch == (size_t)P.d * es && bytes % 16 == 0) {
+            cudaPointerAttributes at;
+            if (cudaPointerGetAttributes(&at, pr.x) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+                at.devicePointer && ((uintptr_t)at.devicePointer & 15) == 0) {
+              jobs.push_back(CopyJob{(const uint4 *)at.devicePointer, (uint4 *)dst, (int64_t)(bytes / 16)});
+              continue;
+            }
+            cudaGetLastError();  // an unregistered pointer leaves an error behind on some drivers
+          }
+          copy_q[q] = 1;
           continue;
         }
-        cudaGetLastError();  // an unregistered pointer leaves an error behind on some drivers
-      }
-      if (pr.layout == SC_COL_MAJOR) {
         // the columns as stored, then a transpose to rows on the device
         const size_t span = (size_t)((P.d - 1) * pr.ld + P.n) * es, span_al = (span + 255) & ~(size_t)255;
         const size_t need = span_al + (size_t)P.n * P.d * es;
@@ -1709,34 +1733,53 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
         char *rm = (char *)tmp + span_al;
         if (cudaMemcpyAsync(tmp, pr.x, span, cudaMemcpyHostToDevice, B.s) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "upload"); break; }
         if ((r = launch_to_row_major(dtype, tmp, P.n, P.d, pr.ld, rm, B.s)) != SC_OK) break;
-        src = rm;
-        pitch = (size_t)P.d * es;
-        kind = cudaMemcpyDeviceToDevice;
+        const cudaError_t e = P.D == P.d ? cudaMemcpyAsync(dst, rm, bytes, cudaMemcpyDeviceToDevice, B.s)
+                                         : cudaMemcpy2DAsync(dst, (size_t)P.D * es, rm, (size_t)P.d * es,
+                                                             (size_t)P.d * es, (size_t)P.n, cudaMemcpyDeviceToDevice, B.s);
+        if (e != cudaSuccess) r = cuda_fail(e, "upload");
       }
-      cudaError_t e;
-      if (P.D == P.d && pitch == (size_t)P.d * es)
-        e = cudaMemcpyAsync(dst, src, (size_t)P.n * P.d * es, kind, B.s);
-      else
-        e = cudaMemcpy2DAsync(dst, (size_t)P.D * es, src, pitch, (size_t)P.d * es, (size_t)P.n, kind, B.s);
-      if (e != cudaSuccess) r = cuda_fail(e, "upload");
+      je[dc] = (int)jobs.size();
     }
     if (tmp) dev_free(tmp, B.s);
-    if (r == SC_OK && !jobs.empty()) {
-      CopyJob *d_jobs = nullptr;
-      if ((r = dev_alloc((void **)&d_jobs, jobs.size() * sizeof(CopyJob), B.s)) == SC_OK) {
-        int dev = 0, sms = 0;
-        if (cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(CopyJob), cudaMemcpyHostToDevice, B.s) !=
-                cudaSuccess ||
-            cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-          r = cuda_fail(cudaGetLastError(), "upload");
-        } else {
-          gather_host_rows_kernel<<<4 * sms, 256, 0, B.s>>>(d_jobs, (int)jobs.size());
+    if (r != SC_OK) break;
+    if (!jobs.empty()) {
+      if ((r = dev_alloc((void **)&B.d_jobs, jobs.size() * sizeof(CopyJob), B.s)) != SC_OK) break;
+      if (cudaMemcpyAsync(B.d_jobs, jobs.data(), jobs.size() * sizeof(CopyJob), cudaMemcpyHostToDevice, B.s) !=
+          cudaSuccess) { r = cuda_fail(cudaGetLastError(), "upload"); break; }
+    }
+    if ((r = begin_chains(B)) != SC_OK) break;
+    {
+      int dev = 0, sms = 0;
+      EventSet ev;
+      if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        r = cuda_fail(cudaGetLastError(), "upload");
+        break;
+      }
+      if ((r = ev.create()) != SC_OK) break;
+      for (int dc = kNumD - 1; dc >= 0 && r == SC_OK; --dc) {
+        cudaStream_t cs = class_stream(B, dc);
+        if (dc < kNumD - 1 && cudaStreamWaitEvent(cs, ev.e[0], 0) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "upload"); break; }
+        for (int i = B.cls_poff[dc]; i < B.cls_poff[dc + 1] && r == SC_OK; ++i) {
+          const int q = B.cls_probs[i];
+          if (!copy_q[q]) continue;
+          const sc_kmeans_problem &pr = problems[B.order[q]];
+          const BProb &P = B.probs[q];
+          char *dst = (char *)B.X + (size_t)P.x_off * es;
+          const size_t pitch = (size_t)pr.ld * es;
+          const cudaError_t e = (P.D == P.d && pitch == (size_t)P.d * es)
+                                    ? cudaMemcpyAsync(dst, pr.x, (size_t)P.n * P.d * es, cudaMemcpyHostToDevice, cs)
+                                    : cudaMemcpy2DAsync(dst, (size_t)P.D * es, pr.x, pitch, (size_t)P.d * es,
+                                                        (size_t)P.n, cudaMemcpyHostToDevice, cs);
+          if (e != cudaSuccess) r = cuda_fail(e, "upload");
+        }
+        const int nj = je[dc] - jb[dc];
+        if (r == SC_OK && nj > 0) {
+          gather_host_rows_kernel<<<4 * sms, 256, 0, cs>>>(B.d_jobs + jb[dc], nj);
           note_launch();
           const cudaError_t le = cudaGetLastError();
           if (le != cudaSuccess) r = cuda_fail(le, "gather_host_rows_kernel");
         }
-        dev_free(d_jobs, B.s);
+        if (r == SC_OK && cudaEventRecord(ev.e[0], cs) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "upload");
       }
     }
     if (r != SC_OK) break;
@@ -1747,6 +1790,24 @@ sc_status sc_kmeans_fit_batched(sc_kmeans_problem *problems, int64_t count, int3
     r = dtype == SC_F32 ? run_lloyd<float>(B) : run_lloyd<double>(B);
     if (r != SC_OK) break;
     trace.mark("lloyd", B.s);
+    {  // non-finite input: an error, and no output written
+      std::vector<unsigned long long> am(B.count);
+      if (cudaMemcpyAsync(am.data(), B.absmax, am.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, B.s) !=
+              cudaSuccess ||
+          cudaStreamSynchronize(B.s) != cudaSuccess) {
+        r = cuda_fail(cudaGetLastError(), "results");
+        break;
+      }
+      for (int q = 0; q < B.count && r == SC_OK; ++q) {
+        double a;
+        memcpy(&a, &am[q], sizeof a);
+        if (!(a <= DBL_MAX)) {
+          set_error("problem %d: x contains NaN or infinity; the GPU path requires finite input", B.order[q]);
+          r = SC_ERR_INVALID;
+        }
+      }
+      if (r != SC_OK) break;
+    }
     // results back to the callers' buffers
     std::vector<double> cent((size_t)B.kd);
     std::vector<int64_t> sizes((size_t)B.ksum);

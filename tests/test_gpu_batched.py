@@ -164,6 +164,24 @@ def test_pinned_host_rows():
             assert np.array_equal(a.centroids, b.centroids, equal_nan=True)
 
 
+@pytest.mark.parametrize("bad", [np.nan, np.inf], ids=["nan", "inf"])
+def test_non_finite_rows_rejected(bad):
+    """A problem with a non-finite value fails the whole call with the
+    problem's index (the check runs on the device scan of max |x|); the next
+    call works."""
+    probs = batched_problems(count=6, seed0=80, n_range=(500, 5_000))
+    par = [(x.copy(), KMeansParameters(k=k, max_iter=10, seed=s)) for x, k, s in probs]
+    par[3][0][7, 1] = bad
+    from smartcore_gb300.error import Failed
+    with pytest.raises(Failed) as e:
+        KMeans.fit_many(par)
+    assert "problem 3: x contains NaN or infinity" in str(e.value)
+    par[3][0][7, 1] = 0.0
+    fits = KMeans.fit_many(par)
+    r = oracle.kmeans_fit(par[3][0], par[3][1].k, 10, seed=par[3][1].seed)
+    assert np.array_equal(fits[3]._y, r.labels)
+
+
 def test_validation_writes_nothing():
     x, _ = blobs(100, 4, 3, seed=1, dtype=np.float32)
     from smartcore_gb300.error import Failed
