@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <atomic>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -96,6 +97,33 @@ sc_status host_stage(size_t bytes, void **out) {
   }
   *out = g_stage;
   return SC_OK;
+}
+
+// memcpy of a large result out of the staging buffer, split over host
+// threads: the caller's freshly allocated pages are first touched (and
+// faulted in) by several cores at once.
+void stage_copy_out(void *dst, const void *src, size_t bytes) {
+  constexpr size_t kPerThread = 2u << 20;
+  const int nth = (int)std::min<size_t>({(size_t)std::max(1u, std::thread::hardware_concurrency()), 8,
+                                         bytes / kPerThread + 1});
+  if (nth <= 1) {
+    memcpy(dst, src, bytes);
+    return;
+  }
+  const size_t part = (bytes / nth + 63) & ~(size_t)63;
+  auto piece = [&](int t) {
+    const size_t a = std::min(bytes, (size_t)t * part), b = std::min(bytes, a + part);
+    if (b > a) memcpy((char *)dst + a, (const char *)src + a, b - a);
+  };
+  std::vector<std::thread> pool;
+  int started = 1;
+  try {
+    for (; started < nth; ++started) pool.emplace_back(piece, started);
+  } catch (...) {  // no more threads: the rest on this one
+    for (int t = started; t < nth; ++t) piece(t);
+  }
+  piece(0);
+  for (auto &th : pool) th.join();
 }
 
 namespace {
@@ -505,7 +533,7 @@ sc_status sc_kmeans_get(sc_kmeans *h, double *centroids, int64_t *sizes, int64_t
   LloydState st;
   SC_CUDA(cudaMemcpyAsync(&st, h->st, sizeof st, cudaMemcpyDeviceToHost, s));
   SC_CUDA(cudaStreamSynchronize(s));
-  if (stage) memcpy(labels, stage, label_bytes);
+  if (stage) stage_copy_out(labels, stage, label_bytes);
   if (distortion) *distortion = st.distortion;
   if (iters) *iters = st.iters;
   return SC_OK;

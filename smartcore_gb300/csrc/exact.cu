@@ -639,7 +639,9 @@ pp_select_kernel(const T *__restrict__ x, int d, const double *__restrict__ dd,
                  const double *__restrict__ part, int64_t n, int nb,
                  const double *__restrict__ uniform, LloydState *st,
                  T *__restrict__ seed_x, float *__restrict__ seed_cc, int j) {
-  constexpr int kScan = kSelThreads;  // threads that sum chunks of the partials
+  // threads that sum chunks of the partials: fewer than the CTA, since the
+  // scan's FP64 additions (a narrow pipe) cost more than its longer chains
+  constexpr int kScan = 256;
   __shared__ double s_incl[kScan];  // inclusive prefix of the chunk sums
   __shared__ double s_wtot[32];
   __shared__ int s_chunk;
