@@ -876,6 +876,18 @@ __global__ void fastpair_kernel(const T *__restrict__ x, int64_t n, int d, int l
       const int64_t j = r0 + r;
       if (j <= i) continue;
       const T *tr = ts + r * d;
+      if constexpr (sizeof(T) == 4) {
+        // The terms fl32((x_c - y_c)^2) summed in f32 bound the reference's
+        // f64 sum from below by s32 (1 - 1.05 d 2^-24): at or above the
+        // running best the row cannot replace it, and its exact value is
+        // not needed (almost every pair once the best is close).
+        float s32 = 0.f;
+        for (int c = 0; c < d; ++c) {
+          const float df = __fsub_rn(qs[c * nt + tid], tr[c]);
+          s32 = __fadd_rn(s32, __fmul_rn(df, df));
+        }
+        if (__fmul_rd(s32, 1.f - 1.05f * d * 0x1p-24f) >= best) continue;
+      }
       // Euclidian::squared_distance (euclidian.rs:51-63) in the reference's
       // order; f32 rows by the integer reproduction of the sequential sum
       double s = 0.0;
