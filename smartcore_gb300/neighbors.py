@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import enum
+from collections.abc import Mapping
 from dataclasses import dataclass
 
 import numpy as np
@@ -219,6 +220,26 @@ class PairwiseDistance:
     distance: Optional[float]
 
 
+class _NeighbourMap(Mapping):
+    """Row -> PairwiseDistance over the device's neighbour arrays, each entry
+    built when it is read (a map of n entries up front costs more than the
+    scan itself)."""
+
+    def __init__(self, nb, dist):
+        self._nb, self._dist = nb, dist
+
+    def __getitem__(self, i):
+        if not 0 <= i < len(self._nb):
+            raise KeyError(i)
+        return PairwiseDistance(i, int(self._nb[i]), float(self._dist[i]))
+
+    def __len__(self):
+        return len(self._nb)
+
+    def __iter__(self):
+        return iter(range(len(self._nb)))
+
+
 class FastPair:
     """FastPair::new / closest_pair (src/algorithm/neighbour/fastpair.rs:59-182).
 
@@ -242,7 +263,7 @@ class FastPair:
                        FailedError.FindFailed)
         finally:
             s.close()
-        self.distances = {i: PairwiseDistance(i, int(nb[i]), float(dist[i])) for i in range(n)}
+        self.distances = _NeighbourMap(nb, dist)
         self.neighbours = list(range(n))
         self._closest = PairwiseDistance(int(pair[0]), int(pair[1]), float(pd[0]))
 
