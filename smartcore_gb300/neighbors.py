@@ -48,6 +48,7 @@ class LinearKNNSearch:
         h = C.c_void_p()
         _lib.check(L.sc_knn_create(_lib.ptr(a), dt, lay, _lib.MEM_HOST, self.n, self.d, ld, C.byref(h)))
         self._L, self.h, self.form = L, h, form
+        self._per_query = 64.0  # find_radius: rows per query of the previous call, for the output's first size
 
     def _q(self, queries):
         a = as_matrix(queries, dtype=self.dtype)
@@ -74,22 +75,31 @@ class LinearKNNSearch:
 
     def find_radius_batch(self, queries, radius):
         """find_radius() for every row of queries: (counts, idx, dist), the
-        rows of query 0 first, each query's rows in index order."""
+        rows of query 0 first, each query's rows in index order.  The output
+        is sized from the previous call's rows per query, so one call (a
+        counting and a filling pass) usually serves; when the rows do not
+        fit, a second call with the exact size does."""
         a = self._q(queries)
         m = a.shape[0]
         lay, ld = layout_of(a)
         counts = np.zeros(max(m, 1), np.int64)
         total = np.zeros(1, np.int64)
-        _lib.check(self._L.sc_knn_find_radius(self.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, float(radius),
-                                              self.form, _lib.ptr(counts), 0, None, None, _lib.ptr(total)),
-                   FailedError.FindFailed)
+        cap = max(1024, int(1.25 * self._per_query * m))
+        idx = np.empty(cap, np.int64)
+        dist = np.empty(cap, np.float64)
+        rc = self._L.sc_knn_find_radius(self.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, float(radius), self.form,
+                                        _lib.ptr(counts), cap, _lib.ptr(idx), _lib.ptr(dist), _lib.ptr(total))
         t = int(total[0])
-        idx = np.zeros(max(t, 1), np.int64)
-        dist = np.zeros(max(t, 1), np.float64)
-        if t:
+        if rc != _lib.SC_OK and not (rc == _lib.SC_ERR_INVALID and t > cap):
+            _lib.check(rc, FailedError.FindFailed)
+        if t > cap:  # more rows than the first size: the exact size
+            idx = np.empty(t, np.int64)
+            dist = np.empty(t, np.float64)
             _lib.check(self._L.sc_knn_find_radius(self.h, _lib.ptr(a), lay, _lib.MEM_HOST, m, ld, float(radius),
                                                   self.form, _lib.ptr(counts), t, _lib.ptr(idx), _lib.ptr(dist),
                                                   _lib.ptr(total)), FailedError.FindFailed)
+        if m:
+            self._per_query = max(1.0, t / m)
         return counts[:m], idx[:t], dist[:t]
 
     def find_radius(self, from_, radius):

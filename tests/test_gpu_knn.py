@@ -86,6 +86,12 @@ def test_find_radius_matches_oracle(form, dtype):
         assert np.array_equal(counts, rc) and np.array_equal(idx, ridx) and np.array_equal(dist, rdist)
     assert s.find_radius(q[0], 1.5) == [(int(i), float(d)) for i, d in
                                         zip(*oracle.knn_find_radius(train, q[:1], 1.5)[1:])]
+    # every row inside the radius: more rows than the first output size, so a
+    # second call with the exact size serves
+    counts, idx, dist = s.find_radius_batch(q, 100.0)
+    rc, ridx, rdist = oracle.knn_find_radius(train, q, 100.0)
+    assert np.array_equal(counts, rc) and counts.sum() == len(q) * len(train)
+    assert np.array_equal(idx, ridx) and np.array_equal(dist, rdist)
     with pytest.raises(Failed, match="radius should be > 0"):
         s.find_radius(q[0], 0.0)
 
