@@ -244,18 +244,26 @@ class LinearKNNSearch {
 
   // find_radius() for one query (linear_search.rs:89-108): (index, distance)
   // of every row with distance <= radius, in index order.
+  // The output is sized from the previous call's row count, so one library
+  // call (a counting and a filling pass) usually serves; when the rows do not
+  // fit, a second call with the exact size does.
   std::vector<std::pair<size_t, double>> find_radius(const std::vector<T> &from, double radius) const {
     if (from.size() != d_) throw std::invalid_argument("Input vector sizes are different.");
     int64_t count = 0, total = 0;
-    detail::check(sc_knn_find_radius(h_, from.data(), SC_ROW_MAJOR, SC_MEM_HOST, 1, (int64_t)d_, radius,
-                                     (int32_t)form_, &count, 0, nullptr, nullptr, &total),
-                  FailedError::FindFailed);
-    std::vector<int64_t> idx(total ? total : 1);
-    std::vector<double> dist(total ? total : 1);
-    if (total)
+    const int64_t cap = (int64_t)radius_rows_;
+    std::vector<int64_t> idx((size_t)cap);
+    std::vector<double> dist((size_t)cap);
+    const sc_status st = sc_knn_find_radius(h_, from.data(), SC_ROW_MAJOR, SC_MEM_HOST, 1, (int64_t)d_, radius,
+                                            (int32_t)form_, &count, cap, idx.data(), dist.data(), &total);
+    if (st != SC_OK && !(st == SC_ERR_INVALID && total > cap)) detail::check(st, FailedError::FindFailed);
+    if (total > cap) {
+      idx.resize((size_t)total);
+      dist.resize((size_t)total);
       detail::check(sc_knn_find_radius(h_, from.data(), SC_ROW_MAJOR, SC_MEM_HOST, 1, (int64_t)d_, radius,
                                        (int32_t)form_, &count, total, idx.data(), dist.data(), &total),
                     FailedError::FindFailed);
+    }
+    radius_rows_ = std::max<size_t>(64, (size_t)(total + total / 4 + 1));
     std::vector<std::pair<size_t, double>> out;
     for (int64_t s = 0; s < total; ++s) out.emplace_back((size_t)idx[s], dist[s]);
     return out;
@@ -269,6 +277,7 @@ class LinearKNNSearch {
   sc_knn *h_ = nullptr;
   Form form_;
   size_t n_ = 0, d_ = 0;
+  mutable size_t radius_rows_ = 256;  // find_radius: the output's first size
 };
 
 // KNNClassifierParameters (src/neighbors/knn_classifier.rs:48-69, :144-154).
