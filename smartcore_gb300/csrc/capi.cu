@@ -779,6 +779,23 @@ static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double ra
   if (m == 0) return SC_OK;
   int64_t *dcnt = nullptr, *doff = nullptr, *didx = nullptr;
   double *ddist = nullptr;
+  if (form == SC_FORM_SPLIT_BF16) {  // usually one pass
+    sc_status r = split_knn_radius_lists(&h->split, h->dtype, h->train, h->n, (int)h->d, q_dev, m, radius, off,
+                                         &didx, &ddist, h->stream);
+    if (r == SC_OK) {
+      const int64_t total = off[(size_t)m];
+      idx.resize((size_t)total);
+      if (total > 0 && (cudaMemcpyAsync(idx.data(), didx, (size_t)total * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                        h->stream) != cudaSuccess ||
+                        cudaStreamSynchronize(h->stream) != cudaSuccess))
+        r = cuda_fail(cudaGetLastError(), "radius lists");
+      dfree(didx, h->stream);
+      dfree(ddist, h->stream);
+      return r;
+    }
+    if (r != SC_ERR_INVALID) return r;
+    off.assign((size_t)m + 1, 0);  // too many queries for the slots: count, then fill
+  }
   sc_status r = SC_OK;
   do {
     if ((r = dalloc(&dcnt, (size_t)m, h->stream)) != SC_OK || (r = dalloc(&doff, (size_t)m, h->stream)) != SC_OK) break;
@@ -967,6 +984,36 @@ sc_status sc_knn_find_radius(sc_knn *h, const void *queries, int32_t layout, int
   sc_status r = SC_OK;
   std::vector<int64_t> cnt((size_t)m);
   int64_t total = 0;
+  if (form == SC_FORM_SPLIT_BF16 && (idx_out || dist_out)) {  // usually one pass: counts and rows together
+    std::vector<int64_t> off;
+    r = split_knn_radius_lists(&h->split, h->dtype, h->train, h->n, (int)h->d, h->q, m, radius, off, &didx, &ddist,
+                               h->stream);
+    if (r == SC_OK) {
+      total = off[(size_t)m];
+      for (int64_t q = 0; q < m; ++q) cnt[(size_t)q] = off[(size_t)q + 1] - off[(size_t)q];
+      if (counts_out) memcpy(counts_out, cnt.data(), (size_t)m * sizeof(int64_t));
+      if (total_out) *total_out = total;
+      if (capacity < total) {
+        set_error("capacity %lld is smaller than the %lld neighbours found", (long long)capacity, (long long)total);
+        r = SC_ERR_INVALID;
+      } else if (total > 0 &&
+                 ((idx_out && cudaMemcpyAsync(idx_out, didx, (size_t)total * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                              h->stream) != cudaSuccess) ||
+                  (dist_out && cudaMemcpyAsync(dist_out, ddist, (size_t)total * sizeof(double),
+                                               cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) ||
+                  cudaStreamSynchronize(h->stream) != cudaSuccess)) {
+        r = cuda_fail(cudaGetLastError(), "find_radius results");
+      }
+      cudaStreamSynchronize(h->stream);
+      dfree(didx, h->stream);
+      dfree(ddist, h->stream);
+      return r;
+    }
+    if (r != SC_ERR_INVALID) return r;
+    r = SC_OK;  // too many queries for the slots: count, then fill
+    didx = nullptr;
+    ddist = nullptr;
+  }
   do {
     if ((r = dalloc(&dcnt, (size_t)m, h->stream)) != SC_OK || (r = dalloc(&doff, (size_t)m, h->stream)) != SC_OK) break;
     // counting pass

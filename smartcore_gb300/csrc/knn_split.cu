@@ -110,12 +110,14 @@ struct KnnParams {
   unsigned long long *evals;
   int *err;
   // find_radius (linear_search.rs:89-108): rows with sqrt(D) <= radius, in
-  // index order; counts per query (counting pass, idx_out == nullptr) or the
-  // rows from offsets[q] on (filling pass)
+  // index order; counts per query (counting pass, idx_out == nullptr), the
+  // rows from offsets[q] on (filling pass), or both at once (slot pass:
+  // counts, and the first cap_q rows of query q from slot q * cap_q on)
   int radius_mode;
   double radius, r2up;  // r2up >= every D whose sqrt rounds to <= radius
   int64_t *counts;
   const int64_t *offsets;
+  int64_t cap_q;
 };
 
 // The reference keys its heap on d = sqrt(D) (f64).  The heap here holds D
@@ -481,7 +483,8 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       // row j can enter only if acc_j >= lo = -thr / 2 (thr = root^2 - ||q||^2 + e)
       float lo = live ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000);
       s_lo[row] = lo;
-      int64_t rc = 0, rpos = p.radius_mode && p.idx_out && live ? p.offsets[q] : 0;  // find_radius
+      int64_t rc = 0, rpos = 0;  // find_radius: rows found, next output position
+      if (p.radius_mode && p.idx_out && live) rpos = p.offsets ? p.offsets[q] : q * p.cap_q;
       uint32_t qhead = 0, qtail = 0;  // warp-uniform queue cursors
       const int64_t qbase = (int64_t)qt * kQM + lq * 32;
       // one round: exact distances of up to 32 queued entries, then the owners' heap steps
@@ -532,7 +535,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
           if (p.radius_mode) {  // linear_search.rs:100-104: d <= radius, appended in index order
             const double dist = __dsqrt_rn(sr);
             if (dist <= p.radius) {
-              if (p.idx_out) {
+              if (p.idx_out && (p.offsets || rc < p.cap_q)) {
                 p.idx_out[rpos] = Rj[r];
                 p.dist_out[rpos] = dist;
                 ++rpos;
@@ -613,7 +616,7 @@ knn_split_kernel(const __grid_constant__ CUtensorMap tm_qh, const __grid_constan
       }
       while (!stop && qtail != qhead) round(min(32u, qtail - qhead));
       if (p.radius_mode) {
-        if (live && !stop && !p.idx_out) p.counts[q] = rc;
+        if (live && !stop && p.counts) p.counts[q] = rc;
       } else if (live && !stop)
         for (int s = 0; s < p.k; ++s) {
           p.idx_out[q * p.k + s] = hi[s * HS];
@@ -1219,8 +1222,9 @@ sc_status launch_knn_split(int grid, size_t smem, const CUtensorMap &tm_qh, cons
 namespace {
 struct RadiusArgs {
   double radius;
-  int64_t *counts;         // counting pass (idx == nullptr)
+  int64_t *counts;         // counting pass (idx == nullptr), or slot pass
   const int64_t *offsets;  // filling pass
+  int64_t cap_q;           // slot pass: rows kept per query (offsets == nullptr)
 };
 
 struct RadiusArgs;
@@ -1495,6 +1499,7 @@ sc_status run_split_knn(SplitKnnState *s, int dtype, const void *train, int64_t 
     p.r2up = rad->radius * rad->radius * (1.0 + 0x1p-48);  // covers every D with sqrt(D) rounding to <= radius
     p.counts = rad->counts;
     p.offsets = rad->offsets;
+    p.cap_q = rad->cap_q;
   }
   p.evals = s->evals;
   p.err = (int *)(s->evals + 1);
@@ -1542,8 +1547,117 @@ sc_status split_knn(SplitKnnState *s, int dtype, const void *train, int64_t n, i
 sc_status split_knn_radius(SplitKnnState *s, int dtype, const void *train, int64_t n, int d, const void *queries,
                            int64_t m, double radius, int64_t *counts, const int64_t *offsets, int64_t *idx,
                            double *dist, cudaStream_t st) {
-  const RadiusArgs rad{radius, counts, offsets};
+  const RadiusArgs rad{radius, counts, offsets, 0};
   return run_split_knn(s, dtype, train, n, d, queries, m, 0, idx, dist, nullptr, &rad, st);
+}
+
+namespace {
+// Row q's first min(counts[q], cap) slots of the slot pass to its place in
+// the packed lists, one warp per query.
+__global__ void pack_radius_kernel(const int64_t *__restrict__ pad_idx, const double *__restrict__ pad_dist,
+                                   int64_t cap, const int64_t *__restrict__ counts, const int64_t *__restrict__ off,
+                                   int64_t m, int64_t *__restrict__ idx, double *__restrict__ dist) {
+  const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (q >= m) return;
+  const int64_t c = counts[q] < cap ? counts[q] : cap, o = off[q];
+  for (int64_t e = lane; e < c; e += 32) {
+    idx[o + e] = pad_idx[q * cap + e];
+    dist[o + e] = pad_dist[q * cap + e];
+  }
+}
+}  // namespace
+
+// find_radius lists of m device queries in one pass in the usual case: the
+// slot pass keeps each query's first kRadiusSlots rows and counts them all;
+// the packed lists (CSR: off, m + 1 entries on the host; idx / dist on the
+// device, allocated here) take the kept rows, and the queries with more
+// rows than slots run the filling pass alone, writing their whole lists in
+// place.  Returns SC_ERR_INVALID (nothing allocated) when the slots of m
+// queries would take more than 2 GB; the caller then counts and fills.
+sc_status split_knn_radius_lists(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
+                                 const void *queries, int64_t m, double radius, std::vector<int64_t> &off,
+                                 int64_t **idx_out, double **dist_out, cudaStream_t st) {
+  constexpr int64_t kRadiusSlots = 128;
+  *idx_out = nullptr;
+  *dist_out = nullptr;
+  off.assign((size_t)m + 1, 0);
+  if (m == 0) return SC_OK;
+  if (m * kRadiusSlots * 16 > ((int64_t)1 << 31)) return SC_ERR_INVALID;
+  int64_t *pad_idx = nullptr, *cnt = nullptr, *doff = nullptr, *oidx = nullptr, *sub_off = nullptr;
+  double *pad_dist = nullptr, *odist = nullptr;
+  int32_t *sub_rows = nullptr;
+  char *sub_q = nullptr;
+  sc_status r = SC_OK;
+  do {
+    if ((r = dalloc(&pad_idx, (size_t)(m * kRadiusSlots), st)) != SC_OK ||
+        (r = dalloc(&pad_dist, (size_t)(m * kRadiusSlots), st)) != SC_OK || (r = dalloc(&cnt, (size_t)m, st)) != SC_OK ||
+        (r = dalloc(&doff, (size_t)m, st)) != SC_OK)
+      break;
+    if (cudaMemsetAsync(cnt, 0, (size_t)m * sizeof(int64_t), st) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "memset");
+      break;
+    }
+    const RadiusArgs rad{radius, cnt, nullptr, kRadiusSlots};
+    if ((r = run_split_knn(s, dtype, train, n, d, queries, m, 0, pad_idx, pad_dist, nullptr, &rad, st)) != SC_OK) break;
+    std::vector<int64_t> c((size_t)m);
+    if (cudaMemcpyAsync(c.data(), cnt, (size_t)m * sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "radius counts");
+      break;
+    }
+    std::vector<int32_t> over;
+    for (int64_t q = 0; q < m; ++q) {
+      off[(size_t)q + 1] = off[(size_t)q] + c[(size_t)q];
+      if (c[(size_t)q] > kRadiusSlots) over.push_back((int32_t)q);
+    }
+    const int64_t total = off[(size_t)m];
+    if (total == 0) break;
+    if ((r = dalloc(&oidx, (size_t)total, st)) != SC_OK || (r = dalloc(&odist, (size_t)total, st)) != SC_OK) break;
+    if (cudaMemcpyAsync(doff, off.data(), (size_t)m * sizeof(int64_t), cudaMemcpyHostToDevice, st) != cudaSuccess) {
+      r = cuda_fail(cudaGetLastError(), "radius offsets");
+      break;
+    }
+    pack_radius_kernel<<<(int)((m * 32 + 255) / 256), 256, 0, st>>>(pad_idx, pad_dist, kRadiusSlots, cnt, doff, m,
+                                                                     oidx, odist);
+    if (cudaGetLastError() != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "pack_radius_kernel"); break; }
+    note_launch();
+    if (!over.empty()) {  // their whole lists, written at their offsets
+      const int64_t no = (int64_t)over.size();
+      const size_t es = dtype == SC_F32 ? 4 : 8;
+      std::vector<int64_t> so((size_t)no);
+      for (int64_t i = 0; i < no; ++i) so[(size_t)i] = off[(size_t)over[(size_t)i]];
+      if ((r = dalloc(&sub_rows, (size_t)no, st)) != SC_OK || (r = dalloc(&sub_off, (size_t)no, st)) != SC_OK ||
+          (r = dalloc(&sub_q, (size_t)no * d * es, st)) != SC_OK)
+        break;
+      if (cudaMemcpyAsync(sub_rows, over.data(), (size_t)no * sizeof(int32_t), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+          cudaMemcpyAsync(sub_off, so.data(), (size_t)no * sizeof(int64_t), cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        r = cuda_fail(cudaGetLastError(), "radius overflow");
+        break;
+      }
+      const int gb = (int)((no * d + 255) / 256);
+      if (dtype == SC_F32)
+        gather_rows_kernel<float><<<gb, 256, 0, st>>>((const float *)queries, sub_rows, no, d, (float *)sub_q);
+      else
+        gather_rows_kernel<double><<<gb, 256, 0, st>>>((const double *)queries, sub_rows, no, d, (double *)sub_q);
+      if (cudaGetLastError() != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "gather_rows_kernel"); break; }
+      note_launch();
+      const RadiusArgs fill{radius, nullptr, sub_off, 0};
+      if ((r = run_split_knn(s, dtype, train, n, d, sub_q, no, 0, oidx, odist, nullptr, &fill, st)) != SC_OK) break;
+      // sync before the host vectors above (copied from pageable memory) go
+      if (cudaStreamSynchronize(st) != cudaSuccess) { r = cuda_fail(cudaGetLastError(), "radius overflow"); break; }
+    }
+  } while (0);
+  dfree(pad_idx, st); dfree(pad_dist, st); dfree(cnt, st); dfree(doff, st);
+  dfree(sub_rows, st); dfree(sub_off, st); dfree(sub_q, st);
+  if (r != SC_OK) {
+    dfree(oidx, st);
+    dfree(odist, st);
+    return r;
+  }
+  *idx_out = oidx;
+  *dist_out = odist;
+  return SC_OK;
 }
 
 void split_knn_free(SplitKnnState *s, cudaStream_t st) {

@@ -2,6 +2,8 @@
 // error bound, FP64 re-score of every decision inside the bound.
 #pragma once
 
+#include <vector>
+
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -82,6 +84,13 @@ constexpr int kSplitKMeansMaxD = 128;
 sc_status split_knn_radius(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
                            const void *queries, int64_t m, double radius, int64_t *counts,
                            const int64_t *offsets, int64_t *idx, double *dist, cudaStream_t st);
+// find_radius lists of m device queries, usually in one pass: CSR offsets
+// (m + 1, host) and device arrays idx / dist allocated here (dfree them).
+// SC_ERR_INVALID with nothing allocated when m is too large for the slots;
+// the caller then runs the counting and filling passes.
+sc_status split_knn_radius_lists(SplitKnnState *s, int dtype, const void *train, int64_t n, int d,
+                                 const void *queries, int64_t m, double radius, std::vector<int64_t> &off,
+                                 int64_t **idx, double **dist, cudaStream_t st);
 void split_knn_free(SplitKnnState *s, cudaStream_t st);
 
 }  // namespace sc
