@@ -126,3 +126,40 @@ def test_batch_tune_rejects_foreign_files(L, tmp_path):
     assert L.sc_batch_tune_load(str(p).encode()) == _lib.SC_ERR_INVALID
     assert L.sc_batch_tune_load(str(tmp_path / "missing.txt").encode()) == _lib.SC_ERR_INVALID
     assert L.sc_batch_tune_get(200, 5, None, None) == _lib.SC_ERR_INVALID
+
+
+def test_batch_variant_override(L):
+    """sc_debug_batch_variant accepts the assignment variants (2, 4, 8) and -1
+    (the tuning table's choice), rejects anything else, and is what
+    sc_batch_tune_get reports while it is set."""
+    assert L.sc_debug_batch_variant(3) == _lib.SC_ERR_INVALID
+    assert "unknown batched assignment variant 3" in _lib.last_error()
+    cu, rows = np.zeros(1, np.int32), np.zeros(1, np.int32)
+    try:
+        for v in (2, 4, 8):
+            _lib.check(L.sc_debug_batch_variant(v))
+            _lib.check(L.sc_batch_tune_get(32, 16, _lib.ptr(cu), _lib.ptr(rows)))
+            assert int(cu[0]) == v and int(rows[0]) in (1024, 2048, 4096)
+    finally:
+        _lib.check(L.sc_debug_batch_variant(-1))
+
+
+def test_problem_record_matches_the_c_struct():
+    """KMeans.fit_many fills the problem table as NumPy columns: the record's
+    fields sit where sc_kmeans_problem's do."""
+    from smartcore_gb300.cluster import PROBLEM_DTYPE
+    assert PROBLEM_DTYPE.itemsize == C.sizeof(_lib.KMeansProblem)
+    for name in PROBLEM_DTYPE.names:
+        assert PROBLEM_DTYPE.fields[name][1] == getattr(_lib.KMeansProblem, name).offset
+
+
+def test_fastpair_neighbour_map():
+    """FastPair.distances reads like the reference's HashMap of
+    PairwiseDistance, each entry built from the neighbour arrays on access."""
+    from smartcore_gb300.neighbors import PairwiseDistance, _NeighbourMap
+    m = _NeighbourMap(np.array([2, 2, 2]), np.array([0.25, 1.5, 3.4e38]))
+    assert len(m) == 3 and list(m) == [0, 1, 2]
+    assert m[1] == PairwiseDistance(1, 2, 1.5)
+    assert dict(m)[2] == PairwiseDistance(2, 2, 3.4e38)
+    with pytest.raises(KeyError):
+        m[3]
