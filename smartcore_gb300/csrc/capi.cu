@@ -667,6 +667,8 @@ struct sc_knn {
   int64_t aux_cap = 0;
   int64_t rescored = 0;
   SplitKnnState split;
+  int64_t *lists = nullptr;  // pinned host: the last radius lists' row indices
+  size_t lists_cap = 0;
 };
 
 static sc_status knn_reserve(sc_knn *h, int64_t m, int64_t k) {
@@ -718,6 +720,7 @@ void sc_knn_destroy(sc_knn *h) {
     cudaStreamSynchronize(h->stream);
     cudaStreamDestroy(h->stream);
   }
+  if (h->lists) cudaFreeHost(h->lists);
   delete h;
 }
 
@@ -769,13 +772,27 @@ sc_status sc_knn_find(sc_knn *h, const void *queries, int32_t layout, int32_t me
 
 }  // extern "C"
 
+// Pinned host room for `count` row indices in the handle (grows, kept until
+// the handle goes): device copies into it run at the link's speed.
+static sc_status lists_room(sc_knn *h, int64_t count) {
+  if ((size_t)count > h->lists_cap) {
+    if (h->lists) cudaFreeHost(h->lists);
+    h->lists = nullptr;
+    h->lists_cap = 0;
+    SC_CUDA(cudaHostAlloc((void **)&h->lists, (size_t)count * sizeof(int64_t), cudaHostAllocDefault));
+    h->lists_cap = (size_t)count;
+  }
+  return SC_OK;
+}
+
 // Rows of the handle's training set within `radius` of each of m device
-// query rows (row-major), in index order: CSR lists off (m + 1) and idx.
+// query rows (row-major), in index order: CSR lists off (m + 1) and *idx,
+// which points into the handle's pinned buffer until its next radius search.
 static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double radius, int32_t form,
-                              std::vector<int64_t> &off, std::vector<int64_t> &idx) {
+                              std::vector<int64_t> &off, const int64_t **idx_out) {
   if (form == SC_FORM_SPLIT_BF16 && !split_knn_serves((int)h->d, 1, h->dtype, true)) form = SC_FORM_FP64;
   off.assign((size_t)m + 1, 0);
-  idx.clear();
+  *idx_out = nullptr;
   if (m == 0) return SC_OK;
   int64_t *dcnt = nullptr, *doff = nullptr, *didx = nullptr;
   double *ddist = nullptr;
@@ -784,11 +801,14 @@ static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double ra
                                          &didx, &ddist, h->stream);
     if (r == SC_OK) {
       const int64_t total = off[(size_t)m];
-      idx.resize((size_t)total);
-      if (total > 0 && (cudaMemcpyAsync(idx.data(), didx, (size_t)total * sizeof(int64_t), cudaMemcpyDeviceToHost,
-                                        h->stream) != cudaSuccess ||
-                        cudaStreamSynchronize(h->stream) != cudaSuccess))
-        r = cuda_fail(cudaGetLastError(), "radius lists");
+      if (total > 0 && (r = lists_room(h, total)) == SC_OK) {
+        if (cudaMemcpyAsync(h->lists, didx, (size_t)total * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(h->stream) != cudaSuccess)
+          r = cuda_fail(cudaGetLastError(), "radius lists");
+        *idx_out = h->lists;
+      }
+      cudaStreamSynchronize(h->stream);
       dfree(didx, h->stream);
       dfree(ddist, h->stream);
       return r;
@@ -814,7 +834,7 @@ static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double ra
     for (int64_t q = 0; q < m; ++q) off[(size_t)q + 1] += off[(size_t)q];
     const int64_t total = off[(size_t)m];
     if (total == 0) break;
-    idx.resize((size_t)total);
+    if ((r = lists_room(h, total)) != SC_OK) break;
     if ((r = dalloc(&didx, (size_t)total, h->stream)) != SC_OK || (r = dalloc(&ddist, (size_t)total, h->stream)) != SC_OK) break;
     if (cudaMemcpyAsync(doff, off.data(), (size_t)m * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream) !=
         cudaSuccess) {
@@ -827,12 +847,13 @@ static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double ra
             : split_knn_radius(&h->split, h->dtype, h->train, h->n, (int)h->d, q_dev, m, radius, nullptr, doff,
                                didx, ddist, h->stream);
     if (r != SC_OK) break;
-    if (cudaMemcpyAsync(idx.data(), didx, (size_t)total * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream) !=
+    if (cudaMemcpyAsync(h->lists, didx, (size_t)total * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream) !=
             cudaSuccess ||
         cudaStreamSynchronize(h->stream) != cudaSuccess) {
       r = cuda_fail(cudaGetLastError(), "radius lists");
       break;
     }
+    *idx_out = h->lists;
   } while (0);
   cudaStreamSynchronize(h->stream);
   dfree(dcnt, h->stream); dfree(doff, h->stream); dfree(didx, h->stream); dfree(ddist, h->stream);
@@ -844,7 +865,7 @@ static sc_status radius_lists(sc_knn *h, const void *q_dev, int64_t m, double ra
 // row, so computing all of them first changes nothing): the same marks
 // (undefined -3, queued -2, outlier -1), the same LIFO stack of neighbours and
 // the same order of visits.  Returns the number of clusters.
-static int64_t dbscan_expand(int64_t n, const std::vector<int64_t> &off, const std::vector<int64_t> &idx,
+static int64_t dbscan_expand(int64_t n, const std::vector<int64_t> &off, const int64_t *idx,
                              int64_t min_samples, int64_t *y) {
   const int64_t queued = -2, outlier = -1, undefined = -3;
   for (int64_t i = 0; i < n; ++i) y[i] = undefined;
@@ -852,7 +873,7 @@ static int64_t dbscan_expand(int64_t n, const std::vector<int64_t> &off, const s
   std::vector<int64_t> stack;
   for (int64_t i = 0; i < n; ++i) {
     if (y[i] != undefined) continue;
-    const int64_t *nb = idx.data() + off[(size_t)i];
+    const int64_t *nb = idx + off[(size_t)i];
     const int64_t nn = off[(size_t)i + 1] - off[(size_t)i];
     if (nn < min_samples) {
       y[i] = outlier;
@@ -868,7 +889,7 @@ static int64_t dbscan_expand(int64_t n, const std::vector<int64_t> &off, const s
       if (y[index] == outlier) y[index] = k;
       if (y[index] == undefined || y[index] == queued) {
         y[index] = k;
-        const int64_t *sec = idx.data() + off[(size_t)index];
+        const int64_t *sec = idx + off[(size_t)index];
         const int64_t ns = off[(size_t)index + 1] - off[(size_t)index];
         if (ns >= min_samples) {
           for (int64_t j = 0; j < ns; ++j) {
@@ -893,8 +914,9 @@ sc_status sc_dbscan_fit(sc_knn *h, double eps, int64_t min_samples, int32_t form
   if (!(eps > 0.0)) { set_error("Invalid radius: "); return SC_ERR_INVALID; }   // dbscan.rs:282-284
   if (form != SC_FORM_FP64 && form != SC_FORM_SPLIT_BF16) { set_error("unknown form %d", form); return SC_ERR_INVALID; }
   if (!labels_out && h->n > 0) { set_error("null labels"); return SC_ERR_INVALID; }
-  std::vector<int64_t> off, idx;
-  SC_TRY(radius_lists(h, h->train, h->n, eps, form, off, idx));  // every row's neighbourhood
+  std::vector<int64_t> off;
+  const int64_t *idx = nullptr;
+  SC_TRY(radius_lists(h, h->train, h->n, eps, form, off, &idx));  // every row's neighbourhood
   const int64_t k = dbscan_expand(h->n, off, idx, min_samples, labels_out);
   if (n_clusters_out) *n_clusters_out = k;
   return SC_OK;
@@ -911,15 +933,16 @@ sc_status sc_dbscan_predict(sc_knn *h, const void *queries, int32_t layout, int3
   if (m == 0) return SC_OK;
   SC_TRY(knn_reserve(h, m, 1));
   SC_TRY(upload_matrix(queries, h->dtype, layout, mem, m, h->d, ld, h->q, h->stream));
-  std::vector<int64_t> off, idx;
-  SC_TRY(radius_lists(h, h->q, m, eps, form, off, idx));
+  std::vector<int64_t> off;
+  const int64_t *idx = nullptr;
+  SC_TRY(radius_lists(h, h->q, m, eps, form, off, &idx));
   // dbscan.rs:378-397: votes per cluster, noise counted last; the first
   // maximum wins (which_max, src/tree/decision_tree_classifier.rs:490-502)
   std::vector<int64_t> votes((size_t)n_clusters + 1);
   for (int64_t q = 0; q < m; ++q) {
     std::fill(votes.begin(), votes.end(), 0);
     for (int64_t e = off[(size_t)q]; e < off[(size_t)q + 1]; ++e) {
-      const int64_t yi = train_labels[idx[(size_t)e]];
+      const int64_t yi = train_labels[idx[e]];
       ++votes[yi < 0 ? (size_t)n_clusters : (size_t)yi];
     }
     size_t which = 0;
