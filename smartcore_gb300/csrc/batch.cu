@@ -15,18 +15,25 @@
 //   items    the Lloyd work queue: (problem, rows [r0, r1), kernel variant),
 //            largest cost first; one queue head per launch
 //
-// Per Lloyd iteration two launches, captured in one CUDA graph for the loop:
+// The problems are grouped by padded width D into four classes, and each
+// class's work runs as one chain on its own stream (the widest on a
+// high-priority stream): its rows (copied, or read in place from pinned host
+// memory by a gather kernel), the scan of ||x||^2 and max |x| with the
+// start values and fixed-point scales, its k-means++ draws, the initial
+// means, and its Lloyd loop.  Per Lloyd iteration two launches, captured in
+// one CUDA graph per class:
 //   batch_assign_kernel  persistent CTAs pop items; per row an FP32
-//                        difference-form distance to every centroid, a
-//                        certified bound on its error, an FP64 re-score (the
+//                        expansion-form score to every centroid, a certified
+//                        bound on its error, an FP64 re-score (the
 //                        reference's operation order) of the rows whose best
 //                        two centroids fall inside the bound, and the exact
 //                        fixed-point sums of the item's rows in shared memory
 //                        (the rows are read once per iteration)
-//   batch_finalize_kernel one CTA per problem: centroids = sums / sizes,
-//                        distortion, break rule, the next f32 centroid copies
-// k-means++ runs every problem's draw j together: one update launch over the
-// rows of the problems still seeding, one selection launch (a CTA each).
+//   batch_finalize_kernel one CTA per problem of the class: centroids = sums /
+//                        sizes, distortion, break rule, the next f32
+//                        centroid copies
+// k-means++ runs a class's draw j for all its problems still seeding: one
+// update launch over their rows, one selection launch (a CTA each).
 #include <float.h>
 #include <math.h>
 #include <stdio.h>
