@@ -163,3 +163,43 @@ def test_fastpair_neighbour_map():
     assert dict(m)[2] == PairwiseDistance(2, 2, 3.4e38)
     with pytest.raises(KeyError):
         m[3]
+
+
+def test_find_radius_batch_sizing():
+    """find_radius_batch sizes its first output from the previous call's rows
+    per query; when the library reports more rows than that (SC_ERR_INVALID
+    with the total set), it calls once more with the exact size.  A fake
+    library with fixed per-query counts stands in for the device."""
+    from smartcore_gb300.neighbors import LinearKNNSearch
+
+    class Fake:
+        def __init__(self, per_query):
+            self.per_query, self.calls = per_query, []
+
+        def sc_knn_find_radius(self, h, q, lay, mem, m, ld, radius, form, counts, cap, idx, dist, total):
+            self.calls.append(cap)
+            c = np.ctypeslib.as_array(C.cast(counts, C.POINTER(C.c_int64)), (m,))
+            c[:] = self.per_query
+            t = self.per_query * m
+            np.ctypeslib.as_array(C.cast(total, C.POINTER(C.c_int64)), (1,))[0] = t
+            if cap < t:
+                return _lib.SC_ERR_INVALID
+            out = np.ctypeslib.as_array(C.cast(idx, C.POINTER(C.c_int64)), (t,))
+            out[:] = np.tile(np.arange(self.per_query), m)
+            np.ctypeslib.as_array(C.cast(dist, C.POINTER(C.c_double)), (t,))[:] = 0.5
+            return _lib.SC_OK
+
+    s = object.__new__(LinearKNNSearch)
+    s.dtype, s.n, s.d, s.h, s.form, s._per_query = np.dtype(np.float32), 10, 3, None, 1, 64.0
+    q = np.zeros((40, 3), np.float32)
+    s._L = Fake(200)  # 8,000 rows > the first size (1.25 * 64 * 40 = 3,200): two calls
+    counts, idx, dist = s.find_radius_batch(q, 1.0)
+    assert s._L.calls == [3200, 8000]
+    assert counts.tolist() == [200] * 40 and len(idx) == 8000 and idx[:3].tolist() == [0, 1, 2]
+    assert s._per_query == 200.0
+    s._L = Fake(150)  # now sized from 200 rows per query: one call
+    counts, idx, dist = s.find_radius_batch(q, 1.0)
+    assert s._L.calls == [10000] and len(idx) == 6000 and np.all(dist == 0.5)
+    s._L = Fake(0)  # no rows
+    counts, idx, dist = s.find_radius_batch(q, 1.0)
+    assert len(idx) == 0 and counts.sum() == 0
