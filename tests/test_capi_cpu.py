@@ -203,3 +203,52 @@ def test_find_radius_batch_sizing():
     s._L = Fake(0)  # no rows
     counts, idx, dist = s.find_radius_batch(q, 1.0)
     assert len(idx) == 0 and counts.sum() == 0
+
+
+def test_fit_many_problem_table(monkeypatch):
+    """KMeans.fit_many fills one sc_kmeans_problem per fit (shape, layout,
+    k-means++ draws, and each output pointer at the problem's slice of the
+    shared output arrays).  A fake library checks the table and writes each
+    problem's index into its outputs."""
+    from smartcore_gb300 import cluster
+
+    rng = np.random.default_rng(3)
+    shapes = [(50, 4, 3), (7, 2, 5), (120, 9, 2)]
+    xs = [rng.normal(size=(n, d)).astype(np.float32) for n, d, _ in shapes]
+    xs[1] = np.asfortranarray(xs[1])
+    seen = {}
+
+    real = _lib.load()
+
+    class Fake:
+        def __getattr__(self, name):
+            return getattr(real, name)
+
+        def sc_kmeans_fit_batched(self, ptr, m, dt, form):
+            arr = (_lib.KMeansProblem * m).from_address(ptr)
+            for i in range(m):
+                q = arr[i]
+                n, d, k = shapes[i]
+                assert (q.n, q.d, q.k, q.max_iter) == (n, d, k, 9)
+                assert (q.layout, q.ld) == ((_lib.COL_MAJOR, n) if i == 1 else (_lib.ROW_MAJOR, d))
+                first, u = kmeanspp_draws(n, k, 100 + i)
+                got = np.ctypeslib.as_array((C.c_double * (k - 1)).from_address(q.uniforms))
+                assert q.first_index == first and np.array_equal(got, u)
+                for f, cnt, ct in (("labels_out", n, C.c_int64), ("sizes_out", k, C.c_int64),
+                                   ("centroids_out", k * d, C.c_double), ("distortion_out", 1, C.c_double),
+                                   ("iters_out", 1, C.c_int64)):
+                    np.ctypeslib.as_array((ct * cnt).from_address(getattr(q, f)))[:] = i
+                q.rescored, q.pp_replays = 10 + i, 20 + i
+            seen["m"] = m
+            return _lib.SC_OK
+
+    monkeypatch.setattr(cluster._lib, "load", lambda: Fake())
+    stats = []
+    fits = cluster.KMeans.fit_many([(x, KMeansParameters(k=k, max_iter=9, seed=100 + i))
+                                    for i, (x, (_, _, k)) in enumerate(zip(xs, shapes))], stats=stats)
+    assert seen["m"] == 3 and stats == [(10, 20), (11, 21), (12, 22)]
+    for i, (km, (n, d, k)) in enumerate(zip(fits, shapes)):
+        assert km._y.shape == (n,) and np.all(km._y == i)
+        assert km.centroids.shape == (k, d) and np.all(km.centroids == i)
+        assert km.size.shape == (k,) and np.all(km.size == i)
+        assert km.iters == i and km._distortion == float(i)
